@@ -54,3 +54,12 @@ extern "C" int ref_eval_relxilllp_iongrad(const double *params, int iongrad_type
   }
   return 0;
 }
+
+/* Empty the reference's xillver spectrum cache (xilltable.c:30, data_storage)
+ * so that the next evaluation behaves as the first one in a fresh process.
+ * The rows are leaked on purpose: freeing them is the reference's job. */
+extern "C" xillTable *cached_xill_tab;
+extern "C" void ref_reset_xillver_cache(void) {
+  if (cached_xill_tab == nullptr) return;
+  for (int ii = 0; ii < cached_xill_tab->num_elements; ii++) cached_xill_tab->data_storage[ii] = nullptr;
+}
