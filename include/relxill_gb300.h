@@ -1,0 +1,89 @@
+/*
+ * relxill_gb300.h -- C ABI of the GB300 (sm_103a) implementation of relxill's
+ * relativistic convolution path.
+ *
+ * The four local-model entry points keep the signature that the reference's
+ * wrapper generator emits for XSPEC (src/create_wrapper_xspec.py:153-162) and
+ * the parameter order of src/modelfiles/lmodel_relxill_public.dat, so a host
+ * package that loads the reference's librelxill can load this library
+ * instead.  Tables are found through RELXILL_TABLE_PATH as in the reference
+ * (src/relutility.c:320-328).  The same environment switches are honoured:
+ * RELXILL_NUM_RZONES, RELLINE_PHYSICAL_NORM, RELXILL_RENORMALIZE,
+ * RELXILL_CONSTANT_DENSITY.  Returning radiation is not part of this path: a
+ * parameter array with $switch_returnrad != 0 fails with status 3.
+ *
+ * Errors: the void entry points fill `flux` with zeros on failure and record
+ * the status (relx_last_status); the batched calls return it.
+ */
+#ifndef RELXILL_GB300_H
+#define RELXILL_GB300_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* model ids of the batched calls */
+enum { RELX_MODEL_RELLINE = 0, RELX_MODEL_RELCONV = 1, RELX_MODEL_RELXILL = 2, RELX_MODEL_RELXILLLP = 3 };
+
+/* Local models.  Replace c_lmodrelline / c_lmodrelconv / c_lmodrelxill /
+ * c_lmodrelxilllp, generated by src/create_wrapper_xspec.py:153-162 from
+ * lmodel_relxill_public.dat:1,13,46,61 and dispatched through
+ * xspec_C_wrapper_eval_model (src/LocalModel.cpp:143-160).
+ * energy: Nflux+1 ascending bin edges [keV]; parameter: the model's lmodel.dat
+ * parameters in order; flux: Nflux photon fluxes per bin (input spectrum as
+ * well for relconv); spectrum, fluxError and init are unused, as in the
+ * reference. */
+void c_lmodrelline(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                   double *fluxError, const char *init);
+void c_lmodrelconv(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                   double *fluxError, const char *init);
+void c_lmodrelxill(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                   double *fluxError, const char *init);
+void c_lmodrelxilllp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                     double *fluxError, const char *init);
+
+/* Status of the last call on this process (0 = success).  The reference has
+ * no status channel (src/LocalModel.cpp:153-159); this replaces its printed
+ * errors and escaping exceptions. */
+int relx_last_status(void);
+const char *relx_last_error(void);
+
+/* Load the tables from table_path (NULL: RELXILL_TABLE_PATH or "./") onto
+ * the current CUDA device.  Called implicitly by the first evaluation; the
+ * reference loads lazily in the same way (src/reltable.c:235,384,
+ * src/xilltable.c:719). */
+int relx_init(const char *table_path);
+/* bytes of device memory held by the tables */
+int relx_table_bytes(int64_t *bytes);
+/* free all device memory of the library */
+void relx_release(void);
+
+/* Batched evaluation with host buffers; no counterpart in the reference,
+ * which evaluates one parameter set per call.
+ * params: n_sets x npar (npar = 10, 8, 13, 14 for relline, relconv, relxill,
+ *   relxilllp, lmodel.dat order);
+ * energy: concatenated bin edges; set i uses energy[energy_offsets[i] ..
+ *   energy_offsets[i+1]-1] (n_i + 1 edges);
+ * flux: concatenated outputs, set i at flux[energy_offsets[i] - i .. + n_i - 1];
+ * flux_in: relconv input spectra in the same layout as flux (NULL otherwise);
+ * status: n_sets per-set statuses (may be NULL);
+ * ion_grad_type / iongrad_index: per-set hidden ionisation-gradient switch
+ *   (0 const, 1 power law, 2 alpha disk) of relxilllp (NULL: 0).
+ * Returns 0 or the first non-zero set status / API error. */
+int relx_eval_batch(int model, int n_sets, const double *params, const double *energy,
+                    const int64_t *energy_offsets, const double *flux_in, double *flux, int *status,
+                    const int *ion_grad_type, const double *iongrad_index);
+
+/* Same with device buffers, asynchronous on `stream` (a cudaStream_t; NULL:
+ * the library's stream).  flux_in (relconv) uses the energy-edge layout
+ * (set i at energy_offsets[i]).  h_energy_offsets and h_ion_grad_type are host
+ * copies used to size the launch. */
+int relx_eval_batch_device(int model, int n_sets, const double *d_params, const double *d_energy,
+                           const int64_t *d_energy_offsets, const int64_t *h_energy_offsets, const double *d_flux_in,
+                           double *d_flux, int *d_status, const int *d_ion_grad_type, const int *h_ion_grad_type,
+                           const double *d_iongrad_index, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -60,6 +60,9 @@ extern "C" int ref_eval_relxilllp_iongrad(const double *params, int iongrad_type
  * The rows are leaked on purpose: freeing them is the reference's job. */
 extern "C" xillTable *cached_xill_tab;
 extern "C" void ref_reset_xillver_cache(void) {
+  /* the full-output cache is keyed on the public parameters only
+   * (Relcache.h:134-147), so hidden switches would hit it: empty it as well */
+  RelxillCache::instance().empty();
   if (cached_xill_tab == nullptr) return;
   for (int ii = 0; ii < cached_xill_tab->num_elements; ii++) cached_xill_tab->data_storage[ii] = nullptr;
 }

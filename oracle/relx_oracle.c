@@ -72,6 +72,8 @@
 /* relutility.c:24-26 */
 static double interp_lin_1d(double ifac_r, double rlo, double rhi) { return ifac_r * rhi + (1.0 - ifac_r) * rlo; }
 
+double relxo_interp_lin_1d(double f, double lo, double hi) { return interp_lin_1d(f, lo, hi); }
+
 /* relutility.c:41-43 */
 static double interp_log_1d(double ifac_r, double rlo, double rhi) {
   return exp(ifac_r * log(rhi) + (1.0 - ifac_r) * log(rlo));
@@ -80,6 +82,13 @@ static double interp_log_1d(double ifac_r, double rlo, double rhi) {
 /* relutility.c:46-58 */
 static double interp_lin_2d(double f1, double f2, double r11, double r12, double r21, double r22) {
   return (1.0 - f1) * (1.0 - f2) * r11 + (f1) * (1.0 - f2) * r12 + (1.0 - f1) * (f2) * r21 + (f1) * (f2) * r22;
+}
+
+double relxo_interp_lin_2d(double f1, double f2, double r11, double r12, double r21, double r22) {
+  return interp_lin_2d(f1, f2, r11, r12, r21, r22);
+}
+double relxo_interp_lin_2d_float(double f1, double f2, float r11, float r12, float r21, float r22) {
+  return interp_lin_2d(f1, f2, r11, r12, r21, r22);
 }
 
 /* relutility.c:135-151: arr ascending, returns k with arr[k] <= val < arr[k+1] */

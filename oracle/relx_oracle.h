@@ -19,6 +19,9 @@ int relxo_eval_ext(int model, const double *params, int ion_grad_type, double io
                    int n_flux, double *flux);
 
 /* components, for pinning against the reference's known-answer tests */
+double relxo_interp_lin_1d(double f, double lo, double hi);
+double relxo_interp_lin_2d(double f1, double f2, double r11, double r12, double r21, double r22);
+double relxo_interp_lin_2d_float(double f1, double f2, float r11, float r12, float r21, float r22);
 void relxo_rebin_spectrum(const double *ener, double *flu, int nbins, const double *ener0, const double *flu0,
                           int nbins0);
 double relxo_kerr_rms(double a);

@@ -1,0 +1,191 @@
+"""relxill_gb300: relxill's relativistic convolution path on GB300 (sm_103a).
+
+The package is a thin host layer over the C ABI of ``librelxill_gb300.so``
+(include/relxill_gb300.h).  It mirrors the reference's local-model interface:
+one function per model taking the energy grid (bin edges in keV) and the
+parameter array in the order of ``lmodel_relxill_public.dat`` and returning
+the photon flux per bin, plus a batched call for many parameter sets with
+different energy grids.
+
+There is no CPU fallback: if the CUDA library is missing, or no GPU is
+present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "librelxill_gb300.so")
+
+MODELS: Dict[str, int] = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3}
+
+# parameter names and defaults of lmodel_relxill_public.dat:1-75 (in order)
+PARAMS: Dict[str, List[Tuple[str, float]]] = {
+    "relline": [("lineE", 6.4), ("Index1", 3.0), ("Index2", 3.0), ("Rbr", 15.0), ("a", 0.998), ("Incl", 30.0),
+                ("Rin", -1.0), ("Rout", 400.0), ("z", 0.0), ("limb", 0.0)],
+    "relconv": [("Index1", 3.0), ("Index2", 3.0), ("Rbr", 15.0), ("a", 0.998), ("Incl", 30.0), ("Rin", -1.0),
+                ("Rout", 400.0), ("limb", 0.0)],
+    "relxill": [("Index1", 3.0), ("Index2", 3.0), ("Rbr", 15.0), ("a", 0.998), ("Incl", 30.0), ("Rin", -1.0),
+                ("Rout", 400.0), ("z", 0.0), ("gamma", 2.0), ("logxi", 3.1), ("Afe", 1.0), ("Ecut", 300.0),
+                ("refl_frac", 3.0)],
+    "relxilllp": [("h", 6.0), ("beta", 0.0), ("a", 0.998), ("Incl", 30.0), ("Rin", -1.0), ("Rout", 400.0),
+                  ("z", 0.0), ("gamma", 2.0), ("logxi", 3.1), ("Afe", 1.0), ("Ecut", 300.0), ("refl_frac", 1.0),
+                  ("switch_returnrad", 1.0), ("switch_reflfrac_boost", 0.0)],
+}
+
+STATUS = {0: "ok", 1: "parameter out of range", 2: "table inconsistent", 3: "unsupported option",
+          4: "radial grid outside the table", 5: "relconv input sum <= 0", 6: "CUDA error",
+          7: "device memory", 8: "device wait timed out", 9: "bad arguments", 10: "tables not loaded"}
+
+
+class RelxillError(RuntimeError):
+    def __init__(self, status: int, message: str = ""):
+        self.status = status
+        super().__init__(f"relxill_gb300 status {status} ({STATUS.get(status, '?')}){': ' + message if message else ''}")
+
+
+_lib: Optional[ctypes.CDLL] = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lp = ctypes.POINTER(ctypes.c_int64)
+
+
+def lib() -> ctypes.CDLL:
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m relxill_gb300.build`")
+    L = ctypes.CDLL(LIB_PATH)
+    L.relx_init.argtypes = [ctypes.c_char_p]
+    L.relx_init.restype = ctypes.c_int
+    L.relx_last_error.restype = ctypes.c_char_p
+    L.relx_last_status.restype = ctypes.c_int
+    L.relx_eval_batch.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _lp, _dp, _dp, _ip, _ip, _dp]
+    L.relx_eval_batch.restype = ctypes.c_int
+    L.relx_eval_batch_device.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                         _lp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _ip,
+                                         ctypes.c_void_p, ctypes.c_void_p]
+    L.relx_eval_batch_device.restype = ctypes.c_int
+    L.relx_table_bytes.argtypes = [_lp]
+    L.relx_table_bytes.restype = ctypes.c_int
+    for name in ("c_lmodrelline", "c_lmodrelconv", "c_lmodrelxill", "c_lmodrelxilllp"):
+        fn = getattr(L, name)
+        fn.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, ctypes.c_char_p]
+        fn.restype = None
+    _lib = L
+    return L
+
+
+def _ptr(a: np.ndarray, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+def init(table_path: Optional[str] = None) -> None:
+    """Load the tables onto the current GPU (RELXILL_TABLE_PATH if not given)."""
+    L = lib()
+    st = L.relx_init(table_path.encode() if table_path else None)
+    if st:
+        raise RelxillError(st, L.relx_last_error().decode())
+
+
+def last_error() -> str:
+    return lib().relx_last_error().decode()
+
+
+def _as_params(model: str, params) -> np.ndarray:
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    npar = len(PARAMS[model])
+    if p.ndim == 1:
+        p = p[None, :]
+    if p.shape[1] != npar:
+        raise ValueError(f"{model} takes {npar} parameters, got {p.shape[1]}")
+    return p
+
+
+def pack_grids(energies: Sequence[np.ndarray]) -> Tuple[np.ndarray, np.ndarray]:
+    """Concatenate per-set bin-edge arrays; returns (edges, offsets[n_sets+1])."""
+    offs = np.zeros(len(energies) + 1, dtype=np.int64)
+    for i, e in enumerate(energies):
+        offs[i + 1] = offs[i] + len(e)
+    return np.concatenate([np.asarray(e, dtype=np.float64) for e in energies]), offs
+
+
+def eval_batch(model: str, params, energies: Sequence[np.ndarray], flux_in: Optional[Sequence[np.ndarray]] = None,
+               ion_grad_type: Optional[Sequence[int]] = None, iongrad_index: Optional[Sequence[float]] = None,
+               check: bool = True) -> Tuple[List[np.ndarray], np.ndarray]:
+    """Evaluate many parameter sets, each on its own energy grid, in one batch.
+
+    Returns (list of flux arrays, per-set status array)."""
+    L = lib()
+    p = _as_params(model, params)
+    n = p.shape[0]
+    if len(energies) != n:
+        raise ValueError("one energy grid per parameter set")
+    edges, offs = pack_grids(energies)
+    nflux = int(offs[-1]) - n
+    flux = np.zeros(nflux, dtype=np.float64)
+    status = np.zeros(n, dtype=np.int32)
+    fin = None
+    if model == "relconv":
+        if flux_in is None:
+            raise ValueError("relconv needs the input spectra")
+        fin = np.concatenate([np.asarray(f, dtype=np.float64) for f in flux_in])
+    igt = None if ion_grad_type is None else np.ascontiguousarray(ion_grad_type, dtype=np.int32)
+    igi = None if iongrad_index is None else np.ascontiguousarray(iongrad_index, dtype=np.float64)
+    st = L.relx_eval_batch(MODELS[model], n, _ptr(p), _ptr(edges), _ptr(offs, _lp),
+                           _ptr(fin) if fin is not None else None, _ptr(flux), _ptr(status, _ip),
+                           _ptr(igt, _ip) if igt is not None else None, _ptr(igi) if igi is not None else None)
+    if check and st and not np.any(status):
+        raise RelxillError(st, L.relx_last_error().decode())
+    out = [flux[offs[i] - i: offs[i + 1] - i - 1] for i in range(n)]
+    return out, status
+
+
+def _lmod(model: str, energy, params, flux_in=None) -> np.ndarray:
+    L = lib()
+    e = np.ascontiguousarray(energy, dtype=np.float64)
+    p = _as_params(model, params)[0].copy()
+    nflux = len(e) - 1
+    flux = np.zeros(nflux) if flux_in is None else np.array(flux_in, dtype=np.float64)
+    getattr(L, "c_lmod" + model)(_ptr(e), nflux, _ptr(p), 0, _ptr(flux), None, None)
+    st = L.relx_last_status()
+    if st:
+        raise RelxillError(st, L.relx_last_error().decode())
+    return flux
+
+
+def relline(energy, params) -> np.ndarray:
+    """relline photon flux per bin (c_lmodrelline)."""
+    return _lmod("relline", energy, params)
+
+
+def relconv(energy, params, flux) -> np.ndarray:
+    """relconv applied to `flux` on the grid `energy` (c_lmodrelconv)."""
+    return _lmod("relconv", energy, params, flux)
+
+
+def relxill(energy, params) -> np.ndarray:
+    """relxill photon flux per bin (c_lmodrelxill)."""
+    return _lmod("relxill", energy, params)
+
+
+def relxilllp(energy, params) -> np.ndarray:
+    """relxilllp photon flux per bin (c_lmodrelxilllp)."""
+    return _lmod("relxilllp", energy, params)
+
+
+def default_params(model: str) -> np.ndarray:
+    return np.array([v for _, v in PARAMS[model]], dtype=np.float64)
+
+
+def log_grid(emin: float, emax: float, nbins: int) -> np.ndarray:
+    """nbins log-spaced bins (nbins+1 edges), like get_log_grid (relutility.c:399-405)."""
+    return np.exp(np.linspace(np.log(emin), np.log(emax), nbins + 1))

@@ -1,0 +1,153 @@
+// relx_common.h -- definitions shared by the host runtime and the sm_103a kernels
+// of the relativistic convolution path (relline / relconv / relxill / relxilllp).
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define RELX_HD __host__ __device__
+#else
+#define RELX_HD
+#endif
+
+// model ids (lmodel_relxill_public.dat:1,13,46,61)
+enum RelxModel { RELX_RELLINE = 0, RELX_RELCONV = 1, RELX_RELXILL = 2, RELX_RELXILLLP = 3, RELX_NMODELS = 4 };
+
+// error codes written per set and returned by the C ABI
+enum RelxStatus {
+  RELX_OK = 0,
+  RELX_ERR_PARAM = 1,        // parameter out of the allowed range (check_parameter_bounds)
+  RELX_ERR_TABLE = 2,        // table missing or inconsistent
+  RELX_ERR_UNSUPPORTED = 3,  // returning radiation, unsupported model option
+  RELX_ERR_GRID = 4,         // radial interpolation outside the table (Relprofile.cpp:255-278)
+  RELX_ERR_INPUT = 5,        // relconv input spectrum with sum <= 0 (LocalModel.cpp:84-86)
+  RELX_ERR_CUDA = 6,         // CUDA runtime error
+  RELX_ERR_NOMEM = 7,        // device memory budget exceeded
+  RELX_ERR_TIMEOUT = 8,      // a bounded device wait gave up
+  RELX_ERR_ARG = 9,          // bad arguments at the C ABI
+  RELX_ERR_NOTABLE = 10,     // tables not loaded
+};
+
+// constants of the reference (common.h:133-136, Xillspec.h:28-38, Relbase.h:38-39)
+#define RELX_NFRAD 1000
+#define RELX_NZONES 10
+#define RELX_NZONES_IONGRAD 25
+#define RELX_NZMAX 50
+#define RELX_NCONV 4096
+#define RELX_EMIN_CONV 0.00035
+#define RELX_EMAX_CONV 2000.0
+#define RELX_NCOARSE 500
+#define RELX_EMIN_NORM 0.1
+#define RELX_EMAX_NORM 1000.0
+#define RELX_EMIN_XILL 0.01
+#define RELX_EMAX_XILL 1000.0
+#define RELX_GFAC_H 5e-3
+#define RELX_RELTABLE_MAX_R 1000.0
+
+// capacity limits of the device kernels (checked when tables load)
+#define RELX_MAX_NG 64
+#define RELX_MAX_NRTAB 128
+#define RELX_MAX_NRADLP 128
+#define RELX_MAX_INCL 16
+#define RELX_MAX_XPAR 8
+#define RELX_ZDENSE 16            // zones handled with the de-duplicated xillver corner list
+#define RELX_MAX_UCORNER 256      // 16 corners x RELX_ZDENSE zones
+#define RELX_NPARAM_MAX 16
+
+#define RELX_EMIS_BKN 1
+#define RELX_EMIS_LP 2
+
+// Device-resident tables (uploaded once).  All arrays are device pointers.
+struct RelxTables {
+  // relline table (reltable.h:24-48): [a][mu0][r] and [a][mu0][r][g] (float4 = trff1,trff2,cosne1,cosne2)
+  int rel_na, rel_nmu0, rel_nr, rel_ng;
+  const float *rel_a, *rel_mu0;
+  const float *rel_r, *rel_gmin, *rel_gmax;
+  const float4 *rel_tc;
+  // lamp-post table (reltable.h:51-69): [a][h], [a][rad], [a][h][rad]; del, del_inc stored as |x|
+  int lp_na, lp_nh, lp_nrad;
+  const float *lp_a, *lp_h, *lp_rad, *lp_intens, *lp_del, *lp_delinc;
+  // xillver table (common.h:254-277), 5 parameters, Incl last
+  int x_npar, x_nener, x_nener_pad, x_nincl;
+  int x_nvals[RELX_MAX_XPAR];
+  int x_pindex[RELX_MAX_XPAR];
+  int x_has_dens;
+  const float *x_vals;       // [x_npar][x_maxvals]
+  int x_maxvals;
+  const float *x_spec;       // [rows][x_nener_pad], each row divided by 10^logXi of its grid point
+  int64_t x_rows;
+  // conv grid and precomputed maps
+  const double *conv_e;      // [RELX_NCONV+1]
+  const float2 *conv_eff;    // float-float edges
+  const float *conv_inv_emid;  // 1/(0.5(e_j+e_j+1))
+  const float *conv_cf;      // 0.5(e_j+e_j+1)/(e_j+1-e_j)  (Relbase.cpp:93-103)
+  int conv_pos1;             // binary_search(conv_e, 1.0)  (Relbase.cpp:133-137)
+  int conv_band_lo, conv_band_hi;  // bins with e_j >= 0.01 && e_j+1 < 1000 (Relbase.cpp:205)
+  const double *coarse_e;    // [RELX_NCOARSE+1]
+  // rebin map xillver grid -> conv grid (relutility.c:549-601): per conv bin
+  const int *rb_imin, *rb_imax;
+  const float *rb_fmin, *rb_fmax;  // fractions (single-bin case: rb_fmin, rb_imax == rb_imin)
+  const double *x_e;         // xillver edges [x_nener+1] (double of the float table values)
+};
+
+// per-set inputs
+struct RelxSetIn {
+  double p[RELX_NPARAM_MAX];
+  int64_t e_off;     // offset of the set's user energy grid (n+1 edges) in the concatenated grid array
+  int n_ener;        // number of user bins
+  int ion_grad_type; // hidden switch (0 const, 1 PL, 2 ALPHA)
+  double iongrad_index;
+  int nzones_env;    // RELXILL_NUM_RZONES value or 0
+  int flags;         // bit0 RELLINE_PHYSICAL_NORM, bit1 RELXILL_RENORMALIZE, bit2 RELXILL_CONSTANT_DENSITY
+};
+
+// per-set state written by the setup kernel
+struct RelxSetState {
+  int status, model, emis_type, limb, nz, ion_grad_type, boost_switch;
+  int g_n;          // bins of the line-profile grid (user grid for relline, conv grid otherwise)
+  int win_lo, win_hi;  // line-profile bins touched by any radius
+  int ind_a, ind_mu0;
+  float ifac_a, ifac_mu0;
+  int ucount;       // unique xillver corners (dense mode)
+  int pad_;
+  double a, incl, rin, rout, height, beta, gamma, z, lineE;
+  double gam, ect_src, refl_frac;
+  double relline_norm;   // renormalisation target; <= 0 means no renormalisation
+  double g_inf, f_inf_rest, refl_frac_lp, prim_fac, norm_fac_refl, src_norm;
+  double rgrid[RELX_NZMAX + 1];
+  int zi0[RELX_NZMAX], zi1[RELX_NZMAX];   // fine-radius index range of each zone (inclusive)
+  float inv_nc[RELX_NZMAX];               // 1 / normalisation change source->disk (Xillspec.cpp:408-440)
+};
+
+// per-set radial data [RELX_NFRAD] (written by setup, read by the line-profile kernel)
+struct RelxRadial {
+  double re[RELX_NFRAD];
+  double gmin[RELX_NFRAD];
+  double gmax[RELX_NFRAD];
+  double ifac[RELX_NFRAD];
+  float  ew[RELX_NFRAD];      // emissivity * trapez weight / 2
+  float  emis[RELX_NFRAD];
+  float  wt[RELX_NFRAD];
+  float2 gmin_ff[RELX_NFRAD]; // gmin, gmax, gmax-gmin as float-float (hi, lo)
+  float2 gmax_ff[RELX_NFRAD];
+  float2 dg_ff[RELX_NFRAD];
+  float2 eH_ff[RELX_NFRAD];   // gstar2ener(H), gstar2ener(1-H) (relutility.c:260-262)
+  float2 e1H_ff[RELX_NFRAD];
+  float  inv_dg[RELX_NFRAD];  // 1/(gmax-gmin)
+  int    ielo[RELX_NFRAD];    // first line-profile bin touched by the radius (-1: none)
+  int    iehi[RELX_NFRAD];    // last line-profile bin touched
+  short  itab[RELX_NFRAD];    // table radius index: re_tab[itab+1] <= re < re_tab[itab]
+  unsigned char zone[RELX_NFRAD];
+  unsigned char red_H[RELX_NFRAD];  // gstar2ener(H) >= 0.95 (int_romb, Relprofile.cpp:636)
+};
+
+// xillver corners of one set (dense mode: de-duplicated across zones)
+struct RelxCorners {
+  int row[RELX_MAX_UCORNER];              // spectrum row of incl 0 (rows of incl i are row + i)
+  float w[RELX_MAX_UCORNER][RELX_ZDENSE]; // weight of the corner in each zone (0 if unused)
+};
+
+// per-zone corners (used when nz > RELX_ZDENSE)
+struct RelxZoneCorners {
+  int row[RELX_NZMAX][16];
+  float w[RELX_NZMAX][16];
+};

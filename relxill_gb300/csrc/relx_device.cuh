@@ -1,0 +1,138 @@
+// relx_device.cuh -- device helpers shared by the relxill kernels: the
+// reference's search and interpolation conventions, Kerr-metric formulas in
+// FP64, and float-float (double-single) helpers for bin edges.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "relx_common.h"
+
+namespace relx {
+
+constexpr double kPi = 3.14159265358979323846;
+
+// ---- searches with the conventions of relutility.c:135-211 ----------------
+// ascending arr: returns k with arr[k] <= val < arr[k+1], clamped to [0, n-2]
+template <typename T>
+__device__ __forceinline__ int bsearch_asc(const T *arr, int n, T val) {
+  int klo = 0, khi = n - 1;
+  while (khi - klo > 1) {
+    int k = (khi + klo) >> 1;
+    if (arr[k] > val) khi = k; else klo = k;
+  }
+  return klo;
+}
+// descending arr (inv_binary_search, relutility.c:195-211)
+__device__ __forceinline__ int bsearch_desc(const double *arr, int n, double val) {
+  int klo = 0, khi = n - 1;
+  while (khi - klo > 1) {
+    int k = (khi + klo) >> 1;
+    if (arr[k] < val) khi = k; else klo = k;
+  }
+  return klo;
+}
+
+// relutility.c:24-26 and :46-58
+__device__ __forceinline__ double lerp1(double f, double lo, double hi) { return f * hi + (1.0 - f) * lo; }
+__device__ __forceinline__ double lerp2(double f1, double f2, double r11, double r12, double r21, double r22) {
+  return (1.0 - f1) * (1.0 - f2) * r11 + (f1) * (1.0 - f2) * r12 + (1.0 - f1) * (f2) * r21 + (f1) * (f2) * r22;
+}
+
+// ---- Kerr metric (Relphysics.cpp), FP64 -------------------------------------
+__device__ __forceinline__ double kerr_rms(double a) {
+  double sign = (a < 0) ? -1.0 : 1.0;
+  double z1 = 1.0 + pow(1.0 - a * a, 1.0 / 3.0) * (pow(1.0 + a, 1.0 / 3.0) + pow(1.0 - a, 1.0 / 3.0));
+  double z2 = sqrt((3.0 * a * a) + (z1 * z1));
+  return 3.0 + z2 - sign * sqrt((3.0 - z1) * (3.0 + z1 + (2 * z2)));
+}
+__device__ __forceinline__ double kerr_rplus(double a) { return 1 + sqrt(1 - a * a); }
+__device__ __forceinline__ double relat_abberation(double del, double beta) {
+  return acos((cos(del) - beta) / (1 - beta * cos(del)));
+}
+__device__ __forceinline__ double calc_g_inf(double h, double a) { return sqrt(1.0 - (2 * h / (h * h + a * a))); }
+__device__ __forceinline__ double doppler_factor(double del, double bet) {
+  return sqrt(1.0 - bet * bet) / (1.0 + bet * cos(del));
+}
+// gi_potential_lp, Relphysics.cpp:163-207
+__device__ __forceinline__ double gi_potential_lp(double r, double a, double h, double bet, double del) {
+  double sr = sqrt(r);
+  double ut_d = ((r * sr + a) / (sr * sqrt(r * r - 3 * r + 2 * a * sr)));
+  double ut_h = sqrt((h * h + a * a) / (h * h - 2 * h + a * a));
+  double gi = ut_d / ut_h;
+  if (fabs(bet) < 1e-6) return gi;
+  double gam = 1.0 / sqrt(1.0 - bet * bet);
+  double sign = (del > kPi / 2) ? -1.0 : 1.0;
+  double delta_eq = h * h - 2 * h + a * a;
+  double sd = sin(del);
+  double h2a2 = h * h + a * a;
+  double q2 = (sd * sd) * (h2a2 * h2a2 / delta_eq) - a * a;
+  double beta_fac = sqrt(h2a2 * h2a2 - delta_eq * (q2 + a * a));
+  beta_fac = gam * (1.0 + sign * beta_fac / h2a2 * bet);
+  return gi / beta_fac;
+}
+// Relphysics.cpp:123-125
+__device__ __forceinline__ double density_ss73_zone_a(double radius, double rms) {
+  double q = 1 - sqrt(rms / radius);
+  return pow(radius / rms, 1.5) / (q * q);
+}
+
+// ---- float-float (value = hi + lo) ------------------------------------------
+__device__ __forceinline__ float2 ff_from_double(double d) {
+  float hi = __double2float_rn(d);
+  float lo = __double2float_rn(d - (double) hi);
+  return make_float2(hi, lo);
+}
+// (a.hi + a.lo) - (b.hi + b.lo) rounded to float, error ~1 ulp of the result
+__device__ __forceinline__ float ff_sub_to_float(float2 a, float2 b) {
+  float s = __fsub_rn(a.x, b.x);
+  float bb = __fsub_rn(s, a.x);
+  float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(-b.x, bb));  // two-sum error
+  return __fadd_rn(s, __fadd_rn(err, __fsub_rn(a.y, b.y)));
+}
+
+// block-wide sum in FP64 with a fixed reduction tree (deterministic)
+template <int NT>
+__device__ __forceinline__ double block_sum_d(double v, double *scratch) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) scratch[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < NT / 32; i++) r += scratch[i];
+    scratch[NT / 32] = r;
+  }
+  __syncthreads();
+  r = scratch[NT / 32];
+  __syncthreads();
+  return r;
+}
+
+template <int NT>
+__device__ __forceinline__ int block_min_i(int v, int *scratch) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+  __syncthreads();
+  int r = scratch[0];
+  for (int i = 1; i < NT / 32; i++) r = min(r, scratch[i]);
+  __syncthreads();
+  return r;
+}
+template <int NT>
+__device__ __forceinline__ int block_max_i(int v, int *scratch) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+  __syncthreads();
+  int r = scratch[0];
+  for (int i = 1; i < NT / 32; i++) r = max(r, scratch[i]);
+  __syncthreads();
+  return r;
+}
+
+}  // namespace relx

@@ -1,0 +1,49 @@
+// relx_kernels.h -- declarations of the sm_103a kernels and their launch
+// geometry, used by the host runtime (runtime.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "relx_common.h"
+
+namespace relx {
+
+constexpr int kSetupThreadsH = 256;
+constexpr int kLineThreadsH = 256;
+constexpr int kLineTileH = 512;
+constexpr int kXillThreadsH = 256;
+constexpr int kXillTileH = 1024;
+constexpr int kConvThreadsH = 256;
+
+size_t setup_smem_bytes();
+size_t line_smem_bytes(int nr, int ng);
+size_t xill_smem_bytes(int n_incl);
+size_t conv_smem_bytes();
+size_t fin_smem_bytes();
+
+__global__ void setup_kernel(RelxTables tab, int model, const RelxSetIn *sin, const double *user_e, double *line_e,
+                             RelxSetState *sout, RelxRadial *rout, RelxCorners *cout, RelxZoneCorners *zcout);
+
+cudaError_t relline_set_smem(size_t bytes);
+cudaError_t launch_relline(bool hist, dim3 grid, size_t smem, cudaStream_t s, const RelxTables &tab,
+                           const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
+                           int nza, float *prof, float *dist, double *tsum, int ntile_max);
+
+__global__ void xillver_dense_kernel(RelxTables tab, const RelxSetState *sst, const RelxCorners *scor,
+                                     const float *dist_raw, int nza, float *xout, int *err);
+__global__ void xillver_zone_kernel(RelxTables tab, const RelxSetState *sst, const RelxZoneCorners *zcor,
+                                    const float *dist_raw, int nza, float *xout);
+
+__global__ void conv_zone_kernel(RelxTables tab, const RelxSetState *sst, const float *prof, const double *tsum,
+                                 int ntile_max, int tile_bins, const float *xill, int nza, float *cout);
+__global__ void relconv_conv_kernel(RelxTables tab, const RelxSetIn *sin, const RelxSetState *sst, const float *prof,
+                                    const double *tsum, int ntile_max, int tile_bins, int nza, const double *user_e,
+                                    const double *user_f, float *cout, int *sflag);
+__global__ void finalize_relxill_kernel(RelxTables tab, const RelxSetIn *sin, const RelxSetState *sst,
+                                        const float *cout, int nza, const double *user_e, double *flux);
+__global__ void finalize_relconv_kernel(RelxTables tab, const RelxSetIn *sin, const RelxSetState *sst,
+                                        const float *cout, int nza, const double *user_e, const int *sflag,
+                                        double *flux);
+__global__ void finalize_relline_kernel(const RelxSetIn *sin, const RelxSetState *sst, const float *prof,
+                                        const double *tsum, int ntile_max, int tile_bins, int nza, double *flux);
+
+}  // namespace relx

@@ -1,0 +1,801 @@
+// runtime.cu -- host runtime of the relxill GB300 path: table loading and
+// upload, device workspace, the kernel sequence of one batch, and the C ABI
+// (include/relxill_gb300.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/relxill_gb300.h"
+#include "fits_reader.h"
+#include "relx_common.h"
+#include "relx_kernels.h"
+
+namespace relx {
+
+static thread_local std::string g_errmsg;
+static std::atomic<int> g_last_status{0};
+
+#define RELX_CUDA(call)                                                                   \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      g_errmsg = std::string(#call) + ": " + cudaGetErrorString(e_);                       \
+      return RELX_ERR_CUDA;                                                               \
+    }                                                                                     \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  int reserve(size_t n) {
+    if (n <= bytes) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    size_t want = std::max(n, (size_t) 256);
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      g_errmsg = "cudaMalloc of " + std::to_string(want) + " bytes failed";
+      return RELX_ERR_NOMEM;
+    }
+    bytes = want;
+    return 0;
+  }
+  template <typename T>
+  T *as() const { return reinterpret_cast<T *>(p); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+template <typename T>
+static int upload(DevBuf &b, const std::vector<T> &v) {
+  int st = b.reserve(sizeof(T) * std::max<size_t>(v.size(), 1));
+  if (st) return st;
+  if (!v.empty()) RELX_CUDA(cudaMemcpy(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// tables
+// ---------------------------------------------------------------------------
+struct Tables {
+  RelxTables d{};
+  DevBuf rel_a, rel_mu0, rel_r, rel_gmin, rel_gmax, rel_tc;
+  DevBuf lp_a, lp_h, lp_rad, lp_intens, lp_del, lp_delinc;
+  DevBuf x_vals, x_spec, x_e;
+  DevBuf conv_e, conv_eff, conv_inv_emid, conv_cf, coarse_e;
+  DevBuf rb_imin, rb_imax, rb_fmin, rb_fmax;
+  size_t bytes_total = 0;
+  bool loaded = false;
+  void release() {
+    for (DevBuf *b : {&rel_a, &rel_mu0, &rel_r, &rel_gmin, &rel_gmax, &rel_tc, &lp_a, &lp_h, &lp_rad, &lp_intens,
+                      &lp_del, &lp_delinc, &x_vals, &x_spec, &x_e, &conv_e, &conv_eff, &conv_inv_emid, &conv_cf,
+                      &coarse_e, &rb_imin, &rb_imax, &rb_fmin, &rb_fmax})
+      b->release();
+    loaded = false;
+  }
+};
+
+static void log_grid(std::vector<double> &e, int n, double emin, double emax) {
+  // get_log_grid, relutility.c:399-405
+  e.resize(n);
+  for (int ii = 0; ii < n; ii++) e[ii] = std::exp(1.0 * ii / (n - 1) * (std::log(emax) - std::log(emin)) + std::log(emin));
+}
+
+static int load_relline(const std::string &dir, Tables &T) {
+  FitsFile f;
+  std::string err;
+  if (!f.open(dir + "/rel_table_v0.5a.fits", &err)) { g_errmsg = err; return RELX_ERR_NOTABLE; }
+  const FitsHdu *ha = f.find("a"), *hm = f.find("mu0");
+  if (!ha || !hm) { g_errmsg = "relline table: missing a/mu0 extensions"; return RELX_ERR_TABLE; }
+  int na = (int) ha->nrows, nm = (int) hm->nrows;
+  std::vector<float> a(na), mu0(nm);
+  f.read_f32(*ha, ha->col("a"), 0, na, a.data());
+  f.read_f32(*hm, hm->col("mu0"), 0, nm, mu0.data());
+  const auto &H = f.hdus();
+  if ((int) H.size() < na * nm + 3) { g_errmsg = "relline table: too few extensions"; return RELX_ERR_TABLE; }
+  const FitsHdu &h0 = H[3];
+  int nr = (int) h0.nrows, ng = (int) h0.cols[h0.col("trff1")].repeat;
+  if (nr > RELX_MAX_NRTAB || ng > RELX_MAX_NG || nr < 2 || ng < 3) {
+    g_errmsg = "relline table dimensions exceed the kernel limits";
+    return RELX_ERR_TABLE;
+  }
+  std::vector<float> r((size_t) na * nm * nr), gmin(r.size()), gmax(r.size());
+  std::vector<float4> tc((size_t) na * nm * nr * ng);
+  std::vector<float> t1((size_t) nr * ng), t2(t1.size()), c1(t1.size()), c2(t1.size());
+  for (int ii = 0; ii < na; ii++) {
+    for (int jj = 0; jj < nm; jj++) {
+      const FitsHdu &h = H[ii * nm + jj + 3];  // HDU number ii*n_mu0+jj+4 (reltable.c:290)
+      if (h.nrows != nr) { g_errmsg = "relline table: inconsistent rows"; return RELX_ERR_TABLE; }
+      size_t b = (size_t) ii * nm + jj;
+      std::vector<unsigned char> raw((size_t) (nr * h.width));
+      bool ok = f.read_rows(h, 0, nr, raw.data()) && decode_f32(h, h.col("r"), raw.data(), nr, &r[b * nr]) &&
+                decode_f32(h, h.col("gmin"), raw.data(), nr, &gmin[b * nr]) &&
+                decode_f32(h, h.col("gmax"), raw.data(), nr, &gmax[b * nr]) &&
+                decode_f32(h, h.col("trff1"), raw.data(), nr, t1.data()) &&
+                decode_f32(h, h.col("trff2"), raw.data(), nr, t2.data()) &&
+                decode_f32(h, h.col("cosne1"), raw.data(), nr, c1.data()) &&
+                decode_f32(h, h.col("cosne2"), raw.data(), nr, c2.data());
+      if (!ok) { g_errmsg = "relline table: read failed"; return RELX_ERR_TABLE; }
+      for (int q = 0; q < nr * ng; q++) tc[b * nr * ng + q] = make_float4(t1[q], t2[q], c1[q], c2[q]);
+    }
+  }
+  int st;
+  if ((st = upload(T.rel_a, a)) || (st = upload(T.rel_mu0, mu0)) || (st = upload(T.rel_r, r)) ||
+      (st = upload(T.rel_gmin, gmin)) || (st = upload(T.rel_gmax, gmax)) || (st = upload(T.rel_tc, tc)))
+    return st;
+  T.d.rel_na = na; T.d.rel_nmu0 = nm; T.d.rel_nr = nr; T.d.rel_ng = ng;
+  T.d.rel_a = T.rel_a.as<float>(); T.d.rel_mu0 = T.rel_mu0.as<float>();
+  T.d.rel_r = T.rel_r.as<float>(); T.d.rel_gmin = T.rel_gmin.as<float>(); T.d.rel_gmax = T.rel_gmax.as<float>();
+  T.d.rel_tc = T.rel_tc.as<float4>();
+  T.bytes_total += r.size() * 12 + tc.size() * 16;
+  return 0;
+}
+
+static int load_lp(const std::string &dir, Tables &T) {
+  FitsFile f;
+  std::string err;
+  if (!f.open(dir + "/rel_lp_table_v0.5b.fits", &err)) { g_errmsg = err; return RELX_ERR_NOTABLE; }
+  const FitsHdu *h = f.find("I_h");
+  if (!h) { g_errmsg = "lamp-post table: missing I_h"; return RELX_ERR_TABLE; }
+  int na = (int) h->nrows;
+  int nh = (int) h->cols[h->col("hgrid")].repeat, nrad = (int) h->cols[h->col("r")].repeat;
+  if (nrad > RELX_MAX_NRADLP) { g_errmsg = "lamp-post table radii exceed the kernel limit"; return RELX_ERR_TABLE; }
+  std::vector<float> a(na), hg((size_t) na * nh), rad((size_t) na * nrad);
+  std::vector<float> in((size_t) na * nh * nrad), dl(in.size()), di(in.size()), tmp((size_t) na * nrad);
+  std::vector<unsigned char> raw((size_t) (na * h->width));
+  if (!f.read_rows(*h, 0, na, raw.data())) { g_errmsg = "lamp-post table: read failed"; return RELX_ERR_TABLE; }
+  decode_f32(*h, h->col("a"), raw.data(), na, a.data());
+  decode_f32(*h, h->col("hgrid"), raw.data(), na, hg.data());
+  decode_f32(*h, h->col("r"), raw.data(), na, rad.data());
+  for (int k = 0; k < nh; k++) {
+    const std::string ks = std::to_string(k + 1);
+    const char *names[3] = {"h", "del", "del_inc"};
+    std::vector<float> *dst[3] = {&in, &dl, &di};
+    for (int q = 0; q < 3; q++) {
+      int c = h->col(names[q] + ks);
+      if (c < 0 || !decode_f32(*h, c, raw.data(), na, tmp.data())) { g_errmsg = "lamp-post table: column missing"; return RELX_ERR_TABLE; }
+      for (int ia = 0; ia < na; ia++)
+        for (int ir = 0; ir < nrad; ir++) {
+          float v = tmp[(size_t) ia * nrad + ir];
+          if (q > 0) v = std::fabs(v);  // reltable.c:370-377
+          (*dst[q])[((size_t) ia * nh + k) * nrad + ir] = v;
+        }
+    }
+  }
+  int st;
+  if ((st = upload(T.lp_a, a)) || (st = upload(T.lp_h, hg)) || (st = upload(T.lp_rad, rad)) ||
+      (st = upload(T.lp_intens, in)) || (st = upload(T.lp_del, dl)) || (st = upload(T.lp_delinc, di)))
+    return st;
+  T.d.lp_na = na; T.d.lp_nh = nh; T.d.lp_nrad = nrad;
+  T.d.lp_a = T.lp_a.as<float>(); T.d.lp_h = T.lp_h.as<float>(); T.d.lp_rad = T.lp_rad.as<float>();
+  T.d.lp_intens = T.lp_intens.as<float>(); T.d.lp_del = T.lp_del.as<float>(); T.d.lp_delinc = T.lp_delinc.as<float>();
+  T.bytes_total += in.size() * 12;
+  return 0;
+}
+
+static const char *kXillNames[] = {"Gamma", "A_Fe", "logXi", "Ecut", "kTe", "Dens", "kTbb", "A_CO", "Frac", "Incl"};
+static const int kXillIndex[] = {0, 1, 2, 3, 3, 4, 5, 1, 6, 7};  // common.h:141-150, xilltable.c:24-27
+
+static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &xe_host) {
+  FitsFile f;
+  std::string err;
+  if (!f.open(dir + "/xillver-a-Ec5.fits", &err)) { g_errmsg = err; return RELX_ERR_NOTABLE; }
+  const FitsHdu *hp = f.find("PARAMETERS"), *he = f.find("ENERGIES"), *hs = f.find("SPECTRA");
+  if (!hp || !he || !hs) { g_errmsg = "xillver table: missing extensions"; return RELX_ERR_TABLE; }
+  int npar = (int) hp->nrows;
+  if (npar != 5) { g_errmsg = "xillver table: only 5-parameter tables are supported"; return RELX_ERR_TABLE; }
+  std::vector<std::string> names;
+  std::vector<double> nv(npar);
+  f.read_str(*hp, 0, 0, npar, &names);
+  f.read_f64(*hp, 8, 0, npar, nv.data());
+  int maxv = (int) hp->cols[9].repeat;
+  std::vector<float> vals((size_t) npar * maxv);
+  f.read_f32(*hp, 9, 0, npar, vals.data());
+  int pidx[RELX_MAX_XPAR];
+  int nvals[RELX_MAX_XPAR];
+  int has_dens = 0, q_lxi = -1;
+  for (int q = 0; q < npar; q++) {
+    nvals[q] = (int) nv[q];
+    pidx[q] = -1;
+    for (int j = 0; j < 10; j++)
+      if (names[q] == kXillNames[j]) pidx[q] = kXillIndex[j];
+    if (pidx[q] < 0) { g_errmsg = "xillver table: unknown parameter " + names[q]; return RELX_ERR_TABLE; }
+    if (pidx[q] == 4) has_dens = 1;
+    if (pidx[q] == 2) q_lxi = q;
+  }
+  if (pidx[npar - 1] != 7) { g_errmsg = "xillver table: Incl must be the last parameter"; return RELX_ERR_TABLE; }
+  if (nvals[npar - 1] > RELX_MAX_INCL) { g_errmsg = "xillver table: too many inclinations"; return RELX_ERR_TABLE; }
+  int ne = (int) he->nrows;
+  std::vector<float> elo(ne), ehi(ne);
+  f.read_f32(*he, 0, 0, ne, elo.data());
+  f.read_f32(*he, 1, 0, ne, ehi.data());
+  xe_host.resize(ne + 1);
+  for (int i = 0; i < ne; i++) xe_host[i] = elo[i];  // xilltable.c:1104-1109
+  xe_host[ne] = ehi[ne - 1];
+  int64_t rows = 1;
+  for (int q = 0; q < npar; q++) rows *= nvals[q];
+  if (hs->nrows != rows) { g_errmsg = "xillver table: SPECTRA row count"; return RELX_ERR_TABLE; }
+  const FitsColumn &sc = hs->cols[1];
+  if (sc.code != 'E' || sc.repeat != ne) { g_errmsg = "xillver table: SPECTRA column"; return RELX_ERR_TABLE; }
+  const int pad = (ne + 3) / 4 * 4;
+  // strides of the row index (incl fastest, xilltable.c:325-337)
+  int64_t stride_lxi = 1;
+  for (int q = npar - 1; q > q_lxi; q--) stride_lxi *= nvals[q];
+  int st = T.x_spec.reserve(sizeof(float) * (size_t) rows * pad);
+  if (st) return st;
+  // read, renormalise by 10^-logXi of the row's grid point (renorm_xill_spec, xilltable.c:478-485), upload in chunks
+  const int64_t chunk = 4096;
+  std::vector<unsigned char> raw((size_t) (chunk * hs->width));
+  std::vector<float> buf((size_t) chunk * pad);
+  float *dst = T.x_spec.as<float>();
+  for (int64_t r0 = 0; r0 < rows; r0 += chunk) {
+    int64_t nr = std::min(chunk, rows - r0);
+    if (!f.read_rows(*hs, r0, nr, raw.data())) { g_errmsg = "xillver table: read failed"; return RELX_ERR_TABLE; }
+    int nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; t++) {
+      th.emplace_back([&, t]() {
+        for (int64_t r = t; r < nr; r += nth) {
+          int64_t row = r0 + r;
+          double lxi = 0.0;
+          if (q_lxi >= 0) lxi = vals[(size_t) q_lxi * maxv + (row / stride_lxi) % nvals[q_lxi]];
+          const double div = std::pow(10, lxi);
+          const unsigned char *p = raw.data() + r * hs->width + sc.offset;
+          float *o = buf.data() + (size_t) r * pad;
+          for (int e = 0; e < ne; e++) {
+            float v = be_f32(p + 4 * e);
+            v /= div;  // float / double, stored as float (xilltable.c:480)
+            o[e] = v;
+          }
+          for (int e = ne; e < pad; e++) o[e] = 0.0f;
+        }
+      });
+    }
+    for (auto &x : th) x.join();
+    RELX_CUDA(cudaMemcpy(dst + (size_t) r0 * pad, buf.data(), sizeof(float) * (size_t) nr * pad, cudaMemcpyHostToDevice));
+  }
+  std::vector<double> xe = xe_host;
+  if ((st = upload(T.x_vals, vals)) || (st = upload(T.x_e, xe))) return st;
+  T.d.x_npar = npar; T.d.x_nener = ne; T.d.x_nener_pad = pad; T.d.x_nincl = nvals[npar - 1];
+  for (int q = 0; q < RELX_MAX_XPAR; q++) { T.d.x_nvals[q] = q < npar ? nvals[q] : 0; T.d.x_pindex[q] = q < npar ? pidx[q] : -1; }
+  T.d.x_has_dens = has_dens;
+  T.d.x_vals = T.x_vals.as<float>();
+  T.d.x_maxvals = maxv;
+  T.d.x_spec = T.x_spec.as<float>();
+  T.d.x_rows = rows;
+  T.d.x_e = T.x_e.as<double>();
+  T.bytes_total += (size_t) rows * pad * 4;
+  return 0;
+}
+
+// the reference's _rebin_spectrum walk (relutility.c:549-601) as a per-output-bin map
+static void rebin_map(const std::vector<double> &ener, const std::vector<double> &ener0, std::vector<int> &imn,
+                      std::vector<int> &imx, std::vector<float> &fmn, std::vector<float> &fmx) {
+  const int nbins = (int) ener.size() - 1, nbins0 = (int) ener0.size() - 1;
+  imn.assign(nbins, -1);
+  imx.assign(nbins, -1);
+  fmn.assign(nbins, 0.0f);
+  fmx.assign(nbins, 0.0f);
+  int imin = 0, imax = 0;
+  for (int ii = 0; ii < nbins; ii++) {
+    if ((ener0[0] <= ener[ii + 1]) && (ener0[nbins0] >= ener[ii])) {
+      while (imin <= nbins0 && ener0[imin] <= ener[ii]) imin++;
+      if (imin > 0) imin--;
+      while (imax < nbins0 && ener0[imax] <= ener[ii + 1]) imax++;
+      if (imax > 0) imax--;
+      double elo = ener[ii], ehi = ener[ii + 1];
+      if (elo < ener0[imin]) elo = ener0[imin];
+      if (ehi > ener0[imax + 1]) ehi = ener0[imax + 1];
+      imn[ii] = imin;
+      imx[ii] = imax;
+      if (imax == imin) {
+        fmn[ii] = (float) ((ehi - elo) / (ener0[imin + 1] - ener0[imin]));
+      } else {
+        fmn[ii] = (float) ((ener0[imin + 1] - elo) / (ener0[imin + 1] - ener0[imin]));
+        fmx[ii] = (float) ((ehi - ener0[imax]) / (ener0[imax + 1] - ener0[imax]));
+      }
+    }
+  }
+}
+
+static int load_tables(const std::string &dir, Tables &T) {
+  T.release();
+  T.d = RelxTables{};
+  T.bytes_total = 0;
+  std::vector<double> xe;
+  int st;
+  if ((st = load_relline(dir, T)) || (st = load_lp(dir, T)) || (st = load_xillver(dir, T, xe))) return st;
+  // conv grid (get_relxill_conv_energy_grid, Xillspec.cpp:44-54) and derived arrays
+  std::vector<double> ce;
+  log_grid(ce, RELX_NCONV + 1, RELX_EMIN_CONV, RELX_EMAX_CONV);
+  std::vector<float2> ceff(ce.size());
+  std::vector<float> inv_emid(RELX_NCONV), cf(RELX_NCONV);
+  for (size_t i = 0; i < ce.size(); i++) {
+    float hi = (float) ce[i];
+    ceff[i] = make_float2(hi, (float) (ce[i] - (double) hi));
+  }
+  int band_lo = RELX_NCONV, band_hi = -1;
+  for (int j = 0; j < RELX_NCONV; j++) {
+    inv_emid[j] = (float) (1.0 / (0.5 * (ce[j] + ce[j + 1])));
+    cf[j] = (float) (0.5 * (ce[j] + ce[j + 1]) / (ce[j + 1] - ce[j]));  // Relbase.cpp:93-103
+    if (ce[j] >= RELX_EMIN_XILL && ce[j + 1] < RELX_EMAX_XILL) {   // Relbase.cpp:205
+      band_lo = std::min(band_lo, j);
+      band_hi = std::max(band_hi, j);
+    }
+  }
+  int pos1 = 0;
+  {  // binary_search(ener, n+1, 1.0), Relbase.cpp:133-137
+    int klo = 0, khi = RELX_NCONV;
+    while (khi - klo > 1) { int k = (khi + klo) / 2; if (ce[k] > 1.0) khi = k; else klo = k; }
+    pos1 = klo;
+  }
+  std::vector<double> co;
+  log_grid(co, RELX_NCOARSE + 1, RELX_EMIN_NORM, RELX_EMAX_NORM);
+  std::vector<int> imn, imx;
+  std::vector<float> fmn, fmx;
+  rebin_map(ce, xe, imn, imx, fmn, fmx);
+  if ((st = upload(T.conv_e, ce)) || (st = upload(T.conv_eff, ceff)) || (st = upload(T.conv_inv_emid, inv_emid)) ||
+      (st = upload(T.conv_cf, cf)) || (st = upload(T.coarse_e, co)) || (st = upload(T.rb_imin, imn)) ||
+      (st = upload(T.rb_imax, imx)) || (st = upload(T.rb_fmin, fmn)) || (st = upload(T.rb_fmax, fmx)))
+    return st;
+  T.d.conv_e = T.conv_e.as<double>();
+  T.d.conv_eff = T.conv_eff.as<float2>();
+  T.d.conv_inv_emid = T.conv_inv_emid.as<float>();
+  T.d.conv_cf = T.conv_cf.as<float>();
+  T.d.conv_pos1 = pos1;
+  T.d.conv_band_lo = band_lo;
+  T.d.conv_band_hi = band_hi;
+  T.d.coarse_e = T.coarse_e.as<double>();
+  T.d.rb_imin = T.rb_imin.as<int>();
+  T.d.rb_imax = T.rb_imax.as<int>();
+  T.d.rb_fmin = T.rb_fmin.as<float>();
+  T.d.rb_fmax = T.rb_fmax.as<float>();
+  T.loaded = true;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// workspace and batch evaluation
+// ---------------------------------------------------------------------------
+static int model_nparams(int model) {
+  switch (model) {
+    case RELX_RELLINE: return 10;   // lmodel_relxill_public.dat:1-11
+    case RELX_RELCONV: return 8;    // :13-21
+    case RELX_RELXILL: return 13;   // :46-59
+    case RELX_RELXILLLP: return 14; // :61-75
+    default: return -1;
+  }
+}
+
+struct EnvOpts {
+  int nzones_env = 0, flags = 0;
+};
+static EnvOpts read_env() {
+  EnvOpts o;
+  const char *v = std::getenv("RELXILL_NUM_RZONES");
+  if (v) o.nzones_env = (int) std::atof(v);
+  v = std::getenv("RELLINE_PHYSICAL_NORM");
+  if (v && (int) std::strtod(v, nullptr) == 1) o.flags |= 1;
+  v = std::getenv("RELXILL_RENORMALIZE");
+  if (v && (int) std::atof(v) == 1) o.flags |= 2;
+  v = std::getenv("RELXILL_CONSTANT_DENSITY");
+  if (v && (int) std::strtod(v, nullptr) == 1) o.flags |= 4;
+  return o;
+}
+
+// number of zones a set will use (get_num_zones, relutility.c:506-544)
+static int zones_for(int model, int ion_grad_type, int envn) {
+  if (ion_grad_type != 0) return (envn > 9 && envn <= RELX_NZMAX) ? envn : RELX_NZONES_IONGRAD;
+  if (model == RELX_RELXILLLP) return (envn > 0 && envn <= RELX_NZMAX) ? envn : RELX_NZONES;
+  return 1;
+}
+
+struct Workspace {
+  DevBuf setin, st, rad, corners, zcorners, line_e, prof, dist, tsum, xill, cout, user_e, user_f, flux, sflag,
+      status, err, params, eoff, igt, igi;
+  void release() {
+    for (DevBuf *b : {&setin, &st, &rad, &corners, &zcorners, &line_e, &prof, &dist, &tsum, &xill, &cout, &user_e,
+                      &user_f, &flux, &sflag, &status, &err, &params, &eoff, &igt, &igi})
+      b->release();
+  }
+};
+
+struct Context {
+  std::mutex mu;
+  Tables T;
+  Workspace W;
+  cudaStream_t stream = nullptr;
+  int device = -1;
+  std::string table_dir;
+  bool attrs_set = false;
+  // pinned host staging for the host-buffer API
+  void *h_pin = nullptr;
+  size_t h_pin_bytes = 0;
+};
+
+static Context &ctx() {
+  static Context *c = new Context();
+  return *c;
+}
+
+static int set_kernel_attrs(const Tables &T) {
+  RELX_CUDA(cudaFuncSetAttribute(setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) setup_smem_bytes()));
+  size_t ls = line_smem_bytes(T.d.rel_nr, T.d.rel_ng);
+  RELX_CUDA(relline_set_smem(ls));
+  RELX_CUDA(cudaFuncSetAttribute(xillver_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int) xill_smem_bytes(T.d.x_nincl)));
+  RELX_CUDA(cudaFuncSetAttribute(conv_zone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
+  RELX_CUDA(cudaFuncSetAttribute(relconv_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
+  RELX_CUDA(cudaFuncSetAttribute(finalize_relxill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) fin_smem_bytes()));
+  return 0;
+}
+
+static int ensure_init(Context &C, const char *path) {
+  if (C.T.loaded && (!path || C.table_dir == path)) return 0;
+  std::string dir;
+  if (path) dir = path;
+  else {
+    const char *e = std::getenv("RELXILL_TABLE_PATH");  // relutility.c:320-328
+    dir = e ? e : "./";
+  }
+  RELX_CUDA(cudaGetDevice(&C.device));
+  if (!C.stream) RELX_CUDA(cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking));
+  int st = load_tables(dir, C.T);
+  if (st) return st;
+  C.table_dir = dir;
+  if ((st = set_kernel_attrs(C.T))) return st;
+  return 0;
+}
+
+// pack (params, energy offsets) into RelxSetIn on the device
+__global__ void pack_kernel(int n_sets, int npar, const double *__restrict__ params, const int64_t *__restrict__ eoff,
+                            const int *__restrict__ igt, const double *__restrict__ igi, int nzones_env, int flags,
+                            RelxSetIn *__restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_sets) return;
+  RelxSetIn s;
+  for (int q = 0; q < RELX_NPARAM_MAX; q++) s.p[q] = q < npar ? params[(size_t) i * npar + q] : 0.0;
+  s.e_off = eoff[i];
+  s.n_ener = (int) (eoff[i + 1] - eoff[i] - 1);
+  s.ion_grad_type = igt ? igt[i] : 0;
+  s.iongrad_index = igi ? igi[i] : 0.0;
+  s.nzones_env = nzones_env;
+  s.flags = flags;
+  out[i] = s;
+}
+
+__global__ void status_kernel(int n_sets, const RelxSetState *__restrict__ st, const int *__restrict__ sflag,
+                              const int *__restrict__ err, int *__restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_sets) return;
+  int s = st[i].status;
+  if (s == RELX_OK && sflag[i] != RELX_OK) s = sflag[i];
+  if (s == RELX_OK && *err != RELX_OK) s = *err;
+  out[i] = s;
+}
+
+struct BatchShape {
+  int model, n_sets, nza, ntile_max;
+  int64_t n_edges;  // total energy edges
+};
+
+static int reserve_workspace(Context &C, const BatchShape &b, bool need_zone_corners) {
+  Workspace &W = C.W;
+  const size_t S = b.n_sets;
+  const size_t nza = b.nza;
+  int st;
+  if ((st = W.setin.reserve(S * sizeof(RelxSetIn))) || (st = W.st.reserve(S * sizeof(RelxSetState))) ||
+      (st = W.rad.reserve(S * sizeof(RelxRadial))) || (st = W.dist.reserve(S * nza * RELX_MAX_INCL * sizeof(float))) ||
+      (st = W.tsum.reserve(S * b.ntile_max * nza * sizeof(double))) ||
+      (st = W.user_e.reserve(b.n_edges * sizeof(double))) || (st = W.flux.reserve(b.n_edges * sizeof(double))) ||
+      (st = W.sflag.reserve(S * sizeof(int))) || (st = W.status.reserve(S * sizeof(int))) ||
+      (st = W.err.reserve(sizeof(int))))
+    return st;
+  if (b.model == RELX_RELLINE) {
+    if ((st = W.line_e.reserve(b.n_edges * sizeof(double))) || (st = W.prof.reserve(b.n_edges * sizeof(float))))
+      return st;
+  } else {
+    if ((st = W.prof.reserve(S * nza * RELX_NCONV * sizeof(float))) ||
+        (st = W.cout.reserve(S * nza * RELX_NCONV * sizeof(float))))
+      return st;
+    if (b.model == RELX_RELCONV && (st = W.user_f.reserve(b.n_edges * sizeof(double)))) return st;
+  }
+  if (b.model >= RELX_RELXILL) {
+    if ((st = W.corners.reserve(S * sizeof(RelxCorners))) ||
+        (st = W.xill.reserve(S * nza * (size_t) C.T.d.x_nener_pad * sizeof(float))))
+      return st;
+    if (need_zone_corners && (st = W.zcorners.reserve(S * sizeof(RelxZoneCorners)))) return st;
+  }
+  return 0;
+}
+
+// the kernel sequence for one batch; all pointers are device pointers, asynchronous on `s`
+static int launch_batch(Context &C, const BatchShape &b, cudaStream_t s) {
+  const RelxTables &tab = C.T.d;
+  Workspace &W = C.W;
+  const int S = b.n_sets;
+  RelxSetIn *sin = W.setin.as<RelxSetIn>();
+  RelxSetState *sst = W.st.as<RelxSetState>();
+  RelxRadial *rad = W.rad.as<RelxRadial>();
+  RelxCorners *cor = W.corners.as<RelxCorners>();
+  RelxZoneCorners *zcor = W.zcorners.as<RelxZoneCorners>();
+  RELX_CUDA(cudaMemsetAsync(W.sflag.p, 0, S * sizeof(int), s));
+  RELX_CUDA(cudaMemsetAsync(W.err.p, 0, sizeof(int), s));
+  setup_kernel<<<S, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, b.model, sin, W.user_e.as<double>(),
+                                                             W.line_e.as<double>(), sst, rad, cor, zcor);
+  const size_t ls = line_smem_bytes(tab.rel_nr, tab.rel_ng);
+  dim3 lg(b.ntile_max, S);
+  RELX_CUDA(launch_relline(b.model >= RELX_RELXILL, lg, ls, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza,
+                           W.prof.as<float>(), W.dist.as<float>(), W.tsum.as<double>(), b.ntile_max));
+  if (b.model >= RELX_RELXILL) {
+    const int nxt = (tab.x_nener_pad + kXillTileH - 1) / kXillTileH;
+    if (b.nza <= RELX_ZDENSE)
+      xillver_dense_kernel<<<dim3(nxt, S), kXillThreadsH, xill_smem_bytes(tab.x_nincl), s>>>(
+          tab, sst, cor, W.dist.as<float>(), b.nza, W.xill.as<float>(), W.err.as<int>());
+    else
+      xillver_zone_kernel<<<dim3(nxt, S), kXillThreadsH, 0, s>>>(tab, sst, zcor, W.dist.as<float>(), b.nza,
+                                                                 W.xill.as<float>());
+    conv_zone_kernel<<<dim3(b.nza, S), kConvThreadsH, conv_smem_bytes(), s>>>(
+        tab, sst, W.prof.as<float>(), W.tsum.as<double>(), b.ntile_max, kLineTileH, W.xill.as<float>(), b.nza,
+        W.cout.as<float>());
+    finalize_relxill_kernel<<<S, kConvThreadsH, fin_smem_bytes(), s>>>(tab, sin, sst, W.cout.as<float>(), b.nza,
+                                                                       W.user_e.as<double>(), W.flux.as<double>());
+  } else if (b.model == RELX_RELCONV) {
+    relconv_conv_kernel<<<S, kConvThreadsH, conv_smem_bytes(), s>>>(
+        tab, sin, sst, W.prof.as<float>(), W.tsum.as<double>(), b.ntile_max, kLineTileH, b.nza, W.user_e.as<double>(),
+        W.user_f.as<double>(), W.cout.as<float>(), W.sflag.as<int>());
+    finalize_relconv_kernel<<<S, kConvThreadsH, 0, s>>>(tab, sin, sst, W.cout.as<float>(), b.nza,
+                                                        W.user_e.as<double>(), W.sflag.as<int>(), W.flux.as<double>());
+  } else {
+    finalize_relline_kernel<<<S, kConvThreadsH, 0, s>>>(sin, sst, W.prof.as<float>(), W.tsum.as<double>(),
+                                                        b.ntile_max, kLineTileH, b.nza, W.flux.as<double>());
+  }
+  status_kernel<<<(S + 255) / 256, 256, 0, s>>>(S, sst, W.sflag.as<int>(), W.err.as<int>(), W.status.as<int>());
+  RELX_CUDA(cudaGetLastError());
+  return 0;
+}
+
+static int batch_shape(int model, int n_sets, const int64_t *eoff_host, const int *igt_host, const EnvOpts &env,
+                       BatchShape *b, bool *need_zc) {
+  b->model = model;
+  b->n_sets = n_sets;
+  b->n_edges = eoff_host[n_sets];
+  int nza = 1, maxn = 0;
+  for (int i = 0; i < n_sets; i++) {
+    int n = (int) (eoff_host[i + 1] - eoff_host[i] - 1);
+    if (n < 1) return RELX_ERR_ARG;
+    maxn = std::max(maxn, n);
+    nza = std::max(nza, zones_for(model, igt_host ? igt_host[i] : 0, env.nzones_env));
+  }
+  b->nza = nza;
+  const int gmax = (model == RELX_RELLINE) ? maxn : RELX_NCONV;
+  b->ntile_max = (gmax + kLineTileH - 1) / kLineTileH;
+  *need_zc = nza > RELX_ZDENSE;
+  return 0;
+}
+
+static int pinned(Context &C, size_t bytes) {
+  if (bytes <= C.h_pin_bytes) return 0;
+  if (C.h_pin) cudaFreeHost(C.h_pin);
+  C.h_pin = nullptr;
+  C.h_pin_bytes = 0;
+  RELX_CUDA(cudaMallocHost(&C.h_pin, bytes));
+  C.h_pin_bytes = bytes;
+  return 0;
+}
+
+// host-buffer evaluation: copies in, evaluates, copies out, synchronises
+static int eval_host(int model, int n_sets, const double *params, const double *energy, const int64_t *eoff,
+                     const double *flux_in, double *flux, int *status, const int *igt, const double *igi) {
+  if (model < 0 || model >= RELX_NMODELS || n_sets <= 0 || !params || !energy || !eoff || !flux) return RELX_ERR_ARG;
+  if (model == RELX_RELCONV && !flux_in) return RELX_ERR_ARG;
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  int st = ensure_init(C, nullptr);
+  if (st) return st;
+  const EnvOpts env = read_env();
+  BatchShape b;
+  bool need_zc = false;
+  if ((st = batch_shape(model, n_sets, eoff, igt, env, &b, &need_zc))) return st;
+  if ((st = reserve_workspace(C, b, need_zc))) return st;
+  const int npar = model_nparams(model);
+  cudaStream_t s = C.stream;
+  Workspace &W = C.W;
+  // stage inputs through pinned memory
+  const size_t pb = sizeof(double) * (size_t) n_sets * npar, eb = sizeof(double) * (size_t) b.n_edges;
+  const size_t ob = sizeof(int64_t) * (size_t) (n_sets + 1), gb = igt ? sizeof(int) * n_sets : 0,
+               ib = igi ? sizeof(double) * n_sets : 0;
+  const size_t fb = (model == RELX_RELCONV) ? eb : 0;
+  if ((st = pinned(C, pb + eb + ob + gb + ib + fb + eb + 64 * 8))) return st;
+  unsigned char *h = (unsigned char *) C.h_pin;
+  size_t off = 0;
+  auto put = [&](const void *src, size_t n) {
+    size_t o = off;
+    if (n) std::memcpy(h + o, src, n);
+    off += (n + 63) / 64 * 64;
+    return o;
+  };
+  size_t o_p = put(params, pb), o_e = put(energy, eb), o_o = put(eoff, ob);
+  size_t o_g = igt ? put(igt, gb) : 0, o_i = igi ? put(igi, ib) : 0;
+  size_t o_f = 0;
+  if (model == RELX_RELCONV) {
+    // input flux arrives with n per set; spread to the edge layout (offset e_off per set)
+    o_f = off;
+    double *fi = (double *) (h + o_f);
+    for (int i = 0; i < n_sets; i++) {
+      int n = (int) (eoff[i + 1] - eoff[i] - 1);
+      std::memcpy(fi + eoff[i], flux_in + (eoff[i] - i), sizeof(double) * n);
+    }
+    off += (fb + 63) / 64 * 64;
+  }
+  DevBuf &d_params = W.params, &d_eoff = W.eoff, &d_igt = W.igt, &d_igi = W.igi;
+  if ((st = d_params.reserve(pb)) || (st = d_eoff.reserve(ob)) || (igt && (st = d_igt.reserve(gb))) ||
+      (igi && (st = d_igi.reserve(ib))))
+    return st;
+  RELX_CUDA(cudaMemcpyAsync(d_params.p, h + o_p, pb, cudaMemcpyHostToDevice, s));
+  RELX_CUDA(cudaMemcpyAsync(W.user_e.p, h + o_e, eb, cudaMemcpyHostToDevice, s));
+  RELX_CUDA(cudaMemcpyAsync(d_eoff.p, h + o_o, ob, cudaMemcpyHostToDevice, s));
+  if (igt) RELX_CUDA(cudaMemcpyAsync(d_igt.p, h + o_g, gb, cudaMemcpyHostToDevice, s));
+  if (igi) RELX_CUDA(cudaMemcpyAsync(d_igi.p, h + o_i, ib, cudaMemcpyHostToDevice, s));
+  if (model == RELX_RELCONV) RELX_CUDA(cudaMemcpyAsync(W.user_f.p, h + o_f, fb, cudaMemcpyHostToDevice, s));
+  pack_kernel<<<(n_sets + 127) / 128, 128, 0, s>>>(n_sets, npar, d_params.as<double>(), d_eoff.as<int64_t>(),
+                                                   igt ? d_igt.as<int>() : nullptr, igi ? d_igi.as<double>() : nullptr,
+                                                   env.nzones_env, env.flags, W.setin.as<RelxSetIn>());
+  if ((st = launch_batch(C, b, s))) return st;
+  // results: flux (edge layout minus set index) and statuses
+  const size_t nflux = (size_t) (b.n_edges - n_sets);
+  size_t o_out = off;
+  RELX_CUDA(cudaMemcpyAsync(h + o_out, W.flux.p, nflux * sizeof(double), cudaMemcpyDeviceToHost, s));
+  std::vector<int> sts(n_sets);
+  RELX_CUDA(cudaMemcpyAsync(sts.data(), W.status.p, sizeof(int) * n_sets, cudaMemcpyDeviceToHost, s));
+  RELX_CUDA(cudaStreamSynchronize(s));
+  std::memcpy(flux, h + o_out, nflux * sizeof(double));
+  int worst = 0;
+  for (int i = 0; i < n_sets; i++) {
+    if (status) status[i] = sts[i];
+    if (sts[i] != 0 && worst == 0) worst = sts[i];
+  }
+  return worst;
+}
+
+}  // namespace relx
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using namespace relx;
+
+extern "C" {
+
+int relx_init(const char *table_path) {
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  int st = ensure_init(C, table_path);
+  g_last_status = st;
+  return st;
+}
+
+const char *relx_last_error(void) { return g_errmsg.c_str(); }
+
+int relx_last_status(void) { return g_last_status.load(); }
+
+int relx_eval_batch(int model, int n_sets, const double *params, const double *energy,
+                    const int64_t *energy_offsets, const double *flux_in, double *flux, int *status,
+                    const int *ion_grad_type, const double *iongrad_index) {
+  int st = eval_host(model, n_sets, params, energy, energy_offsets, flux_in, flux, status, ion_grad_type,
+                     iongrad_index);
+  g_last_status = st;
+  return st;
+}
+
+int relx_eval_batch_device(int model, int n_sets, const double *d_params, const double *d_energy,
+                           const int64_t *d_energy_offsets, const int64_t *h_energy_offsets, const double *d_flux_in,
+                           double *d_flux, int *d_status, const int *d_ion_grad_type, const int *h_ion_grad_type,
+                           const double *d_iongrad_index, void *stream) {
+  if (model < 0 || model >= RELX_NMODELS || n_sets <= 0 || !d_params || !d_energy || !d_energy_offsets ||
+      !h_energy_offsets || !d_flux)
+    return RELX_ERR_ARG;
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  int st = ensure_init(C, nullptr);
+  if (st) return st;
+  const EnvOpts env = read_env();
+  BatchShape b;
+  bool need_zc = false;
+  if ((st = batch_shape(model, n_sets, h_energy_offsets, h_ion_grad_type, env, &b, &need_zc))) return st;
+  if ((st = reserve_workspace(C, b, need_zc))) return st;
+  cudaStream_t s = stream ? (cudaStream_t) stream : C.stream;
+  Workspace &W = C.W;
+  RELX_CUDA(cudaMemcpyAsync(W.user_e.p, d_energy, sizeof(double) * b.n_edges, cudaMemcpyDeviceToDevice, s));
+  if (model == RELX_RELCONV) {
+    if (!d_flux_in) return RELX_ERR_ARG;
+    RELX_CUDA(cudaMemcpyAsync(W.user_f.p, d_flux_in, sizeof(double) * b.n_edges, cudaMemcpyDeviceToDevice, s));
+  }
+  pack_kernel<<<(n_sets + 127) / 128, 128, 0, s>>>(n_sets, model_nparams(model), d_params, d_energy_offsets,
+                                                   d_ion_grad_type, d_iongrad_index, env.nzones_env, env.flags,
+                                                   W.setin.as<RelxSetIn>());
+  if ((st = launch_batch(C, b, s))) return st;
+  RELX_CUDA(cudaMemcpyAsync(d_flux, W.flux.p, sizeof(double) * (b.n_edges - n_sets), cudaMemcpyDeviceToDevice, s));
+  if (d_status) RELX_CUDA(cudaMemcpyAsync(d_status, W.status.p, sizeof(int) * n_sets, cudaMemcpyDeviceToDevice, s));
+  return 0;
+}
+
+int relx_table_bytes(int64_t *bytes) {
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  if (!C.T.loaded) return RELX_ERR_NOTABLE;
+  *bytes = (int64_t) C.T.bytes_total;
+  return 0;
+}
+
+void relx_release(void) {
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  if (C.stream) cudaStreamSynchronize(C.stream);
+  C.W.release();
+  C.T.release();
+  if (C.h_pin) cudaFreeHost(C.h_pin);
+  C.h_pin = nullptr;
+  C.h_pin_bytes = 0;
+}
+
+// ---- local-model entry points with the XSPEC signature (create_wrapper_xspec.py:153-162) ----
+static void lmod_eval(int model, const double *energy, int Nflux, const double *parameter, double *flux) {
+  if (!energy || !parameter || !flux || Nflux <= 0) {
+    g_last_status = RELX_ERR_ARG;
+    return;
+  }
+  int64_t eoff[2] = {0, (int64_t) Nflux + 1};
+  int status = 0;
+  std::vector<double> out((size_t) Nflux);
+  std::vector<double> in;
+  if (model == RELX_RELCONV) in.assign(flux, flux + Nflux);
+  int st = eval_host(model, 1, parameter, energy, eoff, model == RELX_RELCONV ? in.data() : nullptr, out.data(),
+                     &status, nullptr, nullptr);
+  g_last_status = st ? st : status;
+  if (st == 0 || st == status) {
+    std::memcpy(flux, out.data(), sizeof(double) * Nflux);
+  } else {
+    std::fprintf(stderr, " *** relxill-gb300 error %d: %s\n", st, g_errmsg.c_str());
+    for (int i = 0; i < Nflux; i++) flux[i] = 0.0;
+  }
+}
+
+void c_lmodrelline(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                   double *fluxError, const char *init) {
+  (void) spectrum; (void) fluxError; (void) init;
+  lmod_eval(RELX_RELLINE, energy, Nflux, parameter, flux);
+}
+void c_lmodrelconv(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                   double *fluxError, const char *init) {
+  (void) spectrum; (void) fluxError; (void) init;
+  lmod_eval(RELX_RELCONV, energy, Nflux, parameter, flux);
+}
+void c_lmodrelxill(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                   double *fluxError, const char *init) {
+  (void) spectrum; (void) fluxError; (void) init;
+  lmod_eval(RELX_RELXILL, energy, Nflux, parameter, flux);
+}
+void c_lmodrelxilllp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                     double *fluxError, const char *init) {
+  (void) spectrum; (void) fluxError; (void) init;
+  lmod_eval(RELX_RELXILLLP, energy, Nflux, parameter, flux);
+}
+
+}  // extern "C"

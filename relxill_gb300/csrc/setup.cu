@@ -1,0 +1,645 @@
+// setup.cu -- per-parameter-set preparation kernel (one CTA per set).
+//
+// Everything the reference computes once per evaluation before the line
+// integration: parameter mapping and bounds (ModelDefinition.cpp:153-385),
+// the (a, mu0) interpolation of the relline table on its own radii and the
+// 1000-point fine radial grid (Relprofile.cpp:141-303, relutility.c:666-677),
+// the emissivity (broken power law, Rellp.cpp:91-109,421-437; lamp post,
+// Rellp.cpp:36-285), the radial zones and ionisation gradient
+// (IonGradient.cpp:128-211,340-390,457-492), the xillver brackets and
+// interpolation factors per zone (xilltable.c:297-323,1054-1181) and the
+// primary-continuum normalisations (Xillspec.cpp:179-233,302-332,408-440).
+// FP64 is used for the radii, the zone grid, the ISCO/horizon and the
+// normalisation sums; per-radius transcendental work that has no
+// cancellation runs in FP32.
+#include "relx_device.cuh"
+
+namespace relx {
+
+constexpr int kSetupThreads = 256;
+
+struct SetupSmem {
+  RelxSetState s;
+  double re_tab[RELX_MAX_NRTAB], gmin_t[RELX_MAX_NRTAB], gmax_t[RELX_MAX_NRTAB];
+  double re[RELX_NFRAD], emis[RELX_NFRAD], del_emit[RELX_NFRAD], del_inc[RELX_NFRAD];
+  double jet_rad[RELX_MAX_NRADLP], le_tab[RELX_MAX_NRADLP], lrad[RELX_MAX_NRADLP];
+  double d_tab[RELX_MAX_NRADLP], di_tab[RELX_MAX_NRADLP];
+  double red[40];
+  int ired[40];
+  int ind_rmin, ind_rmax, status;
+  // parameters beyond the state
+  double emis1, emis2, rbr, htop, lxi, afe, dens, iongrad_index;
+  int return_rad, flags, is_relxill;
+  // lamp post interpolation
+  int lp_ind_a, ind_h[2];
+  double lp_ifac_a, ifac_h[2];
+  // zones
+  double rmean[RELX_NZMAX], shift[RELX_NZMAX], zlxi[RELX_NZMAX], zdens[RELX_NZMAX], xscale[RELX_NZMAX];
+  double zdel_emit[RELX_NZMAX];
+  int zind[RELX_NZMAX][RELX_MAX_XPAR];
+  double zfac[RELX_NZMAX][RELX_MAX_XPAR];
+  int crow[RELX_NZMAX * 16];
+  short cfirst[RELX_NZMAX * 16];
+  short cuniq[RELX_NZMAX * 16];
+};
+
+// ---------------------------------------------------------------------------
+// parameter mapping (lmodel_relxill_public.dat:1-75, ModelDefinition.cpp:153-385)
+// ---------------------------------------------------------------------------
+__device__ void map_params(int model, const RelxSetIn &in, SetupSmem &m) {
+  RelxSetState &s = m.s;
+  const double *v = in.p;
+  s.model = model;
+  s.status = RELX_OK;
+  s.limb = 0;
+  s.height = 0;
+  s.beta = 0;
+  s.z = 0;
+  s.lineE = 0;
+  s.gam = 0;
+  s.refl_frac = 0;
+  s.boost_switch = 0;
+  m.emis1 = m.emis2 = m.rbr = 0;
+  m.htop = 0;
+  m.lxi = 0;
+  m.afe = 0;
+  m.dens = 15;     // ModelDefinition.cpp:362
+  s.ect_src = 300; // ModelDefinition.cpp:360
+  m.return_rad = 0;
+  m.is_relxill = 0;
+  m.flags = in.flags;
+  m.iongrad_index = in.iongrad_index;
+  s.ion_grad_type = in.ion_grad_type;
+  switch (model) {
+    case RELX_RELLINE:
+      s.emis_type = RELX_EMIS_BKN;
+      s.lineE = v[0]; m.emis1 = v[1]; m.emis2 = v[2]; m.rbr = v[3]; s.a = v[4]; s.incl = v[5] * kPi / 180;
+      s.rin = v[6]; s.rout = v[7]; s.z = v[8]; s.limb = (int) llround(v[9]);
+      break;
+    case RELX_RELCONV:
+      s.emis_type = RELX_EMIS_BKN;
+      m.emis1 = v[0]; m.emis2 = v[1]; m.rbr = v[2]; s.a = v[3]; s.incl = v[4] * kPi / 180;
+      s.rin = v[5]; s.rout = v[6]; s.limb = (int) llround(v[7]);
+      break;
+    case RELX_RELXILL:
+      m.is_relxill = 1;
+      s.emis_type = RELX_EMIS_BKN;
+      m.emis1 = v[0]; m.emis2 = v[1]; m.rbr = v[2]; s.a = v[3]; s.incl = v[4] * kPi / 180;
+      s.rin = v[5]; s.rout = v[6]; s.z = v[7]; s.gam = v[8]; m.lxi = v[9]; m.afe = v[10];
+      s.ect_src = v[11]; s.refl_frac = v[12];
+      break;
+    case RELX_RELXILLLP:
+      m.is_relxill = 1;
+      s.emis_type = RELX_EMIS_LP;
+      s.height = v[0]; s.beta = v[1]; s.a = v[2]; s.incl = v[3] * kPi / 180; s.rin = v[4]; s.rout = v[5];
+      s.z = v[6]; s.gam = v[7]; m.lxi = v[8]; m.afe = v[9]; s.ect_src = v[10]; s.refl_frac = v[11];
+      m.return_rad = (int) llround(v[12]);
+      s.boost_switch = (int) llround(v[13]);
+      break;
+    default:
+      s.status = RELX_ERR_ARG;
+      return;
+  }
+  s.gamma = s.gam;
+  // check_parameter_bounds, ModelDefinition.cpp:168-273
+  double rms = kerr_rms(s.a);
+  if (s.rin < 0) s.rin = -1.0 * s.rin * rms;
+  if (s.rout < 0) s.rout = -1.0 * s.rout * rms;
+  if (m.rbr < 0) m.rbr = -1.0 * m.rbr * rms;
+  int bad = 0;
+  if (s.rout <= s.rin) bad = 1;
+  if (s.rin < rms) s.rin = rms;
+  if (s.a > 0.9982 || s.a < -1) bad = 1;
+  if (s.incl < 3 * kPi / 180 || s.incl > 87 * kPi / 180) bad = 1;
+  if (s.rout <= s.rin) bad = 1;
+  if (bad) { s.status = RELX_ERR_PARAM; return; }
+  if (s.rout > 1000.0) s.rout = 1000.0;
+  if (s.emis_type == RELX_EMIS_BKN) {
+    if (m.rbr < s.rin) m.rbr = s.rin;
+    if (m.rbr > s.rout) m.rbr = s.rout;
+  }
+  if (s.emis_type == RELX_EMIS_LP) {
+    if (s.beta < 0) s.beta = 0.0;
+    if (s.beta > 0.99) s.beta = 0.99;
+    double rp = kerr_rplus(s.a);
+    if (s.height < 0) s.height = -1.0 * s.height * rp;
+    if ((1.1 * rp - s.height) > 1e-4) s.height = rp * 1.1;
+  }
+  if (m.return_rad != 0) { s.status = RELX_ERR_UNSUPPORTED; return; }
+  // get_num_zones, relutility.c:506-544 (RELXILL_NUM_RZONES arrives in nzones_env)
+  int envn = in.nzones_env;
+  if (s.ion_grad_type != 0) {
+    s.nz = (envn > 9 && envn <= RELX_NZMAX) ? envn : RELX_NZONES_IONGRAD;
+  } else if (m.is_relxill && s.emis_type == RELX_EMIS_LP) {
+    s.nz = (envn > 0 && envn <= RELX_NZMAX) ? envn : RELX_NZONES;
+  } else {
+    s.nz = 1;
+  }
+  // renormalisation target (renorm_relline_profile, Relprofile.cpp:749-781; do_renorm_model, relutility.c:603-623)
+  int phys = in.flags & 1;
+  s.relline_norm = 1.0;
+  if (m.is_relxill) {
+    if (s.emis_type == RELX_EMIS_LP || phys) s.relline_norm = 0.0;
+    else s.relline_norm = 0.5 * cos(s.incl * 180.0 / kPi * kPi / 180);
+  } else if (phys) {
+    s.relline_norm = 0.0;
+  }
+  // energy shift source -> observer (Relphysics.cpp:239-255) and the source-frame Ecut (Relxill.cpp:196-200)
+  s.g_inf = 1.0;
+  if (s.emis_type == RELX_EMIS_LP) {
+    s.g_inf = calc_g_inf(s.height, s.a);
+    if (!(s.beta < 1e-4)) s.g_inf *= doppler_factor(kPi - s.incl, s.beta);
+    s.ect_src /= s.g_inf;
+  }
+}
+
+// get_rzone_grid / RadialGrid::calculate_radial_grid (relutility.c:265-308, IonGradient.cpp:457-492)
+__device__ void zone_grid(double rmin, double rmax, int nz, double h, double *rg) {
+  if (nz == 1) {
+    rg[0] = rmin;
+    rg[1] = rmax;
+    return;
+  }
+  double r_tr = rmin;
+  int indr = 0;
+  if (h > rmin) {
+    r_tr = h;
+    for (int ii = 0; ii < nz + 1; ii++) rg[ii] = exp(1.0 * ii / nz * (log(rmax) - log(rmin)) + log(rmin));
+    indr = bsearch_asc<double>(rg, nz + 1, r_tr);
+    r_tr = rg[indr];
+  }
+  if (indr < nz) {
+    double rlo = r_tr, rhi = rmax;
+    for (int ii = indr; ii < nz + 1; ii++) {
+      rg[ii] = 1.0 * (ii - indr) / (nz - indr) * (1.0 / rhi - 1.0 / rlo) + 1.0 / rlo;
+      rg[ii] = fabs(1.0 / rg[ii]);
+    }
+  }
+}
+
+// x0 descending; index ii with x0[ii] > xn >= x0[ii+1] (inv_rebin_mean, relutility.c:636-663)
+__device__ double rebin_mean_at(const double *x0, const double *y0, int n0, double xn) {
+  int klo = 0, khi = n0 - 1;  // count of x0 > xn via bisection
+  while (khi - klo > 1) {
+    int k = (khi + klo) >> 1;
+    if (x0[k] > xn) klo = k; else khi = k;
+  }
+  int ii = klo;
+  double f = (xn - x0[ii + 1]) / (x0[ii] - x0[ii + 1]);
+  return lerp1(f, y0[ii + 1], y0[ii]);
+}
+
+// spec_cutoffpl term (Xillspec.cpp:215-233) on one bin, FP32 arithmetic
+__device__ __forceinline__ float cutoffpl_term(double elo, double ehi, float ecut, float gam) {
+  float en = (float) (0.5 * (elo + ehi));
+  return expf(1.0f / ecut) * powf(en, -gam) * expf(-en / ecut) * (float) (ehi - elo);
+}
+
+__global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, int model, const RelxSetIn *__restrict__ sin,
+                                                               const double *__restrict__ user_e, double *__restrict__ line_e,
+                                                               RelxSetState *__restrict__ sout, RelxRadial *__restrict__ rout,
+                                                               RelxCorners *__restrict__ cout, RelxZoneCorners *__restrict__ zcout) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SetupSmem &m = *reinterpret_cast<SetupSmem *>(smem_raw);
+  RelxSetState &s = m.s;
+  const int set = blockIdx.x;
+  const int tid = threadIdx.x;
+  const RelxSetIn &in = sin[set];
+  const int NR = RELX_NFRAD;
+
+  if (tid == 0) {
+    map_params(model, in, m);
+    m.status = s.status;
+  }
+  __syncthreads();
+  if (m.status != RELX_OK) {
+    if (tid == 0) { s.win_lo = 0; s.win_hi = 0; s.nz = 0; sout[set] = s; }
+    return;
+  }
+
+  // ---- line-profile grid: user grid (redshift, 1 keV line) for relline, conv grid otherwise
+  const double *ge;
+  int gn;
+  if (model == RELX_RELLINE) {
+    const double *ue = user_e + in.e_off;
+    double *le = line_e + in.e_off;
+    gn = in.n_ener;
+    for (int j = tid; j <= gn; j += kSetupThreads) {
+      double e = ue[j];
+      if (s.z > 0) e *= (1 + s.z);       // shift_energy_grid_redshift, XspecSpectrum.h:70-76
+      le[j] = e / s.lineE;               // shift_energy_grid_1keV, XspecSpectrum.h:61-65
+    }
+    ge = le;
+  } else {
+    ge = tab.conv_e;
+    gn = RELX_NCONV;
+  }
+
+  // ---- relline table in the (a, mu0) plane on the table radii (Relprofile.cpp:159-223)
+  const int nr = tab.rel_nr, nm = tab.rel_nmu0;
+  if (tid == 0) {
+    double mu0 = cos(s.incl);
+    int ia = bsearch_asc<float>(tab.rel_a, tab.rel_na, (float) s.a);
+    int im = bsearch_asc<float>(tab.rel_mu0, nm, (float) mu0);
+    s.ind_a = ia;
+    s.ind_mu0 = im;
+    s.ifac_a = ((float) s.a - tab.rel_a[ia]) / (tab.rel_a[ia + 1] - tab.rel_a[ia]);
+    s.ifac_mu0 = ((float) mu0 - tab.rel_mu0[im]) / (tab.rel_mu0[im + 1] - tab.rel_mu0[im]);
+    s.g_n = gn;
+    zone_grid(s.rin, s.rout, s.nz, s.height, s.rgrid);
+  }
+  __syncthreads();
+  {
+    const size_t b00 = (size_t) s.ind_a * nm + s.ind_mu0, b10 = (size_t) (s.ind_a + 1) * nm + s.ind_mu0;
+    const size_t b01 = b00 + 1, b11 = b10 + 1;
+    const double fa = s.ifac_a, fm = s.ifac_mu0;
+    for (int i = tid; i < nr; i += kSetupThreads) {
+      m.re_tab[i] = lerp1(fa, tab.rel_r[b00 * nr + i], tab.rel_r[b10 * nr + i]);
+      m.gmin_t[i] = lerp2(fa, fm, tab.rel_gmin[b00 * nr + i], tab.rel_gmin[b10 * nr + i], tab.rel_gmin[b01 * nr + i],
+                          tab.rel_gmin[b11 * nr + i]);
+      m.gmax_t[i] = lerp2(fa, fm, tab.rel_gmax[b00 * nr + i], tab.rel_gmax[b10 * nr + i], tab.rel_gmax[b01 * nr + i],
+                          tab.rel_gmax[b11 * nr + i]);
+    }
+  }
+  // fine radial grid (relutility.c:666-677)
+  {
+    const double r1 = 1.0 / sqrt(s.rout), r2 = 1.0 / sqrt(s.rin);
+    for (int ii = tid; ii < NR; ii += kSetupThreads) {
+      double u = ((double) ii) * (r2 - r1) / (NR - 1) + r1;
+      double iu = 1.0 / u;
+      m.re[ii] = iu * iu;
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double rms = kerr_rms(s.a);
+    if (m.re_tab[nr - 1] > rms && (m.re_tab[nr - 1] - rms) / m.re_tab[nr - 1] < 1e-3) m.re_tab[nr - 1] = rms;
+    m.ind_rmin = bsearch_desc(m.re_tab, nr, s.rin);
+    m.ind_rmax = bsearch_desc(m.re_tab, nr, s.rout);
+    if (m.re_tab[m.ind_rmax] < 1000.0 && m.re_tab[m.ind_rmax] * 1.01 > 1000.0) m.re_tab[m.ind_rmax] = 1000.0;
+  }
+  __syncthreads();
+
+  RelxRadial &R = rout[set];
+  // ---- per fine radius: table radius, interpolation factor, gmin/gmax, weight, zone, bin range
+  int my_lo = 1 << 30, my_hi = -1;
+  for (int ii = tid; ii < NR; ii += kSetupThreads) {
+    double r = m.re[ii];
+    // index ind with re_tab[ind+1] <= r < re_tab[ind], as the walk of Relprofile.cpp:252-266
+    int lo = 0, hi = nr;  // count of table radii > r
+    while (lo < hi) {
+      int k = (lo + hi) >> 1;
+      if (m.re_tab[k] > r) lo = k + 1; else hi = k;
+    }
+    int ind = lo - 1;
+    if (ind > m.ind_rmin) ind = m.ind_rmin;
+    if (ind < 0) {
+      if (r - RELX_RELTABLE_MAX_R <= 1e-6) ind = 0; else atomicExch(&m.status, RELX_ERR_GRID);
+    }
+    if (ind < 0) ind = 0;
+    double ifac = (r - m.re_tab[ind + 1]) / (m.re_tab[ind] - m.re_tab[ind + 1]);
+    if (ifac > 1.0 && ind > 0) atomicExch(&m.status, RELX_ERR_GRID);
+    double gmn = lerp1(ifac, m.gmin_t[ind + 1], m.gmin_t[ind]);
+    double gmx = lerp1(ifac, m.gmax_t[ind + 1], m.gmax_t[ind]);
+    R.re[ii] = r;
+    R.ifac[ii] = ifac;
+    R.gmin[ii] = gmn;
+    R.gmax[ii] = gmx;
+    R.gmin_ff[ii] = ff_from_double(gmn);
+    R.gmax_ff[ii] = ff_from_double(gmx);
+    R.dg_ff[ii] = ff_from_double(gmx - gmn);
+    R.inv_dg[ii] = (float) (1. / (gmx - gmn));
+    {
+      double eh = RELX_GFAC_H * (gmx - gmn) + gmn;
+      R.eH_ff[ii] = ff_from_double(eh);
+      R.e1H_ff[ii] = ff_from_double((1 - RELX_GFAC_H) * (gmx - gmn) + gmn);
+      R.red_H[ii] = eh >= 0.95 ? 1 : 0;
+    }
+    R.itab[ii] = (short) ind;
+    // trapez_integ_single / 2 (relutility.c:233-244)
+    double dr;
+    if (ii == 0) dr = 0.5 * (m.re[0] - m.re[1]);
+    else if (ii == NR - 1) dr = 0.5 * (m.re[ii - 1] - m.re[ii]);
+    else dr = 0.5 * (m.re[ii - 1] - m.re[ii + 1]);
+    R.wt[ii] = (float) (r * dr * kPi / 2);
+    R.zone[ii] = (unsigned char) bsearch_asc<double>(s.rgrid, s.nz + 1, r);
+    // bins of the line-profile grid touched by this radius (Relprofile.cpp:863-878)
+    int ielo = -1, iehi = -1;
+    double egmin = gmn, egmax = gmx;
+    if (egmax > ge[0] && egmin < ge[gn]) {
+      if (egmin < ge[0]) egmin = ge[0];
+      if (egmax > ge[gn]) egmax = ge[gn];
+      ielo = bsearch_asc<double>(ge, gn + 1, egmin);
+      iehi = bsearch_asc<double>(ge, gn + 1, egmax);
+      my_lo = min(my_lo, ielo);
+      my_hi = max(my_hi, iehi);
+    }
+    R.ielo[ii] = ielo;
+    R.iehi[ii] = iehi;
+  }
+  int wlo = block_min_i<kSetupThreads>(my_lo, m.ired);
+  int whi = block_max_i<kSetupThreads>(my_hi, m.ired);
+  if (tid == 0) {
+    s.win_lo = (whi >= 0) ? wlo : 0;
+    s.win_hi = (whi >= 0) ? whi + 1 : 0;
+  }
+
+  // ---- emissivity
+  if (s.emis_type == RELX_EMIS_BKN) {
+    // get_emis_bkn + norm_emis_profile (Rellp.cpp:91-109,421-437)
+    double part = 0.0;
+    for (int ii = tid; ii < NR; ii += kSetupThreads) {
+      double r = m.re[ii];
+      double alpha = (r > m.rbr) ? m.emis2 : m.emis1;
+      double e = (double) powf((float) (r / m.rbr), (float) -alpha);
+      m.emis[ii] = e;
+      m.del_emit[ii] = -1.0;
+      m.del_inc[ii] = -1.0;
+      double dr;
+      if (ii == 0) dr = 0.5 * (m.re[0] - m.re[1]);
+      else if (ii == NR - 1) dr = 0.5 * (m.re[ii - 1] - m.re[ii]);
+      else dr = 0.5 * (m.re[ii - 1] - m.re[ii + 1]);
+      part += e * (r * dr * kPi * 2);
+    }
+    double integ = block_sum_d<kSetupThreads>(part, m.red);
+    for (int ii = tid; ii < NR; ii += kSetupThreads) m.emis[ii] /= integ;
+    if (tid == 0) { s.f_inf_rest = 0; s.refl_frac_lp = 0; }
+  } else {
+    // lamp post: interpol_lptable (Rellp.cpp:190-247)
+    const int nh = tab.lp_nh, nrad = tab.lp_nrad;
+    if (tid == 0) {
+      float fa = (float) s.a;
+      int ia = bsearch_asc<float>(tab.lp_a, tab.lp_na, fa);
+      m.lp_ind_a = ia;
+      m.lp_ifac_a = (fa - tab.lp_a[ia]) / (tab.lp_a[ia + 1] - tab.lp_a[ia]);
+      float fh = (float) s.height;
+      for (int q = 0; q < 2; q++) {
+        const float *hg = tab.lp_h + (size_t) (ia + q) * nh;
+        int ih = bsearch_asc<float>(hg, nh, fh);
+        m.ind_h[q] = ih;
+        m.ifac_h[q] = (fh - hg[ih]) / (hg[ih + 1] - hg[ih]);
+      }
+    }
+    __syncthreads();
+    {
+      const int ia = m.lp_ind_a;
+      const double fa = m.lp_ifac_a;
+      for (int k = tid; k < nrad; k += kSetupThreads) {
+        m.jet_rad[k] = lerp1(fa, tab.lp_rad[(size_t) ia * nrad + k], tab.lp_rad[(size_t) (ia + 1) * nrad + k]);
+#define TV(arr, q, h) (double) (arr)[(((size_t) (ia + (q)) * nh) + (h)) * nrad + k]
+        const int h0 = m.ind_h[0], h1 = m.ind_h[1];
+        const double f0 = m.ifac_h[0], f1 = m.ifac_h[1];
+        double e = (1.0 - fa) * lerp1(f0, TV(tab.lp_intens, 0, h0), TV(tab.lp_intens, 0, h0 + 1))
+            + fa * lerp1(f1, TV(tab.lp_intens, 1, h1), TV(tab.lp_intens, 1, h1 + 1));
+        m.d_tab[k] = (1.0 - fa) * lerp1(f0, TV(tab.lp_del, 0, h0), TV(tab.lp_del, 0, h0 + 1))
+            + fa * lerp1(f1, TV(tab.lp_del, 1, h1), TV(tab.lp_del, 1, h1 + 1));
+        m.di_tab[k] = (1.0 - fa) * lerp1(f0, TV(tab.lp_delinc, 0, h0), TV(tab.lp_delinc, 0, h0 + 1))
+            + fa * lerp1(f1, TV(tab.lp_delinc, 1, h1), TV(tab.lp_delinc, 1, h1 + 1));
+#undef TV
+        m.le_tab[k] = log(e);
+        m.lrad[k] = log(m.jet_rad[k]);
+      }
+    }
+    __syncthreads();
+    // rebin_emisprofile_on_radial_grid (Rellp.cpp:120-175)
+    for (int ii = tid; ii < NR; ii += kSetupThreads) {
+      double r = m.re[ii];
+      int kk = bsearch_asc<double>(m.jet_rad, nrad, r);
+      if (r >= m.jet_rad[nrad - 1] && r - RELX_RELTABLE_MAX_R > 1e-6) atomicExch(&m.status, RELX_ERR_GRID);
+      double inter;
+      if (m.d_tab[kk] / kPi * 180.0 <= 75.0) inter = (r - m.jet_rad[kk]) / (m.jet_rad[kk + 1] - m.jet_rad[kk]);
+      else inter = (log(r) - m.lrad[kk]) / (m.lrad[kk + 1] - m.lrad[kk]);
+      m.emis[ii] = exp(inter * m.le_tab[kk + 1] + (1.0 - inter) * m.le_tab[kk]);
+      m.del_emit[ii] = lerp1(inter, m.d_tab[kk], m.d_tab[kk + 1]);
+      m.del_inc[ii] = lerp1(inter, m.di_tab[kk], m.di_tab[kk + 1]);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      // calc_refl_frac (Rellp.cpp:36-89)
+      double ad_max = m.d_tab[nrad - 1];
+      double del_bh = m.del_emit[bsearch_desc(m.re, NR, s.rin)];
+      double del_ad = m.del_emit[bsearch_desc(m.re, NR, s.rout)];
+      if (ad_max < kPi / 2.0) ad_max = kPi / 2.0;
+      if (s.beta > 1e-6) {
+        del_bh = relat_abberation(del_bh, -1. * s.beta);
+        del_ad = relat_abberation(del_ad, -1. * s.beta);
+      }
+      double f_ad = 0.5 * (cos(del_bh) - cos(del_ad));
+      s.f_inf_rest = 0.5 * (1.0 + cos(ad_max));
+      double f_inf = (s.beta > 1e-6) ? 0.5 * (1.0 + cos(relat_abberation(ad_max, -1. * s.beta))) : s.f_inf_rest;
+      s.refl_frac_lp = f_ad / f_inf;
+    }
+    // apply_emis_fluxboost_source_disk (Rellp.cpp:249-253, Relphysics.cpp:301-311)
+    for (int ii = tid; ii < NR; ii += kSetupThreads) {
+      double gi = gi_potential_lp(m.re[ii], s.a, s.height, s.beta, m.del_emit[ii]);
+      double boost = pow(gi, s.gamma);
+      if (s.beta > 1e-6) {
+        double d = doppler_factor(m.del_emit[ii], s.beta);
+        boost *= d * d;
+      }
+      m.emis[ii] *= boost;
+    }
+  }
+  __syncthreads();
+  for (int ii = tid; ii < NR; ii += kSetupThreads) {
+    R.emis[ii] = (float) m.emis[ii];
+    R.ew[ii] = (float) (m.emis[ii] * (double) R.wt[ii]);
+  }
+
+  // ---- zones: fine-radius index ranges (zone is non-increasing with the radius index)
+  if (tid == 0) {
+    for (int z = 0; z < s.nz; z++) { s.zi0[z] = 1; s.zi1[z] = 0; }
+    int cur = -1;
+    for (int ii = 0; ii < NR; ii++) {
+      int z = R.zone[ii];
+      if (z != cur) { s.zi0[z] = ii; cur = z; }
+      s.zi1[z] = ii;
+    }
+  }
+  if (!m.is_relxill) {
+    __syncthreads();
+    if (tid == 0) {
+      if (m.status != RELX_OK) s.status = m.status;
+      s.src_norm = 0;
+      sout[set] = s;
+    }
+    return;
+  }
+
+  // ---- ionisation gradient (IonGradient.cpp:128-211, 340-390)
+  const int nz = s.nz;
+  if (tid < nz) {
+    int z = tid;
+    m.rmean[z] = 0.5 * (s.rgrid[z] + s.rgrid[z + 1]);
+    m.zdel_emit[z] = rebin_mean_at(m.re, m.del_emit, NR, m.rmean[z]);
+    m.shift[z] = (s.emis_type == RELX_EMIS_LP) ? gi_potential_lp(m.rmean[z], s.a, s.height, s.beta, m.zdel_emit[z]) : 1.0;
+    if (s.ion_grad_type == 1) {
+      double l = exp(m.lxi) * pow(m.rmean[z] / (0.5 * (s.rgrid[0] + s.rgrid[1])), -1.0 * m.iongrad_index);
+      m.zlxi[z] = log(l);
+      m.zdens[z] = m.dens;
+    } else if (s.ion_grad_type == 2) {
+      double rin = s.rgrid[0];
+      double irr = rebin_mean_at(m.re, m.emis, NR, m.rmean[z]);
+      double dinc = rebin_mean_at(m.re, m.del_inc, NR, m.rmean[z]);
+      double rad_lxi = (11. / 9.) * (11. / 9.) * rin;
+      int kk = bsearch_desc(m.re, NR, rad_lxi);
+      double ip = (rad_lxi - m.re[kk + 1]) / (m.re[kk] - m.re[kk + 1]);
+      double emis_r = lerp1(ip, m.emis[kk + 1], m.emis[kk]);
+      double dinc_r = lerp1(ip, m.del_inc[kk + 1], m.del_inc[kk]);
+      double lxi_max = log10(4.0 * kPi * emis_r / density_ss73_zone_a(rad_lxi, rin) * (cos(kPi / 4) / cos(dinc_r)));
+      double fac = m.lxi - lxi_max;
+      double dmin = density_ss73_zone_a((25. / 9.) * rin, rin);
+      double dn = (m.flags & 4) ? 1.0 : density_ss73_zone_a(m.rmean[z], rin) / dmin;
+      m.zdens[z] = log10(dn) + m.dens;
+      m.zlxi[z] = log10(4.0 * kPi * irr / dn * (cos(kPi / 4) / cos(dinc))) + fac;
+    } else {
+      m.zlxi[z] = m.lxi;
+      m.zdens[z] = m.dens;
+    }
+    if (m.zlxi[z] < 0.0) m.zlxi[z] = 0.0;
+    else if (m.zlxi[z] > 4.7) m.zlxi[z] = 4.7;
+  }
+  __syncthreads();
+
+  // ---- xillver brackets and factors per zone (xilltable.c:278-323, 1090-1142)
+  const int npar = tab.x_npar;
+  if (tid < nz) {
+    int z = tid;
+    double ect_z = s.ect_src * m.shift[z];
+    float inp[10];
+    for (int q = 0; q < 10; q++) inp[q] = 0.0f;
+    inp[0] = (float) s.gam;
+    inp[1] = (float) m.afe;
+    inp[2] = (float) m.zlxi[z];
+    inp[3] = (float) ect_z;
+    inp[4] = (float) m.zdens[z];
+    inp[7] = (float) (s.incl * 180 / kPi);
+    for (int q = 0; q < npar; q++) {
+      const float *pv = tab.x_vals + q * tab.x_maxvals;
+      int nv = tab.x_nvals[q];
+      int pi = tab.x_pindex[q];
+      int ind = bsearch_asc<float>(pv, nv, inp[pi]);
+      if (ind < 0) ind = 0;
+      else if (ind > nv - 2) ind = nv - 2;
+      m.zind[z][q] = ind;
+      float val = inp[pi];
+      if (pi != 7) {
+        if (val < pv[0]) val = pv[0];
+        else if (val > pv[nv - 1]) val = pv[nv - 1];
+      }
+      float f = (val - pv[ind]) / (pv[ind + 1] - pv[ind]);
+      m.zfac[z][q] = (double) f;
+      if (pi == 3) {  // ensure_ecut_within_boundarys (xilltable.c:1054-1067)
+        if (ect_z <= pv[0]) m.zfac[z][q] = 0.0;
+        if (ect_z >= pv[nv - 1]) m.zfac[z][q] = 1.0;
+      }
+    }
+  }
+  // ---- normalisation of the primary continuum (Xillspec.cpp:179-205, 302-332, 408-440)
+  {
+    const double *ce = tab.coarse_e;
+    const float gam = (float) s.gam;
+    for (int q = -1; q < nz; q++) {
+      double shift = (q < 0) ? 1.0 : m.shift[q];
+      if (q >= 0 && shift == 1.0) {
+        if (tid == 0) m.xscale[q] = 1.0;
+        continue;
+      }
+      float ecut = (float) (s.ect_src * shift);
+      double part = 0.0;
+      for (int b = tid; b < RELX_NCOARSE; b += kSetupThreads) {
+        if (ce[b] >= RELX_EMIN_NORM && ce[b] <= RELX_EMAX_NORM)
+          part += (double) cutoffpl_term(ce[b], ce[b + 1], ecut, gam) * (0.5 * (ce[b] + ce[b + 1]));
+      }
+      double sum = block_sum_d<kSetupThreads>(part, m.red) * 1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi);
+      if (tid == 0) {
+        if (q < 0) s.src_norm = 1.0 / sum;
+        else m.xscale[q] = sum * s.src_norm;  // 1 / (disk factor / source factor)
+      }
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  // ---- the 16 corners of every zone, first-zone density scaling, de-duplication
+  const int ncor = nz * 16;
+  const int ni = tab.x_nincl;
+  for (int e = tid; e < ncor; e += kSetupThreads) {
+    int z = e >> 4, c = e & 15;
+    // corner c: bit0 -> param 0 (+1), bit1 -> param 1, bit2 -> param 2, bit3 -> param 3
+    long row = 0;
+    for (int q = 0; q < 4; q++) row = row * tab.x_nvals[q] + m.zind[z][q] + ((c >> q) & 1);
+    row = row * ni;  // incl index 0
+    m.crow[e] = (int) row;
+  }
+  __syncthreads();
+  for (int e = tid; e < ncor; e += kSetupThreads) {
+    int first = e;
+    for (int f = 0; f < e; f++)
+      if (m.crow[f] == m.crow[e]) { first = f; break; }
+    m.cfirst[e] = (short) first;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int u = 0;
+    for (int e = 0; e < ncor; e++) {
+      if (m.cfirst[e] == e) m.cuniq[e] = (short) u++;
+      else m.cuniq[e] = m.cuniq[m.cfirst[e]];
+    }
+    s.ucount = u;
+  }
+  __syncthreads();
+  const bool dense = nz <= RELX_ZDENSE;
+  if (dense) {
+    RelxCorners &C = cout[set];
+    for (int i = tid; i < RELX_MAX_UCORNER * RELX_ZDENSE; i += kSetupThreads) (&C.w[0][0])[i] = 0.0f;
+    __syncthreads();
+  }
+  for (int e = tid; e < ncor; e += kSetupThreads) {
+    int z = e >> 4, c = e & 15;
+    double w = 1.0;
+    for (int q = 0; q < 4; q++) {
+      double f = m.zfac[z][q];
+      w *= ((c >> q) & 1) ? f : (1.0 - f);
+    }
+    // density division of the row by the zone that loads it first (xilltable.c:478-511)
+    double dscale = 1.0;
+    if (!tab.x_has_dens) {
+      double d = m.zdens[m.cfirst[e] >> 4];
+      if (fabs(d - 15) > 1e-6) dscale = 1.0 / pow(10.0, d - 15);
+    }
+    float wz = (float) (w * dscale * m.xscale[z]);
+    if (dense) {
+      RelxCorners &C = cout[set];
+      int u = m.cuniq[e];
+      C.w[u][z] = wz;  // each (u, z) pair is written by exactly one entry
+      if (m.cfirst[e] == e) C.row[u] = m.crow[e];
+    } else {
+      zcout[set].row[z][c] = m.crow[e];
+      zcout[set].w[z][c] = wz;
+    }
+  }
+  // ---- primary and reflection factors (PrimarySource.cpp:66-125)
+  if (tid == 0) {
+    if (s.emis_type != RELX_EMIS_LP) {
+      s.norm_fac_refl = fabs(s.refl_frac);
+      s.prim_fac = 1.0;
+    } else {
+      double rfi = s.refl_frac;
+      if (s.boost_switch) rfi *= s.refl_frac_lp;
+      double pf = s.f_inf_rest / 0.5 * pow(s.g_inf, s.gam);
+      if (s.beta > 1e-4) {
+        double d = doppler_factor(kPi - s.incl, s.beta);
+        pf *= d * d;
+      }
+      s.prim_fac = pf;
+      s.norm_fac_refl = fabs(rfi) / s.refl_frac_lp;
+    }
+    for (int z = 0; z < nz; z++) s.inv_nc[z] = (float) m.xscale[z];
+    if (m.status != RELX_OK) s.status = m.status;
+    sout[set] = s;
+  }
+}
+
+size_t setup_smem_bytes() { return sizeof(SetupSmem); }
+
+}  // namespace relx

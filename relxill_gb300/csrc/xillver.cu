@@ -1,0 +1,222 @@
+// xillver.cu -- angle-resolved xillver interpolation per radial zone
+// (check_xilltab_cache + interp_5d_tab_incl + calc_xillver_angdep and the
+// normalisation change of the zone; xilltable.c:575-635, 812-876,
+// Xillspec.cpp:557-573, Relxill.cpp:357-386).
+//
+// xill[z][E] = sum_corner sum_incl  w[corner][z] * dist[z][incl] * spec[corner][incl][E]
+// where w holds the 4-D interpolation weight of the corner in zone z, the
+// density division of the row and 1/normalisation-change of the zone, and
+// dist is the zone's normalised emission-angle histogram.
+//
+// Launch: one CTA per (energy tile of 1024 bins, parameter set).  The corner
+// list of a set is de-duplicated across zones by the setup kernel, so every
+// table row a set needs is read from HBM once.  The n_incl row segments of a
+// corner (contiguous rows, incl is the fastest table index) are streamed into
+// shared memory with cp.async.bulk (TMA bulk copies) completing on an
+// mbarrier, three corners in flight; all waits are bounded and report a
+// timeout through the error flag instead of hanging.
+#include "relx_device.cuh"
+
+namespace relx {
+
+constexpr int kXillThreads = 256;
+constexpr int kXillTile = 1024;   // floats per row segment (4 KB)
+constexpr int kXillStages = 3;
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, int count) {
+  asm volatile("mbarrier.init.shared.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// bounded wait (about one second, at most 2^24 polls); returns false on timeout
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+  const unsigned long long t0 = globaltimer_ns();
+  for (int it = 0; it < (1 << 24); it++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255) == 255 && globaltimer_ns() - t0 > kWaitLimitNs) return false;
+  }
+  return false;
+}
+
+struct XillSmem {
+  uint64_t full[kXillStages];
+  float w[RELX_MAX_UCORNER][RELX_ZDENSE];
+  float dist[RELX_ZDENSE][RELX_MAX_INCL];
+  int row[RELX_MAX_UCORNER];
+  int abort_flag;
+  int pad_[3];
+  float4 stage[1];  // [kXillStages][n_incl][kXillTile/4], dynamic tail
+};
+
+__global__ void __launch_bounds__(kXillThreads) xillver_dense_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
+                                                                     const RelxCorners *__restrict__ scor,
+                                                                     const float *__restrict__ dist_raw, int nza,
+                                                                     float *__restrict__ xout, int *__restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  XillSmem &m = *reinterpret_cast<XillSmem *>(smem_raw);
+  const int set = blockIdx.y, tile = blockIdx.x;
+  const RelxSetState &s = sst[set];
+  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.nz > RELX_ZDENSE) return;
+  const int tid = threadIdx.x;
+  const int nz = s.nz, U = s.ucount, ni = tab.x_nincl;
+  const int pitch = tab.x_nener_pad;
+  const int e0 = tile * kXillTile;
+  if (e0 >= pitch) return;
+  const int len = min(kXillTile, pitch - e0);  // multiple of 4 floats (16 bytes)
+  const uint32_t bytes_row = (uint32_t) len * 4u;
+
+  // weights and normalised emission-angle distributions (renorm_relline_profile, Relprofile.cpp:783-795)
+  const RelxCorners &C = scor[set];
+  for (int i = tid; i < U * RELX_ZDENSE; i += kXillThreads) (&m.w[0][0])[i] = (&C.w[0][0])[i];
+  for (int i = tid; i < U; i += kXillThreads) m.row[i] = C.row[i];
+  if (tid < nz) {
+    const float *d = dist_raw + ((size_t) set * nza + tid) * RELX_MAX_INCL;
+    float sum = 0.0f;
+    for (int i = 0; i < ni; i++) sum += d[i];
+    for (int i = 0; i < ni; i++) m.dist[tid][i] = (sum > 1e-8f) ? d[i] / sum : 0.0f;
+  }
+  if (tid == 0) {
+    m.abort_flag = 0;
+    for (int st = 0; st < kXillStages; st++) mbar_init(&m.full[st], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int u) {
+    const int st = u % kXillStages;
+    mbar_expect_tx(&m.full[st], bytes_row * (uint32_t) ni);
+    const float *src = tab.x_spec + (size_t) m.row[u] * pitch + e0;
+    for (int i = 0; i < ni; i++)
+      bulk_g2s(&m.stage[(st * ni + i) * (kXillTile / 4)], src + (size_t) i * pitch, bytes_row, &m.full[st]);
+  };
+  int issued = 0;  // meaningful in thread 0 only
+  if (tid == 0)
+    for (int u = 0; u < min(U, kXillStages); u++) { issue(u); issued = u + 1; }
+
+  float4 acc[RELX_ZDENSE];
+#pragma unroll
+  for (int z = 0; z < RELX_ZDENSE; z++) acc[z] = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int q = tid;  // float4 index inside the tile
+  const bool active = q * 4 < len;
+  int u_stop = U;
+  for (int u = 0; u < U; u++) {
+    const int st = u % kXillStages;
+    const uint32_t parity = (uint32_t) ((u / kXillStages) & 1);
+    if (!mbar_wait_bounded(&m.full[st], parity)) atomicExch(&m.abort_flag, 1);
+    __syncthreads();
+    if (m.abort_flag) { u_stop = u; break; }
+    if (active) {
+      float4 v[RELX_MAX_INCL];
+#pragma unroll
+      for (int i = 0; i < RELX_MAX_INCL; i++)
+        if (i < ni) v[i] = m.stage[(st * ni + i) * (kXillTile / 4) + q];
+#pragma unroll
+      for (int z = 0; z < RELX_ZDENSE; z++) {
+        if (z < nz) {
+          const float wz = m.w[u][z];
+          if (wz != 0.0f) {
+            float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < RELX_MAX_INCL; i++) {
+              if (i < ni) {
+                const float d = m.dist[z][i];
+                t.x += d * v[i].x; t.y += d * v[i].y; t.z += d * v[i].z; t.w += d * v[i].w;
+              }
+            }
+            acc[z].x += wz * t.x; acc[z].y += wz * t.y; acc[z].z += wz * t.z; acc[z].w += wz * t.w;
+          }
+        }
+      }
+    }
+    __syncthreads();  // stage st is free again
+    if (tid == 0 && u + kXillStages < U) { issue(u + kXillStages); issued = u + kXillStages + 1; }
+  }
+  if (m.abort_flag) {
+    // wait (bounded) for the copies this CTA still has in flight, then report
+    if (tid == 0) {
+      for (int u = u_stop; u < issued; u++)
+        (void) mbar_wait_bounded(&m.full[u % kXillStages], (uint32_t) ((u / kXillStages) & 1));
+      atomicExch(err, RELX_ERR_TIMEOUT);
+    }
+    return;
+  }
+  if (active) {
+#pragma unroll
+    for (int z = 0; z < RELX_ZDENSE; z++) {
+      if (z < nz) {
+        float4 *o = reinterpret_cast<float4 *>(xout + ((size_t) set * nza + z) * pitch + e0) + q;
+        *o = acc[z];
+      }
+    }
+  }
+}
+
+// generic path for more than RELX_ZDENSE zones (ionisation gradients): 16 corners per zone, plain loads
+__global__ void __launch_bounds__(kXillThreads) xillver_zone_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
+                                                                    const RelxZoneCorners *__restrict__ zcor,
+                                                                    const float *__restrict__ dist_raw, int nza,
+                                                                    float *__restrict__ xout) {
+  const int set = blockIdx.y, tile = blockIdx.x;
+  const RelxSetState &s = sst[set];
+  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.nz <= RELX_ZDENSE) return;
+  __shared__ float dist[RELX_MAX_INCL];
+  const int tid = threadIdx.x, ni = tab.x_nincl, pitch = tab.x_nener_pad;
+  const int e0 = tile * kXillTile;
+  if (e0 >= pitch) return;
+  const int len = min(kXillTile, pitch - e0);
+  const int q = tid;
+  const bool active = q * 4 < len;
+  for (int z = 0; z < s.nz; z++) {
+    __syncthreads();
+    if (tid == 0) {
+      const float *d = dist_raw + ((size_t) set * nza + z) * RELX_MAX_INCL;
+      float sum = 0.0f;
+      for (int i = 0; i < ni; i++) sum += d[i];
+      for (int i = 0; i < ni; i++) dist[i] = (sum > 1e-8f) ? d[i] / sum : 0.0f;
+    }
+    __syncthreads();
+    if (!active) continue;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int c = 0; c < 16; c++) {
+      const float wz = zcor[set].w[z][c];
+      const float4 *src = reinterpret_cast<const float4 *>(tab.x_spec + (size_t) zcor[set].row[z][c] * pitch + e0) + q;
+      float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int i = 0; i < ni; i++) {
+        float4 v = __ldg(src + (size_t) i * (pitch / 4));
+        t.x += dist[i] * v.x; t.y += dist[i] * v.y; t.z += dist[i] * v.z; t.w += dist[i] * v.w;
+      }
+      acc.x += wz * t.x; acc.y += wz * t.y; acc.z += wz * t.z; acc.w += wz * t.w;
+    }
+    reinterpret_cast<float4 *>(xout + ((size_t) set * nza + z) * pitch + e0)[q] = acc;
+  }
+}
+
+size_t xill_smem_bytes(int n_incl) {
+  return sizeof(XillSmem) + sizeof(float4) * ((size_t) kXillStages * n_incl * (kXillTile / 4) - 1);
+}
+
+}  // namespace relx

@@ -1,0 +1,39 @@
+"""Parameter sets and energy grids of the golden fixtures (shared by the
+fixture generator and the tests)."""
+import numpy as np
+
+
+def log_grid(emin, emax, n):
+    return np.exp(np.linspace(np.log(emin), np.log(emax), n + 1))
+
+
+GRID_LINE = ("line", 0.1, 20.0, 3000)      # relline: 3000 log bins 0.1-20 keV
+GRID_WIDE = ("wide", 0.1, 1000.0, 3000)    # relxill / relxilllp output grid
+GRID_CONV = ("convin", 0.3, 80.0, 500)      # relconv input grid
+
+CASES = [
+    # (name, model, params, grid, iongrad_type, iongrad_index)
+    ("relline_cfg1", "relline", [6.4, 3, 3, 15, 0.998, 30, -1, 400, 0, 0], GRID_LINE, 0, 0.0),
+    ("relline_b", "relline", [6.4, 4, 2.5, 8, 0.5, 60, -1.5, 300, 0.1, 1], GRID_LINE, 0, 0.0),
+    ("relline_c", "relline", [1.0, 3, 3, 15, -0.5, 80, -1, 1000, 0, 2], GRID_LINE, 0, 0.0),
+    ("relline_d", "relline", [6.97, 5, 3, 4, 0.9, 7, -1, 50, 0, 0], GRID_LINE, 0, 0.0),
+    ("relconv_a", "relconv", [3, 3, 15, 0.9, 45, -1, 400, 0], GRID_CONV, 0, 0.0),
+    ("relxill_cfg2", "relxill", [3, 3, 15, 0.9, 45, -1, 400, 0, 2.0, 3.1, 1, 300, 3], GRID_WIDE, 0, 0.0),
+    ("relxill_b", "relxill", [4, 2, 10, 0.3, 20, -2, 200, 0.05, 1.7, 1.0, 3, 100, -1], GRID_WIDE, 0, 0.0),
+    ("relxilllp_a", "relxilllp", [10, 0, 0.9, 45, -1, 400, 0, 2.0, 3.1, 1, 300, 1, 0, 0], GRID_WIDE, 0, 0.0),
+    ("relxilllp_b", "relxilllp", [3, 0.3, 0.998, 70, -1, 400, 0.2, 2.6, 4.0, 5, 50, 2, 0, 1], GRID_WIDE, 0, 0.0),
+    ("relxilllp_c", "relxilllp", [50, 0, -0.5, 10, -3, 100, 0, 1.5, 0.5, 0.7, 800, -1, 0, 0], GRID_WIDE, 0, 0.0),
+    ("relxilllp_pl", "relxilllp", [10, 0, 0.9, 45, -1, 400, 0, 2.0, 3.1, 1, 300, 1, 0, 0], GRID_WIDE, 1, 0.5),
+    ("relxilllp_alpha", "relxilllp", [5, 0, 0.5, 30, -1, 400, 0, 2.2, 2.0, 1, 100, 1, 0, 0], GRID_WIDE, 2, 0.0),
+]
+
+
+def grid(spec):
+    _, lo, hi, n = spec
+    return log_grid(lo, hi, n)
+
+
+def conv_input(e):
+    """relconv input spectrum: a power law with a Gaussian line (per bin)."""
+    em = 0.5 * (e[1:] + e[:-1])
+    return em ** -1.5 * np.diff(e) * (1 + 5 * np.exp(-0.5 * ((em - 6.4) / 0.2) ** 2))
