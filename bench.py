@@ -1,0 +1,408 @@
+#!/usr/bin/env python3
+"""Benchmark: batched relxilllp spectra per second on GB300.
+
+Workload (one step): 4096 relxilllp parameter sets, h ~ U[3,100] rg,
+a ~ U[0,0.998], incl ~ U[5,85] deg, Gamma ~ U[1.4,2.8], logxi ~ U[0,4.5],
+A_Fe = 1, Ecut = 300 keV, beta = 0, Rin = ISCO, Rout = 400 rg, refl_frac = 1,
+returning radiation off; each set has its own energy grid of U{300..5000}
+log-spaced bins over 0.3-80 keV; 10 radial zones.  Tables are the seeded
+synthetic tables in the reference FITS layouts at full size (relline
+25x30x100x40, lamp post 20x250x100, xillver 13x4x16x10x10 x 2999 bins,
+1 GB), written to _tables/full on first use.
+
+value: spectra/s with inputs resident in HBM (device-pointer C ABI).
+e2e:   the same through the host-buffer C ABI (relx_eval_batch), copies
+       of parameters, grids and fluxes included.
+--impl reference: the CPU oracle (C restatement of the reference) on all
+       host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "relxilllp spectra/s batched vs plain GPU at ≤1e-4 rel err; serve p50/p99 ms"
+N_SETS = 4096
+
+
+def workload(n: int, seed_params: int = 2026, seed_grids: int = 7):
+    """Parameter sets and energy grids of the batched relxilllp workload."""
+    rng = np.random.default_rng(seed_params)
+    h = rng.uniform(3, 100, n)
+    a = rng.uniform(0, 0.998, n)
+    inc = rng.uniform(5, 85, n)
+    gam = rng.uniform(1.4, 2.8, n)
+    lxi = rng.uniform(0, 4.5, n)
+    p = np.zeros((n, 14))
+    p[:, 0], p[:, 2], p[:, 3], p[:, 7], p[:, 8] = h, a, inc, gam, lxi
+    p[:, 1] = 0.0      # beta
+    p[:, 4] = -1.0     # Rin = ISCO
+    p[:, 5] = 400.0    # Rout
+    p[:, 9] = 1.0      # A_Fe
+    p[:, 10] = 300.0   # Ecut
+    p[:, 11] = 1.0     # refl_frac
+    rg = np.random.default_rng(seed_grids)
+    nb = rg.integers(300, 5001, n)
+    grids = [np.exp(np.linspace(np.log(0.3), np.log(80.0), int(k) + 1)) for k in nb]
+    return p, grids
+
+
+def tables(kind: str = "full") -> str:
+    from relxill_gb300 import synth_tables
+
+    d = os.path.join(ROOT, "_tables", kind)
+    synth_tables.ensure_tables(d, xill=kind)
+    return d
+
+
+# ----------------------------------------------------------------------------
+# CPU oracle (reference algorithm restated in C), multi-process
+# ----------------------------------------------------------------------------
+_oracle = None
+
+
+def _oracle_init(tdir: str):
+    global _oracle
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+
+    _oracle = oracle_lib
+    oracle_lib.lib(tdir)
+
+
+def _oracle_eval(args):
+    p, e = args
+    st, f = _oracle.evaluate("relxilllp", p, e)
+    return st
+
+
+def cpu_pool(tdir: str, procs: int):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+
+    oracle_lib.build()
+    ctx = mp.get_context("spawn")
+    return ctx.Pool(procs, initializer=_oracle_init, initargs=(tdir,))
+
+
+def cpu_rate(pool, params, grids, idx):
+    t0 = time.perf_counter()
+    sts = pool.map(_oracle_eval, [(params[i], grids[i]) for i in idx], chunksize=1)
+    dt = time.perf_counter() - t0
+    assert not any(sts)
+    return len(idx) / dt, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    tdir = tables("full")
+    procs = os.cpu_count() or 1
+    params, grids = workload(N_SETS)
+    pool = cpu_pool(tdir, procs)
+    per_step = max(procs * 2, 32)
+    rng = np.random.default_rng(11)
+    # warm-up (table loads)
+    for _ in range(args.warmup):
+        cpu_rate(pool, params, grids, rng.choice(N_SETS, per_step, replace=False))
+    times = []
+    for _ in range(args.steps):
+        r, dt = cpu_rate(pool, params, grids, rng.choice(N_SETS, per_step, replace=False))
+        times.append(dt)
+    pool.close()
+    total = per_step * args.steps / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": total, "unit": "spectra/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"relxilllp, {per_step} sets per step drawn from the 4096-set batched workload",
+                   "tables": "synthetic full-size (xillver 1 GB)"},
+        "cpu_baseline": {"value": total, "unit": "spectra/s", "cores": procs, "kind": "port",
+                         "sample": f"{per_step} sets per step x {args.steps} steps on {procs} processes"},
+        "e2e": {"value": total, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# clocks during the timed region
+# ----------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        out = os.path.join(ROOT, "gpurun_out") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv", dir=out)
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [x for x in sm if x > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+
+    import relxill_gb300 as R
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    tdir = tables("full")
+    # CPU baseline pool first (spawned processes, before the GPU context exists in them)
+    pool = None
+    procs = os.cpu_count() or 1
+    if rank == 0 and not args.no_cpu_baseline:
+        pool = cpu_pool(tdir, procs)
+    L = R.lib()
+    R.init(tdir)
+    L.relx_profile_enable.argtypes = [ctypes.c_int]
+    L.relx_profile_read.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64), ctypes.c_int]
+    L.relx_profile_name.restype = ctypes.c_char_p
+    L.relx_launch_count.restype = ctypes.c_int64
+    L.relx_batch_stats.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
+    tb = ctypes.c_int64(0)
+    L.relx_table_bytes(ctypes.byref(tb))
+
+    S = args.sets
+    params, grids = workload(S, seed_params=2026 + rank, seed_grids=7 + rank)
+    edges, offs = R.pack_grids(grids)
+    nflux = int(offs[-1]) - S
+    dev = torch.device("cuda", local)
+    d_params = torch.from_numpy(params).to(dev)
+    d_e = torch.from_numpy(edges).to(dev)
+    d_off = torch.from_numpy(offs).to(dev)
+    d_flux = torch.empty(nflux, dtype=torch.float64, device=dev)
+    d_status = torch.empty(S, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    offs_ptr = offs.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+    def step():
+        st = L.relx_eval_batch_device(3, S, d_params.data_ptr(), d_e.data_ptr(), d_off.data_ptr(), offs_ptr, None,
+                                      d_flux.data_ptr(), d_status.data_ptr(), None, None, None, stream.cuda_stream)
+        if st:
+            raise RuntimeError(f"relx_eval_batch_device: {st} {R.last_error()}")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    assert int((d_status != 0).sum()) == 0, "sets failed"
+    st6 = (ctypes.c_int64 * 3)()
+    L.relx_batch_stats(S, st6)
+
+    clocks = Clocks(local)
+    clocks.start()
+    L.relx_profile_enable(1)
+    l0 = L.relx_launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        ev0.record()
+    for _ in range(args.steps):
+        step()
+    with torch.cuda.stream(stream):
+        ev1.record()
+    torch.cuda.synchronize()
+    barrier()
+    launches = L.relx_launch_count() - l0
+    ms_k = (ctypes.c_double * 7)()
+    n_k = (ctypes.c_int64 * 7)()
+    L.relx_profile_read(ms_k, n_k, 7)
+    L.relx_profile_enable(0)
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * S * args.steps / (ms / 1e3)
+
+    # end-to-end through the host-buffer C ABI (copies in the timed region)
+    e2e = None
+    if not args.no_e2e:
+        flux = np.zeros(nflux)
+        status = np.zeros(S, dtype=np.int32)
+        pp = params.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        ep = edges.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        fp = flux.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        sp = status.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        for _ in range(max(1, args.warmup // 2)):
+            L.relx_eval_batch(3, S, pp, ep, offs_ptr, None, fp, sp, None, None)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rc = L.relx_eval_batch(3, S, pp, ep, offs_ptr, None, fp, sp, None, None)
+            assert rc == 0
+        t1 = time.perf_counter()
+        dt = t1 - t0
+        if dist is not None:
+            t = torch.tensor([dt], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        e2e = {"value": world * S * args.steps / dt, "unit": "spectra/s",
+               "h2d_bytes_per_step": int(params.nbytes + edges.nbytes + offs.nbytes),
+               "d2h_bytes_per_step": int(flux.nbytes + status.nbytes)}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
+    # plain path: one synchronous c_lmodrelxilllp call per spectrum
+    plain = None
+    if not args.no_plain:
+        n_plain = 64
+        for i in range(4):
+            R.relxilllp(grids[i], params[i])
+        t0 = time.perf_counter()
+        for i in range(n_plain):
+            R.relxilllp(grids[i], params[i])
+        plain = {"value": n_plain / (time.perf_counter() - t0), "unit": "spectra/s",
+                 "sample": f"{n_plain} single c_lmodrelxilllp calls"}
+
+    # parity spot check against the oracle (outside the timed region)
+    out = d_flux.cpu().numpy()
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+
+    oracle_lib.lib(tdir)
+    max_err = 0.0
+    for i in range(4):
+        s, ref = oracle_lib.evaluate("relxilllp", params[i], grids[i])
+        got = out[offs[i] - i: offs[i + 1] - i - 1]
+        m = ref > 1e-6 * ref.max()
+        max_err = max(max_err, float(np.max(np.abs(got[m] / ref[m] - 1))))
+
+    # CPU baseline on a bounded sample
+    cpu = None
+    if pool is not None:
+        idx = np.arange(min(args.cpu_sample, S))
+        cpu_rate(pool, params, grids, idx[: procs])  # warm the workers
+        r, dt = cpu_rate(pool, params, grids, idx)
+        pool.close()
+        cpu = {"value": r, "unit": "spectra/s", "cores": procs, "kind": "port",
+               "sample": f"{len(idx)} sets of the workload on {procs} spawned processes ({dt:.1f} s)"}
+
+    # roofline of the dominant kernel
+    names = [L.relx_profile_name(k).decode() for k in range(7)]
+    per = {names[k]: (ms_k[k] / max(n_k[k], 1), int(n_k[k])) for k in range(7)}
+    total_k = sum(ms_k[k] for k in range(7))
+    dom = max(range(7), key=lambda k: ms_k[k])
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    x_pad = 3000
+    ucount = int(st6[0])
+    nz_sum = int(st6[1])
+    # algorithmic bytes of the xillver kernel per launch: unique corner rows x incl x energies (read) + zone spectra (write)
+    xill_bytes = ucount * 10 * x_pad * 4 + nz_sum * x_pad * 4
+    xill_ms = per["xillver"][0]
+    roof = {"kernel": "xillver", "bound": "hbm", "achieved": xill_bytes / (xill_ms * 1e-3) / 1e9, "peak": hbm_peak,
+            "unit": "GB/s", "frac": None, "traffic": None, "peak_source": "measured" if peaks else "fallback"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    kernels = {n: {"ms_per_launch": round(per[n][0], 4), "launches": per[n][1],
+                   "share": round(ms_k[k] / total_k, 4) if total_k else None} for k, n in enumerate(names)}
+    line = {
+        "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 radii, grids and normalisation sums)", "data": "synthetic",
+        "config": {"workload": "relxilllp batched, 4096 sets per GPU, per-set grids 300-5000 log bins 0.3-80 keV, "
+                               "10 radial zones", "sets_per_gpu": S, "parallelism": f"replicas x{world}",
+                   "tables": f"synthetic full-size, {tb.value / 1e9:.2f} GB on the device",
+                   "l2": "inputs larger than L2 (1 GB xillver table, ~2 GB workspace per step)"},
+        "e2e": e2e, "plain_gpu": plain, "batched_over_plain": (value / world / plain["value"]) if plain else None,
+        "max_rel_err_vs_oracle": max_err, "gpu_launches": int(launches), "clocks": clk,
+        "roofline": roof, "dominant_kernel": names[dom], "kernels": kernels, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--sets", type=int, default=N_SETS)
+    ap.add_argument("--cpu-sample", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

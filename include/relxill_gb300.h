@@ -83,6 +83,19 @@ int relx_eval_batch_device(int model, int n_sets, const double *d_params, const 
                            double *d_flux, int *d_status, const int *d_ion_grad_type, const int *h_ion_grad_type,
                            const double *d_iongrad_index, void *stream);
 
+/* Measurement hooks (no counterpart in the reference).  When enabled, every
+ * kernel of every batch is bracketed by CUDA events on its launching stream;
+ * relx_profile_read synchronises and returns the accumulated milliseconds
+ * and launch counts per kernel kind (relx_profile_name(k), k < 7). */
+int relx_profile_enable(int on);
+int relx_profile_read(double *ms, int64_t *launches, int n);
+const char *relx_profile_name(int k);
+/* number of kernel launches issued by the library since load */
+int64_t relx_launch_count(void);
+/* statistics of the last batch of n_sets sets: out[0] de-duplicated xillver
+ * corners, out[1] radial zones, out[2] line-profile window bins (sums) */
+int relx_batch_stats(int n_sets, int64_t *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -490,6 +490,59 @@ __global__ void status_kernel(int n_sets, const RelxSetState *__restrict__ st, c
   out[i] = s;
 }
 
+// ---- optional per-kernel timing with CUDA events on the launching stream ----
+enum ProfKernel { PK_PACK, PK_SETUP, PK_LINE, PK_XILL, PK_CONV, PK_FIN, PK_STATUS, PK_N };
+static const char *kProfNames[PK_N] = {"pack", "setup", "relline", "xillver", "conv", "finalize", "status"};
+struct Profiler {
+  bool on = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> rec;
+  double ms[PK_N] = {0};
+  int64_t n[PK_N] = {0};
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t get() {
+    if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+};
+static Profiler g_prof;
+static std::atomic<int64_t> g_launches{0};
+
+struct ProfScope {
+  int k;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr, b = nullptr;
+  ProfScope(int kid, cudaStream_t st) : k(kid), s(st) {
+    g_launches++;
+    if (g_prof.on) {
+      a = g_prof.get();
+      b = g_prof.get();
+      cudaEventRecord(a, s);
+    }
+  }
+  ~ProfScope() {
+    if (g_prof.on) {
+      cudaEventRecord(b, s);
+      g_prof.rec.push_back({k, {a, b}});
+    }
+  }
+};
+
+static int prof_collect() {
+  for (auto &r : g_prof.rec) {
+    RELX_CUDA(cudaEventSynchronize(r.second.second));
+    float ms = 0;
+    RELX_CUDA(cudaEventElapsedTime(&ms, r.second.first, r.second.second));
+    g_prof.ms[r.first] += ms;
+    g_prof.n[r.first] += 1;
+    g_prof.pool.push_back(r.second.first);
+    g_prof.pool.push_back(r.second.second);
+  }
+  g_prof.rec.clear();
+  return 0;
+}
+
 struct BatchShape {
   int model, n_sets, nza, ntile_max;
   int64_t n_edges;  // total energy edges
@@ -537,36 +590,56 @@ static int launch_batch(Context &C, const BatchShape &b, cudaStream_t s) {
   RelxZoneCorners *zcor = W.zcorners.as<RelxZoneCorners>();
   RELX_CUDA(cudaMemsetAsync(W.sflag.p, 0, S * sizeof(int), s));
   RELX_CUDA(cudaMemsetAsync(W.err.p, 0, sizeof(int), s));
-  setup_kernel<<<S, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, b.model, sin, W.user_e.as<double>(),
-                                                             W.line_e.as<double>(), sst, rad, cor, zcor);
+  {
+    ProfScope ps(PK_SETUP, s);
+    setup_kernel<<<S, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, b.model, sin, W.user_e.as<double>(),
+                                                               W.line_e.as<double>(), sst, rad, cor, zcor);
+  }
   const size_t ls = line_smem_bytes(tab.rel_nr, tab.rel_ng);
   dim3 lg(b.ntile_max, S);
-  RELX_CUDA(launch_relline(b.model >= RELX_RELXILL, lg, ls, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza,
-                           W.prof.as<float>(), W.dist.as<float>(), W.tsum.as<double>(), b.ntile_max));
+  {
+    ProfScope ps(PK_LINE, s);
+    RELX_CUDA(launch_relline(b.model >= RELX_RELXILL, lg, ls, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza,
+                             W.prof.as<float>(), W.dist.as<float>(), W.tsum.as<double>(), b.ntile_max));
+  }
   if (b.model >= RELX_RELXILL) {
     const int nxt = (tab.x_nener_pad + kXillTileH - 1) / kXillTileH;
-    if (b.nza <= RELX_ZDENSE)
-      xillver_dense_kernel<<<dim3(nxt, S), kXillThreadsH, xill_smem_bytes(tab.x_nincl), s>>>(
-          tab, sst, cor, W.dist.as<float>(), b.nza, W.xill.as<float>(), W.err.as<int>());
-    else
-      xillver_zone_kernel<<<dim3(nxt, S), kXillThreadsH, 0, s>>>(tab, sst, zcor, W.dist.as<float>(), b.nza,
-                                                                 W.xill.as<float>());
-    conv_zone_kernel<<<dim3(b.nza, S), kConvThreadsH, conv_smem_bytes(), s>>>(
-        tab, sst, W.prof.as<float>(), W.tsum.as<double>(), b.ntile_max, kLineTileH, W.xill.as<float>(), b.nza,
-        W.cout.as<float>());
-    finalize_relxill_kernel<<<S, kConvThreadsH, fin_smem_bytes(), s>>>(tab, sin, sst, W.cout.as<float>(), b.nza,
-                                                                       W.user_e.as<double>(), W.flux.as<double>());
+    {
+      ProfScope ps(PK_XILL, s);
+      if (b.nza <= RELX_ZDENSE)
+        xillver_dense_kernel<<<dim3(nxt, S), kXillThreadsH, xill_smem_bytes(tab.x_nincl), s>>>(
+            tab, sst, cor, W.dist.as<float>(), b.nza, W.xill.as<float>(), W.err.as<int>());
+      else
+        xillver_zone_kernel<<<dim3(nxt, S), kXillThreadsH, 0, s>>>(tab, sst, zcor, W.dist.as<float>(), b.nza,
+                                                                   W.xill.as<float>());
+    }
+    {
+      ProfScope ps(PK_CONV, s);
+      conv_zone_kernel<<<dim3(b.nza, S), kConvThreadsH, conv_smem_bytes(), s>>>(
+          tab, sst, W.prof.as<float>(), W.tsum.as<double>(), b.ntile_max, kLineTileH, W.xill.as<float>(), b.nza,
+          W.cout.as<float>());
+    }
+    {
+      ProfScope ps(PK_FIN, s);
+      finalize_relxill_kernel<<<S, kConvThreadsH, fin_smem_bytes(), s>>>(tab, sin, sst, W.cout.as<float>(), b.nza,
+                                                                         W.user_e.as<double>(), W.flux.as<double>());
+    }
   } else if (b.model == RELX_RELCONV) {
+    ProfScope ps(PK_CONV, s);
     relconv_conv_kernel<<<S, kConvThreadsH, conv_smem_bytes(), s>>>(
         tab, sin, sst, W.prof.as<float>(), W.tsum.as<double>(), b.ntile_max, kLineTileH, b.nza, W.user_e.as<double>(),
         W.user_f.as<double>(), W.cout.as<float>(), W.sflag.as<int>());
     finalize_relconv_kernel<<<S, kConvThreadsH, 0, s>>>(tab, sin, sst, W.cout.as<float>(), b.nza,
                                                         W.user_e.as<double>(), W.sflag.as<int>(), W.flux.as<double>());
   } else {
+    ProfScope ps(PK_FIN, s);
     finalize_relline_kernel<<<S, kConvThreadsH, 0, s>>>(sin, sst, W.prof.as<float>(), W.tsum.as<double>(),
                                                         b.ntile_max, kLineTileH, b.nza, W.flux.as<double>());
   }
-  status_kernel<<<(S + 255) / 256, 256, 0, s>>>(S, sst, W.sflag.as<int>(), W.err.as<int>(), W.status.as<int>());
+  {
+    ProfScope ps(PK_STATUS, s);
+    status_kernel<<<(S + 255) / 256, 256, 0, s>>>(S, sst, W.sflag.as<int>(), W.err.as<int>(), W.status.as<int>());
+  }
   RELX_CUDA(cudaGetLastError());
   return 0;
 }
@@ -654,9 +727,13 @@ static int eval_host(int model, int n_sets, const double *params, const double *
   if (igt) RELX_CUDA(cudaMemcpyAsync(d_igt.p, h + o_g, gb, cudaMemcpyHostToDevice, s));
   if (igi) RELX_CUDA(cudaMemcpyAsync(d_igi.p, h + o_i, ib, cudaMemcpyHostToDevice, s));
   if (model == RELX_RELCONV) RELX_CUDA(cudaMemcpyAsync(W.user_f.p, h + o_f, fb, cudaMemcpyHostToDevice, s));
-  pack_kernel<<<(n_sets + 127) / 128, 128, 0, s>>>(n_sets, npar, d_params.as<double>(), d_eoff.as<int64_t>(),
-                                                   igt ? d_igt.as<int>() : nullptr, igi ? d_igi.as<double>() : nullptr,
-                                                   env.nzones_env, env.flags, W.setin.as<RelxSetIn>());
+  {
+    ProfScope ps(PK_PACK, s);
+    pack_kernel<<<(n_sets + 127) / 128, 128, 0, s>>>(n_sets, npar, d_params.as<double>(), d_eoff.as<int64_t>(),
+                                                     igt ? d_igt.as<int>() : nullptr,
+                                                     igi ? d_igi.as<double>() : nullptr, env.nzones_env, env.flags,
+                                                     W.setin.as<RelxSetIn>());
+  }
   if ((st = launch_batch(C, b, s))) return st;
   // results: flux (edge layout minus set index) and statuses
   const size_t nflux = (size_t) (b.n_edges - n_sets);
@@ -727,12 +804,57 @@ int relx_eval_batch_device(int model, int n_sets, const double *d_params, const 
     if (!d_flux_in) return RELX_ERR_ARG;
     RELX_CUDA(cudaMemcpyAsync(W.user_f.p, d_flux_in, sizeof(double) * b.n_edges, cudaMemcpyDeviceToDevice, s));
   }
-  pack_kernel<<<(n_sets + 127) / 128, 128, 0, s>>>(n_sets, model_nparams(model), d_params, d_energy_offsets,
-                                                   d_ion_grad_type, d_iongrad_index, env.nzones_env, env.flags,
-                                                   W.setin.as<RelxSetIn>());
+  {
+    ProfScope ps(PK_PACK, s);
+    pack_kernel<<<(n_sets + 127) / 128, 128, 0, s>>>(n_sets, model_nparams(model), d_params, d_energy_offsets,
+                                                     d_ion_grad_type, d_iongrad_index, env.nzones_env, env.flags,
+                                                     W.setin.as<RelxSetIn>());
+  }
   if ((st = launch_batch(C, b, s))) return st;
   RELX_CUDA(cudaMemcpyAsync(d_flux, W.flux.p, sizeof(double) * (b.n_edges - n_sets), cudaMemcpyDeviceToDevice, s));
   if (d_status) RELX_CUDA(cudaMemcpyAsync(d_status, W.status.p, sizeof(int) * n_sets, cudaMemcpyDeviceToDevice, s));
+  return 0;
+}
+
+int relx_profile_enable(int on) {
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  int st = prof_collect();
+  for (int k = 0; k < PK_N; k++) { g_prof.ms[k] = 0; g_prof.n[k] = 0; }
+  g_prof.on = on != 0;
+  return st;
+}
+
+int relx_profile_read(double *ms, int64_t *launches, int n) {
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  int st = prof_collect();
+  for (int k = 0; k < n && k < PK_N; k++) {
+    if (ms) ms[k] = g_prof.ms[k];
+    if (launches) launches[k] = g_prof.n[k];
+  }
+  return st;
+}
+
+const char *relx_profile_name(int k) { return (k >= 0 && k < PK_N) ? kProfNames[k] : ""; }
+
+int64_t relx_launch_count(void) { return g_launches.load(); }
+
+int relx_batch_stats(int n_sets, int64_t *out) {
+  // out[0] = sum of de-duplicated xillver corners, out[1] = sum of zones, out[2] = sum of line-profile window bins
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  if ((size_t) n_sets * sizeof(RelxSetState) > C.W.st.bytes) return RELX_ERR_ARG;
+  std::vector<RelxSetState> st((size_t) n_sets);
+  RELX_CUDA(cudaStreamSynchronize(C.stream));
+  RELX_CUDA(cudaMemcpy(st.data(), C.W.st.p, sizeof(RelxSetState) * n_sets, cudaMemcpyDeviceToHost));
+  out[0] = out[1] = out[2] = 0;
+  for (auto &x : st) {
+    if (x.status) continue;
+    out[0] += x.ucount;
+    out[1] += x.nz;
+    out[2] += x.win_hi - x.win_lo;
+  }
   return 0;
 }
 
