@@ -17,24 +17,33 @@
 
 namespace relx {
 
-constexpr int kConvThreads = 256;
-constexpr int kConvR = 16;  // output bins per thread
+constexpr int kConvThreads = 256;  // convolution kernels
+constexpr int kFinThreads = 128;   // finalize kernels
+constexpr int kConvR = 16;         // output bins per thread and work item
 constexpr int kN = RELX_NCONV;
-static_assert(kConvThreads * kConvR == kN, "conv tiling covers the grid");
+constexpr int kPre = 4;            // prefix sums are kept at every kPre-th bin
+static_assert(kN % (kConvThreads * kPre) == 0, "scan tiling");
 
 __device__ __forceinline__ int skew(int m) { return m + (m >> 4); }
 
 struct ConvSmem {
-  float xs[kN + kN / 16];    // x * cf, skewed
-  float hr[kN + kConvR];     // rel * cf over the profile window, zero padded
-  double red[kConvThreads / 32 + 1];
+  float xs[kN + kN / 16];      // x * cf, skewed
+  float hr[kN + kConvR];       // rel * cf over the zone's profile window, zero padded
+  float2 pre[kN / kPre + 1];   // float-float prefix sums of xs at bins 0, kPre, 2 kPre, ...
+  float2 red[kConvThreads / 32 + 2];
+  float2 wsum[kConvThreads / 32];
+  double dred[kConvThreads / 32 + 2];
+  double zsum[RELX_NZMAX];
+  float bc[2];                 // broadcast scalars
 };
 
-// y[k0 + r] = sum_{i in [wlo, whi)} hr[i - wlo] * xs[(k0 + r + p - i) mod N]
-__device__ __forceinline__ void conv_tile(const ConvSmem &m, int k0, int p, int wlo, int whi, float y[kConvR]) {
+// y[k0 + r] = sum_{i in [clo, chi)} hr[i - wlo] * xs[(k0 + r + p - i) mod N]; hr is zero padded
+// past the window, so chi - clo need not be a multiple of kConvR
+__device__ __forceinline__ void conv_tile(const ConvSmem &m, int k0, int p, int wlo, int clo, int chi,
+                                          float y[kConvR]) {
 #pragma unroll
   for (int r = 0; r < kConvR; r++) y[r] = 0.0f;
-  for (int i0 = wlo; i0 < whi; i0 += kConvR) {
+  for (int i0 = clo; i0 < chi; i0 += kConvR) {
     const int base = k0 + p - i0 - (kConvR - 1);
     float xr[2 * kConvR - 1];
 #pragma unroll
@@ -48,43 +57,147 @@ __device__ __forceinline__ void conv_tile(const ConvSmem &m, int k0, int p, int 
   }
 }
 
-// sum over tiles of the per-(tile, zone) profile sums written by the line kernel
-__device__ __forceinline__ double zone_profile_sum(const double *tsum, int set, int ntile_max, int nza, int z, int ntiles) {
-  double s = 0.0;
-  for (int t = 0; t < ntiles; t++) s += tsum[((size_t) set * ntile_max + t) * nza + z];
-  return s;
-}
-
-// relline renormalisation (renorm_relline_profile, Relprofile.cpp:766-781)
-__device__ __forceinline__ double profile_scale(const RelxSetState &s, const double *tsum, int set, int ntile_max,
-                                                int nza, int tile_bins) {
-  if (!(s.relline_norm > 0.0)) return 1.0;
-  const int ntiles = (s.win_hi - s.win_lo + tile_bins - 1) / tile_bins;
-  double sum = 0.0;
-  for (int z = 0; z < s.nz; z++) sum += zone_profile_sum(tsum, set, ntile_max, nza, z, ntiles);
-  return s.relline_norm / sum;
-}
-
-// shared part: convolution of xs with hr, normalisation, output (fout * norm)
-__device__ void conv_normalize_store(ConvSmem &m, const RelxTables &tab, int wlo, int whi, double sx, double sr,
-                                     float *out) {
+// relline renormalisation factor (renorm_relline_profile, Relprofile.cpp:766-781) and the zone
+// sums of the profile, from the per-(tile, zone) sums of the line kernel.  Warp 0: one lane per
+// zone sums its tiles in order, lane 0 sums the zones in order.  Results in m.zsum (scaled) and
+// m.bc[0] (scale).
+__device__ void profile_sums(ConvSmem &m, const RelxSetState &s, const double *tsum, int set, int ntile_max, int nza,
+                             int tile_bins) {
   const int tid = threadIdx.x;
-  const int k0 = tid * kConvR;
-  float y[kConvR];
-  conv_tile(m, k0, tab.conv_pos1, wlo, whi, y);
-  double part = 0.0;
-#pragma unroll
-  for (int r = 0; r < kConvR; r++) {
-    const int k = k0 + r;
-    y[r] = y[r] / tab.conv_cf[k];
-    if (k >= tab.conv_band_lo && k <= tab.conv_band_hi) part += (double) y[r];
+  if (tid < 32) {
+    const int ntiles = (s.win_hi - s.win_lo + tile_bins - 1) / tile_bins;
+    for (int z = tid; z < s.nz; z += 32) {
+      double zs = 0.0;
+      for (int t = 0; t < ntiles; t++) zs += tsum[((size_t) set * ntile_max + t) * nza + z];
+      m.zsum[z] = zs;
+    }
+    __syncwarp();
+    if (tid == 0) {
+      double scale = 1.0;
+      if (s.relline_norm > 0.0) {
+        double sum = 0.0;
+        for (int z = 0; z < s.nz; z++) sum += m.zsum[z];
+        scale = s.relline_norm / sum;
+      }
+      for (int z = 0; z < s.nz; z++) m.zsum[z] *= scale;
+      m.bc[0] = (float) scale;
+    }
   }
-  const double sc = block_sum_d<kConvThreads>(part, m.red);
-  const float norm = (float) (sr * sx / sc);
+  __syncthreads();
+}
+
+// float-float prefix of xs at bin x (0 <= x <= N)
+__device__ __forceinline__ float2 prefix_at(const ConvSmem &m, int x) {
+  const int q = x / kPre;
+  float2 v = m.pre[q];
+  for (int j = q * kPre; j < x; j++) v = ff_addf(v, m.xs[skew(j)]);
+  return v;
+}
+
+// cost of a split of the window into S segments: rounds of work items times segment length
+__device__ __forceinline__ int split_cost(int nt, int nc, int S) {
+  return ((nt * S + kConvThreads - 1) / kConvThreads) * ((nc + S - 1) / S);
+}
+
+// Convolution of xs with hr, normalised as calcFFTNormFactor (Relbase.cpp:199-222), written for the
+// conv bins [olo, ohi] the caller's grid needs.  The 0.01-1000 keV sum of the convolution is
+// sum_i hr_i * (window sum of xs) / cf, from prefix sums of xs (cf = E/dE is the same in every
+// bin of the log grid up to rounding), so bins outside [olo, ohi] are never convolved.  The sums
+// are float-float (about 48 significant bits, on the FP32 pipe).
+__device__ void conv_normalize_store(ConvSmem &m, const RelxTables &tab, int wlo, int whi, int olo, int ohi,
+                                     float2 sx, float2 sr, float *out) {
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  // prefix sums of xs at every kPre-th bin
+  {
+    constexpr int per = kN / kConvThreads;
+    float2 grp[per / kPre];
+    float2 loc = make_float2(0.0f, 0.0f);
 #pragma unroll
-  for (int r = 0; r < kConvR; r += 4) {
-    float4 v = make_float4(y[r] * norm, y[r + 1] * norm, y[r + 2] * norm, y[r + 3] * norm);
-    *reinterpret_cast<float4 *>(out + k0 + r) = v;
+    for (int g = 0; g < per / kPre; g++) {
+      float2 gs = make_float2(0.0f, 0.0f);
+#pragma unroll
+      for (int q = 0; q < kPre; q++) gs = ff_addf(gs, m.xs[skew(tid * per + g * kPre + q)]);
+      grp[g] = gs;
+      loc = ff_add(loc, gs);
+    }
+    float2 inc = loc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      float2 t;
+      t.x = __shfl_up_sync(0xffffffffu, inc.x, o);
+      t.y = __shfl_up_sync(0xffffffffu, inc.y, o);
+      if (lane >= o) inc = ff_add(t, inc);
+    }
+    float2 exc;
+    exc.x = __shfl_up_sync(0xffffffffu, inc.x, 1);
+    exc.y = __shfl_up_sync(0xffffffffu, inc.y, 1);
+    if (lane == 0) exc = make_float2(0.0f, 0.0f);
+    if (lane == 31) m.wsum[w] = inc;
+    __syncthreads();
+    float2 run = make_float2(0.0f, 0.0f);
+    for (int q = 0; q < w; q++) run = ff_add(run, m.wsum[q]);
+    run = ff_add(run, exc);
+#pragma unroll
+    for (int g = 0; g < per / kPre; g++) {
+      m.pre[(tid * per) / kPre + g] = run;
+      run = ff_add(run, grp[g]);
+    }
+    if (tid == kConvThreads - 1) m.pre[kN / kPre] = run;
+    __syncthreads();
+  }
+  const int p = tab.conv_pos1;
+  const int blo = tab.conv_band_lo, L = tab.conv_band_hi - tab.conv_band_lo + 1;
+  float2 part = make_float2(0.0f, 0.0f);
+  for (int i = wlo + tid; i < whi; i += kConvThreads) {
+    const int a = (blo + p - i) & (kN - 1);
+    float2 ws;
+    if (a + L <= kN) ws = ff_add(prefix_at(m, a + L), ff_neg(prefix_at(m, a)));
+    else ws = ff_add(ff_add(m.pre[kN / kPre], ff_neg(prefix_at(m, a))), prefix_at(m, a + L - kN));
+    part = ff_add(part, ff_mulf(ws, m.hr[i - wlo]));
+  }
+  const float2 scf = block_sum_ff<kConvThreads>(part, m.red);
+  if (tid == 0) {
+    const double sc = ff_to_double(scf) / (double) tab.conv_cf[blo];
+    m.bc[1] = (float) (ff_to_double(sr) * ff_to_double(sx) / sc);
+  }
+  __syncthreads();
+  const float norm = m.bc[1];
+  if (olo > ohi) return;
+  // work items: (16-bin output tile, window segment).  The window is split into S (a power of two)
+  // segments so that narrow output ranges still occupy every thread; the S partials of a tile sit
+  // in adjacent lanes and are added by a fixed shuffle tree, so the result depends only on this
+  // set's own sizes.
+  const int nt = (ohi - olo + 1 + kConvR - 1) / kConvR;
+  const int nc = (whi - wlo + kConvR - 1) / kConvR;
+  int S = 1, best = split_cost(nt, nc, 1);
+  for (int c = 2; c <= 32 && c <= nc; c <<= 1) {
+    const int cost = split_cost(nt, nc, c);
+    if (cost < best) { best = cost; S = c; }
+  }
+  const int seg = ((nc + S - 1) / S) * kConvR;  // window bins per segment
+  const int nitems = nt * S;
+  for (int q0 = 0; q0 < nitems; q0 += kConvThreads) {
+    const int q = q0 + tid;
+    const int t = q / S, sg = q % S;
+    float y[kConvR];
+    if (q < nitems) {
+      const int clo = wlo + sg * seg, chi = min(whi, clo + seg);
+      conv_tile(m, olo + t * kConvR, p, wlo, clo, chi, y);
+    } else {
+#pragma unroll
+      for (int r = 0; r < kConvR; r++) y[r] = 0.0f;
+    }
+    for (int o = S >> 1; o > 0; o >>= 1) {
+#pragma unroll
+      for (int r = 0; r < kConvR; r++) y[r] += __shfl_xor_sync(0xffffffffu, y[r], o);
+    }
+    if (q < nitems && sg == 0) {
+#pragma unroll
+      for (int r = 0; r < kConvR; r++) {
+        const int k = olo + t * kConvR + r;
+        if (k <= ohi) out[k] = y[r] / tab.conv_cf[k] * norm;
+      }
+    }
   }
 }
 
@@ -99,32 +212,30 @@ __global__ void __launch_bounds__(kConvThreads) conv_zone_kernel(RelxTables tab,
   const RelxSetState &s = sst[set];
   if (s.status != RELX_OK || s.model < RELX_RELXILL || z >= s.nz) return;
   float *out = cout + ((size_t) set * nza + z) * kN;
-  const double scale = profile_scale(s, tsum, set, ntile_max, nza, tile_bins);
-  const int ntiles = (s.win_hi - s.win_lo + tile_bins - 1) / tile_bins;
+  profile_sums(m, s, tsum, set, ntile_max, nza, tile_bins);
   // relxill_convolution_multizone skips zones without flux (Relxill.cpp:455-457)
-  const double zsum = zone_profile_sum(tsum, set, ntile_max, nza, z, ntiles) * scale;
-  if (zsum < 1e-12) {
-    for (int k = tid; k < kN; k += kConvThreads) out[k] = 0.0f;
+  if (m.zsum[z] < 1e-12) {
+    for (int k = s.out_lo + tid; k <= s.out_hi; k += kConvThreads) out[k] = 0.0f;
     return;
   }
-  const int wlo = s.win_lo, whi = s.win_hi;
-  const float fscale = (float) scale;
+  const int wlo = s.zw_lo[z], whi = s.zw_hi[z];  // the zone's profile is zero outside
+  const float fscale = m.bc[0];
   const float *pz = prof + ((size_t) set * nza + z) * kN;
   // relline profile weighted by E/dE over its window; band sum of the profile
-  double pr = 0.0;
+  float2 pr = make_float2(0.0f, 0.0f);
   for (int i = tid; i < whi - wlo + kConvR; i += kConvThreads) {
     const int j = wlo + i;
     float v = 0.0f;
     if (j < whi) {
       const float fr = pz[j] * fscale;
       v = fr * tab.conv_cf[j];
-      if (j >= tab.conv_band_lo && j <= tab.conv_band_hi) pr += (double) fr;
+      if (j >= tab.conv_band_lo && j <= tab.conv_band_hi) pr = ff_addf(pr, fr);
     }
     m.hr[i] = v;
   }
   // xillver spectrum of the zone rebinned onto the conv grid (_rebin_spectrum, relutility.c:549-601)
   const float *xz = xill + ((size_t) set * nza + z) * tab.x_nener_pad;
-  double px = 0.0;
+  float2 px = make_float2(0.0f, 0.0f);
   for (int j = tid; j < kN; j += kConvThreads) {
     const int i0 = tab.rb_imin[j], i1 = tab.rb_imax[j];
     float v = 0.0f;
@@ -136,12 +247,12 @@ __global__ void __launch_bounds__(kConvThreads) conv_zone_kernel(RelxTables tab,
         for (int q = i0 + 1; q <= i1 - 1; q++) v += xz[q];
       }
     }
-    if (j >= tab.conv_band_lo && j <= tab.conv_band_hi) px += (double) v;
+    if (j >= tab.conv_band_lo && j <= tab.conv_band_hi) px = ff_addf(px, v);
     m.xs[skew(j)] = v * tab.conv_cf[j];
   }
-  const double sr = block_sum_d<kConvThreads>(pr, m.red);
-  const double sx = block_sum_d<kConvThreads>(px, m.red);
-  conv_normalize_store(m, tab, wlo, whi, sx, sr, out);
+  const float2 sr = block_sum_ff<kConvThreads>(pr, m.red);
+  const float2 sx = block_sum_ff<kConvThreads>(px, m.red);
+  conv_normalize_store(m, tab, wlo, whi, s.out_lo, s.out_hi, sx, sr, out);
 }
 
 // relconv (relconv_kernel, Relbase.cpp:257-289): the caller's spectrum is
@@ -167,28 +278,28 @@ __global__ void __launch_bounds__(kConvThreads) relconv_conv_kernel(RelxTables t
   // conv_model requires a positive input sum (LocalModel.cpp:84-86)
   double ps = 0.0;
   for (int i = tid; i < nu; i += kConvThreads) ps += uf[i];
-  const double usum = block_sum_d<kConvThreads>(ps, m.red);
+  const double usum = block_sum_d<kConvThreads>(ps, m.dred);
   if (!(usum > 0.0)) {
     if (tid == 0) sflag[set] = RELX_ERR_INPUT;
     return;
   }
-  const double scale = profile_scale(s, tsum, set, ntile_max, nza, tile_bins);
+  profile_sums(m, s, tsum, set, ntile_max, nza, tile_bins);
   const int wlo = s.win_lo, whi = s.win_hi;
-  const float fscale = (float) scale;
+  const float fscale = m.bc[0];
   const float *pz = prof + (size_t) set * nza * kN;
-  double pr = 0.0;
+  float2 pr = make_float2(0.0f, 0.0f);
   for (int i = tid; i < whi - wlo + kConvR; i += kConvThreads) {
     const int j = wlo + i;
     float v = 0.0f;
     if (j < whi) {
       const float fr = pz[j] * fscale;
       v = fr * tab.conv_cf[j];
-      if (j >= tab.conv_band_lo && j <= tab.conv_band_hi) pr += (double) fr;
+      if (j >= tab.conv_band_lo && j <= tab.conv_band_hi) pr = ff_addf(pr, fr);
     }
     m.hr[i] = v;
   }
   // _rebin_spectrum(conv grid <- user grid)
-  double px = 0.0;
+  float2 px = make_float2(0.0f, 0.0f);
   const double *ce = tab.conv_e;
   for (int j = tid; j < kN; j += kConvThreads) {
     const double elo0 = ce[j], ehi0 = ce[j + 1];
@@ -217,25 +328,23 @@ __global__ void __launch_bounds__(kConvThreads) relconv_conv_kernel(RelxTables t
         v = (float) acc;
       }
     }
-    if (j >= tab.conv_band_lo && j <= tab.conv_band_hi) px += (double) v;
+    if (j >= tab.conv_band_lo && j <= tab.conv_band_hi) px = ff_addf(px, v);
     m.xs[skew(j)] = v * tab.conv_cf[j];
   }
-  const double sr = block_sum_d<kConvThreads>(pr, m.red);
-  const double sx = block_sum_d<kConvThreads>(px, m.red);
-  conv_normalize_store(m, tab, wlo, whi, sx, sr, out);
+  const float2 sr = block_sum_ff<kConvThreads>(pr, m.red);
+  const float2 sx = block_sum_ff<kConvThreads>(px, m.red);
+  conv_normalize_store(m, tab, wlo, whi, s.out_lo, s.out_hi, sx, sr, out);
 }
 
-// _rebin_spectrum for one output bin (relutility.c:549-601); ener0 has n0+1 edges
-__device__ __forceinline__ double rebin_bin(double elo0, double ehi0, const double *__restrict__ e0, int n0,
+// _rebin_spectrum (relutility.c:549-601) of one output bin from the conv grid; the bin indices
+// are those of the reference's walk, found from the logarithm and exact comparisons
+__device__ __forceinline__ double rebin_bin(const RelxTables &tab, double elo0, double ehi0,
                                            const float *__restrict__ f0) {
+  constexpr int n0 = kN;
+  const double *e0 = tab.conv_e;
   if (!(e0[0] <= ehi0 && e0[n0] >= elo0)) return 0.0;
-  int lo = 0, hi = n0 + 1;
-  while (lo < hi) { int k = (lo + hi) >> 1; if (e0[k] <= elo0) lo = k + 1; else hi = k; }
-  int imin = lo > 0 ? lo - 1 : 0;
-  lo = 0;
-  hi = n0;
-  while (lo < hi) { int k = (lo + hi) >> 1; if (e0[k] <= ehi0) lo = k + 1; else hi = k; }
-  int imax = lo > 0 ? lo - 1 : 0;
+  const int imin = conv_index(tab, elo0);
+  const int imax = conv_index(tab, ehi0);
   const double elo = elo0 < e0[imin] ? e0[imin] : elo0;
   const double ehi = ehi0 > e0[imax + 1] ? e0[imax + 1] : ehi0;
   if (imax == imin) {
@@ -251,14 +360,14 @@ __device__ __forceinline__ double rebin_bin(double elo0, double ehi0, const doub
 
 struct FinSmem {
   float spec[kN];
-  double red[kConvThreads / 32 + 1];
+  double red[kFinThreads / 32 + 1];
   float nrm;
 };
 
 // zone sum, primary continuum (PrimarySource.cpp:66-125), optional 3 keV
 // renormalisation (Relxill.cpp:249-259) and rebin to the caller's grid
 // (rebin_and_normalize_relxill_for_xspec, Relxill.cpp:267-278).
-__global__ void __launch_bounds__(kConvThreads) finalize_relxill_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
+__global__ void __launch_bounds__(kFinThreads) finalize_relxill_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
                                                                         const RelxSetState *__restrict__ sst,
                                                                         const float *__restrict__ cout, int nza,
                                                                         const double *__restrict__ user_e,
@@ -272,7 +381,7 @@ __global__ void __launch_bounds__(kConvThreads) finalize_relxill_kernel(RelxTabl
   double *fo = flux + in.e_off - set;  // flux offsets: e_off counts n+1 edges per set
   if (s.status != RELX_OK || s.model < RELX_RELXILL) {
     if (s.model != RELX_RELCONV || s.status != RELX_OK)
-      for (int i = tid; i < nu; i += kConvThreads) fo[i] = 0.0;
+      for (int i = tid; i < nu; i += kFinThreads) fo[i] = 0.0;
     return;
   }
   const double *ce = tab.conv_e;
@@ -281,7 +390,7 @@ __global__ void __launch_bounds__(kConvThreads) finalize_relxill_kernel(RelxTabl
   const float pnorm = (float) (s.src_norm * s.prim_fac);
   const float rfac = (float) s.norm_fac_refl;
   const bool add_prim = s.refl_frac >= 0;
-  for (int k = tid; k < kN; k += kConvThreads) {
+  for (int k = s.out_lo + tid; k <= s.out_hi; k += kFinThreads) {
     float r = 0.0f;
     for (int z = 0; z < s.nz; z++) r += cout[((size_t) set * nza + z) * kN + k];
     r *= rfac;
@@ -299,20 +408,20 @@ __global__ void __launch_bounds__(kConvThreads) finalize_relxill_kernel(RelxTabl
       m.nrm = (float) ((ce[ind + 1] - ce[ind]) / (double) m.spec[ind]);
     }
     __syncthreads();
-    for (int k = tid; k < kN; k += kConvThreads) m.spec[k] *= m.nrm;
+    for (int k = s.out_lo + tid; k <= s.out_hi; k += kFinThreads) m.spec[k] *= m.nrm;
     __syncthreads();
   }
   const double *ue = user_e + in.e_off;
   const double zf = (s.z > 0) ? (1 + s.z) : 1.0;
-  for (int i = tid; i < nu; i += kConvThreads) {
+  for (int i = tid; i < nu; i += kFinThreads) {
     double elo = ue[i], ehi = ue[i + 1];
     if (s.z > 0) { elo *= zf; ehi *= zf; }
-    fo[i] = rebin_bin(elo, ehi, ce, kN, m.spec);
+    fo[i] = rebin_bin(tab, elo, ehi, m.spec);
   }
 }
 
 // relconv: rebin the convolved spectrum back to the caller's grid, zero outside 0.01-1000 keV
-__global__ void __launch_bounds__(kConvThreads) finalize_relconv_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
+__global__ void __launch_bounds__(kFinThreads) finalize_relconv_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
                                                                         const RelxSetState *__restrict__ sst,
                                                                         const float *__restrict__ cout, int nza,
                                                                         const double *__restrict__ user_e,
@@ -325,20 +434,20 @@ __global__ void __launch_bounds__(kConvThreads) finalize_relconv_kernel(RelxTabl
   const int nu = in.n_ener;
   double *fo = flux + in.e_off - set;
   if (s.status != RELX_OK || sflag[set] != RELX_OK) {
-    for (int i = tid; i < nu; i += kConvThreads) fo[i] = 0.0;
+    for (int i = tid; i < nu; i += kFinThreads) fo[i] = 0.0;
     return;
   }
   const double *ue = user_e + in.e_off;
   const float *sp = cout + (size_t) set * nza * kN;
-  for (int i = tid; i < nu; i += kConvThreads) {
-    double v = rebin_bin(ue[i], ue[i + 1], tab.conv_e, kN, sp);
+  for (int i = tid; i < nu; i += kFinThreads) {
+    double v = rebin_bin(tab, ue[i], ue[i + 1], sp);
     if (ue[i + 1] < 0.01 || ue[i] > 1000.0) v = 0.0;  // Relbase.cpp:233-246
     fo[i] = v;
   }
 }
 
 // relline: profile on the caller's grid, normalised (Relprofile.cpp:749-781, LocalModel.cpp:43-45)
-__global__ void __launch_bounds__(kConvThreads) finalize_relline_kernel(const RelxSetIn *__restrict__ sin,
+__global__ void __launch_bounds__(kFinThreads) finalize_relline_kernel(const RelxSetIn *__restrict__ sin,
                                                                         const RelxSetState *__restrict__ sst,
                                                                         const float *__restrict__ prof,
                                                                         const double *__restrict__ tsum, int ntile_max,
@@ -350,14 +459,31 @@ __global__ void __launch_bounds__(kConvThreads) finalize_relline_kernel(const Re
   const int nu = in.n_ener;
   double *fo = flux + in.e_off - set;
   if (s.status != RELX_OK) {
-    for (int i = tid; i < nu; i += kConvThreads) fo[i] = 0.0;
+    for (int i = tid; i < nu; i += kFinThreads) fo[i] = 0.0;
     return;
   }
-  const double scale = profile_scale(s, tsum, set, ntile_max, nza, tile_bins);
+  __shared__ double scale_sh;
+  if (tid == 0) {
+    // renorm_relline_profile (Relprofile.cpp:766-781): zones in order, tiles in order within a zone
+    double scale = 1.0;
+    if (s.relline_norm > 0.0) {
+      const int ntiles = (s.win_hi - s.win_lo + tile_bins - 1) / tile_bins;
+      double sum = 0.0;
+      for (int z = 0; z < s.nz; z++) {
+        double zs = 0.0;
+        for (int t = 0; t < ntiles; t++) zs += tsum[((size_t) set * ntile_max + t) * nza + z];
+        sum += zs;
+      }
+      scale = s.relline_norm / sum;
+    }
+    scale_sh = scale;
+  }
+  __syncthreads();
+  const double scale = scale_sh;
   const float *p = prof + in.e_off;
   // bins outside the window hold 0; with an empty profile the reference's
   // renormalisation multiplies 0 by relline_norm/0 and returns NaN, as here
-  for (int i = tid; i < nu; i += kConvThreads)
+  for (int i = tid; i < nu; i += kFinThreads)
     fo[i] = ((i >= s.win_lo && i < s.win_hi) ? (double) p[i] : 0.0) * scale;
 }
 

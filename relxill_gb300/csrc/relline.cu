@@ -26,39 +26,6 @@ constexpr int kLineThreads = kLineWarps * 32;
 constexpr int kLineTile = 512;   // energy bins per CTA
 constexpr float kH = 5e-3f;
 
-// ---- float-float arithmetic ---------------------------------------------
-__device__ __forceinline__ float2 two_sum(float a, float b) {
-  float s = __fadd_rn(a, b);
-  float bb = __fsub_rn(s, a);
-  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-  return make_float2(s, e);
-}
-__device__ __forceinline__ float2 qts(float a, float b) {
-  float s = __fadd_rn(a, b);
-  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
-}
-__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
-  float2 s = two_sum(a.x, b.x);
-  return qts(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
-}
-__device__ __forceinline__ float2 ff_neg(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
-  float p = __fmul_rn(a.x, b.x);
-  float e = fmaf(a.x, b.x, -p);
-  e = __fadd_rn(e, __fadd_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
-  return qts(p, e);
-}
-__device__ __forceinline__ float2 ff_mulf(float2 a, float b) {
-  float p = __fmul_rn(a.x, b);
-  float e = fmaf(a.x, b, -p);
-  e = __fadd_rn(e, __fmul_rn(a.y, b));
-  return qts(p, e);
-}
-__device__ __forceinline__ bool ff_ge(float2 a, float2 b) {
-  float2 d = ff_add(a, ff_neg(b));
-  return d.x > 0.0f || (d.x == 0.0f && d.y >= 0.0f);
-}
-
 // per-radius constants (warp uniform)
 struct RadC {
   float2 gmin, gmax, dg;  // float-float
@@ -66,7 +33,6 @@ struct RadC {
   float edge_lo, edge_hi; // 2 sqrt(H) sum_k F_k(H), same at 1-H (emissivity factored out)
   float2 eH, e1H;         // gstar2ener(H), gstar2ener(1-H) in float-float
   bool red_H;             // gstar2ener(H) >= 0.95
-  float ew;               // emissivity * weight
   int ng, limb;
   float inv_dgs;          // (ng-1) / (1-2H)
   const float2 *gs;       // table g* points as float-float (shared memory)
@@ -78,9 +44,15 @@ struct Absc {
   int n, i;       // Romberg level and index (n = -1: midpoint)
 };
 
+// transfer functions at one radius: trff (and cosne for limb laws) at the table g* points
+template <bool LIMB> struct TW;
+template <> struct TW<false> { float2 t; };
+template <> struct TW<true> { float4 t; };
+
 // integrand F_k(x) = E^3 trf_k(x) [limb] / sqrt(x (1-x)), k = 0, 1  (relb_func,
 // Relprofile.cpp:489-521 times (gmax - gmin) / emis)
-__device__ __forceinline__ float2 eval_F(float x, float y, const RadC &rc, const float4 *__restrict__ tw,
+template <bool LIMB>
+__device__ __forceinline__ float2 eval_F(float x, float y, const RadC &rc, const TW<LIMB> *__restrict__ tw,
                                          const Absc &ab) {
   const int ng = rc.ng;
   float t = (x - kH) * rc.inv_dgs;
@@ -104,38 +76,44 @@ __device__ __forceinline__ float2 eval_F(float x, float y, const RadC &rc, const
     ind = (int) floorf(t);
     ind = max(0, min(ind, ng - 2));
   }
-  float inte = t - (float) ind;
-  float inte1 = 1.0f - inte;
-  float4 A = tw[ind], B = tw[ind + 1];
-  float e = rc.gminf + x * rc.dgf;
-  float e3 = e * e * e * rsqrtf(x * y);
-  float f0 = e3 * (inte * A.x + inte1 * B.x);
-  float f1 = e3 * (inte * A.y + inte1 * B.y);
-  if (rc.limb) {
+  const float inte = t - (float) ind;
+  const float inte1 = 1.0f - inte;
+  const float e = rc.gminf + x * rc.dgf;
+  const float e3 = e * e * e * rsqrtf(x * y);
+  if constexpr (!LIMB) {
+    const float2 A = tw[ind].t, B = tw[ind + 1].t;
+    return make_float2(e3 * (inte * A.x + inte1 * B.x), e3 * (inte * A.y + inte1 * B.y));
+  } else {
+    const float4 A = tw[ind].t, B = tw[ind + 1].t;
+    float f0 = e3 * (inte * A.x + inte1 * B.x);
+    float f1 = e3 * (inte * A.y + inte1 * B.y);
     float m0 = inte * A.z + inte1 * B.z, m1 = inte * A.w + inte1 * B.w;
     if (rc.limb == 1) { f0 *= (1.0f + 2.06f * m0); f1 *= (1.0f + 2.06f * m1); }
-    else { f0 *= logf(1.0f + 1.0f / m0); f1 *= logf(1.0f + 1.0f / m1); }
+    else if (rc.limb == 2) { f0 *= logf(1.0f + 1.0f / m0); f1 *= logf(1.0f + 1.0f / m1); }
+    return make_float2(f0, f1);
   }
-  return make_float2(f0, f1);
 }
 
-// romberg_integration (Relprofile.cpp:524-579) over [ga, gb] in g*, both
-// branches in lock step; interior sums reuse the previous level's points.
+// romberg_integration (Relprofile.cpp:524-579) over [ga, gb] in g*, both branches in
+// lock step; interior sums reuse the previous level's points; the Romberg table is
+// updated in place (p[ii] holds t[ii][n-ii] of the last completed level).
+template <bool LIMB>
 __device__ __forceinline__ float romberg2(float ga, float ca, float gb, float cb, const RadC &rc,
-                                          const float4 *__restrict__ tw, Absc ab) {
+                                          const TW<LIMB> *__restrict__ tw, Absc ab) {
   const float pas0 = gb - ga;
   ab.n = 0;
   ab.i = 0;
-  float2 fa = eval_F(ga, ca, rc, tw, ab);
+  const float2 fa = eval_F<LIMB>(ga, ca, rc, tw, ab);
   ab.i = 1;
-  float2 fb = eval_F(gb, cb, rc, tw, ab);
-  float ta0 = (fa.x + fb.x) * 0.5f, ta1 = (fa.y + fb.y) * 0.5f;
+  const float2 fb = eval_F<LIMB>(gb, cb, rc, tw, ab);
+  const float ta0 = (fa.x + fb.x) * 0.5f, ta1 = (fa.y + fb.y) * 0.5f;
   float p0[7], p1[7];
   p0[0] = ta0 * pas0;
   p1[0] = ta1 * pas0;
   float s0 = 0.0f, s1 = 0.0f;
   bool c0 = false, c1 = false;
   float r0 = 0.0f, r1 = 0.0f;
+  constexpr float inv4m1[7] = {0.f, 1.f / 3.f, 1.f / 15.f, 1.f / 63.f, 1.f / 255.f, 1.f / 1023.f, 1.f / 4095.f};
 #pragma unroll
   for (int n = 1; n <= 6; n++) {
     const float sc = ldexpf(1.0f, -n);
@@ -143,30 +121,33 @@ __device__ __forceinline__ float romberg2(float ga, float ca, float gb, float cb
     float a0 = 0.0f, a1 = 0.0f;
     ab.n = n;
     for (int i = 1; i < (1 << n); i += 2) {
-      float u = pas0 * ((float) i * sc);
+      const float u = pas0 * ((float) i * sc);
       ab.i = i;
-      float2 f = eval_F(ga + u, ca - u, rc, tw, ab);
+      const float2 f = eval_F<LIMB>(ga + u, ca - u, rc, tw, ab);
       a0 += f.x;
       a1 += f.y;
     }
     s0 += a0;
     s1 += a1;
-    float q0[7], q1[7];
-    q0[0] = (ta0 + s0) * pas;
-    q1[0] = (ta1 + s1) * pas;
+    const float old0 = p0[n - 1], old1 = p1[n - 1];
+    float t0 = (ta0 + s0) * pas, t1 = (ta1 + s1) * pas;
     float r = 1.0f;
 #pragma unroll
     for (int ii = 1; ii <= n; ii++) {
       r *= 4.0f;
-      q0[ii] = (r * q0[ii - 1] - p0[ii - 1]) / (r - 1.0f);
-      q1[ii] = (r * q1[ii - 1] - p1[ii - 1]) / (r - 1.0f);
+      const float n0 = (r * t0 - p0[ii - 1]) * inv4m1[ii];
+      const float n1 = (r * t1 - p1[ii - 1]) * inv4m1[ii];
+      p0[ii - 1] = t0;
+      p1[ii - 1] = t1;
+      t0 = n0;
+      t1 = n1;
     }
-    float o0 = fabsf(q0[n] - p0[n - 1]) / q0[n];
-    float o1 = fabsf(q1[n] - p1[n - 1]) / q1[n];
-    if (!c0) { r0 = q0[n]; if (!(o0 > 0.02f)) c0 = true; }
-    if (!c1) { r1 = q1[n]; if (!(o1 > 0.02f)) c1 = true; }
-#pragma unroll
-    for (int ii = 0; ii <= n; ii++) { p0[ii] = q0[ii]; p1[ii] = q1[ii]; }
+    p0[n] = t0;
+    p1[n] = t1;
+    const float o0 = fabsf(t0 - old0) / t0;
+    const float o1 = fabsf(t1 - old1) / t1;
+    if (!c0) { r0 = t0; if (!(o0 > 0.02f)) c0 = true; }
+    if (!c1) { r1 = t1; if (!(o1 > 0.02f)) c1 = true; }
     if (c0 && c1) break;
   }
   return r0 + r1;
@@ -181,8 +162,9 @@ __device__ __forceinline__ float sqrt_diff(float hi, float lo) {
 }
 
 // integ_relline_bin (Relprofile.cpp:650-726) with the emissivity factored out
+template <bool LIMB>
 __device__ __forceinline__ float integ_bin(float2 Elo, float2 Ehi, bool red_lo, const RadC &rc,
-                                           const float4 *__restrict__ tw) {
+                                           const TW<LIMB> *__restrict__ tw) {
   float glo = ff_sub_to_float(Elo, rc.gmin) * rc.inv_dg;
   float clo = ff_sub_to_float(rc.gmax, Elo) * rc.inv_dg;
   if (glo < 0.0f) { glo = 0.0f; clo = 1.0f; } else if (glo > 1.0f) { glo = 1.0f; clo = 0.0f; }
@@ -216,29 +198,200 @@ __device__ __forceinline__ float integ_bin(float2 Elo, float2 Ehi, bool red_lo, 
   }
   if (has_lo && has_hi) {
     if (red) {
-      flu += romberg2(ga, ca, gb, cb, rc, tw, ab);
+      flu += romberg2<LIMB>(ga, ca, gb, cb, rc, tw, ab);
     } else {
       ab.n = -1;
-      float2 f = eval_F(0.5f * (ga + gb), 0.5f * (ca + cb), rc, tw, ab);
+      const float2 f = eval_F<LIMB>(0.5f * (ga + gb), 0.5f * (ca + cb), rc, tw, ab);
       flu += (f.x + f.y) * (gb - ga);
     }
   }
   return flu;
 }
 
+constexpr int kChunk = 128;  // radius records staged per chunk
+
+template <bool LIMB>
 struct LineSmem {
   float acc[kLineWarps][kLineTile];
   float2 eff[kLineTile + 1];
   unsigned char red[kLineTile];
+  TW<LIMB> tw[kLineWarps][RELX_MAX_NG];
+  RelxRadRec rec[kChunk];
+  float2 gs[RELX_MAX_NG];   // table g* points (Relprofile.cpp:104-106) as float-float
+  double red_sum[kLineWarps + 1];
+  TW<LIMB> tab[1];          // (a, mu0)-interpolated table [n_r][n_g], dynamic tail
+};
+static_assert(offsetof(LineSmem<false>, rec) % 16 == 0 && offsetof(LineSmem<true>, rec) % 16 == 0,
+              "radius records are staged as int4 rows");
+
+// limb law at one table point (Relprofile.cpp:512-519)
+__device__ __forceinline__ float limb_factor(int limb, float mu) {
+  if (limb == 1) return 1.0f + 2.06f * mu;
+  if (limb == 2) return logf(1.0f + 1.0f / mu);
+  return 1.0f;
+}
+
+template <bool LIMB>
+__global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
+                                                                  const RelxSetState *__restrict__ sst,
+                                                                  const RelxRadial *__restrict__ srad,
+                                                                  const double *__restrict__ line_e, int nza,
+                                                                  float *__restrict__ prof, double *__restrict__ tsum,
+                                                                  int ntile_max) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  LineSmem<LIMB> &m = *reinterpret_cast<LineSmem<LIMB> *>(smem_raw);
+  const int set = blockIdx.y, tile = blockIdx.x;
+  const RelxSetState &s = sst[set];
+  if (s.status != RELX_OK) return;
+  if ((s.limb != 0) != LIMB) return;
+  const int tlo = s.win_lo + tile * kLineTile;
+  const int thi = min(s.win_hi, tlo + kLineTile);
+  if (tlo >= thi) return;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const RelxRadial &R = srad[set];
+  const int nr = tab.rel_nr, nm = tab.rel_nmu0, ng = tab.rel_ng;
+  const int nz = s.nz;
+  const bool is_line = (s.model == RELX_RELLINE);
+  const double *ge = is_line ? (line_e + sin[set].e_off) : tab.conv_e;
+  const size_t pbase = is_line ? (size_t) sin[set].e_off : (size_t) set * nza * RELX_NCONV;
+  const size_t zstride = is_line ? 0 : RELX_NCONV;
+  TW<LIMB> *tabI = m.tab;
+
+  // stage the (a, mu0) interpolation of the transfer functions (interpol_a_mu0, Relprofile.cpp:39-80)
+  {
+    const size_t b00 = (size_t) s.ind_a * nm + s.ind_mu0, b10 = (size_t) (s.ind_a + 1) * nm + s.ind_mu0;
+    const size_t b01 = b00 + 1, b11 = b10 + 1;
+    const float f1 = s.ifac_a, f2 = s.ifac_mu0;
+    const float w00 = (1.0f - f1) * (1.0f - f2), w10 = f1 * (1.0f - f2), w01 = (1.0f - f1) * f2, w11 = f1 * f2;
+    for (int q = tid; q < nr * ng; q += kLineThreads) {
+      const float4 a = __ldg(&tab.rel_tc[b00 * nr * ng + q]), b = __ldg(&tab.rel_tc[b10 * nr * ng + q]);
+      const float4 c = __ldg(&tab.rel_tc[b01 * nr * ng + q]), d = __ldg(&tab.rel_tc[b11 * nr * ng + q]);
+      if constexpr (!LIMB) {
+        tabI[q].t = make_float2(w00 * a.x + w10 * b.x + w01 * c.x + w11 * d.x,
+                                w00 * a.y + w10 * b.y + w01 * c.y + w11 * d.y);
+      } else {
+        tabI[q].t = make_float4(w00 * a.x + w10 * b.x + w01 * c.x + w11 * d.x,
+                                w00 * a.y + w10 * b.y + w01 * c.y + w11 * d.y,
+                                w00 * a.z + w10 * b.z + w01 * c.z + w11 * d.z,
+                                w00 * a.w + w10 * b.w + w01 * c.w + w11 * d.w);
+      }
+    }
+    for (int j = tid; j <= thi - tlo; j += kLineThreads) m.eff[j] = ff_from_double(ge[tlo + j]);
+    for (int j = tid; j < thi - tlo; j += kLineThreads) m.red[j] = ge[tlo + j] >= 0.95 ? 1 : 0;
+    for (int i = tid; i < kLineWarps * kLineTile; i += kLineThreads) (&m.acc[0][0])[i] = 0.0f;
+    for (int g = tid; g < ng; g += kLineThreads)
+      m.gs[g] = ff_from_double(5e-3 + (1.0 - 2 * 5e-3) / (ng - 1) * ((float) g));
+  }
+  __syncthreads();
+
+  const float inv_dgs = (float) ((ng - 1) / (1.0 - 2 * 5e-3));
+  const float sH = sqrtf(kH), isq = rsqrtf(kH * (1.0f - kH));
+  for (int z = 0; z < nz; z++) {
+    const int i0 = s.zi0[z], i1 = s.zi1[z];
+    for (int c0 = i0; c0 <= i1; c0 += kChunk) {
+      const int cn = min(kChunk, i1 + 1 - c0);
+      // stage the chunk's radius records (64-byte rows, coalesced)
+      {
+        const int4 *src = reinterpret_cast<const int4 *>(&R.rec[c0]);
+        int4 *dst = reinterpret_cast<int4 *>(m.rec);
+        for (int q = tid; q < cn * 4; q += kLineThreads) dst[q] = src[q];
+      }
+      __syncthreads();
+      for (int ci = warp; ci < cn; ci += kLineWarps) {
+        const RelxRadRec &rr = m.rec[ci];
+        const int ielo = rr.ielo, iehi = rr.iehi;
+        if (!(ielo >= 0 && ielo < thi && iehi >= tlo)) continue;
+        // trf(g*) at this radius: interp_lin_1d(ifac_r, T[ind+1], T[ind]) (Relprofile.cpp:280-293)
+        const int it = rr.itab;
+        const float fr = rr.ifac;
+        for (int g = lane; g < ng; g += 32) {
+          const auto lo = tabI[(it + 1) * ng + g].t, hi = tabI[it * ng + g].t;
+          if constexpr (!LIMB) {
+            m.tw[warp][g].t = make_float2(fr * hi.x + (1.0f - fr) * lo.x, fr * hi.y + (1.0f - fr) * lo.y);
+          } else {
+            m.tw[warp][g].t = make_float4(fr * hi.x + (1.0f - fr) * lo.x, fr * hi.y + (1.0f - fr) * lo.y,
+                                          fr * hi.z + (1.0f - fr) * lo.z, fr * hi.w + (1.0f - fr) * lo.w);
+          }
+        }
+        __syncwarp();
+        const TW<LIMB> *tw = m.tw[warp];
+        RadC rc;
+        rc.gmin = rr.gmin;
+        rc.gmax = rr.gmax;
+        rc.dg = rr.dg;
+        rc.gminf = rc.gmin.x;
+        rc.dgf = rc.dg.x;
+        rc.inv_dg = rr.inv_dg;
+        rc.ng = ng;
+        rc.limb = s.limb;
+        rc.inv_dgs = inv_dgs;
+        rc.eH = rr.eH;
+        rc.e1H = rr.e1H;
+        rc.red_H = rr.red_H != 0;
+        rc.gs = m.gs;
+        {
+          // int_edge norms (Relprofile.cpp:585-621): trf at g* = H is T[1], at 1 - H is T[ng-2]
+          float e = rc.gminf + kH * rc.dgf;
+          float e3 = e * e * e * isq;
+          float f0, f1;
+          if constexpr (!LIMB) {
+            f0 = tw[1].t.x;
+            f1 = tw[1].t.y;
+          } else {
+            f0 = tw[1].t.x * limb_factor(rc.limb, tw[1].t.z);
+            f1 = tw[1].t.y * limb_factor(rc.limb, tw[1].t.w);
+          }
+          rc.edge_lo = 2.0f * sH * e3 * (f0 + f1);
+          e = rc.gminf + (1.0f - kH) * rc.dgf;
+          e3 = e * e * e * isq;
+          if constexpr (!LIMB) {
+            f0 = tw[ng - 2].t.x;
+            f1 = tw[ng - 2].t.y;
+          } else {
+            f0 = tw[ng - 2].t.x * limb_factor(rc.limb, tw[ng - 2].t.z);
+            f1 = tw[ng - 2].t.y * limb_factor(rc.limb, tw[ng - 2].t.w);
+          }
+          rc.edge_hi = 2.0f * sH * e3 * (f0 + f1);
+        }
+        const float ew = rr.ew;
+        const int jlo = max(ielo, tlo), jhi = min(iehi, thi - 1);
+        for (int j = jlo + lane; j <= jhi; j += 32) {
+          const int jj = j - tlo;
+          const float v = integ_bin<LIMB>(m.eff[jj], m.eff[jj + 1], m.red[jj] != 0, rc, tw);
+          m.acc[warp][jj] += v * ew;
+        }
+        __syncwarp();
+      }
+      __syncthreads();
+    }
+    // zone end: sum the warp rows in order, divide by the bin centre (renorm_relline_profile, Relprofile.cpp:753-762)
+    double part = 0.0;
+    for (int jj = tid; jj < thi - tlo; jj += kLineThreads) {
+      float v = 0.0f;
+#pragma unroll
+      for (int w = 0; w < kLineWarps; w++) { v += m.acc[w][jj]; m.acc[w][jj] = 0.0f; }
+      const float emid = 0.5f * (m.eff[jj].x + m.eff[jj + 1].x);
+      const float pv = v / emid;
+      prof[pbase + z * zstride + tlo + jj] = pv;
+      part += (double) pv;
+    }
+    const double zs = block_sum_d<kLineThreads>(part, m.red_sum);
+    if (tid == 0) tsum[((size_t) set * ntile_max + tile) * nza + z] = zs;
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// emission-angle distribution per zone (Relprofile.cpp:908-938), one CTA per set
+// ---------------------------------------------------------------------------
+struct HistSmem {
   float4 tw[kLineWarps][RELX_MAX_NG];
   float hterm[kLineWarps][2 * RELX_MAX_NG];
   unsigned char hbin[kLineWarps][2 * RELX_MAX_NG];
   float hist[kLineWarps][RELX_MAX_INCL];
-  float gfac[RELX_MAX_NG];  // d_gstar / sqrt(g*(1-g*)) at the table g* points
-  float2 gs[RELX_MAX_NG];   // table g* points (Relprofile.cpp:104-106) as float-float
-  double red_sum[kLineWarps + 1];
-  // the (a, mu0)-interpolated table, [n_r][n_g]
-  float4 tab[1];  // dynamic tail
+  float gfac[RELX_MAX_NG];   // d_gstar / sqrt(g*(1-g*))
+  float gsf[RELX_MAX_NG];
+  float4 tab[1];
 };
 
 // FP64 emission-angle cosine of one fine radius, table point g, branch k
@@ -258,177 +411,79 @@ __device__ double cosne_fp64(const RelxTables &tab, const RelxSetState &s, int i
   return lerp1(ifac, v[0], v[1]);
 }
 
-template <bool HIST>
-__global__ void __launch_bounds__(kLineThreads) relline_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
-                                                               const RelxSetState *__restrict__ sst,
-                                                               const RelxRadial *__restrict__ srad,
-                                                               const double *__restrict__ line_e, int nza,
-                                                               float *__restrict__ prof, float *__restrict__ dist,
-                                                               double *__restrict__ tsum, int ntile_max) {
+__global__ void __launch_bounds__(kLineThreads) hist_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
+                                                            const RelxRadial *__restrict__ srad, int nza,
+                                                            float *__restrict__ dist) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  LineSmem &m = *reinterpret_cast<LineSmem *>(smem_raw);
-  const int set = blockIdx.y, tile = blockIdx.x;
+  HistSmem &m = *reinterpret_cast<HistSmem *>(smem_raw);
+  const int set = blockIdx.x;
   const RelxSetState &s = sst[set];
-  if (s.status != RELX_OK) return;
-  const int tlo = s.win_lo + tile * kLineTile;
-  const int thi = min(s.win_hi, tlo + kLineTile);
-  const bool do_hist = HIST && tile == 0;
-  if (tlo >= thi && !do_hist) return;
+  if (s.status != RELX_OK || s.model < RELX_RELXILL) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const RelxRadial &R = srad[set];
-  const int nr = tab.rel_nr, nm = tab.rel_nmu0, ng = tab.rel_ng;
-  const int nz = s.nz;
-  const bool is_line = (s.model == RELX_RELLINE);
-  const double *ge = is_line ? (line_e + sin[set].e_off) : tab.conv_e;
-  const size_t pbase = is_line ? (size_t) sin[set].e_off : (size_t) set * nza * RELX_NCONV;
-  const size_t zstride = is_line ? 0 : RELX_NCONV;
-  float4 *tabI = m.tab;
-
-  // stage the (a, mu0) interpolation of the transfer functions (interpol_a_mu0, Relprofile.cpp:39-80)
+  const int nr = tab.rel_nr, nm = tab.rel_nmu0, ng = tab.rel_ng, n_incl = tab.x_nincl;
   {
     const size_t b00 = (size_t) s.ind_a * nm + s.ind_mu0, b10 = (size_t) (s.ind_a + 1) * nm + s.ind_mu0;
     const size_t b01 = b00 + 1, b11 = b10 + 1;
     const float f1 = s.ifac_a, f2 = s.ifac_mu0;
     const float w00 = (1.0f - f1) * (1.0f - f2), w10 = f1 * (1.0f - f2), w01 = (1.0f - f1) * f2, w11 = f1 * f2;
     for (int q = tid; q < nr * ng; q += kLineThreads) {
-      float4 a = __ldg(&tab.rel_tc[b00 * nr * ng + q]), b = __ldg(&tab.rel_tc[b10 * nr * ng + q]);
-      float4 c = __ldg(&tab.rel_tc[b01 * nr * ng + q]), d = __ldg(&tab.rel_tc[b11 * nr * ng + q]);
-      float4 r;
-      r.x = w00 * a.x + w10 * b.x + w01 * c.x + w11 * d.x;
-      r.y = w00 * a.y + w10 * b.y + w01 * c.y + w11 * d.y;
-      r.z = w00 * a.z + w10 * b.z + w01 * c.z + w11 * d.z;
-      r.w = w00 * a.w + w10 * b.w + w01 * c.w + w11 * d.w;
-      tabI[q] = r;
+      const float4 a = __ldg(&tab.rel_tc[b00 * nr * ng + q]), b = __ldg(&tab.rel_tc[b10 * nr * ng + q]);
+      const float4 c = __ldg(&tab.rel_tc[b01 * nr * ng + q]), d = __ldg(&tab.rel_tc[b11 * nr * ng + q]);
+      m.tab[q] = make_float4(w00 * a.x + w10 * b.x + w01 * c.x + w11 * d.x, w00 * a.y + w10 * b.y + w01 * c.y + w11 * d.y,
+                             w00 * a.z + w10 * b.z + w01 * c.z + w11 * d.z, w00 * a.w + w10 * b.w + w01 * c.w + w11 * d.w);
     }
-    for (int j = tid; j <= thi - tlo && tlo < thi; j += kLineThreads) m.eff[j] = ff_from_double(ge[tlo + j]);
-    for (int j = tid; j < thi - tlo; j += kLineThreads) m.red[j] = ge[tlo + j] >= 0.95 ? 1 : 0;
-    for (int i = tid; i < kLineWarps * kLineTile; i += kLineThreads) (&m.acc[0][0])[i] = 0.0f;
-    for (int g = tid; g < ng; g += kLineThreads)
-      m.gs[g] = ff_from_double(5e-3 + (1.0 - 2 * 5e-3) / (ng - 1) * ((float) g));
-    if (do_hist) {
-      for (int g = tid; g < ng; g += kLineThreads) {
-        double gs = 5e-3 + (1.0 - 2 * 5e-3) / (ng - 1) * ((float) g);
-        double gs1 = 5e-3 + (1.0 - 2 * 5e-3) / (ng - 1) * ((float) 1);
-        double gs0 = 5e-3;
-        double dgs = (g == 0 || g == ng - 1) ? 0.5 * (gs1 - gs0) + 5e-3 : gs1 - gs0;
-        m.gfac[g] = (float) (dgs / sqrt(gs - gs * gs));
-      }
-      for (int i = tid; i < kLineWarps * RELX_MAX_INCL; i += kLineThreads) (&m.hist[0][0])[i] = 0.0f;
+    for (int g = tid; g < ng; g += kLineThreads) {
+      double gs = 5e-3 + (1.0 - 2 * 5e-3) / (ng - 1) * ((float) g);
+      double gs1 = 5e-3 + (1.0 - 2 * 5e-3) / (ng - 1) * ((float) 1);
+      double dgs = (g == 0 || g == ng - 1) ? 0.5 * (gs1 - 5e-3) + 5e-3 : gs1 - 5e-3;
+      m.gfac[g] = (float) (dgs / sqrt(gs - gs * gs));
+      m.gsf[g] = (float) gs;
     }
+    for (int i = tid; i < kLineWarps * RELX_MAX_INCL; i += kLineThreads) (&m.hist[0][0])[i] = 0.0f;
   }
   __syncthreads();
-
-  const int n_incl = tab.x_nincl;
-  const float inv_dgs = (float) ((ng - 1) / (1.0 - 2 * 5e-3));
-  for (int z = 0; z < nz; z++) {
-    const int i0 = s.zi0[z], i1 = s.zi1[z];
-    for (int ii = i0 + warp; ii <= i1; ii += kLineWarps) {
-      const int ielo = R.ielo[ii], iehi = R.iehi[ii];
-      const bool overlap = (ielo >= 0) && (ielo < thi) && (iehi >= tlo);
-      if (!overlap && !do_hist) continue;
-      // trf(g*) at this radius: interp_lin_1d(ifac_r, T[ind+1], T[ind]) (Relprofile.cpp:280-293)
-      const int it = R.itab[ii];
-      const float fr = (float) R.ifac[ii];
+  for (int z = 0; z < s.nz; z++) {
+    for (int ii = s.zi0[z] + warp; ii <= s.zi1[z]; ii += kLineWarps) {
+      const RelxRadRec rr = R.rec[ii];
+      if (rr.ielo < 0) continue;  // radius outside the line-profile grid (Relprofile.cpp:863)
+      const int it = rr.itab;
+      const float fr = rr.ifac;
       for (int g = lane; g < ng; g += 32) {
-        float4 lo = tabI[(it + 1) * ng + g], hi = tabI[it * ng + g];
-        float4 r;
-        r.x = fr * hi.x + (1.0f - fr) * lo.x;
-        r.y = fr * hi.y + (1.0f - fr) * lo.y;
-        r.z = fr * hi.z + (1.0f - fr) * lo.z;
-        r.w = fr * hi.w + (1.0f - fr) * lo.w;
-        m.tw[warp][g] = r;
+        const float4 lo = m.tab[(it + 1) * ng + g], hi = m.tab[it * ng + g];
+        m.tw[warp][g] = make_float4(fr * hi.x + (1.0f - fr) * lo.x, fr * hi.y + (1.0f - fr) * lo.y,
+                                    fr * hi.z + (1.0f - fr) * lo.z, fr * hi.w + (1.0f - fr) * lo.w);
       }
       __syncwarp();
-      const float4 *tw = m.tw[warp];
-      RadC rc;
-      rc.gmin = R.gmin_ff[ii];
-      rc.gmax = R.gmax_ff[ii];
-      rc.dg = R.dg_ff[ii];
-      rc.gminf = rc.gmin.x;
-      rc.dgf = rc.dg.x;
-      rc.inv_dg = R.inv_dg[ii];
-      rc.ng = ng;
-      rc.limb = s.limb;
-      rc.inv_dgs = inv_dgs;
-      rc.ew = R.ew[ii];
-      rc.eH = R.eH_ff[ii];
-      rc.e1H = R.e1H_ff[ii];
-      rc.red_H = R.red_H[ii] != 0;
-      rc.gs = m.gs;
-      {
-        // int_edge norms (Relprofile.cpp:585-621): trf at g* = H is T[1], at 1 - H is T[ng-2]
-        const float sH = sqrtf(kH), isq = rsqrtf(kH * (1.0f - kH));
-        float e = rc.gminf + kH * rc.dgf;
-        float e3 = e * e * e * isq;
-        float4 A = tw[1];
-        float f0 = A.x, f1 = A.y;
-        if (rc.limb == 1) { f0 *= 1.0f + 2.06f * A.z; f1 *= 1.0f + 2.06f * A.w; }
-        else if (rc.limb == 2) { f0 *= logf(1.0f + 1.0f / A.z); f1 *= logf(1.0f + 1.0f / A.w); }
-        rc.edge_lo = 2.0f * sH * e3 * (f0 + f1);
-        e = rc.gminf + (1.0f - kH) * rc.dgf;
-        e3 = e * e * e * isq;
-        A = tw[ng - 2];
-        f0 = A.x;
-        f1 = A.y;
-        if (rc.limb == 1) { f0 *= 1.0f + 2.06f * A.z; f1 *= 1.0f + 2.06f * A.w; }
-        else if (rc.limb == 2) { f0 *= logf(1.0f + 1.0f / A.z); f1 *= logf(1.0f + 1.0f / A.w); }
-        rc.edge_hi = 2.0f * sH * e3 * (f0 + f1);
+      const float re = (float) R.re[ii];
+      const float c = re * re * re * (float) (4.0 * kPi * kPi) * rr.ew;
+      for (int q = lane; q < 2 * ng; q += 32) {
+        const int g = q >> 1, k = q & 1;
+        const float4 T = m.tw[warp][g];
+        const float ge_ = m.gsf[g] * rr.dg.x + rr.gmin.x;
+        m.hterm[warp][q] = c * ge_ * ge_ * m.gfac[g] * (k ? T.y : T.x);
+        const float mu = k ? T.w : T.z;
+        const float xb = (float) n_incl * (1.0f - mu);
+        int b;
+        if (fabsf(xb - rintf(xb)) < 1e-5f) {
+          const double mud = cosne_fp64(tab, s, it, R.ifac[ii], g, k);
+          b = ((int) (n_incl * (1 - mud) + 1)) - 1;  // get_cosne_bin, Relprofile.cpp:799-801
+        } else {
+          b = ((int) (xb + 1.0f)) - 1;
+        }
+        m.hbin[warp][q] = (unsigned char) max(0, min(b, n_incl - 1));
       }
-      if (overlap) {
-        const int jlo = max(ielo, tlo), jhi = min(iehi, thi - 1);
-        for (int j = jlo + lane; j <= jhi; j += 32) {
-          const int jj = j - tlo;
-          float v = integ_bin(m.eff[jj], m.eff[jj + 1], m.red[jj] != 0, rc, tw);
-          m.acc[warp][jj] += v * rc.ew;
-        }
-      }
-      if (do_hist) {
-        // emission-angle distribution (Relprofile.cpp:908-938)
-        const float re = (float) R.re[ii];
-        const float c = re * re * re * (float) (4.0 * kPi * kPi) * rc.ew;
-        for (int q = lane; q < 2 * ng; q += 32) {
-          const int g = q >> 1, k = q & 1;
-          const float4 T = tw[g];
-          const float ge_ = m.gs[g].x * rc.dgf + rc.gminf;
-          const float trf = k ? T.y : T.x;
-          m.hterm[warp][q] = c * ge_ * ge_ * m.gfac[g] * trf;
-          float mu = k ? T.w : T.z;
-          float xb = (float) n_incl * (1.0f - mu);
-          float xr = rintf(xb);
-          if (fabsf(xb - xr) < 1e-5f) {
-            double mud = cosne_fp64(tab, s, it, R.ifac[ii], g, k);
-            int b = ((int) (n_incl * (1 - mud) + 1)) - 1;
-            m.hbin[warp][q] = (unsigned char) max(0, min(b, n_incl - 1));
-          } else {
-            int b = ((int) (xb + 1.0f)) - 1;
-            m.hbin[warp][q] = (unsigned char) max(0, min(b, n_incl - 1));
-          }
-        }
-        __syncwarp();
-        if (lane < n_incl) {
-          float acc = 0.0f;
-          for (int q = 0; q < 2 * ng; q++)
-            if (m.hbin[warp][q] == lane) acc += m.hterm[warp][q];
-          m.hist[warp][lane] += acc;
-        }
+      __syncwarp();
+      if (lane < n_incl) {
+        float acc = 0.0f;
+        for (int q = 0; q < 2 * ng; q++)
+          if (m.hbin[warp][q] == lane) acc += m.hterm[warp][q];
+        m.hist[warp][lane] += acc;
       }
       __syncwarp();
     }
     __syncthreads();
-    // zone end: sum the warp rows in order, divide by the bin centre (renorm_relline_profile, Relprofile.cpp:753-762)
-    double part = 0.0;
-    for (int jj = tid; jj < thi - tlo; jj += kLineThreads) {
-      float v = 0.0f;
-#pragma unroll
-      for (int w = 0; w < kLineWarps; w++) { v += m.acc[w][jj]; m.acc[w][jj] = 0.0f; }
-      const float emid = 0.5f * (m.eff[jj].x + m.eff[jj + 1].x);
-      float pv = v / emid;
-      prof[pbase + z * zstride + tlo + jj] = pv;
-      part += (double) pv;
-    }
-    double zs = block_sum_d<kLineThreads>(part, m.red_sum);
-    if (tid == 0) tsum[((size_t) set * ntile_max + tile) * nza + z] = zs;
-    if (do_hist && tid < n_incl) {
+    if (tid < n_incl) {
       float h = 0.0f;
       for (int w = 0; w < kLineWarps; w++) { h += m.hist[w][tid]; m.hist[w][tid] = 0.0f; }
       dist[((size_t) set * nza + z) * RELX_MAX_INCL + tid] = h;
@@ -437,21 +492,32 @@ __global__ void __launch_bounds__(kLineThreads) relline_kernel(RelxTables tab, c
   }
 }
 
-size_t line_smem_bytes(int nr, int ng) { return sizeof(LineSmem) + sizeof(float4) * (size_t) (nr * ng - 1); }
+size_t line_smem_bytes(int nr, int ng, bool limb) {
+  return limb ? sizeof(LineSmem<true>) + sizeof(TW<true>) * (size_t) (nr * ng - 1)
+              : sizeof(LineSmem<false>) + sizeof(TW<false>) * (size_t) (nr * ng - 1);
+}
+size_t hist_smem_bytes(int nr, int ng) { return sizeof(HistSmem) + sizeof(float4) * (size_t) (nr * ng - 1); }
 
-cudaError_t relline_set_smem(size_t bytes) {
-  cudaError_t e = cudaFuncSetAttribute(relline_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+cudaError_t relline_set_smem(size_t bytes_nolimb, size_t bytes_limb, size_t bytes_hist) {
+  cudaError_t e = cudaFuncSetAttribute(relline_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int) bytes_nolimb);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(relline_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+  e = cudaFuncSetAttribute(relline_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes_limb);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes_hist);
 }
 
-cudaError_t launch_relline(bool hist, dim3 grid, size_t smem, cudaStream_t s, const RelxTables &tab,
-                           const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
-                           int nza, float *prof, float *dist, double *tsum, int ntile_max) {
-  if (hist)
-    relline_kernel<true><<<grid, kLineThreads, smem, s>>>(tab, sin, sst, srad, line_e, nza, prof, dist, tsum, ntile_max);
-  else
-    relline_kernel<false><<<grid, kLineThreads, smem, s>>>(tab, sin, sst, srad, line_e, nza, prof, dist, tsum, ntile_max);
+// launches the line profile (both variants: a set runs in the one matching its limb law) and,
+// for relxill models, the emission-angle histogram
+cudaError_t launch_relline(bool hist, dim3 grid, cudaStream_t s, const RelxTables &tab, const RelxSetIn *sin,
+                           const RelxSetState *sst, const RelxRadial *srad, const double *line_e, int nza, float *prof,
+                           float *dist, double *tsum, int ntile_max, bool any_limb) {
+  relline_kernel<false><<<grid, kLineThreads, line_smem_bytes(tab.rel_nr, tab.rel_ng, false), s>>>(
+      tab, sin, sst, srad, line_e, nza, prof, tsum, ntile_max);
+  if (any_limb)
+    relline_kernel<true><<<grid, kLineThreads, line_smem_bytes(tab.rel_nr, tab.rel_ng, true), s>>>(
+        tab, sin, sst, srad, line_e, nza, prof, tsum, ntile_max);
+  if (hist) hist_kernel<<<grid.y, kLineThreads, hist_smem_bytes(tab.rel_nr, tab.rel_ng), s>>>(tab, sst, srad, nza, dist);
   return cudaGetLastError();
 }
 

@@ -81,8 +81,11 @@ struct RelxTables {
   const float *conv_inv_emid;  // 1/(0.5(e_j+e_j+1))
   const float *conv_cf;      // 0.5(e_j+e_j+1)/(e_j+1-e_j)  (Relbase.cpp:93-103)
   int conv_pos1;             // binary_search(conv_e, 1.0)  (Relbase.cpp:133-137)
+  float conv_lg0, conv_ilg;  // log(conv_e[0]) and N / log(conv_e[N] / conv_e[0]): first guess of a bin index
   int conv_band_lo, conv_band_hi;  // bins with e_j >= 0.01 && e_j+1 < 1000 (Relbase.cpp:205)
   const double *coarse_e;    // [RELX_NCOARSE+1]
+  const float4 *coarse_t;    // per coarse bin: (float) centre, (float) width, centre as float-float; zero
+                             // centre weight outside [RELX_EMIN_NORM, RELX_EMAX_NORM] (Xillspec.cpp:185-190)
   // rebin map xillver grid -> conv grid (relutility.c:549-601): per conv bin
   const int *rb_imin, *rb_imax;
   const float *rb_fmin, *rb_fmax;  // fractions (single-bin case: rb_fmin, rb_imax == rb_imin)
@@ -108,37 +111,39 @@ struct RelxSetState {
   int ind_a, ind_mu0;
   float ifac_a, ifac_mu0;
   int ucount;       // unique xillver corners (dense mode)
-  int pad_;
+  int out_lo, out_hi;  // conv-grid bins the caller's grid needs (inclusive)
   double a, incl, rin, rout, height, beta, gamma, z, lineE;
   double gam, ect_src, refl_frac;
   double relline_norm;   // renormalisation target; <= 0 means no renormalisation
   double g_inf, f_inf_rest, refl_frac_lp, prim_fac, norm_fac_refl, src_norm;
   double rgrid[RELX_NZMAX + 1];
   int zi0[RELX_NZMAX], zi1[RELX_NZMAX];   // fine-radius index range of each zone (inclusive)
+  int zw_lo[RELX_NZMAX], zw_hi[RELX_NZMAX]; // line-profile bins touched by the zone's radii [lo, hi)
   float inv_nc[RELX_NZMAX];               // 1 / normalisation change source->disk (Xillspec.cpp:408-440)
 };
 
-// per-set radial data [RELX_NFRAD] (written by setup, read by the line-profile kernel)
-struct RelxRadial {
-  double re[RELX_NFRAD];
-  double gmin[RELX_NFRAD];
-  double gmax[RELX_NFRAD];
-  double ifac[RELX_NFRAD];
-  float  ew[RELX_NFRAD];      // emissivity * trapez weight / 2
-  float  emis[RELX_NFRAD];
-  float  wt[RELX_NFRAD];
-  float2 gmin_ff[RELX_NFRAD]; // gmin, gmax, gmax-gmin as float-float (hi, lo)
-  float2 gmax_ff[RELX_NFRAD];
-  float2 dg_ff[RELX_NFRAD];
-  float2 eH_ff[RELX_NFRAD];   // gstar2ener(H), gstar2ener(1-H) (relutility.c:260-262)
-  float2 e1H_ff[RELX_NFRAD];
-  float  inv_dg[RELX_NFRAD];  // 1/(gmax-gmin)
-  int    ielo[RELX_NFRAD];    // first line-profile bin touched by the radius (-1: none)
-  int    iehi[RELX_NFRAD];    // last line-profile bin touched
-  short  itab[RELX_NFRAD];    // table radius index: re_tab[itab+1] <= re < re_tab[itab]
-  unsigned char zone[RELX_NFRAD];
-  unsigned char red_H[RELX_NFRAD];  // gstar2ener(H) >= 0.95 (int_romb, Relprofile.cpp:636)
+// per-radius record of the line-profile kernels (64 bytes, staged into shared memory as int4 rows)
+struct __align__(16) RelxRadRec {
+  float2 gmin, gmax, dg;  // float-float gmin, gmax, gmax - gmin
+  float2 eH, e1H;         // gstar2ener(H), gstar2ener(1-H) (relutility.c:260-262)
+  float inv_dg;           // 1/(gmax-gmin)
+  float ew;               // emissivity * trapez weight / 2
+  float ifac;             // radial interpolation factor of the table
+  int ielo, iehi;         // line-profile bins touched (-1: none)
+  short itab;             // table radius index: re_tab[itab+1] <= re < re_tab[itab]
+  unsigned char red_H;    // gstar2ener(H) >= 0.95 (int_romb, Relprofile.cpp:636)
+  unsigned char zone;
 };
+static_assert(sizeof(RelxRadRec) == 64, "radius record is four int4 rows");
+
+// per-set radial data [RELX_NFRAD] (written by setup, read by the line-profile kernels)
+struct RelxRadial {
+  RelxRadRec rec[RELX_NFRAD];
+  double re[RELX_NFRAD];
+  double ifac[RELX_NFRAD];    // FP64 radial factor (emission-angle bin decisions near bin edges)
+  float  wt[RELX_NFRAD];      // trapez weight / 2
+};
+static_assert(sizeof(RelxRadial) % 16 == 0, "per-set radial records stay 16-byte aligned");
 
 // xillver corners of one set (dense mode: de-duplicated across zones)
 struct RelxCorners {

@@ -22,6 +22,43 @@ __device__ __forceinline__ int bsearch_asc(const T *arr, int n, T val) {
   }
   return klo;
 }
+// index k of the log conv grid with ge[k] <= e < ge[k+1] (clamped to [0, N-1]), as
+// binary_search would return it: a first guess from the logarithm, then exact comparisons
+__device__ __forceinline__ int conv_index(const RelxTables &tab, double e) {
+  const double *ge = tab.conv_e;
+  const float2 *gf = tab.conv_eff;  // .x = (float) ge
+  const float ef = (float) e;
+  int k = (int) floorf((__logf(ef) - tab.conv_lg0) * tab.conv_ilg);
+  k = max(0, min(k, RELX_NCONV - 1));
+  // ge[k] > e, decided in float unless the float values tie
+  while (k > 0 && (gf[k].x > ef || (gf[k].x == ef && ge[k] > e))) k--;
+  while (k < RELX_NCONV - 1 && (gf[k + 1].x < ef || (gf[k + 1].x == ef && ge[k + 1] <= e))) k++;
+  return k;
+}
+
+// Searches over FP64 arrays guided by float copies.  Rounding to float is monotone, so a strict
+// float comparison decides the FP64 one; only float ties are compared in FP64 (FP64 compares
+// share the narrow FP64 pipe).
+// number of entries of the descending array a that are > v
+__device__ __forceinline__ int count_gt_desc(const double *a, const float *af, int n, double v, float vf) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int k = (lo + hi) >> 1;
+    if (af[k] > vf) lo = k + 1; else hi = k;
+  }
+  while (lo < n && af[lo] == vf && a[lo] > v) lo++;
+  return lo;
+}
+// bsearch_asc (largest k in [0, n-2] with a[k] <= v, 0 below the range) of an ascending array
+__device__ __forceinline__ int bsearch_asc_exact(const double *a, const float *af, int n, double v, float vf) {
+  int lo = 0, hi = n;  // count of entries < v in float
+  while (lo < hi) {
+    const int k = (lo + hi) >> 1;
+    if (af[k] < vf) lo = k + 1; else hi = k;
+  }
+  while (lo < n && af[lo] == vf && a[lo] <= v) lo++;  // lo = count of entries <= v
+  return max(0, min(lo - 1, n - 2));
+}
 // descending arr (inv_binary_search, relutility.c:195-211)
 __device__ __forceinline__ int bsearch_desc(const double *arr, int n, double val) {
   int klo = 0, khi = n - 1;
@@ -88,6 +125,70 @@ __device__ __forceinline__ float ff_sub_to_float(float2 a, float2 b) {
   float bb = __fsub_rn(s, a.x);
   float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(-b.x, bb));  // two-sum error
   return __fadd_rn(s, __fadd_rn(err, __fsub_rn(a.y, b.y)));
+}
+
+// ---- float-float arithmetic on the FP32 pipe (FP64 runs at 1/64 of the FP32 rate on this part)
+__device__ __forceinline__ float2 two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return make_float2(s, e);
+}
+__device__ __forceinline__ float2 qts(float a, float b) {
+  float s = __fadd_rn(a, b);
+  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+  float2 s = two_sum(a.x, b.x);
+  return qts(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
+}
+__device__ __forceinline__ float2 ff_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+  float p = __fmul_rn(a.x, b.x);
+  float e = fmaf(a.x, b.x, -p);
+  e = __fadd_rn(e, __fadd_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+  return qts(p, e);
+}
+__device__ __forceinline__ float2 ff_mulf(float2 a, float b) {
+  float p = __fmul_rn(a.x, b);
+  float e = fmaf(a.x, b, -p);
+  e = __fadd_rn(e, __fmul_rn(a.y, b));
+  return qts(p, e);
+}
+__device__ __forceinline__ bool ff_ge(float2 a, float2 b) {
+  float2 d = ff_add(a, ff_neg(b));
+  return d.x > 0.0f || (d.x == 0.0f && d.y >= 0.0f);
+}
+
+__device__ __forceinline__ float2 ff_addf(float2 a, float b) {
+  float2 s = two_sum(a.x, b);
+  return qts(s.x, __fadd_rn(s.y, a.y));
+}
+__device__ __forceinline__ double ff_to_double(float2 a) { return (double) a.x + (double) a.y; }
+
+// block-wide float-float sum with a fixed reduction tree (deterministic); scratch holds NT/32 + 1
+template <int NT>
+__device__ __forceinline__ float2 block_sum_ff(float2 v, float2 *scratch) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    float2 t;
+    t.x = __shfl_xor_sync(0xffffffffu, v.x, o);
+    t.y = __shfl_xor_sync(0xffffffffu, v.y, o);
+    v = ff_add(v, t);
+  }
+  __syncthreads();
+  if (lane == 0) scratch[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float2 r = make_float2(0.0f, 0.0f);
+    for (int i = 0; i < NT / 32; i++) r = ff_add(r, scratch[i]);
+    scratch[NT / 32] = r;
+  }
+  __syncthreads();
+  const float2 r = scratch[NT / 32];
+  __syncthreads();
+  return r;
 }
 
 // block-wide sum in FP64 with a fixed reduction tree (deterministic)

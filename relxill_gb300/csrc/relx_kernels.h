@@ -13,9 +13,11 @@ constexpr int kLineTileH = 512;
 constexpr int kXillThreadsH = 256;
 constexpr int kXillTileH = 1024;
 constexpr int kConvThreadsH = 256;
+constexpr int kFinThreadsH = 128;
 
 size_t setup_smem_bytes();
-size_t line_smem_bytes(int nr, int ng);
+size_t line_smem_bytes(int nr, int ng, bool limb);
+size_t hist_smem_bytes(int nr, int ng);
 size_t xill_smem_bytes(int n_incl);
 size_t conv_smem_bytes();
 size_t fin_smem_bytes();
@@ -23,10 +25,10 @@ size_t fin_smem_bytes();
 __global__ void setup_kernel(RelxTables tab, int model, const RelxSetIn *sin, const double *user_e, double *line_e,
                              RelxSetState *sout, RelxRadial *rout, RelxCorners *cout, RelxZoneCorners *zcout);
 
-cudaError_t relline_set_smem(size_t bytes);
-cudaError_t launch_relline(bool hist, dim3 grid, size_t smem, cudaStream_t s, const RelxTables &tab,
-                           const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
-                           int nza, float *prof, float *dist, double *tsum, int ntile_max);
+cudaError_t relline_set_smem(size_t bytes_nolimb, size_t bytes_limb, size_t bytes_hist);
+cudaError_t launch_relline(bool hist, dim3 grid, cudaStream_t s, const RelxTables &tab, const RelxSetIn *sin,
+                           const RelxSetState *sst, const RelxRadial *srad, const double *line_e, int nza, float *prof,
+                           float *dist, double *tsum, int ntile_max, bool any_limb);
 
 __global__ void xillver_dense_kernel(RelxTables tab, const RelxSetState *sst, const RelxCorners *scor,
                                      const float *dist_raw, int nza, float *xout, int *err);

@@ -78,14 +78,14 @@ struct Tables {
   DevBuf rel_a, rel_mu0, rel_r, rel_gmin, rel_gmax, rel_tc;
   DevBuf lp_a, lp_h, lp_rad, lp_intens, lp_del, lp_delinc;
   DevBuf x_vals, x_spec, x_e;
-  DevBuf conv_e, conv_eff, conv_inv_emid, conv_cf, coarse_e;
+  DevBuf conv_e, conv_eff, conv_inv_emid, conv_cf, coarse_e, coarse_t;
   DevBuf rb_imin, rb_imax, rb_fmin, rb_fmax;
   size_t bytes_total = 0;
   bool loaded = false;
   void release() {
     for (DevBuf *b : {&rel_a, &rel_mu0, &rel_r, &rel_gmin, &rel_gmax, &rel_tc, &lp_a, &lp_h, &lp_rad, &lp_intens,
                       &lp_del, &lp_delinc, &x_vals, &x_spec, &x_e, &conv_e, &conv_eff, &conv_inv_emid, &conv_cf,
-                      &coarse_e, &rb_imin, &rb_imax, &rb_fmin, &rb_fmax})
+                      &coarse_e, &coarse_t, &rb_imin, &rb_imax, &rb_fmin, &rb_fmax})
       b->release();
     loaded = false;
   }
@@ -347,11 +347,18 @@ static int load_tables(const std::string &dir, Tables &T) {
   }
   std::vector<double> co;
   log_grid(co, RELX_NCOARSE + 1, RELX_EMIN_NORM, RELX_EMAX_NORM);
+  std::vector<float4> ct(RELX_NCOARSE);
+  for (int b = 0; b < RELX_NCOARSE; b++) {
+    const double em = 0.5 * (co[b] + co[b + 1]);
+    const bool in_band = co[b] >= RELX_EMIN_NORM && co[b] <= RELX_EMAX_NORM;
+    const float hi = (float) em;
+    ct[b] = make_float4(hi, (float) (co[b + 1] - co[b]), in_band ? hi : 0.0f, in_band ? (float) (em - (double) hi) : 0.0f);
+  }
   std::vector<int> imn, imx;
   std::vector<float> fmn, fmx;
   rebin_map(ce, xe, imn, imx, fmn, fmx);
   if ((st = upload(T.conv_e, ce)) || (st = upload(T.conv_eff, ceff)) || (st = upload(T.conv_inv_emid, inv_emid)) ||
-      (st = upload(T.conv_cf, cf)) || (st = upload(T.coarse_e, co)) || (st = upload(T.rb_imin, imn)) ||
+      (st = upload(T.conv_cf, cf)) || (st = upload(T.coarse_e, co)) || (st = upload(T.coarse_t, ct)) || (st = upload(T.rb_imin, imn)) ||
       (st = upload(T.rb_imax, imx)) || (st = upload(T.rb_fmin, fmn)) || (st = upload(T.rb_fmax, fmx)))
     return st;
   T.d.conv_e = T.conv_e.as<double>();
@@ -359,9 +366,12 @@ static int load_tables(const std::string &dir, Tables &T) {
   T.d.conv_inv_emid = T.conv_inv_emid.as<float>();
   T.d.conv_cf = T.conv_cf.as<float>();
   T.d.conv_pos1 = pos1;
+  T.d.conv_lg0 = (float) std::log(RELX_EMIN_CONV);
+  T.d.conv_ilg = (float) (RELX_NCONV / std::log(RELX_EMAX_CONV / RELX_EMIN_CONV));
   T.d.conv_band_lo = band_lo;
   T.d.conv_band_hi = band_hi;
   T.d.coarse_e = T.coarse_e.as<double>();
+  T.d.coarse_t = T.coarse_t.as<float4>();
   T.d.rb_imin = T.rb_imin.as<int>();
   T.d.rb_imax = T.rb_imax.as<int>();
   T.d.rb_fmin = T.rb_fmin.as<float>();
@@ -436,8 +446,8 @@ static Context &ctx() {
 
 static int set_kernel_attrs(const Tables &T) {
   RELX_CUDA(cudaFuncSetAttribute(setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) setup_smem_bytes()));
-  size_t ls = line_smem_bytes(T.d.rel_nr, T.d.rel_ng);
-  RELX_CUDA(relline_set_smem(ls));
+  RELX_CUDA(relline_set_smem(line_smem_bytes(T.d.rel_nr, T.d.rel_ng, false), line_smem_bytes(T.d.rel_nr, T.d.rel_ng, true),
+                             hist_smem_bytes(T.d.rel_nr, T.d.rel_ng)));
   RELX_CUDA(cudaFuncSetAttribute(xillver_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int) xill_smem_bytes(T.d.x_nincl)));
   RELX_CUDA(cudaFuncSetAttribute(conv_zone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
@@ -545,6 +555,7 @@ static int prof_collect() {
 
 struct BatchShape {
   int model, n_sets, nza, ntile_max;
+  bool any_limb = false;  // some set uses a limb-darkening law (relline / relconv limb parameter)
   int64_t n_edges;  // total energy edges
 };
 
@@ -595,12 +606,11 @@ static int launch_batch(Context &C, const BatchShape &b, cudaStream_t s) {
     setup_kernel<<<S, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, b.model, sin, W.user_e.as<double>(),
                                                                W.line_e.as<double>(), sst, rad, cor, zcor);
   }
-  const size_t ls = line_smem_bytes(tab.rel_nr, tab.rel_ng);
   dim3 lg(b.ntile_max, S);
   {
     ProfScope ps(PK_LINE, s);
-    RELX_CUDA(launch_relline(b.model >= RELX_RELXILL, lg, ls, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza,
-                             W.prof.as<float>(), W.dist.as<float>(), W.tsum.as<double>(), b.ntile_max));
+    RELX_CUDA(launch_relline(b.model >= RELX_RELXILL, lg, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza,
+                             W.prof.as<float>(), W.dist.as<float>(), W.tsum.as<double>(), b.ntile_max, b.any_limb));
   }
   if (b.model >= RELX_RELXILL) {
     const int nxt = (tab.x_nener_pad + kXillTileH - 1) / kXillTileH;
@@ -621,7 +631,7 @@ static int launch_batch(Context &C, const BatchShape &b, cudaStream_t s) {
     }
     {
       ProfScope ps(PK_FIN, s);
-      finalize_relxill_kernel<<<S, kConvThreadsH, fin_smem_bytes(), s>>>(tab, sin, sst, W.cout.as<float>(), b.nza,
+      finalize_relxill_kernel<<<S, kFinThreadsH, fin_smem_bytes(), s>>>(tab, sin, sst, W.cout.as<float>(), b.nza,
                                                                          W.user_e.as<double>(), W.flux.as<double>());
     }
   } else if (b.model == RELX_RELCONV) {
@@ -629,11 +639,11 @@ static int launch_batch(Context &C, const BatchShape &b, cudaStream_t s) {
     relconv_conv_kernel<<<S, kConvThreadsH, conv_smem_bytes(), s>>>(
         tab, sin, sst, W.prof.as<float>(), W.tsum.as<double>(), b.ntile_max, kLineTileH, b.nza, W.user_e.as<double>(),
         W.user_f.as<double>(), W.cout.as<float>(), W.sflag.as<int>());
-    finalize_relconv_kernel<<<S, kConvThreadsH, 0, s>>>(tab, sin, sst, W.cout.as<float>(), b.nza,
+    finalize_relconv_kernel<<<S, kFinThreadsH, 0, s>>>(tab, sin, sst, W.cout.as<float>(), b.nza,
                                                         W.user_e.as<double>(), W.sflag.as<int>(), W.flux.as<double>());
   } else {
     ProfScope ps(PK_FIN, s);
-    finalize_relline_kernel<<<S, kConvThreadsH, 0, s>>>(sin, sst, W.prof.as<float>(), W.tsum.as<double>(),
+    finalize_relline_kernel<<<S, kFinThreadsH, 0, s>>>(sin, sst, W.prof.as<float>(), W.tsum.as<double>(),
                                                         b.ntile_max, kLineTileH, b.nza, W.flux.as<double>());
   }
   {
@@ -657,6 +667,7 @@ static int batch_shape(int model, int n_sets, const int64_t *eoff_host, const in
     nza = std::max(nza, zones_for(model, igt_host ? igt_host[i] : 0, env.nzones_env));
   }
   b->nza = nza;
+  b->any_limb = (model == RELX_RELLINE || model == RELX_RELCONV);
   const int gmax = (model == RELX_RELLINE) ? maxn : RELX_NCONV;
   b->ntile_max = (gmax + kLineTileH - 1) / kLineTileH;
   *need_zc = nza > RELX_ZDENSE;

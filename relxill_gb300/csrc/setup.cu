@@ -22,10 +22,20 @@ struct SetupSmem {
   RelxSetState s;
   double re_tab[RELX_MAX_NRTAB], gmin_t[RELX_MAX_NRTAB], gmax_t[RELX_MAX_NRTAB];
   double re[RELX_NFRAD], emis[RELX_NFRAD], del_emit[RELX_NFRAD], del_inc[RELX_NFRAD];
+  double sqre[RELX_NFRAD];   // 1/u of the fine grid, i.e. sqrt(re)
+  double inv_dtab[RELX_MAX_NRTAB];
+  float re_tab_f[RELX_MAX_NRTAB];    // float copies guide the searches; FP64 decides float ties only
+  float jet_rad_f[RELX_MAX_NRADLP], rgrid_f[RELX_NZMAX + 1];
+  float lp_dle[RELX_MAX_NRADLP], lp_dlr[RELX_MAX_NRADLP], lp_d[RELX_MAX_NRADLP], lp_di[RELX_MAX_NRADLP];
+  double inv_jr[RELX_MAX_NRADLP];
+  unsigned char lp_log[RELX_MAX_NRADLP];  // logarithmic radial factor (emission angle above 75 deg)
+  double qsum[RELX_NZMAX + 1];       // normalisation sums of the primary continuum
+  double e_tab[RELX_MAX_NRADLP], inv_drad[RELX_MAX_NRADLP];
   double jet_rad[RELX_MAX_NRADLP], le_tab[RELX_MAX_NRADLP], lrad[RELX_MAX_NRADLP];
   double d_tab[RELX_MAX_NRADLP], di_tab[RELX_MAX_NRADLP];
   double red[40];
   int ired[40];
+  int zlo[RELX_NZMAX], zhi[RELX_NZMAX];  // per-zone profile windows (inclusive bins)
   int ind_rmin, ind_rmax, status;
   // parameters beyond the state
   double emis1, emis2, rbr, htop, lxi, afe, dens, iongrad_index;
@@ -189,11 +199,6 @@ __device__ double rebin_mean_at(const double *x0, const double *y0, int n0, doub
   return lerp1(f, y0[ii + 1], y0[ii]);
 }
 
-// spec_cutoffpl term (Xillspec.cpp:215-233) on one bin, FP32 arithmetic
-__device__ __forceinline__ float cutoffpl_term(double elo, double ehi, float ecut, float gam) {
-  float en = (float) (0.5 * (elo + ehi));
-  return expf(1.0f / ecut) * powf(en, -gam) * expf(-en / ecut) * (float) (ehi - elo);
-}
 
 __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, int model, const RelxSetIn *__restrict__ sin,
                                                                const double *__restrict__ user_e, double *__restrict__ line_e,
@@ -211,6 +216,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     map_params(model, in, m);
     m.status = s.status;
   }
+  for (int z = tid; z < RELX_NZMAX; z += kSetupThreads) { m.zlo[z] = 1 << 30; m.zhi[z] = -1; }
   __syncthreads();
   if (m.status != RELX_OK) {
     if (tid == 0) { s.win_lo = 0; s.win_hi = 0; s.nz = 0; sout[set] = s; }
@@ -266,8 +272,9 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     const double r1 = 1.0 / sqrt(s.rout), r2 = 1.0 / sqrt(s.rin);
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
       double u = ((double) ii) * (r2 - r1) / (NR - 1) + r1;
-      double iu = 1.0 / u;
+      double iu = __drcp_rn(u);
       m.re[ii] = iu * iu;
+      m.sqre[ii] = iu;
     }
   }
   __syncthreads();
@@ -279,69 +286,84 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     if (m.re_tab[m.ind_rmax] < 1000.0 && m.re_tab[m.ind_rmax] * 1.01 > 1000.0) m.re_tab[m.ind_rmax] = 1000.0;
   }
   __syncthreads();
+  for (int i = tid; i < nr - 1; i += kSetupThreads) m.inv_dtab[i] = 1.0 / (m.re_tab[i] - m.re_tab[i + 1]);
+  for (int i = tid; i < nr; i += kSetupThreads) m.re_tab_f[i] = (float) m.re_tab[i];
+  for (int i = tid; i <= s.nz; i += kSetupThreads) m.rgrid_f[i] = (float) s.rgrid[i];
+  __syncthreads();
 
   RelxRadial &R = rout[set];
   // ---- per fine radius: table radius, interpolation factor, gmin/gmax, weight, zone, bin range
   int my_lo = 1 << 30, my_hi = -1;
   for (int ii = tid; ii < NR; ii += kSetupThreads) {
     double r = m.re[ii];
+    const float rf = (float) r;
     // index ind with re_tab[ind+1] <= r < re_tab[ind], as the walk of Relprofile.cpp:252-266
-    int lo = 0, hi = nr;  // count of table radii > r
-    while (lo < hi) {
-      int k = (lo + hi) >> 1;
-      if (m.re_tab[k] > r) lo = k + 1; else hi = k;
-    }
+    const int lo = count_gt_desc(m.re_tab, m.re_tab_f, nr, r, rf);  // count of table radii > r
     int ind = lo - 1;
     if (ind > m.ind_rmin) ind = m.ind_rmin;
     if (ind < 0) {
       if (r - RELX_RELTABLE_MAX_R <= 1e-6) ind = 0; else atomicExch(&m.status, RELX_ERR_GRID);
     }
     if (ind < 0) ind = 0;
-    double ifac = (r - m.re_tab[ind + 1]) / (m.re_tab[ind] - m.re_tab[ind + 1]);
+    double ifac = (r - m.re_tab[ind + 1]) * m.inv_dtab[ind];
     if (ifac > 1.0 && ind > 0) atomicExch(&m.status, RELX_ERR_GRID);
     double gmn = lerp1(ifac, m.gmin_t[ind + 1], m.gmin_t[ind]);
     double gmx = lerp1(ifac, m.gmax_t[ind + 1], m.gmax_t[ind]);
     R.re[ii] = r;
     R.ifac[ii] = ifac;
-    R.gmin[ii] = gmn;
-    R.gmax[ii] = gmx;
-    R.gmin_ff[ii] = ff_from_double(gmn);
-    R.gmax_ff[ii] = ff_from_double(gmx);
-    R.dg_ff[ii] = ff_from_double(gmx - gmn);
-    R.inv_dg[ii] = (float) (1. / (gmx - gmn));
+    RelxRadRec rr;
+    rr.gmin = ff_from_double(gmn);
+    rr.gmax = ff_from_double(gmx);
+    rr.dg = ff_from_double(gmx - gmn);
+    rr.inv_dg = 1.0f / (float) (gmx - gmn);
     {
       double eh = RELX_GFAC_H * (gmx - gmn) + gmn;
-      R.eH_ff[ii] = ff_from_double(eh);
-      R.e1H_ff[ii] = ff_from_double((1 - RELX_GFAC_H) * (gmx - gmn) + gmn);
-      R.red_H[ii] = eh >= 0.95 ? 1 : 0;
+      rr.eH = ff_from_double(eh);
+      rr.e1H = ff_from_double((1 - RELX_GFAC_H) * (gmx - gmn) + gmn);
+      rr.red_H = eh >= 0.95 ? 1 : 0;
     }
-    R.itab[ii] = (short) ind;
+    rr.itab = (short) ind;
+    rr.ifac = (float) ifac;
+    rr.ew = 0.0f;  // set with the emissivity below
     // trapez_integ_single / 2 (relutility.c:233-244)
     double dr;
     if (ii == 0) dr = 0.5 * (m.re[0] - m.re[1]);
     else if (ii == NR - 1) dr = 0.5 * (m.re[ii - 1] - m.re[ii]);
     else dr = 0.5 * (m.re[ii - 1] - m.re[ii + 1]);
     R.wt[ii] = (float) (r * dr * kPi / 2);
-    R.zone[ii] = (unsigned char) bsearch_asc<double>(s.rgrid, s.nz + 1, r);
+    rr.zone = (unsigned char) bsearch_asc_exact(s.rgrid, m.rgrid_f, s.nz + 1, r, rf);
     // bins of the line-profile grid touched by this radius (Relprofile.cpp:863-878)
     int ielo = -1, iehi = -1;
     double egmin = gmn, egmax = gmx;
     if (egmax > ge[0] && egmin < ge[gn]) {
       if (egmin < ge[0]) egmin = ge[0];
       if (egmax > ge[gn]) egmax = ge[gn];
-      ielo = bsearch_asc<double>(ge, gn + 1, egmin);
-      iehi = bsearch_asc<double>(ge, gn + 1, egmax);
+      if (model == RELX_RELLINE) {
+        ielo = bsearch_asc<double>(ge, gn + 1, egmin);
+        iehi = bsearch_asc<double>(ge, gn + 1, egmax);
+      } else {
+        ielo = conv_index(tab, egmin);
+        iehi = conv_index(tab, egmax);
+      }
       my_lo = min(my_lo, ielo);
       my_hi = max(my_hi, iehi);
+      atomicMin(&m.zlo[rr.zone], ielo);
+      atomicMax(&m.zhi[rr.zone], iehi);
     }
-    R.ielo[ii] = ielo;
-    R.iehi[ii] = iehi;
+    rr.ielo = ielo;
+    rr.iehi = iehi;
+    R.rec[ii] = rr;
   }
   int wlo = block_min_i<kSetupThreads>(my_lo, m.ired);
   int whi = block_max_i<kSetupThreads>(my_hi, m.ired);
   if (tid == 0) {
     s.win_lo = (whi >= 0) ? wlo : 0;
     s.win_hi = (whi >= 0) ? whi + 1 : 0;
+  }
+  for (int z = tid; z < s.nz; z += kSetupThreads) {
+    // profile bins outside a zone's window stay exactly zero
+    s.zw_lo[z] = (m.zhi[z] >= 0) ? m.zlo[z] : s.win_lo;
+    s.zw_hi[z] = (m.zhi[z] >= 0) ? m.zhi[z] + 1 : s.win_lo;
   }
 
   // ---- emissivity
@@ -397,21 +419,41 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
             + fa * lerp1(f1, TV(tab.lp_delinc, 1, h1), TV(tab.lp_delinc, 1, h1 + 1));
 #undef TV
         m.le_tab[k] = log(e);
+        m.e_tab[k] = e;
         m.lrad[k] = log(m.jet_rad[k]);
       }
+    }
+    __syncthreads();
+    for (int k = tid; k < nrad; k += kSetupThreads) {
+      if (k < nrad - 1) {
+        m.inv_drad[k] = 1.0 / (m.jet_rad[k + 1] - m.jet_rad[k]);
+        m.lp_dle[k] = (float) (m.le_tab[k + 1] - m.le_tab[k]);
+        m.lp_dlr[k] = (float) (m.lrad[k + 1] - m.lrad[k]);
+      }
+      m.jet_rad_f[k] = (float) m.jet_rad[k];
+      m.inv_jr[k] = 1.0 / m.jet_rad[k];
+      m.lp_d[k] = (float) m.d_tab[k];
+      m.lp_di[k] = (float) m.di_tab[k];
+      m.lp_log[k] = (m.d_tab[k] / kPi * 180.0 <= 75.0) ? 0 : 1;
     }
     __syncthreads();
     // rebin_emisprofile_on_radial_grid (Rellp.cpp:120-175)
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
       double r = m.re[ii];
-      int kk = bsearch_asc<double>(m.jet_rad, nrad, r);
+      int kk = bsearch_asc_exact(m.jet_rad, m.jet_rad_f, nrad, r, (float) r);
       if (r >= m.jet_rad[nrad - 1] && r - RELX_RELTABLE_MAX_R > 1e-6) atomicExch(&m.status, RELX_ERR_GRID);
-      double inter;
-      if (m.d_tab[kk] / kPi * 180.0 <= 75.0) inter = (r - m.jet_rad[kk]) / (m.jet_rad[kk + 1] - m.jet_rad[kk]);
-      else inter = (log(r) - m.lrad[kk]) / (m.lrad[kk + 1] - m.lrad[kk]);
-      m.emis[ii] = exp(inter * m.le_tab[kk + 1] + (1.0 - inter) * m.le_tab[kk]);
-      m.del_emit[ii] = lerp1(inter, m.d_tab[kk], m.d_tab[kk + 1]);
-      m.del_inc[ii] = lerp1(inter, m.di_tab[kk], m.di_tab[kk + 1]);
+      // get_ipol_factor_radius (relutility.c:407-417); r - rlo in FP64, the rest in FP32
+      const double dr = r - m.jet_rad[kk];
+      float inter;
+      if (!m.lp_log[kk]) {
+        inter = (float) (dr * m.inv_drad[kk]);
+      } else {
+        inter = log1pf((float) (dr * m.inv_jr[kk])) / m.lp_dlr[kk];
+      }
+      // interp_log_1d (relutility.c:41-43) as e_lo * exp(inter * (log e_hi - log e_lo))
+      m.emis[ii] = m.e_tab[kk] * (double) expf(inter * m.lp_dle[kk]);
+      m.del_emit[ii] = (double) (inter * m.lp_d[kk + 1] + (1.0f - inter) * m.lp_d[kk]);
+      m.del_inc[ii] = (double) (inter * m.lp_di[kk + 1] + (1.0f - inter) * m.lp_di[kk]);
     }
     __syncthreads();
     if (tid == 0) {
@@ -429,32 +471,53 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       double f_inf = (s.beta > 1e-6) ? 0.5 * (1.0 + cos(relat_abberation(ad_max, -1. * s.beta))) : s.f_inf_rest;
       s.refl_frac_lp = f_ad / f_inf;
     }
-    // apply_emis_fluxboost_source_disk (Rellp.cpp:249-253, Relphysics.cpp:301-311)
+    // apply_emis_fluxboost_source_disk (Rellp.cpp:249-253, Relphysics.cpp:301-311).  gi_potential_lp
+    // with sqrt(r) = 1/u of the fine grid; r^2 - 3r + 2a sqrt(r) cancels near the ISCO and stays FP64.
+    const double hh = s.height, aa = s.a;
+    const float ut_h = (float) sqrt((hh * hh + aa * aa) / (hh * hh - 2 * hh + aa * aa));
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
-      double gi = gi_potential_lp(m.re[ii], s.a, s.height, s.beta, m.del_emit[ii]);
-      double boost = pow(gi, s.gamma);
+      const double r = m.re[ii], sr = m.sqre[ii];
+      const double t = r * r - 3 * r + 2 * aa * sr;
+      const float ut_d = (float) (r * sr + aa) / ((float) sr * sqrtf((float) t));
+      float gi = ut_d / ut_h;
+      if (fabs(s.beta) >= 1e-6) gi = (float) gi_potential_lp(r, aa, hh, s.beta, m.del_emit[ii]);
+      float boost = powf(gi, (float) s.gamma);
       if (s.beta > 1e-6) {
-        double d = doppler_factor(m.del_emit[ii], s.beta);
+        float d = (float) doppler_factor(m.del_emit[ii], s.beta);
         boost *= d * d;
       }
-      m.emis[ii] *= boost;
+      m.emis[ii] *= (double) boost;
     }
   }
   __syncthreads();
   for (int ii = tid; ii < NR; ii += kSetupThreads) {
-    R.emis[ii] = (float) m.emis[ii];
-    R.ew[ii] = (float) (m.emis[ii] * (double) R.wt[ii]);
+    R.rec[ii].ew = (float) (m.emis[ii] * (double) R.wt[ii]);
   }
 
   // ---- zones: fine-radius index ranges (zone is non-increasing with the radius index)
-  if (tid == 0) {
-    for (int z = 0; z < s.nz; z++) { s.zi0[z] = 1; s.zi1[z] = 0; }
-    int cur = -1;
-    for (int ii = 0; ii < NR; ii++) {
-      int z = R.zone[ii];
-      if (z != cur) { s.zi0[z] = ii; cur = z; }
-      s.zi1[z] = ii;
+  for (int z = tid; z < s.nz; z += kSetupThreads) { s.zi0[z] = 1; s.zi1[z] = 0; }
+  __syncthreads();
+  for (int ii = tid; ii < NR; ii += kSetupThreads) {
+    const int z = R.rec[ii].zone;
+    if (ii == 0 || R.rec[ii - 1].zone != z) s.zi0[z] = ii;
+    if (ii == NR - 1 || R.rec[ii + 1].zone != z) s.zi1[z] = ii;
+  }
+  __syncthreads();
+  // conv-grid bins the final rebin to the caller's grid reads (Relxill.cpp:267-278, Relbase.cpp:281-284)
+  if (tid == 0 && model != RELX_RELLINE) {
+    const double *ue = user_e + in.e_off;
+    double zf = (model != RELX_RELCONV && s.z > 0) ? (1 + s.z) : 1.0;
+    double elo = ue[0] * zf, ehi = ue[in.n_ener] * zf;
+    const double *ce = tab.conv_e;
+    int lo = bsearch_asc<double>(ce, RELX_NCONV + 1, elo);
+    int hi = bsearch_asc<double>(ce, RELX_NCONV + 1, ehi);
+    if (in.flags & 2) {  // RELXILL_RENORMALIZE reads the bin at 3 keV
+      int k3 = bsearch_asc<double>(ce, RELX_NCONV, 3.0);
+      lo = min(lo, k3);
+      hi = max(hi, k3);
     }
+    s.out_lo = max(0, lo - 1);
+    s.out_hi = min(RELX_NCONV - 1, hi + 1);
   }
   if (!m.is_relxill) {
     __syncthreads();
@@ -535,29 +598,36 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       }
     }
   }
-  // ---- normalisation of the primary continuum (Xillspec.cpp:179-205, 302-332, 408-440)
+  // ---- normalisation of the primary continuum (Xillspec.cpp:179-205, 302-332, 408-440): one warp
+  // per continuum (source, then every zone), float-float sums of FP32 terms times the bin centre
   {
-    const double *ce = tab.coarse_e;
     const float gam = (float) s.gam;
-    for (int q = -1; q < nz; q++) {
-      double shift = (q < 0) ? 1.0 : m.shift[q];
-      if (q >= 0 && shift == 1.0) {
-        if (tid == 0) m.xscale[q] = 1.0;
-        continue;
+    const int lane = tid & 31, warp = tid >> 5;
+    for (int qq = warp; qq <= nz; qq += kSetupThreads / 32) {
+      const double shift = (qq == 0) ? 1.0 : m.shift[qq - 1];
+      if (qq > 0 && shift == 1.0) continue;
+      const float ecut = (float) (s.ect_src * shift);
+      float2 part = make_float2(0.0f, 0.0f);
+      for (int b = lane; b < RELX_NCOARSE; b += 32) {
+        const float4 t = tab.coarse_t[b];  // bin centre, width, centre as float-float (0 outside the band)
+        // spec_cutoffpl term (Xillspec.cpp:215-233), FP32 arithmetic
+        const float term = expf(1.0f / ecut) * powf(t.x, -gam) * expf(-t.x / ecut) * t.y;
+        part = ff_add(part, ff_mulf(make_float2(t.z, t.w), term));
       }
-      float ecut = (float) (s.ect_src * shift);
-      double part = 0.0;
-      for (int b = tid; b < RELX_NCOARSE; b += kSetupThreads) {
-        if (ce[b] >= RELX_EMIN_NORM && ce[b] <= RELX_EMAX_NORM)
-          part += (double) cutoffpl_term(ce[b], ce[b + 1], ecut, gam) * (0.5 * (ce[b] + ce[b + 1]));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        float2 u;
+        u.x = __shfl_xor_sync(0xffffffffu, part.x, o);
+        u.y = __shfl_xor_sync(0xffffffffu, part.y, o);
+        part = ff_add(part, u);
       }
-      double sum = block_sum_d<kSetupThreads>(part, m.red) * 1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi);
-      if (tid == 0) {
-        if (q < 0) s.src_norm = 1.0 / sum;
-        else m.xscale[q] = sum * s.src_norm;  // 1 / (disk factor / source factor)
-      }
-      __syncthreads();
+      if (lane == 0) m.qsum[qq] = ff_to_double(part) * 1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi);
     }
+    __syncthreads();
+    const double src_norm = 1.0 / m.qsum[0];
+    if (tid == 0) s.src_norm = src_norm;
+    for (int z = tid; z < nz; z += kSetupThreads)
+      m.xscale[z] = (m.shift[z] == 1.0) ? 1.0 : m.qsum[z + 1] * src_norm;  // 1 / (disk factor / source factor)
   }
   __syncthreads();
   // ---- the 16 corners of every zone, first-zone density scaling, de-duplication
