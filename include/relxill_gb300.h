@@ -83,6 +83,23 @@ int relx_eval_batch_device(int model, int n_sets, const double *d_params, const 
                            double *d_flux, int *d_status, const int *d_ion_grad_type, const int *h_ion_grad_type,
                            const double *d_iongrad_index, void *stream);
 
+/* One parameter set, device buffers, no device allocation; no counterpart in
+ * the reference.  For callers that must not allocate device memory while they
+ * evaluate (memory owned by another framework's caching allocator, a fixed
+ * memory budget, or a loop where cudaMalloc/cudaFree would stall other
+ * streams).  Intermediate arrays live in one static device array of about
+ * 3 MB shared by all calls: calls whose device work overlaps race on it, so
+ * issue them on one stream or synchronise between them.  The first call on a
+ * device looks up that array's address; make it before any stream capture.
+ * Limits: one set, relline grids of at most 16384 bins, tables loaded by
+ * relx_init on the current device beforehand (RELX_ERR_NOTABLE otherwise).
+ * d_params: npar doubles; d_energy: n_bins + 1 edges; d_flux_in: relconv input
+ * (n_bins, else NULL); d_flux: n_bins outputs; d_status: one int (may be NULL).
+ * Asynchronous on `stream` (a cudaStream_t; NULL: the default stream). */
+int relx_eval_one_noalloc(int model, const double *d_params, const double *d_energy, int n_bins,
+                          const double *d_flux_in, double *d_flux, int *d_status, int ion_grad_type,
+                          double iongrad_index, void *stream);
+
 /* Measurement hooks (no counterpart in the reference).  When enabled, every
  * kernel of every batch is bracketed by CUDA events on its launching stream;
  * relx_profile_read synchronises and returns the accumulated milliseconds

@@ -762,6 +762,26 @@ static int eval_host(int model, int n_sets, const double *params, const double *
   return worst;
 }
 
+// ---- hooks for the other host translation units (not part of the C ABI) ----
+const RelxTables *runtime_tables(int *device) {
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  if (!C.T.loaded) return nullptr;
+  if (device) *device = C.device;
+  return &C.T.d;
+}
+int runtime_zones(int model, int ion_grad_type, int *nzones_env, int *flags) {
+  const EnvOpts env = read_env();
+  if (nzones_env) *nzones_env = env.nzones_env;
+  if (flags) *flags = env.flags;
+  return zones_for(model, ion_grad_type, env.nzones_env);
+}
+int runtime_nparams(int model) { return model_nparams(model); }
+void runtime_set_error(int status, const char *msg) {
+  if (msg) g_errmsg = msg;
+  g_last_status = status;
+}
+
 }  // namespace relx
 
 // ===========================================================================

@@ -1,0 +1,111 @@
+"""relx_eval_one_noalloc: one parameter set through the entry point whose
+intermediate arrays live in a static device array, against the batched entry
+point on the same inputs.  The caller's buffers come from torch; the entry
+point itself allocates nothing."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from cases import CASES, conv_input, grid
+from tolerance import assert_close
+
+pytestmark = pytest.mark.gpu
+
+MODELS = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3}
+RELX_ERR_ARG = 9
+
+
+def _fn(R):
+    L = R.lib()
+    f = L.relx_eval_one_noalloc
+    f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                  ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    return f
+
+
+class _Call:
+    """Device buffers of one call, made once by the caller."""
+
+    def __init__(self, torch, model, params, e, igt=0, igi=0.0):
+        dev = torch.device("cuda:0")
+        self.model, self.igt, self.igi = model, igt, igi
+        self.n = len(e) - 1
+        self.params = torch.tensor(np.asarray(params, dtype=np.float64), device=dev)
+        self.energy = torch.tensor(np.asarray(e, dtype=np.float64), device=dev)
+        self.fin = torch.tensor(conv_input(e), device=dev) if model == "relconv" else None
+        self.flux = torch.full((self.n,), -1.0, dtype=torch.float64, device=dev)
+        self.status = torch.full((1,), -1, dtype=torch.int32, device=dev)
+
+    def run(self, f):
+        return f(MODELS[self.model], self.params.data_ptr(), self.energy.data_ptr(), self.n,
+                 self.fin.data_ptr() if self.fin is not None else None, self.flux.data_ptr(), self.status.data_ptr(),
+                 self.igt, self.igi, None)
+
+
+def _batch(R, model, params, e, igt=0, igi=0.0):
+    fin = [conv_input(e)] if model == "relconv" else None
+    out, st = R.eval_batch(model, np.asarray(params)[None], [e], flux_in=fin,
+                           ion_grad_type=[igt] if igt else None, iongrad_index=[igi] if igt else None)
+    assert st[0] == 0, R.last_error()
+    return out[0]
+
+
+def _case(name):
+    return next(c for c in CASES if c[0] == name)
+
+
+def test_noalloc_matches_batch_on_two_calls_in_a_row(gpu):
+    torch = pytest.importorskip("torch")
+    f = _fn(gpu)
+    names = ["relxilllp_a", "relxill_cfg2", "relline_cfg1", "relconv_a", "relxilllp_alpha", "relxilllp_b"]
+    for name in names:
+        _, model, params, gspec, igt, igi = _case(name)
+        e = grid(gspec)
+        want = _batch(gpu, model, params, e, igt, igi)
+        call = _Call(torch, model, params, e, igt, igi)
+        for k in range(2):
+            call.flux.fill_(-1.0)
+            assert call.run(f) == 0, gpu.last_error()
+            torch.cuda.synchronize()
+            assert int(call.status.item()) == 0
+            assert_close(call.flux.cpu().numpy(), want, f"{name} no-alloc call {k + 1}")
+
+
+def test_noalloc_alternating_sets_keep_their_results(gpu):
+    """Two different sets back to back share the scratch; each result matches its own batch result."""
+    torch = pytest.importorskip("torch")
+    f = _fn(gpu)
+    a, b = _case("relxilllp_a"), _case("relxilllp_c")
+    ea, eb = grid(a[3]), grid(b[3])
+    ca = _Call(torch, "relxilllp", a[2], ea)
+    cb = _Call(torch, "relxilllp", b[2], eb)
+    assert ca.run(f) == 0 and cb.run(f) == 0, gpu.last_error()
+    torch.cuda.synchronize()
+    assert_close(ca.flux.cpu().numpy(), _batch(gpu, "relxilllp", a[2], ea), "set A")
+    assert_close(cb.flux.cpu().numpy(), _batch(gpu, "relxilllp", b[2], eb), "set B")
+
+
+def test_noalloc_allocates_no_device_memory(gpu):
+    torch = pytest.importorskip("torch")
+    f = _fn(gpu)
+    _, model, params, gspec, _, _ = _case("relxilllp_a")
+    call = _Call(torch, model, params, grid(gspec))
+    assert call.run(f) == 0  # set-up on the first call of the device
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        assert call.run(f) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
+def test_noalloc_rejects_relline_grid_beyond_limit(gpu):
+    torch = pytest.importorskip("torch")
+    f = _fn(gpu)
+    _, _, params, _, _, _ = _case("relline_cfg1")
+    e = np.exp(np.linspace(np.log(0.1), np.log(10.0), 16386))
+    call = _Call(torch, "relline", params, e)
+    assert call.run(f) == RELX_ERR_ARG
+    assert "16384" in gpu.last_error()
