@@ -210,12 +210,7 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
   NOALLOC_CUDA(launch_relline(model >= RELX_RELXILL, dim3(ntile_max, 1), s, tab, p.sin, p.sst, p.rad, p.line_e, nza,
                               p.prof, p.dist, p.tsum, ntile_max, model == RELX_RELLINE || model == RELX_RELCONV));
   if (model >= RELX_RELXILL) {
-    const int nxt = (tab.x_nener_pad + kXillTileH - 1) / kXillTileH;
-    if (nza <= RELX_ZDENSE)
-      xillver_dense_kernel<<<dim3(nxt, 1), kXillThreadsH, xill_smem_bytes(tab.x_nincl), s>>>(tab, p.sst, p.cor,
-                                                                                              p.dist, nza, p.xill, p.err);
-    else
-      xillver_zone_kernel<<<dim3(nxt, 1), kXillThreadsH, 0, s>>>(tab, p.sst, p.zcor, p.dist, nza, p.xill);
+    NOALLOC_CUDA(launch_xillver(s, tab, 1, nza, p.sst, p.cor, p.zcor, p.dist, p.xill, p.err, nullptr));
     conv_zone_kernel<<<dim3(nza, 1), kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sst, p.prof, p.tsum, ntile_max,
                                                                             kLineTileH, p.xill, nza, p.cout);
     finalize_relxill_kernel<<<1, kFinThreadsH, fin_smem_bytes(), s>>>(tab, p.sin, p.sst, p.cout, nza, d_energy, d_flux);

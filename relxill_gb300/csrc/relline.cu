@@ -385,14 +385,15 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
 // emission-angle distribution per zone (Relprofile.cpp:908-938), one CTA per set
 // ---------------------------------------------------------------------------
 struct HistSmem {
-  float4 tw[kLineWarps][RELX_MAX_NG];
-  float hterm[kLineWarps][2 * RELX_MAX_NG];
-  unsigned char hbin[kLineWarps][2 * RELX_MAX_NG];
+  RelxRadRec rec[kChunk];    // radius records of the current chunk
+  float re[kChunk];
+  float lh[kLineWarps][RELX_MAX_INCL][32];  // per-lane histograms, lane fastest (no bank conflicts)
   float hist[kLineWarps][RELX_MAX_INCL];
   float gfac[RELX_MAX_NG];   // d_gstar / sqrt(g*(1-g*))
   float gsf[RELX_MAX_NG];
-  float4 tab[1];
+  float4 tab[1];             // (a, mu0)-interpolated table [n_r][n_g], dynamic tail
 };
+static_assert(offsetof(HistSmem, rec) % 16 == 0, "radius records are staged as int4 rows");
 
 // FP64 emission-angle cosine of one fine radius, table point g, branch k
 // (interp_lin_2d_float then interp_lin_1d as Relprofile.cpp:67-77, 287-290)
@@ -411,7 +412,7 @@ __device__ double cosne_fp64(const RelxTables &tab, const RelxSetState &s, int i
   return lerp1(ifac, v[0], v[1]);
 }
 
-__global__ void __launch_bounds__(kLineThreads) hist_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
+__global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
                                                             const RelxRadial *__restrict__ srad, int nza,
                                                             float *__restrict__ dist) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -440,52 +441,68 @@ __global__ void __launch_bounds__(kLineThreads) hist_kernel(RelxTables tab, cons
       m.gfac[g] = (float) (dgs / sqrt(gs - gs * gs));
       m.gsf[g] = (float) gs;
     }
-    for (int i = tid; i < kLineWarps * RELX_MAX_INCL; i += kLineThreads) (&m.hist[0][0])[i] = 0.0f;
   }
   __syncthreads();
+  // Each lane owns (g*, branch) pairs q = lane, lane + 32, ... and keeps a private histogram in
+  // shared memory; at the end of a zone the lanes are added by a shuffle tree and the warps in order.
+  float(*lh)[32] = m.lh[warp];
+  for (int j = 0; j < RELX_MAX_INCL; j++) lh[j][lane] = 0.0f;
+  const float c4pi2 = (float) (4.0 * kPi * kPi);
   for (int z = 0; z < s.nz; z++) {
-    for (int ii = s.zi0[z] + warp; ii <= s.zi1[z]; ii += kLineWarps) {
-      const RelxRadRec rr = R.rec[ii];
-      if (rr.ielo < 0) continue;  // radius outside the line-profile grid (Relprofile.cpp:863)
-      const int it = rr.itab;
-      const float fr = rr.ifac;
-      for (int g = lane; g < ng; g += 32) {
-        const float4 lo = m.tab[(it + 1) * ng + g], hi = m.tab[it * ng + g];
-        m.tw[warp][g] = make_float4(fr * hi.x + (1.0f - fr) * lo.x, fr * hi.y + (1.0f - fr) * lo.y,
-                                    fr * hi.z + (1.0f - fr) * lo.z, fr * hi.w + (1.0f - fr) * lo.w);
+    const int i0 = s.zi0[z], i1 = s.zi1[z];
+    for (int c0 = i0; c0 <= i1; c0 += kChunk) {
+      const int cn = min(kChunk, i1 + 1 - c0);
+      {
+        const int4 *src = reinterpret_cast<const int4 *>(&R.rec[c0]);
+        int4 *dst = reinterpret_cast<int4 *>(m.rec);
+        for (int q = tid; q < cn * 4; q += kLineThreads) dst[q] = src[q];
+        for (int q = tid; q < cn; q += kLineThreads) m.re[q] = (float) R.re[c0 + q];
       }
-      __syncwarp();
-      const float re = (float) R.re[ii];
-      const float c = re * re * re * (float) (4.0 * kPi * kPi) * rr.ew;
-      for (int q = lane; q < 2 * ng; q += 32) {
-        const int g = q >> 1, k = q & 1;
-        const float4 T = m.tw[warp][g];
-        const float ge_ = m.gsf[g] * rr.dg.x + rr.gmin.x;
-        m.hterm[warp][q] = c * ge_ * ge_ * m.gfac[g] * (k ? T.y : T.x);
-        const float mu = k ? T.w : T.z;
-        const float xb = (float) n_incl * (1.0f - mu);
-        int b;
-        if (fabsf(xb - rintf(xb)) < 1e-5f) {
-          const double mud = cosne_fp64(tab, s, it, R.ifac[ii], g, k);
-          b = ((int) (n_incl * (1 - mud) + 1)) - 1;  // get_cosne_bin, Relprofile.cpp:799-801
-        } else {
-          b = ((int) (xb + 1.0f)) - 1;
+      __syncthreads();
+      for (int ci = warp; ci < cn; ci += kLineWarps) {
+        const RelxRadRec &rr = m.rec[ci];
+        if (rr.ielo < 0) continue;  // radius outside the line-profile grid (Relprofile.cpp:863)
+        const int it = rr.itab;
+        const float fr = rr.ifac;
+        const float re = m.re[ci];
+        const float c = re * re * re * c4pi2 * rr.ew;
+        const float dg = rr.dg.x, gmn = rr.gmin.x;
+        for (int g = lane; g < ng; g += 32) {
+          // trf(g*) and cosne(g*) at this radius: interp_lin_1d(ifac_r, T[ind+1], T[ind]) (Relprofile.cpp:280-293)
+          const float4 lo = m.tab[(it + 1) * ng + g], hi = m.tab[it * ng + g];
+          const float ge_ = m.gsf[g] * dg + gmn;
+          const float cg = c * ge_ * ge_ * m.gfac[g];
+#pragma unroll
+          for (int k = 0; k < 2; k++) {
+            const float trf = k ? fr * hi.y + (1.0f - fr) * lo.y : fr * hi.x + (1.0f - fr) * lo.x;
+            const float mu = k ? fr * hi.w + (1.0f - fr) * lo.w : fr * hi.z + (1.0f - fr) * lo.z;
+            const float xb = (float) n_incl * (1.0f - mu);
+            int b;
+            if (fabsf(xb - rintf(xb)) < 1e-5f) {
+              const double mud = cosne_fp64(tab, s, it, R.ifac[c0 + ci], g, k);
+              b = ((int) (n_incl * (1 - mud) + 1)) - 1;  // get_cosne_bin, Relprofile.cpp:799-801
+            } else {
+              b = ((int) (xb + 1.0f)) - 1;
+            }
+            b = max(0, min(b, n_incl - 1));
+            lh[b][lane] += cg * trf;
+          }
         }
-        m.hbin[warp][q] = (unsigned char) max(0, min(b, n_incl - 1));
       }
-      __syncwarp();
-      if (lane < n_incl) {
-        float acc = 0.0f;
-        for (int q = 0; q < 2 * ng; q++)
-          if (m.hbin[warp][q] == lane) acc += m.hterm[warp][q];
-        m.hist[warp][lane] += acc;
-      }
-      __syncwarp();
+      __syncthreads();
+    }
+    // zone end: lanes by a shuffle tree, warps in order
+    for (int j = 0; j < n_incl; j++) {
+      float v = lh[j][lane];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) m.hist[warp][j] = v;
+      lh[j][lane] = 0.0f;
     }
     __syncthreads();
     if (tid < n_incl) {
       float h = 0.0f;
-      for (int w = 0; w < kLineWarps; w++) { h += m.hist[w][tid]; m.hist[w][tid] = 0.0f; }
+      for (int w = 0; w < kLineWarps; w++) h += m.hist[w][tid];
       dist[((size_t) set * nza + z) * RELX_MAX_INCL + tid] = h;
     }
     __syncthreads();

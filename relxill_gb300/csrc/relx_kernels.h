@@ -10,15 +10,12 @@ namespace relx {
 constexpr int kSetupThreadsH = 256;
 constexpr int kLineThreadsH = 256;
 constexpr int kLineTileH = 512;
-constexpr int kXillThreadsH = 256;
-constexpr int kXillTileH = 1024;
 constexpr int kConvThreadsH = 256;
 constexpr int kFinThreadsH = 128;
 
 size_t setup_smem_bytes();
 size_t line_smem_bytes(int nr, int ng, bool limb);
 size_t hist_smem_bytes(int nr, int ng);
-size_t xill_smem_bytes(int n_incl);
 size_t conv_smem_bytes();
 size_t fin_smem_bytes();
 
@@ -30,10 +27,13 @@ cudaError_t launch_relline(bool hist, dim3 grid, cudaStream_t s, const RelxTable
                            const RelxSetState *sst, const RelxRadial *srad, const double *line_e, int nza, float *prof,
                            float *dist, double *tsum, int ntile_max, bool any_limb);
 
-__global__ void xillver_dense_kernel(RelxTables tab, const RelxSetState *sst, const RelxCorners *scor,
-                                     const float *dist_raw, int nza, float *xout, int *err);
-__global__ void xillver_zone_kernel(RelxTables tab, const RelxSetState *sst, const RelxZoneCorners *zcor,
-                                    const float *dist_raw, int nza, float *xout);
+cudaError_t xillver_set_smem(int n_incl);
+// order: the sets in visiting order (launch_xill_order), or null for batch order
+cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, int nza, const RelxSetState *sst,
+                           const RelxCorners *cor, const RelxZoneCorners *zcor, const float *dist, float *xout,
+                           int *err, const int *order);
+void launch_xill_order(cudaStream_t s, const RelxSetState *sst, const RelxCorners *cor, const RelxZoneCorners *zcor,
+                       int n_sets, int *order);
 
 __global__ void conv_zone_kernel(RelxTables tab, const RelxSetState *sst, const float *prof, const double *tsum,
                                  int ntile_max, int tile_bins, const float *xill, int nza, float *cout);

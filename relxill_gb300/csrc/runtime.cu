@@ -418,10 +418,10 @@ static int zones_for(int model, int ion_grad_type, int envn) {
 
 struct Workspace {
   DevBuf setin, st, rad, corners, zcorners, line_e, prof, dist, tsum, xill, cout, user_e, user_f, flux, sflag,
-      status, err, params, eoff, igt, igi;
+      status, err, params, eoff, igt, igi, order;
   void release() {
     for (DevBuf *b : {&setin, &st, &rad, &corners, &zcorners, &line_e, &prof, &dist, &tsum, &xill, &cout, &user_e,
-                      &user_f, &flux, &sflag, &status, &err, &params, &eoff, &igt, &igi})
+                      &user_f, &flux, &sflag, &status, &err, &params, &eoff, &igt, &igi, &order})
       b->release();
   }
 };
@@ -448,8 +448,7 @@ static int set_kernel_attrs(const Tables &T) {
   RELX_CUDA(cudaFuncSetAttribute(setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) setup_smem_bytes()));
   RELX_CUDA(relline_set_smem(line_smem_bytes(T.d.rel_nr, T.d.rel_ng, false), line_smem_bytes(T.d.rel_nr, T.d.rel_ng, true),
                              hist_smem_bytes(T.d.rel_nr, T.d.rel_ng)));
-  RELX_CUDA(cudaFuncSetAttribute(xillver_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int) xill_smem_bytes(T.d.x_nincl)));
+  RELX_CUDA(xillver_set_smem(T.d.x_nincl));
   RELX_CUDA(cudaFuncSetAttribute(conv_zone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
   RELX_CUDA(cudaFuncSetAttribute(relconv_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
   RELX_CUDA(cudaFuncSetAttribute(finalize_relxill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) fin_smem_bytes()));
@@ -523,8 +522,9 @@ struct ProfScope {
   int k;
   cudaStream_t s;
   cudaEvent_t a = nullptr, b = nullptr;
-  ProfScope(int kid, cudaStream_t st) : k(kid), s(st) {
-    g_launches++;
+  // kid: kernel kind; nk: kernels launched inside the scope
+  ProfScope(int kid, cudaStream_t st, int nk = 1) : k(kid), s(st) {
+    g_launches += nk;
     if (g_prof.on) {
       a = g_prof.get();
       b = g_prof.get();
@@ -581,7 +581,7 @@ static int reserve_workspace(Context &C, const BatchShape &b, bool need_zone_cor
     if (b.model == RELX_RELCONV && (st = W.user_f.reserve(b.n_edges * sizeof(double)))) return st;
   }
   if (b.model >= RELX_RELXILL) {
-    if ((st = W.corners.reserve(S * sizeof(RelxCorners))) ||
+    if ((st = W.corners.reserve(S * sizeof(RelxCorners))) || (st = W.order.reserve(S * sizeof(int))) ||
         (st = W.xill.reserve(S * nza * (size_t) C.T.d.x_nener_pad * sizeof(float))))
       return st;
     if (need_zone_corners && (st = W.zcorners.reserve(S * sizeof(RelxZoneCorners)))) return st;
@@ -608,20 +608,16 @@ static int launch_batch(Context &C, const BatchShape &b, cudaStream_t s) {
   }
   dim3 lg(b.ntile_max, S);
   {
-    ProfScope ps(PK_LINE, s);
+    ProfScope ps(PK_LINE, s, 1 + (b.any_limb ? 1 : 0) + (b.model >= RELX_RELXILL ? 1 : 0));
     RELX_CUDA(launch_relline(b.model >= RELX_RELXILL, lg, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza,
                              W.prof.as<float>(), W.dist.as<float>(), W.tsum.as<double>(), b.ntile_max, b.any_limb));
   }
   if (b.model >= RELX_RELXILL) {
-    const int nxt = (tab.x_nener_pad + kXillTileH - 1) / kXillTileH;
     {
-      ProfScope ps(PK_XILL, s);
-      if (b.nza <= RELX_ZDENSE)
-        xillver_dense_kernel<<<dim3(nxt, S), kXillThreadsH, xill_smem_bytes(tab.x_nincl), s>>>(
-            tab, sst, cor, W.dist.as<float>(), b.nza, W.xill.as<float>(), W.err.as<int>());
-      else
-        xillver_zone_kernel<<<dim3(nxt, S), kXillThreadsH, 0, s>>>(tab, sst, zcor, W.dist.as<float>(), b.nza,
-                                                                   W.xill.as<float>());
+      ProfScope ps(PK_XILL, s, b.nza <= RELX_ZDENSE ? 2 : 1);
+      if (b.nza <= RELX_ZDENSE) launch_xill_order(s, sst, cor, zcor, S, W.order.as<int>());
+      RELX_CUDA(launch_xillver(s, tab, S, b.nza, sst, cor, zcor, W.dist.as<float>(), W.xill.as<float>(),
+                               W.err.as<int>(), W.order.as<int>()));
     }
     {
       ProfScope ps(PK_CONV, s);
@@ -635,7 +631,7 @@ static int launch_batch(Context &C, const BatchShape &b, cudaStream_t s) {
                                                                          W.user_e.as<double>(), W.flux.as<double>());
     }
   } else if (b.model == RELX_RELCONV) {
-    ProfScope ps(PK_CONV, s);
+    ProfScope ps(PK_CONV, s, 2);  // convolution and finalize
     relconv_conv_kernel<<<S, kConvThreadsH, conv_smem_bytes(), s>>>(
         tab, sin, sst, W.prof.as<float>(), W.tsum.as<double>(), b.ntile_max, kLineTileH, b.nza, W.user_e.as<double>(),
         W.user_f.as<double>(), W.cout.as<float>(), W.sflag.as<int>());

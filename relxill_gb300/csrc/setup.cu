@@ -51,6 +51,8 @@ struct SetupSmem {
   int crow[RELX_NZMAX * 16];
   short cfirst[RELX_NZMAX * 16];
   short cuniq[RELX_NZMAX * 16];
+  float cw[RELX_NZMAX * 16];            // weight of every (zone, corner) entry
+  unsigned char clive[RELX_NZMAX * 16]; // row has a non-zero weight in some zone
 };
 
 // ---------------------------------------------------------------------------
@@ -649,21 +651,6 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     m.cfirst[e] = (short) first;
   }
   __syncthreads();
-  if (tid == 0) {
-    int u = 0;
-    for (int e = 0; e < ncor; e++) {
-      if (m.cfirst[e] == e) m.cuniq[e] = (short) u++;
-      else m.cuniq[e] = m.cuniq[m.cfirst[e]];
-    }
-    s.ucount = u;
-  }
-  __syncthreads();
-  const bool dense = nz <= RELX_ZDENSE;
-  if (dense) {
-    RelxCorners &C = cout[set];
-    for (int i = tid; i < RELX_MAX_UCORNER * RELX_ZDENSE; i += kSetupThreads) (&C.w[0][0])[i] = 0.0f;
-    __syncthreads();
-  }
   for (int e = tid; e < ncor; e += kSetupThreads) {
     int z = e >> 4, c = e & 15;
     double w = 1.0;
@@ -677,15 +664,42 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       double d = m.zdens[m.cfirst[e] >> 4];
       if (fabs(d - 15) > 1e-6) dscale = 1.0 / pow(10.0, d - 15);
     }
-    float wz = (float) (w * dscale * m.xscale[z]);
+    m.cw[e] = (float) (w * dscale * m.xscale[z]);
+    m.clive[e] = 0;
+  }
+  __syncthreads();
+  // a row is read only if some zone gives it a non-zero weight (a parameter on a grid value
+  // puts exactly zero weight on the upper bracket)
+  for (int e = tid; e < ncor; e += kSetupThreads)
+    if (m.cw[e] != 0.0f) m.clive[m.cfirst[e]] = 1;
+  __syncthreads();
+  if (tid == 0) {
+    int u = 0;
+    for (int e = 0; e < ncor; e++) {
+      if (m.cfirst[e] == e) m.cuniq[e] = m.clive[e] ? (short) u++ : (short) -1;
+      else m.cuniq[e] = m.cuniq[m.cfirst[e]];
+    }
+    s.ucount = u;
+  }
+  __syncthreads();
+  const bool dense = nz <= RELX_ZDENSE;
+  if (dense) {
+    RelxCorners &C = cout[set];
+    for (int i = tid; i < RELX_MAX_UCORNER * RELX_ZDENSE; i += kSetupThreads) (&C.w[0][0])[i] = 0.0f;
+    __syncthreads();
+  }
+  for (int e = tid; e < ncor; e += kSetupThreads) {
+    int z = e >> 4, c = e & 15;
     if (dense) {
       RelxCorners &C = cout[set];
-      int u = m.cuniq[e];
-      C.w[u][z] = wz;  // each (u, z) pair is written by exactly one entry
-      if (m.cfirst[e] == e) C.row[u] = m.crow[e];
+      const int u = m.cuniq[e];
+      if (u >= 0) {
+        C.w[u][z] = m.cw[e];  // each (u, z) pair is written by exactly one entry
+        if (m.cfirst[e] == e) C.row[u] = m.crow[e];
+      }
     } else {
       zcout[set].row[z][c] = m.crow[e];
-      zcout[set].w[z][c] = wz;
+      zcout[set].w[z][c] = m.cw[e];
     }
   }
   // ---- primary and reflection factors (PrimarySource.cpp:66-125)

@@ -8,21 +8,24 @@
 // density division of the row and 1/normalisation-change of the zone, and
 // dist is the zone's normalised emission-angle histogram.
 //
-// Launch: one CTA per (energy tile of 1024 bins, parameter set).  The corner
-// list of a set is de-duplicated across zones by the setup kernel, so every
-// table row a set needs is read from HBM once.  The n_incl row segments of a
-// corner (contiguous rows, incl is the fastest table index) are streamed into
-// shared memory with cp.async.bulk (TMA bulk copies) completing on an
-// mbarrier, three corners in flight; all waits are bounded and report a
-// timeout through the error flag instead of hanging.
+// Launch: one CTA of 128 threads per (energy tile of 512 bins, parameter set),
+// three CTAs per SM.  The corner list of a set is de-duplicated across zones by
+// the setup kernel and holds only rows with a non-zero weight, so every table
+// row a set needs is read once; sets are visited in table-row order
+// (xill_order_kernel) so that sets sharing rows find them in L2.  The n_incl
+// row segments of a corner (contiguous rows, incl is the fastest table index)
+// are streamed into shared memory with cp.async.bulk (TMA bulk copies)
+// completing on an mbarrier, three corners in flight per CTA; all waits are
+// bounded and report a timeout through the error flag instead of hanging.
 #include "relx_device.cuh"
 
 namespace relx {
 
-constexpr int kXillThreads = 256;
-constexpr int kXillTile = 1024;   // floats per row segment (4 KB)
+constexpr int kXillThreads = 128;
+constexpr int kXillTile = 512;    // floats per row segment (2 KB), one float4 per thread
 constexpr int kXillStages = 3;
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
+static_assert(kXillTile == 4 * kXillThreads, "one float4 per thread");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -63,27 +66,84 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
   return false;
 }
 
+template <int NZ>
 struct XillSmem {
   uint64_t full[kXillStages];
-  float w[RELX_MAX_UCORNER][RELX_ZDENSE];
-  float dist[RELX_ZDENSE][RELX_MAX_INCL];
+  float w[RELX_MAX_UCORNER][NZ];        // corner weight per zone
+  float dist[NZ][RELX_MAX_INCL];        // normalised emission-angle distribution per zone
   int row[RELX_MAX_UCORNER];
   int abort_flag;
   int pad_[3];
   float4 stage[1];  // [kXillStages][n_incl][kXillTile/4], dynamic tail
 };
 
-__global__ void __launch_bounds__(kXillThreads) xillver_dense_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
-                                                                     const RelxCorners *__restrict__ scor,
-                                                                     const float *__restrict__ dist_raw, int nza,
-                                                                     float *__restrict__ xout, int *__restrict__ err) {
+// Order in which the xillver kernel visits the sets: sets whose zones use the same table rows run
+// next to each other, so that a row read from HBM by one set is found in L2 by the next.  Key: the
+// first corner row of the set (table order).  Sorted in chunks of kOrderN sets (bitonic sort in
+// shared memory); the results do not depend on the order.
+constexpr int kOrderN = 4096;
+constexpr int kOrderThreads = 1024;
+__global__ void __launch_bounds__(kOrderThreads) xill_order_kernel(const RelxSetState *__restrict__ sst,
+                                                                   const RelxCorners *__restrict__ scor,
+                                                                   const RelxZoneCorners *__restrict__ zcor,
+                                                                   int n_sets, int *__restrict__ order) {
+  __shared__ unsigned long long key[kOrderN];
+  const int base = blockIdx.x * kOrderN;
+  const int n = min(kOrderN, n_sets - base);
+  for (int i = threadIdx.x; i < kOrderN; i += kOrderThreads) {
+    unsigned long long k = ~0ull;
+    if (i < n) {
+      const int set = base + i;
+      const RelxSetState &s = sst[set];
+      unsigned int r = 0xffffffffu;
+      if (s.status == RELX_OK && s.model >= RELX_RELXILL) {
+        if (s.nz <= RELX_ZDENSE) {
+          if (s.ucount > 0) r = (unsigned int) scor[set].row[0];
+        } else {
+          r = (unsigned int) zcor[set].row[0][0];
+        }
+      }
+      k = ((unsigned long long) r << 32) | (unsigned int) set;
+    }
+    key[i] = k;
+  }
+  __syncthreads();
+  for (int size = 2; size <= kOrderN; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < kOrderN / 2; i += kOrderThreads) {
+        const int lo = 2 * i - (i & (stride - 1));
+        const int hi = lo + stride;
+        const bool up = (lo & size) == 0;
+        const unsigned long long a = key[lo], b = key[hi];
+        if ((a > b) == up) { key[lo] = b; key[hi] = a; }
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = threadIdx.x; i < n; i += kOrderThreads) order[base + i] = (int) (key[i] & 0xffffffffull);
+}
+
+void launch_xill_order(cudaStream_t s, const RelxSetState *sst, const RelxCorners *cor, const RelxZoneCorners *zcor,
+                       int n_sets, int *order) {
+  xill_order_kernel<<<(n_sets + kOrderN - 1) / kOrderN, kOrderThreads, 0, s>>>(sst, cor, zcor, n_sets, order);
+}
+
+// NZ: zones held in registers (a set with more zones runs in a wider instance);
+// NI: inclinations unrolled at compile time (0: any count up to RELX_MAX_INCL).
+template <int NZ, int NI>
+__global__ void __launch_bounds__(kXillThreads, 3) xillver_dense_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
+                                                                        const RelxCorners *__restrict__ scor,
+                                                                        const float *__restrict__ dist_raw, int nza,
+                                                                        float *__restrict__ xout, int *__restrict__ err,
+                                                                        const int *__restrict__ order) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  XillSmem &m = *reinterpret_cast<XillSmem *>(smem_raw);
-  const int set = blockIdx.y, tile = blockIdx.x;
+  XillSmem<NZ> &m = *reinterpret_cast<XillSmem<NZ> *>(smem_raw);
+  const int set = order ? order[blockIdx.y] : blockIdx.y, tile = blockIdx.x;
   const RelxSetState &s = sst[set];
-  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.nz > RELX_ZDENSE) return;
+  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.nz > NZ) return;
+  constexpr int NIU = NI > 0 ? NI : RELX_MAX_INCL;
   const int tid = threadIdx.x;
-  const int nz = s.nz, U = s.ucount, ni = tab.x_nincl;
+  const int nz = s.nz, U = s.ucount, ni = NI > 0 ? NI : tab.x_nincl;
   const int pitch = tab.x_nener_pad;
   const int e0 = tile * kXillTile;
   if (e0 >= pitch) return;
@@ -92,7 +152,10 @@ __global__ void __launch_bounds__(kXillThreads) xillver_dense_kernel(RelxTables 
 
   // weights and normalised emission-angle distributions (renorm_relline_profile, Relprofile.cpp:783-795)
   const RelxCorners &C = scor[set];
-  for (int i = tid; i < U * RELX_ZDENSE; i += kXillThreads) (&m.w[0][0])[i] = (&C.w[0][0])[i];
+  for (int i = tid; i < U * NZ; i += kXillThreads) {
+    const int u = i / NZ, z = i - u * NZ;
+    m.w[u][z] = (z < nz) ? C.w[u][z] : 0.0f;
+  }
   for (int i = tid; i < U; i += kXillThreads) m.row[i] = C.row[i];
   if (tid < nz) {
     const float *d = dist_raw + ((size_t) set * nza + tid) * RELX_MAX_INCL;
@@ -117,9 +180,9 @@ __global__ void __launch_bounds__(kXillThreads) xillver_dense_kernel(RelxTables 
   if (tid == 0)
     for (int u = 0; u < min(U, kXillStages); u++) { issue(u); issued = u + 1; }
 
-  float4 acc[RELX_ZDENSE];
+  float4 acc[NZ];
 #pragma unroll
-  for (int z = 0; z < RELX_ZDENSE; z++) acc[z] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int z = 0; z < NZ; z++) acc[z] = make_float4(0.f, 0.f, 0.f, 0.f);
   const int q = tid;  // float4 index inside the tile
   const bool active = q * 4 < len;
   int u_stop = U;
@@ -130,25 +193,23 @@ __global__ void __launch_bounds__(kXillThreads) xillver_dense_kernel(RelxTables 
     __syncthreads();
     if (m.abort_flag) { u_stop = u; break; }
     if (active) {
-      float4 v[RELX_MAX_INCL];
+      float4 v[NIU];
 #pragma unroll
-      for (int i = 0; i < RELX_MAX_INCL; i++)
+      for (int i = 0; i < NIU; i++)
         if (i < ni) v[i] = m.stage[(st * ni + i) * (kXillTile / 4) + q];
 #pragma unroll
-      for (int z = 0; z < RELX_ZDENSE; z++) {
-        if (z < nz) {
-          const float wz = m.w[u][z];
-          if (wz != 0.0f) {
-            float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int z = 0; z < NZ; z++) {
+        const float wz = m.w[u][z];
+        if (wz != 0.0f) {
+          float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-            for (int i = 0; i < RELX_MAX_INCL; i++) {
-              if (i < ni) {
-                const float d = m.dist[z][i];
-                t.x += d * v[i].x; t.y += d * v[i].y; t.z += d * v[i].z; t.w += d * v[i].w;
-              }
+          for (int i = 0; i < NIU; i++) {
+            if (i < ni) {
+              const float d = m.dist[z][i];
+              t.x += d * v[i].x; t.y += d * v[i].y; t.z += d * v[i].z; t.w += d * v[i].w;
             }
-            acc[z].x += wz * t.x; acc[z].y += wz * t.y; acc[z].z += wz * t.z; acc[z].w += wz * t.w;
           }
+          acc[z].x += wz * t.x; acc[z].y += wz * t.y; acc[z].z += wz * t.z; acc[z].w += wz * t.w;
         }
       }
     }
@@ -166,13 +227,18 @@ __global__ void __launch_bounds__(kXillThreads) xillver_dense_kernel(RelxTables 
   }
   if (active) {
 #pragma unroll
-    for (int z = 0; z < RELX_ZDENSE; z++) {
+    for (int z = 0; z < NZ; z++) {
       if (z < nz) {
         float4 *o = reinterpret_cast<float4 *>(xout + ((size_t) set * nza + z) * pitch + e0) + q;
         *o = acc[z];
       }
     }
   }
+}
+
+template <int NZ>
+static size_t xill_smem_nz(int n_incl) {
+  return sizeof(XillSmem<NZ>) + sizeof(float4) * ((size_t) kXillStages * n_incl * (kXillTile / 4) - 1);
 }
 
 // generic path for more than RELX_ZDENSE zones (ionisation gradients): 16 corners per zone, plain loads
@@ -203,6 +269,7 @@ __global__ void __launch_bounds__(kXillThreads) xillver_zone_kernel(RelxTables t
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int c = 0; c < 16; c++) {
       const float wz = zcor[set].w[z][c];
+      if (wz == 0.0f) continue;  // zero weight: the row adds exactly nothing
       const float4 *src = reinterpret_cast<const float4 *>(tab.x_spec + (size_t) zcor[set].row[z][c] * pitch + e0) + q;
       float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
       for (int i = 0; i < ni; i++) {
@@ -215,8 +282,40 @@ __global__ void __launch_bounds__(kXillThreads) xillver_zone_kernel(RelxTables t
   }
 }
 
-size_t xill_smem_bytes(int n_incl) {
-  return sizeof(XillSmem) + sizeof(float4) * ((size_t) kXillStages * n_incl * (kXillTile / 4) - 1);
+#define RELX_XILL_INSTANCES(X) X(1, 10) X(10, 10) X(16, 10) X(1, 0) X(10, 0) X(16, 0)
+
+cudaError_t xillver_set_smem(int n_incl) {
+#define X(nz, ni)                                                                                   \
+  {                                                                                                 \
+    cudaError_t e = cudaFuncSetAttribute(xillver_dense_kernel<nz, ni>,                              \
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,               \
+                                         (int) xill_smem_nz<nz>(n_incl));                           \
+    if (e != cudaSuccess) return e;                                                                 \
+  }
+  RELX_XILL_INSTANCES(X)
+#undef X
+  return cudaSuccess;
+}
+
+// xillver stage of a batch: the dense kernel (instance by the batch's zone count and the table's
+// inclination count) for sets with at most RELX_ZDENSE zones, the zone kernel otherwise
+cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, int nza, const RelxSetState *sst,
+                           const RelxCorners *cor, const RelxZoneCorners *zcor, const float *dist, float *xout,
+                           int *err, const int *order) {
+  const dim3 grid((tab.x_nener_pad + kXillTile - 1) / kXillTile, n_sets);
+  if (nza > RELX_ZDENSE) {
+    xillver_zone_kernel<<<grid, kXillThreads, 0, s>>>(tab, sst, zcor, dist, nza, xout);
+    return cudaGetLastError();
+  }
+  const int nzk = nza <= 1 ? 1 : (nza <= 10 ? 10 : 16);
+  const int nik = tab.x_nincl == 10 ? 10 : 0;
+#define X(nz, ni)                                                                                           \
+  if (nzk == nz && nik == ni)                                                                               \
+    xillver_dense_kernel<nz, ni><<<grid, kXillThreads, xill_smem_nz<nz>(tab.x_nincl), s>>>(tab, sst, cor, dist, \
+                                                                                         nza, xout, err, order);
+  RELX_XILL_INSTANCES(X)
+#undef X
+  return cudaGetLastError();
 }
 
 }  // namespace relx
