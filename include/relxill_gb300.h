@@ -100,6 +100,46 @@ int relx_eval_one_noalloc(int model, const double *d_params, const double *d_ene
                           const double *d_flux_in, double *d_flux, int *d_status, int ion_grad_type,
                           double iongrad_index, void *stream);
 
+/* Device line-profile cache, the counterpart of the reference's relbase
+ * cache (src/Relcache.cpp:311-331, src/Relbase.cpp:461-538): sets whose
+ * relativistic parameters match a cached entry reuse its line profile and skip
+ * the line-profile kernels.  slots entries of about 260 KB each (rounded up to
+ * a power of two); 0 turns it off (the default).  Used by every batched,
+ * device and serving call; relline (whose profile lives on the caller's grid)
+ * and sets with more than 16 zones are not cached. */
+int relx_cache_config(int slots);
+/* out[0] lookups, out[1] hits, out[2] slots */
+int relx_cache_stats(int64_t *out);
+
+/* Serving engine (no counterpart in the reference): continuous batching of
+ * single-spectrum requests from many clients onto the batched path.  A
+ * scheduler thread forms a batch of waiting requests (one model, arrival
+ * order) whenever one of two batch slots is free, so a new batch is staged
+ * while the previous one runs; a completion thread copies results to the
+ * clients' buffers.  hbm_budget_bytes bounds the device workspace of the two
+ * slots (admission control); max_batch bounds a batch; cache_slots > 0 turns
+ * on the line-profile cache with that many entries.  Results do not depend
+ * on which requests share a batch. */
+typedef struct relx_server relx_server;
+relx_server *relx_serve_create(int64_t hbm_budget_bytes, int max_batch, int cache_slots);
+/* Queue one evaluation.  energy (n_bins + 1 edges), flux_in (relconv) and
+ * flux_out (n_bins) are the caller's host buffers and must stay valid until
+ * the request completes.  Returns the request id (>= 0) or -status. */
+int64_t relx_serve_submit(relx_server *s, int model, const double *params, const double *energy, int n_bins,
+                          const double *flux_in, double *flux_out, int ion_grad_type, double iongrad_index);
+/* Completed requests since the last poll (at most max): ids, statuses and
+ * latencies (submit to result in the caller's buffer, ms).  Completions are
+ * kept until a poll returns them.  Returns the count. */
+int relx_serve_poll(relx_server *s, int64_t *ids, int *status, double *latency_ms, int max);
+/* Block until request id has completed (and has not yet been polled). */
+int relx_serve_wait(relx_server *s, int64_t id, int *status);
+/* out[0] completed, [1] batches, [2] mean batch size, [3] p50 ms, [4] p99 ms,
+ * [5] max ms, [6] waiting requests, [7] last error; reset != 0 restarts the
+ * latency and batch statistics. */
+int relx_serve_stats(relx_server *s, double *out, int n, int reset);
+/* Finish the queued requests and stop the engine. */
+void relx_serve_destroy(relx_server *s);
+
 /* Measurement hooks (no counterpart in the reference).  When enabled, every
  * kernel of every batch is bracketed by CUDA events on its launching stream;
  * relx_profile_read synchronises and returns the accumulated milliseconds

@@ -76,6 +76,23 @@ def lib() -> ctypes.CDLL:
     L.relx_eval_batch_device.restype = ctypes.c_int
     L.relx_table_bytes.argtypes = [_lp]
     L.relx_table_bytes.restype = ctypes.c_int
+    L.relx_cache_config.argtypes = [ctypes.c_int]
+    L.relx_cache_config.restype = ctypes.c_int
+    L.relx_cache_stats.argtypes = [_lp]
+    L.relx_cache_stats.restype = ctypes.c_int
+    L.relx_serve_create.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int]
+    L.relx_serve_create.restype = ctypes.c_void_p
+    L.relx_serve_submit.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_int, _dp, _dp, ctypes.c_int,
+                                    ctypes.c_double]
+    L.relx_serve_submit.restype = ctypes.c_int64
+    L.relx_serve_poll.argtypes = [ctypes.c_void_p, _lp, _ip, _dp, ctypes.c_int]
+    L.relx_serve_poll.restype = ctypes.c_int
+    L.relx_serve_wait.argtypes = [ctypes.c_void_p, ctypes.c_int64, _ip]
+    L.relx_serve_wait.restype = ctypes.c_int
+    L.relx_serve_stats.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int]
+    L.relx_serve_stats.restype = ctypes.c_int
+    L.relx_serve_destroy.argtypes = [ctypes.c_void_p]
+    L.relx_serve_destroy.restype = None
     for name in ("c_lmodrelline", "c_lmodrelconv", "c_lmodrelxill", "c_lmodrelxilllp"):
         fn = getattr(L, name)
         fn.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, ctypes.c_char_p]
@@ -189,3 +206,83 @@ def default_params(model: str) -> np.ndarray:
 def log_grid(emin: float, emax: float, nbins: int) -> np.ndarray:
     """nbins log-spaced bins (nbins+1 edges), like get_log_grid (relutility.c:399-405)."""
     return np.exp(np.linspace(np.log(emin), np.log(emax), nbins + 1))
+
+
+def cache_config(slots: int) -> None:
+    """Device line-profile cache with `slots` entries (0 turns it off)."""
+    st = lib().relx_cache_config(int(slots))
+    if st:
+        raise RelxillError(st, last_error())
+
+
+def cache_stats() -> Dict[str, int]:
+    out = np.zeros(3, dtype=np.int64)
+    st = lib().relx_cache_stats(_ptr(out, _lp))
+    if st:
+        raise RelxillError(st, last_error())
+    return {"lookups": int(out[0]), "hits": int(out[1]), "slots": int(out[2])}
+
+
+class Server:
+    """Serving engine (relx_serve_*): continuous batching of single-spectrum requests.
+
+    The energy grid, the input spectrum (relconv) and the output array of a
+    request must stay alive until the request completes; `submit` keeps
+    references to them."""
+
+    STATS = ("completed", "batches", "mean_batch", "p50_ms", "p99_ms", "max_ms", "waiting", "last_error")
+
+    def __init__(self, hbm_budget_bytes: int = 8 << 30, max_batch: int = 4096, cache_slots: int = 0):
+        L = lib()
+        self._h = L.relx_serve_create(int(hbm_budget_bytes), int(max_batch), int(cache_slots))
+        if not self._h:
+            raise RelxillError(last_status_or(6), last_error())
+        self._keep: Dict[int, tuple] = {}
+
+    def submit(self, model: str, params, energy: np.ndarray, out: np.ndarray, flux_in: Optional[np.ndarray] = None,
+               ion_grad_type: int = 0, iongrad_index: float = 0.0) -> int:
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        if energy.dtype != np.float64 or not energy.flags.c_contiguous:
+            raise ValueError("energy must be a contiguous float64 array")
+        if out.dtype != np.float64 or not out.flags.c_contiguous or len(out) != len(energy) - 1:
+            raise ValueError("out must be a contiguous float64 array of len(energy) - 1")
+        rid = lib().relx_serve_submit(self._h, MODELS[model], _ptr(p), _ptr(energy), len(energy) - 1,
+                                      _ptr(flux_in) if flux_in is not None else None, _ptr(out),
+                                      int(ion_grad_type), float(iongrad_index))
+        if rid < 0:
+            raise RelxillError(int(-rid), last_error())
+        self._keep[rid] = (p, energy, out, flux_in)
+        return int(rid)
+
+    def poll(self, max_n: int = 4096) -> List[Tuple[int, int, float]]:
+        ids = np.zeros(max_n, dtype=np.int64)
+        sts = np.zeros(max_n, dtype=np.int32)
+        lat = np.zeros(max_n, dtype=np.float64)
+        n = lib().relx_serve_poll(self._h, _ptr(ids, _lp), _ptr(sts, _ip), _ptr(lat), max_n)
+        res = [(int(ids[i]), int(sts[i]), float(lat[i])) for i in range(n)]
+        for rid, _, _ in res:
+            self._keep.pop(rid, None)
+        return res
+
+    def stats(self, reset: bool = False) -> Dict[str, float]:
+        out = np.zeros(8)
+        lib().relx_serve_stats(self._h, _ptr(out), 8, 1 if reset else 0)
+        return dict(zip(self.STATS, out.tolist()))
+
+    def close(self) -> None:
+        if self._h:
+            lib().relx_serve_destroy(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def last_status_or(default: int) -> int:
+    st = lib().relx_last_status()
+    return st if st else default
+

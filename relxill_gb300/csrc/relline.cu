@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
   LineSmem<LIMB> &m = *reinterpret_cast<LineSmem<LIMB> *>(smem_raw);
   const int set = blockIdx.y, tile = blockIdx.x;
   const RelxSetState &s = sst[set];
-  if (s.status != RELX_OK) return;
+  if (s.status != RELX_OK || s.cached) return;
   if ((s.limb != 0) != LIMB) return;
   const int tlo = s.win_lo + tile * kLineTile;
   const int thi = min(s.win_hi, tlo + kLineTile);
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, c
   HistSmem &m = *reinterpret_cast<HistSmem *>(smem_raw);
   const int set = blockIdx.x;
   const RelxSetState &s = sst[set];
-  if (s.status != RELX_OK || s.model < RELX_RELXILL) return;
+  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.cached) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const RelxRadial &R = srad[set];
   const int nr = tab.rel_nr, nm = tab.rel_nmu0, ng = tab.rel_ng, n_incl = tab.x_nincl;

@@ -106,6 +106,7 @@ struct RelxSetIn {
 // per-set state written by the setup kernel
 struct RelxSetState {
   int status, model, emis_type, limb, nz, ion_grad_type, boost_switch;
+  int cached;       // line profile, tile sums and angle histograms come from the profile cache
   int g_n;          // bins of the line-profile grid (user grid for relline, conv grid otherwise)
   int win_lo, win_hi;  // line-profile bins touched by any radius
   int ind_a, ind_mu0;

@@ -18,6 +18,8 @@
 #include "fits_reader.h"
 #include "relx_common.h"
 #include "relx_kernels.h"
+#include "relx_runtime.h"
+#include "relcache.h"
 
 namespace relx {
 
@@ -58,6 +60,30 @@ struct DevBuf {
   void release() {
     if (p) cudaFree(p);
     p = nullptr;
+    bytes = 0;
+  }
+};
+
+// page-locked host staging buffer (grown on demand)
+struct Pinned {
+  void *h = nullptr;
+  size_t bytes = 0;
+  int reserve(size_t n) {
+    if (n <= bytes) return 0;
+    if (h) cudaFreeHost(h);
+    h = nullptr;
+    bytes = 0;
+    if (cudaMallocHost(&h, n) != cudaSuccess) {
+      cudaGetLastError();
+      g_errmsg = "cudaMallocHost of " + std::to_string(n) + " bytes failed";
+      return RELX_ERR_NOMEM;
+    }
+    bytes = n;
+    return 0;
+  }
+  void release() {
+    if (h) cudaFreeHost(h);
+    h = nullptr;
     bytes = 0;
   }
 };
@@ -418,10 +444,10 @@ static int zones_for(int model, int ion_grad_type, int envn) {
 
 struct Workspace {
   DevBuf setin, st, rad, corners, zcorners, line_e, prof, dist, tsum, xill, cout, user_e, user_f, flux, sflag,
-      status, err, params, eoff, igt, igi, order;
+      status, err, params, eoff, igt, igi, order, cslot;
   void release() {
     for (DevBuf *b : {&setin, &st, &rad, &corners, &zcorners, &line_e, &prof, &dist, &tsum, &xill, &cout, &user_e,
-                      &user_f, &flux, &sflag, &status, &err, &params, &eoff, &igt, &igi, &order})
+                      &user_f, &flux, &sflag, &status, &err, &params, &eoff, &igt, &igi, &order, &cslot})
       b->release();
   }
 };
@@ -434,9 +460,10 @@ struct Context {
   int device = -1;
   std::string table_dir;
   bool attrs_set = false;
-  // pinned host staging for the host-buffer API
-  void *h_pin = nullptr;
-  size_t h_pin_bytes = 0;
+  Pinned pin;             // host staging of the host-buffer API
+  RelCache cache;         // line-profile cache (off until relx_cache_config)
+  cudaEvent_t cache_ev = nullptr;  // recorded after the last batch's cache store
+  bool cache_ev_valid = false;
 };
 
 static Context &ctx() {
@@ -468,6 +495,7 @@ static int ensure_init(Context &C, const char *path) {
   int st = load_tables(dir, C.T);
   if (st) return st;
   C.table_dir = dir;
+  RELX_CUDA(C.cache.clear(C.stream));  // cached profiles belong to the previous tables
   if ((st = set_kernel_attrs(C.T))) return st;
   return 0;
 }
@@ -559,8 +587,7 @@ struct BatchShape {
   int64_t n_edges;  // total energy edges
 };
 
-static int reserve_workspace(Context &C, const BatchShape &b, bool need_zone_corners) {
-  Workspace &W = C.W;
+static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b, bool need_zone_corners) {
   const size_t S = b.n_sets;
   const size_t nza = b.nza;
   int st;
@@ -569,7 +596,7 @@ static int reserve_workspace(Context &C, const BatchShape &b, bool need_zone_cor
       (st = W.tsum.reserve(S * b.ntile_max * nza * sizeof(double))) ||
       (st = W.user_e.reserve(b.n_edges * sizeof(double))) || (st = W.flux.reserve(b.n_edges * sizeof(double))) ||
       (st = W.sflag.reserve(S * sizeof(int))) || (st = W.status.reserve(S * sizeof(int))) ||
-      (st = W.err.reserve(sizeof(int))))
+      (st = W.err.reserve(sizeof(int))) || (st = W.cslot.reserve(S * sizeof(int))))
     return st;
   if (b.model == RELX_RELLINE) {
     if ((st = W.line_e.reserve(b.n_edges * sizeof(double))) || (st = W.prof.reserve(b.n_edges * sizeof(float))))
@@ -582,7 +609,7 @@ static int reserve_workspace(Context &C, const BatchShape &b, bool need_zone_cor
   }
   if (b.model >= RELX_RELXILL) {
     if ((st = W.corners.reserve(S * sizeof(RelxCorners))) || (st = W.order.reserve(S * sizeof(int))) ||
-        (st = W.xill.reserve(S * nza * (size_t) C.T.d.x_nener_pad * sizeof(float))))
+        (st = W.xill.reserve(S * nza * (size_t) T.d.x_nener_pad * sizeof(float))))
       return st;
     if (need_zone_corners && (st = W.zcorners.reserve(S * sizeof(RelxZoneCorners)))) return st;
   }
@@ -590,9 +617,11 @@ static int reserve_workspace(Context &C, const BatchShape &b, bool need_zone_cor
 }
 
 // the kernel sequence for one batch; all pointers are device pointers, asynchronous on `s`
-static int launch_batch(Context &C, const BatchShape &b, cudaStream_t s) {
+// cache: the line-profile cache or null.  Its steps are ordered after the previous batch's cache
+// store (C.cache_ev), so batches on different streams never read a slot while it is written.
+static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStream_t s, bool use_cache) {
   const RelxTables &tab = C.T.d;
-  Workspace &W = C.W;
+  const bool cached = use_cache && C.cache.enabled() && b.model != RELX_RELLINE;
   const int S = b.n_sets;
   RelxSetIn *sin = W.setin.as<RelxSetIn>();
   RelxSetState *sst = W.st.as<RelxSetState>();
@@ -606,11 +635,26 @@ static int launch_batch(Context &C, const BatchShape &b, cudaStream_t s) {
     setup_kernel<<<S, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, b.model, sin, W.user_e.as<double>(),
                                                                W.line_e.as<double>(), sst, rad, cor, zcor);
   }
+  if (cached) {
+    ProfScope ps(PK_SETUP, s, 2);
+    if (C.cache_ev_valid) RELX_CUDA(cudaStreamWaitEvent(s, C.cache_ev, 0));
+    RELX_CUDA(cache_lookup(C.cache, s, sin, sst, S, W.cslot.as<int>()));
+    RELX_CUDA(cache_fill(C.cache, s, sst, W.cslot.as<int>(), S, b.nza, b.ntile_max, kLineTileH, W.prof.as<float>(),
+                         W.tsum.as<double>(), W.dist.as<float>()));
+  }
   dim3 lg(b.ntile_max, S);
   {
     ProfScope ps(PK_LINE, s, 1 + (b.any_limb ? 1 : 0) + (b.model >= RELX_RELXILL ? 1 : 0));
     RELX_CUDA(launch_relline(b.model >= RELX_RELXILL, lg, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza,
                              W.prof.as<float>(), W.dist.as<float>(), W.tsum.as<double>(), b.ntile_max, b.any_limb));
+  }
+  if (cached) {
+    ProfScope ps(PK_LINE, s);
+    RELX_CUDA(cache_store(C.cache, s, sin, sst, W.cslot.as<int>(), S, b.nza, b.ntile_max, kLineTileH,
+                          W.prof.as<float>(), W.tsum.as<double>(), W.dist.as<float>()));
+    if (!C.cache_ev) RELX_CUDA(cudaEventCreateWithFlags(&C.cache_ev, cudaEventDisableTiming));
+    RELX_CUDA(cudaEventRecord(C.cache_ev, s));
+    C.cache_ev_valid = true;
   }
   if (b.model >= RELX_RELXILL) {
     {
@@ -670,92 +714,170 @@ static int batch_shape(int model, int n_sets, const int64_t *eoff_host, const in
   return 0;
 }
 
-static int pinned(Context &C, size_t bytes) {
-  if (bytes <= C.h_pin_bytes) return 0;
-  if (C.h_pin) cudaFreeHost(C.h_pin);
-  C.h_pin = nullptr;
-  C.h_pin_bytes = 0;
-  RELX_CUDA(cudaMallocHost(&C.h_pin, bytes));
-  C.h_pin_bytes = bytes;
+// Stages the inputs of a host batch through pinned memory, launches the batch and queues the
+// copies of the results (flux, then per-set statuses) back into pinned memory, all asynchronous on
+// s.  *o_flux / *o_status: their offsets in P.  Caller holds C.mu.
+static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t s, const HostBatch &hb,
+                              bool use_cache, size_t *o_flux, size_t *o_status) {
+  const int model = hb.model, n_sets = hb.n_sets;
+  if (model < 0 || model >= RELX_NMODELS || n_sets <= 0 || !hb.params || !hb.energy || !hb.eoff) return RELX_ERR_ARG;
+  if (model == RELX_RELCONV && !hb.flux_in) return RELX_ERR_ARG;
+  const EnvOpts env = read_env();
+  BatchShape b;
+  bool need_zc = false;
+  int st;
+  if ((st = batch_shape(model, n_sets, hb.eoff, hb.igt, env, &b, &need_zc))) return st;
+  if ((st = reserve_workspace(C.T, W, b, need_zc))) return st;
+  const int npar = model_nparams(model);
+  const size_t pb = sizeof(double) * (size_t) n_sets * npar, eb = sizeof(double) * (size_t) b.n_edges;
+  const size_t ob = sizeof(int64_t) * (size_t) (n_sets + 1), gb = hb.igt ? sizeof(int) * n_sets : 0,
+               ib = hb.igi ? sizeof(double) * n_sets : 0;
+  const size_t fb = (model == RELX_RELCONV) ? eb : 0;
+  const size_t nflux = (size_t) (b.n_edges - n_sets);
+  if ((st = P.reserve(pb + eb + ob + gb + ib + fb + nflux * sizeof(double) + sizeof(int) * n_sets + 64 * 10)))
+    return st;
+  unsigned char *h = (unsigned char *) P.h;
+  size_t off = 0;
+  auto put = [&](const void *src, size_t n) {
+    size_t o = off;
+    if (n && src) std::memcpy(h + o, src, n);
+    off += (n + 63) / 64 * 64;
+    return o;
+  };
+  size_t o_p = put(hb.params, pb), o_e = put(hb.energy, eb), o_o = put(hb.eoff, ob);
+  size_t o_g = hb.igt ? put(hb.igt, gb) : 0, o_i = hb.igi ? put(hb.igi, ib) : 0;
+  size_t o_f = 0;
+  if (model == RELX_RELCONV) {
+    // input flux arrives with n per set; spread to the edge layout (offset e_off per set)
+    o_f = put(nullptr, fb);
+    double *fi = (double *) (h + o_f);
+    for (int i = 0; i < n_sets; i++) {
+      int n = (int) (hb.eoff[i + 1] - hb.eoff[i] - 1);
+      std::memcpy(fi + hb.eoff[i], hb.flux_in + (hb.eoff[i] - i), sizeof(double) * n);
+    }
+  }
+  *o_flux = put(nullptr, nflux * sizeof(double));
+  *o_status = put(nullptr, sizeof(int) * n_sets);
+  if ((st = W.params.reserve(pb)) || (st = W.eoff.reserve(ob)) || (hb.igt && (st = W.igt.reserve(gb))) ||
+      (hb.igi && (st = W.igi.reserve(ib))))
+    return st;
+  RELX_CUDA(cudaMemcpyAsync(W.params.p, h + o_p, pb, cudaMemcpyHostToDevice, s));
+  RELX_CUDA(cudaMemcpyAsync(W.user_e.p, h + o_e, eb, cudaMemcpyHostToDevice, s));
+  RELX_CUDA(cudaMemcpyAsync(W.eoff.p, h + o_o, ob, cudaMemcpyHostToDevice, s));
+  if (hb.igt) RELX_CUDA(cudaMemcpyAsync(W.igt.p, h + o_g, gb, cudaMemcpyHostToDevice, s));
+  if (hb.igi) RELX_CUDA(cudaMemcpyAsync(W.igi.p, h + o_i, ib, cudaMemcpyHostToDevice, s));
+  if (model == RELX_RELCONV) RELX_CUDA(cudaMemcpyAsync(W.user_f.p, h + o_f, fb, cudaMemcpyHostToDevice, s));
+  {
+    ProfScope ps(PK_PACK, s);
+    pack_kernel<<<(n_sets + 127) / 128, 128, 0, s>>>(n_sets, npar, W.params.as<double>(), W.eoff.as<int64_t>(),
+                                                     hb.igt ? W.igt.as<int>() : nullptr,
+                                                     hb.igi ? W.igi.as<double>() : nullptr, env.nzones_env, env.flags,
+                                                     W.setin.as<RelxSetIn>());
+  }
+  if ((st = launch_batch(C, W, b, s, use_cache))) return st;
+  RELX_CUDA(cudaMemcpyAsync(h + *o_flux, W.flux.p, nflux * sizeof(double), cudaMemcpyDeviceToHost, s));
+  RELX_CUDA(cudaMemcpyAsync(h + *o_status, W.status.p, sizeof(int) * n_sets, cudaMemcpyDeviceToHost, s));
   return 0;
 }
 
 // host-buffer evaluation: copies in, evaluates, copies out, synchronises
-static int eval_host(int model, int n_sets, const double *params, const double *energy, const int64_t *eoff,
-                     const double *flux_in, double *flux, int *status, const int *igt, const double *igi) {
-  if (model < 0 || model >= RELX_NMODELS || n_sets <= 0 || !params || !energy || !eoff || !flux) return RELX_ERR_ARG;
-  if (model == RELX_RELCONV && !flux_in) return RELX_ERR_ARG;
+static int eval_host(const HostBatch &hb, double *flux, int *status) {
+  if (!flux) return RELX_ERR_ARG;
   Context &C = ctx();
   std::lock_guard<std::mutex> lock(C.mu);
   int st = ensure_init(C, nullptr);
   if (st) return st;
-  const EnvOpts env = read_env();
-  BatchShape b;
-  bool need_zc = false;
-  if ((st = batch_shape(model, n_sets, eoff, igt, env, &b, &need_zc))) return st;
-  if ((st = reserve_workspace(C, b, need_zc))) return st;
-  const int npar = model_nparams(model);
-  cudaStream_t s = C.stream;
-  Workspace &W = C.W;
-  // stage inputs through pinned memory
-  const size_t pb = sizeof(double) * (size_t) n_sets * npar, eb = sizeof(double) * (size_t) b.n_edges;
-  const size_t ob = sizeof(int64_t) * (size_t) (n_sets + 1), gb = igt ? sizeof(int) * n_sets : 0,
-               ib = igi ? sizeof(double) * n_sets : 0;
-  const size_t fb = (model == RELX_RELCONV) ? eb : 0;
-  if ((st = pinned(C, pb + eb + ob + gb + ib + fb + eb + 64 * 8))) return st;
-  unsigned char *h = (unsigned char *) C.h_pin;
-  size_t off = 0;
-  auto put = [&](const void *src, size_t n) {
-    size_t o = off;
-    if (n) std::memcpy(h + o, src, n);
-    off += (n + 63) / 64 * 64;
-    return o;
-  };
-  size_t o_p = put(params, pb), o_e = put(energy, eb), o_o = put(eoff, ob);
-  size_t o_g = igt ? put(igt, gb) : 0, o_i = igi ? put(igi, ib) : 0;
-  size_t o_f = 0;
-  if (model == RELX_RELCONV) {
-    // input flux arrives with n per set; spread to the edge layout (offset e_off per set)
-    o_f = off;
-    double *fi = (double *) (h + o_f);
-    for (int i = 0; i < n_sets; i++) {
-      int n = (int) (eoff[i + 1] - eoff[i] - 1);
-      std::memcpy(fi + eoff[i], flux_in + (eoff[i] - i), sizeof(double) * n);
-    }
-    off += (fb + 63) / 64 * 64;
-  }
-  DevBuf &d_params = W.params, &d_eoff = W.eoff, &d_igt = W.igt, &d_igi = W.igi;
-  if ((st = d_params.reserve(pb)) || (st = d_eoff.reserve(ob)) || (igt && (st = d_igt.reserve(gb))) ||
-      (igi && (st = d_igi.reserve(ib))))
-    return st;
-  RELX_CUDA(cudaMemcpyAsync(d_params.p, h + o_p, pb, cudaMemcpyHostToDevice, s));
-  RELX_CUDA(cudaMemcpyAsync(W.user_e.p, h + o_e, eb, cudaMemcpyHostToDevice, s));
-  RELX_CUDA(cudaMemcpyAsync(d_eoff.p, h + o_o, ob, cudaMemcpyHostToDevice, s));
-  if (igt) RELX_CUDA(cudaMemcpyAsync(d_igt.p, h + o_g, gb, cudaMemcpyHostToDevice, s));
-  if (igi) RELX_CUDA(cudaMemcpyAsync(d_igi.p, h + o_i, ib, cudaMemcpyHostToDevice, s));
-  if (model == RELX_RELCONV) RELX_CUDA(cudaMemcpyAsync(W.user_f.p, h + o_f, fb, cudaMemcpyHostToDevice, s));
-  {
-    ProfScope ps(PK_PACK, s);
-    pack_kernel<<<(n_sets + 127) / 128, 128, 0, s>>>(n_sets, npar, d_params.as<double>(), d_eoff.as<int64_t>(),
-                                                     igt ? d_igt.as<int>() : nullptr,
-                                                     igi ? d_igi.as<double>() : nullptr, env.nzones_env, env.flags,
-                                                     W.setin.as<RelxSetIn>());
-  }
-  if ((st = launch_batch(C, b, s))) return st;
-  // results: flux (edge layout minus set index) and statuses
-  const size_t nflux = (size_t) (b.n_edges - n_sets);
-  size_t o_out = off;
-  RELX_CUDA(cudaMemcpyAsync(h + o_out, W.flux.p, nflux * sizeof(double), cudaMemcpyDeviceToHost, s));
-  std::vector<int> sts(n_sets);
-  RELX_CUDA(cudaMemcpyAsync(sts.data(), W.status.p, sizeof(int) * n_sets, cudaMemcpyDeviceToHost, s));
-  RELX_CUDA(cudaStreamSynchronize(s));
-  std::memcpy(flux, h + o_out, nflux * sizeof(double));
+  size_t o_flux = 0, o_status = 0;
+  if ((st = enqueue_host_batch(C, C.W, C.pin, C.stream, hb, true, &o_flux, &o_status))) return st;
+  RELX_CUDA(cudaStreamSynchronize(C.stream));
+  const unsigned char *h = (const unsigned char *) C.pin.h;
+  std::memcpy(flux, h + o_flux, sizeof(double) * (size_t) (hb.eoff[hb.n_sets] - hb.n_sets));
+  const int *sts = (const int *) (h + o_status);
   int worst = 0;
-  for (int i = 0; i < n_sets; i++) {
+  for (int i = 0; i < hb.n_sets; i++) {
     if (status) status[i] = sts[i];
     if (sts[i] != 0 && worst == 0) worst = sts[i];
   }
   return worst;
+}
+
+// ---- batch slots of the serving engine ----
+struct BatchSlot {
+  Workspace W;
+  Pinned P;
+  cudaStream_t s = nullptr;
+  cudaEvent_t done = nullptr;
+  size_t o_flux = 0, o_status = 0;
+  bool pending = false;
+};
+
+int slot_create(BatchSlot **out) {
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  int st = ensure_init(C, nullptr);
+  if (st) return st;
+  BatchSlot *b = new BatchSlot();
+  if (cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    delete b;
+    g_errmsg = "slot stream or event creation failed";
+    return RELX_ERR_CUDA;
+  }
+  *out = b;
+  return 0;
+}
+
+void slot_destroy(BatchSlot *b) {
+  if (!b) return;
+  if (b->s) cudaStreamSynchronize(b->s);
+  b->W.release();
+  b->P.release();
+  if (b->done) cudaEventDestroy(b->done);
+  if (b->s) cudaStreamDestroy(b->s);
+  delete b;
+}
+
+int slot_enqueue(BatchSlot *b, const HostBatch &hb, bool use_cache) {
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  int st = enqueue_host_batch(C, b->W, b->P, b->s, hb, use_cache, &b->o_flux, &b->o_status);
+  if (st) return st;
+  RELX_CUDA(cudaEventRecord(b->done, b->s));
+  b->pending = true;
+  return 0;
+}
+
+int slot_wait(BatchSlot *b, const double **flux, const int **status) {
+  if (!b->pending) return RELX_ERR_ARG;
+  cudaError_t e = cudaEventSynchronize(b->done);
+  b->pending = false;
+  if (e != cudaSuccess) {
+    g_errmsg = std::string("batch slot: ") + cudaGetErrorString(e);
+    return RELX_ERR_CUDA;
+  }
+  *flux = (const double *) ((const unsigned char *) b->P.h + b->o_flux);
+  *status = (const int *) ((const unsigned char *) b->P.h + b->o_status);
+  return 0;
+}
+
+size_t batch_device_bytes(int model, int n_sets, int64_t n_edges, int nza) {
+  size_t per_set = sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(RelxRadial) + sizeof(int) * 4 +
+                   sizeof(float) * nza * RELX_MAX_INCL + sizeof(double) * (RELX_NCONV / kLineTileH) * nza;
+  if (model != RELX_RELLINE) per_set += 2 * sizeof(float) * (size_t) nza * RELX_NCONV;
+  if (model >= RELX_RELXILL) per_set += sizeof(RelxCorners) + sizeof(float) * (size_t) nza * 4096;
+  return per_set * (size_t) n_sets + sizeof(double) * 3 * (size_t) n_edges;
+}
+
+int cache_configure(int slots) {
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  if (C.stream) RELX_CUDA(cudaStreamSynchronize(C.stream));
+  RELX_CUDA(cudaDeviceSynchronize());  // no batch may use the old cache
+  C.cache.release();
+  C.cache_ev_valid = false;
+  if (slots <= 0) return 0;
+  return C.cache.create(slots);
 }
 
 // ---- hooks for the other host translation units (not part of the C ABI) ----
@@ -802,8 +924,16 @@ int relx_last_status(void) { return g_last_status.load(); }
 int relx_eval_batch(int model, int n_sets, const double *params, const double *energy,
                     const int64_t *energy_offsets, const double *flux_in, double *flux, int *status,
                     const int *ion_grad_type, const double *iongrad_index) {
-  int st = eval_host(model, n_sets, params, energy, energy_offsets, flux_in, flux, status, ion_grad_type,
-                     iongrad_index);
+  HostBatch hb;
+  hb.model = model;
+  hb.n_sets = n_sets;
+  hb.params = params;
+  hb.energy = energy;
+  hb.eoff = energy_offsets;
+  hb.flux_in = flux_in;
+  hb.igt = ion_grad_type;
+  hb.igi = iongrad_index;
+  int st = eval_host(hb, flux, status);
   g_last_status = st;
   return st;
 }
@@ -823,7 +953,7 @@ int relx_eval_batch_device(int model, int n_sets, const double *d_params, const 
   BatchShape b;
   bool need_zc = false;
   if ((st = batch_shape(model, n_sets, h_energy_offsets, h_ion_grad_type, env, &b, &need_zc))) return st;
-  if ((st = reserve_workspace(C, b, need_zc))) return st;
+  if ((st = reserve_workspace(C.T, C.W, b, need_zc))) return st;
   cudaStream_t s = stream ? (cudaStream_t) stream : C.stream;
   Workspace &W = C.W;
   RELX_CUDA(cudaMemcpyAsync(W.user_e.p, d_energy, sizeof(double) * b.n_edges, cudaMemcpyDeviceToDevice, s));
@@ -837,7 +967,7 @@ int relx_eval_batch_device(int model, int n_sets, const double *d_params, const 
                                                      d_ion_grad_type, d_iongrad_index, env.nzones_env, env.flags,
                                                      W.setin.as<RelxSetIn>());
   }
-  if ((st = launch_batch(C, b, s))) return st;
+  if ((st = launch_batch(C, W, b, s, true))) return st;
   RELX_CUDA(cudaMemcpyAsync(d_flux, W.flux.p, sizeof(double) * (b.n_edges - n_sets), cudaMemcpyDeviceToDevice, s));
   if (d_status) RELX_CUDA(cudaMemcpyAsync(d_status, W.status.p, sizeof(int) * n_sets, cudaMemcpyDeviceToDevice, s));
   return 0;
@@ -885,6 +1015,27 @@ int relx_batch_stats(int n_sets, int64_t *out) {
   return 0;
 }
 
+int relx_cache_config(int slots) {
+  int st = cache_configure(slots);
+  g_last_status = st;
+  return st;
+}
+
+int relx_cache_stats(int64_t *out) {
+  if (!out) return RELX_ERR_ARG;
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  out[0] = out[1] = out[2] = 0;
+  if (!C.cache.enabled()) return 0;
+  RELX_CUDA(cudaDeviceSynchronize());
+  unsigned long long c[2];
+  RELX_CUDA(cudaMemcpy(c, C.cache.d.counters, sizeof(c), cudaMemcpyDeviceToHost));
+  out[0] = (int64_t) c[0];
+  out[1] = (int64_t) c[1];
+  out[2] = C.cache.d.n_slots;
+  return 0;
+}
+
 int relx_table_bytes(int64_t *bytes) {
   Context &C = ctx();
   std::lock_guard<std::mutex> lock(C.mu);
@@ -899,9 +1050,9 @@ void relx_release(void) {
   if (C.stream) cudaStreamSynchronize(C.stream);
   C.W.release();
   C.T.release();
-  if (C.h_pin) cudaFreeHost(C.h_pin);
-  C.h_pin = nullptr;
-  C.h_pin_bytes = 0;
+  C.pin.release();
+  C.cache.release();
+  C.cache_ev_valid = false;
 }
 
 // ---- local-model entry points with the XSPEC signature (create_wrapper_xspec.py:153-162) ----
@@ -915,8 +1066,14 @@ static void lmod_eval(int model, const double *energy, int Nflux, const double *
   std::vector<double> out((size_t) Nflux);
   std::vector<double> in;
   if (model == RELX_RELCONV) in.assign(flux, flux + Nflux);
-  int st = eval_host(model, 1, parameter, energy, eoff, model == RELX_RELCONV ? in.data() : nullptr, out.data(),
-                     &status, nullptr, nullptr);
+  HostBatch hb;
+  hb.model = model;
+  hb.n_sets = 1;
+  hb.params = parameter;
+  hb.energy = energy;
+  hb.eoff = eoff;
+  hb.flux_in = model == RELX_RELCONV ? in.data() : nullptr;
+  int st = eval_host(hb, out.data(), &status);
   g_last_status = st ? st : status;
   if (st == 0 || st == status) {
     std::memcpy(flux, out.data(), sizeof(double) * Nflux);

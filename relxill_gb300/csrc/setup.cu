@@ -63,6 +63,7 @@ __device__ void map_params(int model, const RelxSetIn &in, SetupSmem &m) {
   const double *v = in.p;
   s.model = model;
   s.status = RELX_OK;
+  s.cached = 0;
   s.limb = 0;
   s.height = 0;
   s.beta = 0;

@@ -1,0 +1,136 @@
+"""Line-profile cache and serving engine: results are the same numbers as the
+plain batched path, alone and in any mix of requests."""
+import time
+
+import numpy as np
+import pytest
+
+from cases import conv_input, log_grid
+
+pytestmark = pytest.mark.gpu
+
+
+def _lp_sets(n, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        out.append([rng.uniform(3, 100), 0.0, rng.uniform(0, 0.998), rng.uniform(5, 85), -1, 400, 0,
+                    rng.uniform(1.4, 2.8), rng.uniform(0, 4.5), 1.0, 300, 1.0, 0, 0])
+    return np.array(out)
+
+
+def _bkn_sets(n, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        out.append([rng.uniform(2, 4), 3, 15, rng.uniform(0, 0.998), rng.uniform(5, 85), -1, 400, 0,
+                    rng.uniform(1.4, 2.8), rng.uniform(0, 4.5), 1.0, 300, 2.0])
+    return np.array(out)
+
+
+def _grids(n, seed):
+    rng = np.random.default_rng(seed)
+    return [log_grid(0.3, 80.0, int(rng.integers(300, 1200))) for _ in range(n)]
+
+
+def _batch(R, model, params, grids, flux_in=None):
+    out, st = R.eval_batch(model, params, grids, flux_in=flux_in)
+    assert not np.any(st), R.last_error()
+    return out
+
+
+@pytest.fixture
+def cache(gpu):
+    gpu.cache_config(256)
+    try:
+        yield gpu
+    finally:
+        gpu.cache_config(0)
+
+
+def test_cache_hits_return_the_uncached_numbers(gpu):
+    lp, bkn = _lp_sets(12, 5), _bkn_sets(6, 6)
+    g_lp, g_bkn = _grids(12, 7), _grids(6, 8)
+    want_lp = _batch(gpu, "relxilllp", lp, g_lp)
+    want_bkn = _batch(gpu, "relxill", bkn, g_bkn)
+    gpu.cache_config(256)
+    try:
+        for _ in range(2):  # misses, then hits
+            got = _batch(gpu, "relxilllp", lp, g_lp)
+            for a, b in zip(got, want_lp):
+                np.testing.assert_array_equal(a, b)
+            got = _batch(gpu, "relxill", bkn, g_bkn)
+            for a, b in zip(got, want_bkn):
+                np.testing.assert_array_equal(a, b)
+        st = gpu.cache_stats()
+        # direct mapped: a set whose slot another set of its batch claimed is not stored
+        assert st["lookups"] == 36 and st["hits"] >= 15, st
+    finally:
+        gpu.cache_config(0)
+
+
+def test_cache_xillver_only_change_and_duplicates(cache):
+    R = cache
+    base = _bkn_sets(1, 11)[0]
+    sets = []
+    for lxi in (0.5, 1.5, 2.5, 3.5):  # same relativistic parameters, other xillver parameters
+        p = base.copy()
+        p[9] = lxi
+        sets.append(p)
+    sets = np.array(sets + [sets[0], sets[0]])  # duplicates inside one batch
+    grids = _grids(len(sets), 12)
+    R.cache_config(0)
+    want = _batch(R, "relxill", sets, grids)
+    R.cache_config(256)
+    got1 = _batch(R, "relxill", sets, grids)
+    got2 = _batch(R, "relxill", sets, grids)
+    for a, b, c in zip(got1, got2, want):
+        np.testing.assert_array_equal(a, c)
+        np.testing.assert_array_equal(b, c)
+    assert R.cache_stats()["hits"] >= len(sets)
+
+
+def test_relconv_through_cache(cache):
+    R = cache
+    p = np.array([[3, 3, 15, 0.9, 45, -1, 400, 0], [4, 3, 10, 0.5, 30, -1, 300, 1]], dtype=float)
+    e = [log_grid(0.3, 80.0, 500), log_grid(0.5, 50.0, 700)]
+    fin = [conv_input(x) for x in e]
+    a = _batch(R, "relconv", p, e, fin)
+    b = _batch(R, "relconv", p, e, fin)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_serve_results_match_batch_alone(gpu):
+    lp, bkn = _lp_sets(40, 21), _bkn_sets(24, 22)
+    g_lp, g_bkn = _grids(40, 23), _grids(24, 24)
+    want_lp = [_batch(gpu, "relxilllp", lp[i:i + 1], [g_lp[i]])[0] for i in range(len(lp))]
+    want_bkn = [_batch(gpu, "relxill", bkn[i:i + 1], [g_bkn[i]])[0] for i in range(len(bkn))]
+    with gpu.Server(hbm_budget_bytes=4 << 30, max_batch=16, cache_slots=64) as srv:
+        outs = {}
+        order = [("relxilllp", i) for i in range(len(lp))] + [("relxill", i) for i in range(len(bkn))]
+        rng = np.random.default_rng(3)
+        rng.shuffle(order)
+        for rep in range(2):  # the second round hits the cache
+            for model, i in order:
+                p, g = (lp[i], g_lp[i]) if model == "relxilllp" else (bkn[i], g_bkn[i])
+                out = np.empty(len(g) - 1)
+                rid = srv.submit(model, p, g, out)
+                outs[rid] = (model, i, out)
+            done = 0
+            t0 = time.time()
+            while done < len(order) and time.time() - t0 < 60:
+                for rid, st, lat in srv.poll():
+                    assert st == 0
+                    assert lat >= 0.0
+                    done += 1
+                time.sleep(0.001)
+            assert done == len(order)
+        for rid, (model, i, out) in outs.items():
+            want = want_lp[i] if model == "relxilllp" else want_bkn[i]
+            np.testing.assert_array_equal(out, want)
+        s = srv.stats()
+        assert s["completed"] == 2 * len(order)
+        assert s["p99_ms"] >= s["p50_ms"] > 0.0
+        assert s["batches"] >= 2
+    gpu.cache_config(0)
