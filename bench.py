@@ -60,6 +60,122 @@ def workload(n: int, seed_params: int = 2026, seed_grids: int = 7):
     return p, grids
 
 
+# ----------------------------------------------------------------------------
+# serving workload: walkers of a sampler, Poisson arrivals
+# ----------------------------------------------------------------------------
+# relxilllp: h, a, incl move on full steps; Gamma, logxi, A_Fe, Ecut, refl_frac on every step
+LP_SPEC = {"rel": {0: (1.0, 3.0, 100.0), 2: (0.01, 0.0, 0.998), 3: (1.0, 5.0, 85.0)},
+           "xill": {7: (0.02, 1.4, 2.8), 8: (0.05, 0.0, 4.5), 9: (0.05, 0.5, 10.0), 10: (5.0, 20.0, 1000.0),
+                    11: (0.05, 0.1, 10.0)}}
+# relxill: Index1, a, incl on full steps; Gamma, logxi, A_Fe, Ecut, refl_frac on every step
+BKN_SPEC = {"rel": {0: (0.05, 1.5, 5.0), 3: (0.01, 0.0, 0.998), 4: (1.0, 5.0, 85.0)},
+            "xill": {8: (0.02, 1.4, 2.8), 9: (0.05, 0.0, 4.5), 10: (0.05, 0.5, 10.0), 11: (5.0, 20.0, 1000.0),
+                     12: (0.05, 0.1, 10.0)}}
+
+
+def serve_walkers(n_walkers: int, seed: int = 42):
+    """Walkers: half relxilllp, half relxill, each with a fixed grid of U{300..5000} bins over 0.3-80 keV."""
+    rng = np.random.default_rng(seed)
+    lp, _ = workload(n_walkers, seed_params=seed + 1, seed_grids=seed + 2)
+    models, params, grids = [], [], []
+    for w in range(n_walkers):
+        nb = int(rng.integers(300, 5001))
+        grids.append(np.exp(np.linspace(np.log(0.3), np.log(80.0), nb + 1)))
+        if w % 2 == 0:
+            models.append("relxilllp")
+            params.append(lp[w].copy())
+        else:
+            models.append("relxill")
+            params.append(np.array([rng.uniform(2, 4), 3.0, 15.0, rng.uniform(0, 0.998), rng.uniform(5, 85), -1.0,
+                                    400.0, 0.0, rng.uniform(1.4, 2.8), rng.uniform(0, 4.5), 1.0, 300.0, 2.0]))
+    return models, params, grids
+
+
+def run_serve(R, seconds: float, rate: float, n_walkers: int, budget_gb: float, seed: int = 42):
+    """Open-loop Poisson arrivals from sampler walkers through the serving engine (relx_serve_*).
+
+    Each request moves its walker: with probability 0.7 only the xillver parameters change
+    (Gamma, logxi, A_Fe, Ecut, refl_frac), otherwise the relativistic ones too.  Latency is
+    submit to result in the client's buffer."""
+    L = R.lib()
+    models, params, grids = serve_walkers(n_walkers, seed)
+    rng = np.random.default_rng(seed + 3)
+    n_req = int(seconds * rate)
+    t_arr = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    who = rng.integers(0, n_walkers, n_req)
+    full = rng.random(n_req) >= 0.7
+    noise = rng.standard_normal((n_req, 14))
+    ring = 16
+    outs = [[np.zeros(len(g) - 1) for _ in range(ring)] for g in grids]
+    count = np.zeros(n_walkers, dtype=np.int64)
+    dp = ctypes.POINTER(ctypes.c_double)
+    mid = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3}
+    keep = {}  # sampled requests for the parity check: id -> (model, params, walker, ring slot, walker's request no.)
+    srv = R.Server(hbm_budget_bytes=int(budget_gb * (1 << 30)), max_batch=2048, cache_slots=4096)
+    try:
+        # warm-up: one request per walker
+        for w in range(n_walkers):
+            srv.submit(models[w], params[w], grids[w], outs[w][0])
+        t0 = time.perf_counter()
+        while srv.stats()["completed"] < n_walkers and time.perf_counter() - t0 < 60:
+            srv.poll()
+            time.sleep(0.001)
+        srv.poll()
+        srv.stats(reset=True)
+        c0 = R.cache_stats()
+        done = 0
+        start = time.perf_counter()
+        for k in range(n_req):
+            w = int(who[k])
+            spec = LP_SPEC if models[w] == "relxilllp" else BKN_SPEC
+            p = params[w]
+            for i, (sd, lo, hi) in spec["xill"].items():
+                p[i] = min(max(p[i] + sd * noise[k, i], lo), hi)
+            if full[k]:
+                for i, (sd, lo, hi) in spec["rel"].items():
+                    p[i] = min(max(p[i] + sd * noise[k, i], lo), hi)
+            slot = int(count[w] % ring)
+            count[w] += 1
+            out = outs[w][slot]
+            while time.perf_counter() - start < t_arr[k]:
+                pass
+            rid = L.relx_serve_submit(srv._h, mid[models[w]], p.ctypes.data_as(dp), grids[w].ctypes.data_as(dp),
+                                      len(grids[w]) - 1, None, out.ctypes.data_as(dp), 0, 0.0)
+            if rid < 0:
+                raise RuntimeError(f"relx_serve_submit: {-rid}")
+            if k >= n_req - 4096 and k % 61 == 0:
+                keep[int(rid)] = (models[w], p.copy(), w, slot, int(count[w] - 1))
+            if k % 64 == 0:
+                done += len(srv.poll())
+        t_sub = time.perf_counter() - start
+        while done < n_req and time.perf_counter() - start < t_sub + 60:
+            done += len(srv.poll())
+            time.sleep(0.0005)
+        elapsed = time.perf_counter() - start
+        st = srv.stats()
+        c1 = R.cache_stats()
+        # the sampled results against the same sets evaluated alone (ring slots are not reused for
+        # 16 requests of the walker, so check only requests that are still in place)
+        same = True
+        checked = 0
+        for rid, (model, pp, w, slot, nw) in keep.items():
+            if count[w] - 1 - nw >= ring:  # the ring slot has been reused since
+                continue
+            alone, sts = R.eval_batch(model, pp[None], [grids[w]])
+            same = same and bool(np.array_equal(alone[0], outs[w][slot]))
+            checked += 1
+    finally:
+        srv.close()
+        R.cache_config(0)
+    lookups = c1["lookups"] - c0["lookups"]
+    return {"walkers": n_walkers, "models": "relxilllp and relxill (half each)", "offered_rate": rate,
+            "achieved_submit_rate": n_req / t_sub, "requests": n_req, "seconds": round(elapsed, 3),
+            "spectra_s": done / elapsed, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+            "batches": int(st["batches"]), "mean_batch": st["mean_batch"], "hbm_budget_gb": budget_gb,
+            "cache_hit_rate": (c1["hits"] - c0["hits"]) / lookups if lookups else None,
+            "xillver_only_steps": 0.7, "identical_to_alone": same, "checked": checked}
+
+
 def tables(kind: str = "full") -> str:
     from relxill_gb300 import synth_tables
 
@@ -347,6 +463,10 @@ def run_gpu(args):
         cpu = {"value": r, "unit": "spectra/s", "cores": procs, "kind": "port",
                "sample": f"{len(idx)} sets of the workload on {procs} spawned processes ({dt:.1f} s)"}
 
+    serve = None
+    if not args.no_serve:
+        serve = run_serve(R, args.serve_seconds, args.serve_rate, args.walkers, args.serve_budget_gb)
+
     # roofline of the dominant kernel
     names = [L.relx_profile_name(k).decode() for k in range(7)]
     per = {names[k]: (ms_k[k] / max(n_k[k], 1), int(n_k[k])) for k in range(7)}
@@ -380,6 +500,7 @@ def run_gpu(args):
         "e2e": e2e, "plain_gpu": plain, "batched_over_plain": (value / world / plain["value"]) if plain else None,
         "max_rel_err_vs_oracle": max_err, "gpu_launches": int(launches), "clocks": clk,
         "roofline": roof, "dominant_kernel": names[dom], "kernels": kernels, "cpu_baseline": cpu,
+        "serve": serve,
     }
     print(json.dumps(line))
     if dist is not None:
@@ -398,6 +519,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-rate", type=float, default=50000.0)
+    ap.add_argument("--walkers", type=int, default=256)
+    ap.add_argument("--serve-budget-gb", type=float, default=160.0)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
