@@ -459,7 +459,11 @@ __global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, c
         for (int q = tid; q < cn; q += kLineThreads) m.re[q] = (float) R.re[c0 + q];
       }
       __syncthreads();
-      for (int ci = warp; ci < cn; ci += kLineWarps) {
+      // four radii per warp: 8 lanes per radius, each lane takes table points g = sub, sub + 8, ...
+      const int grp = lane >> 3, sub = lane & 7;
+      for (int cb = warp * 4; cb < cn; cb += kLineWarps * 4) {
+        const int ci = cb + grp;
+        if (ci >= cn) continue;
         const RelxRadRec &rr = m.rec[ci];
         if (rr.ielo < 0) continue;  // radius outside the line-profile grid (Relprofile.cpp:863)
         const int it = rr.itab;
@@ -467,7 +471,10 @@ __global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, c
         const float re = m.re[ci];
         const float c = re * re * re * c4pi2 * rr.ew;
         const float dg = rr.dg.x, gmn = rr.gmin.x;
-        for (int g = lane; g < ng; g += 32) {
+        // consecutive table points mostly fall into the same angle bin: add runs, flush on a change
+        int cur0 = -1, cur1 = -1;
+        float run0 = 0.0f, run1 = 0.0f;
+        for (int g = sub; g < ng; g += 8) {
           // trf(g*) and cosne(g*) at this radius: interp_lin_1d(ifac_r, T[ind+1], T[ind]) (Relprofile.cpp:280-293)
           const float4 lo = m.tab[(it + 1) * ng + g], hi = m.tab[it * ng + g];
           const float ge_ = m.gsf[g] * dg + gmn;
@@ -485,9 +492,19 @@ __global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, c
               b = ((int) (xb + 1.0f)) - 1;
             }
             b = max(0, min(b, n_incl - 1));
-            lh[b][lane] += cg * trf;
+            const float term = cg * trf;
+            int &cur = k ? cur1 : cur0;
+            float &run = k ? run1 : run0;
+            if (b != cur) {
+              if (cur >= 0) lh[cur][lane] += run;
+              cur = b;
+              run = 0.0f;
+            }
+            run += term;
           }
         }
+        if (cur0 >= 0) lh[cur0][lane] += run0;
+        if (cur1 >= 0) lh[cur1][lane] += run1;
       }
       __syncthreads();
     }

@@ -462,6 +462,8 @@ struct Context {
   bool attrs_set = false;
   Pinned pin;             // host staging of the host-buffer API
   RelCache cache;         // line-profile cache (off until relx_cache_config)
+  cudaStream_t aux[2] = {nullptr, nullptr};      // streams of pipelined chunks
+  cudaEvent_t aux_ev[2] = {nullptr, nullptr}, fork_ev = nullptr;
   cudaEvent_t cache_ev = nullptr;  // recorded after the last batch's cache store
   bool cache_ev_valid = false;
 };
@@ -617,41 +619,47 @@ static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b,
 }
 
 // the kernel sequence for one batch; all pointers are device pointers, asynchronous on `s`
-// cache: the line-profile cache or null.  Its steps are ordered after the previous batch's cache
-// store (C.cache_ev), so batches on different streams never read a slot while it is written.
-static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStream_t s, bool use_cache) {
+// The kernel sequence for the sets [base, base + n) of a batch, asynchronous on s.  Per-set
+// arrays are addressed from the range's first set; energy grids and fluxes keep the batch's
+// absolute offsets.  cached: use the line-profile cache (whole batches only).
+static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStream_t s, int base, int n, bool cached) {
   const RelxTables &tab = C.T.d;
-  const bool cached = use_cache && C.cache.enabled() && b.model != RELX_RELLINE;
-  const int S = b.n_sets;
-  RelxSetIn *sin = W.setin.as<RelxSetIn>();
-  RelxSetState *sst = W.st.as<RelxSetState>();
-  RelxRadial *rad = W.rad.as<RelxRadial>();
-  RelxCorners *cor = W.corners.as<RelxCorners>();
-  RelxZoneCorners *zcor = W.zcorners.as<RelxZoneCorners>();
-  RELX_CUDA(cudaMemsetAsync(W.sflag.p, 0, S * sizeof(int), s));
-  RELX_CUDA(cudaMemsetAsync(W.err.p, 0, sizeof(int), s));
+  const size_t nza = b.nza;
+  const bool conv_grid = b.model != RELX_RELLINE;
+  RelxSetIn *sin = W.setin.as<RelxSetIn>() + base;
+  RelxSetState *sst = W.st.as<RelxSetState>() + base;
+  RelxRadial *rad = W.rad.as<RelxRadial>() + base;
+  RelxCorners *cor = W.corners.p ? W.corners.as<RelxCorners>() + base : nullptr;
+  RelxZoneCorners *zcor = W.zcorners.p ? W.zcorners.as<RelxZoneCorners>() + base : nullptr;
+  float *prof = conv_grid ? W.prof.as<float>() + (size_t) base * nza * RELX_NCONV : W.prof.as<float>();
+  float *dist = W.dist.as<float>() + (size_t) base * nza * RELX_MAX_INCL;
+  double *tsum = W.tsum.as<double>() + (size_t) base * b.ntile_max * nza;
+  float *xill = W.xill.p ? W.xill.as<float>() + (size_t) base * nza * tab.x_nener_pad : nullptr;
+  float *cout = W.cout.p ? W.cout.as<float>() + (size_t) base * nza * RELX_NCONV : nullptr;
+  int *sflag = W.sflag.as<int>() + base;
+  double *flux = W.flux.as<double>() - base;  // kernels address set i at e_off(i) - i
+  const double *user_e = W.user_e.as<double>();
   {
     ProfScope ps(PK_SETUP, s);
-    setup_kernel<<<S, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, b.model, sin, W.user_e.as<double>(),
-                                                               W.line_e.as<double>(), sst, rad, cor, zcor);
+    setup_kernel<<<n, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, b.model, sin, user_e, W.line_e.as<double>(), sst,
+                                                               rad, cor, zcor);
   }
   if (cached) {
     ProfScope ps(PK_SETUP, s, 2);
     if (C.cache_ev_valid) RELX_CUDA(cudaStreamWaitEvent(s, C.cache_ev, 0));
-    RELX_CUDA(cache_lookup(C.cache, s, sin, sst, S, W.cslot.as<int>()));
-    RELX_CUDA(cache_fill(C.cache, s, sst, W.cslot.as<int>(), S, b.nza, b.ntile_max, kLineTileH, W.prof.as<float>(),
-                         W.tsum.as<double>(), W.dist.as<float>()));
+    RELX_CUDA(cache_lookup(C.cache, s, sin, sst, n, W.cslot.as<int>() + base));
+    RELX_CUDA(cache_fill(C.cache, s, sst, W.cslot.as<int>() + base, n, b.nza, b.ntile_max, kLineTileH, prof, tsum,
+                         dist));
   }
-  dim3 lg(b.ntile_max, S);
   {
     ProfScope ps(PK_LINE, s, 1 + (b.any_limb ? 1 : 0) + (b.model >= RELX_RELXILL ? 1 : 0));
-    RELX_CUDA(launch_relline(b.model >= RELX_RELXILL, lg, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza,
-                             W.prof.as<float>(), W.dist.as<float>(), W.tsum.as<double>(), b.ntile_max, b.any_limb));
+    RELX_CUDA(launch_relline(b.model >= RELX_RELXILL, dim3(b.ntile_max, n), s, tab, sin, sst, rad,
+                             W.line_e.as<double>(), b.nza, prof, dist, tsum, b.ntile_max, b.any_limb));
   }
   if (cached) {
     ProfScope ps(PK_LINE, s);
-    RELX_CUDA(cache_store(C.cache, s, sin, sst, W.cslot.as<int>(), S, b.nza, b.ntile_max, kLineTileH,
-                          W.prof.as<float>(), W.tsum.as<double>(), W.dist.as<float>()));
+    RELX_CUDA(cache_store(C.cache, s, sin, sst, W.cslot.as<int>() + base, n, b.nza, b.ntile_max, kLineTileH, prof,
+                          tsum, dist));
     if (!C.cache_ev) RELX_CUDA(cudaEventCreateWithFlags(&C.cache_ev, cudaEventDisableTiming));
     RELX_CUDA(cudaEventRecord(C.cache_ev, s));
     C.cache_ev_valid = true;
@@ -659,38 +667,69 @@ static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   if (b.model >= RELX_RELXILL) {
     {
       ProfScope ps(PK_XILL, s, b.nza <= RELX_ZDENSE ? 2 : 1);
-      if (b.nza <= RELX_ZDENSE) launch_xill_order(s, sst, cor, zcor, S, W.order.as<int>());
-      RELX_CUDA(launch_xillver(s, tab, S, b.nza, sst, cor, zcor, W.dist.as<float>(), W.xill.as<float>(),
-                               W.err.as<int>(), W.order.as<int>()));
+      int *order = W.order.as<int>() + base;
+      if (b.nza <= RELX_ZDENSE) launch_xill_order(s, sst, cor, zcor, n, order);
+      RELX_CUDA(launch_xillver(s, tab, n, b.nza, sst, cor, zcor, dist, xill, W.err.as<int>(), order));
     }
     {
       ProfScope ps(PK_CONV, s);
-      conv_zone_kernel<<<dim3(b.nza, S), kConvThreadsH, conv_smem_bytes(), s>>>(
-          tab, sst, W.prof.as<float>(), W.tsum.as<double>(), b.ntile_max, kLineTileH, W.xill.as<float>(), b.nza,
-          W.cout.as<float>());
+      conv_zone_kernel<<<dim3(b.nza, n), kConvThreadsH, conv_smem_bytes(), s>>>(tab, sst, prof, tsum, b.ntile_max,
+                                                                              kLineTileH, xill, b.nza, cout);
     }
     {
       ProfScope ps(PK_FIN, s);
-      finalize_relxill_kernel<<<S, kFinThreadsH, fin_smem_bytes(), s>>>(tab, sin, sst, W.cout.as<float>(), b.nza,
-                                                                         W.user_e.as<double>(), W.flux.as<double>());
+      finalize_relxill_kernel<<<n, kFinThreadsH, fin_smem_bytes(), s>>>(tab, sin, sst, cout, b.nza, user_e, flux);
     }
   } else if (b.model == RELX_RELCONV) {
     ProfScope ps(PK_CONV, s, 2);  // convolution and finalize
-    relconv_conv_kernel<<<S, kConvThreadsH, conv_smem_bytes(), s>>>(
-        tab, sin, sst, W.prof.as<float>(), W.tsum.as<double>(), b.ntile_max, kLineTileH, b.nza, W.user_e.as<double>(),
-        W.user_f.as<double>(), W.cout.as<float>(), W.sflag.as<int>());
-    finalize_relconv_kernel<<<S, kFinThreadsH, 0, s>>>(tab, sin, sst, W.cout.as<float>(), b.nza,
-                                                        W.user_e.as<double>(), W.sflag.as<int>(), W.flux.as<double>());
+    relconv_conv_kernel<<<n, kConvThreadsH, conv_smem_bytes(), s>>>(tab, sin, sst, prof, tsum, b.ntile_max,
+                                                                    kLineTileH, b.nza, user_e, W.user_f.as<double>(),
+                                                                    cout, sflag);
+    finalize_relconv_kernel<<<n, kFinThreadsH, 0, s>>>(tab, sin, sst, cout, b.nza, user_e, sflag, flux);
   } else {
     ProfScope ps(PK_FIN, s);
-    finalize_relline_kernel<<<S, kFinThreadsH, 0, s>>>(sin, sst, W.prof.as<float>(), W.tsum.as<double>(),
-                                                        b.ntile_max, kLineTileH, b.nza, W.flux.as<double>());
+    finalize_relline_kernel<<<n, kFinThreadsH, 0, s>>>(sin, sst, prof, tsum, b.ntile_max, kLineTileH, b.nza, flux);
   }
   {
     ProfScope ps(PK_STATUS, s);
-    status_kernel<<<(S + 255) / 256, 256, 0, s>>>(S, sst, W.sflag.as<int>(), W.err.as<int>(), W.status.as<int>());
+    status_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, sst, sflag, W.err.as<int>(), W.status.as<int>() + base);
   }
   RELX_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// Sets per pipelined chunk (0: one range).  Chunks alternate between two streams so that the
+// kernels of one chunk overlap those of the next (the FP64-bound set-up, the ALU-bound line
+// profile and the HBM-bound xillver stage use different units).
+static int chunk_sets() {
+  const char *v = std::getenv("RELX_CHUNK_SETS");
+  return v ? std::max(0, std::atoi(v)) : 0;
+}
+
+// cache: the line-profile cache, whose steps are ordered after the previous batch's cache store
+// (C.cache_ev), so batches on different streams never read a slot while it is written.
+static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStream_t s, bool use_cache) {
+  const bool cached = use_cache && C.cache.enabled() && b.model != RELX_RELLINE;
+  const int S = b.n_sets;
+  RELX_CUDA(cudaMemsetAsync(W.sflag.p, 0, S * sizeof(int), s));
+  RELX_CUDA(cudaMemsetAsync(W.err.p, 0, sizeof(int), s));
+  const int chunk = chunk_sets();
+  if (cached || chunk <= 0 || S < 2 * chunk) return launch_range(C, W, b, s, 0, S, cached);
+  for (int k = 0; k < 2; k++) {
+    if (!C.aux[k]) RELX_CUDA(cudaStreamCreateWithFlags(&C.aux[k], cudaStreamNonBlocking));
+    if (!C.aux_ev[k]) RELX_CUDA(cudaEventCreateWithFlags(&C.aux_ev[k], cudaEventDisableTiming));
+  }
+  if (!C.fork_ev) RELX_CUDA(cudaEventCreateWithFlags(&C.fork_ev, cudaEventDisableTiming));
+  RELX_CUDA(cudaEventRecord(C.fork_ev, s));
+  for (int k = 0; k < 2; k++) RELX_CUDA(cudaStreamWaitEvent(C.aux[k], C.fork_ev, 0));
+  int st = 0;
+  for (int base = 0, i = 0; base < S; base += chunk, i++) {
+    if ((st = launch_range(C, W, b, C.aux[i & 1], base, std::min(chunk, S - base), false))) return st;
+  }
+  for (int k = 0; k < 2; k++) {
+    RELX_CUDA(cudaEventRecord(C.aux_ev[k], C.aux[k]));
+    RELX_CUDA(cudaStreamWaitEvent(s, C.aux_ev[k], 0));
+  }
   return 0;
 }
 
