@@ -485,8 +485,19 @@ def run_gpu(args):
     xill_bytes = ucount * 10 * x_pad * 4 + nz_sum * x_pad * 4
     xill_ms = per["xillver"][0]
     roof = {"kernel": "xillver", "bound": "hbm", "achieved": xill_bytes / (xill_ms * 1e-3) / 1e9, "peak": hbm_peak,
-            "unit": "GB/s", "frac": None, "traffic": None, "peak_source": "measured" if peaks else "fallback"}
+            "unit": "GB/s", "frac": None, "traffic": None, "peak_source": "measured" if peaks else "fallback",
+            "algorithmic_bytes": xill_bytes}
     roof["frac"] = roof["achieved"] / roof["peak"]
+    # DRAM bytes of the same launch from a one-pass ncu capture of this workload (committed summary)
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "dram_traffic_relxilllp_4096sets.json")))
+        k = tr["kernels"]["xillver_dense_kernel"]
+        if S == N_SETS:
+            roof["traffic"] = k["dram_read_bytes"] + k["dram_write_bytes"]
+            roof["traffic_source"] = "profiles/dram_traffic_relxilllp_4096sets.json (ncu, one pass, full-size launch)"
+            roof["l2_bytes"] = k["l2_bytes"]
+    except (OSError, KeyError, ValueError):
+        pass
     kernels = {n: {"ms_per_launch": round(per[n][0], 4), "launches": per[n][1],
                    "share": round(ms_k[k] / total_k, 4) if total_k else None} for k, n in enumerate(names)}
     line = {
@@ -499,7 +510,9 @@ def run_gpu(args):
                    "l2": "inputs larger than L2 (1 GB xillver table, ~2 GB workspace per step)"},
         "e2e": e2e, "plain_gpu": plain, "batched_over_plain": (value / world / plain["value"]) if plain else None,
         "max_rel_err_vs_oracle": max_err, "gpu_launches": int(launches), "clocks": clk,
-        "roofline": roof, "dominant_kernel": names[dom], "kernels": kernels, "cpu_baseline": cpu,
+        "roofline": roof, "dominant_kernel": names[dom],
+        "dominant_kernel_bound": "FP32 ALU issue (line profile: Romberg g*-integration; see profiles/)",
+        "kernels": kernels, "cpu_baseline": cpu,
         "serve": serve,
     }
     print(json.dumps(line))
