@@ -140,6 +140,18 @@ int relx_serve_stats(relx_server *s, double *out, int n, int reset);
 /* Finish the queued requests and stop the engine. */
 void relx_serve_destroy(relx_server *s);
 
+/* Launch tuning (no counterpart in the reference).  autotune != 0: the first
+ * batch of a (model, batch-size class, zone count) is run once per candidate
+ * of (line-kernel tile of 256 or 512 bins, pipelined chunks of 1024 sets) and
+ * the fastest is kept for the class; that batch synchronises its stream.
+ * graphs != 0: a batch shape that recurs on the same workspace is captured
+ * into a CUDA graph on its second launch and replayed afterwards.  Both are on
+ * by default; every choice gives the same numbers. */
+int relx_tuning_config(int autotune, int graphs);
+/* tuned classes, 6 doubles each: model, size class (log2 of the set count),
+ * zones, line tile, chunk, best ms; returns the count (at most max) */
+int relx_tuning_report(double *out, int max);
+
 /* Measurement hooks (no counterpart in the reference).  When enabled, every
  * kernel of every batch is bracketed by CUDA events on its launching stream;
  * relx_profile_read synchronises and returns the accumulated milliseconds

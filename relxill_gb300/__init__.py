@@ -76,6 +76,10 @@ def lib() -> ctypes.CDLL:
     L.relx_eval_batch_device.restype = ctypes.c_int
     L.relx_table_bytes.argtypes = [_lp]
     L.relx_table_bytes.restype = ctypes.c_int
+    L.relx_tuning_config.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.relx_tuning_config.restype = ctypes.c_int
+    L.relx_tuning_report.argtypes = [_dp, ctypes.c_int]
+    L.relx_tuning_report.restype = ctypes.c_int
     L.relx_cache_config.argtypes = [ctypes.c_int]
     L.relx_cache_config.restype = ctypes.c_int
     L.relx_cache_stats.argtypes = [_lp]
@@ -206,6 +210,18 @@ def default_params(model: str) -> np.ndarray:
 def log_grid(emin: float, emax: float, nbins: int) -> np.ndarray:
     """nbins log-spaced bins (nbins+1 edges), like get_log_grid (relutility.c:399-405)."""
     return np.exp(np.linspace(np.log(emin), np.log(emax), nbins + 1))
+
+
+def tuning_config(autotune: bool = True, graphs: bool = True) -> None:
+    """Autotuned line-kernel tiles / pipelined chunks, and CUDA-graph replay of recurring batch shapes."""
+    lib().relx_tuning_config(1 if autotune else 0, 1 if graphs else 0)
+
+
+def tuning_report() -> List[Dict[str, float]]:
+    out = np.zeros(64 * 6)
+    n = lib().relx_tuning_report(_ptr(out), 64)
+    keys = ("model", "size_class", "zones", "line_tile", "chunk", "best_ms")
+    return [dict(zip(keys, out[i * 6:(i + 1) * 6].tolist())) for i in range(n)]
 
 
 def cache_config(slots: int) -> None:

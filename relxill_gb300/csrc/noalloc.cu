@@ -54,7 +54,7 @@ constexpr size_t kScratchBytes =
     align_up(sizeof(float) * (size_t) (RELX_NZMAX * RELX_NCONV > kMaxLineBins ? RELX_NZMAX * RELX_NCONV
                                                                                : kMaxLineBins)) +  // profile
     align_up(sizeof(float) * RELX_NZMAX * RELX_MAX_INCL) +                                   // angle histogram
-    align_up(sizeof(double) * (size_t) ((kMaxLineBins + kLineTileH - 1) / kLineTileH) * RELX_NZMAX) +  // tile sums
+    align_up(sizeof(double) * (size_t) ((kMaxLineBins + kSumBinsH - 1) / kSumBinsH) * RELX_NZMAX) +  // block sums
     align_up(sizeof(float) * (size_t) RELX_NZMAX * kMaxXillBins) +                           // xillver spectra
     align_up(sizeof(float) * (size_t) RELX_NZMAX * RELX_NCONV) +                             // convolved spectra
     3 * kAlign;                                                                              // flags
@@ -195,7 +195,7 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
   const int nza = runtime_zones(model, ion_grad_type, &nzones_env, &flags);
   if (nza < 1 || nza > RELX_NZMAX) return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: zone count out of range");
   const int gbins = (model == RELX_RELLINE) ? n_bins : RELX_NCONV;
-  const int ntile_max = (gbins + kLineTileH - 1) / kLineTileH;
+  const int ntile_max = (gbins + kSumBinsH - 1) / kSumBinsH;  // 256-bin profile-sum blocks
   unsigned char *base = nullptr;
   int st = scratch_for_device(dev, &base);
   if (st) return st;
@@ -207,20 +207,20 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
                                        nzones_env, flags, p.sin, p.sflag, p.err);
   setup_kernel<<<1, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, model, p.sin, d_energy, p.line_e, p.sst, p.rad,
                                                             p.cor, p.zcor);
-  NOALLOC_CUDA(launch_relline(model >= RELX_RELXILL, dim3(ntile_max, 1), s, tab, p.sin, p.sst, p.rad, p.line_e, nza,
-                              p.prof, p.dist, p.tsum, ntile_max, model == RELX_RELLINE || model == RELX_RELCONV));
+  NOALLOC_CUDA(launch_relline(model >= RELX_RELXILL, 1, 512, ntile_max, s, tab, p.sin, p.sst, p.rad, p.line_e, nza,
+                              p.prof, p.dist, p.tsum, model == RELX_RELLINE || model == RELX_RELCONV));
   if (model >= RELX_RELXILL) {
     NOALLOC_CUDA(launch_xillver(s, tab, 1, nza, p.sst, p.cor, p.zcor, p.dist, p.xill, p.err, nullptr));
     conv_zone_kernel<<<dim3(nza, 1), kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sst, p.prof, p.tsum, ntile_max,
-                                                                            kLineTileH, p.xill, nza, p.cout);
+                                                                            kSumBinsH, p.xill, nza, p.cout);
     finalize_relxill_kernel<<<1, kFinThreadsH, fin_smem_bytes(), s>>>(tab, p.sin, p.sst, p.cout, nza, d_energy, d_flux);
   } else if (model == RELX_RELCONV) {
     relconv_conv_kernel<<<1, kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sin, p.sst, p.prof, p.tsum, ntile_max,
-                                                                    kLineTileH, nza, d_energy, d_flux_in, p.cout,
+                                                                    kSumBinsH, nza, d_energy, d_flux_in, p.cout,
                                                                     p.sflag);
     finalize_relconv_kernel<<<1, kFinThreadsH, 0, s>>>(tab, p.sin, p.sst, p.cout, nza, d_energy, p.sflag, d_flux);
   } else {
-    finalize_relline_kernel<<<1, kFinThreadsH, 0, s>>>(p.sin, p.sst, p.prof, p.tsum, ntile_max, kLineTileH, nza,
+    finalize_relline_kernel<<<1, kFinThreadsH, 0, s>>>(p.sin, p.sst, p.prof, p.tsum, ntile_max, kSumBinsH, nza,
                                                         d_flux);
   }
   noalloc_status_kernel<<<1, 32, 0, s>>>(p.sst, p.sflag, p.err, p.status, d_status);

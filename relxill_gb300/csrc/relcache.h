@@ -8,7 +8,7 @@ namespace relx {
 
 constexpr int kCacheKeyLen = 12;
 constexpr int kCacheZones = RELX_ZDENSE;       // zones per entry (sets with more zones are not cached)
-constexpr int kCacheTiles = RELX_NCONV / 512;  // line-kernel tiles over the conv grid
+constexpr int kCacheTiles = RELX_NCONV / 256;  // 256-bin profile-sum blocks over the conv grid
 
 struct RelCacheDev {
   int n_slots = 0;        // power of two
@@ -16,7 +16,7 @@ struct RelCacheDev {
   int *valid = nullptr;   // [n_slots]
   int *claim = nullptr;   // [n_slots] lowest missing set of the current batch mapping to the slot
   float *prof = nullptr;  // [n_slots][kCacheZones][RELX_NCONV] (the set's profile window is used)
-  double *tsum = nullptr; // [n_slots][kCacheTiles][kCacheZones]
+  double *tsum = nullptr; // [n_slots][kCacheTiles][kCacheZones] profile sums per 256-bin block
   float *dist = nullptr;  // [n_slots][kCacheZones][RELX_MAX_INCL]
   unsigned long long *counters = nullptr;  // [0] lookups, [1] hits
 };

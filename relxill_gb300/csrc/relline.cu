@@ -23,7 +23,8 @@ namespace relx {
 
 constexpr int kLineWarps = 8;
 constexpr int kLineThreads = kLineWarps * 32;
-constexpr int kLineTile = 512;   // energy bins per CTA
+constexpr int kSumBins = 256;    // profile sums are kept per block of 256 bins, whatever the tile
+static_assert(kSumBins == kLineThreads, "one bin per thread and block in the sums");
 constexpr float kH = 5e-3f;
 
 // per-radius constants (warp uniform)
@@ -210,18 +211,23 @@ __device__ __forceinline__ float integ_bin(float2 Elo, float2 Ehi, bool red_lo, 
 
 constexpr int kChunk = 128;  // radius records staged per chunk
 
-template <bool LIMB>
+template <bool LIMB, int TILE>
 struct LineSmem {
-  float acc[kLineWarps][kLineTile];
-  float2 eff[kLineTile + 1];
-  unsigned char red[kLineTile];
+  float acc[kLineWarps][TILE];
+  float2 eff[TILE + 1];
+  unsigned char red[TILE];
   TW<LIMB> tw[kLineWarps][RELX_MAX_NG];
   RelxRadRec rec[kChunk];
   float2 gs[RELX_MAX_NG];   // table g* points (Relprofile.cpp:104-106) as float-float
   double red_sum[kLineWarps + 1];
   TW<LIMB> tab[1];          // (a, mu0)-interpolated table [n_r][n_g], dynamic tail
 };
-static_assert(offsetof(LineSmem<false>, rec) % 16 == 0 && offsetof(LineSmem<true>, rec) % 16 == 0,
+using LineSmemF512 = LineSmem<false, 512>;
+using LineSmemT512 = LineSmem<true, 512>;
+using LineSmemF256 = LineSmem<false, 256>;
+using LineSmemT256 = LineSmem<true, 256>;
+static_assert(offsetof(LineSmemF512, rec) % 16 == 0 && offsetof(LineSmemT512, rec) % 16 == 0 &&
+                  offsetof(LineSmemF256, rec) % 16 == 0 && offsetof(LineSmemT256, rec) % 16 == 0,
               "radius records are staged as int4 rows");
 
 // limb law at one table point (Relprofile.cpp:512-519)
@@ -231,21 +237,24 @@ __device__ __forceinline__ float limb_factor(int limb, float mu) {
   return 1.0f;
 }
 
-template <bool LIMB>
+// TILE: energy bins per CTA (256 or 512).  tsum holds the profile sum of every (256-bin block,
+// zone), nblk blocks per set, so that the sums do not depend on TILE.
+template <bool LIMB, int TILE>
 __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
                                                                   const RelxSetState *__restrict__ sst,
                                                                   const RelxRadial *__restrict__ srad,
                                                                   const double *__restrict__ line_e, int nza,
                                                                   float *__restrict__ prof, double *__restrict__ tsum,
-                                                                  int ntile_max) {
+                                                                  int nblk) {
+  static_assert(TILE % kSumBins == 0, "tiles are whole sum blocks");
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  LineSmem<LIMB> &m = *reinterpret_cast<LineSmem<LIMB> *>(smem_raw);
+  LineSmem<LIMB, TILE> &m = *reinterpret_cast<LineSmem<LIMB, TILE> *>(smem_raw);
   const int set = blockIdx.y, tile = blockIdx.x;
   const RelxSetState &s = sst[set];
   if (s.status != RELX_OK || s.cached) return;
   if ((s.limb != 0) != LIMB) return;
-  const int tlo = s.win_lo + tile * kLineTile;
-  const int thi = min(s.win_hi, tlo + kLineTile);
+  const int tlo = s.win_lo + tile * TILE;
+  const int thi = min(s.win_hi, tlo + TILE);
   if (tlo >= thi) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const RelxRadial &R = srad[set];
@@ -278,7 +287,7 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
     }
     for (int j = tid; j <= thi - tlo; j += kLineThreads) m.eff[j] = ff_from_double(ge[tlo + j]);
     for (int j = tid; j < thi - tlo; j += kLineThreads) m.red[j] = ge[tlo + j] >= 0.95 ? 1 : 0;
-    for (int i = tid; i < kLineWarps * kLineTile; i += kLineThreads) (&m.acc[0][0])[i] = 0.0f;
+    for (int i = tid; i < kLineWarps * TILE; i += kLineThreads) (&m.acc[0][0])[i] = 0.0f;
     for (int g = tid; g < ng; g += kLineThreads)
       m.gs[g] = ff_from_double(5e-3 + (1.0 - 2 * 5e-3) / (ng - 1) * ((float) g));
   }
@@ -365,18 +374,22 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
       __syncthreads();
     }
     // zone end: sum the warp rows in order, divide by the bin centre (renorm_relline_profile, Relprofile.cpp:753-762)
-    double part = 0.0;
-    for (int jj = tid; jj < thi - tlo; jj += kLineThreads) {
-      float v = 0.0f;
 #pragma unroll
-      for (int w = 0; w < kLineWarps; w++) { v += m.acc[w][jj]; m.acc[w][jj] = 0.0f; }
-      const float emid = 0.5f * (m.eff[jj].x + m.eff[jj + 1].x);
-      const float pv = v / emid;
-      prof[pbase + z * zstride + tlo + jj] = pv;
-      part += (double) pv;
+    for (int b = 0; b < TILE / kSumBins; b++) {
+      const int jj = b * kSumBins + tid;
+      double part = 0.0;
+      if (jj < thi - tlo) {
+        float v = 0.0f;
+#pragma unroll
+        for (int w = 0; w < kLineWarps; w++) { v += m.acc[w][jj]; m.acc[w][jj] = 0.0f; }
+        const float emid = 0.5f * (m.eff[jj].x + m.eff[jj + 1].x);
+        const float pv = v / emid;
+        prof[pbase + z * zstride + tlo + jj] = pv;
+        part = (double) pv;
+      }
+      const double zs = block_sum_d<kLineThreads>(part, m.red_sum);
+      if (tid == 0 && b * kSumBins < thi - tlo) tsum[((size_t) set * nblk + tile * (TILE / kSumBins) + b) * nza + z] = zs;
     }
-    const double zs = block_sum_d<kLineThreads>(part, m.red_sum);
-    if (tid == 0) tsum[((size_t) set * ntile_max + tile) * nza + z] = zs;
     __syncthreads();
   }
 }
@@ -526,32 +539,49 @@ __global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, c
   }
 }
 
-size_t line_smem_bytes(int nr, int ng, bool limb) {
-  return limb ? sizeof(LineSmem<true>) + sizeof(TW<true>) * (size_t) (nr * ng - 1)
-              : sizeof(LineSmem<false>) + sizeof(TW<false>) * (size_t) (nr * ng - 1);
+template <bool LIMB, int TILE>
+static size_t line_smem_t(int nr, int ng) {
+  return sizeof(LineSmem<LIMB, TILE>) + sizeof(TW<LIMB>) * (size_t) (nr * ng - 1);
+}
+size_t line_smem_bytes(int nr, int ng, bool limb, int tile) {
+  if (tile == 256) return limb ? line_smem_t<true, 256>(nr, ng) : line_smem_t<false, 256>(nr, ng);
+  return limb ? line_smem_t<true, 512>(nr, ng) : line_smem_t<false, 512>(nr, ng);
 }
 size_t hist_smem_bytes(int nr, int ng) { return sizeof(HistSmem) + sizeof(float4) * (size_t) (nr * ng - 1); }
 
-cudaError_t relline_set_smem(size_t bytes_nolimb, size_t bytes_limb, size_t bytes_hist) {
-  cudaError_t e = cudaFuncSetAttribute(relline_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int) bytes_nolimb);
+cudaError_t relline_set_smem(int nr, int ng) {
+  cudaError_t e;
+#define SET(L, T)                                                                                          \
+  e = cudaFuncSetAttribute(relline_kernel<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,             \
+                           (int) line_smem_t<L, T>(nr, ng));                                               \
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(relline_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes_limb);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes_hist);
+  SET(false, 256) SET(true, 256) SET(false, 512) SET(true, 512)
+#undef SET
+  return cudaFuncSetAttribute(hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) hist_smem_bytes(nr, ng));
 }
 
-// launches the line profile (both variants: a set runs in the one matching its limb law) and,
-// for relxill models, the emission-angle histogram
-cudaError_t launch_relline(bool hist, dim3 grid, cudaStream_t s, const RelxTables &tab, const RelxSetIn *sin,
-                           const RelxSetState *sst, const RelxRadial *srad, const double *line_e, int nza, float *prof,
-                           float *dist, double *tsum, int ntile_max, bool any_limb) {
-  relline_kernel<false><<<grid, kLineThreads, line_smem_bytes(tab.rel_nr, tab.rel_ng, false), s>>>(
-      tab, sin, sst, srad, line_e, nza, prof, tsum, ntile_max);
-  if (any_limb)
-    relline_kernel<true><<<grid, kLineThreads, line_smem_bytes(tab.rel_nr, tab.rel_ng, true), s>>>(
-        tab, sin, sst, srad, line_e, nza, prof, tsum, ntile_max);
-  if (hist) hist_kernel<<<grid.y, kLineThreads, hist_smem_bytes(tab.rel_nr, tab.rel_ng), s>>>(tab, sst, srad, nza, dist);
+// launches the line profile (both variants: a set runs in the one matching its limb law) with
+// tiles of `tile` bins (256 or 512) and, for relxill models, the emission-angle histogram
+cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream_t s, const RelxTables &tab,
+                           const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
+                           int nza, float *prof, float *dist, double *tsum, bool any_limb) {
+  const int nr = tab.rel_nr, ng = tab.rel_ng;
+  const int ntile = (nblk * kSumBins + tile - 1) / tile;
+  const dim3 grid(ntile, n_sets);
+  if (tile == 256) {
+    relline_kernel<false, 256><<<grid, kLineThreads, line_smem_t<false, 256>(nr, ng), s>>>(tab, sin, sst, srad, line_e,
+                                                                                           nza, prof, tsum, nblk);
+    if (any_limb)
+      relline_kernel<true, 256><<<grid, kLineThreads, line_smem_t<true, 256>(nr, ng), s>>>(tab, sin, sst, srad, line_e,
+                                                                                           nza, prof, tsum, nblk);
+  } else {
+    relline_kernel<false, 512><<<grid, kLineThreads, line_smem_t<false, 512>(nr, ng), s>>>(tab, sin, sst, srad, line_e,
+                                                                                           nza, prof, tsum, nblk);
+    if (any_limb)
+      relline_kernel<true, 512><<<grid, kLineThreads, line_smem_t<true, 512>(nr, ng), s>>>(tab, sin, sst, srad, line_e,
+                                                                                           nza, prof, tsum, nblk);
+  }
+  if (hist) hist_kernel<<<n_sets, kLineThreads, hist_smem_bytes(nr, ng), s>>>(tab, sst, srad, nza, dist);
   return cudaGetLastError();
 }
 

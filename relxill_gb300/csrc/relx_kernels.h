@@ -9,12 +9,12 @@ namespace relx {
 
 constexpr int kSetupThreadsH = 256;
 constexpr int kLineThreadsH = 256;
-constexpr int kLineTileH = 512;
+constexpr int kSumBinsH = 256;   // bins per profile-sum block (tsum)
 constexpr int kConvThreadsH = 256;
 constexpr int kFinThreadsH = 128;
 
 size_t setup_smem_bytes();
-size_t line_smem_bytes(int nr, int ng, bool limb);
+size_t line_smem_bytes(int nr, int ng, bool limb, int tile);
 size_t hist_smem_bytes(int nr, int ng);
 size_t conv_smem_bytes();
 size_t fin_smem_bytes();
@@ -22,10 +22,11 @@ size_t fin_smem_bytes();
 __global__ void setup_kernel(RelxTables tab, int model, const RelxSetIn *sin, const double *user_e, double *line_e,
                              RelxSetState *sout, RelxRadial *rout, RelxCorners *cout, RelxZoneCorners *zcout);
 
-cudaError_t relline_set_smem(size_t bytes_nolimb, size_t bytes_limb, size_t bytes_hist);
-cudaError_t launch_relline(bool hist, dim3 grid, cudaStream_t s, const RelxTables &tab, const RelxSetIn *sin,
-                           const RelxSetState *sst, const RelxRadial *srad, const double *line_e, int nza, float *prof,
-                           float *dist, double *tsum, int ntile_max, bool any_limb);
+cudaError_t relline_set_smem(int nr, int ng);
+// tile: energy bins per line-kernel CTA (256 or 512); nblk: 256-bin profile-sum blocks per set
+cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream_t s, const RelxTables &tab,
+                           const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
+                           int nza, float *prof, float *dist, double *tsum, bool any_limb);
 
 cudaError_t xillver_set_smem(int n_incl);
 // order: the sets in visiting order (launch_xill_order), or null for batch order

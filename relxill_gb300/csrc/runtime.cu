@@ -464,9 +464,29 @@ struct Context {
   RelCache cache;         // line-profile cache (off until relx_cache_config)
   cudaStream_t aux[2] = {nullptr, nullptr};      // streams of pipelined chunks
   cudaEvent_t aux_ev[2] = {nullptr, nullptr}, fork_ev = nullptr;
+  // CUDA graphs of recent batch shapes (replayed when the shape and workspace recur)
+  struct GraphEntry {
+    std::vector<uintptr_t> key;
+    cudaGraphExec_t exec = nullptr;
+    int kernels = 0;
+    uint64_t used = 0;
+  };
+  std::vector<GraphEntry> graphs;
+  std::vector<std::vector<uintptr_t>> graph_seen;  // shapes launched once (captured on the second launch)
+  uint64_t graph_clock = 0;
+  bool graphs_on = true;
+  // autotuned line tile and chunking per (model, batch-size class, zones)
+  struct TuneEntry {
+    int model, sclass, nza, line_tile, chunk;
+    double ms[4];
+  };
+  std::vector<TuneEntry> tune;
+  bool autotune_on = true;
   cudaEvent_t cache_ev = nullptr;  // recorded after the last batch's cache store
   bool cache_ev_valid = false;
 };
+
+static void graphs_clear(Context &C);
 
 static Context &ctx() {
   static Context *c = new Context();
@@ -475,8 +495,7 @@ static Context &ctx() {
 
 static int set_kernel_attrs(const Tables &T) {
   RELX_CUDA(cudaFuncSetAttribute(setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) setup_smem_bytes()));
-  RELX_CUDA(relline_set_smem(line_smem_bytes(T.d.rel_nr, T.d.rel_ng, false), line_smem_bytes(T.d.rel_nr, T.d.rel_ng, true),
-                             hist_smem_bytes(T.d.rel_nr, T.d.rel_ng)));
+  RELX_CUDA(relline_set_smem(T.d.rel_nr, T.d.rel_ng));
   RELX_CUDA(xillver_set_smem(T.d.x_nincl));
   RELX_CUDA(cudaFuncSetAttribute(conv_zone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
   RELX_CUDA(cudaFuncSetAttribute(relconv_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
@@ -498,6 +517,7 @@ static int ensure_init(Context &C, const char *path) {
   if (st) return st;
   C.table_dir = dir;
   RELX_CUDA(C.cache.clear(C.stream));  // cached profiles belong to the previous tables
+  graphs_clear(C);
   if ((st = set_kernel_attrs(C.T))) return st;
   return 0;
 }
@@ -584,7 +604,10 @@ static int prof_collect() {
 }
 
 struct BatchShape {
-  int model, n_sets, nza, ntile_max;
+  int model, n_sets, nza;
+  int nblk;           // 256-bin profile-sum blocks per set
+  int line_tile = 512;  // energy bins per line-kernel CTA (256 or 512)
+  int chunk = 0;      // sets per pipelined chunk (0: one range)
   bool any_limb = false;  // some set uses a limb-darkening law (relline / relconv limb parameter)
   int64_t n_edges;  // total energy edges
 };
@@ -595,7 +618,7 @@ static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b,
   int st;
   if ((st = W.setin.reserve(S * sizeof(RelxSetIn))) || (st = W.st.reserve(S * sizeof(RelxSetState))) ||
       (st = W.rad.reserve(S * sizeof(RelxRadial))) || (st = W.dist.reserve(S * nza * RELX_MAX_INCL * sizeof(float))) ||
-      (st = W.tsum.reserve(S * b.ntile_max * nza * sizeof(double))) ||
+      (st = W.tsum.reserve(S * b.nblk * nza * sizeof(double))) ||
       (st = W.user_e.reserve(b.n_edges * sizeof(double))) || (st = W.flux.reserve(b.n_edges * sizeof(double))) ||
       (st = W.sflag.reserve(S * sizeof(int))) || (st = W.status.reserve(S * sizeof(int))) ||
       (st = W.err.reserve(sizeof(int))) || (st = W.cslot.reserve(S * sizeof(int))))
@@ -633,7 +656,7 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   RelxZoneCorners *zcor = W.zcorners.p ? W.zcorners.as<RelxZoneCorners>() + base : nullptr;
   float *prof = conv_grid ? W.prof.as<float>() + (size_t) base * nza * RELX_NCONV : W.prof.as<float>();
   float *dist = W.dist.as<float>() + (size_t) base * nza * RELX_MAX_INCL;
-  double *tsum = W.tsum.as<double>() + (size_t) base * b.ntile_max * nza;
+  double *tsum = W.tsum.as<double>() + (size_t) base * b.nblk * nza;
   float *xill = W.xill.p ? W.xill.as<float>() + (size_t) base * nza * tab.x_nener_pad : nullptr;
   float *cout = W.cout.p ? W.cout.as<float>() + (size_t) base * nza * RELX_NCONV : nullptr;
   int *sflag = W.sflag.as<int>() + base;
@@ -648,17 +671,17 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     ProfScope ps(PK_SETUP, s, 2);
     if (C.cache_ev_valid) RELX_CUDA(cudaStreamWaitEvent(s, C.cache_ev, 0));
     RELX_CUDA(cache_lookup(C.cache, s, sin, sst, n, W.cslot.as<int>() + base));
-    RELX_CUDA(cache_fill(C.cache, s, sst, W.cslot.as<int>() + base, n, b.nza, b.ntile_max, kLineTileH, prof, tsum,
+    RELX_CUDA(cache_fill(C.cache, s, sst, W.cslot.as<int>() + base, n, b.nza, b.nblk, kSumBinsH, prof, tsum,
                          dist));
   }
   {
     ProfScope ps(PK_LINE, s, 1 + (b.any_limb ? 1 : 0) + (b.model >= RELX_RELXILL ? 1 : 0));
-    RELX_CUDA(launch_relline(b.model >= RELX_RELXILL, dim3(b.ntile_max, n), s, tab, sin, sst, rad,
-                             W.line_e.as<double>(), b.nza, prof, dist, tsum, b.ntile_max, b.any_limb));
+    RELX_CUDA(launch_relline(b.model >= RELX_RELXILL, n, b.line_tile, b.nblk, s, tab, sin, sst, rad,
+                             W.line_e.as<double>(), b.nza, prof, dist, tsum, b.any_limb));
   }
   if (cached) {
     ProfScope ps(PK_LINE, s);
-    RELX_CUDA(cache_store(C.cache, s, sin, sst, W.cslot.as<int>() + base, n, b.nza, b.ntile_max, kLineTileH, prof,
+    RELX_CUDA(cache_store(C.cache, s, sin, sst, W.cslot.as<int>() + base, n, b.nza, b.nblk, kSumBinsH, prof,
                           tsum, dist));
     if (!C.cache_ev) RELX_CUDA(cudaEventCreateWithFlags(&C.cache_ev, cudaEventDisableTiming));
     RELX_CUDA(cudaEventRecord(C.cache_ev, s));
@@ -673,8 +696,8 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     }
     {
       ProfScope ps(PK_CONV, s);
-      conv_zone_kernel<<<dim3(b.nza, n), kConvThreadsH, conv_smem_bytes(), s>>>(tab, sst, prof, tsum, b.ntile_max,
-                                                                              kLineTileH, xill, b.nza, cout);
+      conv_zone_kernel<<<dim3(b.nza, n), kConvThreadsH, conv_smem_bytes(), s>>>(tab, sst, prof, tsum, b.nblk,
+                                                                              kSumBinsH, xill, b.nza, cout);
     }
     {
       ProfScope ps(PK_FIN, s);
@@ -682,13 +705,13 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     }
   } else if (b.model == RELX_RELCONV) {
     ProfScope ps(PK_CONV, s, 2);  // convolution and finalize
-    relconv_conv_kernel<<<n, kConvThreadsH, conv_smem_bytes(), s>>>(tab, sin, sst, prof, tsum, b.ntile_max,
-                                                                    kLineTileH, b.nza, user_e, W.user_f.as<double>(),
+    relconv_conv_kernel<<<n, kConvThreadsH, conv_smem_bytes(), s>>>(tab, sin, sst, prof, tsum, b.nblk,
+                                                                    kSumBinsH, b.nza, user_e, W.user_f.as<double>(),
                                                                     cout, sflag);
     finalize_relconv_kernel<<<n, kFinThreadsH, 0, s>>>(tab, sin, sst, cout, b.nza, user_e, sflag, flux);
   } else {
     ProfScope ps(PK_FIN, s);
-    finalize_relline_kernel<<<n, kFinThreadsH, 0, s>>>(sin, sst, prof, tsum, b.ntile_max, kLineTileH, b.nza, flux);
+    finalize_relline_kernel<<<n, kFinThreadsH, 0, s>>>(sin, sst, prof, tsum, b.nblk, kSumBinsH, b.nza, flux);
   }
   {
     ProfScope ps(PK_STATUS, s);
@@ -706,14 +729,12 @@ static int chunk_sets() {
   return v ? std::max(0, std::atoi(v)) : 0;
 }
 
-// cache: the line-profile cache, whose steps are ordered after the previous batch's cache store
-// (C.cache_ev), so batches on different streams never read a slot while it is written.
-static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStream_t s, bool use_cache) {
-  const bool cached = use_cache && C.cache.enabled() && b.model != RELX_RELLINE;
+// the batch as launched, without graphs
+static int launch_direct(Context &C, Workspace &W, const BatchShape &b, cudaStream_t s, bool cached) {
   const int S = b.n_sets;
   RELX_CUDA(cudaMemsetAsync(W.sflag.p, 0, S * sizeof(int), s));
   RELX_CUDA(cudaMemsetAsync(W.err.p, 0, sizeof(int), s));
-  const int chunk = chunk_sets();
+  const int chunk = b.chunk;
   if (cached || chunk <= 0 || S < 2 * chunk) return launch_range(C, W, b, s, 0, S, cached);
   for (int k = 0; k < 2; k++) {
     if (!C.aux[k]) RELX_CUDA(cudaStreamCreateWithFlags(&C.aux[k], cudaStreamNonBlocking));
@@ -733,6 +754,138 @@ static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   return 0;
 }
 
+static std::vector<uintptr_t> graph_key(const Workspace &W, const BatchShape &b) {
+  std::vector<uintptr_t> k = {(uintptr_t) b.model, (uintptr_t) b.n_sets, (uintptr_t) b.nza, (uintptr_t) b.nblk,
+                              (uintptr_t) b.line_tile, (uintptr_t) b.chunk, (uintptr_t) b.any_limb,
+                              (uintptr_t) b.n_edges};
+  for (const DevBuf *d : {&W.setin, &W.st, &W.rad, &W.corners, &W.zcorners, &W.line_e, &W.prof, &W.dist, &W.tsum,
+                          &W.xill, &W.cout, &W.user_e, &W.user_f, &W.flux, &W.sflag, &W.status, &W.err, &W.order})
+    k.push_back((uintptr_t) d->p);
+  return k;
+}
+
+static void graphs_clear(Context &C) {
+  for (auto &g : C.graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  C.graphs.clear();
+  C.graph_seen.clear();
+}
+
+// cache: the line-profile cache, whose steps are ordered after the previous batch's cache store
+// (C.cache_ev), so batches on different streams never read a slot while it is written.
+// Without the cache and without per-kernel profiling, the kernel sequence of a batch is captured
+// into a CUDA graph on its first launch and replayed whenever the same shape meets the same
+// workspace buffers (a sampler or fit that evaluates the same number of sets on the same grids
+// every step).
+static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStream_t s, bool use_cache) {
+  const bool cached = use_cache && C.cache.enabled() && b.model != RELX_RELLINE;
+  if (cached || g_prof.on || !C.graphs_on || s == nullptr) return launch_direct(C, W, b, s, cached);
+  const std::vector<uintptr_t> key = graph_key(W, b);
+  for (auto &g : C.graphs) {
+    if (g.key == key) {
+      g.used = ++C.graph_clock;
+      g_launches += g.kernels;
+      RELX_CUDA(cudaGraphLaunch(g.exec, s));
+      return 0;
+    }
+  }
+  // capture only shapes that recur: the first launch of a shape runs directly
+  if (std::find(C.graph_seen.begin(), C.graph_seen.end(), key) == C.graph_seen.end()) {
+    if (C.graph_seen.size() >= 32) C.graph_seen.erase(C.graph_seen.begin());
+    C.graph_seen.push_back(key);
+    return launch_direct(C, W, b, s, false);
+  }
+  const int64_t l0 = g_launches.load();
+  RELX_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  const int st = launch_direct(C, W, b, s, false);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s, &graph);
+  if (st || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    if (st) return st;
+    g_errmsg = std::string("graph capture: ") + cudaGetErrorString(e);
+    return RELX_ERR_CUDA;
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) {
+    g_errmsg = std::string("graph instantiate: ") + cudaGetErrorString(ei);
+    return RELX_ERR_CUDA;
+  }
+  if (C.graphs.size() >= 16) {  // drop the least recently used
+    auto lru = std::min_element(C.graphs.begin(), C.graphs.end(),
+                                [](const Context::GraphEntry &a, const Context::GraphEntry &c) { return a.used < c.used; });
+    cudaGraphExecDestroy(lru->exec);
+    C.graphs.erase(lru);
+  }
+  Context::GraphEntry g;
+  g.key = key;
+  g.exec = exec;
+  g.kernels = (int) (g_launches.load() - l0);
+  g.used = ++C.graph_clock;
+  C.graphs.push_back(g);
+  RELX_CUDA(cudaGraphLaunch(exec, s));
+  return 0;
+}
+
+// Autotuner: the first batch of a (model, batch-size class, zone count) runs once with every
+// candidate of (line tile, pipelined chunk) and keeps the fastest; later batches of the class use
+// it.  Every candidate gives the same numbers (the profile sums are per 256-bin block whatever the
+// tile, and the chunks only reorder independent sets), so the last trial's results stand.  The
+// trials synchronise the stream.
+static int tuned_launch(Context &C, Workspace &W, BatchShape &b, cudaStream_t s, bool use_cache) {
+  const bool cached = use_cache && C.cache.enabled() && b.model != RELX_RELLINE;
+  const char *tile_env = std::getenv("RELX_LINE_TILE");
+  if (tile_env) b.line_tile = std::atoi(tile_env) == 256 ? 256 : 512;  // explicit choice
+  const bool explicit_choice = tile_env || std::getenv("RELX_CHUNK_SETS") != nullptr;
+  if (!C.autotune_on || g_prof.on || cached || explicit_choice || b.model == RELX_RELLINE)
+    return launch_batch(C, W, b, s, use_cache);
+  int sclass = 0;
+  while ((1 << (sclass + 1)) <= b.n_sets) sclass++;
+  for (auto &t : C.tune) {
+    if (t.model == b.model && t.sclass == sclass && t.nza == b.nza) {
+      b.line_tile = t.line_tile;
+      b.chunk = t.chunk;
+      return launch_batch(C, W, b, s, use_cache);
+    }
+  }
+  struct Cand { int tile, chunk; };
+  std::vector<Cand> cands = {{512, 0}, {256, 0}};
+  if (b.n_sets >= 2048) cands.push_back({512, 1024});
+  cudaEvent_t e0, e1;
+  RELX_CUDA(cudaEventCreate(&e0));
+  RELX_CUDA(cudaEventCreate(&e1));
+  Context::TuneEntry t{b.model, sclass, b.nza, 512, 0, {0, 0, 0, 0}};
+  float best = 1e30f;
+  int st = 0;
+  for (size_t i = 0; i < cands.size() && !st; i++) {
+    b.line_tile = cands[i].tile;
+    b.chunk = cands[i].chunk;
+    cudaEventRecord(e0, s);
+    st = launch_direct(C, W, b, s, false);
+    cudaEventRecord(e1, s);
+    if (!st && cudaEventSynchronize(e1) == cudaSuccess) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      t.ms[i] = ms;
+      if (ms < best) {
+        best = ms;
+        t.line_tile = cands[i].tile;
+        t.chunk = cands[i].chunk;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  C.tune.push_back(t);
+  b.line_tile = t.line_tile;
+  b.chunk = t.chunk;
+  return 0;  // the workspace holds the last trial's results
+}
+
 static int batch_shape(int model, int n_sets, const int64_t *eoff_host, const int *igt_host, const EnvOpts &env,
                        BatchShape *b, bool *need_zc) {
   b->model = model;
@@ -746,9 +899,10 @@ static int batch_shape(int model, int n_sets, const int64_t *eoff_host, const in
     nza = std::max(nza, zones_for(model, igt_host ? igt_host[i] : 0, env.nzones_env));
   }
   b->nza = nza;
+  b->chunk = chunk_sets();
   b->any_limb = (model == RELX_RELLINE || model == RELX_RELCONV);
   const int gmax = (model == RELX_RELLINE) ? maxn : RELX_NCONV;
-  b->ntile_max = (gmax + kLineTileH - 1) / kLineTileH;
+  b->nblk = (gmax + kSumBinsH - 1) / kSumBinsH;
   *need_zc = nza > RELX_ZDENSE;
   return 0;
 }
@@ -813,7 +967,7 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
                                                      hb.igi ? W.igi.as<double>() : nullptr, env.nzones_env, env.flags,
                                                      W.setin.as<RelxSetIn>());
   }
-  if ((st = launch_batch(C, W, b, s, use_cache))) return st;
+  if ((st = tuned_launch(C, W, b, s, use_cache))) return st;
   RELX_CUDA(cudaMemcpyAsync(h + *o_flux, W.flux.p, nflux * sizeof(double), cudaMemcpyDeviceToHost, s));
   RELX_CUDA(cudaMemcpyAsync(h + *o_status, W.status.p, sizeof(int) * n_sets, cudaMemcpyDeviceToHost, s));
   return 0;
@@ -902,7 +1056,7 @@ int slot_wait(BatchSlot *b, const double **flux, const int **status) {
 
 size_t batch_device_bytes(int model, int n_sets, int64_t n_edges, int nza) {
   size_t per_set = sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(RelxRadial) + sizeof(int) * 4 +
-                   sizeof(float) * nza * RELX_MAX_INCL + sizeof(double) * (RELX_NCONV / kLineTileH) * nza;
+                   sizeof(float) * nza * RELX_MAX_INCL + sizeof(double) * (RELX_NCONV / kSumBinsH) * nza;
   if (model != RELX_RELLINE) per_set += 2 * sizeof(float) * (size_t) nza * RELX_NCONV;
   if (model >= RELX_RELXILL) per_set += sizeof(RelxCorners) + sizeof(float) * (size_t) nza * 4096;
   return per_set * (size_t) n_sets + sizeof(double) * 3 * (size_t) n_edges;
@@ -1006,7 +1160,7 @@ int relx_eval_batch_device(int model, int n_sets, const double *d_params, const 
                                                      d_ion_grad_type, d_iongrad_index, env.nzones_env, env.flags,
                                                      W.setin.as<RelxSetIn>());
   }
-  if ((st = launch_batch(C, W, b, s, true))) return st;
+  if ((st = tuned_launch(C, W, b, s, true))) return st;
   RELX_CUDA(cudaMemcpyAsync(d_flux, W.flux.p, sizeof(double) * (b.n_edges - n_sets), cudaMemcpyDeviceToDevice, s));
   if (d_status) RELX_CUDA(cudaMemcpyAsync(d_status, W.status.p, sizeof(int) * n_sets, cudaMemcpyDeviceToDevice, s));
   return 0;
@@ -1054,6 +1208,35 @@ int relx_batch_stats(int n_sets, int64_t *out) {
   return 0;
 }
 
+int relx_tuning_config(int autotune, int graphs) {
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  C.autotune_on = autotune != 0;
+  C.graphs_on = graphs != 0;
+  if (!C.graphs_on) {
+    if (C.stream) cudaStreamSynchronize(C.stream);
+    graphs_clear(C);
+  }
+  return 0;
+}
+
+int relx_tuning_report(double *out, int max) {
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  int n = 0;
+  for (const auto &t : C.tune) {
+    if (n >= max) break;
+    double best = 1e30;
+    for (double m : t.ms)
+      if (m > 0 && m < best) best = m;
+    const double v[6] = {(double) t.model, (double) t.sclass, (double) t.nza, (double) t.line_tile, (double) t.chunk,
+                         best < 1e30 ? best : 0.0};
+    for (int i = 0; i < 6; i++) out[n * 6 + i] = v[i];
+    n++;
+  }
+  return n;
+}
+
 int relx_cache_config(int slots) {
   int st = cache_configure(slots);
   g_last_status = st;
@@ -1087,6 +1270,7 @@ void relx_release(void) {
   Context &C = ctx();
   std::lock_guard<std::mutex> lock(C.mu);
   if (C.stream) cudaStreamSynchronize(C.stream);
+  graphs_clear(C);
   C.W.release();
   C.T.release();
   C.pin.release();

@@ -134,3 +134,28 @@ def test_serve_results_match_batch_alone(gpu):
         assert s["p99_ms"] >= s["p50_ms"] > 0.0
         assert s["batches"] >= 2
     gpu.cache_config(0)
+
+
+def test_tiles_chunks_and_graphs_give_the_same_numbers(gpu, monkeypatch):
+    """Line-kernel tiles of 256 and 512 bins, pipelined chunks and CUDA-graph replay change nothing."""
+    lp = _lp_sets(9, 31)
+    g = _grids(9, 32)
+    gpu.tuning_config(autotune=False, graphs=False)
+    try:
+        want = _batch(gpu, "relxilllp", lp, g)
+        for tile in ("256", "512"):
+            monkeypatch.setenv("RELX_LINE_TILE", tile)
+            for a, b in zip(_batch(gpu, "relxilllp", lp, g), want):
+                np.testing.assert_array_equal(a, b)
+        monkeypatch.delenv("RELX_LINE_TILE")
+        monkeypatch.setenv("RELX_CHUNK_SETS", "2")
+        for a, b in zip(_batch(gpu, "relxilllp", lp, g), want):
+            np.testing.assert_array_equal(a, b)
+        monkeypatch.delenv("RELX_CHUNK_SETS")
+        gpu.tuning_config(autotune=True, graphs=True)
+        for _ in range(3):  # tuning trials, a direct launch, then a captured graph and its replay
+            for a, b in zip(_batch(gpu, "relxilllp", lp, g), want):
+                np.testing.assert_array_equal(a, b)
+        assert any(t["model"] == 3 for t in gpu.tuning_report())
+    finally:
+        gpu.tuning_config(autotune=True, graphs=True)
