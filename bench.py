@@ -176,6 +176,64 @@ def run_serve(R, seconds: float, rate: float, n_walkers: int, budget_gb: float, 
             "xillver_only_steps": 0.7, "identical_to_alone": same, "checked": checked}
 
 
+def run_iongrad(R, L, torch, dev, steps: int, warmup: int, n: int = 2048):
+    """Batched relxilllp with the ALPHA ionisation gradient (IonGradient.cpp:128-171) over 10 zones:
+    2048 sets of the same draws, device buffers, CUDA events on the launching stream."""
+    os.environ["RELXILL_NUM_RZONES"] = "10"
+    try:
+        params, grids = workload(n, seed_params=2027, seed_grids=8)
+        edges, offs = R.pack_grids(grids)
+        nflux = int(offs[-1]) - n
+        igt = np.full(n, 2, dtype=np.int32)
+        d_params = torch.from_numpy(params).to(dev)
+        d_e = torch.from_numpy(edges).to(dev)
+        d_off = torch.from_numpy(offs).to(dev)
+        d_igt = torch.from_numpy(igt).to(dev)
+        d_igi = torch.zeros(n, dtype=torch.float64, device=dev)
+        d_flux = torch.empty(nflux, dtype=torch.float64, device=dev)
+        d_status = torch.empty(n, dtype=torch.int32, device=dev)
+        stream = torch.cuda.Stream(device=dev)
+        offs_ptr = offs.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        igt_ptr = igt.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+        def step():
+            st = L.relx_eval_batch_device(3, n, d_params.data_ptr(), d_e.data_ptr(), d_off.data_ptr(), offs_ptr, None,
+                                          d_flux.data_ptr(), d_status.data_ptr(), d_igt.data_ptr(), igt_ptr,
+                                          d_igi.data_ptr(), stream.cuda_stream)
+            if st:
+                raise RuntimeError(f"relx_eval_batch_device: {st} {R.last_error()}")
+
+        for _ in range(warmup):
+            step()
+        torch.cuda.synchronize()
+        assert int((d_status != 0).sum()) == 0
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            ev0.record()
+        for _ in range(steps):
+            step()
+        with torch.cuda.stream(stream):
+            ev1.record()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        out = d_flux.cpu().numpy()
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+
+        max_err = 0.0
+        for i in range(2):
+            st, ref = oracle_lib.evaluate("relxilllp", params[i], grids[i], None, 2, 0.0)
+            got = out[offs[i] - i: offs[i + 1] - i - 1]
+            m = ref > 1e-6 * ref.max()
+            max_err = max(max_err, float(np.max(np.abs(got[m] / ref[m] - 1))))
+        return {"value": n * steps / (ms / 1e3), "unit": "spectra/s", "sets": n, "zones": 10, "steps": steps,
+                "ms_per_step": ms / steps, "mode": "ALPHA ionisation gradient (IonGradient.cpp:128-171)",
+                "max_rel_err_vs_oracle": max_err}
+    finally:
+        os.environ.pop("RELXILL_NUM_RZONES", None)
+
+
 def tables(kind: str = "full") -> str:
     from relxill_gb300 import synth_tables
 
@@ -470,6 +528,10 @@ def run_gpu(args):
         cpu = {"value": r, "unit": "spectra/s", "cores": procs, "kind": "port",
                "sample": f"{len(idx)} sets of the workload on {procs} spawned processes ({dt:.1f} s)"}
 
+    iongrad = None
+    if not args.no_iongrad:
+        iongrad = run_iongrad(R, L, torch, dev, args.steps, args.warmup)
+
     serve = None
     if not args.no_serve:
         serve = run_serve(R, args.serve_seconds, args.serve_rate, args.walkers, args.serve_budget_gb)
@@ -521,7 +583,7 @@ def run_gpu(args):
         "roofline": roof, "dominant_kernel": names[dom],
         "dominant_kernel_bound": "FP32 ALU issue (line profile: Romberg g*-integration; see profiles/)",
         "kernels": kernels, "cpu_baseline": cpu,
-        "serve": serve,
+        "serve": serve, "ion_gradient": iongrad,
     }
     print(json.dumps(line))
     if dist is not None:
@@ -541,6 +603,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-iongrad", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-rate", type=float, default=50000.0)
     ap.add_argument("--walkers", type=int, default=256)

@@ -837,20 +837,23 @@ static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStrea
 // trials synchronise the stream.
 static int tuned_launch(Context &C, Workspace &W, BatchShape &b, cudaStream_t s, bool use_cache) {
   const bool cached = use_cache && C.cache.enabled() && b.model != RELX_RELLINE;
-  const char *tile_env = std::getenv("RELX_LINE_TILE");
-  if (tile_env) b.line_tile = std::atoi(tile_env) == 256 ? 256 : 512;  // explicit choice
-  const bool explicit_choice = tile_env || std::getenv("RELX_CHUNK_SETS") != nullptr;
-  if (!C.autotune_on || g_prof.on || cached || explicit_choice || b.model == RELX_RELLINE)
-    return launch_batch(C, W, b, s, use_cache);
   int sclass = 0;
   while ((1 << (sclass + 1)) <= b.n_sets) sclass++;
-  for (auto &t : C.tune) {
-    if (t.model == b.model && t.sclass == sclass && t.nza == b.nza) {
-      b.line_tile = t.line_tile;
-      b.chunk = t.chunk;
-      return launch_batch(C, W, b, s, use_cache);
-    }
+  const Context::TuneEntry *known = nullptr;
+  for (const auto &t : C.tune)
+    if (t.model == b.model && t.sclass == sclass && t.nza == b.nza) known = &t;
+  const char *tile_env = std::getenv("RELX_LINE_TILE");
+  const bool explicit_choice = tile_env || std::getenv("RELX_CHUNK_SETS") != nullptr;
+  if (tile_env) {
+    b.line_tile = std::atoi(tile_env) == 256 ? 256 : 512;  // explicit choice
+  } else if (known) {
+    b.line_tile = known->line_tile;
+    if (!cached && b.chunk == 0) b.chunk = known->chunk;
+  } else {
+    b.line_tile = b.n_sets <= 1024 ? 256 : 512;  // small batches: more CTAs per set
   }
+  if (known || !C.autotune_on || g_prof.on || cached || explicit_choice || b.model == RELX_RELLINE)
+    return launch_batch(C, W, b, s, use_cache);
   struct Cand { int tile, chunk; };
   std::vector<Cand> cands = {{512, 0}, {256, 0}};
   if (b.n_sets >= 2048) cands.push_back({512, 1024});
