@@ -371,9 +371,9 @@ def run_gpu(args):
 
     import relxill_gb300 as R
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from relxill_gb300 import replicas
+
+    rank, world, local = replicas.rank_info()
     torch.cuda.set_device(local)
     dist = None
     if world > 1:
@@ -397,7 +397,8 @@ def run_gpu(args):
     L.relx_table_bytes(ctypes.byref(tb))
 
     S = args.sets
-    params, grids = workload(S, seed_params=2026 + rank, seed_grids=7 + rank)
+    seed_p, seed_g = replicas.rank_seeds(rank)
+    params, grids = workload(S, seed_params=seed_p, seed_grids=seed_g)
     edges, offs = R.pack_grids(grids)
     nflux = int(offs[-1]) - S
     dev = torch.device("cuda", local)
@@ -456,11 +457,8 @@ def run_gpu(args):
     n_k = (ctypes.c_int64 * 7)()
     L.relx_profile_read(ms_k, n_k, 7)
     L.relx_profile_enable(0)
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * S * args.steps / (ms / 1e3)
+    ms = replicas.max_over_ranks(ms, dist, dev)
+    value = replicas.job_throughput(S, args.steps, world, ms / 1e3)
 
     # end-to-end through the host-buffer C ABI (copies in the timed region)
     e2e = None
@@ -479,12 +477,8 @@ def run_gpu(args):
             rc = L.relx_eval_batch(3, S, pp, ep, offs_ptr, None, fp, sp, None, None)
             assert rc == 0
         t1 = time.perf_counter()
-        dt = t1 - t0
-        if dist is not None:
-            t = torch.tensor([dt], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
-        e2e = {"value": world * S * args.steps / dt, "unit": "spectra/s",
+        dt = replicas.max_over_ranks(t1 - t0, dist, dev)
+        e2e = {"value": replicas.job_throughput(S, args.steps, world, dt), "unit": "spectra/s",
                "h2d_bytes_per_step": int(params.nbytes + edges.nbytes + offs.nbytes),
                "d2h_bytes_per_step": int(flux.nbytes + status.nbytes)}
 

@@ -140,6 +140,12 @@ int relx_serve_stats(relx_server *s, double *out, int n, int reset);
 /* Finish the queued requests and stop the engine. */
 void relx_serve_destroy(relx_server *s);
 
+/* Self-test of the bounded waits of the TMA pipeline (no counterpart in the
+ * reference): one kernel waits, with a limit of limit_ms (at most 1000), on an
+ * mbarrier that nothing completes and reports the status it saw in *status
+ * (RELX_ERR_TIMEOUT).  No copy is issued; the context stays usable. */
+int relx_selftest_wait_timeout(double limit_ms, int *status);
+
 /* Launch tuning (no counterpart in the reference).  autotune != 0: the first
  * batch of a (model, batch-size class, zone count) is run once per candidate
  * of (line-kernel tile of 256 or 512 bins, pipelined chunks of 1024 sets) and

@@ -1211,6 +1211,22 @@ int relx_batch_stats(int n_sets, int64_t *out) {
   return 0;
 }
 
+int relx_selftest_wait_timeout(double limit_ms, int *status) {
+  if (!status || !(limit_ms > 0.0) || limit_ms > 1000.0) return RELX_ERR_ARG;
+  Context &C = ctx();
+  std::lock_guard<std::mutex> lock(C.mu);
+  int *d = nullptr;
+  RELX_CUDA(cudaMalloc(&d, sizeof(int)));
+  cudaError_t e = launch_wait_selftest(nullptr, (unsigned long long) (limit_ms * 1e6), d);
+  if (e == cudaSuccess) e = cudaMemcpy(status, d, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    g_errmsg = std::string("wait self-test: ") + cudaGetErrorString(e);
+    return RELX_ERR_CUDA;
+  }
+  return 0;
+}
+
 int relx_tuning_config(int autotune, int graphs) {
   Context &C = ctx();
   std::lock_guard<std::mutex> lock(C.mu);

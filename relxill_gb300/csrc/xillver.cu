@@ -56,14 +56,32 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// bounded wait (about one second, at most 2^24 polls); returns false on timeout
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+// bounded wait (limit_ns, at most 2^24 polls); returns false on timeout
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                  unsigned long long limit_ns = kWaitLimitNs) {
   const unsigned long long t0 = globaltimer_ns();
   for (int it = 0; it < (1 << 24); it++) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 255) == 255 && globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    if ((it & 255) == 255 && globaltimer_ns() - t0 > limit_ns) return false;
   }
   return false;
+}
+
+// Self-test of the timeout path: one thread waits, with a short limit, on an mbarrier that
+// expects 16 bytes no copy will deliver, and reports what the wait returned.  No copy is issued,
+// so nothing is in flight when the CTA exits.
+__global__ void wait_selftest_kernel(unsigned long long limit_ns, int *out) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  mbar_expect_tx(&bar, 16);  // the arrival completes, the 16 transaction bytes never do
+  *out = mbar_wait_bounded(&bar, 0, limit_ns) ? RELX_OK : RELX_ERR_TIMEOUT;
+}
+
+cudaError_t launch_wait_selftest(cudaStream_t s, unsigned long long limit_ns, int *out) {
+  wait_selftest_kernel<<<1, 32, 0, s>>>(limit_ns, out);
+  return cudaGetLastError();
 }
 
 template <int NZ>

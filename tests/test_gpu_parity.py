@@ -130,3 +130,20 @@ def test_relline_normalised_to_one(gpu):
     e = grid(CASES[0][3])
     f = gpu.relline(e, CASES[0][2])
     assert abs(f.sum() - 1.0) < 1e-6
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(gpu):
+    """The TMA pipeline's bounded mbarrier wait gives up after its limit with status 8, without
+    a fault; evaluations work afterwards."""
+    import ctypes
+    import time
+
+    L = gpu.lib()
+    L.relx_selftest_wait_timeout.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
+    st = ctypes.c_int(-1)
+    t0 = time.time()
+    assert L.relx_selftest_wait_timeout(5.0, ctypes.byref(st)) == 0
+    assert st.value == 8
+    assert time.time() - t0 < 10.0
+    e = grid(CASES[7][3])
+    _gpu_eval(gpu, "relxilllp", CASES[7][2], e)
