@@ -448,11 +448,14 @@ def run_gpu(args):
     ms = ev0.elapsed_time(ev1)
     # second timed region of the same steps with every kernel bracketed by CUDA events on its
     # stream (no graph replay while profiling): per-kernel times and the roofline
+    # (one range per batch: with pipelined chunks the kernels of two streams overlap in time)
+    os.environ["RELX_CHUNK_SETS"] = "0"
     L.relx_profile_enable(1)
     torch.cuda.synchronize()
     for _ in range(args.steps):
         step()
     torch.cuda.synchronize()
+    os.environ.pop("RELX_CHUNK_SETS", None)
     ms_k = (ctypes.c_double * 7)()
     n_k = (ctypes.c_int64 * 7)()
     L.relx_profile_read(ms_k, n_k, 7)

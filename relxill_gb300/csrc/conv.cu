@@ -14,45 +14,60 @@
 // conv_zone_kernel: one CTA per (zone, set), 256 threads x 16 output bins,
 // register-tiled (16 x 16 products per 47 shared-memory loads).
 #include "relx_device.cuh"
+#include "relx_tma.cuh"
 
 namespace relx {
 
 constexpr int kConvThreads = 256;  // convolution kernels
 constexpr int kFinThreads = 128;   // finalize kernels
 constexpr int kConvR = 16;         // output bins per thread and work item
+constexpr int kConvD = 16;         // window bins per step of the register tile
 constexpr int kN = RELX_NCONV;
 constexpr int kPre = 4;            // prefix sums are kept at every kPre-th bin
+constexpr int kXStage = 3072;      // xillver bins staged in shared memory (larger tables read global memory)
 static_assert(kN % (kConvThreads * kPre) == 0, "scan tiling");
 
 __device__ __forceinline__ int skew(int m) { return m + (m >> 4); }
 
 struct ConvSmem {
   float xs[kN + kN / 16];      // x * cf, skewed
-  float hr[kN + kConvR];       // rel * cf over the zone's profile window, zero padded
+  float hr[kN + kConvR];       // rel * cf over the zone's profile window, zero padded (16-byte aligned)
   float2 pre[kN / kPre + 1];   // float-float prefix sums of xs at bins 0, kPre, 2 kPre, ...
   float2 red[kConvThreads / 32 + 2];
   float2 wsum[kConvThreads / 32];
   double dred[kConvThreads / 32 + 2];
   double zsum[RELX_NZMAX];
   float bc[2];                 // broadcast scalars
+  int abort_flag;
+  uint64_t bar;                // completion of the bulk copy of the zone's xillver spectrum
+  alignas(16) float xz[kXStage];  // the zone's xillver spectrum (bulk copy)
 };
+static_assert(offsetof(ConvSmem, hr) % 16 == 0, "the profile window is read as float4");
 
 // y[k0 + r] = sum_{i in [clo, chi)} hr[i - wlo] * xs[(k0 + r + p - i) mod N]; hr is zero padded
-// past the window, so chi - clo need not be a multiple of kConvR
+// past the window, so chi - clo need not be a multiple of kConvD.  Register tile: kConvR outputs x
+// kConvD window bins per step, kConvR + kConvD - 1 loads of xs and kConvD/4 float4 loads of hr for
+// kConvR * kConvD FMAs.
 __device__ __forceinline__ void conv_tile(const ConvSmem &m, int k0, int p, int wlo, int clo, int chi,
                                           float y[kConvR]) {
 #pragma unroll
   for (int r = 0; r < kConvR; r++) y[r] = 0.0f;
-  for (int i0 = clo; i0 < chi; i0 += kConvR) {
-    const int base = k0 + p - i0 - (kConvR - 1);
-    float xr[2 * kConvR - 1];
+  for (int i0 = clo; i0 < chi; i0 += kConvD) {
+    const int base = k0 + p - i0 - (kConvD - 1);
+    float xr[kConvR + kConvD - 1];
 #pragma unroll
-    for (int c = 0; c < 2 * kConvR - 1; c++) xr[c] = m.xs[skew((base + c) & (kN - 1))];
+    for (int c = 0; c < kConvR + kConvD - 1; c++) xr[c] = m.xs[skew((base + c) & (kN - 1))];
+    const float4 *h4 = reinterpret_cast<const float4 *>(&m.hr[i0 - wlo]);
 #pragma unroll
-    for (int d = 0; d < kConvR; d++) {
-      const float h = m.hr[i0 - wlo + d];
+    for (int d4 = 0; d4 < kConvD / 4; d4++) {
+      const float4 hv = h4[d4];
+      const float hs[4] = {hv.x, hv.y, hv.z, hv.w};
 #pragma unroll
-      for (int r = 0; r < kConvR; r++) y[r] = fmaf(h, xr[r - d + kConvR - 1], y[r]);
+      for (int e = 0; e < 4; e++) {
+        const int d = d4 * 4 + e;
+#pragma unroll
+        for (int r = 0; r < kConvR; r++) y[r] = fmaf(hs[e], xr[r - d + kConvD - 1], y[r]);
+      }
     }
   }
 }
@@ -168,13 +183,13 @@ __device__ void conv_normalize_store(ConvSmem &m, const RelxTables &tab, int wlo
   // in adjacent lanes and are added by a fixed shuffle tree, so the result depends only on this
   // set's own sizes.
   const int nt = (ohi - olo + 1 + kConvR - 1) / kConvR;
-  const int nc = (whi - wlo + kConvR - 1) / kConvR;
+  const int nc = (whi - wlo + kConvD - 1) / kConvD;
   int S = 1, best = split_cost(nt, nc, 1);
   for (int c = 2; c <= 32 && c <= nc; c <<= 1) {
     const int cost = split_cost(nt, nc, c);
     if (cost < best) { best = cost; S = c; }
   }
-  const int seg = ((nc + S - 1) / S) * kConvR;  // window bins per segment
+  const int seg = ((nc + S - 1) / S) * kConvD;  // window bins per segment
   const int nitems = nt * S;
   for (int q0 = 0; q0 < nitems; q0 += kConvThreads) {
     const int q = q0 + tid;
@@ -205,7 +220,7 @@ __global__ void __launch_bounds__(kConvThreads) conv_zone_kernel(RelxTables tab,
                                                                  const float *__restrict__ prof,
                                                                  const double *__restrict__ tsum, int ntile_max,
                                                                  int tile_bins, const float *__restrict__ xill, int nza,
-                                                                 float *__restrict__ cout) {
+                                                                 float *__restrict__ cout, int *__restrict__ err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ConvSmem &m = *reinterpret_cast<ConvSmem *>(smem_raw);
   const int z = blockIdx.x, set = blockIdx.y, tid = threadIdx.x;
@@ -221,6 +236,17 @@ __global__ void __launch_bounds__(kConvThreads) conv_zone_kernel(RelxTables tab,
   const int wlo = s.zw_lo[z], whi = s.zw_hi[z];  // the zone's profile is zero outside
   const float fscale = m.bc[0];
   const float *pz = prof + ((size_t) set * nza + z) * kN;
+  // the zone's xillver spectrum: one bulk copy into shared memory, overlapped with the profile loads
+  const float *xz = xill + ((size_t) set * nza + z) * tab.x_nener_pad;
+  // bulk copies need 16-byte aligned rows of a 16-byte multiple (the loader pads rows to 4 floats)
+  const bool staged = tab.x_nener_pad <= kXStage && (tab.x_nener_pad & 3) == 0 && (((uintptr_t) xz) & 15) == 0;
+  if (staged && tid == 0) {
+    m.abort_flag = 0;
+    mbar_init(&m.bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_expect_tx(&m.bar, (uint32_t) tab.x_nener_pad * 4u);
+    bulk_g2s(m.xz, xz, (uint32_t) tab.x_nener_pad * 4u, &m.bar);
+  }
   // relline profile weighted by E/dE over its window; band sum of the profile
   float2 pr = make_float2(0.0f, 0.0f);
   for (int i = tid; i < whi - wlo + kConvR; i += kConvThreads) {
@@ -233,18 +259,32 @@ __global__ void __launch_bounds__(kConvThreads) conv_zone_kernel(RelxTables tab,
     }
     m.hr[i] = v;
   }
+  if (staged) {
+    __syncthreads();  // the barrier is initialised
+    if (!mbar_wait_bounded(&m.bar, 0)) atomicExch(&m.abort_flag, 1);
+    __syncthreads();
+    if (m.abort_flag) {
+      if (tid == 0) {
+        (void) mbar_wait_bounded(&m.bar, 0);  // give the copy in flight another bounded wait
+        atomicExch(err, RELX_ERR_TIMEOUT);
+      }
+      return;
+    }
+  }
+  const float *xs_src = staged ? m.xz : xz;
   // xillver spectrum of the zone rebinned onto the conv grid (_rebin_spectrum, relutility.c:549-601)
-  const float *xz = xill + ((size_t) set * nza + z) * tab.x_nener_pad;
   float2 px = make_float2(0.0f, 0.0f);
   for (int j = tid; j < kN; j += kConvThreads) {
-    const int i0 = tab.rb_imin[j], i1 = tab.rb_imax[j];
+    const int4 rb = tab.rb_pack[j];  // first and last xillver bin, end fractions
+    const int i0 = rb.x, i1 = rb.y;
     float v = 0.0f;
     if (i0 >= 0) {
+      const float fmin = __int_as_float(rb.z), fmax = __int_as_float(rb.w);
       if (i0 == i1) {
-        v = tab.rb_fmin[j] * xz[i0];
+        v = fmin * xs_src[i0];
       } else {
-        v = xz[i0] * tab.rb_fmin[j] + xz[i1] * tab.rb_fmax[j];
-        for (int q = i0 + 1; q <= i1 - 1; q++) v += xz[q];
+        v = xs_src[i0] * fmin + xs_src[i1] * fmax;
+        for (int q = i0 + 1; q <= i1 - 1; q++) v += xs_src[q];
       }
     }
     if (j >= tab.conv_band_lo && j <= tab.conv_band_hi) px = ff_addf(px, v);
@@ -347,12 +387,13 @@ __device__ __forceinline__ double rebin_bin(const RelxTables &tab, double elo0, 
   const int imax = conv_index(tab, ehi0);
   const double elo = elo0 < e0[imin] ? e0[imin] : elo0;
   const double ehi = ehi0 > e0[imax + 1] ? e0[imax + 1] : ehi0;
+  // bin widths of the conv grid as floats, (float) (e0[k + 1] - e0[k])
   if (imax == imin) {
-    float fr = (float) (ehi - elo) / (float) (e0[imin + 1] - e0[imin]);
+    float fr = (float) (ehi - elo) / tab.conv_cw[imin].y;
     return (double) (fr * f0[imin]);
   }
-  float dmin = (float) (e0[imin + 1] - elo) / (float) (e0[imin + 1] - e0[imin]);
-  float dmax = (float) (ehi - e0[imax]) / (float) (e0[imax + 1] - e0[imax]);
+  float dmin = (float) (e0[imin + 1] - elo) / tab.conv_cw[imin].y;
+  float dmax = (float) (ehi - e0[imax]) / tab.conv_cw[imax].y;
   float acc = f0[imin] * dmin + f0[imax] * dmax;
   for (int q = imin + 1; q <= imax - 1; q++) acc += f0[q];
   return (double) acc;
@@ -395,8 +436,9 @@ __global__ void __launch_bounds__(kFinThreads) finalize_relxill_kernel(RelxTable
     for (int z = 0; z < s.nz; z++) r += cout[((size_t) set * nza + z) * kN + k];
     r *= rfac;
     if (add_prim) {
-      float en = (float) (0.5 * (ce[k] + ce[k + 1]));
-      float pl = expf(1.0f / ecut) * powf(en, -gam) * expf(-en / ecut) * (float) (ce[k + 1] - ce[k]);
+      const float2 cd = tab.conv_cw[k];  // (float) bin centre, (float) bin width
+      const float en = cd.x;
+      float pl = expf(1.0f / ecut) * powf(en, -gam) * expf(-en / ecut) * cd.y;
       r += pl * pnorm;
     }
     m.spec[k] = r;

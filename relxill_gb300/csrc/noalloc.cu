@@ -212,7 +212,8 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
   if (model >= RELX_RELXILL) {
     NOALLOC_CUDA(launch_xillver(s, tab, 1, nza, p.sst, p.cor, p.zcor, p.dist, p.xill, p.err, nullptr));
     conv_zone_kernel<<<dim3(nza, 1), kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sst, p.prof, p.tsum, ntile_max,
-                                                                            kSumBinsH, p.xill, nza, p.cout);
+                                                                            kSumBinsH, p.xill, nza, p.cout,
+                                                                            p.err);
     finalize_relxill_kernel<<<1, kFinThreadsH, fin_smem_bytes(), s>>>(tab, p.sin, p.sst, p.cout, nza, d_energy, d_flux);
   } else if (model == RELX_RELCONV) {
     relconv_conv_kernel<<<1, kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sin, p.sst, p.prof, p.tsum, ntile_max,

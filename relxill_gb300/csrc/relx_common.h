@@ -80,6 +80,7 @@ struct RelxTables {
   const float2 *conv_eff;    // float-float edges
   const float *conv_inv_emid;  // 1/(0.5(e_j+e_j+1))
   const float *conv_cf;      // 0.5(e_j+e_j+1)/(e_j+1-e_j)  (Relbase.cpp:93-103)
+  const float2 *conv_cw;     // (float) 0.5(e_j+e_j+1), (float) (e_j+1-e_j)
   int conv_pos1;             // binary_search(conv_e, 1.0)  (Relbase.cpp:133-137)
   float conv_lg0, conv_ilg;  // log(conv_e[0]) and N / log(conv_e[N] / conv_e[0]): first guess of a bin index
   int conv_band_lo, conv_band_hi;  // bins with e_j >= 0.01 && e_j+1 < 1000 (Relbase.cpp:205)
@@ -89,6 +90,7 @@ struct RelxTables {
   // rebin map xillver grid -> conv grid (relutility.c:549-601): per conv bin
   const int *rb_imin, *rb_imax;
   const float *rb_fmin, *rb_fmax;  // fractions (single-bin case: rb_fmin, rb_imax == rb_imin)
+  const int4 *rb_pack;       // per conv bin: imin, imax, fmin and fmax as float bits
   const double *x_e;         // xillver edges [x_nener+1] (double of the float table values)
 };
 

@@ -39,7 +39,7 @@ void launch_xill_order(cudaStream_t s, const RelxSetState *sst, const RelxCorner
                        int n_sets, int *order);
 
 __global__ void conv_zone_kernel(RelxTables tab, const RelxSetState *sst, const float *prof, const double *tsum,
-                                 int ntile_max, int tile_bins, const float *xill, int nza, float *cout);
+                                 int ntile_max, int tile_bins, const float *xill, int nza, float *cout, int *err);
 __global__ void relconv_conv_kernel(RelxTables tab, const RelxSetIn *sin, const RelxSetState *sst, const float *prof,
                                     const double *tsum, int ntile_max, int tile_bins, int nza, const double *user_e,
                                     const double *user_f, float *cout, int *sflag);

@@ -104,14 +104,14 @@ struct Tables {
   DevBuf rel_a, rel_mu0, rel_r, rel_gmin, rel_gmax, rel_tc;
   DevBuf lp_a, lp_h, lp_rad, lp_intens, lp_del, lp_delinc;
   DevBuf x_vals, x_spec, x_e;
-  DevBuf conv_e, conv_eff, conv_inv_emid, conv_cf, coarse_e, coarse_t;
-  DevBuf rb_imin, rb_imax, rb_fmin, rb_fmax;
+  DevBuf conv_e, conv_eff, conv_inv_emid, conv_cf, conv_cw, coarse_e, coarse_t;
+  DevBuf rb_imin, rb_imax, rb_fmin, rb_fmax, rb_pack;
   size_t bytes_total = 0;
   bool loaded = false;
   void release() {
     for (DevBuf *b : {&rel_a, &rel_mu0, &rel_r, &rel_gmin, &rel_gmax, &rel_tc, &lp_a, &lp_h, &lp_rad, &lp_intens,
                       &lp_del, &lp_delinc, &x_vals, &x_spec, &x_e, &conv_e, &conv_eff, &conv_inv_emid, &conv_cf,
-                      &coarse_e, &coarse_t, &rb_imin, &rb_imax, &rb_fmin, &rb_fmax})
+                      &conv_cw, &coarse_e, &coarse_t, &rb_imin, &rb_imax, &rb_fmin, &rb_fmax, &rb_pack})
       b->release();
     loaded = false;
   }
@@ -352,6 +352,7 @@ static int load_tables(const std::string &dir, Tables &T) {
   log_grid(ce, RELX_NCONV + 1, RELX_EMIN_CONV, RELX_EMAX_CONV);
   std::vector<float2> ceff(ce.size());
   std::vector<float> inv_emid(RELX_NCONV), cf(RELX_NCONV);
+  std::vector<float2> cw(RELX_NCONV);
   for (size_t i = 0; i < ce.size(); i++) {
     float hi = (float) ce[i];
     ceff[i] = make_float2(hi, (float) (ce[i] - (double) hi));
@@ -360,6 +361,7 @@ static int load_tables(const std::string &dir, Tables &T) {
   for (int j = 0; j < RELX_NCONV; j++) {
     inv_emid[j] = (float) (1.0 / (0.5 * (ce[j] + ce[j + 1])));
     cf[j] = (float) (0.5 * (ce[j] + ce[j + 1]) / (ce[j + 1] - ce[j]));  // Relbase.cpp:93-103
+    cw[j] = make_float2((float) (0.5 * (ce[j] + ce[j + 1])), (float) (ce[j + 1] - ce[j]));
     if (ce[j] >= RELX_EMIN_XILL && ce[j + 1] < RELX_EMAX_XILL) {   // Relbase.cpp:205
       band_lo = std::min(band_lo, j);
       band_hi = std::max(band_hi, j);
@@ -383,14 +385,22 @@ static int load_tables(const std::string &dir, Tables &T) {
   std::vector<int> imn, imx;
   std::vector<float> fmn, fmx;
   rebin_map(ce, xe, imn, imx, fmn, fmx);
+  std::vector<int4> rbp(imn.size());
+  for (size_t j = 0; j < imn.size(); j++) {
+    int fa, fb;
+    std::memcpy(&fa, &fmn[j], 4);
+    std::memcpy(&fb, &fmx[j], 4);
+    rbp[j] = make_int4(imn[j], imx[j], fa, fb);
+  }
   if ((st = upload(T.conv_e, ce)) || (st = upload(T.conv_eff, ceff)) || (st = upload(T.conv_inv_emid, inv_emid)) ||
-      (st = upload(T.conv_cf, cf)) || (st = upload(T.coarse_e, co)) || (st = upload(T.coarse_t, ct)) || (st = upload(T.rb_imin, imn)) ||
-      (st = upload(T.rb_imax, imx)) || (st = upload(T.rb_fmin, fmn)) || (st = upload(T.rb_fmax, fmx)))
+      (st = upload(T.conv_cf, cf)) || (st = upload(T.conv_cw, cw)) || (st = upload(T.coarse_e, co)) || (st = upload(T.coarse_t, ct)) || (st = upload(T.rb_imin, imn)) ||
+      (st = upload(T.rb_imax, imx)) || (st = upload(T.rb_fmin, fmn)) || (st = upload(T.rb_fmax, fmx)) || (st = upload(T.rb_pack, rbp)))
     return st;
   T.d.conv_e = T.conv_e.as<double>();
   T.d.conv_eff = T.conv_eff.as<float2>();
   T.d.conv_inv_emid = T.conv_inv_emid.as<float>();
   T.d.conv_cf = T.conv_cf.as<float>();
+  T.d.conv_cw = T.conv_cw.as<float2>();
   T.d.conv_pos1 = pos1;
   T.d.conv_lg0 = (float) std::log(RELX_EMIN_CONV);
   T.d.conv_ilg = (float) (RELX_NCONV / std::log(RELX_EMAX_CONV / RELX_EMIN_CONV));
@@ -402,6 +412,7 @@ static int load_tables(const std::string &dir, Tables &T) {
   T.d.rb_imax = T.rb_imax.as<int>();
   T.d.rb_fmin = T.rb_fmin.as<float>();
   T.d.rb_fmax = T.rb_fmax.as<float>();
+  T.d.rb_pack = T.rb_pack.as<int4>();
   T.loaded = true;
   return 0;
 }
@@ -697,7 +708,8 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     {
       ProfScope ps(PK_CONV, s);
       conv_zone_kernel<<<dim3(b.nza, n), kConvThreadsH, conv_smem_bytes(), s>>>(tab, sst, prof, tsum, b.nblk,
-                                                                              kSumBinsH, xill, b.nza, cout);
+                                                                              kSumBinsH, xill, b.nza, cout,
+                                                                              W.err.as<int>());
     }
     {
       ProfScope ps(PK_FIN, s);
@@ -848,7 +860,7 @@ static int tuned_launch(Context &C, Workspace &W, BatchShape &b, cudaStream_t s,
     b.line_tile = std::atoi(tile_env) == 256 ? 256 : 512;  // explicit choice
   } else if (known) {
     b.line_tile = known->line_tile;
-    if (!cached && b.chunk == 0) b.chunk = known->chunk;
+    if (!cached && !explicit_choice) b.chunk = known->chunk;
   } else {
     b.line_tile = b.n_sets <= 1024 ? 256 : 512;  // small batches: more CTAs per set
   }

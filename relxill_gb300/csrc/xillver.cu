@@ -18,54 +18,14 @@
 // completing on an mbarrier, three corners in flight per CTA; all waits are
 // bounded and report a timeout through the error flag instead of hanging.
 #include "relx_device.cuh"
+#include "relx_tma.cuh"
 
 namespace relx {
 
 constexpr int kXillThreads = 128;
 constexpr int kXillTile = 512;    // floats per row segment (2 KB), one float4 per thread
 constexpr int kXillStages = 3;
-constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
 static_assert(kXillTile == 4 * kXillThreads, "one float4 per thread");
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, int count) {
-  asm volatile("mbarrier.init.shared.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ unsigned long long globaltimer_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-// bounded wait (limit_ns, at most 2^24 polls); returns false on timeout
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
-                                                  unsigned long long limit_ns = kWaitLimitNs) {
-  const unsigned long long t0 = globaltimer_ns();
-  for (int it = 0; it < (1 << 24); it++) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 255) == 255 && globaltimer_ns() - t0 > limit_ns) return false;
-  }
-  return false;
-}
 
 // Self-test of the timeout path: one thread waits, with a short limit, on an mbarrier that
 // expects 16 bytes no copy will deliver, and reports what the wait returned.  No copy is issued,
