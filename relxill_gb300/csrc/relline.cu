@@ -39,10 +39,11 @@ struct RadC {
   const float2 *gs;       // table g* points as float-float (shared memory)
 };
 
-// abscissa of the reference in energy (for the grid-point side decision)
+// abscissa of the reference in energy (for the grid-point side decision, read only there)
 struct Absc {
-  float2 lo, hi;  // rlo, rhi of the real integration
-  int n, i;       // Romberg level and index (n = -1: midpoint)
+  const float2 *eb;  // the bin's edges E_lo, E_hi (float-float, shared memory)
+  bool lo_H, hi_H;   // the lower / upper end is replaced by gstar2ener(H) / gstar2ener(1-H)
+  int n, i;          // Romberg level and index (n = -1: midpoint)
 };
 
 // transfer functions at one radius: trff (and cosne for limb laws) at the table g* points
@@ -62,14 +63,16 @@ __device__ __forceinline__ float2 eval_F(float x, float y, const RadC &rc, const
   if (fabsf(t - tr) < 4e-6f && tr >= 1.0f && tr <= (float) (ng - 2)) {
     // side of grid point k from the reference's abscissa (float-float)
     int k = (int) tr;
+    const float2 alo = ab.lo_H ? rc.eH : ab.eb[0];
+    const float2 ahi = ab.hi_H ? rc.e1H : ab.eb[1];
     float2 eg;
     if (ab.n < 0) {
-      eg = ff_mulf(ff_add(ab.lo, ab.hi), 0.5f);
+      eg = ff_mulf(ff_add(alo, ahi), 0.5f);
     } else if (ab.i == (1 << ab.n)) {
-      eg = ab.hi;
+      eg = ahi;
     } else {
-      float2 w = ff_add(ab.hi, ff_neg(ab.lo));
-      eg = ff_add(ab.lo, ff_mulf(w, ldexpf((float) ab.i, -ab.n)));
+      float2 w = ff_add(ahi, ff_neg(alo));
+      eg = ff_add(alo, ff_mulf(w, ldexpf((float) ab.i, -ab.n)));
     }
     float2 G = ff_add(rc.gmin, ff_mul(rc.gs[k], rc.dg));
     ind = ff_ge(eg, G) ? k : k - 1;
@@ -162,30 +165,34 @@ __device__ __forceinline__ float sqrt_diff(float hi, float lo) {
   return den > 0.0f ? d / den : 0.0f;
 }
 
-// integ_relline_bin (Relprofile.cpp:650-726) with the emissivity factored out
+// g* and 1 - g* of a bin edge, clamped to [0, 1] (integ_relline_bin, Relprofile.cpp:653-666)
+__device__ __forceinline__ float2 edge_gc(float2 E, const RadC &rc) {
+  float g = ff_sub_to_float(E, rc.gmin) * rc.inv_dg;
+  float c = ff_sub_to_float(rc.gmax, E) * rc.inv_dg;
+  if (g < 0.0f) { g = 0.0f; c = 1.0f; } else if (g > 1.0f) { g = 1.0f; c = 0.0f; }
+  return make_float2(g, c);
+}
+
+// integ_relline_bin (Relprofile.cpp:650-726) with the emissivity factored out, from the clamped
+// g* of the bin's edges; eb: the bin's edges (for the rare grid-point side decision)
 template <bool LIMB>
-__device__ __forceinline__ float integ_bin(float2 Elo, float2 Ehi, bool red_lo, const RadC &rc,
-                                           const TW<LIMB> *__restrict__ tw) {
-  float glo = ff_sub_to_float(Elo, rc.gmin) * rc.inv_dg;
-  float clo = ff_sub_to_float(rc.gmax, Elo) * rc.inv_dg;
-  if (glo < 0.0f) { glo = 0.0f; clo = 1.0f; } else if (glo > 1.0f) { glo = 1.0f; clo = 0.0f; }
-  float ghi = ff_sub_to_float(Ehi, rc.gmin) * rc.inv_dg;
-  float chi = ff_sub_to_float(rc.gmax, Ehi) * rc.inv_dg;
-  if (ghi < 0.0f) { ghi = 0.0f; chi = 1.0f; } else if (ghi > 1.0f) { ghi = 1.0f; chi = 0.0f; }
+__device__ __forceinline__ float integ_bin(float glo, float clo, float ghi, float chi, const float2 *eb, bool red_lo,
+                                           const RadC &rc, const TW<LIMB> *__restrict__ tw) {
   if (ghi == 0.0f) return 0.0f;
   float flu = 0.0f;
   bool has_lo = true, has_hi = true;
   float ga = glo, ca = clo, gb = ghi, cb = chi;
   bool red = red_lo;
   Absc ab;
-  ab.lo = Elo;
-  ab.hi = Ehi;
+  ab.eb = eb;
+  ab.lo_H = false;
+  ab.hi_H = false;
   if (glo <= kH) {
     float hhi = kH;
     ga = kH;
     ca = 1.0f - kH;
     red = rc.red_H;
-    ab.lo = rc.eH;
+    ab.lo_H = true;
     if (ghi <= kH) { hhi = ghi; has_lo = false; }
     flu += rc.edge_lo * sqrt_diff(hhi, glo);
   }
@@ -193,7 +200,7 @@ __device__ __forceinline__ float integ_bin(float2 Elo, float2 Ehi, bool red_lo, 
     float hi_c = kH;  // 1 - hlo
     gb = 1.0f - kH;
     cb = kH;
-    ab.hi = rc.e1H;
+    ab.hi_H = true;
     if (glo >= 1.0f - kH) { hi_c = clo; has_hi = false; }
     flu += rc.edge_hi * sqrt_diff(hi_c, chi);
   }
@@ -366,7 +373,8 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
         const int jlo = max(ielo, tlo), jhi = min(iehi, thi - 1);
         for (int j = jlo + lane; j <= jhi; j += 32) {
           const int jj = j - tlo;
-          const float v = integ_bin<LIMB>(m.eff[jj], m.eff[jj + 1], m.red[jj] != 0, rc, tw);
+          const float2 lo = edge_gc(m.eff[jj], rc), hi = edge_gc(m.eff[jj + 1], rc);
+          const float v = integ_bin<LIMB>(lo.x, lo.y, hi.x, hi.y, &m.eff[jj], m.red[jj] != 0, rc, tw);
           m.acc[warp][jj] += v * ew;
         }
         __syncwarp();
