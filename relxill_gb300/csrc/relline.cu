@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
                                 w00 * a.w + w10 * b.w + w01 * c.w + w11 * d.w);
       }
     }
-    for (int j = tid; j <= thi - tlo; j += kLineThreads) m.eff[j] = ff_from_double(ge[tlo + j]);
+    for (int j = tid; j <= thi - tlo; j += kLineThreads) m.eff[j] = ff_split(ge[tlo + j]);
     for (int j = tid; j < thi - tlo; j += kLineThreads) m.red[j] = ge[tlo + j] >= 0.95 ? 1 : 0;
     for (int i = tid; i < kLineWarps * TILE; i += kLineThreads) (&m.acc[0][0])[i] = 0.0f;
     for (int g = tid; g < ng; g += kLineThreads)

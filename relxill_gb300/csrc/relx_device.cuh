@@ -119,6 +119,21 @@ __device__ __forceinline__ float2 ff_from_double(double d) {
   float lo = __double2float_rn(d - (double) hi);
   return make_float2(hi, lo);
 }
+// double -> float-float without the FP64 pipe (which runs at 2 lanes/clk/SM): hi keeps the
+// leading 24 significant bits of d (truncated), lo is the rest rounded to float, so hi + lo = d to
+// about 2^-48 relative.  For |d| in [2^-60, 2^61); other values use the conversion instructions.
+__device__ __forceinline__ float2 ff_split(double d) {
+  const unsigned long long b = (unsigned long long) __double_as_longlong(d);
+  const unsigned long long ab = b & 0x7fffffffffffffffull;
+  const int e = (int) (ab >> 52) - 1023;
+  if (e < -60 || e > 60) return ff_from_double(d);
+  const unsigned int sgn = (unsigned int) (b >> 32) & 0x80000000u;
+  const float hi = __uint_as_float(sgn | ((unsigned int) (e + 127) << 23) | ((unsigned int) (ab >> 29) & 0x7fffffu));
+  const float r = __uint2float_rn((unsigned int) (ab & 0x1fffffffull));
+  const float sc = __uint_as_float((unsigned int) (e - 52 + 127) << 23);
+  const float lo = __uint_as_float(__float_as_uint(r * sc) | sgn);
+  return make_float2(hi, lo);
+}
 // (a.hi + a.lo) - (b.hi + b.lo) rounded to float, error ~1 ulp of the result
 __device__ __forceinline__ float ff_sub_to_float(float2 a, float2 b) {
   float s = __fsub_rn(a.x, b.x);

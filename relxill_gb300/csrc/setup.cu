@@ -37,6 +37,7 @@ struct SetupSmem {
   int ired[40];
   int zlo[RELX_NZMAX], zhi[RELX_NZMAX];  // per-zone profile windows (inclusive bins)
   int ind_rmin, ind_rmax, status;
+  double rms;        // ISCO radius of the set's spin
   // parameters beyond the state
   double emis1, emis2, rbr, htop, lxi, afe, dens, iongrad_index;
   int return_rad, flags, is_relxill;
@@ -116,6 +117,7 @@ __device__ void map_params(int model, const RelxSetIn &in, SetupSmem &m) {
   s.gamma = s.gam;
   // check_parameter_bounds, ModelDefinition.cpp:168-273
   double rms = kerr_rms(s.a);
+  m.rms = rms;
   if (s.rin < 0) s.rin = -1.0 * s.rin * rms;
   if (s.rout < 0) s.rout = -1.0 * s.rout * rms;
   if (m.rbr < 0) m.rbr = -1.0 * m.rbr * rms;
@@ -166,28 +168,34 @@ __device__ void map_params(int model, const RelxSetIn &in, SetupSmem &m) {
   }
 }
 
-// get_rzone_grid / RadialGrid::calculate_radial_grid (relutility.c:265-308, IonGradient.cpp:457-492)
-__device__ void zone_grid(double rmin, double rmax, int nz, double h, double *rg) {
+// get_rzone_grid / RadialGrid::calculate_radial_grid (relutility.c:265-308, IonGradient.cpp:457-492),
+// one warp: every lane computes its own edges (the same formula per edge as the serial loop)
+__device__ void zone_grid_warp(double rmin, double rmax, int nz, double h, double *rg) {
+  const int lane = threadIdx.x & 31;
   if (nz == 1) {
-    rg[0] = rmin;
-    rg[1] = rmax;
+    if (lane == 0) { rg[0] = rmin; rg[1] = rmax; }
+    __syncwarp();
     return;
   }
   double r_tr = rmin;
   int indr = 0;
   if (h > rmin) {
     r_tr = h;
-    for (int ii = 0; ii < nz + 1; ii++) rg[ii] = exp(1.0 * ii / nz * (log(rmax) - log(rmin)) + log(rmin));
-    indr = bsearch_asc<double>(rg, nz + 1, r_tr);
+    for (int ii = lane; ii < nz + 1; ii += 32) rg[ii] = exp(1.0 * ii / nz * (log(rmax) - log(rmin)) + log(rmin));
+    __syncwarp();
+    if (lane == 0) indr = bsearch_asc<double>(rg, nz + 1, r_tr);
+    indr = __shfl_sync(0xffffffffu, indr, 0);
     r_tr = rg[indr];
+    __syncwarp();
   }
   if (indr < nz) {
     double rlo = r_tr, rhi = rmax;
-    for (int ii = indr; ii < nz + 1; ii++) {
-      rg[ii] = 1.0 * (ii - indr) / (nz - indr) * (1.0 / rhi - 1.0 / rlo) + 1.0 / rlo;
-      rg[ii] = fabs(1.0 / rg[ii]);
+    for (int ii = indr + lane; ii < nz + 1; ii += 32) {
+      double v = 1.0 * (ii - indr) / (nz - indr) * (1.0 / rhi - 1.0 / rlo) + 1.0 / rlo;
+      rg[ii] = fabs(1.0 / v);
     }
   }
+  __syncwarp();
 }
 
 // x0 descending; index ii with x0[ii] > xn >= x0[ii+1] (inv_rebin_mean, relutility.c:636-663)
@@ -255,8 +263,8 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     s.ifac_a = ((float) s.a - tab.rel_a[ia]) / (tab.rel_a[ia + 1] - tab.rel_a[ia]);
     s.ifac_mu0 = ((float) mu0 - tab.rel_mu0[im]) / (tab.rel_mu0[im + 1] - tab.rel_mu0[im]);
     s.g_n = gn;
-    zone_grid(s.rin, s.rout, s.nz, s.height, s.rgrid);
   }
+  if (tid < 32) zone_grid_warp(s.rin, s.rout, s.nz, s.height, s.rgrid);
   __syncthreads();
   {
     const size_t b00 = (size_t) s.ind_a * nm + s.ind_mu0, b10 = (size_t) (s.ind_a + 1) * nm + s.ind_mu0;
@@ -273,8 +281,9 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   // fine radial grid (relutility.c:666-677)
   {
     const double r1 = 1.0 / sqrt(s.rout), r2 = 1.0 / sqrt(s.rin);
+    const double du = (r2 - r1) / (NR - 1);  // the step once, not a division per radius
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
-      double u = ((double) ii) * (r2 - r1) / (NR - 1) + r1;
+      double u = ((double) ii) * du + r1;
       double iu = __drcp_rn(u);
       m.re[ii] = iu * iu;
       m.sqre[ii] = iu;
@@ -282,7 +291,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   }
   __syncthreads();
   if (tid == 0) {
-    double rms = kerr_rms(s.a);
+    const double rms = m.rms;
     if (m.re_tab[nr - 1] > rms && (m.re_tab[nr - 1] - rms) / m.re_tab[nr - 1] < 1e-3) m.re_tab[nr - 1] = rms;
     m.ind_rmin = bsearch_desc(m.re_tab, nr, s.rin);
     m.ind_rmax = bsearch_desc(m.re_tab, nr, s.rout);
@@ -315,14 +324,14 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     R.re[ii] = r;
     R.ifac[ii] = ifac;
     RelxRadRec rr;
-    rr.gmin = ff_from_double(gmn);
-    rr.gmax = ff_from_double(gmx);
-    rr.dg = ff_from_double(gmx - gmn);
+    rr.gmin = ff_split(gmn);
+    rr.gmax = ff_split(gmx);
+    rr.dg = ff_split(gmx - gmn);
     rr.inv_dg = 1.0f / (float) (gmx - gmn);
     {
       double eh = RELX_GFAC_H * (gmx - gmn) + gmn;
-      rr.eH = ff_from_double(eh);
-      rr.e1H = ff_from_double((1 - RELX_GFAC_H) * (gmx - gmn) + gmn);
+      rr.eH = ff_split(eh);
+      rr.e1H = ff_split((1 - RELX_GFAC_H) * (gmx - gmn) + gmn);
       rr.red_H = eh >= 0.95 ? 1 : 0;
     }
     rr.itab = (short) ind;
