@@ -71,6 +71,7 @@ __device__ __forceinline__ int bsearch_desc(const double *arr, int n, double val
 
 // relutility.c:24-26 and :46-58
 __device__ __forceinline__ double lerp1(double f, double lo, double hi) { return f * hi + (1.0 - f) * lo; }
+__device__ __forceinline__ float lerp1(float f, float lo, float hi) { return f * hi + (1.0f - f) * lo; }
 __device__ __forceinline__ double lerp2(double f1, double f2, double r11, double r12, double r21, double r22) {
   return (1.0 - f1) * (1.0 - f2) * r11 + (f1) * (1.0 - f2) * r12 + (1.0 - f1) * (f2) * r21 + (f1) * (f2) * r22;
 }

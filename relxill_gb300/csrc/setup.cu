@@ -27,12 +27,10 @@ struct SetupSmem {
   float re_tab_f[RELX_MAX_NRTAB];    // float copies guide the searches; FP64 decides float ties only
   float jet_rad_f[RELX_MAX_NRADLP], rgrid_f[RELX_NZMAX + 1];
   float lp_dle[RELX_MAX_NRADLP], lp_dlr[RELX_MAX_NRADLP], lp_d[RELX_MAX_NRADLP], lp_di[RELX_MAX_NRADLP];
-  double inv_jr[RELX_MAX_NRADLP];
+  float lp_e[RELX_MAX_NRADLP], inv_jr_f[RELX_MAX_NRADLP], inv_drad_f[RELX_MAX_NRADLP];
   unsigned char lp_log[RELX_MAX_NRADLP];  // logarithmic radial factor (emission angle above 75 deg)
   double qsum[RELX_NZMAX + 1];       // normalisation sums of the primary continuum
-  double e_tab[RELX_MAX_NRADLP], inv_drad[RELX_MAX_NRADLP];
-  double jet_rad[RELX_MAX_NRADLP], le_tab[RELX_MAX_NRADLP], lrad[RELX_MAX_NRADLP];
-  double d_tab[RELX_MAX_NRADLP], di_tab[RELX_MAX_NRADLP];
+  double jet_rad[RELX_MAX_NRADLP], d_tab[RELX_MAX_NRADLP];
   double red[40];
   int ired[40];
   int zlo[RELX_NZMAX], zhi[RELX_NZMAX];  // per-zone profile windows (inclusive bins)
@@ -418,34 +416,33 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     {
       const int ia = m.lp_ind_a;
       const double fa = m.lp_ifac_a;
+      const float faf = (float) fa, f0f = (float) m.ifac_h[0], f1f = (float) m.ifac_h[1];
       for (int k = tid; k < nrad; k += kSetupThreads) {
         m.jet_rad[k] = lerp1(fa, tab.lp_rad[(size_t) ia * nrad + k], tab.lp_rad[(size_t) (ia + 1) * nrad + k]);
-#define TV(arr, q, h) (double) (arr)[(((size_t) (ia + (q)) * nh) + (h)) * nrad + k]
+#define TV(arr, q, h) (arr)[(((size_t) (ia + (q)) * nh) + (h)) * nrad + k]
         const int h0 = m.ind_h[0], h1 = m.ind_h[1];
         const double f0 = m.ifac_h[0], f1 = m.ifac_h[1];
-        double e = (1.0 - fa) * lerp1(f0, TV(tab.lp_intens, 0, h0), TV(tab.lp_intens, 0, h0 + 1))
-            + fa * lerp1(f1, TV(tab.lp_intens, 1, h1), TV(tab.lp_intens, 1, h1 + 1));
-        m.d_tab[k] = (1.0 - fa) * lerp1(f0, TV(tab.lp_del, 0, h0), TV(tab.lp_del, 0, h0 + 1))
-            + fa * lerp1(f1, TV(tab.lp_del, 1, h1), TV(tab.lp_del, 1, h1 + 1));
-        m.di_tab[k] = (1.0 - fa) * lerp1(f0, TV(tab.lp_delinc, 0, h0), TV(tab.lp_delinc, 0, h0 + 1))
-            + fa * lerp1(f1, TV(tab.lp_delinc, 1, h1), TV(tab.lp_delinc, 1, h1 + 1));
+        // the emission angle decides the radial interpolation mode and the reflection fraction: FP64;
+        // the intensity and the incidence angle only enter FP32 arithmetic: FP32
+        m.d_tab[k] = (1.0 - fa) * lerp1(f0, (double) TV(tab.lp_del, 0, h0), (double) TV(tab.lp_del, 0, h0 + 1))
+            + fa * lerp1(f1, (double) TV(tab.lp_del, 1, h1), (double) TV(tab.lp_del, 1, h1 + 1));
+        m.lp_e[k] = (1.0f - faf) * lerp1(f0f, TV(tab.lp_intens, 0, h0), TV(tab.lp_intens, 0, h0 + 1))
+            + faf * lerp1(f1f, TV(tab.lp_intens, 1, h1), TV(tab.lp_intens, 1, h1 + 1));
+        m.lp_di[k] = (1.0f - faf) * lerp1(f0f, TV(tab.lp_delinc, 0, h0), TV(tab.lp_delinc, 0, h0 + 1))
+            + faf * lerp1(f1f, TV(tab.lp_delinc, 1, h1), TV(tab.lp_delinc, 1, h1 + 1));
 #undef TV
-        m.le_tab[k] = log(e);
-        m.e_tab[k] = e;
-        m.lrad[k] = log(m.jet_rad[k]);
       }
     }
     __syncthreads();
     for (int k = tid; k < nrad; k += kSetupThreads) {
       if (k < nrad - 1) {
-        m.inv_drad[k] = 1.0 / (m.jet_rad[k + 1] - m.jet_rad[k]);
-        m.lp_dle[k] = (float) (m.le_tab[k + 1] - m.le_tab[k]);
-        m.lp_dlr[k] = (float) (m.lrad[k + 1] - m.lrad[k]);
+        m.inv_drad_f[k] = 1.0f / (float) (m.jet_rad[k + 1] - m.jet_rad[k]);
+        m.lp_dle[k] = logf(m.lp_e[k + 1] / m.lp_e[k]);                        // log e_hi - log e_lo
+        m.lp_dlr[k] = logf((float) (m.jet_rad[k + 1] / m.jet_rad[k]));       // log r_hi - log r_lo
       }
       m.jet_rad_f[k] = (float) m.jet_rad[k];
-      m.inv_jr[k] = 1.0 / m.jet_rad[k];
+      m.inv_jr_f[k] = 1.0f / m.jet_rad_f[k];
       m.lp_d[k] = (float) m.d_tab[k];
-      m.lp_di[k] = (float) m.di_tab[k];
       m.lp_log[k] = (m.d_tab[k] / kPi * 180.0 <= 75.0) ? 0 : 1;
     }
     __syncthreads();
@@ -455,15 +452,15 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       int kk = bsearch_asc_exact(m.jet_rad, m.jet_rad_f, nrad, r, (float) r);
       if (r >= m.jet_rad[nrad - 1] && r - RELX_RELTABLE_MAX_R > 1e-6) atomicExch(&m.status, RELX_ERR_GRID);
       // get_ipol_factor_radius (relutility.c:407-417); r - rlo in FP64, the rest in FP32
-      const double dr = r - m.jet_rad[kk];
+      const float dr = (float) (r - m.jet_rad[kk]);
       float inter;
       if (!m.lp_log[kk]) {
-        inter = (float) (dr * m.inv_drad[kk]);
+        inter = dr * m.inv_drad_f[kk];
       } else {
-        inter = log1pf((float) (dr * m.inv_jr[kk])) / m.lp_dlr[kk];
+        inter = log1pf(dr * m.inv_jr_f[kk]) / m.lp_dlr[kk];
       }
       // interp_log_1d (relutility.c:41-43) as e_lo * exp(inter * (log e_hi - log e_lo))
-      m.emis[ii] = m.e_tab[kk] * (double) expf(inter * m.lp_dle[kk]);
+      m.emis[ii] = (double) (m.lp_e[kk] * expf(inter * m.lp_dle[kk]));
       m.del_emit[ii] = (double) (inter * m.lp_d[kk + 1] + (1.0f - inter) * m.lp_d[kk]);
       m.del_inc[ii] = (double) (inter * m.lp_di[kk + 1] + (1.0f - inter) * m.lp_di[kk]);
     }
@@ -521,8 +518,8 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     double zf = (model != RELX_RELCONV && s.z > 0) ? (1 + s.z) : 1.0;
     double elo = ue[0] * zf, ehi = ue[in.n_ener] * zf;
     const double *ce = tab.conv_e;
-    int lo = bsearch_asc<double>(ce, RELX_NCONV + 1, elo);
-    int hi = bsearch_asc<double>(ce, RELX_NCONV + 1, ehi);
+    int lo = conv_index(tab, elo);  // as bsearch_asc over the N + 1 edges
+    int hi = conv_index(tab, ehi);
     if (in.flags & 2) {  // RELXILL_RENORMALIZE reads the bin at 3 keV
       int k3 = bsearch_asc<double>(ce, RELX_NCONV, 3.0);
       lo = min(lo, k3);
@@ -683,14 +680,22 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   for (int e = tid; e < ncor; e += kSetupThreads)
     if (m.cw[e] != 0.0f) m.clive[m.cfirst[e]] = 1;
   __syncthreads();
-  if (tid == 0) {
-    int u = 0;
-    for (int e = 0; e < ncor; e++) {
-      if (m.cfirst[e] == e) m.cuniq[e] = m.clive[e] ? (short) u++ : (short) -1;
-      else m.cuniq[e] = m.cuniq[m.cfirst[e]];
+  if (tid < 32) {  // number the live rows in entry order (warp prefix sums)
+    const int lane = tid;
+    int base = 0;
+    for (int e0 = 0; e0 < ncor; e0 += 32) {
+      const int e = e0 + lane;
+      const bool first = e < ncor && m.cfirst[e] == e;
+      const bool live = first && m.clive[e];
+      const unsigned int mask = __ballot_sync(0xffffffffu, live);
+      if (first) m.cuniq[e] = live ? (short) (base + __popc(mask & ((1u << lane) - 1u))) : (short) -1;
+      base += __popc(mask);
     }
-    s.ucount = u;
+    if (lane == 0) s.ucount = base;
   }
+  __syncthreads();
+  for (int e = tid; e < ncor; e += kSetupThreads)
+    if (m.cfirst[e] != e) m.cuniq[e] = m.cuniq[m.cfirst[e]];  // the first entry is numbered above
   __syncthreads();
   const bool dense = nz <= RELX_ZDENSE;
   if (dense) {
@@ -730,7 +735,13 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     }
     for (int z = 0; z < nz; z++) s.inv_nc[z] = (float) m.xscale[z];
     if (m.status != RELX_OK) s.status = m.status;
-    sout[set] = s;
+  }
+  __syncthreads();
+  {  // the set state out, by all threads
+    static_assert(sizeof(RelxSetState) % 8 == 0, "copied as 8-byte words");
+    const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&s);
+    unsigned long long *dst = reinterpret_cast<unsigned long long *>(&sout[set]);
+    for (int i = tid; i < (int) (sizeof(RelxSetState) / 8); i += kSetupThreads) dst[i] = src[i];
   }
 }
 
