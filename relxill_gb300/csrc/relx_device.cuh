@@ -79,7 +79,8 @@ __device__ __forceinline__ double lerp2(double f1, double f2, double r11, double
 // ---- Kerr metric (Relphysics.cpp), FP64 -------------------------------------
 __device__ __forceinline__ double kerr_rms(double a) {
   double sign = (a < 0) ? -1.0 : 1.0;
-  double z1 = 1.0 + pow(1.0 - a * a, 1.0 / 3.0) * (pow(1.0 + a, 1.0 / 3.0) + pow(1.0 - a, 1.0 / 3.0));
+  // cube roots as cbrt (the reference writes pow(x, 1.0/3.0); the two differ by about an ulp)
+  double z1 = 1.0 + cbrt(1.0 - a * a) * (cbrt(1.0 + a) + cbrt(1.0 - a));
   double z2 = sqrt((3.0 * a * a) + (z1 * z1));
   return 3.0 + z2 - sign * sqrt((3.0 - z1) * (3.0 + z1 + (2 * z2)));
 }

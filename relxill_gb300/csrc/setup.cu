@@ -30,6 +30,7 @@ struct SetupSmem {
   float lp_e[RELX_MAX_NRADLP], inv_jr_f[RELX_MAX_NRADLP], inv_drad_f[RELX_MAX_NRADLP];
   unsigned char lp_log[RELX_MAX_NRADLP];  // logarithmic radial factor (emission angle above 75 deg)
   double qsum[RELX_NZMAX + 1];       // normalisation sums of the primary continuum
+  float cpow[RELX_NCOARSE];          // E^-Gamma at the coarse-grid bin centres
   double jet_rad[RELX_MAX_NRADLP], d_tab[RELX_MAX_NRADLP];
   double red[40];
   int ired[40];
@@ -465,20 +466,28 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       m.del_inc[ii] = (double) (inter * m.lp_di[kk + 1] + (1.0f - inter) * m.lp_di[kk]);
     }
     __syncthreads();
-    if (tid == 0) {
-      // calc_refl_frac (Rellp.cpp:36-89)
+    if (tid < 32) {
+      // calc_refl_frac (Rellp.cpp:36-89); the three cosines on three lanes
       double ad_max = m.d_tab[nrad - 1];
       double del_bh = m.del_emit[bsearch_desc(m.re, NR, s.rin)];
       double del_ad = m.del_emit[bsearch_desc(m.re, NR, s.rout)];
       if (ad_max < kPi / 2.0) ad_max = kPi / 2.0;
+      double ad_obs = ad_max;
       if (s.beta > 1e-6) {
         del_bh = relat_abberation(del_bh, -1. * s.beta);
         del_ad = relat_abberation(del_ad, -1. * s.beta);
+        ad_obs = relat_abberation(ad_max, -1. * s.beta);
       }
-      double f_ad = 0.5 * (cos(del_bh) - cos(del_ad));
-      s.f_inf_rest = 0.5 * (1.0 + cos(ad_max));
-      double f_inf = (s.beta > 1e-6) ? 0.5 * (1.0 + cos(relat_abberation(ad_max, -1. * s.beta))) : s.f_inf_rest;
-      s.refl_frac_lp = f_ad / f_inf;
+      const int lane = tid;
+      const double cx = cos(lane == 0 ? del_bh : lane == 1 ? del_ad : lane == 2 ? ad_max : ad_obs);
+      const double c_bh = __shfl_sync(0xffffffffu, cx, 0), c_ad = __shfl_sync(0xffffffffu, cx, 1);
+      const double c_max = __shfl_sync(0xffffffffu, cx, 2), c_obs = __shfl_sync(0xffffffffu, cx, 3);
+      if (lane == 0) {
+        double f_ad = 0.5 * (c_bh - c_ad);
+        s.f_inf_rest = 0.5 * (1.0 + c_max);
+        double f_inf = (s.beta > 1e-6) ? 0.5 * (1.0 + c_obs) : s.f_inf_rest;
+        s.refl_frac_lp = f_ad / f_inf;
+      }
     }
     // apply_emis_fluxboost_source_disk (Rellp.cpp:249-253, Relphysics.cpp:301-311).  gi_potential_lp
     // with sqrt(r) = 1/u of the fine grid; r^2 - 3r + 2a sqrt(r) cancels near the ISCO and stays FP64.
@@ -612,6 +621,8 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   {
     const float gam = (float) s.gam;
     const int lane = tid & 31, warp = tid >> 5;
+    for (int b = tid; b < RELX_NCOARSE; b += kSetupThreads) m.cpow[b] = powf(tab.coarse_t[b].x, -gam);
+    __syncthreads();
     for (int qq = warp; qq <= nz; qq += kSetupThreads / 32) {
       const double shift = (qq == 0) ? 1.0 : m.shift[qq - 1];
       if (qq > 0 && shift == 1.0) continue;
@@ -620,7 +631,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       for (int b = lane; b < RELX_NCOARSE; b += 32) {
         const float4 t = tab.coarse_t[b];  // bin centre, width, centre as float-float (0 outside the band)
         // spec_cutoffpl term (Xillspec.cpp:215-233), FP32 arithmetic
-        const float term = expf(1.0f / ecut) * powf(t.x, -gam) * expf(-t.x / ecut) * t.y;
+        const float term = expf(1.0f / ecut) * m.cpow[b] * expf(-t.x / ecut) * t.y;
         part = ff_add(part, ff_mulf(make_float2(t.z, t.w), term));
       }
 #pragma unroll
