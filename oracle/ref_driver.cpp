@@ -19,6 +19,9 @@ static ModelName model_from_id(int id) {
     case 1: return ModelName::relconv;
     case 2: return ModelName::relxill;
     case 3: return ModelName::relxilllp;
+    case 4: return ModelName::relline_lp;
+    case 5: return ModelName::relconv_lp;
+    case 6: return ModelName::xillver;
     default: return ModelName::relline;
   }
 }

@@ -373,6 +373,21 @@ static int map_params(int model, const double *v, int ion_grad_type, double iong
       p->refl_frac = v[11]; p->return_rad = (int) lround(v[12]);
       p->interpret_reflfrac_as_boost = (int) lround(v[13]);
       break;
+    case RELXO_RELLINELP:  /* lmodel_relxill_public.dat:23-33 */
+      p->emis_type = EMIS_TYPE_LP;
+      p->lineE = v[0]; p->height = v[1]; p->a = v[2]; p->incl = v[3] * M_PI / 180; p->rin = v[4]; p->rout = v[5];
+      p->z = v[6]; p->limb = (int) lround(v[7]); p->gam = v[8]; p->return_rad = (int) lround(v[9]);
+      break;
+    case RELXO_RELCONVLP:  /* lmodel_relxill_public.dat:35-44 */
+      p->emis_type = EMIS_TYPE_LP;
+      p->height = v[0]; p->beta = v[1]; p->a = v[2]; p->incl = v[3] * M_PI / 180; p->rin = v[4]; p->rout = v[5];
+      p->limb = (int) lround(v[6]); p->gam = v[7]; p->return_rad = (int) lround(v[8]);
+      break;
+    case RELXO_XILLVER:  /* lmodel_relxill_public.dat:77-84, get_xill_params (ModelDefinition.cpp:339-388) */
+      p->gam = v[0]; p->afe = v[1]; p->ect = v[2]; p->lxi = v[3]; p->z = v[4];
+      p->incl = v[5];  /* degrees: xillParam keeps the inclination in degrees */
+      p->refl_frac = v[6];
+      return 0;      /* no relativistic parameters (get_rel_params returns none for xillver models) */
     default:
       return 1;
   }
@@ -1255,6 +1270,69 @@ static int xillver_spectra_all_incl(XillTable *t, double gam, double afe, double
   return 0;
 }
 
+/* get_xilltab_indices_for_paramvals + interp_xill_table + interp_5d_tab (xilltable.c:278-323,
+ * 878-995, 1090-1181) for the xillver model: all five parameters, the inclination included,
+ * are interpolated (32 corner spectra) */
+static int xillver_spectrum_at_incl(XillTable *t, double gam, double afe, double lxi, double ect, double incl_deg,
+                                    double dens, double *flu /* [n_ener] */) {
+  float inp[10] = {0};
+  inp[PARAM_GAM] = (float) gam;
+  inp[PARAM_AFE] = (float) afe;
+  inp[PARAM_LXI] = (float) lxi;
+  inp[PARAM_ECT] = (float) ect;
+  inp[PARAM_DNS] = (float) dens;
+  inp[PARAM_INC] = (float) incl_deg;
+  int ind[5];
+  for (int ii = 0; ii < t->num_param; ii++) {
+    ind[ii] = binary_search_float(t->param_vals[ii], t->num_param_vals[ii], inp[t->param_index[ii]]);
+    if (ind[ii] < 0) ind[ii] = 0;
+    else if (ind[ii] > t->num_param_vals[ii] - 2) ind[ii] = t->num_param_vals[ii] - 2;
+  }
+  double ipol[5];
+  for (int ii = 0; ii < t->num_param; ii++) {
+    int pind = t->param_index[ii];
+    /* resetInpvalsToBoundaries (xilltable.c:1069-1088), the inclination included for xillver models */
+    float lo = t->param_vals[ii][0], hi = t->param_vals[ii][t->num_param_vals[ii] - 1];
+    if (inp[pind] < lo) inp[pind] = lo;
+    else if (inp[pind] > hi) inp[pind] = hi;
+    ipol[ii] = (inp[pind] - t->param_vals[ii][ind[ii]]) / (t->param_vals[ii][ind[ii] + 1] - t->param_vals[ii][ind[ii]]);
+  }
+  int iect = xilltab_param_index(t, PARAM_ECT);
+  if (iect >= 0) {  /* ensure_ecut_within_boundarys, xilltable.c:1054-1067 */
+    const float *ev = t->param_vals[t->param_index[iect]];
+    if (ect <= ev[0]) ipol[iect] = 0.0;
+    if (ect >= ev[t->num_param_vals[t->param_index[iect]] - 1]) ipol[iect] = 1.0;
+  }
+  const double f1 = ipol[0], f2 = ipol[1], f3 = ipol[2], f4 = ipol[3], f5 = ipol[4];
+  /* the 32 corners in the order of interp_5d_tab's weights and sum (xilltable.c:884-992):
+   * bits (c1 c2 c3 c4 c5) of the corner offsets */
+  static const int corner[32][5] = {
+      {0, 0, 0, 0, 0}, {1, 0, 0, 0, 0}, {0, 1, 0, 0, 0}, {0, 0, 1, 0, 0}, {1, 1, 0, 0, 0}, {1, 0, 1, 0, 0},
+      {0, 1, 1, 0, 0}, {1, 1, 1, 0, 0}, {0, 0, 0, 1, 0}, {1, 0, 0, 1, 0}, {0, 1, 0, 1, 0}, {0, 0, 1, 1, 0},
+      {1, 1, 0, 1, 0}, {1, 0, 1, 1, 0}, {0, 1, 1, 1, 0}, {1, 1, 1, 1, 0}, {0, 0, 0, 0, 1}, {1, 0, 0, 0, 1},
+      {0, 1, 0, 0, 1}, {0, 0, 1, 0, 1}, {1, 1, 0, 0, 1}, {1, 0, 1, 0, 1}, {0, 1, 1, 0, 1}, {1, 1, 1, 0, 1},
+      {0, 0, 0, 1, 1}, {1, 0, 0, 1, 1}, {0, 1, 0, 1, 1}, {0, 0, 1, 1, 1}, {1, 1, 0, 1, 1}, {1, 0, 1, 1, 1},
+      {0, 1, 1, 1, 1}, {1, 1, 1, 1, 1}};
+  double w[32];
+  const float *d[32];
+  float *buf = malloc(sizeof(float) * 32 * (size_t) t->n_ener);
+  for (int c = 0; c < 32; c++) {
+    const int *o = corner[c];
+    w[c] = (o[0] ? f1 : (1.0 - f1)) * (o[1] ? f2 : (1.0 - f2)) * (o[2] ? f3 : (1.0 - f3)) * (o[3] ? f4 : (1 - f4)) *
+           (o[4] ? f5 : (1 - f5));
+    d[c] = xill_spec(t, ind[0] + o[0], ind[1] + o[1], ind[2] + o[2], ind[3] + o[3], ind[4] + o[4], dens,
+                     buf + (size_t) c * t->n_ener);
+    if (!d[c]) { free(buf); return 1; }
+  }
+  for (int ii = 0; ii < t->n_ener; ii++) {
+    double acc = w[0] * (double) d[0][ii];
+    for (int c = 1; c < 32; c++) acc = acc + w[c] * (double) d[c][ii];
+    flu[ii] = acc;
+  }
+  free(buf);
+  return 0;
+}
+
 /* ======================================================================= */
 /* models                                                                   */
 /* ======================================================================= */
@@ -1413,6 +1491,35 @@ static int relxill_kernel(const Params *p, double *out_conv /* [N_ENER_CONV] */)
   return status;
 }
 
+/* xillver_model (LocalModel.cpp:103-128): the table spectrum at the inclination, the
+ * semi-infinite slab factor 0.5 cos(incl) (Xillspec.cpp:528-545), rebinned to the caller's grid,
+ * and add_primary_component without relativistic parameters (Relbase.cpp:294-349) */
+static int xillver_model(const Params *p, const double *ener, int n, double *flux) {
+  XillTable *t = g_xill;
+  xill_begin_eval(t);
+  const int nx = t->n_ener;
+  double *spec = malloc(sizeof(double) * nx), *xe = malloc(sizeof(double) * (nx + 1));
+  int status = xillver_spectrum_at_incl(t, p->gam, p->afe, p->lxi, p->ect, p->incl, p->dens, spec);
+  if (!status) {
+    const double nf = 0.5 * cos(p->incl * M_PI / 180);
+    for (int ii = 0; ii < nx; ii++) spec[ii] *= nf;
+    for (int ii = 0; ii < nx; ii++) xe[ii] = t->elo[ii];
+    xe[nx] = t->ehi[nx - 1];
+    relxo_rebin_spectrum(ener, flux, n, xe, spec, nx);
+    /* calc_normalized_primary_spectrum (Xillspec.cpp:302-332) on the caller's grid */
+    double *pl = malloc(sizeof(double) * n);
+    spec_cutoffpl(pl, ener, n, p->ect, p->gam, 1.0);
+    const double norm = relxo_primary_norm_factor(p->ect, p->gam);
+    for (int ii = 0; ii < n; ii++) pl[ii] *= norm;
+    for (int ii = 0; ii < n; ii++) flux[ii] *= fabs(p->refl_frac);
+    if (p->refl_frac >= 0)
+      for (int ii = 0; ii < n; ii++) flux[ii] += pl[ii];
+    free(pl);
+  }
+  free(spec); free(xe);
+  return status;
+}
+
 /* ======================================================================= */
 /* public entry points                                                      */
 /* ======================================================================= */
@@ -1426,9 +1533,10 @@ int relxo_set_table_path(const char *path) {
 int relxo_eval_ext(int model, const double *params, int ion_grad_type, double iongrad_index, const double *energy,
                    int n_flux, double *flux) {
   Params p;
-  for (int ii = 0; ii < n_flux; ii++) if (model != RELXO_RELCONV) flux[ii] = 0.0;
+  const int is_conv = (model == RELXO_RELCONV || model == RELXO_RELCONVLP);
+  for (int ii = 0; ii < n_flux; ii++) if (!is_conv) flux[ii] = 0.0;
   if (map_params(model, params, ion_grad_type, iongrad_index, &p)) return 1;
-  int is_rx = (model == RELXO_RELXILL || model == RELXO_RELXILLLP);
+  int is_rx = (model == RELXO_RELXILL || model == RELXO_RELXILLLP || model == RELXO_XILLVER);
   if (ensure_tables(is_rx)) return 2;
   /* XspecSpectrum copy + shift_energy_grid_redshift (XspecSpectrum.h:35-76) */
   double *ener = malloc(sizeof(double) * (n_flux + 1));
@@ -1436,11 +1544,13 @@ int relxo_eval_ext(int model, const double *params, int ion_grad_type, double io
   if (p.z > 0)
     for (int ii = 0; ii <= n_flux; ii++) ener[ii] *= (1 + p.z);
   int status = 0;
-  if (model == RELXO_RELLINE) {
+  if (model == RELXO_XILLVER) {
+    status = xillver_model(&p, ener, n_flux, flux);
+  } else if (model == RELXO_RELLINE || model == RELXO_RELLINELP) {
     /* line_model, LocalModel.cpp:32-51 */
     for (int ii = 0; ii <= n_flux; ii++) ener[ii] /= p.lineE;
     status = relbase_single(&p, ener, n_flux, flux);
-  } else if (model == RELXO_RELCONV) {
+  } else if (model == RELXO_RELCONV || model == RELXO_RELCONVLP) {
     /* conv_model + relconv_kernel, LocalModel.cpp:82-98, Relbase.cpp:257-289 */
     double s = 0.0;
     for (int ii = 0; ii < n_flux; ii++) s += flux[ii];

@@ -9,7 +9,8 @@
 extern "C" {
 #endif
 
-enum { RELXO_RELLINE = 0, RELXO_RELCONV = 1, RELXO_RELXILL = 2, RELXO_RELXILLLP = 3 };
+enum { RELXO_RELLINE = 0, RELXO_RELCONV = 1, RELXO_RELXILL = 2, RELXO_RELXILLLP = 3, RELXO_RELLINELP = 4,
+       RELXO_RELCONVLP = 5, RELXO_XILLVER = 6 };
 
 int relxo_set_table_path(const char *path);
 /* one model evaluation; params in lmodel.dat order; returns 0 on success */
