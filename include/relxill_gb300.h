@@ -2,7 +2,7 @@
  * relxill_gb300.h -- C ABI of the GB300 (sm_103a) implementation of relxill's
  * relativistic convolution path.
  *
- * The four local-model entry points keep the signature that the reference's
+ * The seven local-model entry points keep the signature that the reference's
  * wrapper generator emits for XSPEC (src/create_wrapper_xspec.py:153-162) and
  * the parameter order of src/modelfiles/lmodel_relxill_public.dat, so a host
  * package that loads the reference's librelxill can load this library
@@ -23,7 +23,10 @@ extern "C" {
 #endif
 
 /* model ids of the batched calls */
-enum { RELX_MODEL_RELLINE = 0, RELX_MODEL_RELCONV = 1, RELX_MODEL_RELXILL = 2, RELX_MODEL_RELXILLLP = 3 };
+enum {
+  RELX_MODEL_RELLINE = 0, RELX_MODEL_RELCONV = 1, RELX_MODEL_RELXILL = 2, RELX_MODEL_RELXILLLP = 3,
+  RELX_MODEL_RELLINELP = 4, RELX_MODEL_RELCONVLP = 5, RELX_MODEL_XILLVER = 6
+};
 
 /* Local models.  Replace c_lmodrelline / c_lmodrelconv / c_lmodrelxill /
  * c_lmodrelxilllp, generated by src/create_wrapper_xspec.py:153-162 from
@@ -41,6 +44,18 @@ void c_lmodrelxill(const double *energy, int Nflux, const double *parameter, int
                    double *fluxError, const char *init);
 void c_lmodrelxilllp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
                      double *fluxError, const char *init);
+/* The lamp-post line and convolution models and the non-relativistic xillver
+ * model (lmodel_relxill_public.dat:23,35,77; the same generated wrappers):
+ * relline_lp takes lineE, h, a, Incl, Rin, Rout, z, limb, gamma,
+ * switch_returnrad; relconv_lp h, beta, a, Incl, Rin, Rout, limb, gamma,
+ * switch_returnrad (flux carries the input spectrum); xillver gamma, Afe,
+ * Ecut, logxi, z, Incl, refl_frac. */
+void c_lmodrellinelp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                     double *fluxError, const char *init);
+void c_lmodrelconvlp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                     double *fluxError, const char *init);
+void c_lmodxillver(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                   double *fluxError, const char *init);
 
 /* Status of the last call on this process (0 = success).  The reference has
  * no status channel (src/LocalModel.cpp:153-159); this replaces its printed
@@ -60,12 +75,13 @@ void relx_release(void);
 
 /* Batched evaluation with host buffers; no counterpart in the reference,
  * which evaluates one parameter set per call.
- * params: n_sets x npar (npar = 10, 8, 13, 14 for relline, relconv, relxill,
- *   relxilllp, lmodel.dat order);
+ * params: n_sets x npar (npar = 10, 8, 13, 14, 10, 9, 7 for relline, relconv,
+ *   relxill, relxilllp, relline_lp, relconv_lp, xillver; lmodel.dat order);
  * energy: concatenated bin edges; set i uses energy[energy_offsets[i] ..
  *   energy_offsets[i+1]-1] (n_i + 1 edges);
  * flux: concatenated outputs, set i at flux[energy_offsets[i] - i .. + n_i - 1];
- * flux_in: relconv input spectra in the same layout as flux (NULL otherwise);
+ * flux_in: relconv / relconv_lp input spectra in the same layout as flux
+ *   (NULL otherwise);
  * status: n_sets per-set statuses (may be NULL);
  * ion_grad_type / iongrad_index: per-set hidden ionisation-gradient switch
  *   (0 const, 1 power law, 2 alpha disk) of relxilllp (NULL: 0).

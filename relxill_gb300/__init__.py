@@ -22,9 +22,11 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "librelxill_gb300.so")
 
-MODELS: Dict[str, int] = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3}
+MODELS: Dict[str, int] = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3, "relline_lp": 4,
+                          "relconv_lp": 5, "xillver": 6}
+CONV_MODELS = ("relconv", "relconv_lp")  # models that take the caller's spectrum in `flux`
 
-# parameter names and defaults of lmodel_relxill_public.dat:1-75 (in order)
+# parameter names and defaults of lmodel_relxill_public.dat:1-84 (in order)
 PARAMS: Dict[str, List[Tuple[str, float]]] = {
     "relline": [("lineE", 6.4), ("Index1", 3.0), ("Index2", 3.0), ("Rbr", 15.0), ("a", 0.998), ("Incl", 30.0),
                 ("Rin", -1.0), ("Rout", 400.0), ("z", 0.0), ("limb", 0.0)],
@@ -36,7 +38,16 @@ PARAMS: Dict[str, List[Tuple[str, float]]] = {
     "relxilllp": [("h", 6.0), ("beta", 0.0), ("a", 0.998), ("Incl", 30.0), ("Rin", -1.0), ("Rout", 400.0),
                   ("z", 0.0), ("gamma", 2.0), ("logxi", 3.1), ("Afe", 1.0), ("Ecut", 300.0), ("refl_frac", 1.0),
                   ("switch_returnrad", 1.0), ("switch_reflfrac_boost", 0.0)],
+    "relline_lp": [("lineE", 6.4), ("h", 6.0), ("a", 0.998), ("Incl", 30.0), ("Rin", -1.0), ("Rout", 400.0),
+                   ("z", 0.0), ("limb", 0.0), ("gamma", 2.0), ("switch_returnrad", 1.0)],
+    "relconv_lp": [("h", 6.0), ("beta", 0.0), ("a", 0.998), ("Incl", 30.0), ("Rin", -1.0), ("Rout", 400.0),
+                   ("limb", 0.0), ("gamma", 2.0), ("switch_returnrad", 1.0)],
+    "xillver": [("gamma", 2.0), ("Afe", 1.0), ("Ecut", 300.0), ("logxi", 3.1), ("z", 0.0), ("Incl", 30.0),
+                ("refl_frac", -1.0)],
 }
+LMOD_SYMBOL = {"relline": "c_lmodrelline", "relconv": "c_lmodrelconv", "relxill": "c_lmodrelxill",
+               "relxilllp": "c_lmodrelxilllp", "relline_lp": "c_lmodrellinelp", "relconv_lp": "c_lmodrelconvlp",
+               "xillver": "c_lmodxillver"}
 
 STATUS = {0: "ok", 1: "parameter out of range", 2: "table inconsistent", 3: "unsupported option",
           4: "radial grid outside the table", 5: "relconv input sum <= 0", 6: "CUDA error",
@@ -97,7 +108,7 @@ def lib() -> ctypes.CDLL:
     L.relx_serve_stats.restype = ctypes.c_int
     L.relx_serve_destroy.argtypes = [ctypes.c_void_p]
     L.relx_serve_destroy.restype = None
-    for name in ("c_lmodrelline", "c_lmodrelconv", "c_lmodrelxill", "c_lmodrelxilllp"):
+    for name in LMOD_SYMBOL.values():
         fn = getattr(L, name)
         fn.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, ctypes.c_char_p]
         fn.restype = None
@@ -155,9 +166,9 @@ def eval_batch(model: str, params, energies: Sequence[np.ndarray], flux_in: Opti
     flux = np.zeros(nflux, dtype=np.float64)
     status = np.zeros(n, dtype=np.int32)
     fin = None
-    if model == "relconv":
+    if model in CONV_MODELS:
         if flux_in is None:
-            raise ValueError("relconv needs the input spectra")
+            raise ValueError(f"{model} needs the input spectra")
         fin = np.concatenate([np.asarray(f, dtype=np.float64) for f in flux_in])
     igt = None if ion_grad_type is None else np.ascontiguousarray(ion_grad_type, dtype=np.int32)
     igi = None if iongrad_index is None else np.ascontiguousarray(iongrad_index, dtype=np.float64)
@@ -176,7 +187,7 @@ def _lmod(model: str, energy, params, flux_in=None) -> np.ndarray:
     p = _as_params(model, params)[0].copy()
     nflux = len(e) - 1
     flux = np.zeros(nflux) if flux_in is None else np.array(flux_in, dtype=np.float64)
-    getattr(L, "c_lmod" + model)(_ptr(e), nflux, _ptr(p), 0, _ptr(flux), None, None)
+    getattr(L, LMOD_SYMBOL[model])(_ptr(e), nflux, _ptr(p), 0, _ptr(flux), None, None)
     st = L.relx_last_status()
     if st:
         raise RelxillError(st, L.relx_last_error().decode())
@@ -201,6 +212,21 @@ def relxill(energy, params) -> np.ndarray:
 def relxilllp(energy, params) -> np.ndarray:
     """relxilllp photon flux per bin (c_lmodrelxilllp)."""
     return _lmod("relxilllp", energy, params)
+
+
+def relline_lp(energy, params) -> np.ndarray:
+    """relline_lp photon flux per bin (c_lmodrellinelp)."""
+    return _lmod("relline_lp", energy, params)
+
+
+def relconv_lp(energy, params, flux) -> np.ndarray:
+    """relconv_lp applied to `flux` on the grid `energy` (c_lmodrelconvlp)."""
+    return _lmod("relconv_lp", energy, params, flux)
+
+
+def xillver(energy, params) -> np.ndarray:
+    """xillver photon flux per bin (c_lmodxillver)."""
+    return _lmod("xillver", energy, params)
 
 
 def default_params(model: str) -> np.ndarray:

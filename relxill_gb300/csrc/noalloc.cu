@@ -86,7 +86,7 @@ static size_t carve(unsigned char *base, int model, int nza, int nbins, int ntil
   p->rad = (RelxRadial *) take(sizeof(RelxRadial));
   p->cor = (RelxCorners *) take(sizeof(RelxCorners));
   p->zcor = (RelxZoneCorners *) take(sizeof(RelxZoneCorners));
-  const bool line = (model == RELX_RELLINE);
+  const bool line = (relx_kind(model) == RELX_RELLINE);
   p->line_e = (double *) take(line ? sizeof(double) * (nbins + 1) : 0);
   p->prof = (float *) take(sizeof(float) * (line ? (size_t) nbins : (size_t) nza * RELX_NCONV));
   p->dist = (float *) take(sizeof(float) * nza * RELX_MAX_INCL);
@@ -173,11 +173,12 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
                             double iongrad_index, cudaStream_t s) {
   if (model < 0 || model >= RELX_NMODELS || !d_params || !d_energy || !d_flux || n_bins < 1)
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: bad arguments");
-  if (model == RELX_RELCONV && !d_flux_in)
+  const int kind = relx_kind(model);
+  if (kind == RELX_RELCONV && !d_flux_in)
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: relconv needs the input spectrum");
   if (ion_grad_type < 0 || ion_grad_type > 2)
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: ion_grad_type must be 0, 1 or 2");
-  if (model == RELX_RELLINE && n_bins > kMaxLineBins) {
+  if (kind == RELX_RELLINE && n_bins > kMaxLineBins) {
     char msg[160];
     std::snprintf(msg, sizeof(msg), "relx_eval_one_noalloc: relline grid of %d bins exceeds the limit of %d bins",
                   n_bins, kMaxLineBins);
@@ -189,12 +190,12 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
   NOALLOC_CUDA(cudaGetDevice(&dev));
   if (dev != tab_dev) return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: the tables live on another device");
   const RelxTables tab = *tp;
-  if (model >= RELX_RELXILL && tab.x_nener_pad > kMaxXillBins)
+  if ((relx_is_relxill(kind) || kind == RELX_XILLVER) && tab.x_nener_pad > kMaxXillBins)
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: xillver table has more energy bins than the scratch holds");
   int nzones_env = 0, flags = 0;
   const int nza = runtime_zones(model, ion_grad_type, &nzones_env, &flags);
   if (nza < 1 || nza > RELX_NZMAX) return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: zone count out of range");
-  const int gbins = (model == RELX_RELLINE) ? n_bins : RELX_NCONV;
+  const int gbins = (kind == RELX_RELLINE) ? n_bins : RELX_NCONV;
   const int ntile_max = (gbins + kSumBinsH - 1) / kSumBinsH;  // 256-bin profile-sum blocks
   unsigned char *base = nullptr;
   int st = scratch_for_device(dev, &base);
@@ -205,17 +206,24 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
 
   noalloc_pack_kernel<<<1, 32, 0, s>>>(runtime_nparams(model), d_params, n_bins, ion_grad_type, iongrad_index,
                                        nzones_env, flags, p.sin, p.sflag, p.err);
+  if (kind == RELX_XILLVER) {
+    NOALLOC_CUDA(launch_xillver_model(s, tab, 1, p.sin, d_energy, p.sst, d_flux));
+    noalloc_status_kernel<<<1, 32, 0, s>>>(p.sst, p.sflag, p.err, p.status, d_status);
+    NOALLOC_CUDA(cudaGetLastError());
+    runtime_set_error(RELX_OK, "");
+    return RELX_OK;
+  }
   setup_kernel<<<1, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, model, p.sin, d_energy, p.line_e, p.sst, p.rad,
                                                             p.cor, p.zcor);
-  NOALLOC_CUDA(launch_relline(model >= RELX_RELXILL, 1, 512, ntile_max, s, tab, p.sin, p.sst, p.rad, p.line_e, nza,
-                              p.prof, p.dist, p.tsum, model == RELX_RELLINE || model == RELX_RELCONV));
-  if (model >= RELX_RELXILL) {
+  NOALLOC_CUDA(launch_relline(relx_is_relxill(kind), 1, 512, ntile_max, s, tab, p.sin, p.sst, p.rad, p.line_e, nza,
+                              p.prof, p.dist, p.tsum, kind == RELX_RELLINE || kind == RELX_RELCONV));
+  if (relx_is_relxill(kind)) {
     NOALLOC_CUDA(launch_xillver(s, tab, 1, nza, p.sst, p.cor, p.zcor, p.dist, p.xill, p.err, nullptr));
     conv_zone_kernel<<<dim3(nza, 1), kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sst, p.prof, p.tsum, ntile_max,
                                                                             kSumBinsH, p.xill, nza, p.cout,
                                                                             p.err);
     finalize_relxill_kernel<<<1, kFinThreadsH, fin_smem_bytes(), s>>>(tab, p.sin, p.sst, p.cout, nza, d_energy, d_flux);
-  } else if (model == RELX_RELCONV) {
+  } else if (kind == RELX_RELCONV) {
     relconv_conv_kernel<<<1, kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sin, p.sst, p.prof, p.tsum, ntile_max,
                                                                     kSumBinsH, nza, d_energy, d_flux_in, p.cout,
                                                                     p.sflag);

@@ -25,22 +25,30 @@ __device__ __forceinline__ bool cache_key(const RelxSetIn &in, const RelxSetStat
   if (s.status != RELX_OK || s.model == RELX_RELLINE || s.nz > kCacheZones) return false;
 #pragma unroll
   for (int q = 0; q < kCacheKeyLen; q++) key[q] = 0.0;
-  key[0] = (double) s.model;
+  key[0] = (double) s.pmodel;
   key[1] = (double) s.nz;
-  // relconv: Index1..limb (8); relxill: Index1..z (8); relxilllp: h..gamma (8) and the
-  // returning-radiation switch (lmodel_relxill_public.dat:13-21, 46-59, 61-75)
+  // relconv: Index1..limb (8); relconv_lp: h..gamma (8); relxill: Index1..z (8); relxilllp: h..gamma
+  // (8) and the returning-radiation switch (lmodel_relxill_public.dat:13-21, 35-44, 46-59, 61-75)
 #pragma unroll
   for (int q = 0; q < 8; q++) key[2 + q] = in.p[q];
   if (s.model == RELX_RELXILLLP) key[10] = in.p[12];
   return true;
 }
 
+// FNV-1a over the key's 64-bit words, then the MurmurHash3 64-bit finaliser.  Parameters with
+// short binary fractions (integers, halves) differ only in the high bits of their doubles, and a
+// multiply carries bits upwards only: without the finaliser such keys share their low (slot) bits.
 __device__ __forceinline__ unsigned long long key_hash(const double *key) {
-  unsigned long long h = 1469598103934665603ull;  // FNV-1a over the key's 64-bit words
+  unsigned long long h = 1469598103934665603ull;
   for (int q = 0; q < kCacheKeyLen; q++) {
     h ^= (unsigned long long) __double_as_longlong(key[q]);
     h *= 1099511628211ull;
   }
+  h ^= h >> 33;
+  h *= 0xff51afd7ed558ccdull;
+  h ^= h >> 33;
+  h *= 0xc4ceb9fe1a85ec53ull;
+  h ^= h >> 33;
   return h;
 }
 
@@ -112,7 +120,7 @@ __global__ void cache_store_kernel(RelCacheDev c, const RelxSetIn *__restrict__ 
     const int t = i / s.nz, z = i - t * s.nz;
     c.tsum[((size_t) slot * kCacheTiles + t) * kCacheZones + z] = tsum[((size_t) set * ntile_max + t) * nza + z];
   }
-  const bool has_dist = s.model >= RELX_RELXILL;
+  const bool has_dist = relx_is_relxill(s.model);
   for (int i = tid; i < s.nz * RELX_MAX_INCL; i += nt)
     c.dist[(size_t) slot * kCacheZones * RELX_MAX_INCL + i] = has_dist ? dist[(size_t) set * nza * RELX_MAX_INCL + i] : 0.0f;
   if (tid == 0) {

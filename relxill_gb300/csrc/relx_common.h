@@ -9,8 +9,21 @@
 #define RELX_HD
 #endif
 
-// model ids (lmodel_relxill_public.dat:1,13,46,61)
-enum RelxModel { RELX_RELLINE = 0, RELX_RELCONV = 1, RELX_RELXILL = 2, RELX_RELXILLLP = 3, RELX_NMODELS = 4 };
+// model ids (lmodel_relxill_public.dat:1,13,23,35,46,61,77)
+enum RelxModel {
+  RELX_RELLINE = 0, RELX_RELCONV = 1, RELX_RELXILL = 2, RELX_RELXILLLP = 3,
+  RELX_RELLINELP = 4, RELX_RELCONVLP = 5, RELX_XILLVER = 6, RELX_NMODELS = 7
+};
+
+// The kernels work on four kinds of evaluation: a line profile (relline, relline_lp), a
+// convolution of the caller's spectrum (relconv, relconv_lp), a relativistic reflection
+// spectrum (relxill, relxilllp) and the non-relativistic reflection spectrum (xillver).  The
+// lamp-post line and convolution models differ from their broken-power-law twins only in the
+// emissivity (LocalModel.cpp:32-98 runs the same code for both).
+RELX_HD inline int relx_kind(int model) {
+  return model == RELX_RELLINELP ? RELX_RELLINE : model == RELX_RELCONVLP ? RELX_RELCONV : model;
+}
+RELX_HD inline bool relx_is_relxill(int kind) { return kind == RELX_RELXILL || kind == RELX_RELXILLLP; }
 
 // error codes written per set and returned by the C ABI
 enum RelxStatus {
@@ -92,6 +105,7 @@ struct RelxTables {
   const float *rb_fmin, *rb_fmax;  // fractions (single-bin case: rb_fmin, rb_imax == rb_imin)
   const int4 *rb_pack;       // per conv bin: imin, imax, fmin and fmax as float bits
   const double *x_e;         // xillver edges [x_nener+1] (double of the float table values)
+  const float2 *x_ew;        // per xillver edge: the edge, (float) (x_e[k+1] - x_e[k]) (0 at the last edge)
 };
 
 // per-set inputs
@@ -108,6 +122,7 @@ struct RelxSetIn {
 // per-set state written by the setup kernel
 struct RelxSetState {
   int status, model, emis_type, limb, nz, ion_grad_type, boost_switch;
+  int pmodel;       // the caller's model id (model holds its kind, relx_kind)
   int cached;       // line profile, tile sums and angle histograms come from the profile cache
   int g_n;          // bins of the line-profile grid (user grid for relline, conv grid otherwise)
   int win_lo, win_hi;  // line-profile bins touched by any radius

@@ -253,4 +253,27 @@ __device__ __forceinline__ int block_max_i(int v, int *scratch) {
   return r;
 }
 
+// Sum over the coarse normalisation grid of the cut-off power law times the bin centre, scaled to
+// the xillver table normalisation (calcNormWrtXillverTableSpec with spec_cutoffpl,
+// Xillspec.cpp:179-233): FP32 terms summed as float-float by one warp, every lane returns the
+// total.  cpow: E^-Gamma per coarse bin, or null to compute it here.
+__device__ __forceinline__ double primary_qsum_warp(const RelxTables &tab, float gam, float ecut, const float *cpow) {
+  const int lane = threadIdx.x & 31;
+  float2 part = make_float2(0.0f, 0.0f);
+  for (int b = lane; b < RELX_NCOARSE; b += 32) {
+    const float4 t = tab.coarse_t[b];  // bin centre, width, centre as float-float (0 outside the band)
+    const float pw = cpow ? cpow[b] : powf(t.x, -gam);
+    const float term = expf(1.0f / ecut) * pw * expf(-t.x / ecut) * t.y;
+    part = ff_add(part, ff_mulf(make_float2(t.z, t.w), term));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    float2 u;
+    u.x = __shfl_xor_sync(0xffffffffu, part.x, o);
+    u.y = __shfl_xor_sync(0xffffffffu, part.y, o);
+    part = ff_add(part, u);
+  }
+  return ff_to_double(part) * 1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi);
+}
+
 }  // namespace relx

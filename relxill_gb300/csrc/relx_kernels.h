@@ -12,6 +12,7 @@ constexpr int kLineThreadsH = 256;
 constexpr int kSumBinsH = 256;   // bins per profile-sum block (tsum)
 constexpr int kConvThreadsH = 256;
 constexpr int kFinThreadsH = 128;
+constexpr int kXmodThreadsH = 256;  // xillver model kernel
 
 size_t setup_smem_bytes();
 size_t line_smem_bytes(int nr, int ng, bool limb, int tile);
@@ -37,6 +38,12 @@ cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, in
                            int *err, const int *order);
 void launch_xill_order(cudaStream_t s, const RelxSetState *sst, const RelxCorners *cor, const RelxZoneCorners *zcor,
                        int n_sets, int *order);
+
+// the xillver model: one CTA per set, writes the flux and the status fields of the set state
+size_t xillver_model_smem_bytes(int n_ener, int n_ener_pad);
+cudaError_t xillver_model_set_smem(int n_ener, int n_ener_pad);
+cudaError_t launch_xillver_model(cudaStream_t s, const RelxTables &tab, int n_sets, const RelxSetIn *sin,
+                                 const double *user_e, RelxSetState *sst, double *flux);
 
 __global__ void conv_zone_kernel(RelxTables tab, const RelxSetState *sst, const float *prof, const double *tsum,
                                  int ntile_max, int tile_bins, const float *xill, int nza, float *cout, int *err);

@@ -103,14 +103,14 @@ struct Tables {
   RelxTables d{};
   DevBuf rel_a, rel_mu0, rel_r, rel_gmin, rel_gmax, rel_tc;
   DevBuf lp_a, lp_h, lp_rad, lp_intens, lp_del, lp_delinc;
-  DevBuf x_vals, x_spec, x_e;
+  DevBuf x_vals, x_spec, x_e, x_ew;
   DevBuf conv_e, conv_eff, conv_inv_emid, conv_cf, conv_cw, coarse_e, coarse_t;
   DevBuf rb_imin, rb_imax, rb_fmin, rb_fmax, rb_pack;
   size_t bytes_total = 0;
   bool loaded = false;
   void release() {
     for (DevBuf *b : {&rel_a, &rel_mu0, &rel_r, &rel_gmin, &rel_gmax, &rel_tc, &lp_a, &lp_h, &lp_rad, &lp_intens,
-                      &lp_del, &lp_delinc, &x_vals, &x_spec, &x_e, &conv_e, &conv_eff, &conv_inv_emid, &conv_cf,
+                      &lp_del, &lp_delinc, &x_vals, &x_spec, &x_e, &x_ew, &conv_e, &conv_eff, &conv_inv_emid, &conv_cf,
                       &conv_cw, &coarse_e, &coarse_t, &rb_imin, &rb_imax, &rb_fmin, &rb_fmax, &rb_pack})
       b->release();
     loaded = false;
@@ -297,7 +297,9 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
     RELX_CUDA(cudaMemcpy(dst + (size_t) r0 * pad, buf.data(), sizeof(float) * (size_t) nr * pad, cudaMemcpyHostToDevice));
   }
   std::vector<double> xe = xe_host;
-  if ((st = upload(T.x_vals, vals)) || (st = upload(T.x_e, xe))) return st;
+  std::vector<float2> xew((size_t) ne + 1);
+  for (int i = 0; i <= ne; i++) xew[i] = make_float2((float) xe[i], i < ne ? (float) (xe[i + 1] - xe[i]) : 0.0f);
+  if ((st = upload(T.x_vals, vals)) || (st = upload(T.x_e, xe)) || (st = upload(T.x_ew, xew))) return st;
   T.d.x_npar = npar; T.d.x_nener = ne; T.d.x_nener_pad = pad; T.d.x_nincl = nvals[npar - 1];
   for (int q = 0; q < RELX_MAX_XPAR; q++) { T.d.x_nvals[q] = q < npar ? nvals[q] : 0; T.d.x_pindex[q] = q < npar ? pidx[q] : -1; }
   T.d.x_has_dens = has_dens;
@@ -306,6 +308,7 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
   T.d.x_spec = T.x_spec.as<float>();
   T.d.x_rows = rows;
   T.d.x_e = T.x_e.as<double>();
+  T.d.x_ew = T.x_ew.as<float2>();
   T.bytes_total += (size_t) rows * pad * 4;
   return 0;
 }
@@ -426,6 +429,9 @@ static int model_nparams(int model) {
     case RELX_RELCONV: return 8;    // :13-21
     case RELX_RELXILL: return 13;   // :46-59
     case RELX_RELXILLLP: return 14; // :61-75
+    case RELX_RELLINELP: return 10; // :23-33
+    case RELX_RELCONVLP: return 9;  // :35-44
+    case RELX_XILLVER: return 7;    // :77-84
     default: return -1;
   }
 }
@@ -448,6 +454,7 @@ static EnvOpts read_env() {
 
 // number of zones a set will use (get_num_zones, relutility.c:506-544)
 static int zones_for(int model, int ion_grad_type, int envn) {
+  if (model == RELX_XILLVER) return 1;
   if (ion_grad_type != 0) return (envn > 9 && envn <= RELX_NZMAX) ? envn : RELX_NZONES_IONGRAD;
   if (model == RELX_RELXILLLP) return (envn > 0 && envn <= RELX_NZMAX) ? envn : RELX_NZONES;
   return 1;
@@ -508,6 +515,7 @@ static int set_kernel_attrs(const Tables &T) {
   RELX_CUDA(cudaFuncSetAttribute(setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) setup_smem_bytes()));
   RELX_CUDA(relline_set_smem(T.d.rel_nr, T.d.rel_ng));
   RELX_CUDA(xillver_set_smem(T.d.x_nincl));
+  RELX_CUDA(xillver_model_set_smem(T.d.x_nener, T.d.x_nener_pad));
   RELX_CUDA(cudaFuncSetAttribute(conv_zone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
   RELX_CUDA(cudaFuncSetAttribute(relconv_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
   RELX_CUDA(cudaFuncSetAttribute(finalize_relxill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) fin_smem_bytes()));
@@ -626,24 +634,27 @@ struct BatchShape {
 static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b, bool need_zone_corners) {
   const size_t S = b.n_sets;
   const size_t nza = b.nza;
+  const int kind = relx_kind(b.model);
   int st;
   if ((st = W.setin.reserve(S * sizeof(RelxSetIn))) || (st = W.st.reserve(S * sizeof(RelxSetState))) ||
-      (st = W.rad.reserve(S * sizeof(RelxRadial))) || (st = W.dist.reserve(S * nza * RELX_MAX_INCL * sizeof(float))) ||
-      (st = W.tsum.reserve(S * b.nblk * nza * sizeof(double))) ||
       (st = W.user_e.reserve(b.n_edges * sizeof(double))) || (st = W.flux.reserve(b.n_edges * sizeof(double))) ||
       (st = W.sflag.reserve(S * sizeof(int))) || (st = W.status.reserve(S * sizeof(int))) ||
       (st = W.err.reserve(sizeof(int))) || (st = W.cslot.reserve(S * sizeof(int))))
     return st;
-  if (b.model == RELX_RELLINE) {
+  if (kind == RELX_XILLVER) return 0;  // no line profile, no convolution
+  if ((st = W.rad.reserve(S * sizeof(RelxRadial))) || (st = W.dist.reserve(S * nza * RELX_MAX_INCL * sizeof(float))) ||
+      (st = W.tsum.reserve(S * b.nblk * nza * sizeof(double))))
+    return st;
+  if (kind == RELX_RELLINE) {
     if ((st = W.line_e.reserve(b.n_edges * sizeof(double))) || (st = W.prof.reserve(b.n_edges * sizeof(float))))
       return st;
   } else {
     if ((st = W.prof.reserve(S * nza * RELX_NCONV * sizeof(float))) ||
         (st = W.cout.reserve(S * nza * RELX_NCONV * sizeof(float))))
       return st;
-    if (b.model == RELX_RELCONV && (st = W.user_f.reserve(b.n_edges * sizeof(double)))) return st;
+    if (kind == RELX_RELCONV && (st = W.user_f.reserve(b.n_edges * sizeof(double)))) return st;
   }
-  if (b.model >= RELX_RELXILL) {
+  if (relx_is_relxill(kind)) {
     if ((st = W.corners.reserve(S * sizeof(RelxCorners))) || (st = W.order.reserve(S * sizeof(int))) ||
         (st = W.xill.reserve(S * nza * (size_t) T.d.x_nener_pad * sizeof(float))))
       return st;
@@ -659,7 +670,8 @@ static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b,
 static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStream_t s, int base, int n, bool cached) {
   const RelxTables &tab = C.T.d;
   const size_t nza = b.nza;
-  const bool conv_grid = b.model != RELX_RELLINE;
+  const int kind = relx_kind(b.model);
+  const bool conv_grid = kind != RELX_RELLINE;
   RelxSetIn *sin = W.setin.as<RelxSetIn>() + base;
   RelxSetState *sst = W.st.as<RelxSetState>() + base;
   RelxRadial *rad = W.rad.as<RelxRadial>() + base;
@@ -673,6 +685,16 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   int *sflag = W.sflag.as<int>() + base;
   double *flux = W.flux.as<double>() - base;  // kernels address set i at e_off(i) - i
   const double *user_e = W.user_e.as<double>();
+  if (kind == RELX_XILLVER) {
+    {
+      ProfScope ps(PK_XILL, s);
+      RELX_CUDA(launch_xillver_model(s, tab, n, sin, user_e, sst, flux));
+    }
+    ProfScope ps(PK_STATUS, s);
+    status_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, sst, sflag, W.err.as<int>(), W.status.as<int>() + base);
+    RELX_CUDA(cudaGetLastError());
+    return 0;
+  }
   {
     ProfScope ps(PK_SETUP, s);
     setup_kernel<<<n, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, b.model, sin, user_e, W.line_e.as<double>(), sst,
@@ -686,8 +708,8 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
                          dist));
   }
   {
-    ProfScope ps(PK_LINE, s, 1 + (b.any_limb ? 1 : 0) + (b.model >= RELX_RELXILL ? 1 : 0));
-    RELX_CUDA(launch_relline(b.model >= RELX_RELXILL, n, b.line_tile, b.nblk, s, tab, sin, sst, rad,
+    ProfScope ps(PK_LINE, s, 1 + (b.any_limb ? 1 : 0) + (relx_is_relxill(kind) ? 1 : 0));
+    RELX_CUDA(launch_relline(relx_is_relxill(kind), n, b.line_tile, b.nblk, s, tab, sin, sst, rad,
                              W.line_e.as<double>(), b.nza, prof, dist, tsum, b.any_limb));
   }
   if (cached) {
@@ -698,7 +720,7 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     RELX_CUDA(cudaEventRecord(C.cache_ev, s));
     C.cache_ev_valid = true;
   }
-  if (b.model >= RELX_RELXILL) {
+  if (relx_is_relxill(kind)) {
     {
       ProfScope ps(PK_XILL, s, b.nza <= RELX_ZDENSE ? 2 : 1);
       int *order = W.order.as<int>() + base;
@@ -715,7 +737,7 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
       ProfScope ps(PK_FIN, s);
       finalize_relxill_kernel<<<n, kFinThreadsH, fin_smem_bytes(), s>>>(tab, sin, sst, cout, b.nza, user_e, flux);
     }
-  } else if (b.model == RELX_RELCONV) {
+  } else if (kind == RELX_RELCONV) {
     ProfScope ps(PK_CONV, s, 2);  // convolution and finalize
     relconv_conv_kernel<<<n, kConvThreadsH, conv_smem_bytes(), s>>>(tab, sin, sst, prof, tsum, b.nblk,
                                                                     kSumBinsH, b.nza, user_e, W.user_f.as<double>(),
@@ -790,7 +812,8 @@ static void graphs_clear(Context &C) {
 // workspace buffers (a sampler or fit that evaluates the same number of sets on the same grids
 // every step).
 static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStream_t s, bool use_cache) {
-  const bool cached = use_cache && C.cache.enabled() && b.model != RELX_RELLINE;
+  const bool cached = use_cache && C.cache.enabled() && relx_kind(b.model) != RELX_RELLINE &&
+                      b.model != RELX_XILLVER;
   if (cached || g_prof.on || !C.graphs_on || s == nullptr) return launch_direct(C, W, b, s, cached);
   const std::vector<uintptr_t> key = graph_key(W, b);
   for (auto &g : C.graphs) {
@@ -848,7 +871,8 @@ static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStrea
 // tile, and the chunks only reorder independent sets), so the last trial's results stand.  The
 // trials synchronise the stream.
 static int tuned_launch(Context &C, Workspace &W, BatchShape &b, cudaStream_t s, bool use_cache) {
-  const bool cached = use_cache && C.cache.enabled() && b.model != RELX_RELLINE;
+  const bool cached = use_cache && C.cache.enabled() && relx_kind(b.model) != RELX_RELLINE &&
+                      b.model != RELX_XILLVER;
   int sclass = 0;
   while ((1 << (sclass + 1)) <= b.n_sets) sclass++;
   const Context::TuneEntry *known = nullptr;
@@ -864,7 +888,8 @@ static int tuned_launch(Context &C, Workspace &W, BatchShape &b, cudaStream_t s,
   } else {
     b.line_tile = b.n_sets <= 1024 ? 256 : 512;  // small batches: more CTAs per set
   }
-  if (known || !C.autotune_on || g_prof.on || cached || explicit_choice || b.model == RELX_RELLINE)
+  if (known || !C.autotune_on || g_prof.on || cached || explicit_choice || relx_kind(b.model) == RELX_RELLINE ||
+      b.model == RELX_XILLVER)
     return launch_batch(C, W, b, s, use_cache);
   struct Cand { int tile, chunk; };
   std::vector<Cand> cands = {{512, 0}, {256, 0}};
@@ -915,8 +940,9 @@ static int batch_shape(int model, int n_sets, const int64_t *eoff_host, const in
   }
   b->nza = nza;
   b->chunk = chunk_sets();
-  b->any_limb = (model == RELX_RELLINE || model == RELX_RELCONV);
-  const int gmax = (model == RELX_RELLINE) ? maxn : RELX_NCONV;
+  const int kind = relx_kind(model);
+  b->any_limb = (kind == RELX_RELLINE || kind == RELX_RELCONV);
+  const int gmax = (kind == RELX_RELLINE) ? maxn : RELX_NCONV;
   b->nblk = (gmax + kSumBinsH - 1) / kSumBinsH;
   *need_zc = nza > RELX_ZDENSE;
   return 0;
@@ -929,7 +955,8 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
                               bool use_cache, size_t *o_flux, size_t *o_status) {
   const int model = hb.model, n_sets = hb.n_sets;
   if (model < 0 || model >= RELX_NMODELS || n_sets <= 0 || !hb.params || !hb.energy || !hb.eoff) return RELX_ERR_ARG;
-  if (model == RELX_RELCONV && !hb.flux_in) return RELX_ERR_ARG;
+  const bool conv = relx_kind(model) == RELX_RELCONV;
+  if (conv && !hb.flux_in) return RELX_ERR_ARG;
   const EnvOpts env = read_env();
   BatchShape b;
   bool need_zc = false;
@@ -940,7 +967,7 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
   const size_t pb = sizeof(double) * (size_t) n_sets * npar, eb = sizeof(double) * (size_t) b.n_edges;
   const size_t ob = sizeof(int64_t) * (size_t) (n_sets + 1), gb = hb.igt ? sizeof(int) * n_sets : 0,
                ib = hb.igi ? sizeof(double) * n_sets : 0;
-  const size_t fb = (model == RELX_RELCONV) ? eb : 0;
+  const size_t fb = conv ? eb : 0;
   const size_t nflux = (size_t) (b.n_edges - n_sets);
   if ((st = P.reserve(pb + eb + ob + gb + ib + fb + nflux * sizeof(double) + sizeof(int) * n_sets + 64 * 10)))
     return st;
@@ -955,7 +982,7 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
   size_t o_p = put(hb.params, pb), o_e = put(hb.energy, eb), o_o = put(hb.eoff, ob);
   size_t o_g = hb.igt ? put(hb.igt, gb) : 0, o_i = hb.igi ? put(hb.igi, ib) : 0;
   size_t o_f = 0;
-  if (model == RELX_RELCONV) {
+  if (conv) {
     // input flux arrives with n per set; spread to the edge layout (offset e_off per set)
     o_f = put(nullptr, fb);
     double *fi = (double *) (h + o_f);
@@ -974,7 +1001,7 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
   RELX_CUDA(cudaMemcpyAsync(W.eoff.p, h + o_o, ob, cudaMemcpyHostToDevice, s));
   if (hb.igt) RELX_CUDA(cudaMemcpyAsync(W.igt.p, h + o_g, gb, cudaMemcpyHostToDevice, s));
   if (hb.igi) RELX_CUDA(cudaMemcpyAsync(W.igi.p, h + o_i, ib, cudaMemcpyHostToDevice, s));
-  if (model == RELX_RELCONV) RELX_CUDA(cudaMemcpyAsync(W.user_f.p, h + o_f, fb, cudaMemcpyHostToDevice, s));
+  if (conv) RELX_CUDA(cudaMemcpyAsync(W.user_f.p, h + o_f, fb, cudaMemcpyHostToDevice, s));
   {
     ProfScope ps(PK_PACK, s);
     pack_kernel<<<(n_sets + 127) / 128, 128, 0, s>>>(n_sets, npar, W.params.as<double>(), W.eoff.as<int64_t>(),
@@ -1070,10 +1097,14 @@ int slot_wait(BatchSlot *b, const double **flux, const int **status) {
 }
 
 size_t batch_device_bytes(int model, int n_sets, int64_t n_edges, int nza) {
+  const int kind = relx_kind(model);
+  if (kind == RELX_XILLVER)
+    return (sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(int) * 4) * (size_t) n_sets +
+           sizeof(double) * 2 * (size_t) n_edges;
   size_t per_set = sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(RelxRadial) + sizeof(int) * 4 +
                    sizeof(float) * nza * RELX_MAX_INCL + sizeof(double) * (RELX_NCONV / kSumBinsH) * nza;
-  if (model != RELX_RELLINE) per_set += 2 * sizeof(float) * (size_t) nza * RELX_NCONV;
-  if (model >= RELX_RELXILL) per_set += sizeof(RelxCorners) + sizeof(float) * (size_t) nza * 4096;
+  if (kind != RELX_RELLINE) per_set += 2 * sizeof(float) * (size_t) nza * RELX_NCONV;
+  if (relx_is_relxill(kind)) per_set += sizeof(RelxCorners) + sizeof(float) * (size_t) nza * 4096;
   return per_set * (size_t) n_sets + sizeof(double) * 3 * (size_t) n_edges;
 }
 
@@ -1165,7 +1196,7 @@ int relx_eval_batch_device(int model, int n_sets, const double *d_params, const 
   cudaStream_t s = stream ? (cudaStream_t) stream : C.stream;
   Workspace &W = C.W;
   RELX_CUDA(cudaMemcpyAsync(W.user_e.p, d_energy, sizeof(double) * b.n_edges, cudaMemcpyDeviceToDevice, s));
-  if (model == RELX_RELCONV) {
+  if (relx_kind(model) == RELX_RELCONV) {
     if (!d_flux_in) return RELX_ERR_ARG;
     RELX_CUDA(cudaMemcpyAsync(W.user_f.p, d_flux_in, sizeof(double) * b.n_edges, cudaMemcpyDeviceToDevice, s));
   }
@@ -1319,14 +1350,15 @@ static void lmod_eval(int model, const double *energy, int Nflux, const double *
   int status = 0;
   std::vector<double> out((size_t) Nflux);
   std::vector<double> in;
-  if (model == RELX_RELCONV) in.assign(flux, flux + Nflux);
+  const bool conv = relx_kind(model) == RELX_RELCONV;
+  if (conv) in.assign(flux, flux + Nflux);
   HostBatch hb;
   hb.model = model;
   hb.n_sets = 1;
   hb.params = parameter;
   hb.energy = energy;
   hb.eoff = eoff;
-  hb.flux_in = model == RELX_RELCONV ? in.data() : nullptr;
+  hb.flux_in = conv ? in.data() : nullptr;
   int st = eval_host(hb, out.data(), &status);
   g_last_status = st ? st : status;
   if (st == 0 || st == status) {
@@ -1356,6 +1388,21 @@ void c_lmodrelxilllp(const double *energy, int Nflux, const double *parameter, i
                      double *fluxError, const char *init) {
   (void) spectrum; (void) fluxError; (void) init;
   lmod_eval(RELX_RELXILLLP, energy, Nflux, parameter, flux);
+}
+void c_lmodrellinelp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                     double *fluxError, const char *init) {
+  (void) spectrum; (void) fluxError; (void) init;
+  lmod_eval(RELX_RELLINELP, energy, Nflux, parameter, flux);
+}
+void c_lmodrelconvlp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                     double *fluxError, const char *init) {
+  (void) spectrum; (void) fluxError; (void) init;
+  lmod_eval(RELX_RELCONVLP, energy, Nflux, parameter, flux);
+}
+void c_lmodxillver(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                   double *fluxError, const char *init) {
+  (void) spectrum; (void) fluxError; (void) init;
+  lmod_eval(RELX_XILLVER, energy, Nflux, parameter, flux);
 }
 
 }  // extern "C"

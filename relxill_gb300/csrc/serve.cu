@@ -122,13 +122,14 @@ void Server::scheduler() {
     S.igi.resize(n);
     for (int i = 0; i < n; i++) S.eoff[i + 1] = S.eoff[i] + S.reqs[i].n_bins + 1;
     S.energy.resize((size_t) S.eoff[n]);
-    if (model == RELX_RELCONV) S.flux_in.resize((size_t) (S.eoff[n] - n));
+    const bool conv = relx_kind(model) == RELX_RELCONV;
+    if (conv) S.flux_in.resize((size_t) (S.eoff[n] - n));
     bool any_ig = false;
     for (int i = 0; i < n; i++) {
       const Request &r = S.reqs[i];
       std::memcpy(&S.params[(size_t) i * npar], r.params, sizeof(double) * npar);
       std::memcpy(&S.energy[(size_t) S.eoff[i]], r.energy, sizeof(double) * (r.n_bins + 1));
-      if (model == RELX_RELCONV) std::memcpy(&S.flux_in[(size_t) (S.eoff[i] - i)], r.flux_in, sizeof(double) * r.n_bins);
+      if (conv) std::memcpy(&S.flux_in[(size_t) (S.eoff[i] - i)], r.flux_in, sizeof(double) * r.n_bins);
       S.igt[i] = r.igt;
       S.igi[i] = r.igi;
       any_ig = any_ig || r.igt != 0;
@@ -139,7 +140,7 @@ void Server::scheduler() {
     hb.params = S.params.data();
     hb.energy = S.energy.data();
     hb.eoff = S.eoff.data();
-    hb.flux_in = model == RELX_RELCONV ? S.flux_in.data() : nullptr;
+    hb.flux_in = conv ? S.flux_in.data() : nullptr;
     hb.igt = any_ig ? S.igt.data() : nullptr;
     hb.igi = any_ig ? S.igi.data() : nullptr;
     S.status = slot_enqueue(S.slot, hb, use_cache);
@@ -228,7 +229,7 @@ relx_server *relx_serve_create(int64_t hbm_budget_bytes, int max_batch, int cach
 int64_t relx_serve_submit(relx_server *h, int model, const double *params, const double *energy, int n_bins,
                           const double *flux_in, double *flux_out, int ion_grad_type, double iongrad_index) {
   if (!h || model < 0 || model >= RELX_NMODELS || !params || !energy || !flux_out || n_bins < 1) return -RELX_ERR_ARG;
-  if (model == RELX_RELCONV && !flux_in) return -RELX_ERR_ARG;
+  if (relx_kind(model) == RELX_RELCONV && !flux_in) return -RELX_ERR_ARG;
   Request r;
   r.model = model;
   r.n_bins = n_bins;

@@ -61,7 +61,8 @@ struct SetupSmem {
 __device__ void map_params(int model, const RelxSetIn &in, SetupSmem &m) {
   RelxSetState &s = m.s;
   const double *v = in.p;
-  s.model = model;
+  s.model = relx_kind(model);
+  s.pmodel = model;
   s.status = RELX_OK;
   s.cached = 0;
   s.limb = 0;
@@ -93,6 +94,16 @@ __device__ void map_params(int model, const RelxSetIn &in, SetupSmem &m) {
       s.emis_type = RELX_EMIS_BKN;
       m.emis1 = v[0]; m.emis2 = v[1]; m.rbr = v[2]; s.a = v[3]; s.incl = v[4] * kPi / 180;
       s.rin = v[5]; s.rout = v[6]; s.limb = (int) llround(v[7]);
+      break;
+    case RELX_RELLINELP:  // lmodel_relxill_public.dat:23-33; no source velocity
+      s.emis_type = RELX_EMIS_LP;
+      s.lineE = v[0]; s.height = v[1]; s.a = v[2]; s.incl = v[3] * kPi / 180; s.rin = v[4]; s.rout = v[5];
+      s.z = v[6]; s.limb = (int) llround(v[7]); s.gam = v[8]; m.return_rad = (int) llround(v[9]);
+      break;
+    case RELX_RELCONVLP:  // lmodel_relxill_public.dat:35-44
+      s.emis_type = RELX_EMIS_LP;
+      s.height = v[0]; s.beta = v[1]; s.a = v[2]; s.incl = v[3] * kPi / 180; s.rin = v[4]; s.rout = v[5];
+      s.limb = (int) llround(v[6]); s.gam = v[7]; m.return_rad = (int) llround(v[8]);
       break;
     case RELX_RELXILL:
       m.is_relxill = 1;
@@ -221,6 +232,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   const int tid = threadIdx.x;
   const RelxSetIn &in = sin[set];
   const int NR = RELX_NFRAD;
+  const int kind = relx_kind(model);
 
   if (tid == 0) {
     map_params(model, in, m);
@@ -236,7 +248,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   // ---- line-profile grid: user grid (redshift, 1 keV line) for relline, conv grid otherwise
   const double *ge;
   int gn;
-  if (model == RELX_RELLINE) {
+  if (kind == RELX_RELLINE) {
     const double *ue = user_e + in.e_off;
     double *le = line_e + in.e_off;
     gn = in.n_ener;
@@ -349,7 +361,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     if (egmax > ge[0] && egmin < ge[gn]) {
       if (egmin < ge[0]) egmin = ge[0];
       if (egmax > ge[gn]) egmax = ge[gn];
-      if (model == RELX_RELLINE) {
+      if (kind == RELX_RELLINE) {
         ielo = bsearch_asc<double>(ge, gn + 1, egmin);
         iehi = bsearch_asc<double>(ge, gn + 1, egmax);
       } else {
@@ -522,9 +534,9 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   }
   __syncthreads();
   // conv-grid bins the final rebin to the caller's grid reads (Relxill.cpp:267-278, Relbase.cpp:281-284)
-  if (tid == 0 && model != RELX_RELLINE) {
+  if (tid == 0 && kind != RELX_RELLINE) {
     const double *ue = user_e + in.e_off;
-    double zf = (model != RELX_RELCONV && s.z > 0) ? (1 + s.z) : 1.0;
+    double zf = (kind != RELX_RELCONV && s.z > 0) ? (1 + s.z) : 1.0;
     double elo = ue[0] * zf, ehi = ue[in.n_ener] * zf;
     const double *ce = tab.conv_e;
     int lo = conv_index(tab, elo);  // as bsearch_asc over the N + 1 edges
@@ -627,21 +639,8 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       const double shift = (qq == 0) ? 1.0 : m.shift[qq - 1];
       if (qq > 0 && shift == 1.0) continue;
       const float ecut = (float) (s.ect_src * shift);
-      float2 part = make_float2(0.0f, 0.0f);
-      for (int b = lane; b < RELX_NCOARSE; b += 32) {
-        const float4 t = tab.coarse_t[b];  // bin centre, width, centre as float-float (0 outside the band)
-        // spec_cutoffpl term (Xillspec.cpp:215-233), FP32 arithmetic
-        const float term = expf(1.0f / ecut) * m.cpow[b] * expf(-t.x / ecut) * t.y;
-        part = ff_add(part, ff_mulf(make_float2(t.z, t.w), term));
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        float2 u;
-        u.x = __shfl_xor_sync(0xffffffffu, part.x, o);
-        u.y = __shfl_xor_sync(0xffffffffu, part.y, o);
-        part = ff_add(part, u);
-      }
-      if (lane == 0) m.qsum[qq] = ff_to_double(part) * 1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi);
+      const double q = primary_qsum_warp(tab, gam, ecut, m.cpow);
+      if (lane == 0) m.qsum[qq] = q;
     }
     __syncthreads();
     const double src_norm = 1.0 / m.qsum[0];

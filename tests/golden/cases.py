@@ -10,6 +10,8 @@ def log_grid(emin, emax, n):
 GRID_LINE = ("line", 0.1, 20.0, 3000)      # relline: 3000 log bins 0.1-20 keV
 GRID_WIDE = ("wide", 0.1, 1000.0, 3000)    # relxill / relxilllp output grid
 GRID_CONV = ("convin", 0.3, 80.0, 500)      # relconv input grid
+GRID_XLOW = ("xlow", 0.01, 2000.0, 1500)    # xillver: a grid reaching past both ends of the table
+CONV_MODELS = ("relconv", "relconv_lp")
 
 CASES = [
     # (name, model, params, grid, iongrad_type, iongrad_index)
@@ -25,6 +27,17 @@ CASES = [
     ("relxilllp_c", "relxilllp", [50, 0, -0.5, 10, -3, 100, 0, 1.5, 0.5, 0.7, 800, -1, 0, 0], GRID_WIDE, 0, 0.0),
     ("relxilllp_pl", "relxilllp", [10, 0, 0.9, 45, -1, 400, 0, 2.0, 3.1, 1, 300, 1, 0, 0], GRID_WIDE, 1, 0.5),
     ("relxilllp_alpha", "relxilllp", [5, 0, 0.5, 30, -1, 400, 0, 2.2, 2.0, 1, 100, 1, 0, 0], GRID_WIDE, 2, 0.0),
+    ("rellinelp_a", "relline_lp", [6.4, 6, 0.998, 30, -1, 400, 0, 0, 2, 0], GRID_LINE, 0, 0.0),
+    ("rellinelp_b", "relline_lp", [1.0, 3, 0.5, 60, -1, 100, 0.1, 1, 2.5, 0], GRID_LINE, 0, 0.0),
+    ("rellinelp_c", "relline_lp", [6.97, 50, -0.5, 80, -3, 1000, 0, 2, 1.4, 0], GRID_LINE, 0, 0.0),
+    ("relconvlp_a", "relconv_lp", [6, 0, 0.998, 30, -1, 400, 0, 2, 0], GRID_CONV, 0, 0.0),
+    ("relconvlp_b", "relconv_lp", [20, 0.5, 0.3, 70, -2, 300, 2, 1.6, 0], GRID_CONV, 0, 0.0),
+    ("xillver_a", "xillver", [2, 1, 300, 3.1, 0, 30, -1], GRID_WIDE, 0, 0.0),
+    ("xillver_b", "xillver", [1.7, 3, 80, 1.5, 0.05, 60, 2.5], GRID_WIDE, 0, 0.0),
+    # Ecut and logxi on their upper bounds, incl below the table, primary only
+    ("xillver_c", "xillver", [2.5, 0.7, 1000, 4.7, 0, 5, 0], GRID_XLOW, 0, 0.0),
+    # parameters on grid values or clamped (zero-weight corners), z = 1
+    ("xillver_d", "xillver", [1.0, 10, 5, 0, 1.0, 87, 1], GRID_XLOW, 0, 0.0),
 ]
 
 

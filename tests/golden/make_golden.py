@@ -16,9 +16,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 from relxill_gb300 import synth_tables  # noqa: E402
-from cases import CASES, grid, conv_input  # noqa: E402
+from cases import CASES, CONV_MODELS, grid, conv_input  # noqa: E402
 
-MODEL_ID = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3}
+MODEL_ID = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3, "relline_lp": 4, "relconv_lp": 5, "xillver": 6}
 
 
 def main():
@@ -32,7 +32,7 @@ def main():
     for name, model, params, gspec, igt, igi in CASES:
         e = grid(gspec)
         p = np.asarray(params, dtype=np.float64)
-        f = conv_input(e) if model == "relconv" else np.zeros(len(e) - 1)
+        f = conv_input(e) if model in CONV_MODELS else np.zeros(len(e) - 1)
         ref.ref_reset_xillver_cache()
         if igt:
             rc = ref.ref_eval_relxilllp_iongrad(p.ctypes.data_as(dp), igt, ctypes.c_double(igi), e.ctypes.data_as(dp),

@@ -15,7 +15,8 @@ def declared_functions():
 
 def test_header_declares_the_reference_entry_points():
     names = declared_functions()
-    for n in ("c_lmodrelline", "c_lmodrelconv", "c_lmodrelxill", "c_lmodrelxilllp", "relx_eval_batch",
+    for n in ("c_lmodrelline", "c_lmodrelconv", "c_lmodrelxill", "c_lmodrelxilllp", "c_lmodrellinelp",
+              "c_lmodrelconvlp", "c_lmodxillver", "relx_eval_batch",
               "relx_eval_batch_device", "relx_last_status", "relx_init"):
         assert n in names
 

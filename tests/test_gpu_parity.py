@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import oracle_lib
-from cases import CASES, conv_input, grid
+from cases import CASES, CONV_MODELS, conv_input, grid
 from tolerance import assert_close, compare
 
 pytestmark = pytest.mark.gpu
@@ -20,7 +20,7 @@ def _zones_env(monkeypatch):
 
 
 def _gpu_eval(R, model, params, e, igt=0, igi=0.0):
-    fin = [conv_input(e)] if model == "relconv" else None
+    fin = [conv_input(e)] if model in CONV_MODELS else None
     out, st = R.eval_batch(model, np.asarray(params)[None], [e], flux_in=fin,
                            ion_grad_type=[igt] if igt else None, iongrad_index=[igi] if igt else None)
     assert st[0] == 0, (model, st[0], R.last_error())
@@ -32,7 +32,7 @@ def test_case_vs_oracle_and_reference(gpu, oracle, case):
     name, model, params, gspec, igt, igi = case
     e = grid(gspec)
     got = _gpu_eval(gpu, model, params, e, igt, igi)
-    st, orc = oracle_lib.evaluate(model, params, e, conv_input(e) if model == "relconv" else None, igt, igi)
+    st, orc = oracle_lib.evaluate(model, params, e, conv_input(e) if model in CONV_MODELS else None, igt, igi)
     assert st == 0
     assert_close(got, orc, f"{name} vs oracle")
     ref = np.load(GOLDEN)[name]

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle_lib
-from cases import CASES, conv_input, grid
+from cases import CASES, CONV_MODELS, conv_input, grid
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden_small.npz")
 LIMIT_PREC = 1e-6  # test/unit (LIMIT_PREC of the reference's unit tests)
@@ -87,7 +87,7 @@ def test_all_models_execute(oracle, small_tables):
     # tests-execmodel.cpp:87-105
     for name, model, params, gspec, igt, igi in CASES[:10]:
         e = grid(gspec)
-        st, f = oracle_lib.evaluate(model, params, e, conv_input(e) if model == "relconv" else None)
+        st, f = oracle_lib.evaluate(model, params, e, conv_input(e) if model in CONV_MODELS else None)
         assert st == 0 and f.sum() > 0, name
 
 
@@ -97,7 +97,7 @@ def test_oracle_equals_compiled_reference(oracle, small_tables, monkeypatch, cas
     monkeypatch.setenv("RELXILL_NUM_RZONES", "10")
     name, model, params, gspec, igt, igi = case
     e = grid(gspec)
-    st, f = oracle_lib.evaluate(model, params, e, conv_input(e) if model == "relconv" else None, igt, igi)
+    st, f = oracle_lib.evaluate(model, params, e, conv_input(e) if model in CONV_MODELS else None, igt, igi)
     ref = np.load(GOLDEN)[name]
     assert st == 0
     m = ref > 1e-12 * ref.max()

@@ -7,12 +7,12 @@ import ctypes
 import numpy as np
 import pytest
 
-from cases import CASES, conv_input, grid
+from cases import CASES, CONV_MODELS, conv_input, grid
 from tolerance import assert_close
 
 pytestmark = pytest.mark.gpu
 
-MODELS = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3}
+MODELS = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3, "relline_lp": 4, "relconv_lp": 5, "xillver": 6}
 RELX_ERR_ARG = 9
 
 
@@ -34,7 +34,7 @@ class _Call:
         self.n = len(e) - 1
         self.params = torch.tensor(np.asarray(params, dtype=np.float64), device=dev)
         self.energy = torch.tensor(np.asarray(e, dtype=np.float64), device=dev)
-        self.fin = torch.tensor(conv_input(e), device=dev) if model == "relconv" else None
+        self.fin = torch.tensor(conv_input(e), device=dev) if model in CONV_MODELS else None
         self.flux = torch.full((self.n,), -1.0, dtype=torch.float64, device=dev)
         self.status = torch.full((1,), -1, dtype=torch.int32, device=dev)
 
@@ -45,7 +45,7 @@ class _Call:
 
 
 def _batch(R, model, params, e, igt=0, igi=0.0):
-    fin = [conv_input(e)] if model == "relconv" else None
+    fin = [conv_input(e)] if model in CONV_MODELS else None
     out, st = R.eval_batch(model, np.asarray(params)[None], [e], flux_in=fin,
                            ion_grad_type=[igt] if igt else None, iongrad_index=[igi] if igt else None)
     assert st[0] == 0, R.last_error()
@@ -59,7 +59,8 @@ def _case(name):
 def test_noalloc_matches_batch_on_two_calls_in_a_row(gpu):
     torch = pytest.importorskip("torch")
     f = _fn(gpu)
-    names = ["relxilllp_a", "relxill_cfg2", "relline_cfg1", "relconv_a", "relxilllp_alpha", "relxilllp_b"]
+    names = ["relxilllp_a", "relxill_cfg2", "relline_cfg1", "relconv_a", "relxilllp_alpha", "relxilllp_b",
+             "rellinelp_b", "relconvlp_b", "xillver_b", "xillver_d"]
     for name in names:
         _, model, params, gspec, igt, igi = _case(name)
         e = grid(gspec)
