@@ -17,9 +17,10 @@
  *  - tables are loaded eagerly (relline, lamp post) or per spectrum row on
  *    first use (xillver, like check_xilltab_cache).
  *
- * Scope: models relline, relconv, relxill, relxilllp (cut-off power law,
- * broken power-law or point lamp-post emissivity, ionisation gradients
- * CONST / PL / ALPHA), returning radiation switched off.
+ * Scope: models relline, relconv, relxill, relxilllp, relline_lp, relconv_lp
+ * and xillver (cut-off power law, broken power-law or point lamp-post
+ * emissivity, returning radiation with its xillver correction factors,
+ * ionisation gradients CONST / PL / ALPHA).
  */
 #define _POSIX_C_SOURCE 200809L
 #include "relx_oracle.h"
@@ -901,8 +902,243 @@ static int emis_lamp_post(const LpTable *tab, const Params *p, SysPar *sp) {
   return status;
 }
 
-/* get_system_parameters, Relprofile.cpp:310-358 (without the cache) */
-static SysPar *get_system_parameters(const Params *p, int *status) {
+/* ======================================================================= */
+/* returning radiation (Relreturn_Table.cpp, Relreturn_Corona.cpp)          */
+/* ======================================================================= */
+
+#define RRAD_NR 50  /* RETURNRAD_TABLE_NR / _NG, common.h:127-128 */
+#define RRAD_NG 20
+
+/* one spin of the table (tabulatedReturnFractions, Relreturn_Datastruct.h): row = incident bin,
+ * column = emitting bin */
+typedef struct {
+  double rlo[RRAD_NR], rhi[RRAD_NR];
+  double tf_r[RRAD_NR][RRAD_NR], gmin[RRAD_NR][RRAD_NR], gmax[RRAD_NR][RRAD_NR];
+  double frac_g[RRAD_NR][RRAD_NR][RRAD_NG];
+} RradFrac;
+
+typedef struct {
+  int nspin;
+  double *spin;
+  RradFrac *frac;
+} RradTable;
+
+static RradTable *g_rrad = NULL;
+
+/* fits_read_returnRadTable / fits_rr_load_single_fractions, Relreturn_Table.cpp:180-330 */
+static RradTable *load_rrad_table(void) {
+  char path[2048];
+  fullpath(path, "table_returnRad_v20220301.fits");
+  int st = 0;
+  fitsfile *fp = NULL;
+  if (fits_open_table(&fp, path, READONLY, &st)) return NULL;
+  RradTable *t = calloc(1, sizeof(RradTable));
+  long n = 0;
+  int c = 0;
+  fits_movnam_hdu(fp, BINARY_TBL, "SPIN", 0, &st);
+  fits_get_num_rows(fp, &n, &st);
+  fits_get_colnum(fp, CASEINSEN, "a", &c, &st);
+  if (!st && n > 0 && n <= 99) {
+    t->nspin = (int) n;
+    t->spin = malloc(sizeof(double) * n);
+    t->frac = calloc(n, sizeof(RradFrac));
+    fits_read_col(fp, TDOUBLE, c, 1, 1, n, NULL, t->spin, NULL, &st);
+  } else {
+    st = 1;
+  }
+  for (int k = 0; k < t->nspin && !st; k++) {
+    char ext[16];
+    snprintf(ext, sizeof ext, "FRAC%02d", k + 1);
+    fits_movnam_hdu(fp, BINARY_TBL, ext, 0, &st);
+    long nr = 0;
+    fits_get_num_rows(fp, &nr, &st);
+    if (st || nr != RRAD_NR) { st = 1; break; }
+    RradFrac *f = &t->frac[k];
+    const char *names[6] = {"rlo", "rhi", "tf_r", "gmin", "gmax", "frac_g"};
+    double *dst[6] = {f->rlo, f->rhi, &f->tf_r[0][0], &f->gmin[0][0], &f->gmax[0][0], &f->frac_g[0][0][0]};
+    const long cnt[6] = {RRAD_NR, RRAD_NR, RRAD_NR * RRAD_NR, RRAD_NR * RRAD_NR, RRAD_NR * RRAD_NR,
+                         (long) RRAD_NR * RRAD_NR * RRAD_NG};
+    for (int q = 0; q < 6 && !st; q++) {
+      fits_get_colnum(fp, CASEINSEN, names[q], &c, &st);
+      fits_read_col(fp, TDOUBLE, c, 1, 1, cnt[q], NULL, dst[q], NULL, &st);
+    }
+  }
+  fits_close_file(fp, &st);
+  if (st) {
+    free(t->spin);
+    free(t->frac);
+    free(t);
+    return NULL;
+  }
+  return t;
+}
+
+/* returningFractions (Relreturn_Datastruct.h) on the radial range of a model */
+typedef struct {
+  const RradFrac *tab;
+  int nrad;
+  int irad[RRAD_NR];
+  double rlo[RRAD_NR], rhi[RRAD_NR], rad[RRAD_NR];
+  double tf_r[RRAD_NR][RRAD_NR];
+} RradFractions;
+
+/* rradCorrFactors (common.h:182-189): per ionisation zone */
+typedef struct {
+  int n_zones;
+  double rgrid[N_ZONES_MAX + 1];
+  double corrfac_flux[N_ZONES_MAX], corrfac_gshift[N_ZONES_MAX];
+} RradCorr;
+
+/* get_ring_area_correction_factor, Relreturn_Table.cpp:518-538 */
+static double rrad_area_correction(const RradFractions *rf, int idx, double a) {
+  double rlo_table = rf->tab->rlo[rf->irad[idx]];
+  if (rf->irad[idx] == 0 && rlo_table > relxo_kerr_rms(a)) rlo_table = relxo_kerr_rms(a);
+  double rhi_table = rf->tab->rhi[rf->irad[idx]];
+  double area_table = 0.5 * (rlo_table + rhi_table) * (rhi_table - rlo_table);
+  double area_model = 0.5 * (rf->rlo[idx] + rf->rhi[idx]) * (rf->rhi[idx] - rf->rlo[idx]);
+  return area_model / area_table;
+}
+
+/* get_rrad_fractions: select_spinIndexForTable, allocate_radial_grid, get_interpolated_tfr
+ * (Relreturn_Table.cpp:393-611) */
+static int get_rrad_fractions(double a, double rin, double rout, RradFractions *rf) {
+  const RradTable *t = g_rrad;
+  int k = binary_search(t->spin, t->nspin, a);
+  if (t->spin[k] < a) k++;
+  if (k >= t->nspin || k < 0) return 1;
+  const RradFrac *tab = &t->frac[k];
+  rf->tab = tab;
+  int klo = binary_search(tab->rlo, RRAD_NR, rin);
+  int khi = binary_search(tab->rhi, RRAD_NR, rout);
+  if (fabs(rout - tab->rhi[RRAD_NR - 1]) < 1e-6) khi = RRAD_NR - 1;
+  else khi++;
+  if (fabs(rin - tab->rlo[0]) < 1e-6) klo = 0;
+  int n = (khi + 1) - klo;
+  if (n <= 0 || n > RRAD_NR) return 1;
+  rf->nrad = n;
+  for (int ii = 0; ii < n; ii++) {
+    rf->irad[ii] = klo + ii;
+    rf->rlo[ii] = tab->rlo[rf->irad[ii]];
+    rf->rhi[ii] = tab->rhi[rf->irad[ii]];
+  }
+  if (!(rin >= rf->rlo[0] - 1e-4)) return 1;
+  rf->rlo[0] = rin;
+  rf->rhi[n - 1] = rout;
+  for (int ii = 0; ii < n; ii++) rf->rad[ii] = 0.5 * (rf->rlo[ii] + rf->rhi[ii]);
+  for (int ii = 0; ii < n; ii++)
+    for (int jj = 0; jj < n; jj++) rf->tf_r[ii][jj] = tab->tf_r[rf->irad[ii]][rf->irad[jj]];
+  const double corr_rin = rrad_area_correction(rf, 0, a);
+  const double corr_rout = rrad_area_correction(rf, n - 1, a);
+  if (!(corr_rin - 1 < 1e-6) || !(corr_rout - 1 < 1e-6)) return 1;
+  for (int ii = 0; ii < n - 1; ii++) rf->tf_r[ii][0] *= corr_rin;
+  for (int ii = 0; ii < n - 2; ii++) rf->tf_r[ii][n - 1] *= corr_rout;
+  return 0;
+}
+
+/* corrected_gshift_fluxboost_factor, Relreturn_Corona.cpp:37-86 */
+static double corrected_gshift_fluxboost_factor(double xill_gshift_fac, double g, double gamma) {
+  const double g0 = 2. / 3;
+  double gshift_corr_factor;
+  if (xill_gshift_fac < 1) {
+    double a = (xill_gshift_fac / g0 - 1) / (g0 - 1);
+    double b = 1 - a;
+    gshift_corr_factor = (g >= 1) ? 1. / g * (1. / g * a + b) : g * (g * a + b);
+  } else {
+    double alin = (xill_gshift_fac - 1) / (g0 - 1);
+    double blin = 1 - alin;
+    gshift_corr_factor = (g >= 1) ? (1. / g * alin + blin) : (g * alin + blin);
+  }
+  double fluxboost_factor = pow(g, gamma) * gshift_corr_factor;
+  if (g < 1 && fluxboost_factor > 1) fluxboost_factor = 1;
+  if (fluxboost_factor < 0) fluxboost_factor = 0;
+  return fluxboost_factor;
+}
+
+/* calc_rrad_emis_zone + get_gfac_grid, Relreturn_Corona.cpp:103-123, Relreturn_Datastruct.cpp:51-59 */
+static double rrad_emis_zone(const RradFrac *tab, int ro, int re, double gamma, double corrfac_gshift) {
+  double emis_zone = 0.0;
+  for (int jj = 0; jj < RRAD_NG; jj++) {
+    const double g = (jj + 0.5) / RRAD_NG * (tab->gmax[ro][re] - tab->gmin[ro][re]) + tab->gmin[ro][re];
+    double e = tab->frac_g[ro][re][jj];
+    if (fabs(corrfac_gshift - 1) > 1e-3) e *= corrected_gshift_fluxboost_factor(corrfac_gshift, g, gamma) / g;
+    else if (fabs(g - 1) > 1e-3) e *= pow(g, gamma - 1);
+    emis_zone += e;
+  }
+  return emis_zone;
+}
+
+/* rebin_to_grid, Relreturn_Corona.cpp:208-222 */
+static void rrad_rebin_to_grid(double *value, const double *rmean, int nzones, const double *rgrid0,
+                               const double *value0, int n0) {
+  for (int ii = 0; ii < nzones; ii++) {
+    int ind = binary_search(rgrid0, n0 + 1, rmean[ii]);
+    if (rmean[ii] < rgrid0[0]) ind = 0;
+    else if (rmean[ii] > rgrid0[n0]) ind = n0 - 1;  /* the reference reads value0[n0] here; never reached */
+    value[ii] = value0[ind];
+  }
+}
+
+/* get_rrad_emis_corona + calc_rrad_emis_corona + rebin_emisprofile_on_radial_grid
+ * (Relreturn_Corona.cpp:125-160, 271-321; Rellp.cpp:120-175): the returning-radiation
+ * emissivity on the fine grid of sp from the direct emissivity sp->emis */
+static int get_rrad_emis_corona(const SysPar *sp, const Params *p, const RradCorr *corr, double *emis_ret) {
+  const int nr = sp->nr;
+  RradFractions rf;
+  if (get_rrad_fractions(p->a, sp->re[nr - 1], sp->re[0], &rf)) return 1;
+  const int n = rf.nrad;
+  double emis_in[RRAD_NR], cf_flux[RRAD_NR], cf_g[RRAD_NR], er[RRAD_NR], single[RRAD_NR];
+  if (inv_rebin_mean(sp->re, sp->emis, nr, rf.rad, emis_in, n)) return 1;
+  if (corr) {
+    rrad_rebin_to_grid(cf_flux, rf.rad, n, corr->rgrid, corr->corrfac_flux, corr->n_zones);
+    rrad_rebin_to_grid(cf_g, rf.rad, n, corr->rgrid, corr->corrfac_gshift, corr->n_zones);
+  }
+  for (int ii = 0; ii < n; ii++) {
+    const int ro = rf.irad[ii];
+    for (int jj = 0; jj < n; jj++) {
+      const double cg = corr ? cf_g[jj] : 1.0;
+      single[jj] = rrad_emis_zone(rf.tab, ro, rf.irad[jj], p->gamma, cg) * rf.tf_r[ii][jj] * emis_in[jj];
+    }
+    double sum = 0.0;
+    for (int jj = 0; jj < n; jj++) sum += single[jj];
+    er[ii] = sum;
+    if (corr) er[ii] *= cf_flux[ii];
+  }
+  /* onto the fine grid (descending); the table profile has del_emit = 0, so the radial
+   * interpolation factor is linear (get_ipol_factor_radius) */
+  if (n < 2) return 1;
+  int kk = binary_search(rf.rad, n, sp->re[nr - 1]);
+  for (int ii = nr - 1; ii >= 0; ii--) {
+    while (sp->re[ii] >= rf.rad[kk + 1]) {
+      kk++;
+      if (kk >= n - 1) {
+        if (sp->re[ii] - RELTABLE_MAX_R <= 1e-6) { kk = n - 2; break; }
+        return 1;
+      }
+    }
+    const double inter = get_ipol_factor_radius(rf.rad[kk], rf.rad[kk + 1], 0.0, sp->re[ii]);
+    emis_ret[ii] = interp_log_1d(inter, er[kk], er[kk + 1]);
+  }
+  return 0;
+}
+
+/* add_returnrad_emis, Rellp.cpp:483-509 */
+static int add_returnrad_emis(const Params *p, const RradCorr *corr, SysPar *sp) {
+  if (!g_rrad) g_rrad = load_rrad_table();
+  if (!g_rrad) return 1;
+  double *er = malloc(sizeof(double) * sp->nr);
+  int status = get_rrad_emis_corona(sp, p, corr, er);
+  for (int ii = 0; ii < sp->nr && !status; ii++) {
+    if (p->return_rad == 1) sp->emis[ii] += er[ii];
+    else if (p->return_rad == -1 || p->return_rad == 2) sp->emis[ii] = er[ii];
+    else status = 1;
+  }
+  free(er);
+  return status;
+}
+
+/* get_system_parameters, Relprofile.cpp:310-358 (without the cache); corr: the returning-radiation
+ * correction factors (Relxill.cpp:337-344) or NULL */
+static SysPar *get_system_parameters(const Params *p, const RradCorr *corr, int *status) {
   SysPar *sp = calloc(1, sizeof(SysPar));
   if (interpol_rel_table(g_rel, p->a, p->incl, p->rin, p->rout, sp)) { *status = 1; return sp; }
   sp->limb_law = p->limb;
@@ -912,7 +1148,8 @@ static SysPar *get_system_parameters(const Params *p, int *status) {
   } else {
     if (emis_lamp_post(g_lp, p, sp)) *status = 1;
   }
-  if (p->return_rad != 0) *status = 1; /* returning radiation is not part of this path */
+  /* calc_emis_profile, Rellp.cpp:556-558 */
+  if (!*status && abs(p->return_rad) > 1e-6 && add_returnrad_emis(p, corr, sp)) *status = 1;
   return sp;
 }
 
@@ -1350,7 +1587,7 @@ static const double *conv_grid(void) {
 /* relbase (Relbase.cpp:524-538) for one zone on the grid ener */
 static int relbase_single(const Params *p, const double *ener, int n, double *flux) {
   int status = 0;
-  SysPar *sp = get_system_parameters(p, &status);
+  SysPar *sp = get_system_parameters(p, NULL, &status);
   if (!status) {
     double rgrid[2];
     get_rzone_grid(p->rin, p->rout, 1, p->height, rgrid);
@@ -1360,12 +1597,57 @@ static int relbase_single(const Params *p, const double *ener, int n, double *fl
   return status;
 }
 
+/* get_xillver_fluxcorrection_factors with calc_angle_averaged_xill_spec, get_xillver_fluxcorr and
+ * get_xillver_gshift_fluxcorr (Xillspec.cpp:109-160, 344-361, 457-526) for one zone: flu holds the
+ * zone's spectra per inclination on the xillver grid xener.  The reference weights inclination i
+ * by norm_factor_semi_infinite_slab(incl_i * 180 / pi) / n_incl with incl_i the table value in
+ * degrees, i.e. 0.5 cos(incl_i) with incl_i read as radians; restated as it is. */
+static void xillver_fluxcorrection_factors(const XillTable *t, const double *flu, const double *xener, double ect_zone,
+                                           double gam, double *fac_flux, double *fac_gshift) {
+  const int n_x = t->n_ener, ni = t->n_incl;
+  double *avg = calloc(n_x, sizeof(double)), *ener_z = malloc(sizeof(double) * (n_x + 1)),
+         *flu_z = malloc(sizeof(double) * n_x);
+  for (int ii = 0; ii < ni; ii++) {
+    const double incl_deg = (double) t->incl[ii] * 180 / M_PI;
+    const double incl_factor = 0.5 * cos(incl_deg * M_PI / 180) / ni;
+    for (int jj = 0; jj < n_x; jj++) avg[jj] += incl_factor * flu[(size_t) ii * n_x + jj];
+  }
+  /* energy flux in 0.1-1000 keV of the reflection and of the normalised direct spectrum */
+  double ef_refl = 0.0;
+  for (int ii = 0; ii < n_x; ii++)
+    if (xener[ii] >= 0.1 && xener[ii + 1] <= 1000) ef_refl += avg[ii] * 0.5 * (xener[ii] + xener[ii + 1]);
+  const double *cg = coarse_grid();
+  double direct[N_ENER_COARSE];
+  spec_cutoffpl(direct, cg, N_ENER_COARSE, ect_zone, gam, 1.0);
+  const double nf = 1. / relxo_norm_wrt_xillver(direct, cg, N_ENER_COARSE);
+  double ef_direct = 0.0;
+  for (int ii = 0; ii < N_ENER_COARSE; ii++) {
+    direct[ii] *= nf;
+    if (cg[ii] >= 0.1 && cg[ii + 1] <= 1000) ef_direct += direct[ii] * 0.5 * (cg[ii] + cg[ii + 1]);
+  }
+  *fac_flux = ef_refl / ef_direct;
+  /* photon flux in 0.15-500 keV unshifted and shifted by g = 2/3 */
+  const double g0 = 2. / 3.;
+  for (int ii = 0; ii <= n_x; ii++) ener_z[ii] = xener[ii] / g0;
+  relxo_rebin_spectrum(ener_z, flu_z, n_x, xener, avg, n_x);
+  for (int ii = 0; ii < n_x; ii++) flu_z[ii] *= g0;
+  double pf = 0.0, pf_z = 0.0;
+  for (int ii = 0; ii < n_x; ii++)
+    if (xener[ii] >= 0.15 && xener[ii + 1] <= 500.0) pf += avg[ii];
+  for (int ii = 0; ii < n_x; ii++)
+    if (xener[ii] >= 0.15 && xener[ii + 1] <= 500.0) pf_z += flu_z[ii];
+  *fac_gshift = (pf / pf_z) / pow(1.5, gam);
+  free(avg);
+  free(ener_z);
+  free(flu_z);
+}
+
 /* relxill_kernel, Relxill.cpp:289-413, for relxill / relxilllp */
 static int relxill_kernel(const Params *p, double *out_conv /* [N_ENER_CONV] */) {
   const double *ener = conv_grid();
   int status = 0;
   int nz = p->num_zones;
-  SysPar *sp = get_system_parameters(p, &status);
+  SysPar *sp = get_system_parameters(p, NULL, &status);
   if (status) { free_syspar(sp); return status; }
   /* PrimarySourceParameters (PrimarySource.h:43-218) */
   double g_inf = 1.0;
@@ -1429,18 +1711,37 @@ static int relxill_kernel(const Params *p, double *out_conv /* [N_ENER_CONV] */)
   }
   XillTable *xt = g_xill;
   int n_incl = xt->n_incl, n_x = xt->n_ener;
-  /* relline profile on the conv grid (Relbase.cpp:461-512 with xill_tab != NULL) */
-  double *rel = malloc(sizeof(double) * nz * N_ENER_CONV);
-  double *dist = malloc(sizeof(double) * nz * n_incl);
-  if (!status) status = relline_profile(sp, p, ener, N_ENER_CONV, nz, rgrid, rel, n_incl, dist);
-  /* xillver spectra per zone, angle weighted (Relxill.cpp:357-386) */
   double *xener = malloc(sizeof(double) * (n_x + 1));
   for (int ii = 0; ii < n_x; ii++) xener[ii] = xt->elo[ii];
   xener[n_x] = xt->ehi[n_x - 1];
   double *flu = malloc(sizeof(double) * n_incl * n_x);
+  xill_begin_eval(xt);
+  /* returning-radiation correction factors from the zones' xillver spectra, then the emissivity
+   * again with them (Relxill.cpp:336-344; SPIN_MIN_RRAD_CALC_CORRFAC = 0, Relxill.h:32) */
+  SysPar *sp_rel = sp;
+  if (!status && p->return_rad != 0 && p->a > 0.0) {
+    RradCorr corr;
+    corr.n_zones = nz;
+    for (int ii = 0; ii <= nz; ii++) corr.rgrid[ii] = rgrid[ii];
+    for (int zz = 0; zz < nz && !status; zz++) {
+      double ect_zone = ect_source * shift[zz];
+      if (xillver_spectra_all_incl(xt, p->gam, p->afe, lxi[zz], ect_zone, p->incl * 180 / M_PI, dens[zz], flu)) {
+        status = 1;
+        break;
+      }
+      xillver_fluxcorrection_factors(xt, flu, xener, ect_zone, p->gam, &corr.corrfac_flux[zz],
+                                     &corr.corrfac_gshift[zz]);
+    }
+    if (!status) sp_rel = get_system_parameters(p, &corr, &status);
+  }
+  /* relline profile on the conv grid (Relbase.cpp:461-512 with xill_tab != NULL) */
+  double *rel = malloc(sizeof(double) * nz * N_ENER_CONV);
+  double *dist = malloc(sizeof(double) * nz * n_incl);
+  if (!status) status = relline_profile(sp_rel, p, ener, N_ENER_CONV, nz, rgrid, rel, n_incl, dist);
+  if (sp_rel != sp) free_syspar(sp_rel);
+  /* xillver spectra per zone, angle weighted (Relxill.cpp:357-386) */
   double *xz = malloc(sizeof(double) * nz * n_x);
   double src_norm = relxo_primary_norm_factor(ect_source, p->gam);
-  xill_begin_eval(xt);
   for (int zz = 0; zz < nz && !status; zz++) {
     double ect_zone = ect_source * shift[zz];
     if (xillver_spectra_all_incl(xt, p->gam, p->afe, lxi[zz], ect_zone, p->incl * 180 / M_PI, dens[zz], flu)) {
@@ -1604,7 +1905,7 @@ int relxo_relline_profile_zones(int model, const double *params, const double *e
   if (map_params(model, params, ION_GRAD_TYPE_CONST, 0.0, &p)) return 1;
   if (ensure_tables(0)) return 2;
   int status = 0;
-  SysPar *sp = get_system_parameters(&p, &status);
+  SysPar *sp = get_system_parameters(&p, NULL, &status);
   double rgrid[N_ZONES_MAX + 1];
   get_rzone_grid(p.rin, p.rout, p.num_zones, p.height, rgrid);
   *nzones_out = p.num_zones;

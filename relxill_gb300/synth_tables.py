@@ -23,6 +23,15 @@ works on synthetic tables with the same layout, shapes and value ranges:
   spectrum is a cut-off power law plus a 6.4 keV Gaussian whose equivalent
   width rises with logXi, scaled by 10^logXi, times lognormal noise (sigma
   0.05).
+* returning-radiation table: extension ``SPIN`` (column ``a``), then one
+  extension ``FRAC01``, ``FRAC02``, ... per spin with 50 rows (one per
+  incident radial bin, Relreturn_Table.cpp:180-330) and double columns
+  ``rlo``, ``rhi``, the 50-vectors ``frac_e``, ``tf_r``, ``gmin``, ``gmax``
+  (one element per emitting bin), the 50x20-vector ``frac_g`` and ``f_ret``,
+  ``f_bh``, ``f_inf``.  Radial bins are log-spaced from the table spin's ISCO
+  to 1000; the transfer fractions fall off with the distance between the
+  rings, the energy shifts follow the ratio of the radii and the g
+  distributions are smooth bumps, each with a seeded perturbation.
 
 Dimensions default to the ones the reference loaders hard-code
 (common.h:69-81: 25 spins x 30 mu0 x 100 radii x 40 g*, lamp post
@@ -46,6 +55,10 @@ from . import fits
 RELTABLE_FILENAME = "rel_table_v0.5a.fits"
 LPTABLE_FILENAME = "rel_lp_table_v0.5b.fits"
 XILLTABLE_FILENAME = "xillver-a-Ec5.fits"
+RRADTABLE_FILENAME = "table_returnRad_v20220301.fits"
+RRAD_NR = 50  # common.h:127-128
+RRAD_NG = 20
+RRAD_SPINS = (-0.998, -0.5, 0.0, 0.3, 0.5, 0.7, 0.8, 0.9, 0.95, 0.98, 0.99, 0.998)
 
 GFAC_H = 5e-3
 
@@ -286,19 +299,66 @@ def write_xillver_table(path: str, dims: XillDims | None = None, seed=1234) -> N
         st.close()
 
 
+# ----------------------------------------------------------------------------
+# returning-radiation table
+# ----------------------------------------------------------------------------
+
+def rrad_arrays(spin: float, nr: int = RRAD_NR, ng: int = RRAD_NG, seed: int = 1234):
+    """Transfer fractions of one spin: row i is the incident bin, element j the emitting bin."""
+    rng = np.random.default_rng(seed + 7 + int(round((spin + 1.0) * 1000)))
+    edges = np.exp(np.linspace(np.log(kerr_rms(spin)), np.log(1000.0), nr + 1))
+    rlo, rhi = edges[:-1], edges[1:]
+    rm = 0.5 * (rlo + rhi)
+    li, lj = np.log(rm)[:, None], np.log(rm)[None, :]
+    area = (rhi * rhi - rlo * rlo)[:, None]
+    f_ret = 0.35 * (rm[0] / rm) ** 0.8 * (0.6 + 0.4 * max(spin, 0.0))
+    kern = area * np.exp(-np.abs(li - lj) / 0.7) / rm[:, None] ** 1.5 * _smooth(rng, li, lj, amp=0.02)
+    tf_r = kern / kern.sum(axis=0, keepdims=True) * f_ret[None, :]
+    frac_e = 0.9 * tf_r * _smooth(rng, li, lj, amp=0.02)
+    gc = np.exp(0.15 * (lj - li)) * _smooth(rng, li, lj, amp=0.01)
+    wid = 0.3 + 0.05 * np.sin(li + 2 * lj) ** 2
+    gmin, gmax = gc * (1.0 - wid), gc * (1.0 + wid)
+    x = (np.arange(ng) + 0.5) / ng
+    bump = np.exp(-0.5 * ((x[None, None, :] - 0.45 - 0.1 * np.tanh(lj - li)[:, :, None]) / 0.22) ** 2)
+    bump = bump * _smooth(rng, li[:, :, None], lj[:, :, None], x[None, None, :] * 3, amp=0.05)
+    frac_g = bump / bump.sum(axis=2, keepdims=True)
+    return dict(rlo=rlo, rhi=rhi, frac_e=frac_e, tf_r=tf_r, gmin=gmin, gmax=gmax, frac_g=frac_g, f_ret=f_ret,
+                f_bh=0.3 * (rm[0] / rm), f_inf=1.0 - f_ret - 0.3 * (rm[0] / rm))
+
+
+def write_rrad_table(path: str, spins: Sequence[float] = RRAD_SPINS, seed: int = 1234) -> None:
+    with open(path, "wb") as f:
+        f.write(fits.primary_header())
+        f.write(fits.bintable("SPIN", [fits.Column("a", "D", 1, np.asarray(spins, dtype=np.float64)[:, None])],
+                              len(spins)))
+        for k, a in enumerate(spins):
+            t = rrad_arrays(float(a), seed=seed)
+            nr, ng = t["frac_g"].shape[1], t["frac_g"].shape[2]
+            cols = [fits.Column("rlo", "D", 1, t["rlo"][:, None]), fits.Column("rhi", "D", 1, t["rhi"][:, None])]
+            for name in ("frac_e", "tf_r", "gmin", "gmax"):
+                cols.append(fits.Column(name, "D", nr, t[name]))
+            cols.append(fits.Column("frac_g", "D", nr * ng, t["frac_g"].reshape(nr, nr * ng)))
+            for name in ("f_ret", "f_bh", "f_inf"):
+                cols.append(fits.Column(name, "D", 1, t[name][:, None]))
+            f.write(fits.bintable(f"FRAC{k + 1:02d}", cols, nr))
+
+
 def write_all(outdir: str, xill: str = "full", seed: int = 1234) -> str:
     os.makedirs(outdir, exist_ok=True)
     write_relline_table(os.path.join(outdir, RELTABLE_FILENAME), seed=seed)
     write_lp_table(os.path.join(outdir, LPTABLE_FILENAME), seed=seed)
     write_xillver_table(os.path.join(outdir, XILLTABLE_FILENAME), xill_dims(xill), seed=seed)
+    write_rrad_table(os.path.join(outdir, RRADTABLE_FILENAME), seed=seed)
     return outdir
 
 
 def ensure_tables(outdir: str, xill: str = "full", seed: int = 1234) -> str:
-    """Write the three tables into ``outdir`` unless a complete set is there."""
+    """Write the four tables into ``outdir`` unless a complete set is there."""
     stamp = os.path.join(outdir, f".complete_{xill}_{seed}")
     if not os.path.exists(stamp):
         write_all(outdir, xill=xill, seed=seed)
+    elif not os.path.exists(os.path.join(outdir, RRADTABLE_FILENAME)):
+        write_rrad_table(os.path.join(outdir, RRADTABLE_FILENAME), seed=seed)
         with open(stamp, "w") as fh:
             fh.write("ok\n")
     return outdir

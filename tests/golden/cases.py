@@ -38,6 +38,17 @@ CASES = [
     ("xillver_c", "xillver", [2.5, 0.7, 1000, 4.7, 0, 5, 0], GRID_XLOW, 0, 0.0),
     # parameters on grid values or clamped (zero-weight corners), z = 1
     ("xillver_d", "xillver", [1.0, 10, 5, 0, 1.0, 87, 1], GRID_XLOW, 0, 0.0),
+    # returning radiation ($switch_returnrad = 1, the reference's default for the lamp-post models)
+    ("relxilllp_rr_a", "relxilllp", [10, 0, 0.9, 45, -1, 400, 0, 2.0, 3.1, 1, 300, 1, 1, 0], GRID_WIDE, 0, 0.0),
+    ("relxilllp_rr_b", "relxilllp", [3, 0.3, 0.998, 70, -1, 400, 0.2, 2.6, 4.0, 5, 50, 2, 1, 1], GRID_WIDE, 0, 0.0),
+    # negative spin: no xillver correction factors (Relxill.cpp:338-341)
+    ("relxilllp_rr_neg", "relxilllp", [50, 0, -0.5, 10, -3, 100, 0, 1.5, 0.5, 0.7, 800, -1, 1, 0], GRID_WIDE, 0, 0.0),
+    # only the returning part of the emissivity ($switch_returnrad = -1)
+    ("relxilllp_rr_only", "relxilllp", [6, 0, 0.95, 30, -1, 400, 0, 2.0, 1.0, 1, 300, 1, -1, 0], GRID_WIDE, 0, 0.0),
+    ("relxilllp_rr_alpha", "relxilllp", [5, 0, 0.5, 30, -1, 400, 0, 2.2, 2.0, 1, 100, 1, 1, 0], GRID_WIDE, 2, 0.0),
+    ("relxilllp_rr_pl", "relxilllp", [10, 0, 0.9, 45, -1, 400, 0, 2.0, 3.1, 1, 300, 1, 1, 0], GRID_WIDE, 1, 0.5),
+    ("rellinelp_rr", "relline_lp", [6.4, 6, 0.998, 30, -1, 400, 0, 0, 2.0, 1], GRID_LINE, 0, 0.0),
+    ("relconvlp_rr", "relconv_lp", [6, 0.0, 0.7, 30, -1, 400, 0, 2.0, 1], GRID_CONV, 0, 0.0),
 ]
 
 
