@@ -9,8 +9,9 @@
  * instead.  Tables are found through RELXILL_TABLE_PATH as in the reference
  * (src/relutility.c:320-328).  The same environment switches are honoured:
  * RELXILL_NUM_RZONES, RELLINE_PHYSICAL_NORM, RELXILL_RENORMALIZE,
- * RELXILL_CONSTANT_DENSITY.  Returning radiation is not part of this path: a
- * parameter array with $switch_returnrad != 0 fails with status 3.
+ * RELXILL_CONSTANT_DENSITY.  Returning radiation ($switch_returnrad of the
+ * lamp-post models) reads table_returnRad_v20220301.fits from the same path;
+ * a set that switches it on without that table fails with status 2.
  *
  * Errors: the void entry points fill `flux` with zeros on failure and record
  * the status (relx_last_status); the batched calls return it.

@@ -22,16 +22,21 @@
 namespace relx {
 
 __device__ __forceinline__ bool cache_key(const RelxSetIn &in, const RelxSetState &s, double *key) {
-  if (s.status != RELX_OK || s.model == RELX_RELLINE || s.nz > kCacheZones) return false;
+  // sets whose emissivity holds returning radiation corrected by their xillver spectra depend on
+  // the xillver parameters too and are not cached (the reference does not cache them either,
+  // Relcache.cpp:93-97)
+  if (s.status != RELX_OK || s.model == RELX_RELLINE || s.nz > kCacheZones || s.rr_corr) return false;
 #pragma unroll
   for (int q = 0; q < kCacheKeyLen; q++) key[q] = 0.0;
   key[0] = (double) s.pmodel;
   key[1] = (double) s.nz;
-  // relconv: Index1..limb (8); relconv_lp: h..gamma (8); relxill: Index1..z (8); relxilllp: h..gamma
-  // (8) and the returning-radiation switch (lmodel_relxill_public.dat:13-21, 35-44, 46-59, 61-75)
+  // relconv: Index1..limb (8); relconv_lp: h..gamma (8) and the returning-radiation switch;
+  // relxill: Index1..z (8); relxilllp: h..gamma (8) and the returning-radiation switch
+  // (lmodel_relxill_public.dat:13-21, 35-44, 46-59, 61-75)
 #pragma unroll
   for (int q = 0; q < 8; q++) key[2 + q] = in.p[q];
-  if (s.model == RELX_RELXILLLP) key[10] = in.p[12];
+  if (s.pmodel == RELX_RELXILLLP) key[10] = in.p[12];
+  if (s.pmodel == RELX_RELCONVLP) key[10] = in.p[8];
   return true;
 }
 

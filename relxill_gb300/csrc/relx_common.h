@@ -30,7 +30,7 @@ enum RelxStatus {
   RELX_OK = 0,
   RELX_ERR_PARAM = 1,        // parameter out of the allowed range (check_parameter_bounds)
   RELX_ERR_TABLE = 2,        // table missing or inconsistent
-  RELX_ERR_UNSUPPORTED = 3,  // returning radiation, unsupported model option
+  RELX_ERR_UNSUPPORTED = 3,  // unsupported model option
   RELX_ERR_GRID = 4,         // radial interpolation outside the table (Relprofile.cpp:255-278)
   RELX_ERR_INPUT = 5,        // relconv input spectrum with sum <= 0 (LocalModel.cpp:84-86)
   RELX_ERR_CUDA = 6,         // CUDA runtime error
@@ -65,6 +65,11 @@ enum RelxStatus {
 #define RELX_ZDENSE 16            // zones handled with the de-duplicated xillver corner list
 #define RELX_MAX_UCORNER 256      // 16 corners x RELX_ZDENSE zones
 #define RELX_NPARAM_MAX 16
+
+// returning-radiation table (common.h:127-129)
+#define RELX_RR_NR 50
+#define RELX_RR_NG 20
+#define RELX_RR_MAXSPIN 99
 
 #define RELX_EMIS_BKN 1
 #define RELX_EMIS_LP 2
@@ -106,6 +111,17 @@ struct RelxTables {
   const int4 *rb_pack;       // per conv bin: imin, imax, fmin and fmax as float bits
   const double *x_e;         // xillver edges [x_nener+1] (double of the float table values)
   const float2 *x_ew;        // per xillver edge: the edge, (float) (x_e[k+1] - x_e[k]) (0 at the last edge)
+  // per xillver corner (table row of incl 0 / x_nincl): the inclination-averaged energy flux in
+  // 0.1-1000 keV, photon flux in 0.15-500 keV, and photon flux of the spectrum shifted by g = 2/3
+  // (get_xillver_fluxcorrection_factors, Xillspec.cpp:109-160, 344-361, 457-526)
+  const double *x_fcorr;     // [corners][3]
+  int coarse_b2_skip[2];     // coarse bins in the normalisation band but outside the 0.1-1000 keV flux band (-1: none)
+  // returning-radiation table (Relreturn_Table.cpp:180-330); rr_nspin = 0 when it is not loaded
+  int rr_nspin;
+  const double *rr_spin;     // [nspin]
+  const double *rr_rlo, *rr_rhi;  // [nspin][RELX_RR_NR]
+  const double *rr_tfr;      // [nspin][RELX_RR_NR][RELX_RR_NR], row = incident bin, column = emitting bin
+  const float4 *rr_g;        // [nspin][NR][NR][NG]: frac_g, g, log2 g, 1 if |g - 1| > 1e-3 else 0
 };
 
 // per-set inputs
@@ -123,6 +139,7 @@ struct RelxSetIn {
 struct RelxSetState {
   int status, model, emis_type, limb, nz, ion_grad_type, boost_switch;
   int pmodel;       // the caller's model id (model holds its kind, relx_kind)
+  int rr_corr;      // returning radiation with xillver correction factors (line profile not cacheable)
   int cached;       // line profile, tile sums and angle histograms come from the profile cache
   int g_n;          // bins of the line-profile grid (user grid for relline, conv grid otherwise)
   int win_lo, win_hi;  // line-profile bins touched by any radius

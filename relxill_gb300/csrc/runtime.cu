@@ -103,14 +103,15 @@ struct Tables {
   RelxTables d{};
   DevBuf rel_a, rel_mu0, rel_r, rel_gmin, rel_gmax, rel_tc;
   DevBuf lp_a, lp_h, lp_rad, lp_intens, lp_del, lp_delinc;
-  DevBuf x_vals, x_spec, x_e, x_ew;
+  DevBuf x_vals, x_spec, x_e, x_ew, x_fcorr;
+  DevBuf rr_spin, rr_rlo, rr_rhi, rr_tfr, rr_g;
   DevBuf conv_e, conv_eff, conv_inv_emid, conv_cf, conv_cw, coarse_e, coarse_t;
   DevBuf rb_imin, rb_imax, rb_fmin, rb_fmax, rb_pack;
   size_t bytes_total = 0;
   bool loaded = false;
   void release() {
     for (DevBuf *b : {&rel_a, &rel_mu0, &rel_r, &rel_gmin, &rel_gmax, &rel_tc, &lp_a, &lp_h, &lp_rad, &lp_intens,
-                      &lp_del, &lp_delinc, &x_vals, &x_spec, &x_e, &x_ew, &conv_e, &conv_eff, &conv_inv_emid, &conv_cf,
+                      &lp_del, &lp_delinc, &x_vals, &x_spec, &x_e, &x_ew, &x_fcorr, &rr_spin, &rr_rlo, &rr_rhi, &rr_tfr, &rr_g, &conv_e, &conv_eff, &conv_inv_emid, &conv_cf,
                       &conv_cw, &coarse_e, &coarse_t, &rb_imin, &rb_imax, &rb_fmin, &rb_fmax, &rb_pack})
       b->release();
     loaded = false;
@@ -215,6 +216,8 @@ static int load_lp(const std::string &dir, Tables &T) {
   return 0;
 }
 
+constexpr double kPiHost = 3.14159265358979323846;
+
 static const char *kXillNames[] = {"Gamma", "A_Fe", "logXi", "Ecut", "kTe", "Dens", "kTbb", "A_CO", "Frac", "Incl"};
 static const int kXillIndex[] = {0, 1, 2, 3, 3, 4, 5, 1, 6, 7};  // common.h:141-150, xilltable.c:24-27
 
@@ -260,11 +263,42 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
   const FitsColumn &sc = hs->cols[1];
   if (sc.code != 'E' || sc.repeat != ne) { g_errmsg = "xillver table: SPECTRA column"; return RELX_ERR_TABLE; }
   const int pad = (ne + 3) / 4 * 4;
+  // Flux integrals of every row for the returning-radiation correction factors
+  // (get_xillver_fluxcorrection_factors, Xillspec.cpp:109-160, 344-361, 457-526): the energy flux
+  // in 0.1-1000 keV, the photon flux in 0.15-500 keV, and that photon flux after the rebin of the
+  // spectrum shifted by g = 2/3 (a fixed linear map of the row: coefficients pfz_coef).
+  std::vector<double> pfz_coef(ne, 0.0);
+  {
+    const double g0 = 2. / 3.;
+    std::vector<double> ez(ne + 1);
+    for (int i = 0; i <= ne; i++) ez[i] = xe_host[i] / g0;
+    int imin = 0, imax = 0;  // the walk of _rebin_spectrum (relutility.c:549-601), new grid ez, old grid xe
+    for (int ii = 0; ii < ne; ii++) {
+      if (!((xe_host[0] <= ez[ii + 1]) && (xe_host[ne] >= ez[ii]))) continue;
+      while (imin <= ne && xe_host[imin] <= ez[ii]) imin++;
+      if (imin > 0) imin--;
+      while (imax < ne && xe_host[imax] <= ez[ii + 1]) imax++;
+      if (imax > 0) imax--;
+      if (!(xe_host[ii] >= 0.15 && xe_host[ii + 1] <= 500.0)) continue;  // band of the photon flux
+      double elo = ez[ii], ehi = ez[ii + 1];
+      if (elo < xe_host[imin]) elo = xe_host[imin];
+      if (ehi > xe_host[imax + 1]) ehi = xe_host[imax + 1];
+      if (imax == imin) {
+        pfz_coef[imin] += g0 * (ehi - elo) / (xe_host[imin + 1] - xe_host[imin]);
+      } else {
+        pfz_coef[imin] += g0 * (xe_host[imin + 1] - elo) / (xe_host[imin + 1] - xe_host[imin]);
+        pfz_coef[imax] += g0 * (ehi - xe_host[imax]) / (xe_host[imax + 1] - xe_host[imax]);
+        for (int q = imin + 1; q <= imax - 1; q++) pfz_coef[q] += g0;
+      }
+    }
+  }
+  std::vector<double> rowflux((size_t) 0);
   // strides of the row index (incl fastest, xilltable.c:325-337)
   int64_t stride_lxi = 1;
   for (int q = npar - 1; q > q_lxi; q--) stride_lxi *= nvals[q];
   int st = T.x_spec.reserve(sizeof(float) * (size_t) rows * pad);
   if (st) return st;
+  rowflux.assign((size_t) rows * 3, 0.0);
   // read, renormalise by 10^-logXi of the row's grid point (renorm_xill_spec, xilltable.c:478-485), upload in chunks
   const int64_t chunk = 4096;
   std::vector<unsigned char> raw((size_t) (chunk * hs->width));
@@ -284,22 +318,43 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
           const double div = std::pow(10, lxi);
           const unsigned char *p = raw.data() + r * hs->width + sc.offset;
           float *o = buf.data() + (size_t) r * pad;
+          double ef = 0.0, pf = 0.0, pfz = 0.0;
           for (int e = 0; e < ne; e++) {
             float v = be_f32(p + 4 * e);
             v /= div;  // float / double, stored as float (xilltable.c:480)
             o[e] = v;
+            if (xe_host[e] >= 0.1 && xe_host[e + 1] <= 1000) ef += (double) v * 0.5 * (xe_host[e] + xe_host[e + 1]);
+            if (xe_host[e] >= 0.15 && xe_host[e + 1] <= 500.0) pf += (double) v;
+            pfz += pfz_coef[e] * (double) v;
           }
           for (int e = ne; e < pad; e++) o[e] = 0.0f;
+          rowflux[(size_t) row * 3 + 0] = ef;
+          rowflux[(size_t) row * 3 + 1] = pf;
+          rowflux[(size_t) row * 3 + 2] = pfz;
         }
       });
     }
     for (auto &x : th) x.join();
     RELX_CUDA(cudaMemcpy(dst + (size_t) r0 * pad, buf.data(), sizeof(float) * (size_t) nr * pad, cudaMemcpyHostToDevice));
   }
+  // inclination average per corner (calc_angle_averaged_xill_spec, Xillspec.cpp:109-127): the
+  // reference weights inclination i by norm_factor_semi_infinite_slab(incl_i * 180 / pi) / n_incl
+  // with incl_i the table value in degrees; restated as it is
+  const int ni = nvals[npar - 1];
+  std::vector<double> fcorr((size_t) (rows / ni) * 3, 0.0);
+  for (int64_t c = 0; c < rows / ni; c++) {
+    for (int i = 0; i < ni; i++) {
+      const double incl_deg = (double) vals[(size_t) (npar - 1) * maxv + i] * 180 / kPiHost;
+      const double f = 0.5 * std::cos(incl_deg * kPiHost / 180) / ni;
+      for (int q = 0; q < 3; q++) fcorr[(size_t) c * 3 + q] += f * rowflux[(size_t) (c * ni + i) * 3 + q];
+    }
+  }
   std::vector<double> xe = xe_host;
   std::vector<float2> xew((size_t) ne + 1);
   for (int i = 0; i <= ne; i++) xew[i] = make_float2((float) xe[i], i < ne ? (float) (xe[i + 1] - xe[i]) : 0.0f);
-  if ((st = upload(T.x_vals, vals)) || (st = upload(T.x_e, xe)) || (st = upload(T.x_ew, xew))) return st;
+  if ((st = upload(T.x_vals, vals)) || (st = upload(T.x_e, xe)) || (st = upload(T.x_ew, xew)) ||
+      (st = upload(T.x_fcorr, fcorr)))
+    return st;
   T.d.x_npar = npar; T.d.x_nener = ne; T.d.x_nener_pad = pad; T.d.x_nincl = nvals[npar - 1];
   for (int q = 0; q < RELX_MAX_XPAR; q++) { T.d.x_nvals[q] = q < npar ? nvals[q] : 0; T.d.x_pindex[q] = q < npar ? pidx[q] : -1; }
   T.d.x_has_dens = has_dens;
@@ -309,7 +364,70 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
   T.d.x_rows = rows;
   T.d.x_e = T.x_e.as<double>();
   T.d.x_ew = T.x_ew.as<float2>();
+  T.d.x_fcorr = T.x_fcorr.as<double>();
   T.bytes_total += (size_t) rows * pad * 4;
+  return 0;
+}
+
+// Returning-radiation table (fits_read_returnRadTable, Relreturn_Table.cpp:180-330): extension SPIN
+// (column a), then FRAC01, FRAC02, ... with RELX_RR_NR rows.  Optional: without the file the
+// models run unless a set switches returning radiation on, which then fails with RELX_ERR_TABLE.
+// Per (spin, incident bin, emitting bin, g sample) the device keeps frac_g, the energy shift g of
+// the sample (get_gfac_grid, Relreturn_Datastruct.cpp:51-59), log2 g, and 1 where the reference
+// boosts the sample by g^(gamma-1) (|g - 1| > 1e-3, Relreturn_Corona.cpp:114-116), else 0.
+static int load_rrad(const std::string &dir, Tables &T) {
+  T.d.rr_nspin = 0;
+  FitsFile f;
+  std::string err;
+  if (!f.open(dir + "/table_returnRad_v20220301.fits", &err)) return 0;
+  const FitsHdu *hs = f.find("SPIN");
+  const int ca = hs ? hs->col("a") : -1;
+  if (!hs || ca < 0 || hs->nrows < 1 || hs->nrows > RELX_RR_MAXSPIN) {
+    g_errmsg = "return radiation table: SPIN extension";
+    return RELX_ERR_TABLE;
+  }
+  const int nspin = (int) hs->nrows, NR = RELX_RR_NR, NG = RELX_RR_NG;
+  std::vector<double> spin(nspin), rlo((size_t) nspin * NR), rhi((size_t) nspin * NR),
+      tfr((size_t) nspin * NR * NR);
+  std::vector<float4> g4((size_t) nspin * NR * NR * NG);
+  if (!f.read_f64(*hs, ca, 0, nspin, spin.data())) { g_errmsg = "return radiation table: spins"; return RELX_ERR_TABLE; }
+  std::vector<double> gmin((size_t) NR * NR), gmax((size_t) NR * NR), fg((size_t) NR * NR * NG);
+  for (int k = 0; k < nspin; k++) {
+    char ext[16];
+    std::snprintf(ext, sizeof ext, "FRAC%02d", k + 1);
+    const FitsHdu *h = f.find(ext);
+    if (!h || h->nrows != NR) { g_errmsg = std::string("return radiation table: extension ") + ext; return RELX_ERR_TABLE; }
+    const int c_rlo = h->col("rlo"), c_rhi = h->col("rhi"), c_tfr = h->col("tf_r"), c_gmin = h->col("gmin"),
+              c_gmax = h->col("gmax"), c_fg = h->col("frac_g");
+    if (c_rlo < 0 || c_rhi < 0 || c_tfr < 0 || c_gmin < 0 || c_gmax < 0 || c_fg < 0 || h->cols[c_tfr].repeat != NR ||
+        h->cols[c_gmin].repeat != NR || h->cols[c_gmax].repeat != NR || h->cols[c_fg].repeat != (int64_t) NR * NG ||
+        !f.read_f64(*h, c_rlo, 0, NR, &rlo[(size_t) k * NR]) || !f.read_f64(*h, c_rhi, 0, NR, &rhi[(size_t) k * NR]) ||
+        !f.read_f64(*h, c_tfr, 0, NR, &tfr[(size_t) k * NR * NR]) || !f.read_f64(*h, c_gmin, 0, NR, gmin.data()) ||
+        !f.read_f64(*h, c_gmax, 0, NR, gmax.data()) || !f.read_f64(*h, c_fg, 0, NR, fg.data())) {
+      g_errmsg = std::string("return radiation table: columns of ") + ext;
+      return RELX_ERR_TABLE;
+    }
+    for (int i = 0; i < NR * NR; i++) {
+      for (int jj = 0; jj < NG; jj++) {
+        const double g = (jj + 0.5) / NG * (gmax[i] - gmin[i]) + gmin[i];
+        if (!(g > 0.0)) { g_errmsg = "return radiation table: energy shift <= 0"; return RELX_ERR_TABLE; }
+        const float boosted = std::fabs(g - 1) > 1e-3 ? 1.0f : 0.0f;
+        g4[((size_t) k * NR * NR + i) * NG + jj] =
+            make_float4((float) fg[(size_t) i * NG + jj], (float) g, (float) std::log2(g), boosted);
+      }
+    }
+  }
+  int st;
+  if ((st = upload(T.rr_spin, spin)) || (st = upload(T.rr_rlo, rlo)) || (st = upload(T.rr_rhi, rhi)) ||
+      (st = upload(T.rr_tfr, tfr)) || (st = upload(T.rr_g, g4)))
+    return st;
+  T.d.rr_spin = T.rr_spin.as<double>();
+  T.d.rr_rlo = T.rr_rlo.as<double>();
+  T.d.rr_rhi = T.rr_rhi.as<double>();
+  T.d.rr_tfr = T.rr_tfr.as<double>();
+  T.d.rr_g = T.rr_g.as<float4>();
+  T.d.rr_nspin = nspin;
+  T.bytes_total += g4.size() * sizeof(float4) + tfr.size() * sizeof(double);
   return 0;
 }
 
@@ -349,7 +467,9 @@ static int load_tables(const std::string &dir, Tables &T) {
   T.bytes_total = 0;
   std::vector<double> xe;
   int st;
-  if ((st = load_relline(dir, T)) || (st = load_lp(dir, T)) || (st = load_xillver(dir, T, xe))) return st;
+  if ((st = load_relline(dir, T)) || (st = load_lp(dir, T)) || (st = load_xillver(dir, T, xe)) ||
+      (st = load_rrad(dir, T)))
+    return st;
   // conv grid (get_relxill_conv_energy_grid, Xillspec.cpp:44-54) and derived arrays
   std::vector<double> ce;
   log_grid(ce, RELX_NCONV + 1, RELX_EMIN_CONV, RELX_EMAX_CONV);
@@ -379,6 +499,14 @@ static int load_tables(const std::string &dir, Tables &T) {
   std::vector<double> co;
   log_grid(co, RELX_NCOARSE + 1, RELX_EMIN_NORM, RELX_EMAX_NORM);
   std::vector<float4> ct(RELX_NCOARSE);
+  // bins of the normalisation band (Xillspec.cpp:185-190) outside the band of get_energy_flux_band
+  // (e_lo >= 0.1 and e_hi <= 1000, Xillspec.cpp:132-144); only the end bins can differ
+  T.d.coarse_b2_skip[0] = T.d.coarse_b2_skip[1] = -1;
+  for (int b : {0, RELX_NCOARSE - 1}) {
+    const bool band1 = co[b] >= RELX_EMIN_NORM && co[b] <= RELX_EMAX_NORM;
+    const bool band2 = co[b] >= 0.1 && co[b + 1] <= 1000;
+    if (band1 && !band2) T.d.coarse_b2_skip[b == 0 ? 0 : 1] = b;
+  }
   for (int b = 0; b < RELX_NCOARSE; b++) {
     const double em = 0.5 * (co[b] + co[b + 1]);
     const bool in_band = co[b] >= RELX_EMIN_NORM && co[b] <= RELX_EMAX_NORM;

@@ -18,6 +18,19 @@ namespace relx {
 
 constexpr int kSetupThreads = 256;
 
+// returning radiation of one set on the radial bins of the return table (Relreturn_Corona.cpp)
+struct RradSmem {
+  int n, klo, spin;                  // trimmed bins, first table bin, table spin index
+  double rad[RELX_RR_NR];            // bin centres (ascending)
+  double inv_drad[RELX_RR_NR];       // 1 / (rad[k + 1] - rad[k])
+  double area_in, area_out;          // ring-area corrections of the first and last bin
+  float emis_in[RELX_RR_NR];         // direct emissivity at the bin centres
+  float er[RELX_RR_NR], dl[RELX_RR_NR];  // returning emissivity per bin, log2(er[k + 1] / er[k])
+  float cf_flux[RELX_RR_NR];         // xillver correction factors on the table bins
+  double cf_g[RELX_RR_NR];
+  double zcf_flux[RELX_NZMAX], zcf_g[RELX_NZMAX];  // per ionisation zone
+};
+
 struct SetupSmem {
   RelxSetState s;
   double re_tab[RELX_MAX_NRTAB], gmin_t[RELX_MAX_NRTAB], gmax_t[RELX_MAX_NRTAB];
@@ -53,6 +66,8 @@ struct SetupSmem {
   short cuniq[RELX_NZMAX * 16];
   float cw[RELX_NZMAX * 16];            // weight of every (zone, corner) entry
   unsigned char clive[RELX_NZMAX * 16]; // row has a non-zero weight in some zone
+  RradSmem rr;
+  float emis_lp[RELX_NFRAD];            // direct lamp-post emissivity (returning radiation only)
 };
 
 // ---------------------------------------------------------------------------
@@ -65,6 +80,7 @@ __device__ void map_params(int model, const RelxSetIn &in, SetupSmem &m) {
   s.pmodel = model;
   s.status = RELX_OK;
   s.cached = 0;
+  s.rr_corr = 0;
   s.limb = 0;
   s.height = 0;
   s.beta = 0;
@@ -150,7 +166,12 @@ __device__ void map_params(int model, const RelxSetIn &in, SetupSmem &m) {
     if (s.height < 0) s.height = -1.0 * s.height * rp;
     if ((1.1 * rp - s.height) > 1e-4) s.height = rp * 1.1;
   }
-  if (m.return_rad != 0) { s.status = RELX_ERR_UNSUPPORTED; return; }
+  // $switch_returnrad: 1 adds the returning radiation, -1 and 2 keep only it (add_returnrad_emis,
+  // Rellp.cpp:483-509); the models without the switch pass 0
+  if (m.return_rad != 0 && m.return_rad != 1 && m.return_rad != -1 && m.return_rad != 2) {
+    s.status = RELX_ERR_PARAM;
+    return;
+  }
   // get_num_zones, relutility.c:506-544 (RELXILL_NUM_RZONES arrives in nzones_env)
   int envn = in.nzones_env;
   if (s.ion_grad_type != 0) {
@@ -220,6 +241,118 @@ __device__ double rebin_mean_at(const double *x0, const double *y0, int n0, doub
   return lerp1(f, y0[ii + 1], y0[ii]);
 }
 
+
+// ---------------------------------------------------------------------------
+// returning radiation (Relreturn_Table.cpp:393-611, Relreturn_Corona.cpp:37-321)
+// ---------------------------------------------------------------------------
+
+// get_rrad_fractions for the set (thread 0): spin index (the first table spin >= a), the table
+// bins covering [rin, rout] with the first and last reset to them, their centres and the ring-area
+// corrections of the end bins.  rin, rout: the ends of the fine radial grid (determine_rlo_rhi).
+__device__ int rrad_geometry(const RelxTables &tab, RradSmem &q, double a, double rms, double rin, double rout) {
+  const int NR = RELX_RR_NR;
+  int k = bsearch_asc<double>(tab.rr_spin, tab.rr_nspin, a);
+  if (tab.rr_spin[k] < a) k++;
+  if (k >= tab.rr_nspin || k < 0) return RELX_ERR_TABLE;
+  const double *rlo = tab.rr_rlo + (size_t) k * NR, *rhi = tab.rr_rhi + (size_t) k * NR;
+  int klo = bsearch_asc<double>(rlo, NR, rin);
+  int khi = bsearch_asc<double>(rhi, NR, rout);
+  if (fabs(rout - rhi[NR - 1]) < 1e-6) khi = NR - 1;
+  else khi++;
+  if (fabs(rin - rlo[0]) < 1e-6) klo = 0;
+  const int n = (khi + 1) - klo;
+  // the reference asserts these (Relreturn_Table.cpp:455-456, 480; Rellp.cpp:150-151)
+  if (n < 2 || n > NR || !(rin >= rlo[klo] - 1e-4)) return RELX_ERR_GRID;
+  q.n = n;
+  q.klo = klo;
+  q.spin = k;
+  for (int i = 0; i < n; i++) {
+    const double lo = (i == 0) ? rin : rlo[klo + i], hi = (i == n - 1) ? rout : rhi[klo + i];
+    q.rad[i] = 0.5 * (lo + hi);
+  }
+  for (int i = 0; i + 1 < n; i++) q.inv_drad[i] = 1.0 / (q.rad[i + 1] - q.rad[i]);
+  // get_ring_area_correction_factor (Relreturn_Table.cpp:518-538)
+  for (int e = 0; e < 2; e++) {
+    const int i = e ? n - 1 : 0;
+    double rlo_t = rlo[klo + i];
+    if (klo + i == 0 && rlo_t > rms) rlo_t = rms;
+    const double rhi_t = rhi[klo + i];
+    const double lo = (i == 0) ? rin : rlo[klo + i], hi = (i == n - 1) ? rout : rhi[klo + i];
+    const double c = (0.5 * (lo + hi) * (hi - lo)) / (0.5 * (rlo_t + rhi_t) * (rhi_t - rlo_t));
+    if (!(c - 1 < 1e-6)) return RELX_ERR_GRID;
+    if (e) q.area_out = c; else q.area_in = c;
+  }
+  return RELX_OK;
+}
+
+// corrected_gshift_fluxboost_factor / g (Relreturn_Corona.cpp:37-86), FP32
+__device__ __forceinline__ float rrad_corrected_boost_over_g(float cg, float g, float lg, float gamma) {
+  const float g0 = 2.0f / 3.0f;
+  float gc;
+  if (cg < 1.0f) {
+    const float a = (cg / g0 - 1.0f) / (g0 - 1.0f), b = 1.0f - a;
+    gc = (g >= 1.0f) ? 1.0f / g * (1.0f / g * a + b) : g * (g * a + b);
+  } else {
+    const float al = (cg - 1.0f) / (g0 - 1.0f), bl = 1.0f - al;
+    gc = (g >= 1.0f) ? (1.0f / g * al + bl) : (g * al + bl);
+  }
+  float fb = exp2f(gamma * lg) * gc;
+  if (g < 1.0f && fb > 1.0f) fb = 1.0f;
+  if (fb < 0.0f) fb = 0.0f;
+  return fb / g;
+}
+
+// calc_rrad_emis_corona (Relreturn_Corona.cpp:125-160) on the table bins: er[i] = sum_j
+// h(i, j) tf_r[i][j] emis_in[j] (times the flux correction of bin i), h(i, j) = sum over the g
+// samples of frac_g times g^(gamma-1), or the corrected boost / g where the emitting bin's
+// g-shift correction differs from 1 by more than 1e-3.  One warp per incident bin, lanes over
+// the emitting bins, FP32, a fixed reduction order.
+__device__ void rrad_pass(const RelxTables &tab, RradSmem &q, float gamma, bool corr) {
+  const int NR = RELX_RR_NR, NG = RELX_RR_NG;
+  const int n = q.n, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const double *tfr = tab.rr_tfr + (size_t) q.spin * NR * NR;
+  const float4 *gt = tab.rr_g + (size_t) q.spin * NR * NR * NG;
+  for (int i = warp; i < n; i += kSetupThreads / 32) {
+    const int ro = q.klo + i;
+    float acc = 0.0f;
+    for (int j = lane; j < n; j += 32) {
+      const int re = q.klo + j;
+      double t = tfr[(size_t) ro * NR + re];
+      if (j == 0 && i < n - 1) t *= q.area_in;   // get_interpolated_tfr (Relreturn_Table.cpp:540-572)
+      if (j == n - 1 && i < n - 2) t *= q.area_out;
+      const float4 *g = gt + ((size_t) ro * NR + re) * NG;
+      const bool use_corr = corr && fabs(q.cf_g[j] - 1) > 1e-3;
+      const float cg = (float) (corr ? q.cf_g[j] : 1.0);
+      float h = 0.0f;
+#pragma unroll 4
+      for (int k = 0; k < NG; k++) {
+        const float4 v = __ldg(g + k);  // frac_g, g, log2 g, |g - 1| > 1e-3
+        float e = v.x;
+        if (use_corr) e *= rrad_corrected_boost_over_g(cg, v.y, v.z, gamma);
+        else if (v.w != 0.0f) e *= exp2f((gamma - 1.0f) * v.z);
+        h += e;
+      }
+      acc += h * (float) t * q.emis_in[j];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) q.er[i] = corr ? acc * q.cf_flux[i] : acc;
+  }
+}
+
+// rebin_emisprofile_on_radial_grid of the table-bin profile onto fine radius r (Rellp.cpp:120-175):
+// bins clamped to [0, n-2], linear radial factor (the profile's emission angles are 0), logarithmic
+// interpolation of the emissivity
+__device__ __forceinline__ double rrad_at(const RradSmem &q, double r) {
+  int lo = 0, hi = q.n;  // count of centres <= r
+  while (lo < hi) {
+    const int k = (lo + hi) >> 1;
+    if (q.rad[k] <= r) lo = k + 1; else hi = k;
+  }
+  const int kk = max(0, min(lo - 1, q.n - 2));
+  const float inter = (float) ((r - q.rad[kk]) * q.inv_drad[kk]);
+  return (double) (q.er[kk] * exp2f(inter * q.dl[kk]));
+}
 
 __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, int model, const RelxSetIn *__restrict__ sin,
                                                                const double *__restrict__ user_e, double *__restrict__ line_e,
@@ -520,6 +653,30 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     }
   }
   __syncthreads();
+  // ---- returning radiation without xillver corrections (calc_emis_profile, Rellp.cpp:556-558)
+  const bool rrad = m.return_rad != 0 && m.status == RELX_OK;
+  if (rrad) {
+    if (tid == 0) {
+      const int e = (tab.rr_nspin > 0) ? rrad_geometry(tab, m.rr, s.a, m.rms, m.re[NR - 1], m.re[0]) : RELX_ERR_TABLE;
+      if (e != RELX_OK) m.status = e;
+    }
+    __syncthreads();
+  }
+  if (rrad && m.status == RELX_OK) {
+    RradSmem &q = m.rr;
+    for (int j = tid; j < q.n; j += kSetupThreads) q.emis_in[j] = (float) rebin_mean_at(m.re, m.emis, NR, q.rad[j]);
+    __syncthreads();
+    rrad_pass(tab, q, (float) s.gamma, false);
+    __syncthreads();
+    for (int k = tid; k + 1 < q.n; k += kSetupThreads) q.dl[k] = log2f(q.er[k + 1] / q.er[k]);
+    __syncthreads();
+    for (int ii = tid; ii < NR; ii += kSetupThreads) {
+      m.emis_lp[ii] = (float) m.emis[ii];
+      const double r = rrad_at(q, m.re[ii]);
+      m.emis[ii] = (m.return_rad == 1) ? m.emis[ii] + r : r;
+    }
+    __syncthreads();
+  }
   for (int ii = tid; ii < NR; ii += kSetupThreads) {
     R.rec[ii].ew = (float) (m.emis[ii] * (double) R.wt[ii]);
   }
@@ -726,6 +883,67 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       zcout[set].row[z][c] = m.crow[e];
       zcout[set].w[z][c] = m.cw[e];
     }
+  }
+  // ---- returning radiation with the xillver flux-correction factors of the zones, for relxill models
+  // with a > 0 (Relxill.cpp:336-344, Relxill.h:32): the line profile uses this emissivity, the zones
+  // keep the one above
+  if (rrad && m.is_relxill && s.a > 0.0 && m.status == RELX_OK) {
+    RradSmem &q = m.rr;
+    if (tid < nz) {  // get_xillver_fluxcorrection_factors (Xillspec.cpp:500-526) from per-corner integrals
+      const int z = tid;
+      double ef = 0.0, pf = 0.0, pfz = 0.0;
+      for (int c = 0; c < 16; c++) {
+        const int e = z * 16 + c;
+        double w = 1.0;
+        for (int qq = 0; qq < 4; qq++) {
+          const double f = m.zfac[z][qq];
+          w *= ((c >> qq) & 1) ? f : (1.0 - f);
+        }
+        if (w == 0.0) continue;
+        if (!tab.x_has_dens) {
+          const double d = m.zdens[m.cfirst[e] >> 4];
+          if (fabs(d - 15) > 1e-6) w *= 1.0 / pow(10.0, d - 15);
+        }
+        const double *fc = tab.x_fcorr + (size_t) (m.crow[e] / ni) * 3;
+        ef += w * fc[0];
+        pf += w * fc[1];
+        pfz += w * fc[2];
+      }
+      // energy flux of the normalised direct spectrum in 0.1-1000 keV: the table normalisation,
+      // less the coarse bins outside that band (Xillspec.cpp:179-205, 344-361)
+      const double qz = (m.shift[z] == 1.0) ? m.qsum[0] : m.qsum[z + 1];
+      const float ecut = (float) (s.ect_src * m.shift[z]);
+      double x = 0.0;
+      for (int e2 = 0; e2 < 2; e2++) {
+        const int b = tab.coarse_b2_skip[e2];
+        if (b < 0) continue;
+        const float4 t = tab.coarse_t[b];
+        const float term = expf(1.0f / ecut) * m.cpow[b] * expf(-t.x / ecut) * t.y;
+        x += (double) term * ((double) t.z + (double) t.w);
+      }
+      const double ef_direct = (1e15 / 4.0 / kPi) / (1e20 * 1.602177e-09) - x / qz;
+      q.zcf_flux[z] = ef / ef_direct;
+      q.zcf_g[z] = (pf / pfz) / pow(1.5, s.gam);
+    }
+    __syncthreads();
+    for (int k = tid; k < q.n; k += kSetupThreads) {  // rebin_to_grid (Relreturn_Corona.cpp:208-222)
+      int zi = bsearch_asc<double>(s.rgrid, nz + 1, q.rad[k]);
+      if (q.rad[k] < s.rgrid[0]) zi = 0;
+      else if (q.rad[k] > s.rgrid[nz]) zi = nz - 1;
+      q.cf_flux[k] = (float) q.zcf_flux[zi];
+      q.cf_g[k] = q.zcf_g[zi];
+    }
+    __syncthreads();
+    rrad_pass(tab, q, (float) s.gamma, true);
+    __syncthreads();
+    for (int k = tid; k + 1 < q.n; k += kSetupThreads) q.dl[k] = log2f(q.er[k + 1] / q.er[k]);
+    __syncthreads();
+    for (int ii = tid; ii < NR; ii += kSetupThreads) {
+      const double r = rrad_at(q, m.re[ii]);
+      const double e = (m.return_rad == 1) ? (double) m.emis_lp[ii] + r : r;
+      R.rec[ii].ew = (float) (e * (double) R.wt[ii]);
+    }
+    if (tid == 0) s.rr_corr = 1;
   }
   // ---- primary and reflection factors (PrimarySource.cpp:66-125)
   if (tid == 0) {

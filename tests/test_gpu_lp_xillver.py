@@ -75,11 +75,35 @@ def test_local_model_entry_points_match_batch(gpu):
     np.testing.assert_array_equal(gpu.xillver(w, px), out[0])
 
 
-def test_lamp_post_returning_radiation_is_refused(gpu):
-    e = log_grid(0.1, 20.0, 300)
-    p = np.array([[6.4, 6, 0.998, 30, -1, 400, 0, 0, 2, 1]])
-    out, st = gpu.eval_batch("relline_lp", p, [e], check=False)
-    assert st[0] == 3 and not out[0].any()
+def test_returning_radiation_switch_values(gpu, oracle):
+    """$switch_returnrad 1 adds the returning radiation, -1 and 2 keep only it, other values fail
+    (add_returnrad_emis, Rellp.cpp:483-509)."""
+    e = log_grid(0.1, 20.0, 600)
+    base = [6.4, 6, 0.998, 30, -1, 400, 0, 0, 2, 0]
+    for sw in (1, -1, 2):
+        p = list(base)
+        p[9] = sw
+        out, st = gpu.eval_batch("relline_lp", np.array([p]), [e])
+        s, orc = oracle_lib.evaluate("relline_lp", p, e)
+        assert st[0] == 0 and s == 0
+        assert_close(out[0], orc, f"switch {sw}")
+    p = list(base)
+    p[9] = 3
+    out, st = gpu.eval_batch("relline_lp", np.array([p]), [e], check=False)
+    assert st[0] == 1 and not out[0].any()
+
+
+def test_returning_radiation_random_relxilllp(gpu, oracle):
+    """Random lamp-post sets with returning radiation over both spin signs (corrections only for
+    a > 0) and heights, against the oracle."""
+    rng = np.random.default_rng(45)
+    n = 10
+    p = np.column_stack([rng.uniform(3, 60, n), np.zeros(n), rng.uniform(-0.9, 0.998, n), rng.uniform(5, 85, n),
+                         -np.ones(n), rng.uniform(100, 1000, n), np.zeros(n), rng.uniform(1.4, 2.8, n),
+                         rng.uniform(0, 4.5, n), rng.uniform(0.5, 5, n), rng.uniform(20, 500, n), np.ones(n),
+                         np.ones(n), np.zeros(n)])
+    grids = _rng_grids(rng, n, 0.3, 80.0, 300, 2000)
+    _check_batch(gpu, "relxilllp", p, grids)
 
 
 def test_cache_separates_models(gpu):

@@ -96,9 +96,9 @@ def test_parameter_errors(gpu):
     assert st[0] == 1 and st[1] == 0
     assert not out[0].any() and out[1].sum() > 0
     rr = list(CASES[7][2])
-    rr[12] = 1  # returning radiation is outside this path
+    rr[12] = 3  # $switch_returnrad takes 0, 1, -1 or 2 (Rellp.cpp:497-506)
     out, st = gpu.eval_batch("relxilllp", np.array([rr]), [e], check=False)
-    assert st[0] == 3 and not out[0].any()
+    assert st[0] == 1 and not out[0].any()
     inc = list(CASES[5][2])
     inc[4] = 89.0  # inclination outside 3-87 degrees
     out, st = gpu.eval_batch("relxill", np.array([inc]), [e], check=False)
