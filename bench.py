@@ -176,62 +176,84 @@ def run_serve(R, seconds: float, rate: float, n_walkers: int, budget_gb: float, 
             "xillver_only_steps": 0.7, "identical_to_alone": same, "checked": checked}
 
 
+def _time_device_variant(R, L, torch, dev, steps: int, warmup: int, params, grids, igt_value: int, n_check: int = 2):
+    """Batched relxilllp through the device API on its own stream (CUDA events on that stream):
+    spectra/s, ms per step and the largest per-bin error of n_check sets against the oracle."""
+    n = len(grids)
+    edges, offs = R.pack_grids(grids)
+    nflux = int(offs[-1]) - n
+    igt = np.full(n, igt_value, dtype=np.int32)
+    d_params = torch.from_numpy(params).to(dev)
+    d_e = torch.from_numpy(edges).to(dev)
+    d_off = torch.from_numpy(offs).to(dev)
+    d_igt = torch.from_numpy(igt).to(dev)
+    d_igi = torch.zeros(n, dtype=torch.float64, device=dev)
+    d_flux = torch.empty(nflux, dtype=torch.float64, device=dev)
+    d_status = torch.empty(n, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    offs_ptr = offs.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    igt_ptr = igt.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    use_igt = igt_value != 0
+
+    def step():
+        st = L.relx_eval_batch_device(3, n, d_params.data_ptr(), d_e.data_ptr(), d_off.data_ptr(), offs_ptr, None,
+                                      d_flux.data_ptr(), d_status.data_ptr(), d_igt.data_ptr() if use_igt else None,
+                                      igt_ptr if use_igt else None, d_igi.data_ptr() if use_igt else None,
+                                      stream.cuda_stream)
+        if st:
+            raise RuntimeError(f"relx_eval_batch_device: {st} {R.last_error()}")
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    assert int((d_status != 0).sum()) == 0
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        ev0.record()
+    for _ in range(steps):
+        step()
+    with torch.cuda.stream(stream):
+        ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    out = d_flux.cpu().numpy()
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+
+    max_err = 0.0
+    for i in range(n_check):
+        st, ref = oracle_lib.evaluate("relxilllp", params[i], grids[i], None, igt_value, 0.0)
+        got = out[offs[i] - i: offs[i + 1] - i - 1]
+        m = ref > 1e-6 * ref.max()
+        max_err = max(max_err, float(np.max(np.abs(got[m] / ref[m] - 1))))
+    return {"value": n * steps / (ms / 1e3), "unit": "spectra/s", "sets": n, "steps": steps,
+            "ms_per_step": ms / steps, "max_rel_err_vs_oracle": max_err}
+
+
 def run_iongrad(R, L, torch, dev, steps: int, warmup: int, n: int = 2048):
     """Batched relxilllp with the ALPHA ionisation gradient (IonGradient.cpp:128-171) over 10 zones:
     2048 sets of the same draws, device buffers, CUDA events on the launching stream."""
     os.environ["RELXILL_NUM_RZONES"] = "10"
     try:
         params, grids = workload(n, seed_params=2027, seed_grids=8)
-        edges, offs = R.pack_grids(grids)
-        nflux = int(offs[-1]) - n
-        igt = np.full(n, 2, dtype=np.int32)
-        d_params = torch.from_numpy(params).to(dev)
-        d_e = torch.from_numpy(edges).to(dev)
-        d_off = torch.from_numpy(offs).to(dev)
-        d_igt = torch.from_numpy(igt).to(dev)
-        d_igi = torch.zeros(n, dtype=torch.float64, device=dev)
-        d_flux = torch.empty(nflux, dtype=torch.float64, device=dev)
-        d_status = torch.empty(n, dtype=torch.int32, device=dev)
-        stream = torch.cuda.Stream(device=dev)
-        offs_ptr = offs.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
-        igt_ptr = igt.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
-
-        def step():
-            st = L.relx_eval_batch_device(3, n, d_params.data_ptr(), d_e.data_ptr(), d_off.data_ptr(), offs_ptr, None,
-                                          d_flux.data_ptr(), d_status.data_ptr(), d_igt.data_ptr(), igt_ptr,
-                                          d_igi.data_ptr(), stream.cuda_stream)
-            if st:
-                raise RuntimeError(f"relx_eval_batch_device: {st} {R.last_error()}")
-
-        for _ in range(warmup):
-            step()
-        torch.cuda.synchronize()
-        assert int((d_status != 0).sum()) == 0
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            ev0.record()
-        for _ in range(steps):
-            step()
-        with torch.cuda.stream(stream):
-            ev1.record()
-        torch.cuda.synchronize()
-        ms = ev0.elapsed_time(ev1)
-        out = d_flux.cpu().numpy()
-        sys.path.insert(0, os.path.join(ROOT, "tests"))
-        import oracle_lib
-
-        max_err = 0.0
-        for i in range(2):
-            st, ref = oracle_lib.evaluate("relxilllp", params[i], grids[i], None, 2, 0.0)
-            got = out[offs[i] - i: offs[i + 1] - i - 1]
-            m = ref > 1e-6 * ref.max()
-            max_err = max(max_err, float(np.max(np.abs(got[m] / ref[m] - 1))))
-        return {"value": n * steps / (ms / 1e3), "unit": "spectra/s", "sets": n, "zones": 10, "steps": steps,
-                "ms_per_step": ms / steps, "mode": "ALPHA ionisation gradient (IonGradient.cpp:128-171)",
-                "max_rel_err_vs_oracle": max_err}
+        r = _time_device_variant(R, L, torch, dev, steps, warmup, params, grids, 2)
+        r.update({"zones": 10, "mode": "ALPHA ionisation gradient (IonGradient.cpp:128-171)"})
+        return r
     finally:
         os.environ.pop("RELXILL_NUM_RZONES", None)
+
+
+def run_rrad(R, L, torch, dev, steps: int, warmup: int, n: int = N_SETS):
+    """The 4096-set relxilllp workload with returning radiation switched on ($switch_returnrad = 1,
+    the reference's default): the return-table emissivity, the zones' xillver flux corrections for
+    a > 0 and the emissivity recomputed with them (Relxill.cpp:336-344)."""
+    params, grids = workload(n, seed_params=2028, seed_grids=9)
+    params = params.copy()
+    params[:, 12] = 1.0
+    r = _time_device_variant(R, L, torch, dev, steps, warmup, params, grids, 0)
+    r.update({"zones": 10, "mode": "returning radiation on (Relreturn_Corona.cpp, Relreturn_Table.cpp)"})
+    return r
 
 
 def tables(kind: str = "full") -> str:
@@ -387,7 +409,10 @@ def run_gpu(args):
     if rank == 0 and not args.no_cpu_baseline:
         pool = cpu_pool(tdir, procs)
     L = R.lib()
+    torch.zeros(1, device=f"cuda:{local}")  # the CUDA context first: the load time below is the tables'
+    t_load = time.perf_counter()
     R.init(tdir)
+    table_load_s = time.perf_counter() - t_load
     L.relx_profile_enable.argtypes = [ctypes.c_int]
     L.relx_profile_read.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64), ctypes.c_int]
     L.relx_profile_name.restype = ctypes.c_char_p
@@ -528,6 +553,9 @@ def run_gpu(args):
     iongrad = None
     if not args.no_iongrad:
         iongrad = run_iongrad(R, L, torch, dev, args.steps, args.warmup)
+    rrad = None
+    if not args.no_rrad:
+        rrad = run_rrad(R, L, torch, dev, args.steps, args.warmup)
 
     serve = None
     if not args.no_serve:
@@ -580,7 +608,8 @@ def run_gpu(args):
         "roofline": roof, "dominant_kernel": names[dom],
         "dominant_kernel_bound": "FP32 ALU issue (line profile: Romberg g*-integration; see profiles/)",
         "kernels": kernels, "cpu_baseline": cpu,
-        "serve": serve, "ion_gradient": iongrad,
+        "serve": serve, "ion_gradient": iongrad, "returning_radiation": rrad,
+        "table_load": {"seconds": table_load_s, "bytes": int(tb.value)},
     }
     print(json.dumps(line))
     if dist is not None:
@@ -601,6 +630,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-iongrad", action="store_true")
+    ap.add_argument("--no-rrad", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-rate", type=float, default=50000.0)
     ap.add_argument("--walkers", type=int, default=256)

@@ -35,7 +35,13 @@ struct SetupSmem {
   RelxSetState s;
   double re_tab[RELX_MAX_NRTAB], gmin_t[RELX_MAX_NRTAB], gmax_t[RELX_MAX_NRTAB];
   double re[RELX_NFRAD], emis[RELX_NFRAD], del_emit[RELX_NFRAD], del_inc[RELX_NFRAD];
-  double sqre[RELX_NFRAD];   // 1/u of the fine grid, i.e. sqrt(re)
+  union {
+    double sqre[RELX_NFRAD];   // 1/u of the fine grid, i.e. sqrt(re) (lamp-post flux boost only)
+    struct {                   // returning radiation, after the lamp-post emissivity
+      RradSmem rr;
+      float emis_lp[RELX_NFRAD];  // direct lamp-post emissivity
+    } rt;
+  };
   double inv_dtab[RELX_MAX_NRTAB];
   float re_tab_f[RELX_MAX_NRTAB];    // float copies guide the searches; FP64 decides float ties only
   float jet_rad_f[RELX_MAX_NRADLP], rgrid_f[RELX_NZMAX + 1];
@@ -66,9 +72,9 @@ struct SetupSmem {
   short cuniq[RELX_NZMAX * 16];
   float cw[RELX_NZMAX * 16];            // weight of every (zone, corner) entry
   unsigned char clive[RELX_NZMAX * 16]; // row has a non-zero weight in some zone
-  RradSmem rr;
-  float emis_lp[RELX_NFRAD];            // direct lamp-post emissivity (returning radiation only)
 };
+static_assert(sizeof(RradSmem) + sizeof(float) * RELX_NFRAD <= sizeof(double) * RELX_NFRAD,
+              "returning-radiation scratch fits in the lamp-post scratch it reuses");
 
 // ---------------------------------------------------------------------------
 // parameter mapping (lmodel_relxill_public.dat:1-75, ModelDefinition.cpp:153-385)
@@ -657,13 +663,13 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   const bool rrad = m.return_rad != 0 && m.status == RELX_OK;
   if (rrad) {
     if (tid == 0) {
-      const int e = (tab.rr_nspin > 0) ? rrad_geometry(tab, m.rr, s.a, m.rms, m.re[NR - 1], m.re[0]) : RELX_ERR_TABLE;
+      const int e = (tab.rr_nspin > 0) ? rrad_geometry(tab, m.rt.rr, s.a, m.rms, m.re[NR - 1], m.re[0]) : RELX_ERR_TABLE;
       if (e != RELX_OK) m.status = e;
     }
     __syncthreads();
   }
   if (rrad && m.status == RELX_OK) {
-    RradSmem &q = m.rr;
+    RradSmem &q = m.rt.rr;
     for (int j = tid; j < q.n; j += kSetupThreads) q.emis_in[j] = (float) rebin_mean_at(m.re, m.emis, NR, q.rad[j]);
     __syncthreads();
     rrad_pass(tab, q, (float) s.gamma, false);
@@ -671,7 +677,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     for (int k = tid; k + 1 < q.n; k += kSetupThreads) q.dl[k] = log2f(q.er[k + 1] / q.er[k]);
     __syncthreads();
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
-      m.emis_lp[ii] = (float) m.emis[ii];
+      m.rt.emis_lp[ii] = (float) m.emis[ii];
       const double r = rrad_at(q, m.re[ii]);
       m.emis[ii] = (m.return_rad == 1) ? m.emis[ii] + r : r;
     }
@@ -888,7 +894,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   // with a > 0 (Relxill.cpp:336-344, Relxill.h:32): the line profile uses this emissivity, the zones
   // keep the one above
   if (rrad && m.is_relxill && s.a > 0.0 && m.status == RELX_OK) {
-    RradSmem &q = m.rr;
+    RradSmem &q = m.rt.rr;
     if (tid < nz) {  // get_xillver_fluxcorrection_factors (Xillspec.cpp:500-526) from per-corner integrals
       const int z = tid;
       double ef = 0.0, pf = 0.0, pfz = 0.0;
@@ -940,7 +946,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     __syncthreads();
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
       const double r = rrad_at(q, m.re[ii]);
-      const double e = (m.return_rad == 1) ? (double) m.emis_lp[ii] + r : r;
+      const double e = (m.return_rad == 1) ? (double) m.rt.emis_lp[ii] + r : r;
       R.rec[ii].ew = (float) (e * (double) R.wt[ii]);
     }
     if (tid == 0) s.rr_corr = 1;
