@@ -39,6 +39,23 @@ cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, in
 void launch_xill_order(cudaStream_t s, const RelxSetState *sst, const RelxCorners *cor, const RelxZoneCorners *zcor,
                        int n_sets, int *order);
 
+// decoding of the xillver table's raw FITS rows on the device (table_ingest.cu)
+struct XillIngest {
+  int64_t width, col_off;   // bytes per FITS row, byte offset of the spectrum column
+  int ne, pad;              // energies per spectrum, padded row length
+  const double *lxi_div;    // 10^logXi per logXi grid value
+  int64_t stride_lxi;       // row-index stride of the logXi parameter
+  int n_lxi;                // logXi grid values (0: no logXi parameter)
+  const double *xe;         // xillver energy edges [ne + 1]
+  const double *pfz_coef;   // photon flux of the spectrum shifted by g = 2/3, per energy
+  float *spec;              // [rows][pad] output
+  double *rowflux;          // [rows][3] energy flux, photon flux, shifted photon flux
+  unsigned long long *bad;  // count of values that are not finite
+};
+cudaError_t launch_xill_ingest(cudaStream_t s, const XillIngest &g, const unsigned char *raw, int64_t row0, int nrows);
+cudaError_t launch_xill_corner_flux(cudaStream_t s, const double *rowflux, const double *incl_w, int n_incl,
+                                    int64_t n_corners, double *fcorr);
+
 // the xillver model: one CTA per set, writes the flux and the status fields of the set state
 size_t xillver_model_smem_bytes(int n_ener, int n_ener_pad);
 cudaError_t xillver_model_set_smem(int n_ener, int n_ener_pad);

@@ -267,7 +267,7 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
   // (get_xillver_fluxcorrection_factors, Xillspec.cpp:109-160, 344-361, 457-526): the energy flux
   // in 0.1-1000 keV, the photon flux in 0.15-500 keV, and that photon flux after the rebin of the
   // spectrum shifted by g = 2/3 (a fixed linear map of the row: coefficients pfz_coef).
-  std::vector<double> pfz_coef(ne, 0.0);
+  std::vector<double> pfz_coef(ne, 0.0);  // uploaded for the decoding kernel below
   {
     const double g0 = 2. / 3.;
     std::vector<double> ez(ne + 1);
@@ -292,69 +292,103 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
       }
     }
   }
-  std::vector<double> rowflux((size_t) 0);
   // strides of the row index (incl fastest, xilltable.c:325-337)
   int64_t stride_lxi = 1;
   for (int q = npar - 1; q > q_lxi; q--) stride_lxi *= nvals[q];
   int st = T.x_spec.reserve(sizeof(float) * (size_t) rows * pad);
   if (st) return st;
-  rowflux.assign((size_t) rows * 3, 0.0);
-  // read, renormalise by 10^-logXi of the row's grid point (renorm_xill_spec, xilltable.c:478-485), upload in chunks
-  const int64_t chunk = 4096;
-  std::vector<unsigned char> raw((size_t) (chunk * hs->width));
-  std::vector<float> buf((size_t) chunk * pad);
-  float *dst = T.x_spec.as<float>();
-  for (int64_t r0 = 0; r0 < rows; r0 += chunk) {
-    int64_t nr = std::min(chunk, rows - r0);
-    if (!f.read_rows(*hs, r0, nr, raw.data())) { g_errmsg = "xillver table: read failed"; return RELX_ERR_TABLE; }
-    int nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    std::vector<std::thread> th;
-    for (int t = 0; t < nth; t++) {
-      th.emplace_back([&, t]() {
-        for (int64_t r = t; r < nr; r += nth) {
-          int64_t row = r0 + r;
-          double lxi = 0.0;
-          if (q_lxi >= 0) lxi = vals[(size_t) q_lxi * maxv + (row / stride_lxi) % nvals[q_lxi]];
-          const double div = std::pow(10, lxi);
-          const unsigned char *p = raw.data() + r * hs->width + sc.offset;
-          float *o = buf.data() + (size_t) r * pad;
-          double ef = 0.0, pf = 0.0, pfz = 0.0;
-          for (int e = 0; e < ne; e++) {
-            float v = be_f32(p + 4 * e);
-            v /= div;  // float / double, stored as float (xilltable.c:480)
-            o[e] = v;
-            if (xe_host[e] >= 0.1 && xe_host[e + 1] <= 1000) ef += (double) v * 0.5 * (xe_host[e] + xe_host[e + 1]);
-            if (xe_host[e] >= 0.15 && xe_host[e + 1] <= 500.0) pf += (double) v;
-            pfz += pfz_coef[e] * (double) v;
-          }
-          for (int e = ne; e < pad; e++) o[e] = 0.0f;
-          rowflux[(size_t) row * 3 + 0] = ef;
-          rowflux[(size_t) row * 3 + 1] = pf;
-          rowflux[(size_t) row * 3 + 2] = pfz;
-        }
-      });
-    }
-    for (auto &x : th) x.join();
-    RELX_CUDA(cudaMemcpy(dst + (size_t) r0 * pad, buf.data(), sizeof(float) * (size_t) nr * pad, cudaMemcpyHostToDevice));
-  }
-  // inclination average per corner (calc_angle_averaged_xill_spec, Xillspec.cpp:109-127): the
-  // reference weights inclination i by norm_factor_semi_infinite_slab(incl_i * 180 / pi) / n_incl
-  // with incl_i the table value in degrees; restated as it is
   const int ni = nvals[npar - 1];
-  std::vector<double> fcorr((size_t) (rows / ni) * 3, 0.0);
-  for (int64_t c = 0; c < rows / ni; c++) {
-    for (int i = 0; i < ni; i++) {
-      const double incl_deg = (double) vals[(size_t) (npar - 1) * maxv + i] * 180 / kPiHost;
-      const double f = 0.5 * std::cos(incl_deg * kPiHost / 180) / ni;
-      for (int q = 0; q < 3; q++) fcorr[(size_t) c * 3 + q] += f * rowflux[(size_t) (c * ni + i) * 3 + q];
-    }
-  }
   std::vector<double> xe = xe_host;
   std::vector<float2> xew((size_t) ne + 1);
   for (int i = 0; i <= ne; i++) xew[i] = make_float2((float) xe[i], i < ne ? (float) (xe[i + 1] - xe[i]) : 0.0f);
+  // 10^logXi per logXi grid value (renorm_xill_spec, xilltable.c:478-485) and the inclination
+  // weights of the corner average (calc_angle_averaged_xill_spec, Xillspec.cpp:109-127: the
+  // reference weights inclination i by norm_factor_semi_infinite_slab(incl_i * 180 / pi) / n_incl
+  // with incl_i the table value in degrees; restated as it is)
+  std::vector<double> lxi_div(q_lxi >= 0 ? nvals[q_lxi] : 1, 1.0), incl_w(ni);
+  if (q_lxi >= 0)
+    for (int k = 0; k < nvals[q_lxi]; k++) lxi_div[k] = std::pow(10, (double) vals[(size_t) q_lxi * maxv + k]);
+  for (int i = 0; i < ni; i++) {
+    const double incl_deg = (double) vals[(size_t) (npar - 1) * maxv + i] * 180 / kPiHost;
+    incl_w[i] = 0.5 * std::cos(incl_deg * kPiHost / 180) / ni;
+  }
   if ((st = upload(T.x_vals, vals)) || (st = upload(T.x_e, xe)) || (st = upload(T.x_ew, xew)) ||
-      (st = upload(T.x_fcorr, fcorr)))
+      (st = T.x_fcorr.reserve(sizeof(double) * 3 * (size_t) (rows / ni))))
     return st;
+  // decode on the GPU (table_ingest.cu): raw rows read in chunks into two pinned buffers, so that
+  // the file read of one chunk overlaps the copy and decoding of the previous one
+  const int64_t chunk = 4096;
+  const size_t chunk_bytes = (size_t) chunk * hs->width;
+  DevBuf d_raw[2], d_rowflux, d_div, d_pfz, d_inclw, d_bad;
+  Pinned h_raw[2];
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  auto cleanup = [&]() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (auto &e : done)
+      if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+    for (auto &b : d_raw) b.release();
+    for (auto &b : h_raw) b.release();
+    d_rowflux.release();
+    d_div.release();
+    d_pfz.release();
+    d_inclw.release();
+    d_bad.release();
+  };
+  int rc = 0;
+  if ((rc = d_raw[0].reserve(chunk_bytes)) || (rc = d_raw[1].reserve(chunk_bytes)) ||
+      (rc = h_raw[0].reserve(chunk_bytes)) || (rc = h_raw[1].reserve(chunk_bytes)) ||
+      (rc = d_rowflux.reserve(sizeof(double) * 3 * (size_t) rows)) || (rc = upload(d_div, lxi_div)) ||
+      (rc = upload(d_pfz, pfz_coef)) || (rc = upload(d_inclw, incl_w)) || (rc = d_bad.reserve(8))) {
+    cleanup();
+    return rc;
+  }
+  XillIngest g;
+  g.width = hs->width;
+  g.col_off = sc.offset;
+  g.ne = ne;
+  g.pad = pad;
+  g.lxi_div = d_div.as<double>();
+  g.stride_lxi = stride_lxi;
+  g.n_lxi = q_lxi >= 0 ? nvals[q_lxi] : 0;
+  g.xe = T.x_e.as<double>();
+  g.pfz_coef = d_pfz.as<double>();
+  g.spec = T.x_spec.as<float>();
+  g.rowflux = d_rowflux.as<double>();
+  g.bad = d_bad.as<unsigned long long>();
+  cudaError_t ce = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+  for (int b = 0; b < 2 && ce == cudaSuccess; b++) ce = cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaMemsetAsync(g.bad, 0, 8, stream);
+  for (int64_t r0 = 0, k = 0; r0 < rows && ce == cudaSuccess; r0 += chunk, k++) {
+    const int b = (int) (k & 1);
+    const int64_t nr = std::min(chunk, rows - r0);
+    if (k >= 2 && (ce = cudaEventSynchronize(done[b])) != cudaSuccess) break;  // buffer b is free again
+    if (!f.read_rows(*hs, r0, nr, (unsigned char *) h_raw[b].h)) {
+      g_errmsg = "xillver table: read failed";
+      cleanup();
+      return RELX_ERR_TABLE;
+    }
+    if ((ce = cudaMemcpyAsync(d_raw[b].p, h_raw[b].h, (size_t) nr * hs->width, cudaMemcpyHostToDevice, stream)) !=
+            cudaSuccess ||
+        (ce = launch_xill_ingest(stream, g, d_raw[b].as<unsigned char>(), r0, (int) nr)) != cudaSuccess)
+      break;
+    ce = cudaEventRecord(done[b], stream);
+  }
+  if (ce == cudaSuccess)
+    ce = launch_xill_corner_flux(stream, g.rowflux, d_inclw.as<double>(), ni, rows / ni, T.x_fcorr.as<double>());
+  unsigned long long nbad = 0;
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(&nbad, g.bad, 8, cudaMemcpyDeviceToHost, stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
+  cleanup();
+  if (ce != cudaSuccess) {
+    g_errmsg = std::string("xillver table ingest: ") + cudaGetErrorString(ce);
+    return RELX_ERR_CUDA;
+  }
+  if (nbad) {  // table validation
+    g_errmsg = "xillver table: " + std::to_string(nbad) + " spectrum values are not finite";
+    return RELX_ERR_TABLE;
+  }
   T.d.x_npar = npar; T.d.x_nener = ne; T.d.x_nener_pad = pad; T.d.x_nincl = nvals[npar - 1];
   for (int q = 0; q < RELX_MAX_XPAR; q++) { T.d.x_nvals[q] = q < npar ? nvals[q] : 0; T.d.x_pindex[q] = q < npar ? pidx[q] : -1; }
   T.d.x_has_dens = has_dens;
