@@ -22,6 +22,9 @@ static ModelName model_from_id(int id) {
     case 4: return ModelName::relline_lp;
     case 5: return ModelName::relconv_lp;
     case 6: return ModelName::xillver;
+    case 7: return ModelName::xillverCp;
+    case 8: return ModelName::relxillCp;
+    case 9: return ModelName::relxilllpCp;
     default: return ModelName::relline;
   }
 }
@@ -62,10 +65,13 @@ extern "C" int ref_eval_relxilllp_iongrad(const double *params, int iongrad_type
  * so that the next evaluation behaves as the first one in a fresh process.
  * The rows are leaked on purpose: freeing them is the reference's job. */
 extern "C" xillTable *cached_xill_tab;
+extern "C" xillTable *cached_xill_tab_dens_nthcomp;
 extern "C" void ref_reset_xillver_cache(void) {
   /* the full-output cache is keyed on the public parameters only
    * (Relcache.h:134-147), so hidden switches would hit it: empty it as well */
   RelxillCache::instance().empty();
-  if (cached_xill_tab == nullptr) return;
-  for (int ii = 0; ii < cached_xill_tab->num_elements; ii++) cached_xill_tab->data_storage[ii] = nullptr;
+  for (xillTable *t : {cached_xill_tab, cached_xill_tab_dens_nthcomp}) {
+    if (t == nullptr) continue;
+    for (int ii = 0; ii < t->num_elements; ii++) t->data_storage[ii] = nullptr;
+  }
 }

@@ -297,6 +297,7 @@ typedef struct {
   /* xillver parameters */
   double gam, afe, lxi, ect, dens, refl_frac, iongrad_index;
   int interpret_reflfrac_as_boost;
+  int prim_type;  /* 0: cut-off power law (ect = Ecut), 1: nthcomp (ect = kTe; the Cp models) */
 } Params;
 
 /* get_num_zones, relutility.c:506-544 */
@@ -389,6 +390,32 @@ static int map_params(int model, const double *v, int ion_grad_type, double iong
       p->incl = v[5];  /* degrees: xillParam keeps the inclination in degrees */
       p->refl_frac = v[6];
       return 0;      /* no relativistic parameters (get_rel_params returns none for xillver models) */
+    case RELXO_XILLVERCP:  /* lmodel_relxill_public.dat:86-94 */
+      p->prim_type = 1;
+      p->gam = v[0]; p->afe = v[1]; p->ect = v[2]; p->lxi = v[3]; p->dens = v[4]; p->z = v[5];
+      p->incl = v[6];
+      p->refl_frac = v[7];
+      return 0;
+    case RELXO_RELXILLCP:  /* lmodel_relxill_public.dat:96-110 */
+      p->prim_type = 1;
+      p->is_relxill = 1;
+      p->emis_type = EMIS_TYPE_BKN;
+      p->incl = v[0] * M_PI / 180; p->a = v[1]; p->rin = v[2]; p->rout = v[3]; p->rbr = v[4]; p->emis1 = v[5];
+      p->emis2 = v[6]; p->z = v[7]; p->gam = v[8]; p->lxi = v[9]; p->dens = v[10]; p->afe = v[11]; p->ect = v[12];
+      p->refl_frac = v[13];
+      break;
+    case RELXO_RELXILLLPCP:  /* lmodel_relxill_public.dat:112-129: the ionisation gradient is a parameter */
+      p->prim_type = 1;
+      p->is_relxill = 1;
+      p->emis_type = EMIS_TYPE_LP;
+      p->incl = v[0] * M_PI / 180; p->a = v[1]; p->rin = v[2]; p->rout = v[3]; p->height = v[4]; p->beta = v[5];
+      p->gam = v[6]; p->lxi = v[7]; p->dens = v[8]; p->afe = v[9]; p->ect = v[10]; p->refl_frac = v[11];
+      p->z = v[12];
+      iongrad_index = v[13];
+      ion_grad_type = (int) lround(v[14]);
+      p->return_rad = (int) lround(v[15]);
+      p->interpret_reflfrac_as_boost = (int) lround(v[16]);
+      break;
     default:
       return 1;
   }
@@ -598,10 +625,11 @@ static const char *g_xill_names[] = {"Gamma", "A_Fe", "logXi", "Ecut", "kTe", "D
 static const int g_xill_index[] = {PARAM_GAM, PARAM_AFE, PARAM_LXI, PARAM_ECT, PARAM_ECT, PARAM_DNS, 5, PARAM_AFE, 6,
                                    PARAM_INC};
 
-/* init_xillver_table, xilltable.c:169-276, 410-447 */
-static XillTable *load_xill_table(void) {
+/* init_xillver_table, xilltable.c:169-276, 410-447: 5-parameter tables, and the 6-parameter
+ * nthcomp table (xillverCp_v3.4.fits, common.h:166) */
+static XillTable *load_xill_table_file(const char *fname) {
   char path[2048];
-  fullpath(path, "xillver-a-Ec5.fits");
+  fullpath(path, fname);
   int st = 0;
   fitsfile *fp = NULL;
   if (fits_open_table(&fp, path, READONLY, &st)) return NULL;
@@ -609,7 +637,7 @@ static XillTable *load_xill_table(void) {
   long n;
   fits_get_num_rows(fp, &n, &st);  /* first table = PARAMETERS */
   t->num_param = (int) n;
-  if (t->num_param != 5) { fits_close_file(fp, &st); free(t); return NULL; }
+  if (t->num_param != 5 && t->num_param != 6) { fits_close_file(fp, &st); free(t); return NULL; }
   fits_movnam_hdu(fp, BINARY_TBL, "ENERGIES", 0, &st);
   fits_get_num_rows(fp, &n, &st);
   t->n_ener = (int) n;
@@ -642,10 +670,13 @@ static XillTable *load_xill_table(void) {
   return t;
 }
 
-/* get_xillspec_rownum, xilltable.c:325-337 (5 parameters; 1-based row) */
-static long xill_rownum(const XillTable *t, int ii, int jj, int kk, int ll, int mm) {
-  const int *n = t->num_param_vals;
-  return ((((long) ii * n[1] + jj) * n[2] + kk) * n[3] + ll) * n[4] + mm + 1;
+static XillTable *load_xill_table(void) { return load_xill_table_file("xillver-a-Ec5.fits"); }
+
+/* get_xillspec_rownum, xilltable.c:325-337 (1-based row): idx holds one index per table parameter */
+static long xill_rownum_idx(const XillTable *t, const int *idx) {
+  long row = 0;
+  for (int q = 0; q < t->num_param; q++) row = row * t->num_param_vals[q] + idx[q];
+  return row + 1;
 }
 
 static int xilltab_param_index(const XillTable *t, int ind) {
@@ -663,15 +694,23 @@ static int xilltab_param_index(const XillTable *t, int ind) {
  * the first zone (in zone order) that uses it.  That is the rule restated
  * here: eval_dens[row] remembers the first zone's density within one call. */
 static double *g_eval_dens = NULL;
+static long g_eval_dens_n = 0;
 static float *g_dens_buf = NULL;
 
 static void xill_begin_eval(XillTable *t) {
-  if (!g_eval_dens) g_eval_dens = malloc(sizeof(double) * t->num_elements);
+  if (g_eval_dens_n < t->num_elements) {
+    free(g_eval_dens);
+    g_eval_dens = malloc(sizeof(double) * t->num_elements);
+    g_eval_dens_n = t->num_elements;
+  }
   for (long i = 0; i < t->num_elements; i++) g_eval_dens[i] = NAN;
 }
 
-static const float *xill_spec(XillTable *t, int ii, int jj, int kk, int ll, int mm, double zone_dens, float *buf) {
-  long row = xill_rownum(t, ii, jj, kk, ll, mm);
+/* idx: one index per table parameter.  A table with a density parameter divides its rows by
+ * 10^(logN - 15) of the row's grid point as well (renorm_xill_spec, xilltable.c:478-485). */
+static const float *xill_spec_idx(XillTable *t, const int *idx, double zone_dens, float *buf) {
+  long row = xill_rownum_idx(t, idx);
+  const int ind_dns = xilltab_param_index(t, PARAM_DNS);
   if (t->data[row - 1] == NULL) {
     float *spec = malloc(sizeof(float) * t->n_ener);
     int st = 0;
@@ -679,12 +718,15 @@ static const float *xill_spec(XillTable *t, int ii, int jj, int kk, int ll, int 
     if (st) { free(spec); return NULL; }
     int ind_lxi = xilltab_param_index(t, PARAM_LXI);
     double logxi = 0.0;
-    int idx[5] = {ii, jj, kk, ll, mm};
     if (ind_lxi >= 0) logxi = t->param_vals[ind_lxi][idx[ind_lxi]];
-    for (int i = 0; i < t->n_ener; i++) spec[i] /= pow(10, logxi);
+    const double dens_row = ind_dns >= 0 ? t->param_vals[ind_dns][idx[ind_dns]] : 15.0;
+    for (int i = 0; i < t->n_ener; i++) {
+      spec[i] /= pow(10, logxi);
+      if (fabs(dens_row - 15) > 1e-6) spec[i] /= pow(10, dens_row - 15);
+    }
     t->data[row - 1] = spec;
   }
-  if (xilltab_param_index(t, PARAM_DNS) >= 0) return t->data[row - 1];
+  if (ind_dns >= 0) return t->data[row - 1];
   if (g_eval_dens[row - 1] != g_eval_dens[row - 1]) g_eval_dens[row - 1] = zone_dens;
   double dens = g_eval_dens[row - 1];
   if (!(fabs(dens - 15) > 1e-6)) return t->data[row - 1];
@@ -696,11 +738,19 @@ static const float *xill_spec(XillTable *t, int ii, int jj, int kk, int ll, int 
   return buf;
 }
 
-static int ensure_tables(int need_xill) {
+static const float *xill_spec(XillTable *t, int ii, int jj, int kk, int ll, int mm, double zone_dens, float *buf) {
+  const int idx[5] = {ii, jj, kk, ll, mm};
+  return xill_spec_idx(t, idx, zone_dens, buf);
+}
+
+static XillTable *g_xill_cp = NULL;
+
+static int ensure_tables(int need_xill, int need_cp) {
   if (!g_rel) g_rel = load_rel_table();
   if (!g_lp) g_lp = load_lp_table();
   if (need_xill && !g_xill) g_xill = load_xill_table();
-  return (g_rel && g_lp && (!need_xill || g_xill)) ? 0 : 1;
+  if (need_cp && !g_xill_cp) g_xill_cp = load_xill_table_file("xillverCp_v3.4.fits");
+  return (g_rel && g_lp && (!need_xill || g_xill) && (!need_cp || g_xill_cp)) ? 0 : 1;
 }
 
 /* ======================================================================= */
@@ -1417,6 +1467,228 @@ static const double *coarse_grid(void) {
 }
 
 /* 1/calcNormWrtXillverTableSpec of the cut-off power law on the coarse grid */
+/* ----------------------------------------------------------------------- */
+/* nthcomp (donthcomp.c): thermal Comptonization of disk-blackbody seed     */
+/* photons, the Kompaneets equation with relativistic corrections solved on */
+/* a logarithmic grid (Lightman & Zdziarski 1987; Zdziarski, Johnson &     */
+/* Magdziarz 1996; Zycki, Done & Smith 1999).  Restated for the parameters  */
+/* the Cp models pass (get_nthcomp_param, relutility.c:625-631): seed      */
+/* temperature 0.05 keV, disk-blackbody seed (inp_type 1).                  */
+/* ----------------------------------------------------------------------- */
+
+#define NTH_LOG10E 0.43429448190325182765
+static double nth_lg10(double x) { return NTH_LOG10E * log(x); }
+
+/* multi-colour disk spectrum integrand (Mitsuda et al. 1984, Makishima et al. 1986; interpolation
+ * formula with residual table, donthcomp.c:52-103) */
+static double nth_mcdint(double et) {
+  static const double gc[3] = {.078196667, -1.066202, 1.192418};
+  static const double gw[3] = {.5207874, .513457, .4077983};
+  static const double gn[3] = {.3728691, .039775528, .037766505};
+  static const double res[98] = {
+      9.6198382e-4, .0010901181, .0012310012, .0013841352, .0015481583, .0017210036, .0018988943, .002076939,
+      .0022484281, .0024049483, .0025366202, .0026316255, .0026774985, .0026613059, .0025708784, .0023962965,
+      .002130655, .0017725174, .0013268656, 8.0657672e-4, 2.3337584e-4, -3.6291778e-4, -9.4443569e-4, -.0014678875,
+      -.0018873741, -.0021588493, -.0022448371, -.0021198179, -.0017754602, -.0012246034, -5.0414167e-4,
+      3.2507078e-4, .0011811065, .0019673402, .0025827094, .0029342526, .0029517083, .0026012166, .0018959062,
+      9.0128649e-4, -2.6757144e-4, -.0014567885, -.002492855, -.0032079776, -.0034678637, -.0031988217,
+      -.0024080969, -.001193624, 2.6134145e-4, .0017117758, .0028906898, .0035614435, .0035711778, .0028921374,
+      .0016385898, 4.9857464e-5, -.0015572671, -.0028578151, -.0035924212, -.0036253044, -.002975086,
+      -.0018044436, -3.7796664e-4, .0010076215, .0020937327, .0027090854, .0028031667, .0024276576, .0017175597,
+      8.1030795e-4, -1.2592304e-4, -9.4888491e-4, -.0015544816, -.0018831972, -.0019203142, -.0016905849,
+      -.0012487737, -6.6789911e-4, -2.7079461e-5, 5.9931935e-4, .0011499748, .0015816521, .0018709224,
+      .0020129966, .0020184702, .0019089181, .0017122289, .001458377, .0011760717, 8.9046768e-4, 6.2190822e-4,
+      3.8553762e-4, 1.9155022e-4, 4.5837109e-5, -4.9177834e-5, -9.3670762e-5, -8.9622968e-5, -4.01538532e-5};
+  const double loget = nth_lg10(et);
+  const double lo = 0.001;
+  double pos = (loget - nth_lg10(lo)) / .06 + 1;
+  const int j = (int) pos;
+  double resfact;
+  if (j < 1) {
+    resfact = res[0];
+  } else if (j >= 98) {
+    resfact = res[97];
+  } else {
+    pos -= j;
+    resfact = res[j - 1] * (1. - pos) + res[j] * pos;
+  }
+  double gaufact = 1.;
+  for (int k = 0; k < 3; k++) {
+    const double zz = (loget - gc[k]) / gw[k];
+    gaufact += gn[k] * exp(-zz * zz / 2.);
+  }
+  const double et0 = et / .001;
+  return pow(et0, -.66666666666666663) * 193.21556 * (pow(et, 1.663753) * .52876731 + 1.) * exp(-et) * gaufact *
+         (resfact + 1.);
+}
+
+/* disk-blackbody photon spectrum per bin, five-point Gauss-Legendre per bin (donthcomp.c:137-191):
+ * ear[0..ne], photar[0..ne-1] */
+static void nth_diskbb(const double *ear, int ne, double tin, double *photar) {
+  static const double gw5[5] = {.236926885, .47862867, .568888888, .47862867, .236926885};
+  static const double gx5[5] = {-.906179846, -.53846931, 0., .53846931, .906179846};
+  for (int i = 1; i <= ne; i++) {
+    const double xn = (ear[i] - ear[i - 1]) / 2.f;
+    double acc = 0.f;
+    const double xh = xn + ear[i - 1];
+    for (int k = 0; k < 5; k++) {
+      const double e = xn * gx5[k] + xh;
+      double photon = 0.;
+      if (tin != 0.) photon = nth_mcdint(e / tin) * tin * tin * 1. / 361.;
+      acc += (double) (gw5[k] * photon);
+    }
+    photar[i - 1] = acc * xn;
+  }
+}
+
+/* Kompaneets equation as a tridiagonal system a u(j+1) + b u(j) + c u(j-1) = d, zero flux at both
+ * ends (donthcomp.c:194-280).  x and dphesc are indexed j = 1..jmax (x up to jmax + 1); c2, bet and
+ * dphdot hold the value of point j at j - 1. */
+static void nth_solve(double tautom, double theta, double deltal, const double *x, int jmax, double *dphesc,
+                      const double *dphdot, const double *bet, const double *c2) {
+  double a[900], b[900], c[900], d[900], g[900], u[900], gam[900], alp[900];
+  const double c20 = tautom / deltal;
+  for (int j = 2; j <= jmax - 1; j++) {
+    const double w1 = sqrt(x[j] * x[j + 1]), w2 = sqrt(x[j - 1] * x[j]);
+    a[j - 1] = -c20 * c2[j - 1] * (theta / deltal / w1 + .5);
+    const double t1 = -c20 * c2[j - 1] * (.5 - theta / deltal / w1);
+    const double t2 = c20 * c2[j - 2] * (theta / deltal / w2 + .5);
+    const double t3 = pow(x[j], 3.) * (tautom * bet[j - 1]);
+    b[j - 1] = t1 + t2 + t3;
+    c[j - 1] = c20 * c2[j - 2] * (.5 - theta / deltal / w2);
+    d[j - 1] = x[j] * dphdot[j - 1];
+  }
+  const double x32 = sqrt(x[1] * x[2]);
+  const double aa = (theta / deltal / x32 + .5) / (theta / deltal / x32 - .5);
+  u[jmax - 1] = 0.;
+  alp[1] = b[1] + c[1] * aa;
+  gam[1] = a[1] / alp[1];
+  for (int j = 3; j <= jmax - 1; j++) {
+    alp[j - 1] = b[j - 1] - c[j - 1] * gam[j - 2];
+    gam[j - 1] = a[j - 1] / alp[j - 1];
+  }
+  g[1] = d[1] / alp[1];
+  for (int j = 3; j <= jmax - 2; j++) g[j - 1] = (d[j - 1] - c[j - 1] * g[j - 2]) / alp[j - 1];
+  g[jmax - 2] = (d[jmax - 2] - a[jmax - 2] * u[jmax - 1] - c[jmax - 2] * g[jmax - 3]) / alp[jmax - 2];
+  u[jmax - 2] = g[jmax - 2];
+  for (int j = 3; j <= jmax - 1; j++) {
+    const int jj = jmax + 1 - j;
+    u[jj - 1] = g[jj - 1] - gam[jj - 1] * u[jj];
+  }
+  u[0] = aa * u[1];
+  for (int j = 1; j <= jmax; j++) dphesc[j] = x[j] * x[j] * u[j - 1] * bet[j - 1] * tautom;
+}
+
+/* Comptonized disk-blackbody spectrum in E F_E on the grid x (units of m_e c^2): x[1..jmax + 1],
+ * sptot[1..jmax - 1] (donthcomp.c:458-616) */
+static int nth_thdscompton(double tempbb, double theta, double gamma, double *x, double *sptot) {
+  double c2[901], rel[900], bet[901], dphdot[901], dphesc[901], ear[5001], photar[5000];
+  double d1 = gamma + .5;
+  const double tautom = sqrt(3. / (theta * (d1 * d1 - 2.25)) + 2.25) - 1.5;
+  for (int j = 0; j < 900; j++) {
+    dphesc[j] = dphdot[j] = rel[j] = bet[j] = c2[j] = 0.;
+    sptot[j + 1] = 0.;
+  }
+  const double delta = .02;
+  const double deltal = delta * log(10.);
+  const double xmin = tempbb * 1e-4, xmax = theta * 40.;
+  int jmax = (int) (nth_lg10(xmax / xmin) / delta) + 1;
+  if (jmax > 899) jmax = 899;
+  for (int j = 1; j <= jmax + 1; j++) x[j] = xmin * pow(10., (j - 1) * delta);
+  for (int j = 1; j <= jmax; j++) {
+    const double w = x[j], w1 = sqrt(x[j] * x[j + 1]);
+    c2[j - 1] = (double) (pow(w1, 4.) / (w1 * 4.6 + 1. + w1 * 1.1 * w1));
+    if (w <= .05) {
+      rel[j - 1] = (double) (1 - w * 2 + w * 26 * w / 5);
+    } else {
+      const double z1 = (w + 1) / (w * (w * w)), z2 = w * 2 + 1, z3 = log(z2), z4 = w * 2 * (w + 1) / z2,
+                   z5 = z3 / 2 / w, z6 = (w * 3 + 1) / z2 / z2;
+      rel[j - 1] = (double) ((z1 * (z4 - z3) + z5 - z6) * .75);
+    }
+  }
+  int jmaxth = (int) (nth_lg10(tempbb * 50. / xmin) / delta);
+  if (jmaxth > 900) jmaxth = 900;
+  if (jmaxth > jmax) jmaxth = jmax;
+  for (int j = 1; j <= jmaxth - 1; j++) ear[j - 1] = sqrt(x[j] * x[j + 1]) * 511.;
+  const int ne = jmaxth - 2;
+  nth_diskbb(ear, ne, tempbb * 511., photar);
+  for (int j = 1; j <= ne; j++) dphdot[j] = photar[j - 1] * 511. / (ear[j] - ear[j - 1]);
+  dphdot[0] = dphdot[1];
+  int jnr = (int) (nth_lg10(.1 / xmin) / delta + 1);
+  if (jnr > jmax - 1) jnr = jmax - 1;
+  int jrel = (int) (nth_lg10(1. / xmin) / delta + 1);
+  if (jrel > jmax) jrel = jmax;
+  const double xnr = x[jnr], xr = x[jrel];
+  for (int j = 1; j <= jnr - 1; j++) {
+    const double taukn = tautom * rel[j - 1];
+    bet[j - 1] = 1 / tautom / (taukn / 3 + 1);
+  }
+  for (int j = jnr; j <= jrel; j++) {
+    const double taukn = tautom * rel[j - 1];
+    const double arg = (x[j] - xnr) / (xr - xnr);
+    const double flz = 1 - arg;
+    bet[j - 1] = 1 / tautom / (taukn / 3 * flz + 1);
+  }
+  for (int j = jrel + 1; j <= jmax; j++) bet[j - 1] = 1 / tautom;
+  nth_solve(tautom, theta, deltal, x, jmax, dphesc, dphdot, bet, c2);
+  for (int j = 1; j <= jmax - 1; j++) {
+    const double xj = x[j];
+    sptot[j] = dphesc[j] * (xj * xj);
+  }
+  return jmax;
+}
+
+/* c_donthcomp (donthcomp.c:640-793) with kTbb = 0.05 keV and the disk-blackbody seed: photon flux
+ * per bin on ear[0..ne], normalised to 1 at 1 keV in E F_E (observer frame, redshift z) */
+static void nthcomp_spectrum(const double *ear, int ne, double gamma, double kte, double z, double *photar) {
+  double xth[901], spt[901];
+  const int nth = nth_thdscompton(.05 / 511., kte / 511., gamma, xth, spt);
+  /* xth[1..], spt[1..]: the reference's xth[j-1], spt[j-1] */
+  const double xn = (z + 1) / 511.;
+  const double xx = 1 / (1 / xn);
+  int ih = 2;  /* f_spp__ (donthcomp.c:617-638): linear interpolation in E F_E */
+  while (ih < nth && xx > xth[ih]) ++ih;
+  const int il = ih - 1;
+  const double spp = spt[il] + (spt[ih] - spt[il]) * (xx - xth[il]) / (xth[ih] - xth[il]);
+  const double normfac = 1 / spp;
+  double *prim = calloc(ne + 1, sizeof(double));
+  int j = 1;
+  for (int i = 0; i <= ne; i++) {
+    while (j <= nth && xth[j] * 511. < ear[i] * (z + 1)) ++j;
+    if (j <= nth) {
+      if (j > 1) {
+        const int jl = j - 1;
+        prim[i] = spt[jl] + (ear[i] / 511. * (z + 1) - xth[jl]) * (spt[jl + 1] - spt[jl]) / (xth[jl + 1] - xth[jl]);
+      } else {
+        prim[i] = spt[1];
+      }
+    }
+  }
+  for (int i = 1; i <= ne; i++)
+    photar[i - 1] = (prim[i] / pow(ear[i], 2.) + prim[i - 1] / pow(ear[i - 1], 2.)) * .5 * (ear[i] - ear[i - 1]) * normfac;
+  free(prim);
+}
+
+void relxo_nthcomp(const double *ear, int ne, double gamma, double kte, double z, double *photar) {
+  nthcomp_spectrum(ear, ne, gamma, kte, z, photar);
+}
+
+/* calc_primary_spectrum (Xillspec.cpp:274-300): cut-off power law or nthcomp, shifted by ener_shift */
+#define PRIM_ECUT 0
+#define PRIM_NTHCOMP 1
+static void primary_spectrum(int prim_type, double *out, const double *ener, int n, double ect, double gam,
+                             double ener_shift) {
+  if (prim_type == PRIM_NTHCOMP) nthcomp_spectrum(ener, n, gam, ect, 1 / ener_shift - 1, out);
+  else spec_cutoffpl(out, ener, n, ect, gam, ener_shift);
+}
+
+/* 1 / calcNormWrtXillverTableSpec of the source-frame primary on the coarse grid */
+static double primary_norm_factor(int prim_type, double ect, double gam) {
+  double pl[N_ENER_COARSE];
+  primary_spectrum(prim_type, pl, coarse_grid(), N_ENER_COARSE, ect, gam, 1.0);
+  return 1. / relxo_norm_wrt_xillver(pl, coarse_grid(), N_ENER_COARSE);
+}
+
 double relxo_primary_norm_factor(double ect, double gam) {
   double pl[N_ENER_COARSE];
   spec_cutoffpl(pl, coarse_grid(), N_ENER_COARSE, ect, gam, 1.0);
@@ -1441,14 +1713,15 @@ static int xillver_spectra_all_incl(XillTable *t, double gam, double afe, double
   inp[PARAM_ECT] = (float) ect;
   inp[PARAM_DNS] = (float) dens;
   inp[PARAM_INC] = (float) incl_deg;
-  int ind[5];
-  for (int ii = 0; ii < t->num_param; ii++) {
+  const int np = t->num_param;
+  int ind[6];
+  for (int ii = 0; ii < np; ii++) {
     ind[ii] = binary_search_float(t->param_vals[ii], t->num_param_vals[ii], inp[t->param_index[ii]]);
     if (ind[ii] < 0) ind[ii] = 0;
     else if (ind[ii] > t->num_param_vals[ii] - 2) ind[ii] = t->num_param_vals[ii] - 2;
   }
-  double ipol[5];
-  for (int ii = 0; ii < t->num_param; ii++) {
+  double ipol[6];
+  for (int ii = 0; ii < np; ii++) {
     int pind = t->param_index[ii];
     if (pind != PARAM_INC) {  /* resetInpvalsToBoundaries, xilltable.c:1069-1088 */
       float lo = t->param_vals[ii][0], hi = t->param_vals[ii][t->num_param_vals[ii] - 1];
@@ -1464,47 +1737,57 @@ static int xillver_spectra_all_incl(XillTable *t, double gam, double afe, double
     if (ect <= ev[0]) ipol[iect] = 0.0;
     if (ect >= ev[t->num_param_vals[t->param_index[iect]] - 1]) ipol[iect] = 1.0;
   }
-  double f1 = ipol[0], f2 = ipol[1], f3 = ipol[2], f4 = ipol[3];
-  double f_0000 = (1.0 - f1) * (1.0 - f2) * (1.0 - f3) * (1 - f4);
-  double f_1000 = (f1) * (1.0 - f2) * (1.0 - f3) * (1 - f4);
-  double f_0100 = (1.0 - f1) * (f2) * (1.0 - f3) * (1 - f4);
-  double f_0010 = (1.0 - f1) * (1.0 - f2) * (f3) * (1 - f4);
-  double f_0001 = (1.0 - f1) * (1.0 - f2) * (1.0 - f3) * (f4);
-  double f_1010 = (f1) * (1.0 - f2) * (f3) * (1 - f4);
-  double f_1001 = (f1) * (1.0 - f2) * (1.0 - f3) * (f4);
-  double f_0101 = (1.0 - f1) * (f2) * (1.0 - f3) * (f4);
-  double f_1100 = (f1) * (f2) * (1.0 - f3) * (1 - f4);
-  double f_0110 = (1.0 - f1) * (f2) * (f3) * (1 - f4);
-  double f_0011 = (1.0 - f1) * (1.0 - f2) * (f3) * (f4);
-  double f_1101 = (f1) * (f2) * (1.0 - f3) * (f4);
-  double f_1110 = (f1) * (f2) * (f3) * (1 - f4);
-  double f_1011 = (f1) * (1.0 - f2) * (f3) * (f4);
-  double f_0111 = (1.0 - f1) * (f2) * (f3) * (f4);
-  double f_1111 = (f1) * (f2) * (f3) * (f4);
-  int i1 = ind[0], i2 = ind[1], i3 = ind[2], i4 = ind[3];
-  for (int mm = 0; mm < t->n_incl; mm++) {
-    const float *d[16];
-    /* order of interp_5d_tab_incl, xilltable.c:816-834 */
-    const int off[16][4] = {{0, 0, 0, 0}, {1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {1, 1, 0, 0}, {1, 0, 1, 0},
-                            {0, 1, 1, 0}, {1, 1, 1, 0}, {0, 0, 0, 1}, {1, 0, 0, 1}, {0, 1, 0, 1}, {0, 0, 1, 1},
-                            {1, 1, 0, 1}, {1, 0, 1, 1}, {0, 1, 1, 1}, {1, 1, 1, 1}};
-    if (!g_dens_buf) g_dens_buf = malloc(sizeof(float) * 16 * t->n_ener);
-    for (int c = 0; c < 16; c++) {
-      d[c] = xill_spec(t, i1 + off[c][0], i2 + off[c][1], i3 + off[c][2], i4 + off[c][3], mm, dens,
-                       g_dens_buf + (size_t) c * t->n_ener);
-      if (!d[c]) return 1;
+  /* 5 parameters: interp_5d_tab_incl over parameters 0..3; 6 parameters: interp_6d_tab_incl, the
+   * same over parameters 1..4 at both brackets of parameter 0, then linear in parameter 0
+   * (xilltable.c:812-876, 999-1020) */
+  const int q0 = np - 5;  /* first parameter of the 16-corner block */
+  const double f1 = ipol[q0], f2 = ipol[q0 + 1], f3 = ipol[q0 + 2], f4 = ipol[q0 + 3];
+  const double fw[16] = {
+      (1.0 - f1) * (1.0 - f2) * (1.0 - f3) * (1 - f4), (f1) * (1.0 - f2) * (1.0 - f3) * (1 - f4),
+      (1.0 - f1) * (f2) * (1.0 - f3) * (1 - f4),       (1.0 - f1) * (1.0 - f2) * (f3) * (1 - f4),
+      (f1) * (f2) * (1.0 - f3) * (1 - f4),             (f1) * (1.0 - f2) * (f3) * (1 - f4),
+      (1.0 - f1) * (f2) * (f3) * (1 - f4),             (f1) * (f2) * (f3) * (1 - f4),
+      (1.0 - f1) * (1.0 - f2) * (1.0 - f3) * (f4),     (f1) * (1.0 - f2) * (1.0 - f3) * (f4),
+      (1.0 - f1) * (f2) * (1.0 - f3) * (f4),           (1.0 - f1) * (1.0 - f2) * (f3) * (f4),
+      (f1) * (f2) * (1.0 - f3) * (f4),                 (f1) * (1.0 - f2) * (f3) * (f4),
+      (1.0 - f1) * (f2) * (f3) * (f4),                 (f1) * (f2) * (f3) * (f4)};
+  /* order of interp_5d_tab_incl, xilltable.c:816-834 */
+  const int off[16][4] = {{0, 0, 0, 0}, {1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {1, 1, 0, 0}, {1, 0, 1, 0},
+                          {0, 1, 1, 0}, {1, 1, 1, 0}, {0, 0, 0, 1}, {1, 0, 0, 1}, {0, 1, 0, 1}, {0, 0, 1, 1},
+                          {1, 1, 0, 1}, {1, 0, 1, 1}, {0, 1, 1, 1}, {1, 1, 1, 1}};
+  if (!g_dens_buf) g_dens_buf = malloc(sizeof(float) * 16 * t->n_ener);
+  double *s1 = malloc(sizeof(double) * t->n_ener), *s2 = malloc(sizeof(double) * t->n_ener);
+  int status = 0;
+  for (int mm = 0; mm < t->n_incl && !status; mm++) {
+    for (int half = 0; half < (np == 6 ? 2 : 1) && !status; half++) {
+      const float *d[16];
+      for (int c = 0; c < 16 && !status; c++) {
+        int idx[6];
+        if (np == 6) idx[0] = ind[0] + half;
+        for (int q = 0; q < 4; q++) idx[q0 + q] = ind[q0 + q] + off[c][q];
+        idx[np - 1] = mm;
+        d[c] = xill_spec_idx(t, idx, dens, g_dens_buf + (size_t) c * t->n_ener);
+        if (!d[c]) status = 1;
+      }
+      if (status) break;
+      double *out = (np == 6) ? (half ? s2 : s1) : flu + (size_t) mm * t->n_ener;
+      for (int ii = 0; ii < t->n_ener; ii++) {
+        out[ii] = fw[0] * (double) (d[0][ii]) + fw[1] * (double) (d[1][ii]) + fw[2] * (double) (d[2][ii])
+            + fw[3] * (double) (d[3][ii]) + fw[4] * (double) (d[4][ii]) + fw[5] * (double) (d[5][ii])
+            + fw[6] * (double) (d[6][ii]) + fw[7] * (double) (d[7][ii]) + fw[8] * (double) (d[8][ii])
+            + fw[9] * (double) (d[9][ii]) + fw[10] * (double) (d[10][ii]) + fw[11] * (double) (d[11][ii])
+            + fw[12] * (double) (d[12][ii]) + fw[13] * (double) (d[13][ii]) + fw[14] * (double) (d[14][ii])
+            + fw[15] * (double) (d[15][ii]);
+      }
     }
-    double *out = flu + (size_t) mm * t->n_ener;
-    for (int ii = 0; ii < t->n_ener; ii++) {
-      out[ii] = f_0000 * (double) (d[0][ii]) + f_1000 * (double) (d[1][ii]) + f_0100 * (double) (d[2][ii])
-          + f_0010 * (double) (d[3][ii]) + f_1100 * (double) (d[4][ii]) + f_1010 * (double) (d[5][ii])
-          + f_0110 * (double) (d[6][ii]) + f_1110 * (double) (d[7][ii]) + f_0001 * (double) (d[8][ii])
-          + f_1001 * (double) (d[9][ii]) + f_0101 * (double) (d[10][ii]) + f_0011 * (double) (d[11][ii])
-          + f_1101 * (double) (d[12][ii]) + f_1011 * (double) (d[13][ii]) + f_0111 * (double) (d[14][ii])
-          + f_1111 * (double) (d[15][ii]);
+    if (np == 6 && !status) {
+      double *out = flu + (size_t) mm * t->n_ener;
+      for (int ii = 0; ii < t->n_ener; ii++) out[ii] = interp_lin_1d(ipol[0], s1[ii], s2[ii]);
     }
   }
-  return 0;
+  free(s1);
+  free(s2);
+  return status;
 }
 
 /* get_xilltab_indices_for_paramvals + interp_xill_table + interp_5d_tab (xilltable.c:278-323,
@@ -1519,13 +1802,13 @@ static int xillver_spectrum_at_incl(XillTable *t, double gam, double afe, double
   inp[PARAM_ECT] = (float) ect;
   inp[PARAM_DNS] = (float) dens;
   inp[PARAM_INC] = (float) incl_deg;
-  int ind[5];
+  int ind[6];
   for (int ii = 0; ii < t->num_param; ii++) {
     ind[ii] = binary_search_float(t->param_vals[ii], t->num_param_vals[ii], inp[t->param_index[ii]]);
     if (ind[ii] < 0) ind[ii] = 0;
     else if (ind[ii] > t->num_param_vals[ii] - 2) ind[ii] = t->num_param_vals[ii] - 2;
   }
-  double ipol[5];
+  double ipol[6];
   for (int ii = 0; ii < t->num_param; ii++) {
     int pind = t->param_index[ii];
     /* resetInpvalsToBoundaries (xilltable.c:1069-1088), the inclination included for xillver models */
@@ -1540,7 +1823,10 @@ static int xillver_spectrum_at_incl(XillTable *t, double gam, double afe, double
     if (ect <= ev[0]) ipol[iect] = 0.0;
     if (ect >= ev[t->num_param_vals[t->param_index[iect]] - 1]) ipol[iect] = 1.0;
   }
-  const double f1 = ipol[0], f2 = ipol[1], f3 = ipol[2], f4 = ipol[3], f5 = ipol[4];
+  /* 5 parameters: interp_5d_tab; 6 parameters: interp_6d_tab, the same over parameters 1..5 at both
+   * brackets of parameter 0, then linear in parameter 0 (xilltable.c:878-995, 1022-1043) */
+  const int np = t->num_param, q0 = np - 5;
+  const double f1 = ipol[q0], f2 = ipol[q0 + 1], f3 = ipol[q0 + 2], f4 = ipol[q0 + 3], f5 = ipol[q0 + 4];
   /* the 32 corners in the order of interp_5d_tab's weights and sum (xilltable.c:884-992):
    * bits (c1 c2 c3 c4 c5) of the corner offsets */
   static const int corner[32][5] = {
@@ -1553,20 +1839,29 @@ static int xillver_spectrum_at_incl(XillTable *t, double gam, double afe, double
   double w[32];
   const float *d[32];
   float *buf = malloc(sizeof(float) * 32 * (size_t) t->n_ener);
-  for (int c = 0; c < 32; c++) {
-    const int *o = corner[c];
-    w[c] = (o[0] ? f1 : (1.0 - f1)) * (o[1] ? f2 : (1.0 - f2)) * (o[2] ? f3 : (1.0 - f3)) * (o[3] ? f4 : (1 - f4)) *
-           (o[4] ? f5 : (1 - f5));
-    d[c] = xill_spec(t, ind[0] + o[0], ind[1] + o[1], ind[2] + o[2], ind[3] + o[3], ind[4] + o[4], dens,
-                     buf + (size_t) c * t->n_ener);
-    if (!d[c]) { free(buf); return 1; }
+  double *s1 = malloc(sizeof(double) * t->n_ener);
+  for (int half = 0; half < (np == 6 ? 2 : 1); half++) {
+    for (int c = 0; c < 32; c++) {
+      const int *o = corner[c];
+      w[c] = (o[0] ? f1 : (1.0 - f1)) * (o[1] ? f2 : (1.0 - f2)) * (o[2] ? f3 : (1.0 - f3)) *
+             (o[3] ? f4 : (1 - f4)) * (o[4] ? f5 : (1 - f5));
+      int idx[6];
+      if (np == 6) idx[0] = ind[0] + half;
+      for (int q = 0; q < 5; q++) idx[q0 + q] = ind[q0 + q] + o[q];
+      d[c] = xill_spec_idx(t, idx, dens, buf + (size_t) c * t->n_ener);
+      if (!d[c]) { free(buf); free(s1); return 1; }
+    }
+    double *out = (np == 6 && half == 0) ? s1 : flu;
+    for (int ii = 0; ii < t->n_ener; ii++) {
+      double acc = w[0] * (double) d[0][ii];
+      for (int c = 1; c < 32; c++) acc = acc + w[c] * (double) d[c][ii];
+      out[ii] = acc;
+    }
   }
-  for (int ii = 0; ii < t->n_ener; ii++) {
-    double acc = w[0] * (double) d[0][ii];
-    for (int c = 1; c < 32; c++) acc = acc + w[c] * (double) d[c][ii];
-    flu[ii] = acc;
-  }
+  if (np == 6)
+    for (int ii = 0; ii < t->n_ener; ii++) flu[ii] = interp_lin_1d(ipol[0], s1[ii], flu[ii]);
   free(buf);
+  free(s1);
   return 0;
 }
 
@@ -1602,8 +1897,8 @@ static int relbase_single(const Params *p, const double *ener, int n, double *fl
  * zone's spectra per inclination on the xillver grid xener.  The reference weights inclination i
  * by norm_factor_semi_infinite_slab(incl_i * 180 / pi) / n_incl with incl_i the table value in
  * degrees, i.e. 0.5 cos(incl_i) with incl_i read as radians; restated as it is. */
-static void xillver_fluxcorrection_factors(const XillTable *t, const double *flu, const double *xener, double ect_zone,
-                                           double gam, double *fac_flux, double *fac_gshift) {
+static void xillver_fluxcorrection_factors(const XillTable *t, const double *flu, const double *xener, int prim_type,
+                                           double ect_zone, double gam, double *fac_flux, double *fac_gshift) {
   const int n_x = t->n_ener, ni = t->n_incl;
   double *avg = calloc(n_x, sizeof(double)), *ener_z = malloc(sizeof(double) * (n_x + 1)),
          *flu_z = malloc(sizeof(double) * n_x);
@@ -1618,7 +1913,7 @@ static void xillver_fluxcorrection_factors(const XillTable *t, const double *flu
     if (xener[ii] >= 0.1 && xener[ii + 1] <= 1000) ef_refl += avg[ii] * 0.5 * (xener[ii] + xener[ii + 1]);
   const double *cg = coarse_grid();
   double direct[N_ENER_COARSE];
-  spec_cutoffpl(direct, cg, N_ENER_COARSE, ect_zone, gam, 1.0);
+  primary_spectrum(prim_type, direct, cg, N_ENER_COARSE, ect_zone, gam, 1.0);
   const double nf = 1. / relxo_norm_wrt_xillver(direct, cg, N_ENER_COARSE);
   double ef_direct = 0.0;
   for (int ii = 0; ii < N_ENER_COARSE; ii++) {
@@ -1655,8 +1950,9 @@ static int relxill_kernel(const Params *p, double *out_conv /* [N_ENER_CONV] */)
     g_inf = calc_g_inf(p->height, p->a);
     if (!(p->beta < 1e-4)) g_inf *= doppler_factor(M_PI - p->incl, p->beta);
   }
-  double ect_source = p->ect;
-  if (p->emis_type == EMIS_TYPE_LP) ect_source /= g_inf;
+  double ect_source = p->ect;  /* the cut-off energy of the lamp post is given in the observer frame,
+                                 kTe in the source frame (Relxill.cpp:220-230) */
+  if (p->emis_type == EMIS_TYPE_LP && p->prim_type == PRIM_ECUT) ect_source /= g_inf;
   /* IonGradient (IonGradient.cpp:340-390, 457-492) */
   double rgrid[N_ZONES_MAX + 1], rmean[N_ZONES_MAX], del_emit[N_ZONES_MAX], shift[N_ZONES_MAX];
   double lxi[N_ZONES_MAX], dens[N_ZONES_MAX];
@@ -1709,7 +2005,7 @@ static int relxill_kernel(const Params *p, double *out_conv /* [N_ENER_CONV] */)
     if (lxi[ii] < 0.0) lxi[ii] = 0.0;
     else if (lxi[ii] > 4.7) lxi[ii] = 4.7;
   }
-  XillTable *xt = g_xill;
+  XillTable *xt = (p->prim_type == PRIM_NTHCOMP) ? g_xill_cp : g_xill;
   int n_incl = xt->n_incl, n_x = xt->n_ener;
   double *xener = malloc(sizeof(double) * (n_x + 1));
   for (int ii = 0; ii < n_x; ii++) xener[ii] = xt->elo[ii];
@@ -1729,7 +2025,7 @@ static int relxill_kernel(const Params *p, double *out_conv /* [N_ENER_CONV] */)
         status = 1;
         break;
       }
-      xillver_fluxcorrection_factors(xt, flu, xener, ect_zone, p->gam, &corr.corrfac_flux[zz],
+      xillver_fluxcorrection_factors(xt, flu, xener, p->prim_type, ect_zone, p->gam, &corr.corrfac_flux[zz],
                                      &corr.corrfac_gshift[zz]);
     }
     if (!status) sp_rel = get_system_parameters(p, &corr, &status);
@@ -1741,7 +2037,7 @@ static int relxill_kernel(const Params *p, double *out_conv /* [N_ENER_CONV] */)
   if (sp_rel != sp) free_syspar(sp_rel);
   /* xillver spectra per zone, angle weighted (Relxill.cpp:357-386) */
   double *xz = malloc(sizeof(double) * nz * n_x);
-  double src_norm = relxo_primary_norm_factor(ect_source, p->gam);
+  double src_norm = primary_norm_factor(p->prim_type, ect_source, p->gam);
   for (int zz = 0; zz < nz && !status; zz++) {
     double ect_zone = ect_source * shift[zz];
     if (xillver_spectra_all_incl(xt, p->gam, p->afe, lxi[zz], ect_zone, p->incl * 180 / M_PI, dens[zz], flu)) {
@@ -1752,7 +2048,7 @@ static int relxill_kernel(const Params *p, double *out_conv /* [N_ENER_CONV] */)
     for (int jj = 0; jj < n_x; jj++) xf[jj] = 0.0;
     for (int ii = 0; ii < n_incl; ii++)
       for (int jj = 0; jj < n_x; jj++) xf[jj] += dist[zz * n_incl + ii] * flu[(size_t) ii * n_x + jj];
-    double nf = relxo_primary_norm_factor(ect_zone, p->gam) / src_norm;
+    double nf = primary_norm_factor(p->prim_type, ect_zone, p->gam) / src_norm;
     for (int jj = 0; jj < n_x; jj++) xf[jj] /= nf;
   }
   /* relxill_convolution_multizone, Relxill.cpp:432-482 */
@@ -1770,7 +2066,7 @@ static int relxill_kernel(const Params *p, double *out_conv /* [N_ENER_CONV] */)
   if (!status) {
     double *prim = malloc(sizeof(double) * N_ENER_CONV);
     double eshift = (p->emis_type == EMIS_TYPE_LP) ? g_inf : 1.0;
-    spec_cutoffpl(prim, ener, N_ENER_CONV, ect_source, p->gam, eshift);
+    primary_spectrum(p->prim_type, prim, ener, N_ENER_CONV, ect_source, p->gam, eshift);
     for (int ie = 0; ie < N_ENER_CONV; ie++) prim[ie] *= src_norm;
     if (p->emis_type != EMIS_TYPE_LP) {
       for (int ie = 0; ie < N_ENER_CONV; ie++) out_conv[ie] *= fabs(p->refl_frac);
@@ -1796,7 +2092,7 @@ static int relxill_kernel(const Params *p, double *out_conv /* [N_ENER_CONV] */)
  * semi-infinite slab factor 0.5 cos(incl) (Xillspec.cpp:528-545), rebinned to the caller's grid,
  * and add_primary_component without relativistic parameters (Relbase.cpp:294-349) */
 static int xillver_model(const Params *p, const double *ener, int n, double *flux) {
-  XillTable *t = g_xill;
+  XillTable *t = (p->prim_type == PRIM_NTHCOMP) ? g_xill_cp : g_xill;
   xill_begin_eval(t);
   const int nx = t->n_ener;
   double *spec = malloc(sizeof(double) * nx), *xe = malloc(sizeof(double) * (nx + 1));
@@ -1809,8 +2105,8 @@ static int xillver_model(const Params *p, const double *ener, int n, double *flu
     relxo_rebin_spectrum(ener, flux, n, xe, spec, nx);
     /* calc_normalized_primary_spectrum (Xillspec.cpp:302-332) on the caller's grid */
     double *pl = malloc(sizeof(double) * n);
-    spec_cutoffpl(pl, ener, n, p->ect, p->gam, 1.0);
-    const double norm = relxo_primary_norm_factor(p->ect, p->gam);
+    primary_spectrum(p->prim_type, pl, ener, n, p->ect, p->gam, 1.0);
+    const double norm = primary_norm_factor(p->prim_type, p->ect, p->gam);
     for (int ii = 0; ii < n; ii++) pl[ii] *= norm;
     for (int ii = 0; ii < n; ii++) flux[ii] *= fabs(p->refl_frac);
     if (p->refl_frac >= 0)
@@ -1837,15 +2133,16 @@ int relxo_eval_ext(int model, const double *params, int ion_grad_type, double io
   const int is_conv = (model == RELXO_RELCONV || model == RELXO_RELCONVLP);
   for (int ii = 0; ii < n_flux; ii++) if (!is_conv) flux[ii] = 0.0;
   if (map_params(model, params, ion_grad_type, iongrad_index, &p)) return 1;
+  const int is_cp = (model == RELXO_XILLVERCP || model == RELXO_RELXILLCP || model == RELXO_RELXILLLPCP);
   int is_rx = (model == RELXO_RELXILL || model == RELXO_RELXILLLP || model == RELXO_XILLVER);
-  if (ensure_tables(is_rx)) return 2;
+  if (ensure_tables(is_rx, is_cp)) return 2;
   /* XspecSpectrum copy + shift_energy_grid_redshift (XspecSpectrum.h:35-76) */
   double *ener = malloc(sizeof(double) * (n_flux + 1));
   for (int ii = 0; ii <= n_flux; ii++) ener[ii] = energy[ii];
   if (p.z > 0)
     for (int ii = 0; ii <= n_flux; ii++) ener[ii] *= (1 + p.z);
   int status = 0;
-  if (model == RELXO_XILLVER) {
+  if (model == RELXO_XILLVER || model == RELXO_XILLVERCP) {
     status = xillver_model(&p, ener, n_flux, flux);
   } else if (model == RELXO_RELLINE || model == RELXO_RELLINELP) {
     /* line_model, LocalModel.cpp:32-51 */
@@ -1903,7 +2200,7 @@ int relxo_relline_profile_zones(int model, const double *params, const double *e
                                 double *flux, int n_incl, double *dist) {
   Params p;
   if (map_params(model, params, ION_GRAD_TYPE_CONST, 0.0, &p)) return 1;
-  if (ensure_tables(0)) return 2;
+  if (ensure_tables(0, 0)) return 2;
   int status = 0;
   SysPar *sp = get_system_parameters(&p, NULL, &status);
   double rgrid[N_ZONES_MAX + 1];

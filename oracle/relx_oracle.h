@@ -10,7 +10,7 @@ extern "C" {
 #endif
 
 enum { RELXO_RELLINE = 0, RELXO_RELCONV = 1, RELXO_RELXILL = 2, RELXO_RELXILLLP = 3, RELXO_RELLINELP = 4,
-       RELXO_RELCONVLP = 5, RELXO_XILLVER = 6 };
+       RELXO_RELCONVLP = 5, RELXO_XILLVER = 6, RELXO_XILLVERCP = 7, RELXO_RELXILLCP = 8, RELXO_RELXILLLPCP = 9 };
 
 int relxo_set_table_path(const char *path);
 /* one model evaluation; params in lmodel.dat order; returns 0 on success */
@@ -32,6 +32,8 @@ double relxo_primary_norm_factor(double ect, double gam);
 double relxo_norm_change(double energy_shift, double ect, double gam);
 void relxo_conv_spectrum_normalized(const double *ener, const double *fxill, const double *frel, double *fout, int n);
 void relxo_conv_grid(double *out);
+/* nthcomp photon spectrum per bin (kTbb 0.05 keV, disk-blackbody seed) on ear[0..ne] */
+void relxo_nthcomp(const double *ear, int ne, double gamma, double kte, double z, double *photar);
 int relxo_relline_profile_zones(int model, const double *params, const double *ener, int n_ener, int *nzones_out,
                                 double *flux, int n_incl, double *dist);
 

@@ -23,6 +23,11 @@ works on synthetic tables with the same layout, shapes and value ranges:
   spectrum is a cut-off power law plus a 6.4 keV Gaussian whose equivalent
   width rises with logXi, scaled by 10^logXi, times lognormal noise (sigma
   0.05).
+* xillverCp table (nthcomp continuum, common.h:166): the same OGIP layout
+  with six parameters, Gamma, A_Fe, logXi, kTe, Dens, Incl (row order of the
+  6-parameter get_xillspec_rownum, xilltable.c:325-337); spectra as above
+  with a cut-off at 2.7 kTe and scaled by 10^(Dens - 15) as well (the loader
+  divides by both, xilltable.c:478-485).  Small grid (4 x 3 x 4 x 4 x 3 x 10).
 * returning-radiation table: extension ``SPIN`` (column ``a``), then one
   extension ``FRAC01``, ``FRAC02``, ... per spin with 50 rows (one per
   incident radial bin, Relreturn_Table.cpp:180-330) and double columns
@@ -56,6 +61,7 @@ RELTABLE_FILENAME = "rel_table_v0.5a.fits"
 LPTABLE_FILENAME = "rel_lp_table_v0.5b.fits"
 XILLTABLE_FILENAME = "xillver-a-Ec5.fits"
 RRADTABLE_FILENAME = "table_returnRad_v20220301.fits"
+XILLTABLE_CP_FILENAME = "xillverCp_v3.4.fits"
 RRAD_NR = 50  # common.h:127-128
 RRAD_NG = 20
 RRAD_SPINS = (-0.998, -0.5, 0.0, 0.3, 0.5, 0.7, 0.8, 0.9, 0.95, 0.98, 0.99, 0.998)
@@ -299,6 +305,72 @@ def write_xillver_table(path: str, dims: XillDims | None = None, seed=1234) -> N
         st.close()
 
 
+def write_xillver_cp_table(path: str, seed: int = 1234, n_ener: int = 2999) -> None:
+    rng = np.random.default_rng(seed + 3)
+    gam = np.array([1.2, 1.9, 2.6, 3.4], dtype=np.float32)
+    afe = np.array([0.5, 1.0, 3.0], dtype=np.float32)
+    lxi = np.array([0.0, 1.5, 3.0, 4.7], dtype=np.float32)
+    kte = np.array([5.0, 20.0, 60.0, 400.0], dtype=np.float32)
+    dns = np.array([15.0, 17.5, 20.0], dtype=np.float32)
+    inc = XillDims([1.0], [1.0], [1.0], [1.0]).incl.astype(np.float32)
+    names = ["Gamma", "A_Fe", "logXi", "kTe", "Dens", "Incl"]
+    vals = [gam, afe, lxi, kte, dns, inc]
+    npar = len(vals)
+    nmax = max(len(v) for v in vals)
+    value = np.zeros((npar, nmax), dtype=np.float32)
+    for i, v in enumerate(vals):
+        value[i, : len(v)] = v
+    zeros = np.zeros((npar, 1), dtype=np.float32)
+    params_cols = [
+        fits.Column("NAME", "A", 12, np.array(names)),
+        fits.Column("METHOD", "J", 1, np.zeros((npar, 1), dtype=np.int32)),
+        fits.Column("INITIAL", "E", 1, np.array([[v[len(v) // 2]] for v in vals], dtype=np.float32)),
+        fits.Column("DELTA", "E", 1, zeros + 0.01),
+        fits.Column("MINIMUM", "E", 1, np.array([[v[0]] for v in vals], dtype=np.float32)),
+        fits.Column("BOTTOM", "E", 1, np.array([[v[0]] for v in vals], dtype=np.float32)),
+        fits.Column("TOP", "E", 1, np.array([[v[-1]] for v in vals], dtype=np.float32)),
+        fits.Column("MAXIMUM", "E", 1, np.array([[v[-1]] for v in vals], dtype=np.float32)),
+        fits.Column("NUMBVALS", "J", 1, np.array([[len(v)] for v in vals], dtype=np.int32)),
+        fits.Column("VALUE", "E", nmax, value),
+    ]
+    edges = np.exp(np.linspace(np.log(0.07), np.log(1000.0), n_ener + 1)).astype(np.float32)
+    elo, ehi = edges[:-1], edges[1:]
+    em = 0.5 * (elo.astype(np.float64) + ehi.astype(np.float64))
+    de = ehi.astype(np.float64) - elo.astype(np.float64)
+    mu = np.cos(np.radians(inc.astype(np.float64)))
+    n_rows = int(np.prod([len(v) for v in vals]))
+    with open(path, "wb") as f:
+        f.write(fits.primary_header())
+        f.write(fits.bintable("PARAMETERS", params_cols, npar))
+        f.write(fits.bintable("ENERGIES", [fits.Column("ENERG_LO", "E", 1, elo[:, None]),
+                                           fits.Column("ENERG_HI", "E", 1, ehi[:, None])], n_ener))
+        st = fits.StreamingTable(f, "SPECTRA", [("PARAMVAL", "E", npar), ("INTPSPEC", "E", n_ener)], n_rows)
+        for ig, g in enumerate(gam.astype(np.float64)):
+            E = 2.7 * kte.astype(np.float64)
+            norm = _coarse_norm(np.full(E.shape, g), E)
+            cont = (np.exp(1.0 / E)[:, None] * em[None, :] ** (-g) * np.exp(-em[None, :] / E[:, None])
+                    * de[None, :] * norm[:, None])                                   # (kte, ener)
+            L = lxi.astype(np.float64)[None, :, None, None, None, None]
+            F = afe.astype(np.float64)[:, None, None, None, None, None]
+            D = dns.astype(np.float64)[None, None, None, :, None, None]
+            MU = mu[None, None, None, None, :, None]
+            soft = 1.0 + 0.3 * (D - 15.0) / 5.0 * np.exp(-em / 0.5)[None, None, None, None, None, :]
+            albedo = (0.25 + 0.08 * L) * (0.6 + 0.4 * MU) / (0.8 + 0.1 * np.log(F)) * soft
+            ew = 0.02 * (1.0 + L) * np.sqrt(F)
+            c64 = np.array([np.interp(6.4, em, cont[k] / de) for k in range(len(E))])
+            gauss = np.exp(-0.5 * ((em - 6.4) / 0.12) ** 2) / (0.12 * np.sqrt(2 * np.pi)) * de
+            spec = (cont[None, None, :, None, None, :] * albedo
+                    + ew * c64[None, None, :, None, None, None] * gauss[None, None, None, None, None, :])
+            spec = spec * (10.0 ** L) * (10.0 ** (D - 15.0))
+            spec = np.broadcast_to(spec, (len(afe), len(lxi), len(kte), len(dns), len(inc), n_ener))
+            noise = np.exp(0.05 * rng.standard_normal(spec.shape))
+            spec = (spec * noise).astype(np.float32).reshape(-1, n_ener)
+            grid = np.stack(np.meshgrid(afe, lxi, kte, dns, inc, indexing="ij"), -1).reshape(-1, 5)
+            pv = np.concatenate([np.full((grid.shape[0], 1), gam[ig], np.float32), grid.astype(np.float32)], 1)
+            st.write_rows(PARAMVAL=pv, INTPSPEC=spec)
+        st.close()
+
+
 # ----------------------------------------------------------------------------
 # returning-radiation table
 # ----------------------------------------------------------------------------
@@ -349,16 +421,20 @@ def write_all(outdir: str, xill: str = "full", seed: int = 1234) -> str:
     write_lp_table(os.path.join(outdir, LPTABLE_FILENAME), seed=seed)
     write_xillver_table(os.path.join(outdir, XILLTABLE_FILENAME), xill_dims(xill), seed=seed)
     write_rrad_table(os.path.join(outdir, RRADTABLE_FILENAME), seed=seed)
+    write_xillver_cp_table(os.path.join(outdir, XILLTABLE_CP_FILENAME), seed=seed)
     return outdir
 
 
 def ensure_tables(outdir: str, xill: str = "full", seed: int = 1234) -> str:
-    """Write the four tables into ``outdir`` unless a complete set is there."""
+    """Write the five tables into ``outdir`` unless a complete set is there."""
     stamp = os.path.join(outdir, f".complete_{xill}_{seed}")
     if not os.path.exists(stamp):
         write_all(outdir, xill=xill, seed=seed)
-    elif not os.path.exists(os.path.join(outdir, RRADTABLE_FILENAME)):
-        write_rrad_table(os.path.join(outdir, RRADTABLE_FILENAME), seed=seed)
+    else:
+        if not os.path.exists(os.path.join(outdir, RRADTABLE_FILENAME)):
+            write_rrad_table(os.path.join(outdir, RRADTABLE_FILENAME), seed=seed)
+        if not os.path.exists(os.path.join(outdir, XILLTABLE_CP_FILENAME)):
+            write_xillver_cp_table(os.path.join(outdir, XILLTABLE_CP_FILENAME), seed=seed)
         with open(stamp, "w") as fh:
             fh.write("ok\n")
     return outdir

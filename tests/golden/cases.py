@@ -49,6 +49,21 @@ CASES = [
     ("relxilllp_rr_pl", "relxilllp", [10, 0, 0.9, 45, -1, 400, 0, 2.0, 3.1, 1, 300, 1, 1, 0], GRID_WIDE, 1, 0.5),
     ("rellinelp_rr", "relline_lp", [6.4, 6, 0.998, 30, -1, 400, 0, 0, 2.0, 1], GRID_LINE, 0, 0.0),
     ("relconvlp_rr", "relconv_lp", [6, 0.0, 0.7, 30, -1, 400, 0, 2.0, 1], GRID_CONV, 0, 0.0),
+    # Cp flavour: nthcomp continuum, 6-parameter xillverCp table (lmodel_relxill_public.dat:86-129)
+    ("xillvercp_a", "xillverCp", [2.0, 1.0, 60, 3.1, 15, 0, 30, -1], GRID_WIDE, 0, 0.0),
+    ("xillvercp_b", "xillverCp", [1.7, 3.0, 25, 1.5, 17.0, 0.05, 60, 2.0], GRID_WIDE, 0, 0.0),
+    ("relxillcp_a", "relxillCp", [30, 0.998, -1, 400, 15, 3, 3, 0, 2.0, 3.1, 15, 1, 60, 3], GRID_WIDE, 0, 0.0),
+    ("relxillcp_b", "relxillCp", [60, 0.5, -2, 300, 10, 4, 2.5, 0.1, 1.8, 2.0, 18, 2.0, 100, -1], GRID_WIDE, 0, 0.0),
+    ("relxilllpcp_a", "relxilllpCp", [30, 0.998, -1, 400, 6, 0, 2.0, 3.1, 15, 1, 60, 1, 0, 0, 0, 0, 0], GRID_WIDE,
+     0, 0.0),
+    # returning radiation with its corrections and the reflection-fraction boost
+    ("relxilllpcp_rr", "relxilllpCp", [45, 0.9, -1, 400, 10, 0.2, 2.4, 2.0, 16, 3, 30, 2, 0, 0, 0, 1, 1], GRID_WIDE,
+     0, 0.0),
+    # the ionisation gradient is a parameter of relxilllpCp: ALPHA and power law
+    ("relxilllpcp_alpha", "relxilllpCp", [70, 0.5, -1, 400, 5, 0, 2.2, 2.0, 15, 1, 100, 1, 0, 0.0, 2, 1, 0],
+     GRID_WIDE, 0, 0.0),
+    ("relxilllpcp_pl", "relxilllpCp", [30, 0.9, -1, 400, 10, 0, 2.0, 3.1, 15, 1, 60, 1, 0, 0.5, 1, 0, 0], GRID_WIDE,
+     0, 0.0),
 ]
 
 

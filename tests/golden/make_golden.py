@@ -18,7 +18,8 @@ sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 from relxill_gb300 import synth_tables  # noqa: E402
 from cases import CASES, CONV_MODELS, grid, conv_input  # noqa: E402
 
-MODEL_ID = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3, "relline_lp": 4, "relconv_lp": 5, "xillver": 6}
+MODEL_ID = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3, "relline_lp": 4, "relconv_lp": 5, "xillver": 6,
+            "xillverCp": 7, "relxillCp": 8, "relxilllpCp": 9}
 
 
 def main():

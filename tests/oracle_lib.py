@@ -15,7 +15,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_SO = os.path.join(ORACLE_DIR, "librelx_oracle.so")
 REF_SO = os.path.join(ORACLE_DIR, "_ref", "librelxill_ref.so")
-MODELS = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3, "relline_lp": 4, "relconv_lp": 5, "xillver": 6}
+MODELS = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3, "relline_lp": 4, "relconv_lp": 5, "xillver": 6,
+          "xillverCp": 7, "relxillCp": 8, "relxilllpCp": 9}
 _dp = ctypes.POINTER(ctypes.c_double)
 _lib = None
 
