@@ -26,7 +26,8 @@ extern "C" {
 /* model ids of the batched calls */
 enum {
   RELX_MODEL_RELLINE = 0, RELX_MODEL_RELCONV = 1, RELX_MODEL_RELXILL = 2, RELX_MODEL_RELXILLLP = 3,
-  RELX_MODEL_RELLINELP = 4, RELX_MODEL_RELCONVLP = 5, RELX_MODEL_XILLVER = 6
+  RELX_MODEL_RELLINELP = 4, RELX_MODEL_RELCONVLP = 5, RELX_MODEL_XILLVER = 6,
+  RELX_MODEL_XILLVERCP = 7, RELX_MODEL_RELXILLCP = 8, RELX_MODEL_RELXILLLPCP = 9
 };
 
 /* Local models.  Replace c_lmodrelline / c_lmodrelconv / c_lmodrelxill /
@@ -57,6 +58,19 @@ void c_lmodrelconvlp(const double *energy, int Nflux, const double *parameter, i
                      double *fluxError, const char *init);
 void c_lmodxillver(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
                    double *fluxError, const char *init);
+/* The Cp flavour (lmodel_relxill_public.dat:86,96,112): the nthcomp primary
+ * continuum (seed temperature 0.05 keV) and the 6-parameter table
+ * xillverCp_v3.4.fits.  xillverCp takes gamma, Afe, kTe, logxi, logN, z,
+ * Incl, refl_frac; relxillCp Incl, a, Rin, Rout, Rbr, Index1, Index2, z,
+ * gamma, logxi, logN, Afe, kTe, refl_frac; relxilllpCp Incl, a, Rin, Rout, h,
+ * beta, gamma, logxi, logN, Afe, kTe, refl_frac, z, iongrad_index,
+ * $iongrad_type, $switch_returnrad, $switch_reflfrac_boost. */
+void c_lmodxillverdensnthcomp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                              double *fluxError, const char *init);
+void c_lmodrelxilldensnthcomp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                              double *fluxError, const char *init);
+void c_lmodrelxilllpdensnthcomp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                                double *fluxError, const char *init);
 
 /* Status of the last call on this process (0 = success).  The reference has
  * no status channel (src/LocalModel.cpp:153-159); this replaces its printed
@@ -76,8 +90,9 @@ void relx_release(void);
 
 /* Batched evaluation with host buffers; no counterpart in the reference,
  * which evaluates one parameter set per call.
- * params: n_sets x npar (npar = 10, 8, 13, 14, 10, 9, 7 for relline, relconv,
- *   relxill, relxilllp, relline_lp, relconv_lp, xillver; lmodel.dat order);
+ * params: n_sets x npar (npar = 10, 8, 13, 14, 10, 9, 7, 8, 14, 17 for relline,
+ *   relconv, relxill, relxilllp, relline_lp, relconv_lp, xillver, xillverCp,
+ *   relxillCp, relxilllpCp; lmodel.dat order);
  * energy: concatenated bin edges; set i uses energy[energy_offsets[i] ..
  *   energy_offsets[i+1]-1] (n_i + 1 edges);
  * flux: concatenated outputs, set i at flux[energy_offsets[i] - i .. + n_i - 1];
@@ -94,7 +109,10 @@ int relx_eval_batch(int model, int n_sets, const double *params, const double *e
 /* Same with device buffers, asynchronous on `stream` (a cudaStream_t; NULL:
  * the library's stream).  flux_in (relconv) uses the energy-edge layout
  * (set i at energy_offsets[i]).  h_energy_offsets and h_ion_grad_type are host
- * copies used to size the launch. */
+ * copies used to size the launch; for relxilllpCp, whose ionisation-gradient
+ * type is parameter 15, h_ion_grad_type carries those values (NULL: all 0; a
+ * set that needs more zones than the launch was sized for fails with
+ * status 9). */
 int relx_eval_batch_device(int model, int n_sets, const double *d_params, const double *d_energy,
                            const int64_t *d_energy_offsets, const int64_t *h_energy_offsets, const double *d_flux_in,
                            double *d_flux, int *d_status, const int *d_ion_grad_type, const int *h_ion_grad_type,

@@ -23,7 +23,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "librelxill_gb300.so")
 
 MODELS: Dict[str, int] = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3, "relline_lp": 4,
-                          "relconv_lp": 5, "xillver": 6}
+                          "relconv_lp": 5, "xillver": 6, "xillverCp": 7, "relxillCp": 8, "relxilllpCp": 9}
 CONV_MODELS = ("relconv", "relconv_lp")  # models that take the caller's spectrum in `flux`
 
 # parameter names and defaults of lmodel_relxill_public.dat:1-84 (in order)
@@ -44,10 +44,20 @@ PARAMS: Dict[str, List[Tuple[str, float]]] = {
                    ("limb", 0.0), ("gamma", 2.0), ("switch_returnrad", 1.0)],
     "xillver": [("gamma", 2.0), ("Afe", 1.0), ("Ecut", 300.0), ("logxi", 3.1), ("z", 0.0), ("Incl", 30.0),
                 ("refl_frac", -1.0)],
+    "xillverCp": [("gamma", 2.0), ("Afe", 1.0), ("kTe", 60.0), ("logxi", 3.1), ("logN", 15.0), ("z", 0.0),
+                  ("Incl", 30.0), ("refl_frac", -1.0)],
+    "relxillCp": [("Incl", 30.0), ("a", 0.998), ("Rin", -1.0), ("Rout", 400.0), ("Rbr", 15.0), ("Index1", 3.0),
+                  ("Index2", 3.0), ("z", 0.0), ("gamma", 2.0), ("logxi", 3.1), ("logN", 15.0), ("Afe", 1.0),
+                  ("kTe", 60.0), ("refl_frac", 3.0)],
+    "relxilllpCp": [("Incl", 30.0), ("a", 0.998), ("Rin", -1.0), ("Rout", 400.0), ("h", 6.0), ("beta", 0.0),
+                    ("gamma", 2.0), ("logxi", 3.1), ("logN", 15.0), ("Afe", 1.0), ("kTe", 60.0), ("refl_frac", 1.0),
+                    ("z", 0.0), ("iongrad_index", 0.0), ("iongrad_type", 0.0), ("switch_returnrad", 1.0),
+                    ("switch_reflfrac_boost", 0.0)],
 }
 LMOD_SYMBOL = {"relline": "c_lmodrelline", "relconv": "c_lmodrelconv", "relxill": "c_lmodrelxill",
                "relxilllp": "c_lmodrelxilllp", "relline_lp": "c_lmodrellinelp", "relconv_lp": "c_lmodrelconvlp",
-               "xillver": "c_lmodxillver"}
+               "xillver": "c_lmodxillver", "xillverCp": "c_lmodxillverdensnthcomp",
+               "relxillCp": "c_lmodrelxilldensnthcomp", "relxilllpCp": "c_lmodrelxilllpdensnthcomp"}
 
 STATUS = {0: "ok", 1: "parameter out of range", 2: "table inconsistent", 3: "unsupported option",
           4: "radial grid outside the table", 5: "relconv input sum <= 0", 6: "CUDA error",
@@ -227,6 +237,21 @@ def relconv_lp(energy, params, flux) -> np.ndarray:
 def xillver(energy, params) -> np.ndarray:
     """xillver photon flux per bin (c_lmodxillver)."""
     return _lmod("xillver", energy, params)
+
+
+def xillverCp(energy, params) -> np.ndarray:
+    """xillverCp photon flux per bin (c_lmodxillverdensnthcomp)."""
+    return _lmod("xillverCp", energy, params)
+
+
+def relxillCp(energy, params) -> np.ndarray:
+    """relxillCp photon flux per bin (c_lmodrelxilldensnthcomp)."""
+    return _lmod("relxillCp", energy, params)
+
+
+def relxilllpCp(energy, params) -> np.ndarray:
+    """relxilllpCp photon flux per bin (c_lmodrelxilllpdensnthcomp)."""
+    return _lmod("relxilllpCp", energy, params)
 
 
 def default_params(model: str) -> np.ndarray:

@@ -403,6 +403,7 @@ struct FinSmem {
   float spec[kN];
   double red[kFinThreads / 32 + 1];
   float nrm;
+  double nth_norm;  // nthcomp: 1 / (E F_E at the shifted 1 keV point)
 };
 
 // zone sum, primary continuum (PrimarySource.cpp:66-125), optional 3 keV
@@ -412,7 +413,8 @@ __global__ void __launch_bounds__(kFinThreads) finalize_relxill_kernel(RelxTable
                                                                         const RelxSetState *__restrict__ sst,
                                                                         const float *__restrict__ cout, int nza,
                                                                         const double *__restrict__ user_e,
-                                                                        double *__restrict__ flux) {
+                                                                        double *__restrict__ flux,
+                                                                        const NthTable *__restrict__ nth) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FinSmem &m = *reinterpret_cast<FinSmem *>(smem_raw);
   const int set = blockIdx.x, tid = threadIdx.x;
@@ -431,11 +433,21 @@ __global__ void __launch_bounds__(kFinThreads) finalize_relxill_kernel(RelxTable
   const float pnorm = (float) (s.src_norm * s.prim_fac);
   const float rfac = (float) s.norm_fac_refl;
   const bool add_prim = s.refl_frac >= 0;
+  // nthcomp primary (the Cp models): the source's E F_E table in the frame shifted by g_inf,
+  // z = 1 / g_inf - 1 (spec_nthcomp, Xillspec.cpp:243-253)
+  const bool cp = s.prim == 1;
+  const double zp1 = (1.0 / s.g_inf - 1.0) + 1.0;
+  if (cp && add_prim) {
+    if (tid == 0) m.nth_norm = nth_normfac(nth[set].x, nth[set].sp, nth[set].n, zp1);
+    __syncthreads();
+  }
   for (int k = s.out_lo + tid; k <= s.out_hi; k += kFinThreads) {
     float r = 0.0f;
     for (int z = 0; z < s.nz; z++) r += cout[((size_t) set * nza + z) * kN + k];
     r *= rfac;
-    if (add_prim) {
+    if (add_prim && cp) {
+      r += (float) nth_bin(nth[set], ce[k], ce[k + 1], zp1, m.nth_norm) * pnorm;
+    } else if (add_prim) {
       const float2 cd = tab.conv_cw[k];  // (float) bin centre, (float) bin width
       const float en = cd.x;
       float pl = expf(1.0f / ecut) * powf(en, -gam) * expf(-en / ecut) * cd.y;

@@ -101,8 +101,8 @@ static size_t carve(unsigned char *base, int model, int nza, int nbins, int ntil
 
 // RelxSetIn of the one set (energy offset 0) and the flags that must start at zero
 __global__ void noalloc_pack_kernel(int npar, const double *__restrict__ params, int n_ener, int igt, double igi,
-                                    int nzones_env, int flags, RelxSetIn *__restrict__ out, int *__restrict__ sflag,
-                                    int *__restrict__ err) {
+                                    int nzones_env, int flags, int nza, RelxSetIn *__restrict__ out,
+                                    int *__restrict__ sflag, int *__restrict__ err) {
   if (threadIdx.x != 0) return;
   RelxSetIn s;
   for (int q = 0; q < RELX_NPARAM_MAX; q++) s.p[q] = q < npar ? params[q] : 0.0;
@@ -112,6 +112,7 @@ __global__ void noalloc_pack_kernel(int npar, const double *__restrict__ params,
   s.iongrad_index = igi;
   s.nzones_env = nzones_env;
   s.flags = flags;
+  s.nza = nza;
   *out = s;
   *sflag = RELX_OK;
   *err = RELX_OK;
@@ -174,6 +175,8 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
   if (model < 0 || model >= RELX_NMODELS || !d_params || !d_energy || !d_flux || n_bins < 1)
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: bad arguments");
   const int kind = relx_kind(model);
+  if (relx_is_cp(model))
+    return fail(RELX_ERR_UNSUPPORTED, "relx_eval_one_noalloc: the Cp models are evaluated through the batched calls");
   if (kind == RELX_RELCONV && !d_flux_in)
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: relconv needs the input spectrum");
   if (ion_grad_type < 0 || ion_grad_type > 2)
@@ -205,9 +208,9 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: request exceeds the static scratch");
 
   noalloc_pack_kernel<<<1, 32, 0, s>>>(runtime_nparams(model), d_params, n_bins, ion_grad_type, iongrad_index,
-                                       nzones_env, flags, p.sin, p.sflag, p.err);
+                                       nzones_env, flags, nza, p.sin, p.sflag, p.err);
   if (kind == RELX_XILLVER) {
-    NOALLOC_CUDA(launch_xillver_model(s, tab, 1, p.sin, d_energy, p.sst, d_flux));
+    NOALLOC_CUDA(launch_xillver_model(s, tab, 1, p.sin, d_energy, p.sst, d_flux, nullptr, nullptr));
     noalloc_status_kernel<<<1, 32, 0, s>>>(p.sst, p.sflag, p.err, p.status, d_status);
     NOALLOC_CUDA(cudaGetLastError());
     runtime_set_error(RELX_OK, "");
@@ -222,7 +225,8 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
     conv_zone_kernel<<<dim3(nza, 1), kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sst, p.prof, p.tsum, ntile_max,
                                                                             kSumBinsH, p.xill, nza, p.cout,
                                                                             p.err);
-    finalize_relxill_kernel<<<1, kFinThreadsH, fin_smem_bytes(), s>>>(tab, p.sin, p.sst, p.cout, nza, d_energy, d_flux);
+    finalize_relxill_kernel<<<1, kFinThreadsH, fin_smem_bytes(), s>>>(tab, p.sin, p.sst, p.cout, nza, d_energy, d_flux,
+                                                                      nullptr);
   } else if (kind == RELX_RELCONV) {
     relconv_conv_kernel<<<1, kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sin, p.sst, p.prof, p.tsum, ntile_max,
                                                                     kSumBinsH, nza, d_energy, d_flux_in, p.cout,

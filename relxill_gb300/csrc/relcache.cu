@@ -37,6 +37,7 @@ __device__ __forceinline__ bool cache_key(const RelxSetIn &in, const RelxSetStat
   for (int q = 0; q < 8; q++) key[2 + q] = in.p[q];
   if (s.pmodel == RELX_RELXILLLP) key[10] = in.p[12];
   if (s.pmodel == RELX_RELCONVLP) key[10] = in.p[8];
+  if (s.pmodel == RELX_RELXILLLPCP) key[10] = in.p[15];  // Incl..logxi (8) and the switch (:112-129)
   return true;
 }
 

@@ -165,12 +165,14 @@ __device__ __forceinline__ float sqrt_diff(float hi, float lo) {
   return den > 0.0f ? d / den : 0.0f;
 }
 
-// g* and 1 - g* of a bin edge, clamped to [0, 1] (integ_relline_bin, Relprofile.cpp:653-666)
+// g* and 1 - g* of a bin edge, clamped to [0, 1] (integ_relline_bin, Relprofile.cpp:653-666).
+// The side of gmin and gmax is taken from the signs of the float-float differences: the two
+// rounded quotients alone can give g <= 1 with 1 - g < 0 for an edge just above gmax.
 __device__ __forceinline__ float2 edge_gc(float2 E, const RadC &rc) {
-  float g = ff_sub_to_float(E, rc.gmin) * rc.inv_dg;
-  float c = ff_sub_to_float(rc.gmax, E) * rc.inv_dg;
-  if (g < 0.0f) { g = 0.0f; c = 1.0f; } else if (g > 1.0f) { g = 1.0f; c = 0.0f; }
-  return make_float2(g, c);
+  const float dlo = ff_sub_to_float(E, rc.gmin), dhi = ff_sub_to_float(rc.gmax, E);
+  if (dlo <= 0.0f) return make_float2(0.0f, 1.0f);
+  if (dhi <= 0.0f) return make_float2(1.0f, 0.0f);
+  return make_float2(fminf(dlo * rc.inv_dg, 1.0f), fminf(dhi * rc.inv_dg, 1.0f));
 }
 
 // integ_relline_bin (Relprofile.cpp:650-726) with the emissivity factored out, from the clamped

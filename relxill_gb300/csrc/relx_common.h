@@ -9,10 +9,11 @@
 #define RELX_HD
 #endif
 
-// model ids (lmodel_relxill_public.dat:1,13,23,35,46,61,77)
+// model ids (lmodel_relxill_public.dat:1,13,23,35,46,61,77,86,96,112)
 enum RelxModel {
   RELX_RELLINE = 0, RELX_RELCONV = 1, RELX_RELXILL = 2, RELX_RELXILLLP = 3,
-  RELX_RELLINELP = 4, RELX_RELCONVLP = 5, RELX_XILLVER = 6, RELX_NMODELS = 7
+  RELX_RELLINELP = 4, RELX_RELCONVLP = 5, RELX_XILLVER = 6,
+  RELX_XILLVERCP = 7, RELX_RELXILLCP = 8, RELX_RELXILLLPCP = 9, RELX_NMODELS = 10
 };
 
 // The kernels work on four kinds of evaluation: a line profile (relline, relline_lp), a
@@ -20,8 +21,20 @@ enum RelxModel {
 // spectrum (relxill, relxilllp) and the non-relativistic reflection spectrum (xillver).  The
 // lamp-post line and convolution models differ from their broken-power-law twins only in the
 // emissivity (LocalModel.cpp:32-98 runs the same code for both).
+// The Cp models (relxillCp, relxilllpCp, xillverCp) are the reflection kinds with the nthcomp
+// continuum and the 6-parameter xillverCp table.
 RELX_HD inline int relx_kind(int model) {
-  return model == RELX_RELLINELP ? RELX_RELLINE : model == RELX_RELCONVLP ? RELX_RELCONV : model;
+  switch (model) {
+    case RELX_RELLINELP: return RELX_RELLINE;
+    case RELX_RELCONVLP: return RELX_RELCONV;
+    case RELX_XILLVERCP: return RELX_XILLVER;
+    case RELX_RELXILLCP: return RELX_RELXILL;
+    case RELX_RELXILLLPCP: return RELX_RELXILLLP;
+    default: return model;
+  }
+}
+RELX_HD inline bool relx_is_cp(int model) {
+  return model == RELX_XILLVERCP || model == RELX_RELXILLCP || model == RELX_RELXILLLPCP;
 }
 RELX_HD inline bool relx_is_relxill(int kind) { return kind == RELX_RELXILL || kind == RELX_RELXILLLP; }
 
@@ -64,7 +77,7 @@ enum RelxStatus {
 #define RELX_MAX_XPAR 8
 #define RELX_ZDENSE 16            // zones handled with the de-duplicated xillver corner list
 #define RELX_MAX_UCORNER 256      // 16 corners x RELX_ZDENSE zones
-#define RELX_NPARAM_MAX 16
+#define RELX_NPARAM_MAX 18
 
 // returning-radiation table (common.h:127-129)
 #define RELX_RR_NR 50
@@ -133,12 +146,14 @@ struct RelxSetIn {
   double iongrad_index;
   int nzones_env;    // RELXILL_NUM_RZONES value or 0
   int flags;         // bit0 RELLINE_PHYSICAL_NORM, bit1 RELXILL_RENORMALIZE, bit2 RELXILL_CONSTANT_DENSITY
+  int nza;           // zones the batch's per-set arrays hold (a set needing more fails)
 };
 
 // per-set state written by the setup kernel
 struct RelxSetState {
   int status, model, emis_type, limb, nz, ion_grad_type, boost_switch;
   int pmodel;       // the caller's model id (model holds its kind, relx_kind)
+  int prim;         // primary continuum: 0 cut-off power law, 1 nthcomp (Cp models)
   int rr_corr;      // returning radiation with xillver correction factors (line profile not cacheable)
   int cached;       // line profile, tile sums and angle histograms come from the profile cache
   int g_n;          // bins of the line-profile grid (user grid for relline, conv grid otherwise)
@@ -155,6 +170,15 @@ struct RelxSetState {
   int zi0[RELX_NZMAX], zi1[RELX_NZMAX];   // fine-radius index range of each zone (inclusive)
   int zw_lo[RELX_NZMAX], zw_hi[RELX_NZMAX]; // line-profile bins touched by the zone's radii [lo, hi)
   float inv_nc[RELX_NZMAX];               // 1 / normalisation change source->disk (Xillspec.cpp:408-440)
+  double zshift[RELX_NZMAX];              // energy shift source -> disk of each zone (Ecut / kTe factor)
+};
+
+// nthcomp (nthcomp.cu): E F_E table of a set's source continuum, x[1..n+1] and sp[1..n]
+struct NthTable {
+  double x[901];
+  double sp[901];
+  int n;
+  int pad_[3];
 };
 
 // per-radius record of the line-profile kernels (64 bytes, staged into shared memory as int4 rows)
@@ -188,6 +212,6 @@ struct RelxCorners {
 
 // per-zone corners (used when nz > RELX_ZDENSE)
 struct RelxZoneCorners {
-  int row[RELX_NZMAX][16];
-  float w[RELX_NZMAX][16];
+  int row[RELX_NZMAX][32];   // 16 corners for a 5-parameter table, 32 for the 6-parameter one
+  float w[RELX_NZMAX][32];
 };

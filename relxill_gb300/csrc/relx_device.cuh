@@ -276,4 +276,37 @@ __device__ __forceinline__ double primary_qsum_warp(const RelxTables &tab, float
   return ff_to_double(part) * 1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi);
 }
 
+// E F_E of the table interpolated at photon energy e [keV] in the frame shifted by 1 + z, from the
+// first grid point at or above it (c_donthcomp's walk, donthcomp.c:770-787)
+__device__ __forceinline__ double nth_prim_at(const double *x, const double *sp, int nth, double e, double zp1) {
+  const double t = e * zp1;
+  int lo = 1, hi = nth + 1;  // first j in [1, nth] with x[j] * 511 >= t, nth + 1 if none
+  while (lo < hi) {
+    const int k = (lo + hi) >> 1;
+    if (x[k] * 511. < t) lo = k + 1; else hi = k;
+  }
+  const int j = lo;
+  if (j > nth) return 0.0;
+  if (j == 1) return sp[1];
+  const int jl = j - 1;
+  return sp[jl] + (e / 511. * zp1 - x[jl]) * (sp[jl + 1] - sp[jl]) / (x[jl + 1] - x[jl]);
+}
+
+// 1 / f_spp(1 / xn): the table's E F_E at xn = (1 + z) / 511 (donthcomp.c:617-638, 754-758)
+__device__ __forceinline__ double nth_normfac(const double *x, const double *sp, int nth, double zp1) {
+  const double xn = zp1 / 511.;
+  const double xx = 1 / (1 / xn);
+  int ih = 2;
+  while (ih < nth && xx > x[ih]) ++ih;
+  const int il = ih - 1;
+  return 1 / (sp[il] + (sp[ih] - sp[il]) * (xx - x[il]) / (x[ih] - x[il]));
+}
+
+// photon flux of the nthcomp table on the bin [e0, e1] in the frame shifted by zp1 = 1 + z
+// (c_donthcomp's last loop, donthcomp.c:788-792); normfac from nth_normfac at the same shift
+__device__ __forceinline__ double nth_bin(const NthTable &T, double e0, double e1, double zp1, double normfac) {
+  const double p0 = nth_prim_at(T.x, T.sp, T.n, e0, zp1), p1 = nth_prim_at(T.x, T.sp, T.n, e1, zp1);
+  return (p1 / (e1 * e1) + p0 / (e0 * e0)) * .5 * (e1 - e0) * normfac;
+}
+
 }  // namespace relx

@@ -46,6 +46,9 @@ struct XillIngest {
   const double *lxi_div;    // 10^logXi per logXi grid value
   int64_t stride_lxi;       // row-index stride of the logXi parameter
   int n_lxi;                // logXi grid values (0: no logXi parameter)
+  const double *dns_div;    // 10^(logN - 15) per density grid value (1 where logN = 15)
+  int64_t stride_dns;       // row-index stride of the density parameter
+  int n_dns;                // density grid values (0: no density parameter)
   const double *xe;         // xillver energy edges [ne + 1]
   const double *pfz_coef;   // photon flux of the spectrum shifted by g = 2/3, per energy
   float *spec;              // [rows][pad] output
@@ -56,19 +59,32 @@ cudaError_t launch_xill_ingest(cudaStream_t s, const XillIngest &g, const unsign
 cudaError_t launch_xill_corner_flux(cudaStream_t s, const double *rowflux, const double *incl_w, int n_incl,
                                     int64_t n_corners, double *fcorr);
 
+size_t nthcomp_smem_bytes();
+cudaError_t nthcomp_set_smem();
+// per set: the normalisation (calcNormWrtXillverTableSpec) of the source continuum (q[set][0]) and of
+// every zone's (q[set][z + 1]), q holding RELX_NZMAX + 1 values per set, and the source's table;
+// then the zones' normalisation changes on their corner weights (zcor) and the source normalisation.
+// params: the xillver model, Gamma and kTe from the parameters, the source continuum only.
+cudaError_t launch_nthcomp(cudaStream_t s, const RelxTables &tab, const RelxSetIn *sin, RelxSetState *sst, int n_sets,
+                           int nza, bool params, double *q, NthTable *tabs, RelxZoneCorners *zcor);
+
 // the xillver model: one CTA per set, writes the flux and the status fields of the set state
 size_t xillver_model_smem_bytes(int n_ener, int n_ener_pad);
 cudaError_t xillver_model_set_smem(int n_ener, int n_ener_pad);
+// xillverCp: nthq / nth from launch_nthcomp (params mode); null for xillver
 cudaError_t launch_xillver_model(cudaStream_t s, const RelxTables &tab, int n_sets, const RelxSetIn *sin,
-                                 const double *user_e, RelxSetState *sst, double *flux);
+                                 const double *user_e, RelxSetState *sst, double *flux, const double *nthq,
+                                 const NthTable *nth);
 
 __global__ void conv_zone_kernel(RelxTables tab, const RelxSetState *sst, const float *prof, const double *tsum,
                                  int ntile_max, int tile_bins, const float *xill, int nza, float *cout, int *err);
 __global__ void relconv_conv_kernel(RelxTables tab, const RelxSetIn *sin, const RelxSetState *sst, const float *prof,
                                     const double *tsum, int ntile_max, int tile_bins, int nza, const double *user_e,
                                     const double *user_f, float *cout, int *sflag);
+// nth: the nthcomp tables of the sets (Cp models), or null
 __global__ void finalize_relxill_kernel(RelxTables tab, const RelxSetIn *sin, const RelxSetState *sst,
-                                        const float *cout, int nza, const double *user_e, double *flux);
+                                        const float *cout, int nza, const double *user_e, double *flux,
+                                        const NthTable *nth);
 __global__ void finalize_relconv_kernel(RelxTables tab, const RelxSetIn *sin, const RelxSetState *sst,
                                         const float *cout, int nza, const double *user_e, const int *sflag,
                                         double *flux);

@@ -103,17 +103,27 @@ struct Tables {
   RelxTables d{};
   DevBuf rel_a, rel_mu0, rel_r, rel_gmin, rel_gmax, rel_tc;
   DevBuf lp_a, lp_h, lp_rad, lp_intens, lp_del, lp_delinc;
-  DevBuf x_vals, x_spec, x_e, x_ew, x_fcorr;
+  // one xillver table: the standard one (x) and the nthcomp one of the Cp models (xcp)
+  struct XillBufs {
+    DevBuf vals, spec, e, ew, fcorr, rb_imin, rb_imax, rb_fmin, rb_fmax, rb_pack;
+    void release() {
+      for (DevBuf *b : {&vals, &spec, &e, &ew, &fcorr, &rb_imin, &rb_imax, &rb_fmin, &rb_fmax, &rb_pack}) b->release();
+    }
+  } x, xcp;
+  RelxTables dcp{};     // d with the xillver fields of the nthcomp table (valid if has_cp)
+  bool has_cp = false;
   DevBuf rr_spin, rr_rlo, rr_rhi, rr_tfr, rr_g;
   DevBuf conv_e, conv_eff, conv_inv_emid, conv_cf, conv_cw, coarse_e, coarse_t;
-  DevBuf rb_imin, rb_imax, rb_fmin, rb_fmax, rb_pack;
   size_t bytes_total = 0;
   bool loaded = false;
   void release() {
     for (DevBuf *b : {&rel_a, &rel_mu0, &rel_r, &rel_gmin, &rel_gmax, &rel_tc, &lp_a, &lp_h, &lp_rad, &lp_intens,
-                      &lp_del, &lp_delinc, &x_vals, &x_spec, &x_e, &x_ew, &x_fcorr, &rr_spin, &rr_rlo, &rr_rhi, &rr_tfr, &rr_g, &conv_e, &conv_eff, &conv_inv_emid, &conv_cf,
-                      &conv_cw, &coarse_e, &coarse_t, &rb_imin, &rb_imax, &rb_fmin, &rb_fmax, &rb_pack})
+                      &lp_del, &lp_delinc, &rr_spin, &rr_rlo, &rr_rhi, &rr_tfr, &rr_g, &conv_e, &conv_eff, &conv_inv_emid, &conv_cf,
+                      &conv_cw, &coarse_e, &coarse_t})
       b->release();
+    x.release();
+    xcp.release();
+    has_cp = false;
     loaded = false;
   }
 };
@@ -221,14 +231,24 @@ constexpr double kPiHost = 3.14159265358979323846;
 static const char *kXillNames[] = {"Gamma", "A_Fe", "logXi", "Ecut", "kTe", "Dens", "kTbb", "A_CO", "Frac", "Incl"};
 static const int kXillIndex[] = {0, 1, 2, 3, 3, 4, 5, 1, 6, 7};  // common.h:141-150, xilltable.c:24-27
 
-static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &xe_host) {
+// A xillver table (init_xillver_table, xilltable.c:169-276, 410-447): 5 parameters, or 6 for the
+// nthcomp table of the Cp models (xillverCp_v3.4.fits, common.h:166), Incl last.  X receives the
+// device buffers, d its x_* fields.  missing_ok: an absent file is not an error (*present = false).
+static int load_xillver(const std::string &dir, const char *fname, Tables &T, Tables::XillBufs &X, RelxTables &d,
+                        std::vector<double> &xe_host, bool missing_ok, bool *present) {
   FitsFile f;
   std::string err;
-  if (!f.open(dir + "/xillver-a-Ec5.fits", &err)) { g_errmsg = err; return RELX_ERR_NOTABLE; }
+  if (present) *present = false;
+  if (!f.open(dir + "/" + fname, &err)) {
+    if (missing_ok) return 0;
+    g_errmsg = err;
+    return RELX_ERR_NOTABLE;
+  }
+  if (present) *present = true;
   const FitsHdu *hp = f.find("PARAMETERS"), *he = f.find("ENERGIES"), *hs = f.find("SPECTRA");
   if (!hp || !he || !hs) { g_errmsg = "xillver table: missing extensions"; return RELX_ERR_TABLE; }
   int npar = (int) hp->nrows;
-  if (npar != 5) { g_errmsg = "xillver table: only 5-parameter tables are supported"; return RELX_ERR_TABLE; }
+  if (npar != 5 && npar != 6) { g_errmsg = "xillver table: 5 or 6 parameters expected"; return RELX_ERR_TABLE; }
   std::vector<std::string> names;
   std::vector<double> nv(npar);
   f.read_str(*hp, 0, 0, npar, &names);
@@ -238,14 +258,14 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
   f.read_f32(*hp, 9, 0, npar, vals.data());
   int pidx[RELX_MAX_XPAR];
   int nvals[RELX_MAX_XPAR];
-  int has_dens = 0, q_lxi = -1;
+  int has_dens = 0, q_lxi = -1, q_dns = -1;
   for (int q = 0; q < npar; q++) {
     nvals[q] = (int) nv[q];
     pidx[q] = -1;
     for (int j = 0; j < 10; j++)
       if (names[q] == kXillNames[j]) pidx[q] = kXillIndex[j];
     if (pidx[q] < 0) { g_errmsg = "xillver table: unknown parameter " + names[q]; return RELX_ERR_TABLE; }
-    if (pidx[q] == 4) has_dens = 1;
+    if (pidx[q] == 4) { has_dens = 1; q_dns = q; }
     if (pidx[q] == 2) q_lxi = q;
   }
   if (pidx[npar - 1] != 7) { g_errmsg = "xillver table: Incl must be the last parameter"; return RELX_ERR_TABLE; }
@@ -293,9 +313,10 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
     }
   }
   // strides of the row index (incl fastest, xilltable.c:325-337)
-  int64_t stride_lxi = 1;
+  int64_t stride_lxi = 1, stride_dns = 1;
   for (int q = npar - 1; q > q_lxi; q--) stride_lxi *= nvals[q];
-  int st = T.x_spec.reserve(sizeof(float) * (size_t) rows * pad);
+  for (int q = npar - 1; q > q_dns; q--) stride_dns *= nvals[q];
+  int st = X.spec.reserve(sizeof(float) * (size_t) rows * pad);
   if (st) return st;
   const int ni = nvals[npar - 1];
   std::vector<double> xe = xe_host;
@@ -305,21 +326,28 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
   // weights of the corner average (calc_angle_averaged_xill_spec, Xillspec.cpp:109-127: the
   // reference weights inclination i by norm_factor_semi_infinite_slab(incl_i * 180 / pi) / n_incl
   // with incl_i the table value in degrees; restated as it is)
-  std::vector<double> lxi_div(q_lxi >= 0 ? nvals[q_lxi] : 1, 1.0), incl_w(ni);
+  // a table with a density parameter also divides by 10^(logN - 15) of the row (renorm_xill_spec)
+  std::vector<double> lxi_div(q_lxi >= 0 ? nvals[q_lxi] : 1, 1.0), dns_div(q_dns >= 0 ? nvals[q_dns] : 1, 1.0),
+      incl_w(ni);
   if (q_lxi >= 0)
     for (int k = 0; k < nvals[q_lxi]; k++) lxi_div[k] = std::pow(10, (double) vals[(size_t) q_lxi * maxv + k]);
+  if (q_dns >= 0)
+    for (int k = 0; k < nvals[q_dns]; k++) {
+      const double dn = (double) vals[(size_t) q_dns * maxv + k];
+      if (std::fabs(dn - 15) > 1e-6) dns_div[k] = std::pow(10, dn - 15);
+    }
   for (int i = 0; i < ni; i++) {
     const double incl_deg = (double) vals[(size_t) (npar - 1) * maxv + i] * 180 / kPiHost;
     incl_w[i] = 0.5 * std::cos(incl_deg * kPiHost / 180) / ni;
   }
-  if ((st = upload(T.x_vals, vals)) || (st = upload(T.x_e, xe)) || (st = upload(T.x_ew, xew)) ||
-      (st = T.x_fcorr.reserve(sizeof(double) * 3 * (size_t) (rows / ni))))
+  if ((st = upload(X.vals, vals)) || (st = upload(X.e, xe)) || (st = upload(X.ew, xew)) ||
+      (st = X.fcorr.reserve(sizeof(double) * 3 * (size_t) (rows / ni))))
     return st;
   // decode on the GPU (table_ingest.cu): raw rows read in chunks into two pinned buffers, so that
   // the file read of one chunk overlaps the copy and decoding of the previous one
   const int64_t chunk = 4096;
   const size_t chunk_bytes = (size_t) chunk * hs->width;
-  DevBuf d_raw[2], d_rowflux, d_div, d_pfz, d_inclw, d_bad;
+  DevBuf d_raw[2], d_rowflux, d_div, d_dns, d_pfz, d_inclw, d_bad;
   Pinned h_raw[2];
   cudaStream_t stream = nullptr;
   cudaEvent_t done[2] = {nullptr, nullptr};
@@ -332,6 +360,7 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
     for (auto &b : h_raw) b.release();
     d_rowflux.release();
     d_div.release();
+    d_dns.release();
     d_pfz.release();
     d_inclw.release();
     d_bad.release();
@@ -340,6 +369,7 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
   if ((rc = d_raw[0].reserve(chunk_bytes)) || (rc = d_raw[1].reserve(chunk_bytes)) ||
       (rc = h_raw[0].reserve(chunk_bytes)) || (rc = h_raw[1].reserve(chunk_bytes)) ||
       (rc = d_rowflux.reserve(sizeof(double) * 3 * (size_t) rows)) || (rc = upload(d_div, lxi_div)) ||
+      (rc = upload(d_dns, dns_div)) ||
       (rc = upload(d_pfz, pfz_coef)) || (rc = upload(d_inclw, incl_w)) || (rc = d_bad.reserve(8))) {
     cleanup();
     return rc;
@@ -352,9 +382,12 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
   g.lxi_div = d_div.as<double>();
   g.stride_lxi = stride_lxi;
   g.n_lxi = q_lxi >= 0 ? nvals[q_lxi] : 0;
-  g.xe = T.x_e.as<double>();
+  g.dns_div = d_dns.as<double>();
+  g.stride_dns = stride_dns;
+  g.n_dns = q_dns >= 0 ? nvals[q_dns] : 0;
+  g.xe = X.e.as<double>();
   g.pfz_coef = d_pfz.as<double>();
-  g.spec = T.x_spec.as<float>();
+  g.spec = X.spec.as<float>();
   g.rowflux = d_rowflux.as<double>();
   g.bad = d_bad.as<unsigned long long>();
   cudaError_t ce = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
@@ -376,7 +409,7 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
     ce = cudaEventRecord(done[b], stream);
   }
   if (ce == cudaSuccess)
-    ce = launch_xill_corner_flux(stream, g.rowflux, d_inclw.as<double>(), ni, rows / ni, T.x_fcorr.as<double>());
+    ce = launch_xill_corner_flux(stream, g.rowflux, d_inclw.as<double>(), ni, rows / ni, X.fcorr.as<double>());
   unsigned long long nbad = 0;
   if (ce == cudaSuccess) ce = cudaMemcpyAsync(&nbad, g.bad, 8, cudaMemcpyDeviceToHost, stream);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
@@ -389,16 +422,16 @@ static int load_xillver(const std::string &dir, Tables &T, std::vector<double> &
     g_errmsg = "xillver table: " + std::to_string(nbad) + " spectrum values are not finite";
     return RELX_ERR_TABLE;
   }
-  T.d.x_npar = npar; T.d.x_nener = ne; T.d.x_nener_pad = pad; T.d.x_nincl = nvals[npar - 1];
-  for (int q = 0; q < RELX_MAX_XPAR; q++) { T.d.x_nvals[q] = q < npar ? nvals[q] : 0; T.d.x_pindex[q] = q < npar ? pidx[q] : -1; }
-  T.d.x_has_dens = has_dens;
-  T.d.x_vals = T.x_vals.as<float>();
-  T.d.x_maxvals = maxv;
-  T.d.x_spec = T.x_spec.as<float>();
-  T.d.x_rows = rows;
-  T.d.x_e = T.x_e.as<double>();
-  T.d.x_ew = T.x_ew.as<float2>();
-  T.d.x_fcorr = T.x_fcorr.as<double>();
+  d.x_npar = npar; d.x_nener = ne; d.x_nener_pad = pad; d.x_nincl = nvals[npar - 1];
+  for (int q = 0; q < RELX_MAX_XPAR; q++) { d.x_nvals[q] = q < npar ? nvals[q] : 0; d.x_pindex[q] = q < npar ? pidx[q] : -1; }
+  d.x_has_dens = has_dens;
+  d.x_vals = X.vals.as<float>();
+  d.x_maxvals = maxv;
+  d.x_spec = X.spec.as<float>();
+  d.x_rows = rows;
+  d.x_e = X.e.as<double>();
+  d.x_ew = X.ew.as<float2>();
+  d.x_fcorr = X.fcorr.as<double>();
   T.bytes_total += (size_t) rows * pad * 4;
   return 0;
 }
@@ -499,9 +532,12 @@ static int load_tables(const std::string &dir, Tables &T) {
   T.release();
   T.d = RelxTables{};
   T.bytes_total = 0;
-  std::vector<double> xe;
+  std::vector<double> xe, xe_cp;
   int st;
-  if ((st = load_relline(dir, T)) || (st = load_lp(dir, T)) || (st = load_xillver(dir, T, xe)) ||
+  bool has_cp = false;
+  if ((st = load_relline(dir, T)) || (st = load_lp(dir, T)) ||
+      (st = load_xillver(dir, "xillver-a-Ec5.fits", T, T.x, T.d, xe, false, nullptr)) ||
+      (st = load_xillver(dir, "xillverCp_v3.4.fits", T, T.xcp, T.dcp, xe_cp, true, &has_cp)) ||
       (st = load_rrad(dir, T)))
     return st;
   // conv grid (get_relxill_conv_energy_grid, Xillspec.cpp:44-54) and derived arrays
@@ -547,19 +583,33 @@ static int load_tables(const std::string &dir, Tables &T) {
     const float hi = (float) em;
     ct[b] = make_float4(hi, (float) (co[b + 1] - co[b]), in_band ? hi : 0.0f, in_band ? (float) (em - (double) hi) : 0.0f);
   }
-  std::vector<int> imn, imx;
-  std::vector<float> fmn, fmx;
-  rebin_map(ce, xe, imn, imx, fmn, fmx);
-  std::vector<int4> rbp(imn.size());
-  for (size_t j = 0; j < imn.size(); j++) {
-    int fa, fb;
-    std::memcpy(&fa, &fmn[j], 4);
-    std::memcpy(&fb, &fmx[j], 4);
-    rbp[j] = make_int4(imn[j], imx[j], fa, fb);
-  }
+  // rebin map xillver grid -> conv grid, per xillver table
+  auto rebin_tables = [&](const std::vector<double> &xg, Tables::XillBufs &X, RelxTables &d) {
+    std::vector<int> imn, imx;
+    std::vector<float> fmn, fmx;
+    rebin_map(ce, xg, imn, imx, fmn, fmx);
+    std::vector<int4> rbp(imn.size());
+    for (size_t j = 0; j < imn.size(); j++) {
+      int fa, fb;
+      std::memcpy(&fa, &fmn[j], 4);
+      std::memcpy(&fb, &fmx[j], 4);
+      rbp[j] = make_int4(imn[j], imx[j], fa, fb);
+    }
+    int r;
+    if ((r = upload(X.rb_imin, imn)) || (r = upload(X.rb_imax, imx)) || (r = upload(X.rb_fmin, fmn)) ||
+        (r = upload(X.rb_fmax, fmx)) || (r = upload(X.rb_pack, rbp)))
+      return r;
+    d.rb_imin = X.rb_imin.as<int>();
+    d.rb_imax = X.rb_imax.as<int>();
+    d.rb_fmin = X.rb_fmin.as<float>();
+    d.rb_fmax = X.rb_fmax.as<float>();
+    d.rb_pack = X.rb_pack.as<int4>();
+    return 0;
+  };
+  if ((st = rebin_tables(xe, T.x, T.d)) || (has_cp && (st = rebin_tables(xe_cp, T.xcp, T.dcp)))) return st;
   if ((st = upload(T.conv_e, ce)) || (st = upload(T.conv_eff, ceff)) || (st = upload(T.conv_inv_emid, inv_emid)) ||
-      (st = upload(T.conv_cf, cf)) || (st = upload(T.conv_cw, cw)) || (st = upload(T.coarse_e, co)) || (st = upload(T.coarse_t, ct)) || (st = upload(T.rb_imin, imn)) ||
-      (st = upload(T.rb_imax, imx)) || (st = upload(T.rb_fmin, fmn)) || (st = upload(T.rb_fmax, fmx)) || (st = upload(T.rb_pack, rbp)))
+      (st = upload(T.conv_cf, cf)) || (st = upload(T.conv_cw, cw)) || (st = upload(T.coarse_e, co)) ||
+      (st = upload(T.coarse_t, ct)))
     return st;
   T.d.conv_e = T.conv_e.as<double>();
   T.d.conv_eff = T.conv_eff.as<float2>();
@@ -573,11 +623,24 @@ static int load_tables(const std::string &dir, Tables &T) {
   T.d.conv_band_hi = band_hi;
   T.d.coarse_e = T.coarse_e.as<double>();
   T.d.coarse_t = T.coarse_t.as<float4>();
-  T.d.rb_imin = T.rb_imin.as<int>();
-  T.d.rb_imax = T.rb_imax.as<int>();
-  T.d.rb_fmin = T.rb_fmin.as<float>();
-  T.d.rb_fmax = T.rb_fmax.as<float>();
-  T.d.rb_pack = T.rb_pack.as<int4>();
+  // the nthcomp descriptor: everything of d but the xillver fields
+  if (has_cp) {
+    RelxTables c = T.d;
+    const RelxTables &x = T.dcp;
+    c.x_npar = x.x_npar; c.x_nener = x.x_nener; c.x_nener_pad = x.x_nener_pad; c.x_nincl = x.x_nincl;
+    for (int q = 0; q < RELX_MAX_XPAR; q++) { c.x_nvals[q] = x.x_nvals[q]; c.x_pindex[q] = x.x_pindex[q]; }
+    c.x_has_dens = x.x_has_dens;
+    c.x_vals = x.x_vals;
+    c.x_maxvals = x.x_maxvals;
+    c.x_spec = x.x_spec;
+    c.x_rows = x.x_rows;
+    c.x_e = x.x_e;
+    c.x_ew = x.x_ew;
+    c.x_fcorr = x.x_fcorr;
+    c.rb_imin = x.rb_imin; c.rb_imax = x.rb_imax; c.rb_fmin = x.rb_fmin; c.rb_fmax = x.rb_fmax; c.rb_pack = x.rb_pack;
+    T.dcp = c;
+  }
+  T.has_cp = has_cp;
   T.loaded = true;
   return 0;
 }
@@ -594,6 +657,9 @@ static int model_nparams(int model) {
     case RELX_RELLINELP: return 10; // :23-33
     case RELX_RELCONVLP: return 9;  // :35-44
     case RELX_XILLVER: return 7;    // :77-84
+    case RELX_XILLVERCP: return 8;  // :86-94
+    case RELX_RELXILLCP: return 14; // :96-110
+    case RELX_RELXILLLPCP: return 17;  // :112-129
     default: return -1;
   }
 }
@@ -616,18 +682,20 @@ static EnvOpts read_env() {
 
 // number of zones a set will use (get_num_zones, relutility.c:506-544)
 static int zones_for(int model, int ion_grad_type, int envn) {
-  if (model == RELX_XILLVER) return 1;
+  const int kind = relx_kind(model);
+  if (kind == RELX_XILLVER) return 1;
   if (ion_grad_type != 0) return (envn > 9 && envn <= RELX_NZMAX) ? envn : RELX_NZONES_IONGRAD;
-  if (model == RELX_RELXILLLP) return (envn > 0 && envn <= RELX_NZMAX) ? envn : RELX_NZONES;
+  if (kind == RELX_RELXILLLP) return (envn > 0 && envn <= RELX_NZMAX) ? envn : RELX_NZONES;
   return 1;
 }
 
 struct Workspace {
   DevBuf setin, st, rad, corners, zcorners, line_e, prof, dist, tsum, xill, cout, user_e, user_f, flux, sflag,
-      status, err, params, eoff, igt, igi, order, cslot;
+      status, err, params, eoff, igt, igi, order, cslot, nthq, nthtab;
   void release() {
     for (DevBuf *b : {&setin, &st, &rad, &corners, &zcorners, &line_e, &prof, &dist, &tsum, &xill, &cout, &user_e,
-                      &user_f, &flux, &sflag, &status, &err, &params, &eoff, &igt, &igi, &order, &cslot})
+                      &user_f, &flux, &sflag, &status, &err, &params, &eoff, &igt, &igi, &order, &cslot, &nthq,
+                      &nthtab})
       b->release();
   }
 };
@@ -678,6 +746,8 @@ static int set_kernel_attrs(const Tables &T) {
   RELX_CUDA(relline_set_smem(T.d.rel_nr, T.d.rel_ng));
   RELX_CUDA(xillver_set_smem(T.d.x_nincl));
   RELX_CUDA(xillver_model_set_smem(T.d.x_nener, T.d.x_nener_pad));
+  if (T.has_cp) RELX_CUDA(xillver_model_set_smem(T.dcp.x_nener, T.dcp.x_nener_pad));
+  RELX_CUDA(nthcomp_set_smem());
   RELX_CUDA(cudaFuncSetAttribute(conv_zone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
   RELX_CUDA(cudaFuncSetAttribute(relconv_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
   RELX_CUDA(cudaFuncSetAttribute(finalize_relxill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) fin_smem_bytes()));
@@ -706,7 +776,7 @@ static int ensure_init(Context &C, const char *path) {
 // pack (params, energy offsets) into RelxSetIn on the device
 __global__ void pack_kernel(int n_sets, int npar, const double *__restrict__ params, const int64_t *__restrict__ eoff,
                             const int *__restrict__ igt, const double *__restrict__ igi, int nzones_env, int flags,
-                            RelxSetIn *__restrict__ out) {
+                            int nza, RelxSetIn *__restrict__ out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_sets) return;
   RelxSetIn s;
@@ -717,6 +787,7 @@ __global__ void pack_kernel(int n_sets, int npar, const double *__restrict__ par
   s.iongrad_index = igi ? igi[i] : 0.0;
   s.nzones_env = nzones_env;
   s.flags = flags;
+  s.nza = nza;
   out[i] = s;
 }
 
@@ -803,6 +874,9 @@ static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b,
       (st = W.sflag.reserve(S * sizeof(int))) || (st = W.status.reserve(S * sizeof(int))) ||
       (st = W.err.reserve(sizeof(int))) || (st = W.cslot.reserve(S * sizeof(int))))
     return st;
+  if (relx_is_cp(b.model) && ((st = W.nthq.reserve(S * (RELX_NZMAX + 1) * sizeof(double))) ||
+                              (st = W.nthtab.reserve(S * sizeof(NthTable)))))
+    return st;
   if (kind == RELX_XILLVER) return 0;  // no line profile, no convolution
   if ((st = W.rad.reserve(S * sizeof(RelxRadial))) || (st = W.dist.reserve(S * nza * RELX_MAX_INCL * sizeof(float))) ||
       (st = W.tsum.reserve(S * b.nblk * nza * sizeof(double))))
@@ -818,7 +892,7 @@ static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b,
   }
   if (relx_is_relxill(kind)) {
     if ((st = W.corners.reserve(S * sizeof(RelxCorners))) || (st = W.order.reserve(S * sizeof(int))) ||
-        (st = W.xill.reserve(S * nza * (size_t) T.d.x_nener_pad * sizeof(float))))
+        (st = W.xill.reserve(S * nza * (size_t) std::max(T.d.x_nener_pad, T.dcp.x_nener_pad) * sizeof(float))))
       return st;
     if (need_zone_corners && (st = W.zcorners.reserve(S * sizeof(RelxZoneCorners)))) return st;
   }
@@ -830,7 +904,10 @@ static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b,
 // arrays are addressed from the range's first set; energy grids and fluxes keep the batch's
 // absolute offsets.  cached: use the line-profile cache (whole batches only).
 static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStream_t s, int base, int n, bool cached) {
-  const RelxTables &tab = C.T.d;
+  const bool cp = relx_is_cp(b.model);
+  const RelxTables &tab = cp ? C.T.dcp : C.T.d;  // the Cp models use the xillverCp table
+  double *nthq = cp ? W.nthq.as<double>() + (size_t) base * (RELX_NZMAX + 1) : nullptr;
+  NthTable *ntab = cp ? W.nthtab.as<NthTable>() + base : nullptr;
   const size_t nza = b.nza;
   const int kind = relx_kind(b.model);
   const bool conv_grid = kind != RELX_RELLINE;
@@ -850,7 +927,8 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   if (kind == RELX_XILLVER) {
     {
       ProfScope ps(PK_XILL, s);
-      RELX_CUDA(launch_xillver_model(s, tab, n, sin, user_e, sst, flux));
+      if (cp) RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, 1, true, nthq, ntab, nullptr));
+      RELX_CUDA(launch_xillver_model(s, tab, n, sin, user_e, sst, flux, nthq, ntab));
     }
     ProfScope ps(PK_STATUS, s);
     status_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, sst, sflag, W.err.as<int>(), W.status.as<int>() + base);
@@ -861,6 +939,8 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     ProfScope ps(PK_SETUP, s);
     setup_kernel<<<n, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, b.model, sin, user_e, W.line_e.as<double>(), sst,
                                                                rad, cor, zcor);
+    // Cp: the nthcomp continua of the source and the zones, their normalisations on the corner weights
+    if (cp) RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, b.nza, false, nthq, ntab, zcor));
   }
   if (cached) {
     ProfScope ps(PK_SETUP, s, 2);
@@ -884,9 +964,10 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   }
   if (relx_is_relxill(kind)) {
     {
-      ProfScope ps(PK_XILL, s, b.nza <= RELX_ZDENSE ? 2 : 1);
+      const bool dense = b.nza <= RELX_ZDENSE && !cp;
+      ProfScope ps(PK_XILL, s, dense ? 2 : 1);
       int *order = W.order.as<int>() + base;
-      if (b.nza <= RELX_ZDENSE) launch_xill_order(s, sst, cor, zcor, n, order);
+      if (dense) launch_xill_order(s, sst, cor, zcor, n, order);
       RELX_CUDA(launch_xillver(s, tab, n, b.nza, sst, cor, zcor, dist, xill, W.err.as<int>(), order));
     }
     {
@@ -897,7 +978,8 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     }
     {
       ProfScope ps(PK_FIN, s);
-      finalize_relxill_kernel<<<n, kFinThreadsH, fin_smem_bytes(), s>>>(tab, sin, sst, cout, b.nza, user_e, flux);
+      finalize_relxill_kernel<<<n, kFinThreadsH, fin_smem_bytes(), s>>>(tab, sin, sst, cout, b.nza, user_e, flux,
+                                                                        ntab);
     }
   } else if (kind == RELX_RELCONV) {
     ProfScope ps(PK_CONV, s, 2);  // convolution and finalize
@@ -1088,17 +1170,22 @@ static int tuned_launch(Context &C, Workspace &W, BatchShape &b, cudaStream_t s,
   return 0;  // the workspace holds the last trial's results
 }
 
+// params_host (may be null): the host parameters; relxilllpCp carries its ionisation-gradient type
+// as parameter 15 ($iongrad_type, lmodel_relxill_public.dat:126)
 static int batch_shape(int model, int n_sets, const int64_t *eoff_host, const int *igt_host, const EnvOpts &env,
-                       BatchShape *b, bool *need_zc) {
+                       BatchShape *b, bool *need_zc, const double *params_host = nullptr) {
   b->model = model;
   b->n_sets = n_sets;
   b->n_edges = eoff_host[n_sets];
   int nza = 1, maxn = 0;
+  const int npar = model_nparams(model);
   for (int i = 0; i < n_sets; i++) {
     int n = (int) (eoff_host[i + 1] - eoff_host[i] - 1);
     if (n < 1) return RELX_ERR_ARG;
     maxn = std::max(maxn, n);
-    nza = std::max(nza, zones_for(model, igt_host ? igt_host[i] : 0, env.nzones_env));
+    int igt = igt_host ? igt_host[i] : 0;
+    if (model == RELX_RELXILLLPCP && params_host) igt = (int) std::lround(params_host[(size_t) i * npar + 14]);
+    nza = std::max(nza, zones_for(model, igt, env.nzones_env));
   }
   b->nza = nza;
   b->chunk = chunk_sets();
@@ -1106,7 +1193,7 @@ static int batch_shape(int model, int n_sets, const int64_t *eoff_host, const in
   b->any_limb = (kind == RELX_RELLINE || kind == RELX_RELCONV);
   const int gmax = (kind == RELX_RELLINE) ? maxn : RELX_NCONV;
   b->nblk = (gmax + kSumBinsH - 1) / kSumBinsH;
-  *need_zc = nza > RELX_ZDENSE;
+  *need_zc = nza > RELX_ZDENSE || relx_is_cp(model);  // the 6-parameter table uses per-zone corners
   return 0;
 }
 
@@ -1119,11 +1206,15 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
   if (model < 0 || model >= RELX_NMODELS || n_sets <= 0 || !hb.params || !hb.energy || !hb.eoff) return RELX_ERR_ARG;
   const bool conv = relx_kind(model) == RELX_RELCONV;
   if (conv && !hb.flux_in) return RELX_ERR_ARG;
+  if (relx_is_cp(model) && !C.T.has_cp) {
+    g_errmsg = "xillverCp_v3.4.fits not found: the Cp models need the nthcomp xillver table";
+    return RELX_ERR_NOTABLE;
+  }
   const EnvOpts env = read_env();
   BatchShape b;
   bool need_zc = false;
   int st;
-  if ((st = batch_shape(model, n_sets, hb.eoff, hb.igt, env, &b, &need_zc))) return st;
+  if ((st = batch_shape(model, n_sets, hb.eoff, hb.igt, env, &b, &need_zc, hb.params))) return st;
   if ((st = reserve_workspace(C.T, W, b, need_zc))) return st;
   const int npar = model_nparams(model);
   const size_t pb = sizeof(double) * (size_t) n_sets * npar, eb = sizeof(double) * (size_t) b.n_edges;
@@ -1169,7 +1260,7 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
     pack_kernel<<<(n_sets + 127) / 128, 128, 0, s>>>(n_sets, npar, W.params.as<double>(), W.eoff.as<int64_t>(),
                                                      hb.igt ? W.igt.as<int>() : nullptr,
                                                      hb.igi ? W.igi.as<double>() : nullptr, env.nzones_env, env.flags,
-                                                     W.setin.as<RelxSetIn>());
+                                                     b.nza, W.setin.as<RelxSetIn>());
   }
   if ((st = tuned_launch(C, W, b, s, use_cache))) return st;
   RELX_CUDA(cudaMemcpyAsync(h + *o_flux, W.flux.p, nflux * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1261,12 +1352,15 @@ int slot_wait(BatchSlot *b, const double **flux, const int **status) {
 size_t batch_device_bytes(int model, int n_sets, int64_t n_edges, int nza) {
   const int kind = relx_kind(model);
   if (kind == RELX_XILLVER)
-    return (sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(int) * 4) * (size_t) n_sets +
+    return (sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(int) * 4 +
+            (relx_is_cp(model) ? sizeof(NthTable) + sizeof(double) * (RELX_NZMAX + 1) : 0)) *
+               (size_t) n_sets +
            sizeof(double) * 2 * (size_t) n_edges;
   size_t per_set = sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(RelxRadial) + sizeof(int) * 4 +
                    sizeof(float) * nza * RELX_MAX_INCL + sizeof(double) * (RELX_NCONV / kSumBinsH) * nza;
   if (kind != RELX_RELLINE) per_set += 2 * sizeof(float) * (size_t) nza * RELX_NCONV;
   if (relx_is_relxill(kind)) per_set += sizeof(RelxCorners) + sizeof(float) * (size_t) nza * 4096;
+  if (relx_is_cp(model)) per_set += sizeof(RelxZoneCorners) + sizeof(NthTable) + sizeof(double) * (RELX_NZMAX + 1);
   return per_set * (size_t) n_sets + sizeof(double) * 3 * (size_t) n_edges;
 }
 
@@ -1350,6 +1444,10 @@ int relx_eval_batch_device(int model, int n_sets, const double *d_params, const 
   std::lock_guard<std::mutex> lock(C.mu);
   int st = ensure_init(C, nullptr);
   if (st) return st;
+  if (relx_is_cp(model) && !C.T.has_cp) {
+    g_errmsg = "xillverCp_v3.4.fits not found: the Cp models need the nthcomp xillver table";
+    return RELX_ERR_NOTABLE;
+  }
   const EnvOpts env = read_env();
   BatchShape b;
   bool need_zc = false;
@@ -1366,7 +1464,7 @@ int relx_eval_batch_device(int model, int n_sets, const double *d_params, const 
     ProfScope ps(PK_PACK, s);
     pack_kernel<<<(n_sets + 127) / 128, 128, 0, s>>>(n_sets, model_nparams(model), d_params, d_energy_offsets,
                                                      d_ion_grad_type, d_iongrad_index, env.nzones_env, env.flags,
-                                                     W.setin.as<RelxSetIn>());
+                                                     b.nza, W.setin.as<RelxSetIn>());
   }
   if ((st = tuned_launch(C, W, b, s, true))) return st;
   RELX_CUDA(cudaMemcpyAsync(d_flux, W.flux.p, sizeof(double) * (b.n_edges - n_sets), cudaMemcpyDeviceToDevice, s));
@@ -1565,6 +1663,21 @@ void c_lmodxillver(const double *energy, int Nflux, const double *parameter, int
                    double *fluxError, const char *init) {
   (void) spectrum; (void) fluxError; (void) init;
   lmod_eval(RELX_XILLVER, energy, Nflux, parameter, flux);
+}
+void c_lmodxillverdensnthcomp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                              double *fluxError, const char *init) {
+  (void) spectrum; (void) fluxError; (void) init;
+  lmod_eval(RELX_XILLVERCP, energy, Nflux, parameter, flux);
+}
+void c_lmodrelxilldensnthcomp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                              double *fluxError, const char *init) {
+  (void) spectrum; (void) fluxError; (void) init;
+  lmod_eval(RELX_RELXILLCP, energy, Nflux, parameter, flux);
+}
+void c_lmodrelxilllpdensnthcomp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                                double *fluxError, const char *init) {
+  (void) spectrum; (void) fluxError; (void) init;
+  lmod_eval(RELX_RELXILLLPCP, energy, Nflux, parameter, flux);
 }
 
 }  // extern "C"

@@ -87,6 +87,7 @@ __device__ void map_params(int model, const RelxSetIn &in, SetupSmem &m) {
   s.status = RELX_OK;
   s.cached = 0;
   s.rr_corr = 0;
+  s.prim = relx_is_cp(model) ? 1 : 0;
   s.limb = 0;
   s.height = 0;
   s.beta = 0;
@@ -133,6 +134,23 @@ __device__ void map_params(int model, const RelxSetIn &in, SetupSmem &m) {
       m.emis1 = v[0]; m.emis2 = v[1]; m.rbr = v[2]; s.a = v[3]; s.incl = v[4] * kPi / 180;
       s.rin = v[5]; s.rout = v[6]; s.z = v[7]; s.gam = v[8]; m.lxi = v[9]; m.afe = v[10];
       s.ect_src = v[11]; s.refl_frac = v[12];
+      break;
+    case RELX_RELXILLCP:  // lmodel_relxill_public.dat:96-110
+      m.is_relxill = 1;
+      s.emis_type = RELX_EMIS_BKN;
+      s.incl = v[0] * kPi / 180; s.a = v[1]; s.rin = v[2]; s.rout = v[3]; m.rbr = v[4]; m.emis1 = v[5];
+      m.emis2 = v[6]; s.z = v[7]; s.gam = v[8]; m.lxi = v[9]; m.dens = v[10]; m.afe = v[11]; s.ect_src = v[12];
+      s.refl_frac = v[13];
+      break;
+    case RELX_RELXILLLPCP:  // lmodel_relxill_public.dat:112-129: the ionisation gradient is a parameter
+      m.is_relxill = 1;
+      s.emis_type = RELX_EMIS_LP;
+      s.incl = v[0] * kPi / 180; s.a = v[1]; s.rin = v[2]; s.rout = v[3]; s.height = v[4]; s.beta = v[5];
+      s.gam = v[6]; m.lxi = v[7]; m.dens = v[8]; m.afe = v[9]; s.ect_src = v[10]; s.refl_frac = v[11]; s.z = v[12];
+      m.iongrad_index = v[13];
+      s.ion_grad_type = (int) llround(v[14]);
+      m.return_rad = (int) llround(v[15]);
+      s.boost_switch = (int) llround(v[16]);
       break;
     case RELX_RELXILLLP:
       m.is_relxill = 1;
@@ -187,6 +205,10 @@ __device__ void map_params(int model, const RelxSetIn &in, SetupSmem &m) {
   } else {
     s.nz = 1;
   }
+  if (s.nz > in.nza) {  // the batch's per-set arrays were sized for fewer zones
+    s.status = RELX_ERR_ARG;
+    return;
+  }
   // renormalisation target (renorm_relline_profile, Relprofile.cpp:749-781; do_renorm_model, relutility.c:603-623)
   int phys = in.flags & 1;
   s.relline_norm = 1.0;
@@ -196,12 +218,13 @@ __device__ void map_params(int model, const RelxSetIn &in, SetupSmem &m) {
   } else if (phys) {
     s.relline_norm = 0.0;
   }
-  // energy shift source -> observer (Relphysics.cpp:239-255) and the source-frame Ecut (Relxill.cpp:196-200)
+  // energy shift source -> observer (Relphysics.cpp:239-255) and the source-frame Ecut (Relxill.cpp:196-200);
+  // kTe of the nthcomp continuum is already given in the source frame
   s.g_inf = 1.0;
   if (s.emis_type == RELX_EMIS_LP) {
     s.g_inf = calc_g_inf(s.height, s.a);
     if (!(s.beta < 1e-4)) s.g_inf *= doppler_factor(kPi - s.incl, s.beta);
-    s.ect_src /= s.g_inf;
+    if (s.prim == 0) s.ect_src /= s.g_inf;
   }
 }
 
@@ -793,7 +816,13 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   }
   // ---- normalisation of the primary continuum (Xillspec.cpp:179-205, 302-332, 408-440): one warp
   // per continuum (source, then every zone), float-float sums of FP32 terms times the bin centre
-  {
+  // The nthcomp continuum of the Cp models is normalised by nthcomp_kernel after this kernel
+  // (nthcomp.cu), which also applies the zones' normalisation changes to their corner weights.
+  for (int z = tid; z < nz; z += kSetupThreads) s.zshift[z] = m.shift[z];
+  if (s.prim == 1) {
+    if (tid == 0) s.src_norm = 0.0;
+    for (int z = tid; z < nz; z += kSetupThreads) m.xscale[z] = 1.0;
+  } else {
     const float gam = (float) s.gam;
     const int lane = tid & 31, warp = tid >> 5;
     for (int b = tid; b < RELX_NCOARSE; b += kSetupThreads) m.cpow[b] = powf(tab.coarse_t[b].x, -gam);
@@ -812,9 +841,30 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       m.xscale[z] = (m.shift[z] == 1.0) ? 1.0 : m.qsum[z + 1] * src_norm;  // 1 / (disk factor / source factor)
   }
   __syncthreads();
-  // ---- the 16 corners of every zone, first-zone density scaling, de-duplication
-  const int ncor = nz * 16;
   const int ni = tab.x_nincl;
+  const bool six = tab.x_npar == 6;
+  if (six) {
+    // ---- 6-parameter table (nthcomp, Cp models): 32 corners per zone, the two 16-corner blocks over
+    // parameters 1..4 at both brackets of parameter 0 (interp_6d_tab_incl, xilltable.c:999-1020), in
+    // the per-zone corner lists; the table has a density parameter, so no density division
+    if (!tab.x_has_dens && tid == 0) m.status = RELX_ERR_TABLE;
+    for (int e = tid; e < nz * 32; e += kSetupThreads) {
+      const int z = e >> 5, c = e & 31;
+      long row = 0;
+      double w = 1.0;
+      for (int q = 0; q < 5; q++) {
+        const int up = (c >> q) & 1;
+        row = row * tab.x_nvals[q] + m.zind[z][q] + up;
+        const double f = m.zfac[z][q];
+        w *= up ? f : (1.0 - f);
+      }
+      zcout[set].row[z][c] = (int) (row * ni);
+      zcout[set].w[z][c] = (float) (w * m.xscale[z]);
+    }
+    if (tid == 0) s.ucount = 0;
+  }
+  // ---- the 16 corners of every zone, first-zone density scaling, de-duplication
+  const int ncor = six ? 0 : nz * 16;
   for (int e = tid; e < ncor; e += kSetupThreads) {
     int z = e >> 4, c = e & 15;
     // corner c: bit0 -> param 0 (+1), bit1 -> param 1, bit2 -> param 2, bit3 -> param 3
@@ -870,7 +920,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   for (int e = tid; e < ncor; e += kSetupThreads)
     if (m.cfirst[e] != e) m.cuniq[e] = m.cuniq[m.cfirst[e]];  // the first entry is numbered above
   __syncthreads();
-  const bool dense = nz <= RELX_ZDENSE;
+  const bool dense = nz <= RELX_ZDENSE && !six;
   if (dense) {
     RelxCorners &C = cout[set];
     for (int i = tid; i < RELX_MAX_UCORNER * RELX_ZDENSE; i += kSetupThreads) (&C.w[0][0])[i] = 0.0f;
@@ -897,20 +947,23 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     RradSmem &q = m.rt.rr;
     if (tid < nz) {  // get_xillver_fluxcorrection_factors (Xillspec.cpp:500-526) from per-corner integrals
       const int z = tid;
+      const int nq = tab.x_npar - 1;  // parameters bracketed per corner
       double ef = 0.0, pf = 0.0, pfz = 0.0;
-      for (int c = 0; c < 16; c++) {
-        const int e = z * 16 + c;
+      for (int c = 0; c < (1 << nq); c++) {
         double w = 1.0;
-        for (int qq = 0; qq < 4; qq++) {
+        long corner = 0;
+        for (int qq = 0; qq < nq; qq++) {
           const double f = m.zfac[z][qq];
-          w *= ((c >> qq) & 1) ? f : (1.0 - f);
+          const int up = (c >> qq) & 1;
+          w *= up ? f : (1.0 - f);
+          corner = corner * tab.x_nvals[qq] + m.zind[z][qq] + up;
         }
         if (w == 0.0) continue;
         if (!tab.x_has_dens) {
-          const double d = m.zdens[m.cfirst[e] >> 4];
+          const double d = m.zdens[m.cfirst[z * 16 + c] >> 4];
           if (fabs(d - 15) > 1e-6) w *= 1.0 / pow(10.0, d - 15);
         }
-        const double *fc = tab.x_fcorr + (size_t) (m.crow[e] / ni) * 3;
+        const double *fc = tab.x_fcorr + (size_t) corner * 3;
         ef += w * fc[0];
         pf += w * fc[1];
         pfz += w * fc[2];
@@ -923,6 +976,10 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       for (int e2 = 0; e2 < 2; e2++) {
         const int b = tab.coarse_b2_skip[e2];
         if (b < 0) continue;
+        if (s.prim == 1) {  // the end-bin correction is only restated for the cut-off power law
+          m.status = RELX_ERR_UNSUPPORTED;
+          continue;
+        }
         const float4 t = tab.coarse_t[b];
         const float term = expf(1.0f / ecut) * m.cpow[b] * expf(-t.x / ecut) * t.y;
         x += (double) term * ((double) t.z + (double) t.w);

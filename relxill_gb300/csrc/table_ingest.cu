@@ -6,9 +6,10 @@
 // streamed once: the host reads raw FITS rows in large chunks into pinned
 // memory, the chunk is copied to the device, and one CTA per row
 //  * decodes the big-endian floats of the spectrum column,
-//  * divides them by 10^logXi of the row (the divisor is computed on the host
-//    per logXi grid value, so the quotient is the correctly rounded one the
-//    host would store),
+//  * divides them by 10^logXi of the row and, for a table with a density
+//    parameter, then by 10^(logN - 15) (the divisors are computed on the host
+//    per grid value, so each quotient is the correctly rounded one the host
+//    would store),
 //  * writes the row padded to a multiple of four floats,
 //  * integrates the row for the returning-radiation correction factors
 //    (energy flux in 0.1-1000 keV, photon flux in 0.15-500 keV, and that
@@ -28,13 +29,15 @@ __device__ __forceinline__ float be_to_float(uint32_t w) { return __uint_as_floa
 
 __global__ void __launch_bounds__(kIngestThreads) xill_ingest_kernel(
     const unsigned char *__restrict__ raw, int64_t width, int64_t col_off, int ne, int pad, int64_t row0,
-    const double *__restrict__ lxi_div, int64_t stride_lxi, int n_lxi, const double *__restrict__ xe,
+    const double *__restrict__ lxi_div, int64_t stride_lxi, int n_lxi, const double *__restrict__ dns_div,
+    int64_t stride_dns, int n_dns, const double *__restrict__ xe,
     const double *__restrict__ pfz_coef, float *__restrict__ spec, double *__restrict__ rowflux,
     unsigned long long *__restrict__ bad) {
   __shared__ double red[3][kIngestThreads / 32];
   const int r = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t row = row0 + r;
   const double div = n_lxi > 0 ? lxi_div[(row / stride_lxi) % n_lxi] : 1.0;
+  const double div2 = n_dns > 0 ? dns_div[(row / stride_dns) % n_dns] : 1.0;
   const uint32_t *src = reinterpret_cast<const uint32_t *>(raw + (size_t) r * width + col_off);
   float *dst = spec + (size_t) row * pad;
   double ef = 0.0, pf = 0.0, pfz = 0.0;
@@ -43,6 +46,7 @@ __global__ void __launch_bounds__(kIngestThreads) xill_ingest_kernel(
     float v = 0.0f;
     if (e < ne) {
       v = (float) ((double) be_to_float(__ldg(src + e)) / div);  // float / double, stored as float
+      v = (float) ((double) v / div2);                           // (xilltable.c:478-485, two steps)
       if (!isfinite(v)) nbad++;
       const double lo = xe[e], hi = xe[e + 1];
       if (lo >= 0.1 && hi <= 1000) ef += (double) v * 0.5 * (lo + hi);
@@ -87,8 +91,8 @@ cudaError_t launch_xill_ingest(cudaStream_t s, const XillIngest &g, const unsign
                                int nrows) {
   if (nrows <= 0) return cudaSuccess;
   xill_ingest_kernel<<<nrows, kIngestThreads, 0, s>>>(raw, g.width, g.col_off, g.ne, g.pad, row0, g.lxi_div,
-                                                      g.stride_lxi, g.n_lxi, g.xe, g.pfz_coef, g.spec, g.rowflux,
-                                                      g.bad);
+                                                      g.stride_lxi, g.n_lxi, g.dns_div, g.stride_dns, g.n_dns, g.xe,
+                                                      g.pfz_coef, g.spec, g.rowflux, g.bad);
   return cudaGetLastError();
 }
 

@@ -220,13 +220,15 @@ static size_t xill_smem_nz(int n_incl) {
 }
 
 // generic path for more than RELX_ZDENSE zones (ionisation gradients): 16 corners per zone, plain loads
+// min_nz: sets with at most this many zones are left to the dense kernel (0: none)
 __global__ void __launch_bounds__(kXillThreads) xillver_zone_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
                                                                     const RelxZoneCorners *__restrict__ zcor,
                                                                     const float *__restrict__ dist_raw, int nza,
-                                                                    float *__restrict__ xout) {
+                                                                    float *__restrict__ xout, int min_nz) {
   const int set = blockIdx.y, tile = blockIdx.x;
   const RelxSetState &s = sst[set];
-  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.nz <= RELX_ZDENSE) return;
+  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.nz <= min_nz) return;
+  const int ncz = tab.x_npar == 6 ? 32 : 16;  // corners per zone (16, or 32 for the 6-parameter table)
   __shared__ float dist[RELX_MAX_INCL];
   const int tid = threadIdx.x, ni = tab.x_nincl, pitch = tab.x_nener_pad;
   const int e0 = tile * kXillTile;
@@ -245,7 +247,7 @@ __global__ void __launch_bounds__(kXillThreads) xillver_zone_kernel(RelxTables t
     __syncthreads();
     if (!active) continue;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int c = 0; c < 16; c++) {
+    for (int c = 0; c < ncz; c++) {
       const float wz = zcor[set].w[z][c];
       if (wz == 0.0f) continue;  // zero weight: the row adds exactly nothing
       const float4 *src = reinterpret_cast<const float4 *>(tab.x_spec + (size_t) zcor[set].row[z][c] * pitch + e0) + q;
@@ -281,8 +283,12 @@ cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, in
                            const RelxCorners *cor, const RelxZoneCorners *zcor, const float *dist, float *xout,
                            int *err, const int *order) {
   const dim3 grid((tab.x_nener_pad + kXillTile - 1) / kXillTile, n_sets);
+  if (tab.x_npar == 6) {  // the 6-parameter table: per-zone corner lists for every set
+    xillver_zone_kernel<<<grid, kXillThreads, 0, s>>>(tab, sst, zcor, dist, nza, xout, 0);
+    return cudaGetLastError();
+  }
   if (nza > RELX_ZDENSE) {
-    xillver_zone_kernel<<<grid, kXillThreads, 0, s>>>(tab, sst, zcor, dist, nza, xout);
+    xillver_zone_kernel<<<grid, kXillThreads, 0, s>>>(tab, sst, zcor, dist, nza, xout, RELX_ZDENSE);
     return cudaGetLastError();
   }
   const int nzk = nza <= 1 ? 1 : (nza <= 10 ? 10 : 16);

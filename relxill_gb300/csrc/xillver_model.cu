@@ -22,7 +22,7 @@
 namespace relx {
 
 constexpr int kXmodThreads = kXmodThreadsH;
-constexpr int kXmodCorners = 32;
+constexpr int kXmodCorners = 64;  // 32 for a 5-parameter table, 64 for the 6-parameter one
 
 // count of a[0..n) <= key (a ascending)
 __device__ __forceinline__ int count_le_x(const float2 *a, int n, float key) {
@@ -43,10 +43,13 @@ __device__ __forceinline__ int corner_mask(int c) {
   return (c & ~7) | perm;
 }
 
+// nthq, nth: xillverCp (the 6-parameter table and the nthcomp continuum); null for xillver
 __global__ void __launch_bounds__(kXmodThreads) xillver_model_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
                                                                       const double *__restrict__ user_e,
                                                                       RelxSetState *__restrict__ sst,
-                                                                      double *__restrict__ flux) {
+                                                                      double *__restrict__ flux,
+                                                                      const double *__restrict__ nthq,
+                                                                      const NthTable *__restrict__ nth) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n0 = tab.x_nener, pad = tab.x_nener_pad;
   float *spec = reinterpret_cast<float *>(smem_raw);                    // [pad]
@@ -58,8 +61,13 @@ __global__ void __launch_bounds__(kXmodThreads) xillver_model_kernel(RelxTables 
   const int set = blockIdx.x, tid = threadIdx.x;
   const RelxSetIn &in = sin[set];
   const double *v = in.p;
-  // get_xill_params (ModelDefinition.cpp:339-388); the inclination stays in degrees
-  const double gam = v[0], afe = v[1], ect = v[2], lxi = v[3], z = v[4], incl = v[5], refl_frac = v[6];
+  // get_xill_params (ModelDefinition.cpp:339-388); the inclination stays in degrees.  xillver:
+  // Gamma, A_Fe, Ecut, logxi, z, Incl, refl_frac; xillverCp: Gamma, A_Fe, kTe, logxi, logN, z, Incl,
+  // refl_frac (lmodel_relxill_public.dat:77-94)
+  const bool cp = nthq != nullptr;
+  const double gam = v[0], afe = v[1], ect = v[2], lxi = v[3];
+  const double dens = cp ? v[4] : 15.0;  // density of the xillver model (ModelDefinition.cpp:362)
+  const double z = cp ? v[5] : v[4], incl = cp ? v[6] : v[5], refl_frac = cp ? v[7] : v[6];
 
   if (tid == 0) {
     // get_xilltab_indices_for_paramvals (xilltable.c:278-323) and the interpolation factors
@@ -70,11 +78,12 @@ __global__ void __launch_bounds__(kXmodThreads) xillver_model_kernel(RelxTables 
     inp[1] = (float) afe;
     inp[2] = (float) lxi;
     inp[3] = (float) ect;
-    inp[4] = 15.0f;  // density of the xillver model (ModelDefinition.cpp:362)
+    inp[4] = (float) dens;
     inp[7] = (float) incl;
-    int ind[5];
-    double f[5];
-    for (int q = 0; q < 5; q++) {
+    const int np = tab.x_npar;
+    int ind[6];
+    double f[6];
+    for (int q = 0; q < np; q++) {
       const float *pv = tab.x_vals + q * tab.x_maxvals;
       const int nv = tab.x_nvals[q], pi = tab.x_pindex[q];
       int k = bsearch_asc<float>(pv, nv, inp[pi]);
@@ -90,15 +99,18 @@ __global__ void __launch_bounds__(kXmodThreads) xillver_model_kernel(RelxTables 
         if (ect >= pv[nv - 1]) f[q] = 1.0;
       }
     }
+    // 6 parameters: the 32 corners over parameters 1..5 at both brackets of parameter 0, linear in
+    // parameter 0 (interp_6d_tab, xilltable.c:1022-1043)
+    const int q0 = np - 5;
     int nc = 0;
-    for (int c = 0; c < kXmodCorners; c++) {
-      const int msk = corner_mask(c);
-      double w = 1.0;
-      int64_t row = 0;
+    for (int c = 0; c < (32 << q0); c++) {
+      const int msk = corner_mask(c & 31), half = c >> 5;
+      double w = (q0 == 0) ? 1.0 : (half ? f[0] : 1.0 - f[0]);
+      int64_t row = (q0 == 0) ? 0 : ind[0] + half;
       for (int q = 0; q < 5; q++) {
         const int up = (msk >> q) & 1;
-        w *= up ? f[q] : (1.0 - f[q]);
-        row = row * tab.x_nvals[q] + ind[q] + up;  // incl is the fastest table index
+        w *= up ? f[q0 + q] : (1.0 - f[q0 + q]);
+        row = row * tab.x_nvals[q0 + q] + ind[q0 + q] + up;  // incl is the fastest table index
       }
       if (w != 0.0) {  // a zero weight adds exactly nothing
         w_s[nc] = (float) w;
@@ -129,13 +141,22 @@ __global__ void __launch_bounds__(kXmodThreads) xillver_model_kernel(RelxTables 
       reinterpret_cast<float4 *>(spec)[i4] = make_float4(a.x * nf, a.y * nf, a.z * nf, a.w * nf);
     }
   }
-  // normalisation of the primary continuum (calc_normalized_primary_spectrum, Xillspec.cpp:302-332)
-  if (tid < 32) {
+  // normalisation of the primary continuum (calc_normalized_primary_spectrum, Xillspec.cpp:302-332);
+  // for the nthcomp continuum from nthcomp_kernel, with the E F_E normalisation at 1 keV
+  __shared__ double nth_norm_s;
+  if (cp) {
+    if (tid == 0) {
+      qsum_s = nthq[(size_t) set * (RELX_NZMAX + 1)];
+      nth_norm_s = nth[set].n > 0 ? nth_normfac(nth[set].x, nth[set].sp, nth[set].n, 1.0) : 0.0;
+    }
+  } else if (tid < 32) {
     const double q = primary_qsum_warp(tab, (float) gam, (float) ect, nullptr);
     if (tid == 0) qsum_s = q;
   }
   __syncthreads();
 
+  // xillverCp: kTe without an nthcomp grid gives no spectrum (nthcomp_kernel)
+  const bool ok = !cp || (isfinite(qsum_s) && qsum_s > 0.0 && nth[set].n > 0);
   const int nu = in.n_ener;
   const double *ue = user_e + in.e_off;
   double *fo = flux + in.e_off - set;  // flux offsets: e_off counts n+1 edges per set
@@ -147,6 +168,10 @@ __global__ void __launch_bounds__(kXmodThreads) xillver_model_kernel(RelxTables 
   const float pnorm = (float) (1.0 / qsum_s);
   const double e_first = (double) eb[0].x, e_last = (double) eb[n0].x;
   for (int i = tid; i < nu; i += kXmodThreads) {
+    if (!ok) {
+      fo[i] = 0.0;
+      continue;
+    }
     double elo = ue[i], ehi = ue[i + 1];
     if (z > 0) { elo *= zf; ehi *= zf; }
     double r = 0.0;  // a coarse caller bin sums many table bins: FP64 accumulation
@@ -170,7 +195,9 @@ __global__ void __launch_bounds__(kXmodThreads) xillver_model_kernel(RelxTables 
       }
     }
     r *= arf;
-    if (add_prim) {  // spec_cutoffpl on the shifted grid (Xillspec.cpp:215-233), FP32 arithmetic
+    if (add_prim && cp) {  // nthcomp on the shifted grid (spec_nthcomp with no energy shift)
+      r += nth_bin(nth[set], elo, ehi, 1.0, nth_norm_s) * (1.0 / qsum_s);
+    } else if (add_prim) {  // spec_cutoffpl on the shifted grid (Xillspec.cpp:215-233), FP32 arithmetic
       const float en = (float) (0.5 * (elo + ehi));
       r += (double) (e1 * powf(en, -fg) * expf(-en / fe) * (float) (ehi - elo) * pnorm);
     }
@@ -178,9 +205,10 @@ __global__ void __launch_bounds__(kXmodThreads) xillver_model_kernel(RelxTables 
   }
   if (tid == 0) {  // the fields the status pass and the statistics read
     RelxSetState &s = sst[set];
-    s.status = RELX_OK;
+    s.status = ok ? RELX_OK : RELX_ERR_PARAM;
     s.model = RELX_XILLVER;
-    s.pmodel = RELX_XILLVER;
+    s.pmodel = cp ? RELX_XILLVERCP : RELX_XILLVER;
+    s.prim = cp ? 1 : 0;
     s.cached = 0;
     s.nz = 0;
     s.ucount = 0;
@@ -198,10 +226,11 @@ cudaError_t xillver_model_set_smem(int n_ener, int n_ener_pad) {
 }
 
 cudaError_t launch_xillver_model(cudaStream_t s, const RelxTables &tab, int n_sets, const RelxSetIn *sin,
-                                 const double *user_e, RelxSetState *sst, double *flux) {
+                                 const double *user_e, RelxSetState *sst, double *flux, const double *nthq,
+                                 const NthTable *nth) {
   if (n_sets <= 0) return cudaSuccess;
   xillver_model_kernel<<<n_sets, kXmodThreads, xillver_model_smem_bytes(tab.x_nener, tab.x_nener_pad), s>>>(
-      tab, sin, user_e, sst, flux);
+      tab, sin, user_e, sst, flux, nthq, nth);
   return cudaGetLastError();
 }
 
