@@ -36,6 +36,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "relxilllp spectra/s batched vs plain GPU at ≤1e-4 rel err; serve p50/p99 ms"
 N_SETS = 4096
+N_PROF = 8  # kernel kinds of the per-kernel event profiler (relx_profile_name)
 
 
 def workload(n: int, seed_params: int = 2026, seed_grids: int = 7):
@@ -176,9 +177,12 @@ def run_serve(R, seconds: float, rate: float, n_walkers: int, budget_gb: float, 
             "xillver_only_steps": 0.7, "identical_to_alone": same, "checked": checked}
 
 
-def _time_device_variant(R, L, torch, dev, steps: int, warmup: int, params, grids, igt_value: int, n_check: int = 2):
-    """Batched relxilllp through the device API on its own stream (CUDA events on that stream):
-    spectra/s, ms per step and the largest per-bin error of n_check sets against the oracle."""
+def _time_device_variant(R, L, torch, dev, steps: int, warmup: int, params, grids, igt_value: int, n_check: int = 2,
+                         model: str = "relxilllp", profile_steps: int = 0):
+    """A batched model through the device API on its own stream (CUDA events on that stream):
+    spectra/s, ms per step and the largest per-bin error of n_check sets against the oracle;
+    with profile_steps, per-kernel times of that many further steps (outside the timed region)."""
+    mid = R.MODELS[model]
     n = len(grids)
     edges, offs = R.pack_grids(grids)
     nflux = int(offs[-1]) - n
@@ -196,7 +200,7 @@ def _time_device_variant(R, L, torch, dev, steps: int, warmup: int, params, grid
     use_igt = igt_value != 0
 
     def step():
-        st = L.relx_eval_batch_device(3, n, d_params.data_ptr(), d_e.data_ptr(), d_off.data_ptr(), offs_ptr, None,
+        st = L.relx_eval_batch_device(mid, n, d_params.data_ptr(), d_e.data_ptr(), d_off.data_ptr(), offs_ptr, None,
                                       d_flux.data_ptr(), d_status.data_ptr(), d_igt.data_ptr() if use_igt else None,
                                       igt_ptr if use_igt else None, d_igi.data_ptr() if use_igt else None,
                                       stream.cuda_stream)
@@ -218,17 +222,32 @@ def _time_device_variant(R, L, torch, dev, steps: int, warmup: int, params, grid
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
     out = d_flux.cpu().numpy()
+    kernels = None
+    if profile_steps > 0:
+        L.relx_profile_enable(1)
+        for _ in range(profile_steps):
+            step()
+        torch.cuda.synchronize()
+        ms_k = (ctypes.c_double * N_PROF)()
+        n_k = (ctypes.c_int64 * N_PROF)()
+        L.relx_profile_read(ms_k, n_k, N_PROF)
+        L.relx_profile_enable(0)
+        kernels = {L.relx_profile_name(k).decode(): round(ms_k[k] / profile_steps, 4)
+                   for k in range(N_PROF) if n_k[k] > 0}
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
 
     max_err = 0.0
     for i in range(n_check):
-        st, ref = oracle_lib.evaluate("relxilllp", params[i], grids[i], None, igt_value, 0.0)
+        st, ref = oracle_lib.evaluate(model, params[i], grids[i], None, igt_value, 0.0)
         got = out[offs[i] - i: offs[i + 1] - i - 1]
         m = ref > 1e-6 * ref.max()
         max_err = max(max_err, float(np.max(np.abs(got[m] / ref[m] - 1))))
-    return {"value": n * steps / (ms / 1e3), "unit": "spectra/s", "sets": n, "steps": steps,
-            "ms_per_step": ms / steps, "max_rel_err_vs_oracle": max_err}
+    r = {"value": n * steps / (ms / 1e3), "unit": "spectra/s", "sets": n, "steps": steps,
+         "ms_per_step": ms / steps, "max_rel_err_vs_oracle": max_err}
+    if kernels is not None:
+        r["kernel_ms_per_step"] = kernels
+    return r
 
 
 def run_iongrad(R, L, torch, dev, steps: int, warmup: int, n: int = 2048):
@@ -253,6 +272,22 @@ def run_rrad(R, L, torch, dev, steps: int, warmup: int, n: int = N_SETS):
     params[:, 12] = 1.0
     r = _time_device_variant(R, L, torch, dev, steps, warmup, params, grids, 0)
     r.update({"zones": 10, "mode": "returning radiation on (Relreturn_Corona.cpp, Relreturn_Table.cpp)"})
+    return r
+
+
+def run_cp(R, L, torch, dev, steps: int, warmup: int, n: int = N_SETS):
+    """The 4096-set workload as relxilllpCp: nthcomp continua for the source and the 10 zones
+    (donthcomp.c), 6-parameter xillverCp brackets (32 corners per zone), logN 15-19, kTe 20-300 keV."""
+    base, grids = workload(n, seed_params=2029, seed_grids=10)
+    rng = np.random.default_rng(2030)
+    p = np.zeros((n, 17))
+    p[:, 0], p[:, 1], p[:, 2], p[:, 3] = base[:, 3], base[:, 2], -1.0, 400.0   # Incl, a, Rin, Rout
+    p[:, 4], p[:, 5], p[:, 6], p[:, 7] = base[:, 0], 0.0, base[:, 7], base[:, 8]  # h, beta, gamma, logxi
+    p[:, 8] = rng.uniform(15.0, 19.0, n)                                         # logN
+    p[:, 9], p[:, 10], p[:, 11] = 1.0, rng.uniform(20.0, 300.0, n), 1.0          # Afe, kTe, refl_frac
+    r = _time_device_variant(R, L, torch, dev, steps, warmup, p, grids, 0, model="relxilllpCp", profile_steps=2)
+    r.update({"zones": 10, "mode": "relxilllpCp: nthcomp primary and zone normalisations, 6-parameter xillverCp table "
+                                   "(synthetic, 4x3x4x4x3 grid x 10 inclinations)"})
     return r
 
 
@@ -481,9 +516,9 @@ def run_gpu(args):
         step()
     torch.cuda.synchronize()
     os.environ.pop("RELX_CHUNK_SETS", None)
-    ms_k = (ctypes.c_double * 7)()
-    n_k = (ctypes.c_int64 * 7)()
-    L.relx_profile_read(ms_k, n_k, 7)
+    ms_k = (ctypes.c_double * N_PROF)()
+    n_k = (ctypes.c_int64 * N_PROF)()
+    L.relx_profile_read(ms_k, n_k, N_PROF)
     L.relx_profile_enable(0)
     ms = replicas.max_over_ranks(ms, dist, dev)
     value = replicas.job_throughput(S, args.steps, world, ms / 1e3)
@@ -556,16 +591,19 @@ def run_gpu(args):
     rrad = None
     if not args.no_rrad:
         rrad = run_rrad(R, L, torch, dev, args.steps, args.warmup)
+    cp = None
+    if not args.no_cp:
+        cp = run_cp(R, L, torch, dev, args.steps, args.warmup)
 
     serve = None
     if not args.no_serve:
         serve = run_serve(R, args.serve_seconds, args.serve_rate, args.walkers, args.serve_budget_gb)
 
     # roofline of the dominant kernel
-    names = [L.relx_profile_name(k).decode() for k in range(7)]
-    per = {names[k]: (ms_k[k] / max(n_k[k], 1), int(n_k[k])) for k in range(7)}
-    total_k = sum(ms_k[k] for k in range(7))
-    dom = max(range(7), key=lambda k: ms_k[k])
+    names = [L.relx_profile_name(k).decode() for k in range(N_PROF)]
+    per = {names[k]: (ms_k[k] / max(n_k[k], 1), int(n_k[k])) for k in range(N_PROF)}
+    total_k = sum(ms_k[k] for k in range(N_PROF))
+    dom = max(range(N_PROF), key=lambda k: ms_k[k])
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -608,7 +646,7 @@ def run_gpu(args):
         "roofline": roof, "dominant_kernel": names[dom],
         "dominant_kernel_bound": "FP32 ALU issue (line profile: Romberg g*-integration; see profiles/)",
         "kernels": kernels, "cpu_baseline": cpu,
-        "serve": serve, "ion_gradient": iongrad, "returning_radiation": rrad,
+        "serve": serve, "ion_gradient": iongrad, "returning_radiation": rrad, "cp_flavour": cp,
         "table_load": {"seconds": table_load_s, "bytes": int(tb.value)},
     }
     print(json.dumps(line))
@@ -631,6 +669,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-iongrad", action="store_true")
     ap.add_argument("--no-rrad", action="store_true")
+    ap.add_argument("--no-cp", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-rate", type=float, default=50000.0)
     ap.add_argument("--walkers", type=int, default=256)

@@ -2,7 +2,7 @@
  * relxill_gb300.h -- C ABI of the GB300 (sm_103a) implementation of relxill's
  * relativistic convolution path.
  *
- * The seven local-model entry points keep the signature that the reference's
+ * The ten local-model entry points keep the signature that the reference's
  * wrapper generator emits for XSPEC (src/create_wrapper_xspec.py:153-162) and
  * the parameter order of src/modelfiles/lmodel_relxill_public.dat, so a host
  * package that loads the reference's librelxill can load this library
@@ -196,7 +196,7 @@ int relx_tuning_report(double *out, int max);
 /* Measurement hooks (no counterpart in the reference).  When enabled, every
  * kernel of every batch is bracketed by CUDA events on its launching stream;
  * relx_profile_read synchronises and returns the accumulated milliseconds
- * and launch counts per kernel kind (relx_profile_name(k), k < 7). */
+ * and launch counts per kernel kind (relx_profile_name(k), k < 8). */
 int relx_profile_enable(int on);
 int relx_profile_read(double *ms, int64_t *launches, int n);
 const char *relx_profile_name(int k);

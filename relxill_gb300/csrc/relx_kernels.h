@@ -33,9 +33,9 @@ cudaError_t xillver_set_smem(int n_incl);
 // bounded-wait self-test: writes the status of a wait that cannot complete (RELX_ERR_TIMEOUT)
 cudaError_t launch_wait_selftest(cudaStream_t s, unsigned long long limit_ns, int *out);
 // order: the sets in visiting order (launch_xill_order), or null for batch order
-cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, int nza, const RelxSetState *sst,
-                           const RelxCorners *cor, const RelxZoneCorners *zcor, const float *dist, float *xout,
-                           int *err, const int *order);
+cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, int nza, int nz_min,
+                           const RelxSetState *sst, const RelxCorners *cor, const RelxZoneCorners *zcor,
+                           const float *dist, float *xout, int *err, const int *order);
 void launch_xill_order(cudaStream_t s, const RelxSetState *sst, const RelxCorners *cor, const RelxZoneCorners *zcor,
                        int n_sets, int *order);
 

@@ -802,8 +802,8 @@ __global__ void status_kernel(int n_sets, const RelxSetState *__restrict__ st, c
 }
 
 // ---- optional per-kernel timing with CUDA events on the launching stream ----
-enum ProfKernel { PK_PACK, PK_SETUP, PK_LINE, PK_XILL, PK_CONV, PK_FIN, PK_STATUS, PK_N };
-static const char *kProfNames[PK_N] = {"pack", "setup", "relline", "xillver", "conv", "finalize", "status"};
+enum ProfKernel { PK_PACK, PK_SETUP, PK_LINE, PK_XILL, PK_CONV, PK_FIN, PK_STATUS, PK_NTH, PK_N };
+static const char *kProfNames[PK_N] = {"pack", "setup", "relline", "xillver", "conv", "finalize", "status", "nthcomp"};
 struct Profiler {
   bool on = false;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> rec;
@@ -857,6 +857,7 @@ static int prof_collect() {
 
 struct BatchShape {
   int model, n_sets, nza;
+  int nz_min = 1;     // the smallest zone count of the batch's sets
   int nblk;           // 256-bin profile-sum blocks per set
   int line_tile = 512;  // energy bins per line-kernel CTA (256 or 512)
   int chunk = 0;      // sets per pipelined chunk (0: one range)
@@ -925,9 +926,12 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   double *flux = W.flux.as<double>() - base;  // kernels address set i at e_off(i) - i
   const double *user_e = W.user_e.as<double>();
   if (kind == RELX_XILLVER) {
+    if (cp) {
+      ProfScope ps(PK_NTH, s);
+      RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, 1, true, nthq, ntab, nullptr));
+    }
     {
       ProfScope ps(PK_XILL, s);
-      if (cp) RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, 1, true, nthq, ntab, nullptr));
       RELX_CUDA(launch_xillver_model(s, tab, n, sin, user_e, sst, flux, nthq, ntab));
     }
     ProfScope ps(PK_STATUS, s);
@@ -939,8 +943,10 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     ProfScope ps(PK_SETUP, s);
     setup_kernel<<<n, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, b.model, sin, user_e, W.line_e.as<double>(), sst,
                                                                rad, cor, zcor);
-    // Cp: the nthcomp continua of the source and the zones, their normalisations on the corner weights
-    if (cp) RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, b.nza, false, nthq, ntab, zcor));
+  }
+  if (cp) {  // the nthcomp continua of the source and the zones, their normalisations on the corner weights
+    ProfScope ps(PK_NTH, s, 2);
+    RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, b.nza, false, nthq, ntab, zcor));
   }
   if (cached) {
     ProfScope ps(PK_SETUP, s, 2);
@@ -965,10 +971,11 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   if (relx_is_relxill(kind)) {
     {
       const bool dense = b.nza <= RELX_ZDENSE && !cp;
-      ProfScope ps(PK_XILL, s, dense ? 2 : 1);
-      int *order = W.order.as<int>() + base;
+      const bool both = b.nza > RELX_ZDENSE && b.nz_min <= RELX_ZDENSE && !cp;  // zone and dense kernels
+      ProfScope ps(PK_XILL, s, (dense || both) ? 2 : 1);
+      int *order = dense ? W.order.as<int>() + base : nullptr;
       if (dense) launch_xill_order(s, sst, cor, zcor, n, order);
-      RELX_CUDA(launch_xillver(s, tab, n, b.nza, sst, cor, zcor, dist, xill, W.err.as<int>(), order));
+      RELX_CUDA(launch_xillver(s, tab, n, b.nza, b.nz_min, sst, cor, zcor, dist, xill, W.err.as<int>(), order));
     }
     {
       ProfScope ps(PK_CONV, s);
@@ -1033,9 +1040,9 @@ static int launch_direct(Context &C, Workspace &W, const BatchShape &b, cudaStre
 }
 
 static std::vector<uintptr_t> graph_key(const Workspace &W, const BatchShape &b) {
-  std::vector<uintptr_t> k = {(uintptr_t) b.model, (uintptr_t) b.n_sets, (uintptr_t) b.nza, (uintptr_t) b.nblk,
-                              (uintptr_t) b.line_tile, (uintptr_t) b.chunk, (uintptr_t) b.any_limb,
-                              (uintptr_t) b.n_edges};
+  std::vector<uintptr_t> k = {(uintptr_t) b.model, (uintptr_t) b.n_sets, (uintptr_t) b.nza, (uintptr_t) b.nz_min,
+                              (uintptr_t) b.nblk, (uintptr_t) b.line_tile, (uintptr_t) b.chunk,
+                              (uintptr_t) b.any_limb, (uintptr_t) b.n_edges};
   for (const DevBuf *d : {&W.setin, &W.st, &W.rad, &W.corners, &W.zcorners, &W.line_e, &W.prof, &W.dist, &W.tsum,
                           &W.xill, &W.cout, &W.user_e, &W.user_f, &W.flux, &W.sflag, &W.status, &W.err, &W.order})
     k.push_back((uintptr_t) d->p);
@@ -1177,7 +1184,7 @@ static int batch_shape(int model, int n_sets, const int64_t *eoff_host, const in
   b->model = model;
   b->n_sets = n_sets;
   b->n_edges = eoff_host[n_sets];
-  int nza = 1, maxn = 0;
+  int nza = 1, nz_min = RELX_NZMAX, maxn = 0;
   const int npar = model_nparams(model);
   for (int i = 0; i < n_sets; i++) {
     int n = (int) (eoff_host[i + 1] - eoff_host[i] - 1);
@@ -1185,9 +1192,12 @@ static int batch_shape(int model, int n_sets, const int64_t *eoff_host, const in
     maxn = std::max(maxn, n);
     int igt = igt_host ? igt_host[i] : 0;
     if (model == RELX_RELXILLLPCP && params_host) igt = (int) std::lround(params_host[(size_t) i * npar + 14]);
-    nza = std::max(nza, zones_for(model, igt, env.nzones_env));
+    const int nz = zones_for(model, igt, env.nzones_env);
+    nza = std::max(nza, nz);
+    nz_min = std::min(nz_min, nz);
   }
   b->nza = nza;
+  b->nz_min = std::min(nz_min, nza);
   b->chunk = chunk_sets();
   const int kind = relx_kind(model);
   b->any_limb = (kind == RELX_RELLINE || kind == RELX_RELCONV);

@@ -278,10 +278,12 @@ cudaError_t xillver_set_smem(int n_incl) {
 }
 
 // xillver stage of a batch: the dense kernel (instance by the batch's zone count and the table's
-// inclination count) for sets with at most RELX_ZDENSE zones, the zone kernel otherwise
-cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, int nza, const RelxSetState *sst,
-                           const RelxCorners *cor, const RelxZoneCorners *zcor, const float *dist, float *xout,
-                           int *err, const int *order) {
+// inclination count) for sets with at most RELX_ZDENSE zones, the zone kernel for sets with more.
+// nz_min: the smallest zone count of the batch's sets; a batch with more than RELX_ZDENSE zones
+// runs both kernels when it also holds sets with at most RELX_ZDENSE zones (order is then unused).
+cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, int nza, int nz_min,
+                           const RelxSetState *sst, const RelxCorners *cor, const RelxZoneCorners *zcor,
+                           const float *dist, float *xout, int *err, const int *order) {
   const dim3 grid((tab.x_nener_pad + kXillTile - 1) / kXillTile, n_sets);
   if (tab.x_npar == 6) {  // the 6-parameter table: per-zone corner lists for every set
     xillver_zone_kernel<<<grid, kXillThreads, 0, s>>>(tab, sst, zcor, dist, nza, xout, 0);
@@ -289,7 +291,8 @@ cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, in
   }
   if (nza > RELX_ZDENSE) {
     xillver_zone_kernel<<<grid, kXillThreads, 0, s>>>(tab, sst, zcor, dist, nza, xout, RELX_ZDENSE);
-    return cudaGetLastError();
+    if (nz_min > RELX_ZDENSE) return cudaGetLastError();
+    order = nullptr;
   }
   const int nzk = nza <= 1 ? 1 : (nza <= 10 ? 10 : 16);
   const int nik = tab.x_nincl == 10 ? 10 : 0;

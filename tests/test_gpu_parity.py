@@ -126,6 +126,58 @@ def test_relline_grid_without_line_and_single_bin(gpu, oracle):
     np.testing.assert_allclose(out[0], orc, rtol=1e-6)
 
 
+def test_relline_profile_edges_on_conv_grid(gpu, oracle):
+    """Line profiles on the 4096-bin convolution grid, where the blue and red
+    edges of single radii fall on bin edges in every possible position: a
+    geometry whose gmax at one radius lies a hair below a bin edge (the edge
+    term of that radius must stay in the bin below), and random geometries."""
+    cg = oracle_lib.conv_grid()
+    rng = np.random.default_rng(71)
+    rows = [[1.0, 2.3746189592624702, 2.633860796331297, 6.812861314634864, -0.4762755685025275,
+             50.195840694470434, -1.0, 131.52308866238963, 0.0, 0.0]]
+    for _ in range(47):
+        rows.append([rng.uniform(0.3, 30.0), rng.uniform(1.0, 5.0), rng.uniform(1.0, 5.0), rng.uniform(3.0, 30.0),
+                     rng.uniform(-0.998, 0.998), rng.uniform(5.0, 85.0), -1.0, rng.uniform(20.0, 1000.0), 0.0,
+                     float(rng.integers(0, 3))])
+    p = np.array(rows)
+    out, st = gpu.eval_batch("relline", p, [cg] * len(p))
+    assert not st.any()
+    for i in range(len(p)):
+        s, orc = oracle_lib.evaluate("relline", p[i], cg)
+        assert s == 0
+        assert_close(out[i], orc, f"relline geometry {i}")
+
+
+def test_mixed_zone_counts_in_one_batch(gpu, oracle, monkeypatch):
+    """One batch whose sets need different zone counts: relxill sets without an ionisation
+    gradient (1 zone) beside power-law and alpha-disc gradients (25 zones), and relxilllp sets
+    with 10 zones beside 25; every set against the oracle with its own switch."""
+    monkeypatch.delenv("RELXILL_NUM_RZONES", raising=False)  # the default zone counts differ per switch
+    rng = np.random.default_rng(73)
+    e = [np.exp(np.linspace(np.log(0.3), np.log(80.0), int(k) + 1)) for k in rng.integers(200, 900, 6)]
+    igt = np.array([0, 1, 0, 2, 0, 1], dtype=np.int32)
+    igi = np.where(igt == 1, 1.5, 0.0)
+    p = np.column_stack([rng.uniform(2.5, 4, 6), rng.uniform(2.5, 4, 6), rng.uniform(8, 30, 6),
+                         rng.uniform(0, 0.998, 6), rng.uniform(10, 80, 6), -np.ones(6), np.full(6, 400.0),
+                         np.zeros(6), rng.uniform(1.5, 2.8, 6), rng.uniform(1, 4, 6), np.ones(6),
+                         np.full(6, 300.0), np.ones(6)])
+    out, st = gpu.eval_batch("relxill", p, e, ion_grad_type=igt, iongrad_index=igi)
+    assert not st.any()
+    for i in range(6):
+        s, orc = oracle_lib.evaluate("relxill", p[i], e[i], None, int(igt[i]), float(igi[i]))
+        assert s == 0
+        assert_close(out[i], orc, f"relxill set {i} (ion_grad_type {igt[i]})")
+    q = np.column_stack([rng.uniform(3, 30, 6), np.zeros(6), rng.uniform(0, 0.998, 6), rng.uniform(10, 80, 6),
+                         -np.ones(6), np.full(6, 400.0), np.zeros(6), rng.uniform(1.5, 2.8, 6),
+                         rng.uniform(1, 4, 6), np.ones(6), np.full(6, 300.0), np.ones(6), np.zeros(6), np.zeros(6)])
+    out, st = gpu.eval_batch("relxilllp", q, e, ion_grad_type=igt, iongrad_index=igi)
+    assert not st.any()
+    for i in range(6):
+        s, orc = oracle_lib.evaluate("relxilllp", q[i], e[i], None, int(igt[i]), float(igi[i]))
+        assert s == 0
+        assert_close(out[i], orc, f"relxilllp set {i} (ion_grad_type {igt[i]})")
+
+
 def test_relline_normalised_to_one(gpu):
     e = grid(CASES[0][3])
     f = gpu.relline(e, CASES[0][2])
