@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(kFinThreads) finalize_relxill_kernel(RelxTable
   const bool cp = s.prim == 1;
   const double zp1 = (1.0 / s.g_inf - 1.0) + 1.0;
   if (cp && add_prim) {
-    if (tid == 0) m.nth_norm = nth_normfac(nth[set].x, nth[set].sp, nth[set].n, zp1);
+    if (tid == 0) m.nth_norm = nth_normfac(tab.nth_grid->x, nth[set].sp, nth[set].n, zp1);
     __syncthreads();
   }
   for (int k = s.out_lo + tid; k <= s.out_hi; k += kFinThreads) {
@@ -446,7 +446,7 @@ __global__ void __launch_bounds__(kFinThreads) finalize_relxill_kernel(RelxTable
     for (int z = 0; z < s.nz; z++) r += cout[((size_t) set * nza + z) * kN + k];
     r *= rfac;
     if (add_prim && cp) {
-      r += (float) nth_bin(nth[set], ce[k], ce[k + 1], zp1, m.nth_norm) * pnorm;
+      r += (float) nth_bin(tab.nth_grid->x, nth[set], ce[k], ce[k + 1], zp1, m.nth_norm) * pnorm;
     } else if (add_prim) {
       const float2 cd = tab.conv_cw[k];  // (float) bin centre, (float) bin width
       const float en = cd.x;

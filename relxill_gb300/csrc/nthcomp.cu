@@ -9,206 +9,203 @@
 // primary continuum and for the normalisation of every zone's continuum
 // (kTe times the zone's energy shift, Xillspec.cpp:243-253, 408-440).
 //
-// nthcomp_kernel: one CTA of 128 threads per (continuum, set).  The grid, the
-// Kompaneets coefficients and the escape probabilities are FP64, computed in
-// parallel; the disk-blackbody seed spectrum (five-point Gauss-Legendre per
-// bin of the multi-colour disk formula, donthcomp.c:52-191) is FP32, its
-// relative error of about 1e-7 carries linearly into the spectrum; the
-// tridiagonal system is solved by one thread in FP64.  Outputs: the
-// continuum's normalisation with respect to the xillver table
-// (calcNormWrtXillverTableSpec on the 500-bin coarse grid, Xillspec.cpp:179-205)
-// and, for the source continuum, the E F_E table that the primary spectrum is
-// interpolated from (c_donthcomp, donthcomp.c:640-793).
+// With the seed temperature fixed, the photon grid, Cooper's coefficient, the
+// Klein-Nishina factor and the disk-blackbody seed spectrum do not depend on
+// kTe or Gamma: they are computed once on the host in FP64 (NthGrid), as are
+// the weights that turn an E F_E table into its normalisation on the 500-bin
+// coarse grid (calcNormWrtXillverTableSpec, Xillspec.cpp:179-205): that
+// normalisation is linear in the table, sum_j G_j sp_j times the inverse of the
+// table at the 1 keV point.
+//
+// nthcomp_kernel: one thread per continuum (the source, and each zone whose
+// energy shift differs from 1).  The tridiagonal coefficients are formed on
+// the fly from the grid and the continuum's tautom and theta, and the system
+// is solved by the Thomas algorithm (thermlc, donthcomp.c:194-280) in
+// float-float arithmetic on the FP32 pipe (about 48 significant bits; the FP64
+// pipe of this part runs at 1/64 of the FP32 rate).  The forward sweep keeps
+// its two recurrences per point in a scratch laid out [point][continuum], so a
+// warp's accesses are contiguous; the back sweep recovers the solution, forms
+// E F_E (donthcomp.c:603-610) and accumulates the normalisation.  The source
+// continuum also writes its table for the primary spectrum (c_donthcomp,
+// donthcomp.c:640-793).
 // nthcomp_apply_kernel: the normalisation changes of the zones on their corner
 // weights and the source normalisation of the primary.
+#include <cmath>
+#include <vector>
+
 #include "relx_device.cuh"
 #include "relx_kernels.h"
 
 namespace relx {
 
-constexpr int kNthThreads = 128;
-constexpr int kNthMax = 900;
+constexpr int kNthThreads = 64;
+constexpr int kNthMaxJ = 899;  // the reference's largest grid index (donthcomp.c:360)
 
-struct NthSmem {
-  double x[kNthMax + 1];     // photon energies / m_e c^2, index 1..jmax+1
-  double c2[kNthMax];        // Cooper's coefficient, then E F_E (sptot), index j-1 -> j
-  double bet[kNthMax];       // escape probability per Thomson time
-  double dph[kNthMax];       // seed photon production rate
-  double a[kNthMax], b[kNthMax], c[kNthMax], d[kNthMax];
-  double red[kNthThreads / 32];
-  int jmax, jmaxth, ne_seed;
-};
-
-__device__ __forceinline__ double nth_lg10(double x) { return 0.43429448190325182765 * log(x); }
+static double lg10_h(double x) { return 0.43429448190325182765 * std::log(x); }
 
 // residuals of the multi-colour disk interpolation formula in 0.06 dex steps from E/T = 1e-3
 // (Mitsuda et al. 1984; the table of donthcomp.c:57-79)
-__constant__ float c_mcd_res[98] = {
-    9.6198382e-4f, .0010901181f, .0012310012f, .0013841352f, .0015481583f, .0017210036f, .0018988943f,
-    .002076939f, .0022484281f, .0024049483f, .0025366202f, .0026316255f, .0026774985f, .0026613059f,
-    .0025708784f, .0023962965f, .002130655f, .0017725174f, .0013268656f, 8.0657672e-4f, 2.3337584e-4f,
-    -3.6291778e-4f, -9.4443569e-4f, -.0014678875f, -.0018873741f, -.0021588493f, -.0022448371f, -.0021198179f,
-    -.0017754602f, -.0012246034f, -5.0414167e-4f, 3.2507078e-4f, .0011811065f, .0019673402f, .0025827094f,
-    .0029342526f, .0029517083f, .0026012166f, .0018959062f, 9.0128649e-4f, -2.6757144e-4f, -.0014567885f,
-    -.002492855f, -.0032079776f, -.0034678637f, -.0031988217f, -.0024080969f, -.001193624f, 2.6134145e-4f,
-    .0017117758f, .0028906898f, .0035614435f, .0035711778f, .0028921374f, .0016385898f, 4.9857464e-5f,
-    -.0015572671f, -.0028578151f, -.0035924212f, -.0036253044f, -.002975086f, -.0018044436f, -3.7796664e-4f,
-    .0010076215f, .0020937327f, .0027090854f, .0028031667f, .0024276576f, .0017175597f, 8.1030795e-4f,
-    -1.2592304e-4f, -9.4888491e-4f, -.0015544816f, -.0018831972f, -.0019203142f, -.0016905849f, -.0012487737f,
-    -6.6789911e-4f, -2.7079461e-5f, 5.9931935e-4f, .0011499748f, .0015816521f, .0018709224f, .0020129966f,
-    .0020184702f, .0019089181f, .0017122289f, .001458377f, .0011760717f, 8.9046768e-4f, 6.2190822e-4f,
-    3.8553762e-4f, 1.9155022e-4f, 4.5837109e-5f, -4.9177834e-5f, -9.3670762e-5f, -8.9622968e-5f,
-    -4.01538532e-5f};
+static const double kMcdRes[98] = {
+    9.6198382e-4, .0010901181, .0012310012, .0013841352, .0015481583, .0017210036, .0018988943, .002076939,
+    .0022484281, .0024049483, .0025366202, .0026316255, .0026774985, .0026613059, .0025708784, .0023962965,
+    .002130655, .0017725174, .0013268656, 8.0657672e-4, 2.3337584e-4, -3.6291778e-4, -9.4443569e-4,
+    -.0014678875, -.0018873741, -.0021588493, -.0022448371, -.0021198179, -.0017754602, -.0012246034,
+    -5.0414167e-4, 3.2507078e-4, .0011811065, .0019673402, .0025827094, .0029342526, .0029517083, .0026012166,
+    .0018959062, 9.0128649e-4, -2.6757144e-4, -.0014567885, -.002492855, -.0032079776, -.0034678637,
+    -.0031988217, -.0024080969, -.001193624, 2.6134145e-4, .0017117758, .0028906898, .0035614435, .0035711778,
+    .0028921374, .0016385898, 4.9857464e-5, -.0015572671, -.0028578151, -.0035924212, -.0036253044,
+    -.002975086, -.0018044436, -3.7796664e-4, .0010076215, .0020937327, .0027090854, .0028031667, .0024276576,
+    .0017175597, 8.1030795e-4, -1.2592304e-4, -9.4888491e-4, -.0015544816, -.0018831972, -.0019203142,
+    -.0016905849, -.0012487737, -6.6789911e-4, -2.7079461e-5, 5.9931935e-4, .0011499748, .0015816521,
+    .0018709224, .0020129966, .0020184702, .0019089181, .0017122289, .001458377, .0011760717, 8.9046768e-4,
+    6.2190822e-4, 3.8553762e-4, 1.9155022e-4, 4.5837109e-5, -4.9177834e-5, -9.3670762e-5, -8.9622968e-5,
+    -4.01538532e-5};
 
-// multi-colour disk integrand (donthcomp.c:52-103), FP32
-__device__ __forceinline__ float nth_mcdint_f(float et) {
-  const float gc[3] = {.078196667f, -1.066202f, 1.192418f};
-  const float gw[3] = {.5207874f, .513457f, .4077983f};
-  const float gn[3] = {.3728691f, .039775528f, .037766505f};
-  const float loget = log10f(et);
-  float pos = (loget + 3.0f) / .06f + 1.0f;  // log10(et) - log10(0.001), in 0.06 dex steps
+// multi-colour disk integrand (mcdint, donthcomp.c:52-103)
+static double mcdint_h(double et) {
+  static const double gc[3] = {.078196667, -1.066202, 1.192418};
+  static const double gw[3] = {.5207874, .513457, .4077983};
+  static const double gn[3] = {.3728691, .039775528, .037766505};
+  const double loget = lg10_h(et);
+  double pos = (loget - lg10_h(0.001)) / .06 + 1;
   const int j = (int) pos;
-  float resfact;
+  double resfact;
   if (j < 1) {
-    resfact = c_mcd_res[0];
+    resfact = kMcdRes[0];
   } else if (j >= 98) {
-    resfact = c_mcd_res[97];
+    resfact = kMcdRes[97];
   } else {
-    pos -= (float) j;
-    resfact = c_mcd_res[j - 1] * (1.0f - pos) + c_mcd_res[j] * pos;
+    pos -= j;
+    resfact = kMcdRes[j - 1] * (1 - pos) + kMcdRes[j] * pos;
   }
-  float gaufact = 1.0f;
-#pragma unroll
+  double gaufact = 1.0;
   for (int k = 0; k < 3; k++) {
-    const float zz = (loget - gc[k]) / gw[k];
-    gaufact += gn[k] * expf(-zz * zz * 0.5f);
+    const double zz = (loget - gc[k]) / gw[k];
+    gaufact += gn[k] * std::exp(-zz * zz / 2.);
   }
-  return powf(et * 1000.0f, -2.0f / 3.0f) * 193.21556f * (powf(et, 1.663753f) * .52876731f + 1.0f) * expf(-et) *
-         gaufact * (resfact + 1.0f);
+  return std::pow(et / .001, -.66666666666666663) * 193.21556 * (std::pow(et, 1.663753) * .52876731 + 1.) *
+         std::exp(-et) * gaufact * (resfact + 1.);
 }
 
-// Comptonized spectrum of one (theta, gamma): fills m.x[1..jmax+1] and m.c2[j] = sptot[j] for
-// j = 1..jmax (sptot[jmax] = 0, as the reference's cleared array), returns jmax, or 0 when kTe gives
-// fewer than 4 grid points (kTe <= 0 or far below the seed temperature): nothing is computed then
-__device__ int nth_compton(NthSmem &m, double tempbb, double theta, double gamma) {
-  const int tid = threadIdx.x;
-  const double d1 = gamma + .5;
-  const double tautom = sqrt(3. / (theta * (d1 * d1 - 2.25)) + 2.25) - 1.5;
-  const double delta = .02, deltal = delta * log(10.);
-  const double xmin = tempbb * 1e-4, xmax = theta * 40.;
-  if (tid == 0) {
-    int jmax = (int) (nth_lg10(xmax / xmin) / delta) + 1;
-    if (jmax > 899) jmax = 899;
-    int jmaxth = (int) (nth_lg10(tempbb * 50. / xmin) / delta);
-    if (jmaxth > 900) jmaxth = 900;
-    if (jmaxth > jmax) jmaxth = jmax;
-    m.jmax = jmax;
-    m.jmaxth = jmaxth;
-    m.ne_seed = jmaxth - 2;
+static float2 ff_h(double d) {
+  const float hi = (float) d;
+  return make_float2(hi, (float) (d - (double) hi));
+}
+
+int nth_grid_build(const std::vector<double> &co, double band_lo, double band_hi, NthGrid &G) {
+  const double tempbb = .05 / 511., delta = .02, deltal = delta * std::log(10.);
+  const double xmin = tempbb * 1e-4;
+  std::vector<double> x(RELX_NTH_N + 3, 0.0), seed(RELX_NTH_N + 2, 0.0);
+  for (int j = 1; j <= RELX_NTH_N + 2; j++) x[j] = xmin * std::pow(10., (j - 1) * delta);
+  // seed photons: the disk blackbody per bin of the grid's geometric midpoints (xsdskb,
+  // donthcomp.c:137-191, five-point Gauss-Legendre), as a rate per unit energy
+  int jmaxth = (int) (lg10_h(tempbb * 50. / xmin) / delta);
+  if (jmaxth > 900) jmaxth = 900;
+  const int ne = jmaxth - 2;
+  const double tin = tempbb * 511.;
+  static const double gw5[5] = {.236926885, .47862867, .568888888, .47862867, .236926885};
+  static const double gx5[5] = {-.906179846, -.53846931, 0., .53846931, .906179846};
+  for (int i = 1; i <= ne; i++) {
+    const double elo = std::sqrt(x[i] * x[i + 1]) * 511., ehi = std::sqrt(x[i + 1] * x[i + 2]) * 511.;
+    const double xn = (ehi - elo) / 2.f, xh = xn + elo;
+    double acc = 0.;
+    for (int k = 0; k < 5; k++) acc += gw5[k] * (mcdint_h((xn * gx5[k] + xh) / tin) * tin * tin * 1. / 361.);
+    seed[i] = acc * xn * 511. / (ehi - elo);
   }
-  __syncthreads();
-  const int jmax = m.jmax, ne = m.ne_seed;
-  if (!(jmax >= 4 && jmax <= 899)) return 0;  // block-uniform
-  for (int j = 1 + tid; j <= jmax + 1; j += kNthThreads) m.x[j] = xmin * exp((double) (j - 1) * deltal);
-  for (int j = tid; j < kNthMax; j += kNthThreads) m.dph[j] = 0.0;
-  __syncthreads();
-  // Cooper's coefficient and the Klein-Nishina escape probability (donthcomp.c:511-585)
-  const int jnr = min((int) (nth_lg10(.1 / xmin) / delta + 1), jmax - 1);
-  const int jrel = min((int) (nth_lg10(1. / xmin) / delta + 1), jmax);
-  const double xnr = m.x[jnr], xr = m.x[jrel];
-  for (int j = 1 + tid; j <= jmax; j += kNthThreads) {
-    const double w = m.x[j], w1 = sqrt(m.x[j] * m.x[j + 1]);
-    const double w12 = w1 * w1;
-    m.c2[j - 1] = w12 * w12 / (w1 * 4.6 + 1. + w1 * 1.1 * w1);
-    double rel;
+  seed[0] = seed[1];
+  // normalisation weights: p(E) at the coarse edges is linear in the table (interpolation of
+  // donthcomp.c:768-786, the reference's search over x * 511), the bin photon flux is the
+  // trapezoid of p / E^2, weighted by the bin centre inside the band
+  const int nb = (int) co.size() - 1;
+  std::vector<double> W(co.size(), 0.0), Gw(RELX_NTH_N + 2, 0.0);
+  for (int b = 0; b < nb; b++) {
+    const bool in_band = co[b] >= band_lo && co[b] <= band_hi;
+    if (!in_band) continue;
+    const double em = 0.5 * (co[b] + co[b + 1]), hw = .5 * (co[b + 1] - co[b]) * em;
+    W[b] += hw / (co[b] * co[b]);
+    W[b + 1] += hw / (co[b + 1] * co[b + 1]);
+  }
+  for (size_t k = 0; k < co.size(); k++) {
+    if (W[k] == 0.0) continue;
+    int j = 1;
+    while (j <= RELX_NTH_N - 1 && x[j] * 511. < co[k]) ++j;
+    if (j == 1) {
+      Gw[1] += W[k];
+    } else {
+      const int jl = j - 1;
+      const double w = (co[k] / 511. - x[jl]) / (x[jl + 1] - x[jl]);
+      Gw[jl] += W[k] * (1 - w);
+      Gw[jl + 1] += W[k] * w;
+    }
+  }
+  for (int j = 1; j <= RELX_NTH_N; j++) {
+    const double w = x[j], w1 = std::sqrt(x[j] * x[j + 1]);
+    const double c2 = std::pow(w1, 4.) / (w1 * 4.6 + 1. + w1 * 1.1 * w1);  // Cooper (donthcomp.c:511-521)
+    double rel;                                                           // (donthcomp.c:557-570)
     if (w <= .05) {
       rel = 1 - w * 2 + w * 26 * w / 5;
     } else {
-      const double z1 = (w + 1) / (w * (w * w)), z2 = w * 2 + 1, z3 = log(z2), z4 = w * 2 * (w + 1) / z2,
+      const double z1 = (w + 1) / (w * (w * w)), z2 = w * 2 + 1, z3 = std::log(z2), z4 = w * 2 * (w + 1) / z2,
                    z5 = z3 / 2 / w, z6 = (w * 3 + 1) / z2 / z2;
       rel = (z1 * (z4 - z3) + z5 - z6) * .75;
     }
-    const double taukn = tautom * rel;
-    double bet;
-    if (j <= jnr - 1) bet = 1 / tautom / (taukn / 3 + 1);
-    else if (j <= jrel) bet = 1 / tautom / (taukn / 3 * (1 - (w - xnr) / (xr - xnr)) + 1);
-    else bet = 1 / tautom;
-    m.bet[j - 1] = bet;
+    NthPoint &P = G.p[j];
+    P.cd = ff_h(c2 / deltal);
+    P.iw = ff_h(1. / (deltal * w1));
+    P.rel3 = ff_h(rel / 3.);
+    P.x3 = ff_h(w * w * w);
+    P.xd = ff_h(w * ((j - 1 <= ne) ? seed[j - 1] : 0.0));
+    P.x4 = ff_h(w * w * w * w);
+    P.g = ff_h(Gw[j]);
+    P.x = ff_h(w);
   }
-  // seed photons: the disk-blackbody spectrum per bin (xsdskb, donthcomp.c:137-191), FP32
-  {
-    const float gw5[5] = {.236926885f, .47862867f, .568888888f, .47862867f, .236926885f};
-    const float gx5[5] = {-.906179846f, -.53846931f, 0.f, .53846931f, .906179846f};
-    const float tin = (float) (tempbb * 511.);
-    for (int i = 1 + tid; i <= ne; i += kNthThreads) {
-      const double elo = sqrt(m.x[i] * m.x[i + 1]) * 511., ehi = sqrt(m.x[i + 1] * m.x[i + 2]) * 511.;
-      const float xn = (float) ((ehi - elo) / 2.), xh = xn + (float) elo;
-      float acc = 0.0f;
-#pragma unroll
-      for (int k = 0; k < 5; k++) {
-        const float e = xn * gx5[k] + xh;
-        acc += gw5[k] * (nth_mcdint_f(e / tin) * tin * tin / 361.0f);
-      }
-      m.dph[i] = (double) (acc * xn) * 511. / (ehi - elo);
-    }
-  }
-  __syncthreads();
-  if (tid == 0) m.dph[0] = m.dph[1];
-  __syncthreads();
-  // tridiagonal coefficients a u(j+1) + b u(j) + c u(j-1) = d (thermlc, donthcomp.c:194-280)
-  const double c20 = tautom / deltal, td = theta / deltal;
-  for (int j = 2 + tid; j <= jmax - 1; j += kNthThreads) {
-    const double w1 = sqrt(m.x[j] * m.x[j + 1]), w2 = sqrt(m.x[j - 1] * m.x[j]);
-    m.a[j - 1] = -c20 * m.c2[j - 1] * (td / w1 + .5);
-    const double t1 = -c20 * m.c2[j - 1] * (.5 - td / w1);
-    const double t2 = c20 * m.c2[j - 2] * (td / w2 + .5);
-    const double xj = m.x[j];
-    const double t3 = xj * xj * xj * (tautom * m.bet[j - 1]);
-    m.b[j - 1] = t1 + t2 + t3;
-    m.c[j - 1] = c20 * m.c2[j - 2] * (.5 - td / w2);
-    m.d[j - 1] = xj * m.dph[j - 1];
-  }
-  __syncthreads();
-  if (tid == 0) {  // Thomas algorithm: gam in a, alp in b, g then u in d
-    const double x32 = sqrt(m.x[1] * m.x[2]);
-    const double aa = (td / x32 + .5) / (td / x32 - .5);
-    double alp = m.b[1] + m.c[1] * aa;
-    m.a[1] = m.a[1] / alp;
-    m.d[1] = m.d[1] / alp;
-    for (int j = 3; j <= jmax - 1; j++) {
-      alp = m.b[j - 1] - m.c[j - 1] * m.a[j - 2];
-      const double ia = 1.0 / alp;
-      m.a[j - 1] = m.a[j - 1] * ia;
-      m.d[j - 1] = (m.d[j - 1] - m.c[j - 1] * m.d[j - 2]) * ia;
-    }
-    // u(jmax) = 0: the last row is the same recurrence
-    m.d[jmax - 1] = 0.0;
-    for (int jj = jmax - 2; jj >= 2; jj--) m.d[jj - 1] = m.d[jj - 1] - m.a[jj - 1] * m.d[jj];
-    m.d[0] = aa * m.d[1];
-  }
-  __syncthreads();
-  // E F_E of the escaping photons (donthcomp.c:603-610); c2 is free now
-  for (int j = 1 + tid; j <= jmax; j += kNthThreads) {
-    const double xj = m.x[j];
-    const double dphesc = xj * xj * m.d[j - 1] * m.bet[j - 1] * tautom;
-    m.c2[j] = (j <= jmax - 1) ? dphesc * (xj * xj) : 0.0;
-  }
-  __syncthreads();
-  return jmax;
+  G.p[0] = NthPoint{};
+  for (int j = 0; j <= RELX_NTH_N + 1; j++) G.x[j] = x[j];
+  G.jnr0 = (int) (lg10_h(.1 / xmin) / delta + 1);
+  G.jrel0 = (int) (lg10_h(1. / xmin) / delta + 1);
+  const double xx = 1 / (1 / (1. / 511.));
+  int ih = 2;
+  while (ih < kNthMaxJ && xx > x[ih]) ++ih;
+  G.ih0 = ih;
+  return 0;
 }
 
-// continuum k of set: k = 0 the source (kTe), k = z + 1 zone z (kTe times the zone's energy shift);
-// params: the xillver model reads Gamma and kTe from its parameters (p[0], p[2])
-__global__ void __launch_bounds__(kNthThreads) nthcomp_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
+__device__ __forceinline__ double nth_lg10(double x) { return 0.43429448190325182765 * log(x); }
+
+// reciprocal in float-float: the float reciprocal and one Newton step
+__device__ __forceinline__ float2 ff_rcp(float2 a) {
+  const float r = __frcp_rn(a.x);
+  const float p = __fmul_rn(a.x, r);
+  const float pe = fmaf(a.x, r, -p);
+  const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p), pe), __fmul_rn(a.y, r));
+  return qts(r, __fmul_rn(r, e));
+}
+
+// tautom times the escape probability at point j (donthcomp.c:572-585): 1 / (taukn / 3 + 1) below
+// the non-relativistic bound, the same with taukn tapered linearly up to the relativistic one, 1 above
+__device__ __forceinline__ float2 nth_bt(const NthPoint &P, int j, float2 tau, int jnr, int jrel, float2 xnr,
+                                         float2 invdx) {
+  if (j > jrel) return make_float2(1.0f, 0.0f);
+  float2 y = ff_mul(tau, P.rel3);
+  if (j >= jnr) y = ff_mul(y, ff_addf(ff_neg(ff_mul(ff_add(P.x, ff_neg(xnr)), invdx)), 1.0f));
+  return ff_rcp(ff_addf(y, 1.0f));
+}
+
+// continuum c of the launch: set = c / per, k = c % per; k = 0 the source (kTe), k = z + 1 zone z
+// (kTe times the zone's energy shift).  params: the xillver model reads Gamma and kTe from its
+// parameters (p[0], p[2]).  scr: [point][continuum] with stride ncont_all, this launch's
+// continua from c_off.
+__global__ void __launch_bounds__(kNthThreads) nthcomp_kernel(const NthGrid *__restrict__ G,
+                                                              const RelxSetIn *__restrict__ sin,
                                                               const RelxSetState *__restrict__ sst, bool params,
-                                                              int nq, double *__restrict__ qout,
-                                                              NthTable *__restrict__ tabs) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  NthSmem &m = *reinterpret_cast<NthSmem *>(smem_raw);
-  const int k = blockIdx.x, set = blockIdx.y, tid = threadIdx.x;
+                                                              int per, int n_sets, int nq, double *__restrict__ qout,
+                                                              NthTable *__restrict__ tabs, float4 *__restrict__ scr,
+                                                              int64_t ncont_all, int64_t c_off) {
+  const int64_t c = (int64_t) blockIdx.x * kNthThreads + threadIdx.x;
+  if (c >= (int64_t) n_sets * per) return;
+  const int set = (int) (c / per), k = (int) (c - (int64_t) set * per);
   double gam, kte;
   if (params) {
-    if (k > 0) return;
     gam = sin[set].p[0];
     kte = sin[set].p[2];
   } else {
@@ -219,44 +216,88 @@ __global__ void __launch_bounds__(kNthThreads) nthcomp_kernel(RelxTables tab, co
     gam = s.gam;
     kte = s.ect_src * shift;
   }
-  const int jmax = nth_compton(m, .05 / 511., kte / 511., gam);
-  if (jmax == 0) {  // no spectrum: a non-finite normalisation marks the set as failed
-    if (tid == 0) {
-      qout[(size_t) set * nq + k] = __longlong_as_double(0x7ff8000000000000ll);
-      if (k == 0) tabs[set].n = 0;
-    }
+  double *q = qout + (size_t) set * nq + k;
+  NthTable *T = (k == 0) ? &tabs[set] : nullptr;
+  // grid length and scalars (donthcomp.c:320-375); a kTe that leaves fewer than 4 points (kTe <= 0 or
+  // far below the seed temperature) has no spectrum: a non-finite normalisation marks the set
+  const double tempbb = .05 / 511., theta = kte / 511.;
+  const double d1 = gam + .5;
+  const double tautom = sqrt(3. / (theta * (d1 * d1 - 2.25)) + 2.25) - 1.5;
+  const double xmin = tempbb * 1e-4, xmax = theta * 40.;
+  const double r = nth_lg10(xmax / xmin) / .02;
+  if (!(r >= 3.0)) {
+    *q = __longlong_as_double(0x7ff8000000000000ll);
+    if (T) T->n = 0;
     return;
   }
-  const double *x = m.x, *sp = m.c2;
-  // normalisation on the coarse grid (calcNormWrtXillverTableSpec, Xillspec.cpp:179-205): the
-  // E F_E table at the 501 edges in FP32, the per-bin photon flux times the bin centre summed in FP64
-  const double normfac = nth_normfac(x, sp, jmax, 1.0);
-  double part = 0.0;
-  for (int bn = tid; bn < RELX_NCOARSE; bn += kNthThreads) {
-    const double e0 = tab.coarse_e[bn], e1 = tab.coarse_e[bn + 1];
-    const float4 t = tab.coarse_t[bn];  // zero centre weight outside the normalisation band
-    if (t.z == 0.0f) continue;
-    const double p0 = nth_prim_at(x, sp, jmax, e0, 1.0), p1 = nth_prim_at(x, sp, jmax, e1, 1.0);
-    const double ph = (p1 / (e1 * e1) + p0 / (e0 * e0)) * .5 * (e1 - e0) * normfac;
-    part += ph * ((double) t.z + (double) t.w);
+  const int jmax = r >= (double) kNthMaxJ ? kNthMaxJ : min((int) r + 1, kNthMaxJ);
+  const int jnr = min(G->jnr0, jmax - 1), jrel = min(G->jrel0, jmax);
+  const float2 tau = ff_from_double(tautom), th = ff_from_double(theta);
+  const float2 xnr = G->p[jnr].x, invdx = ff_from_double(1.0 / (G->x[jrel] - G->x[jnr]));
+  float4 *sc = scr + c_off + c;
+
+  // forward sweep: a u(j+1) + b u(j) + c u(j-1) = d for j = 2 .. jmax - 1, u(1) = aa u(2), u(jmax) = 0
+  // a_j = -A_j, c_j = T_{j-1}, b_j = A_{j-1} - T_j + x_j^3 bt_j with
+  // A_j = tautom cd_j (theta iw_j + 1/2), T_j = tautom cd_j (1/2 - theta iw_j)
+  const float2 u1 = ff_mul(th, G->p[1].iw);
+  const float2 aa = ff_mul(ff_addf(u1, .5f), ff_rcp(ff_addf(u1, -.5f)));
+  float2 Ap, Tp;
+  {
+    const float2 P1 = ff_mul(tau, G->p[1].cd);
+    Ap = ff_mul(P1, ff_addf(u1, .5f));
+    Tp = ff_mul(P1, ff_addf(ff_neg(u1), .5f));
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-  if ((tid & 31) == 0) m.red[tid >> 5] = part;
-  __syncthreads();
-  if (tid == 0) {
-    double sum = 0.0;
-    for (int w = 0; w < kNthThreads / 32; w++) sum += m.red[w];
-    qout[(size_t) set * nq + k] = sum * 1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi);
-  }
-  if (k == 0) {  // the source's table for the primary spectrum
-    NthTable &T = tabs[set];
-    for (int j = tid; j <= jmax + 1; j += kNthThreads) {
-      T.x[j] = x[j];
-      T.sp[j] = (j >= 1 && j <= jmax) ? sp[j] : 0.0;
+  float2 gm = make_float2(0.f, 0.f), dd = make_float2(0.f, 0.f);
+  for (int j = 2; j <= jmax - 1; j++) {
+    const NthPoint P = G->p[j];
+    const float2 u = ff_mul(th, P.iw);
+    const float2 Pj = ff_mul(tau, P.cd);
+    const float2 A = ff_mul(Pj, ff_addf(u, .5f)), Tj = ff_mul(Pj, ff_addf(ff_neg(u), .5f));
+    const float2 bt = nth_bt(P, j, tau, jnr, jrel, xnr, invdx);
+    const float2 b = ff_add(ff_add(Ap, ff_neg(Tj)), ff_mul(P.x3, bt));
+    float2 alp, num;
+    if (j == 2) {
+      alp = ff_add(b, ff_mul(Tp, aa));
+      num = P.xd;
+    } else {
+      alp = ff_add(b, ff_neg(ff_mul(Tp, gm)));
+      num = ff_add(P.xd, ff_neg(ff_mul(Tp, dd)));
     }
-    if (tid == 0) T.n = jmax;
+    const float2 ia = ff_rcp(alp);
+    gm = ff_mul(ff_neg(A), ia);
+    dd = ff_mul(num, ia);
+    sc[(size_t) j * ncont_all] = make_float4(gm.x, gm.y, dd.x, dd.y);
+    Ap = A;
+    Tp = Tj;
   }
+  // back sweep: u, E F_E = x^4 u bt (donthcomp.c:603-610), the normalisation sum and the table
+  const int ih = min(G->ih0, jmax), il = ih - 1;
+  float2 un = make_float2(0.f, 0.f), qs = make_float2(0.f, 0.f), s_il = un, s_ih = un;
+  for (int j = jmax - 1; j >= 1; j--) {
+    float2 uj;
+    if (j >= 2) {
+      const float4 v = sc[(size_t) j * ncont_all];
+      uj = ff_add(make_float2(v.z, v.w), ff_neg(ff_mul(make_float2(v.x, v.y), un)));
+    } else {
+      uj = ff_mul(aa, un);
+    }
+    const NthPoint P = G->p[j];
+    const float2 sp = ff_mul(ff_mul(P.x4, uj), nth_bt(P, j, tau, jnr, jrel, xnr, invdx));
+    qs = ff_add(qs, ff_mul(P.g, sp));
+    if (j == il) s_il = sp;
+    if (j == ih) s_ih = sp;
+    if (T) T->sp[j] = ff_to_double(sp);
+    un = uj;
+  }
+  if (T) {
+    T->sp[jmax] = 0.0;
+    T->n = jmax;
+  }
+  // 1 / E F_E at the 1 keV point (donthcomp.c:617-638, 754-758) and the normalisation on the coarse grid
+  const double xx = 1 / (1 / (1. / 511.));
+  const double sil = ff_to_double(s_il), sih = ff_to_double(s_ih);
+  const double normfac = 1 / (sil + (sih - sil) * (xx - G->x[il]) / (G->x[ih] - G->x[il]));
+  *q = ff_to_double(qs) * normfac * (1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi));
 }
 
 // normalisation changes of the zones on their corner weights, source normalisation of the primary
@@ -282,18 +323,19 @@ __global__ void nthcomp_apply_kernel(RelxSetState *__restrict__ sst, const doubl
   if (tid == 0) s.src_norm = 1.0 / q0;
 }
 
-size_t nthcomp_smem_bytes() { return sizeof(NthSmem); }
-
-cudaError_t nthcomp_set_smem() {
-  return cudaFuncSetAttribute(nthcomp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sizeof(NthSmem));
+size_t nthcomp_scratch_bytes(int n_sets, int nza, bool params) {
+  return (size_t) n_sets * (params ? 1 : nza + 1) * (kNthMaxJ + 1) * sizeof(float4);
 }
 
 cudaError_t launch_nthcomp(cudaStream_t s, const RelxTables &tab, const RelxSetIn *sin, RelxSetState *sst, int n_sets,
-                           int nza, bool params, double *q, NthTable *tabs, RelxZoneCorners *zcor) {
+                           int nza, bool params, double *q, NthTable *tabs, RelxZoneCorners *zcor, float4 *scr,
+                           int64_t ncont_all, int64_t c_off) {
   if (n_sets <= 0) return cudaSuccess;
   const int nq = RELX_NZMAX + 1;
-  nthcomp_kernel<<<dim3(params ? 1 : nza + 1, n_sets), kNthThreads, sizeof(NthSmem), s>>>(tab, sin, sst, params, nq,
-                                                                                        q, tabs);
+  const int per = params ? 1 : nza + 1;
+  const int64_t ncont = (int64_t) n_sets * per;
+  nthcomp_kernel<<<(unsigned) ((ncont + kNthThreads - 1) / kNthThreads), kNthThreads, 0, s>>>(
+      tab.nth_grid, sin, sst, params, per, n_sets, nq, q, tabs, scr, ncont_all, c_off);
   if (!params && zcor) nthcomp_apply_kernel<<<n_sets, 128, 0, s>>>(sst, q, nq, zcor);
   return cudaGetLastError();
 }

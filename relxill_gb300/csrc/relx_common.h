@@ -88,6 +88,7 @@ enum RelxStatus {
 #define RELX_EMIS_LP 2
 
 // Device-resident tables (uploaded once).  All arrays are device pointers.
+struct NthGrid;
 struct RelxTables {
   // relline table (reltable.h:24-48): [a][mu0][r] and [a][mu0][r][g] (float4 = trff1,trff2,cosne1,cosne2)
   int rel_na, rel_nmu0, rel_nr, rel_ng;
@@ -135,6 +136,8 @@ struct RelxTables {
   const double *rr_rlo, *rr_rhi;  // [nspin][RELX_RR_NR]
   const double *rr_tfr;      // [nspin][RELX_RR_NR][RELX_RR_NR], row = incident bin, column = emitting bin
   const float4 *rr_g;        // [nspin][NR][NR][NG]: frac_g, g, log2 g, 1 if |g - 1| > 1e-3 else 0
+  // nthcomp photon grid of the Cp models (nthcomp.cu)
+  const NthGrid *nth_grid;
 };
 
 // per-set inputs
@@ -173,10 +176,23 @@ struct RelxSetState {
   double zshift[RELX_NZMAX];              // energy shift source -> disk of each zone (Ecut / kTe factor)
 };
 
-// nthcomp (nthcomp.cu): E F_E table of a set's source continuum, x[1..n+1] and sp[1..n]
+// nthcomp (nthcomp.cu): the photon grid of the Kompaneets solve.  The seed temperature is fixed
+// (0.05 keV), so the grid and every quantity on it that does not depend on kTe or Gamma are computed
+// once: per point j (float-float) Cooper's coefficient / deltal, 1 / (deltal sqrt(x_j x_j+1)), the
+// Klein-Nishina factor / 3, x^3, x times the seed photon rate, x^4, the normalisation weight of the
+// point on the 500-bin coarse grid, and x itself.
+#define RELX_NTH_N 901
+struct __align__(16) NthPoint {
+  float2 cd, iw, rel3, x3, xd, x4, g, x;
+};
+struct NthGrid {
+  NthPoint p[RELX_NTH_N + 1];  // j = 1..901
+  double x[RELX_NTH_N + 2];    // x_j (FP64), j = 1..902
+  int jnr0, jrel0, ih0, pad_;  // region bounds of the escape probability, index of the 1 keV point
+};
+// E F_E table of a set's source continuum, sp[1..n] on the grid's x
 struct NthTable {
-  double x[901];
-  double sp[901];
+  double sp[RELX_NTH_N];
   int n;
   int pad_[3];
 };

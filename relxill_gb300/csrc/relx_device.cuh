@@ -304,8 +304,9 @@ __device__ __forceinline__ double nth_normfac(const double *x, const double *sp,
 
 // photon flux of the nthcomp table on the bin [e0, e1] in the frame shifted by zp1 = 1 + z
 // (c_donthcomp's last loop, donthcomp.c:788-792); normfac from nth_normfac at the same shift
-__device__ __forceinline__ double nth_bin(const NthTable &T, double e0, double e1, double zp1, double normfac) {
-  const double p0 = nth_prim_at(T.x, T.sp, T.n, e0, zp1), p1 = nth_prim_at(T.x, T.sp, T.n, e1, zp1);
+__device__ __forceinline__ double nth_bin(const double *x, const NthTable &T, double e0, double e1, double zp1,
+                                          double normfac) {
+  const double p0 = nth_prim_at(x, T.sp, T.n, e0, zp1), p1 = nth_prim_at(x, T.sp, T.n, e1, zp1);
   return (p1 / (e1 * e1) + p0 / (e0 * e0)) * .5 * (e1 - e0) * normfac;
 }
 

@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "relx_common.h"
 
 namespace relx {
@@ -59,14 +61,20 @@ cudaError_t launch_xill_ingest(cudaStream_t s, const XillIngest &g, const unsign
 cudaError_t launch_xill_corner_flux(cudaStream_t s, const double *rowflux, const double *incl_w, int n_incl,
                                     int64_t n_corners, double *fcorr);
 
-size_t nthcomp_smem_bytes();
-cudaError_t nthcomp_set_smem();
+// the nthcomp photon grid and its per-point constants (host, FP64); co: the coarse normalisation
+// grid's edges, bins starting inside [band_lo, band_hi] count
+int nth_grid_build(const std::vector<double> &co, double band_lo, double band_hi, NthGrid &G);
+// scratch of launch_nthcomp for n_sets sets (float4 per grid point and continuum)
+size_t nthcomp_scratch_bytes(int n_sets, int nza, bool params);
 // per set: the normalisation (calcNormWrtXillverTableSpec) of the source continuum (q[set][0]) and of
 // every zone's (q[set][z + 1]), q holding RELX_NZMAX + 1 values per set, and the source's table;
 // then the zones' normalisation changes on their corner weights (zcor) and the source normalisation.
 // params: the xillver model, Gamma and kTe from the parameters, the source continuum only.
+// scr: scratch of nthcomp_scratch_bytes for the whole batch, ncont_all continua per grid point,
+// this launch's continua starting at c_off.
 cudaError_t launch_nthcomp(cudaStream_t s, const RelxTables &tab, const RelxSetIn *sin, RelxSetState *sst, int n_sets,
-                           int nza, bool params, double *q, NthTable *tabs, RelxZoneCorners *zcor);
+                           int nza, bool params, double *q, NthTable *tabs, RelxZoneCorners *zcor, float4 *scr,
+                           int64_t ncont_all, int64_t c_off);
 
 // the xillver model: one CTA per set, writes the flux and the status fields of the set state
 size_t xillver_model_smem_bytes(int n_ener, int n_ener_pad);

@@ -113,13 +113,13 @@ struct Tables {
   RelxTables dcp{};     // d with the xillver fields of the nthcomp table (valid if has_cp)
   bool has_cp = false;
   DevBuf rr_spin, rr_rlo, rr_rhi, rr_tfr, rr_g;
-  DevBuf conv_e, conv_eff, conv_inv_emid, conv_cf, conv_cw, coarse_e, coarse_t;
+  DevBuf conv_e, conv_eff, conv_inv_emid, conv_cf, conv_cw, coarse_e, coarse_t, nth_grid;
   size_t bytes_total = 0;
   bool loaded = false;
   void release() {
     for (DevBuf *b : {&rel_a, &rel_mu0, &rel_r, &rel_gmin, &rel_gmax, &rel_tc, &lp_a, &lp_h, &lp_rad, &lp_intens,
                       &lp_del, &lp_delinc, &rr_spin, &rr_rlo, &rr_rhi, &rr_tfr, &rr_g, &conv_e, &conv_eff, &conv_inv_emid, &conv_cf,
-                      &conv_cw, &coarse_e, &coarse_t})
+                      &conv_cw, &coarse_e, &coarse_t, &nth_grid})
       b->release();
     x.release();
     xcp.release();
@@ -623,6 +623,11 @@ static int load_tables(const std::string &dir, Tables &T) {
   T.d.conv_band_hi = band_hi;
   T.d.coarse_e = T.coarse_e.as<double>();
   T.d.coarse_t = T.coarse_t.as<float4>();
+  {  // the nthcomp photon grid of the Cp models
+    std::vector<NthGrid> g(1);
+    if ((st = nth_grid_build(co, RELX_EMIN_NORM, RELX_EMAX_NORM, g[0])) || (st = upload(T.nth_grid, g))) return st;
+    T.d.nth_grid = T.nth_grid.as<NthGrid>();
+  }
   // the nthcomp descriptor: everything of d but the xillver fields
   if (has_cp) {
     RelxTables c = T.d;
@@ -691,11 +696,11 @@ static int zones_for(int model, int ion_grad_type, int envn) {
 
 struct Workspace {
   DevBuf setin, st, rad, corners, zcorners, line_e, prof, dist, tsum, xill, cout, user_e, user_f, flux, sflag,
-      status, err, params, eoff, igt, igi, order, cslot, nthq, nthtab;
+      status, err, params, eoff, igt, igi, order, cslot, nthq, nthtab, nthscr;
   void release() {
     for (DevBuf *b : {&setin, &st, &rad, &corners, &zcorners, &line_e, &prof, &dist, &tsum, &xill, &cout, &user_e,
                       &user_f, &flux, &sflag, &status, &err, &params, &eoff, &igt, &igi, &order, &cslot, &nthq,
-                      &nthtab})
+                      &nthtab, &nthscr})
       b->release();
   }
 };
@@ -747,7 +752,6 @@ static int set_kernel_attrs(const Tables &T) {
   RELX_CUDA(xillver_set_smem(T.d.x_nincl));
   RELX_CUDA(xillver_model_set_smem(T.d.x_nener, T.d.x_nener_pad));
   if (T.has_cp) RELX_CUDA(xillver_model_set_smem(T.dcp.x_nener, T.dcp.x_nener_pad));
-  RELX_CUDA(nthcomp_set_smem());
   RELX_CUDA(cudaFuncSetAttribute(conv_zone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
   RELX_CUDA(cudaFuncSetAttribute(relconv_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
   RELX_CUDA(cudaFuncSetAttribute(finalize_relxill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) fin_smem_bytes()));
@@ -875,8 +879,9 @@ static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b,
       (st = W.sflag.reserve(S * sizeof(int))) || (st = W.status.reserve(S * sizeof(int))) ||
       (st = W.err.reserve(sizeof(int))) || (st = W.cslot.reserve(S * sizeof(int))))
     return st;
-  if (relx_is_cp(b.model) && ((st = W.nthq.reserve(S * (RELX_NZMAX + 1) * sizeof(double))) ||
-                              (st = W.nthtab.reserve(S * sizeof(NthTable)))))
+  if (relx_is_cp(b.model) &&
+      ((st = W.nthq.reserve(S * (RELX_NZMAX + 1) * sizeof(double))) || (st = W.nthtab.reserve(S * sizeof(NthTable))) ||
+       (st = W.nthscr.reserve(nthcomp_scratch_bytes((int) S, (int) nza, kind == RELX_XILLVER)))))
     return st;
   if (kind == RELX_XILLVER) return 0;  // no line profile, no convolution
   if ((st = W.rad.reserve(S * sizeof(RelxRadial))) || (st = W.dist.reserve(S * nza * RELX_MAX_INCL * sizeof(float))) ||
@@ -928,7 +933,8 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   if (kind == RELX_XILLVER) {
     if (cp) {
       ProfScope ps(PK_NTH, s);
-      RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, 1, true, nthq, ntab, nullptr));
+      RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, 1, true, nthq, ntab, nullptr, W.nthscr.as<float4>(),
+                               (int64_t) b.n_sets, (int64_t) base));
     }
     {
       ProfScope ps(PK_XILL, s);
@@ -946,7 +952,8 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   }
   if (cp) {  // the nthcomp continua of the source and the zones, their normalisations on the corner weights
     ProfScope ps(PK_NTH, s, 2);
-    RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, b.nza, false, nthq, ntab, zcor));
+    RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, b.nza, false, nthq, ntab, zcor, W.nthscr.as<float4>(),
+                             (int64_t) b.n_sets * (b.nza + 1), (int64_t) base * (b.nza + 1)));
   }
   if (cached) {
     ProfScope ps(PK_SETUP, s, 2);
@@ -1365,13 +1372,14 @@ size_t batch_device_bytes(int model, int n_sets, int64_t n_edges, int nza) {
     return (sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(int) * 4 +
             (relx_is_cp(model) ? sizeof(NthTable) + sizeof(double) * (RELX_NZMAX + 1) : 0)) *
                (size_t) n_sets +
-           sizeof(double) * 2 * (size_t) n_edges;
+           (relx_is_cp(model) ? nthcomp_scratch_bytes(n_sets, 1, true) : 0) + sizeof(double) * 2 * (size_t) n_edges;
   size_t per_set = sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(RelxRadial) + sizeof(int) * 4 +
                    sizeof(float) * nza * RELX_MAX_INCL + sizeof(double) * (RELX_NCONV / kSumBinsH) * nza;
   if (kind != RELX_RELLINE) per_set += 2 * sizeof(float) * (size_t) nza * RELX_NCONV;
   if (relx_is_relxill(kind)) per_set += sizeof(RelxCorners) + sizeof(float) * (size_t) nza * 4096;
   if (relx_is_cp(model)) per_set += sizeof(RelxZoneCorners) + sizeof(NthTable) + sizeof(double) * (RELX_NZMAX + 1);
-  return per_set * (size_t) n_sets + sizeof(double) * 3 * (size_t) n_edges;
+  return per_set * (size_t) n_sets + sizeof(double) * 3 * (size_t) n_edges +
+         (relx_is_cp(model) ? nthcomp_scratch_bytes(n_sets, nza, false) : 0);
 }
 
 int cache_configure(int slots) {

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kXmodThreads) xillver_model_kernel(RelxTables 
   if (cp) {
     if (tid == 0) {
       qsum_s = nthq[(size_t) set * (RELX_NZMAX + 1)];
-      nth_norm_s = nth[set].n > 0 ? nth_normfac(nth[set].x, nth[set].sp, nth[set].n, 1.0) : 0.0;
+      nth_norm_s = nth[set].n > 0 ? nth_normfac(tab.nth_grid->x, nth[set].sp, nth[set].n, 1.0) : 0.0;
     }
   } else if (tid < 32) {
     const double q = primary_qsum_warp(tab, (float) gam, (float) ect, nullptr);
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(kXmodThreads) xillver_model_kernel(RelxTables 
     }
     r *= arf;
     if (add_prim && cp) {  // nthcomp on the shifted grid (spec_nthcomp with no energy shift)
-      r += nth_bin(nth[set], elo, ehi, 1.0, nth_norm_s) * (1.0 / qsum_s);
+      r += nth_bin(tab.nth_grid->x, nth[set], elo, ehi, 1.0, nth_norm_s) * (1.0 / qsum_s);
     } else if (add_prim) {  // spec_cutoffpl on the shifted grid (Xillspec.cpp:215-233), FP32 arithmetic
       const float en = (float) (0.5 * (elo + ehi));
       r += (double) (e1 * powf(en, -fg) * expf(-en / fe) * (float) (ehi - elo) * pnorm);
