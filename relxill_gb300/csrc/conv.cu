@@ -445,8 +445,11 @@ __global__ void __launch_bounds__(kFinThreads) finalize_relxill_kernel(RelxTable
     float r = 0.0f;
     for (int z = 0; z < s.nz; z++) r += cout[((size_t) set * nza + z) * kN + k];
     r *= rfac;
-    if (add_prim && cp) {
-      r += (float) nth_bin(tab.nth_grid->x, nth[set], ce[k], ce[k + 1], zp1, m.nth_norm) * pnorm;
+    if (add_prim && cp) {  // FP32: the bin's photon flux as the trapezoid of E F_E / E^2 (donthcomp.c:788-792)
+      const float e0 = tab.conv_eff[k].x, e1 = tab.conv_eff[k + 1].x, zf1 = (float) zp1;
+      const float p0 = nth_prim_f(*tab.nth_grid, nth[set], e0 * zf1);
+      const float p1 = nth_prim_f(*tab.nth_grid, nth[set], e1 * zf1);
+      r += (p1 / (e1 * e1) + p0 / (e0 * e0)) * 0.5f * tab.conv_cw[k].y * ((float) m.nth_norm * pnorm);
     } else if (add_prim) {
       const float2 cd = tab.conv_cw[k];  // (float) bin centre, (float) bin width
       const float en = cd.x;

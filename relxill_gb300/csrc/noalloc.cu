@@ -221,7 +221,7 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
   NOALLOC_CUDA(launch_relline(relx_is_relxill(kind), 1, 512, ntile_max, s, tab, p.sin, p.sst, p.rad, p.line_e, nza,
                               p.prof, p.dist, p.tsum, kind == RELX_RELLINE || kind == RELX_RELCONV));
   if (relx_is_relxill(kind)) {
-    NOALLOC_CUDA(launch_xillver(s, tab, 1, nza, nza, p.sst, p.cor, p.zcor, p.dist, p.xill, p.err, nullptr));
+    NOALLOC_CUDA(launch_xillver(s, tab, 1, nza, nza > RELX_ZDENSE, nza <= RELX_ZDENSE, p.sst, p.cor, p.zcor, p.dist, p.xill, p.err, nullptr));
     conv_zone_kernel<<<dim3(nza, 1), kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sst, p.prof, p.tsum, ntile_max,
                                                                             kSumBinsH, p.xill, nza, p.cout,
                                                                             p.err);

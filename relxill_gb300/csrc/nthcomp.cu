@@ -167,6 +167,8 @@ int nth_grid_build(const std::vector<double> &co, double band_lo, double band_hi
   int ih = 2;
   while (ih < kNthMaxJ && xx > x[ih]) ++ih;
   G.ih0 = ih;
+  G.l2x511 = (float) std::log2(x[1] * 511.);
+  G.inv_l2step = (float) (1.0 / (delta * std::log2(10.)));
   return 0;
 }
 
@@ -286,11 +288,15 @@ __global__ void __launch_bounds__(kNthThreads) nthcomp_kernel(const NthGrid *__r
     qs = ff_add(qs, ff_mul(P.g, sp));
     if (j == il) s_il = sp;
     if (j == ih) s_ih = sp;
-    if (T) T->sp[j] = ff_to_double(sp);
+    if (T) {
+      T->sp[j] = ff_to_double(sp);
+      T->spf[j] = __fadd_rn(sp.x, sp.y);
+    }
     un = uj;
   }
   if (T) {
     T->sp[jmax] = 0.0;
+    T->spf[jmax] = 0.0f;
     T->n = jmax;
   }
   // 1 / E F_E at the 1 keV point (donthcomp.c:617-638, 754-758) and the normalisation on the coarse grid
@@ -300,9 +306,10 @@ __global__ void __launch_bounds__(kNthThreads) nthcomp_kernel(const NthGrid *__r
   *q = ff_to_double(qs) * normfac * (1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi));
 }
 
-// normalisation changes of the zones on their corner weights, source normalisation of the primary
+// normalisation changes of the zones on their corner weights (the de-duplicated list or the per-zone
+// lists), source normalisation of the primary
 __global__ void nthcomp_apply_kernel(RelxSetState *__restrict__ sst, const double *__restrict__ q, int nq,
-                                     RelxZoneCorners *__restrict__ zcor) {
+                                     RelxCorners *__restrict__ cor, RelxZoneCorners *__restrict__ zcor) {
   const int set = blockIdx.x, tid = threadIdx.x;
   RelxSetState &s = sst[set];
   if (s.status != RELX_OK || s.prim != 1) return;
@@ -314,12 +321,22 @@ __global__ void nthcomp_apply_kernel(RelxSetState *__restrict__ sst, const doubl
     if (tid == 0) s.status = RELX_ERR_PARAM;
     return;
   }
-  for (int e = tid; e < s.nz * 32; e += blockDim.x) {
-    const int z = e >> 5, c = e & 31;
-    const double xs = (s.zshift[z] == 1.0) ? 1.0 : q[(size_t) set * nq + z + 1] * (1.0 / q0);
-    zcor[set].w[z][c] = (float) ((double) zcor[set].w[z][c] * xs);
-    if (c == 0) s.inv_nc[z] = (float) xs;
+  const int nz = s.nz;
+  if (s.xdense) {
+    for (int e = tid; e < s.ucount * nz; e += blockDim.x) {
+      const int u = e / nz, z = e - u * nz;
+      const double xs = (s.zshift[z] == 1.0) ? 1.0 : q[(size_t) set * nq + z + 1] * (1.0 / q0);
+      cor[set].w[u][z] = (float) ((double) cor[set].w[u][z] * xs);
+    }
+  } else {
+    for (int e = tid; e < nz * 32; e += blockDim.x) {
+      const int z = e >> 5, c = e & 31;
+      const double xs = (s.zshift[z] == 1.0) ? 1.0 : q[(size_t) set * nq + z + 1] * (1.0 / q0);
+      zcor[set].w[z][c] = (float) ((double) zcor[set].w[z][c] * xs);
+    }
   }
+  for (int z = tid; z < nz; z += blockDim.x)
+    s.inv_nc[z] = (float) ((s.zshift[z] == 1.0) ? 1.0 : q[(size_t) set * nq + z + 1] * (1.0 / q0));
   if (tid == 0) s.src_norm = 1.0 / q0;
 }
 
@@ -328,15 +345,15 @@ size_t nthcomp_scratch_bytes(int n_sets, int nza, bool params) {
 }
 
 cudaError_t launch_nthcomp(cudaStream_t s, const RelxTables &tab, const RelxSetIn *sin, RelxSetState *sst, int n_sets,
-                           int nza, bool params, double *q, NthTable *tabs, RelxZoneCorners *zcor, float4 *scr,
-                           int64_t ncont_all, int64_t c_off) {
+                           int nza, bool params, double *q, NthTable *tabs, RelxCorners *cor, RelxZoneCorners *zcor,
+                           float4 *scr, int64_t ncont_all, int64_t c_off) {
   if (n_sets <= 0) return cudaSuccess;
   const int nq = RELX_NZMAX + 1;
   const int per = params ? 1 : nza + 1;
   const int64_t ncont = (int64_t) n_sets * per;
   nthcomp_kernel<<<(unsigned) ((ncont + kNthThreads - 1) / kNthThreads), kNthThreads, 0, s>>>(
       tab.nth_grid, sin, sst, params, per, n_sets, nq, q, tabs, scr, ncont_all, c_off);
-  if (!params && zcor) nthcomp_apply_kernel<<<n_sets, 128, 0, s>>>(sst, q, nq, zcor);
+  if (!params) nthcomp_apply_kernel<<<n_sets, 128, 0, s>>>(sst, q, nq, cor, zcor);
   return cudaGetLastError();
 }
 

@@ -164,6 +164,8 @@ struct RelxSetState {
   int ind_a, ind_mu0;
   float ifac_a, ifac_mu0;
   int ucount;       // unique xillver corners (dense mode)
+  int xdense;       // 1: the zone spectra come from the de-duplicated corner list (RelxCorners),
+                    // 0: from the per-zone lists (RelxZoneCorners)
   int out_lo, out_hi;  // conv-grid bins the caller's grid needs (inclusive)
   double a, incl, rin, rout, height, beta, gamma, z, lineE;
   double gam, ect_src, refl_frac;
@@ -189,10 +191,12 @@ struct NthGrid {
   NthPoint p[RELX_NTH_N + 1];  // j = 1..901
   double x[RELX_NTH_N + 2];    // x_j (FP64), j = 1..902
   int jnr0, jrel0, ih0, pad_;  // region bounds of the escape probability, index of the 1 keV point
+  float l2x511, inv_l2step;    // log2(x_1 511 keV), 1 / (log2 of the grid ratio): grid position of an energy
 };
-// E F_E table of a set's source continuum, sp[1..n] on the grid's x
+// E F_E table of a set's source continuum, sp[1..n] on the grid's x, and its float copy
 struct NthTable {
   double sp[RELX_NTH_N];
+  float spf[RELX_NTH_N];
   int n;
   int pad_[3];
 };

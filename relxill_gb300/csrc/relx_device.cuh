@@ -310,4 +310,19 @@ __device__ __forceinline__ double nth_bin(const double *x, const NthTable &T, do
   return (p1 / (e1 * e1) + p0 / (e0 * e0)) * .5 * (e1 - e0) * normfac;
 }
 
+// E F_E of the nthcomp table at t = E (1 + z) in keV, FP32 from the table's float copy.  The
+// interpolation is continuous in t (linear between grid points, zero at the table's last point), so
+// the bracketing point comes from the grid position log2(t / (x_1 511)) / step without exact
+// comparisons; beyond the table 0, below its first point the first value (donthcomp.c:768-786)
+__device__ __forceinline__ float nth_prim_f(const NthGrid &G, const NthTable &T, float t) {
+  const float L = (log2f(t) - G.l2x511) * G.inv_l2step;
+  if (!(L > 0.0f)) return T.spf[1];
+  const int j = (int) ceilf(L) + 1;  // first point with x_j 511 >= t (to rounding)
+  if (j > T.n) return 0.0f;
+  const int jl = j - 1;
+  const float xl = G.p[jl].x.x, xh = G.p[jl + 1].x.x;
+  const float f = (t * (1.0f / 511.0f) - xl) / (xh - xl);
+  return T.spf[jl] + f * (T.spf[jl + 1] - T.spf[jl]);
+}
+
 }  // namespace relx

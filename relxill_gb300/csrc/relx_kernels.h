@@ -35,7 +35,7 @@ cudaError_t xillver_set_smem(int n_incl);
 // bounded-wait self-test: writes the status of a wait that cannot complete (RELX_ERR_TIMEOUT)
 cudaError_t launch_wait_selftest(cudaStream_t s, unsigned long long limit_ns, int *out);
 // order: the sets in visiting order (launch_xill_order), or null for batch order
-cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, int nza, int nz_min,
+cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, int nza, bool zone, bool dense,
                            const RelxSetState *sst, const RelxCorners *cor, const RelxZoneCorners *zcor,
                            const float *dist, float *xout, int *err, const int *order);
 void launch_xill_order(cudaStream_t s, const RelxSetState *sst, const RelxCorners *cor, const RelxZoneCorners *zcor,
@@ -68,13 +68,14 @@ int nth_grid_build(const std::vector<double> &co, double band_lo, double band_hi
 size_t nthcomp_scratch_bytes(int n_sets, int nza, bool params);
 // per set: the normalisation (calcNormWrtXillverTableSpec) of the source continuum (q[set][0]) and of
 // every zone's (q[set][z + 1]), q holding RELX_NZMAX + 1 values per set, and the source's table;
-// then the zones' normalisation changes on their corner weights (zcor) and the source normalisation.
+// then the zones' normalisation changes on their corner weights (cor for sets with the de-duplicated
+// list, zcor for the others) and the source normalisation.
 // params: the xillver model, Gamma and kTe from the parameters, the source continuum only.
 // scr: scratch of nthcomp_scratch_bytes for the whole batch, ncont_all continua per grid point,
 // this launch's continua starting at c_off.
 cudaError_t launch_nthcomp(cudaStream_t s, const RelxTables &tab, const RelxSetIn *sin, RelxSetState *sst, int n_sets,
-                           int nza, bool params, double *q, NthTable *tabs, RelxZoneCorners *zcor, float4 *scr,
-                           int64_t ncont_all, int64_t c_off);
+                           int nza, bool params, double *q, NthTable *tabs, RelxCorners *cor, RelxZoneCorners *zcor,
+                           float4 *scr, int64_t ncont_all, int64_t c_off);
 
 // the xillver model: one CTA per set, writes the flux and the status fields of the set state
 size_t xillver_model_smem_bytes(int n_ener, int n_ener_pad);

@@ -933,7 +933,7 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   if (kind == RELX_XILLVER) {
     if (cp) {
       ProfScope ps(PK_NTH, s);
-      RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, 1, true, nthq, ntab, nullptr, W.nthscr.as<float4>(),
+      RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, 1, true, nthq, ntab, nullptr, nullptr, W.nthscr.as<float4>(),
                                (int64_t) b.n_sets, (int64_t) base));
     }
     {
@@ -952,7 +952,7 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   }
   if (cp) {  // the nthcomp continua of the source and the zones, their normalisations on the corner weights
     ProfScope ps(PK_NTH, s, 2);
-    RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, b.nza, false, nthq, ntab, zcor, W.nthscr.as<float4>(),
+    RELX_CUDA(launch_nthcomp(s, tab, sin, sst, n, b.nza, false, nthq, ntab, cor, zcor, W.nthscr.as<float4>(),
                              (int64_t) b.n_sets * (b.nza + 1), (int64_t) base * (b.nza + 1)));
   }
   if (cached) {
@@ -977,12 +977,14 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   }
   if (relx_is_relxill(kind)) {
     {
-      const bool dense = b.nza <= RELX_ZDENSE && !cp;
-      const bool both = b.nza > RELX_ZDENSE && b.nz_min <= RELX_ZDENSE && !cp;  // zone and dense kernels
-      ProfScope ps(PK_XILL, s, (dense || both) ? 2 : 1);
+      // the zone kernel for sets with more than RELX_ZDENSE zones and for 6-parameter sets whose
+      // corners do not fit the de-duplicated list; the dense kernel, in table-row order, for the rest
+      const bool zone = b.nza > RELX_ZDENSE || cp;
+      const bool dense = b.nz_min <= RELX_ZDENSE;
+      ProfScope ps(PK_XILL, s, (zone ? 1 : 0) + (dense ? 2 : 0));
       int *order = dense ? W.order.as<int>() + base : nullptr;
       if (dense) launch_xill_order(s, sst, cor, zcor, n, order);
-      RELX_CUDA(launch_xillver(s, tab, n, b.nza, b.nz_min, sst, cor, zcor, dist, xill, W.err.as<int>(), order));
+      RELX_CUDA(launch_xillver(s, tab, n, b.nza, zone, dense, sst, cor, zcor, dist, xill, W.err.as<int>(), order));
     }
     {
       ProfScope ps(PK_CONV, s);

@@ -843,11 +843,14 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   __syncthreads();
   const int ni = tab.x_nincl;
   const bool six = tab.x_npar == 6;
-  if (six) {
-    // ---- 6-parameter table (nthcomp, Cp models): 32 corners per zone, the two 16-corner blocks over
-    // parameters 1..4 at both brackets of parameter 0 (interp_6d_tab_incl, xilltable.c:999-1020), in
-    // the per-zone corner lists; the table has a density parameter, so no density division
-    if (!tab.x_has_dens && tid == 0) m.status = RELX_ERR_TABLE;
+  // corners per zone: 16 over parameters 0..3 of the 5-parameter table (interp_5d_tab_incl,
+  // xilltable.c:812-876); 32 over parameters 0..4 of the 6-parameter table (the two 16-corner
+  // blocks of interp_6d_tab_incl, xilltable.c:999-1020), which has a density parameter and so no
+  // density division
+  const int ncz = six ? 32 : 16, nbits = six ? 5 : 4;
+  if (six && !tab.x_has_dens && tid == 0) m.status = RELX_ERR_TABLE;
+  const bool listed = nz * ncz <= RELX_NZMAX * 16;  // the entries fit the de-duplication arrays
+  if (!listed) {  // 6-parameter table and more than 25 zones: per-zone lists, no de-duplication
     for (int e = tid; e < nz * 32; e += kSetupThreads) {
       const int z = e >> 5, c = e & 31;
       long row = 0;
@@ -861,15 +864,18 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       zcout[set].row[z][c] = (int) (row * ni);
       zcout[set].w[z][c] = (float) (w * m.xscale[z]);
     }
-    if (tid == 0) s.ucount = 0;
+    if (tid == 0) {
+      s.ucount = 0;
+      s.xdense = 0;
+    }
   }
-  // ---- the 16 corners of every zone, first-zone density scaling, de-duplication
-  const int ncor = six ? 0 : nz * 16;
+  // ---- the corners of every zone, first-zone density scaling, de-duplication
+  const int ncor = listed ? nz * ncz : 0;
   for (int e = tid; e < ncor; e += kSetupThreads) {
-    int z = e >> 4, c = e & 15;
-    // corner c: bit0 -> param 0 (+1), bit1 -> param 1, bit2 -> param 2, bit3 -> param 3
+    const int z = e / ncz, c = e - z * ncz;
+    // corner c: bit q -> upper bracket of parameter q
     long row = 0;
-    for (int q = 0; q < 4; q++) row = row * tab.x_nvals[q] + m.zind[z][q] + ((c >> q) & 1);
+    for (int q = 0; q < nbits; q++) row = row * tab.x_nvals[q] + m.zind[z][q] + ((c >> q) & 1);
     row = row * ni;  // incl index 0
     m.crow[e] = (int) row;
   }
@@ -882,16 +888,16 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   }
   __syncthreads();
   for (int e = tid; e < ncor; e += kSetupThreads) {
-    int z = e >> 4, c = e & 15;
+    const int z = e / ncz, c = e - z * ncz;
     double w = 1.0;
-    for (int q = 0; q < 4; q++) {
+    for (int q = 0; q < nbits; q++) {
       double f = m.zfac[z][q];
       w *= ((c >> q) & 1) ? f : (1.0 - f);
     }
     // density division of the row by the zone that loads it first (xilltable.c:478-511)
     double dscale = 1.0;
     if (!tab.x_has_dens) {
-      double d = m.zdens[m.cfirst[e] >> 4];
+      double d = m.zdens[m.cfirst[e] / ncz];
       if (fabs(d - 15) > 1e-6) dscale = 1.0 / pow(10.0, d - 15);
     }
     m.cw[e] = (float) (w * dscale * m.xscale[z]);
@@ -903,7 +909,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   for (int e = tid; e < ncor; e += kSetupThreads)
     if (m.cw[e] != 0.0f) m.clive[m.cfirst[e]] = 1;
   __syncthreads();
-  if (tid < 32) {  // number the live rows in entry order (warp prefix sums)
+  if (tid < 32 && listed) {  // number the live rows in entry order (warp prefix sums)
     const int lane = tid;
     int base = 0;
     for (int e0 = 0; e0 < ncor; e0 += 32) {
@@ -914,20 +920,26 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       if (first) m.cuniq[e] = live ? (short) (base + __popc(mask & ((1u << lane) - 1u))) : (short) -1;
       base += __popc(mask);
     }
-    if (lane == 0) s.ucount = base;
+    if (lane == 0) {
+      s.ucount = base;
+      m.ired[0] = base;
+    }
   }
   __syncthreads();
   for (int e = tid; e < ncor; e += kSetupThreads)
     if (m.cfirst[e] != e) m.cuniq[e] = m.cuniq[m.cfirst[e]];  // the first entry is numbered above
+  // dense: at most RELX_ZDENSE zones and RELX_MAX_UCORNER distinct live rows (always so for the
+  // 5-parameter table: 16 corners x 16 zones)
+  const bool dense = listed && nz <= RELX_ZDENSE && m.ired[0] <= RELX_MAX_UCORNER;
   __syncthreads();
-  const bool dense = nz <= RELX_ZDENSE && !six;
+  if (tid == 0 && listed) s.xdense = dense ? 1 : 0;
   if (dense) {
     RelxCorners &C = cout[set];
     for (int i = tid; i < RELX_MAX_UCORNER * RELX_ZDENSE; i += kSetupThreads) (&C.w[0][0])[i] = 0.0f;
     __syncthreads();
   }
   for (int e = tid; e < ncor; e += kSetupThreads) {
-    int z = e >> 4, c = e & 15;
+    const int z = e / ncz, c = e - z * ncz;
     if (dense) {
       RelxCorners &C = cout[set];
       const int u = m.cuniq[e];

@@ -75,9 +75,9 @@ __global__ void __launch_bounds__(kOrderThreads) xill_order_kernel(const RelxSet
       const RelxSetState &s = sst[set];
       unsigned int r = 0xffffffffu;
       if (s.status == RELX_OK && s.model >= RELX_RELXILL) {
-        if (s.nz <= RELX_ZDENSE) {
+        if (s.xdense) {
           if (s.ucount > 0) r = (unsigned int) scor[set].row[0];
-        } else {
+        } else if (zcor) {
           r = (unsigned int) zcor[set].row[0][0];
         }
       }
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(kXillThreads, 3) xillver_dense_kernel(RelxTabl
   XillSmem<NZ> &m = *reinterpret_cast<XillSmem<NZ> *>(smem_raw);
   const int set = order ? order[blockIdx.y] : blockIdx.y, tile = blockIdx.x;
   const RelxSetState &s = sst[set];
-  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.nz > NZ) return;
+  if (s.status != RELX_OK || s.model < RELX_RELXILL || !s.xdense || s.nz > NZ) return;
   constexpr int NIU = NI > 0 ? NI : RELX_MAX_INCL;
   const int tid = threadIdx.x;
   const int nz = s.nz, U = s.ucount, ni = NI > 0 ? NI : tab.x_nincl;
@@ -219,15 +219,15 @@ static size_t xill_smem_nz(int n_incl) {
   return sizeof(XillSmem<NZ>) + sizeof(float4) * ((size_t) kXillStages * n_incl * (kXillTile / 4) - 1);
 }
 
-// generic path for more than RELX_ZDENSE zones (ionisation gradients): 16 corners per zone, plain loads
-// min_nz: sets with at most this many zones are left to the dense kernel (0: none)
+// generic path for the sets without the de-duplicated corner list (more than RELX_ZDENSE zones, or
+// more distinct rows than RELX_MAX_UCORNER): 16 or 32 corners per zone, plain loads
 __global__ void __launch_bounds__(kXillThreads) xillver_zone_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
                                                                     const RelxZoneCorners *__restrict__ zcor,
                                                                     const float *__restrict__ dist_raw, int nza,
-                                                                    float *__restrict__ xout, int min_nz) {
+                                                                    float *__restrict__ xout) {
   const int set = blockIdx.y, tile = blockIdx.x;
   const RelxSetState &s = sst[set];
-  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.nz <= min_nz) return;
+  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.xdense) return;
   const int ncz = tab.x_npar == 6 ? 32 : 16;  // corners per zone (16, or 32 for the 6-parameter table)
   __shared__ float dist[RELX_MAX_INCL];
   const int tid = threadIdx.x, ni = tab.x_nincl, pitch = tab.x_nener_pad;
@@ -278,22 +278,14 @@ cudaError_t xillver_set_smem(int n_incl) {
 }
 
 // xillver stage of a batch: the dense kernel (instance by the batch's zone count and the table's
-// inclination count) for sets with at most RELX_ZDENSE zones, the zone kernel for sets with more.
-// nz_min: the smallest zone count of the batch's sets; a batch with more than RELX_ZDENSE zones
-// runs both kernels when it also holds sets with at most RELX_ZDENSE zones (order is then unused).
-cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, int nza, int nz_min,
+// inclination count) for the sets with the de-duplicated corner list, the zone kernel for the others.
+// zone: some set may need the zone kernel; dense: some set may use the dense kernel.
+cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, int nza, bool zone, bool dense,
                            const RelxSetState *sst, const RelxCorners *cor, const RelxZoneCorners *zcor,
                            const float *dist, float *xout, int *err, const int *order) {
   const dim3 grid((tab.x_nener_pad + kXillTile - 1) / kXillTile, n_sets);
-  if (tab.x_npar == 6) {  // the 6-parameter table: per-zone corner lists for every set
-    xillver_zone_kernel<<<grid, kXillThreads, 0, s>>>(tab, sst, zcor, dist, nza, xout, 0);
-    return cudaGetLastError();
-  }
-  if (nza > RELX_ZDENSE) {
-    xillver_zone_kernel<<<grid, kXillThreads, 0, s>>>(tab, sst, zcor, dist, nza, xout, RELX_ZDENSE);
-    if (nz_min > RELX_ZDENSE) return cudaGetLastError();
-    order = nullptr;
-  }
+  if (zone) xillver_zone_kernel<<<grid, kXillThreads, 0, s>>>(tab, sst, zcor, dist, nza, xout);
+  if (!dense) return cudaGetLastError();
   const int nzk = nza <= 1 ? 1 : (nza <= 10 ? 10 : 16);
   const int nik = tab.x_nincl == 10 ? 10 : 0;
 #define X(nz, ni)                                                                                           \

@@ -72,3 +72,38 @@ def test_kte_without_grid_is_a_parameter_error(gpu):
     q[12] = -5.0
     out, st = gpu.eval_batch("relxillCp", q[None], [w], check=False)
     assert st[0] == 1 and not out[0].any()
+
+
+@pytest.mark.parametrize("zones", [16, 20, 30])
+def test_relxilllpcp_zone_counts(gpu, oracle, monkeypatch, zones):
+    """The 6-parameter corners of a set come from the de-duplicated list (at most 16 zones), the
+    per-zone lists (more zones) or, beyond 25 zones, per-zone lists built without de-duplication;
+    ionisation gradients give every zone its own logxi and density brackets."""
+    monkeypatch.setenv("RELXILL_NUM_RZONES", str(zones))
+    rng = np.random.default_rng(54 + zones)
+    n = 4
+    p = np.column_stack([rng.uniform(10, 80, n), rng.uniform(0.1, 0.998, n), -np.ones(n), np.full(n, 400.0),
+                         rng.uniform(3, 50, n), np.zeros(n), rng.uniform(1.4, 3.0, n), rng.uniform(0, 4.5, n),
+                         rng.uniform(15, 19, n), rng.uniform(0.5, 3, n), rng.uniform(10, 300, n), np.ones(n),
+                         np.zeros(n), np.zeros(n), np.array([1, 2, 2, 1]), np.zeros(n), np.zeros(n)])
+    _check(gpu, "relxilllpCp", p, [log_grid(0.3, 80.0, int(rng.integers(300, 1500))) for _ in range(n)])
+
+
+def test_relxillcp_mixed_zone_counts(gpu, oracle, monkeypatch):
+    """relxillCp sets without (1 zone) and with an ionisation gradient (25 zones) in one batch."""
+    monkeypatch.delenv("RELXILL_NUM_RZONES", raising=False)
+    rng = np.random.default_rng(58)
+    n = 4
+    p = np.column_stack([rng.uniform(10, 80, n), rng.uniform(-0.5, 0.998, n), -np.ones(n), rng.uniform(100, 500, n),
+                         rng.uniform(5, 30, n), rng.uniform(2, 4, n), rng.uniform(2, 4, n), np.zeros(n),
+                         rng.uniform(1.4, 3.0, n), rng.uniform(0, 4.5, n), rng.uniform(15, 19, n),
+                         rng.uniform(0.5, 3, n), rng.uniform(10, 300, n), rng.uniform(0.5, 3, n)])
+    igt = np.array([0, 1, 0, 2], dtype=np.int32)
+    igi = np.where(igt == 1, 1.2, 0.0)
+    grids = [log_grid(0.3, 80.0, int(rng.integers(300, 1000))) for _ in range(n)]
+    out, st = gpu.eval_batch("relxillCp", p, grids, ion_grad_type=igt, iongrad_index=igi)
+    assert not st.any(), (st, gpu.last_error())
+    for i in range(n):
+        s, orc = oracle_lib.evaluate("relxillCp", p[i], grids[i], None, int(igt[i]), float(igi[i]))
+        assert s == 0
+        assert_close(out[i], orc, f"relxillCp set {i} (ion_grad_type {igt[i]})")
