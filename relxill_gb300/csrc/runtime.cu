@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <condition_variable>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -86,6 +87,97 @@ struct Pinned {
     h = nullptr;
     bytes = 0;
   }
+};
+
+// Host copies to and from pinned staging, split over a few worker threads: one thread copies at
+// a fraction of the host's memory bandwidth, and a batch of 4096 spectra moves about 90 MB of
+// energy edges in and as much flux out.  Jobs of concurrent callers run one after the other.
+struct CopyPiece {
+  void *dst;
+  const void *src;
+  size_t n;
+};
+class CopyPool {
+ public:
+  static CopyPool &get() {
+    static CopyPool *p = new CopyPool();  // workers live for the process
+    return *p;
+  }
+  // performs every copy of `jobs`, pieces of at most kPiece bytes spread over the workers and the caller
+  void run(const std::vector<CopyPiece> &jobs) {
+    size_t total = 0;
+    for (const auto &j : jobs) total += j.n;
+    if (nthreads_ == 0 || total < kMinParallel) {
+      for (const auto &j : jobs)
+        if (j.n) std::memcpy(j.dst, j.src, j.n);
+      return;
+    }
+    std::lock_guard<std::mutex> one(call_mu_);  // one job at a time
+    std::unique_lock<std::mutex> lk(mu_);      // no worker is inside a job here (active_ == 0)
+    pieces_.clear();
+    for (const auto &j : jobs)
+      for (size_t o = 0; o < j.n; o += kPiece)
+        pieces_.push_back({(unsigned char *) j.dst + o, (const unsigned char *) j.src + o, std::min(kPiece, j.n - o)});
+    next_.store(0);
+    remaining_ = pieces_.size();
+    open_ = true;
+    ++gen_;
+    lk.unlock();
+    cv_.notify_all();
+    work();
+    lk.lock();
+    done_cv_.wait(lk, [&] { return remaining_ == 0; });
+    open_ = false;  // late workers skip this job; wait for those still inside it
+    done_cv_.wait(lk, [&] { return active_ == 0; });
+  }
+
+ private:
+  static constexpr size_t kPiece = 1 << 20, kMinParallel = 4 << 20;
+  CopyPool() {
+    const char *e = std::getenv("RELX_COPY_THREADS");
+    unsigned hc = std::thread::hardware_concurrency();
+    int n = e ? std::atoi(e) : (int) std::min(12u, hc > 1 ? hc - hc / 4 : 0u);
+    nthreads_ = std::max(0, std::min(n, 32));
+    for (int i = 0; i < nthreads_; i++) std::thread([this] { loop(); }).detach();
+  }
+  void work() {
+    size_t done = 0;
+    for (;;) {
+      const size_t i = next_.fetch_add(1);
+      if (i >= pieces_.size()) break;
+      std::memcpy(pieces_[i].dst, pieces_[i].src, pieces_[i].n);
+      done++;
+    }
+    if (done) {
+      std::lock_guard<std::mutex> g(mu_);
+      remaining_ -= done;
+      if (remaining_ == 0) done_cv_.notify_all();
+    }
+  }
+  void loop() {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+        if (!open_) continue;
+        active_++;
+      }
+      work();
+      std::lock_guard<std::mutex> g(mu_);
+      if (--active_ == 0) done_cv_.notify_all();
+    }
+  }
+  int nthreads_ = 0;
+  std::mutex call_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  std::vector<CopyPiece> pieces_;
+  std::atomic<size_t> next_{0};
+  size_t remaining_ = 0;
+  int active_ = 0;
+  bool open_ = false;
+  uint64_t gen_ = 0;
 };
 
 template <typename T>
@@ -713,7 +805,11 @@ struct Context {
   int device = -1;
   std::string table_dir;
   bool attrs_set = false;
-  Pinned pin;             // host staging of the host-buffer API
+  Pinned pin;             // host staging of the host-buffer API (its first group)
+  std::vector<Pinned> pin_groups;      // staging of the further groups of a large host batch
+  std::vector<cudaEvent_t> group_ev;   // completion of each group's copies back
+  Workspace W2;                        // workspace of the odd groups
+  cudaStream_t gstream[2] = {nullptr, nullptr};  // streams of the even and odd groups
   RelCache cache;         // line-profile cache (off until relx_cache_config)
   cudaStream_t aux[2] = {nullptr, nullptr};      // streams of pipelined chunks
   cudaEvent_t aux_ev[2] = {nullptr, nullptr}, fork_ev = nullptr;
@@ -1245,9 +1341,10 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
     return st;
   unsigned char *h = (unsigned char *) P.h;
   size_t off = 0;
+  std::vector<CopyPiece> jobs;
   auto put = [&](const void *src, size_t n) {
     size_t o = off;
-    if (n && src) std::memcpy(h + o, src, n);
+    if (n && src) jobs.push_back({h + o, src, n});
     off += (n + 63) / 64 * 64;
     return o;
   };
@@ -1260,9 +1357,10 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
     double *fi = (double *) (h + o_f);
     for (int i = 0; i < n_sets; i++) {
       int n = (int) (hb.eoff[i + 1] - hb.eoff[i] - 1);
-      std::memcpy(fi + hb.eoff[i], hb.flux_in + (hb.eoff[i] - i), sizeof(double) * n);
+      jobs.push_back({fi + hb.eoff[i], hb.flux_in + (hb.eoff[i] - i), sizeof(double) * n});
     }
   }
+  CopyPool::get().run(jobs);
   *o_flux = put(nullptr, nflux * sizeof(double));
   *o_status = put(nullptr, sizeof(int) * n_sets);
   if ((st = W.params.reserve(pb)) || (st = W.eoff.reserve(ob)) || (hb.igt && (st = W.igt.reserve(gb))) ||
@@ -1287,23 +1385,92 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
   return 0;
 }
 
-// host-buffer evaluation: copies in, evaluates, copies out, synchronises
+// host-buffer evaluation: copies in, evaluates, copies out, synchronises.  A large batch runs as
+// groups of consecutive sets, each with its own pinned staging, alternating between two streams
+// and two workspaces: the host stages group g + 1 while the GPU computes group g, the copies of
+// one group overlap the kernels of the other, and the host copies the results of group g out while
+// the GPU computes the later groups.  Both workspaces are reserved for the largest group before the
+// first one is queued (no buffer is reallocated while a group is in flight).
+static int host_groups(int n_sets) {
+  if (n_sets < 2048) return 1;
+  return std::min(8, n_sets / 1024);
+}
+
 static int eval_host(const HostBatch &hb, double *flux, int *status) {
   if (!flux) return RELX_ERR_ARG;
   Context &C = ctx();
   std::lock_guard<std::mutex> lock(C.mu);
   int st = ensure_init(C, nullptr);
   if (st) return st;
-  size_t o_flux = 0, o_status = 0;
-  if ((st = enqueue_host_batch(C, C.W, C.pin, C.stream, hb, true, &o_flux, &o_status))) return st;
-  RELX_CUDA(cudaStreamSynchronize(C.stream));
-  const unsigned char *h = (const unsigned char *) C.pin.h;
-  std::memcpy(flux, h + o_flux, sizeof(double) * (size_t) (hb.eoff[hb.n_sets] - hb.n_sets));
-  const int *sts = (const int *) (h + o_status);
+  const int n = hb.n_sets;
+  if (hb.model < 0 || hb.model >= RELX_NMODELS || n <= 0 || !hb.params || !hb.energy || !hb.eoff)
+    return RELX_ERR_ARG;
+  const int ng = host_groups(n);
+  const int npar = model_nparams(hb.model);
+  const bool conv = relx_kind(hb.model) == RELX_RELCONV;
+  std::vector<std::vector<int64_t>> offs(ng);
+  std::vector<HostBatch> sub(ng);
+  std::vector<int> s0(ng + 1);
+  for (int g = 0; g <= ng; g++) s0[g] = (int) ((int64_t) g * n / ng);
+  for (int g = 0; g < ng; g++) {
+    const int a = s0[g], m = s0[g + 1] - a;
+    const int64_t e0 = hb.eoff[a];
+    offs[g].resize(m + 1);
+    for (int i = 0; i <= m; i++) offs[g][i] = hb.eoff[a + i] - e0;
+    HostBatch &b = sub[g];
+    b = hb;
+    b.n_sets = m;
+    b.params = hb.params + (size_t) a * npar;
+    b.energy = hb.energy + e0;
+    b.eoff = offs[g].data();
+    b.flux_in = (conv && hb.flux_in) ? hb.flux_in + (e0 - a) : hb.flux_in;
+    b.igt = hb.igt ? hb.igt + a : nullptr;
+    b.igi = hb.igi ? hb.igi + a : nullptr;
+  }
+  if (ng > 1) {
+    const EnvOpts env = read_env();
+    for (int g = 0; g < ng; g++) {
+      BatchShape b;
+      bool need_zc = false;
+      if ((st = batch_shape(sub[g].model, sub[g].n_sets, sub[g].eoff, sub[g].igt, env, &b, &need_zc, sub[g].params)) ||
+          (st = reserve_workspace(C.T, C.W, b, need_zc)) || (st = reserve_workspace(C.T, C.W2, b, need_zc)))
+        return st;
+    }
+    for (int k = 0; k < 2; k++)
+      if (!C.gstream[k]) RELX_CUDA(cudaStreamCreateWithFlags(&C.gstream[k], cudaStreamNonBlocking));
+  }
+  if ((int) C.pin_groups.size() < ng) C.pin_groups.resize(ng);
+  while ((int) C.group_ev.size() < ng) {
+    cudaEvent_t e;
+    RELX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    C.group_ev.push_back(e);
+  }
+  std::vector<size_t> o_flux(ng), o_status(ng);
+  for (int g = 0; g < ng; g++) {
+    Pinned &P = (g == 0) ? C.pin : C.pin_groups[g];
+    Workspace &W = (g & 1) ? C.W2 : C.W;
+    cudaStream_t gs = (ng > 1) ? C.gstream[g & 1] : C.stream;
+    if ((st = enqueue_host_batch(C, W, P, gs, sub[g], true, &o_flux[g], &o_status[g])) ||
+        cudaEventRecord(C.group_ev[g], gs) != cudaSuccess) {
+      cudaDeviceSynchronize();  // earlier groups may still read their staging
+      cudaGetLastError();
+      return st ? st : RELX_ERR_CUDA;
+    }
+  }
   int worst = 0;
-  for (int i = 0; i < hb.n_sets; i++) {
-    if (status) status[i] = sts[i];
-    if (sts[i] != 0 && worst == 0) worst = sts[i];
+  std::vector<CopyPiece> out;
+  for (int g = 0; g < ng; g++) {
+    RELX_CUDA(cudaEventSynchronize(C.group_ev[g]));
+    const unsigned char *h = (const unsigned char *) ((g == 0) ? C.pin.h : C.pin_groups[g].h);
+    const int a = s0[g], m = s0[g + 1] - a;
+    const int64_t nf = offs[g][m] - m;
+    out.assign(1, CopyPiece{flux + (hb.eoff[a] - a), h + o_flux[g], sizeof(double) * (size_t) nf});
+    CopyPool::get().run(out);
+    const int *sts = (const int *) (h + o_status[g]);
+    for (int i = 0; i < m; i++) {
+      if (status) status[a + i] = sts[i];
+      if (sts[i] != 0 && worst == 0) worst = sts[i];
+    }
   }
   return worst;
 }
@@ -1614,8 +1781,10 @@ void relx_release(void) {
   if (C.stream) cudaStreamSynchronize(C.stream);
   graphs_clear(C);
   C.W.release();
+  C.W2.release();
   C.T.release();
   C.pin.release();
+  for (auto &p : C.pin_groups) p.release();
   C.cache.release();
   C.cache_ev_valid = false;
 }
