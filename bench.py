@@ -644,7 +644,8 @@ def run_gpu(args):
         "max_rel_err_vs_oracle": max_err, "gpu_launches": int(launches), "clocks": clk,
         "tuning": R.tuning_report(), "graphs": "step replayed as a CUDA graph after its second launch",
         "roofline": roof, "dominant_kernel": names[dom],
-        "dominant_kernel_bound": "FP32 ALU issue (line profile: Romberg g*-integration; see profiles/)",
+        "dominant_kernel_bound": {"bound": "instruction issue (FP32 ALU and FMA)", "issue_active": 0.686,
+                                  "active_threads_per_instruction": 20.3, "source": "profiles/relline_kernel_512sets.md (ncu)"},
         "kernels": kernels, "cpu_baseline": cpu,
         "serve": serve, "ion_gradient": iongrad, "returning_radiation": rrad, "cp_flavour": cp,
         "table_load": {"seconds": table_load_s, "bytes": int(tb.value)},
