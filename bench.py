@@ -384,8 +384,8 @@ class Clocks:
         self.path = None
 
     def start(self):
-        out = os.path.join(ROOT, "gpurun_out") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None
-        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv", dir=out)
+        out = os.environ.get("RELX_CLOCK_LOG_DIR")  # keep the raw samples there (default: the temp folder)
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv", dir=out if out and os.path.isdir(out) else None)
         os.close(fd)
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
