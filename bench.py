@@ -553,8 +553,8 @@ def run_gpu(args):
     # plain path: one synchronous c_lmodrelxilllp call per spectrum
     plain = None
     if not args.no_plain:
-        n_plain = 64
-        for i in range(4):
+        n_plain = min(64, S)
+        for i in range(min(4, S)):
             R.relxilllp(grids[i], params[i])
         t0 = time.perf_counter()
         for i in range(n_plain):
@@ -569,7 +569,7 @@ def run_gpu(args):
 
     oracle_lib.lib(tdir)
     max_err = 0.0
-    for i in range(4):
+    for i in range(min(4, S)):
         s, ref = oracle_lib.evaluate("relxilllp", params[i], grids[i])
         got = out[offs[i] - i: offs[i + 1] - i - 1]
         m = ref > 1e-6 * ref.max()

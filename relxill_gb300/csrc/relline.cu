@@ -595,4 +595,10 @@ cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream
   return cudaGetLastError();
 }
 
+cudaError_t launch_hist(int n_sets, cudaStream_t s, const RelxTables &tab, const RelxSetState *sst,
+                        const RelxRadial *srad, int nza, float *dist) {
+  hist_kernel<<<n_sets, kLineThreads, hist_smem_bytes(tab.rel_nr, tab.rel_ng), s>>>(tab, sst, srad, nza, dist);
+  return cudaGetLastError();
+}
+
 }  // namespace relx

@@ -30,6 +30,9 @@ cudaError_t relline_set_smem(int nr, int ng);
 cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream_t s, const RelxTables &tab,
                            const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
                            int nza, float *prof, float *dist, double *tsum, bool any_limb);
+// the emission-angle histograms alone (relxill models), for a launch on its own stream
+cudaError_t launch_hist(int n_sets, cudaStream_t s, const RelxTables &tab, const RelxSetState *sst,
+                        const RelxRadial *srad, int nza, float *dist);
 
 cudaError_t xillver_set_smem(int n_incl);
 // bounded-wait self-test: writes the status of a wait that cannot complete (RELX_ERR_TIMEOUT)

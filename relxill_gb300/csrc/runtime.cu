@@ -812,6 +812,13 @@ struct Context {
   cudaStream_t gstream[2] = {nullptr, nullptr};  // streams of the even and odd groups
   RelCache cache;         // line-profile cache (off until relx_cache_config)
   cudaStream_t aux[2] = {nullptr, nullptr};      // streams of pipelined chunks
+  // per launching stream, a side stream for the emission-angle histograms and the xillver stage,
+  // which depend on the set-up only and run beside the line profile (fork and join events)
+  struct Side {
+    cudaStream_t main, side;
+    cudaEvent_t fork, join;
+  };
+  std::vector<Side> sides;
   cudaEvent_t aux_ev[2] = {nullptr, nullptr}, fork_ev = nullptr;
   // CUDA graphs of recent batch shapes (replayed when the shape and workspace recur)
   struct GraphEntry {
@@ -1001,6 +1008,24 @@ static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b,
   return 0;
 }
 
+// the side stream of launching stream s (null when none can be made: the work then stays on s)
+static Context::Side *side_of(Context &C, cudaStream_t s) {
+  for (auto &x : C.sides)
+    if (x.main == s) return &x;
+  if (C.sides.size() >= 16) return nullptr;
+  Context::Side x{s, nullptr, nullptr, nullptr};
+  if (cudaStreamCreateWithFlags(&x.side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&x.fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    if (x.side) cudaStreamDestroy(x.side);
+    if (x.fork) cudaEventDestroy(x.fork);
+    return nullptr;
+  }
+  C.sides.push_back(x);
+  return &C.sides.back();
+}
+
 // the kernel sequence for one batch; all pointers are device pointers, asynchronous on `s`
 // The kernel sequence for the sets [base, base + n) of a batch, asynchronous on s.  Per-set
 // arrays are addressed from the range's first set; energy grids and fluxes keep the batch's
@@ -1058,10 +1083,39 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     RELX_CUDA(cache_fill(C.cache, s, sst, W.cslot.as<int>() + base, n, b.nza, b.nblk, kSumBinsH, prof, tsum,
                          dist));
   }
+  // relxill models: the emission-angle histograms and the xillver zone spectra depend on the set-up
+  // only; they run on a side stream while the line profile runs on s, and s waits for them
+  const bool relxill = relx_is_relxill(kind);
+  Context::Side *sd = relxill ? side_of(C, s) : nullptr;
+  cudaStream_t xs = sd ? sd->side : s;
+  if (sd) {
+    RELX_CUDA(cudaEventRecord(sd->fork, s));
+    RELX_CUDA(cudaStreamWaitEvent(xs, sd->fork, 0));
+  }
   {
-    ProfScope ps(PK_LINE, s, 1 + (b.any_limb ? 1 : 0) + (relx_is_relxill(kind) ? 1 : 0));
-    RELX_CUDA(launch_relline(relx_is_relxill(kind), n, b.line_tile, b.nblk, s, tab, sin, sst, rad,
-                             W.line_e.as<double>(), b.nza, prof, dist, tsum, b.any_limb));
+    ProfScope ps(PK_LINE, s, 1 + (b.any_limb ? 1 : 0));
+    RELX_CUDA(launch_relline(false, n, b.line_tile, b.nblk, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza,
+                             prof, dist, tsum, b.any_limb));
+  }
+  if (relxill) {
+    {
+      ProfScope ps(PK_LINE, xs);
+      RELX_CUDA(launch_hist(n, xs, tab, sst, rad, b.nza, dist));
+    }
+    {
+      // the zone kernel for sets with more than RELX_ZDENSE zones and for 6-parameter sets whose
+      // corners do not fit the de-duplicated list; the dense kernel, in table-row order, for the rest
+      const bool zone = b.nza > RELX_ZDENSE || cp;
+      const bool dense = b.nz_min <= RELX_ZDENSE;
+      ProfScope ps(PK_XILL, xs, (zone ? 1 : 0) + (dense ? 2 : 0));
+      int *order = dense ? W.order.as<int>() + base : nullptr;
+      if (dense) launch_xill_order(xs, sst, cor, zcor, n, order);
+      RELX_CUDA(launch_xillver(xs, tab, n, b.nza, zone, dense, sst, cor, zcor, dist, xill, W.err.as<int>(), order));
+    }
+    if (sd) {
+      RELX_CUDA(cudaEventRecord(sd->join, xs));
+      RELX_CUDA(cudaStreamWaitEvent(s, sd->join, 0));
+    }
   }
   if (cached) {
     ProfScope ps(PK_LINE, s);
@@ -1071,17 +1125,7 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     RELX_CUDA(cudaEventRecord(C.cache_ev, s));
     C.cache_ev_valid = true;
   }
-  if (relx_is_relxill(kind)) {
-    {
-      // the zone kernel for sets with more than RELX_ZDENSE zones and for 6-parameter sets whose
-      // corners do not fit the de-duplicated list; the dense kernel, in table-row order, for the rest
-      const bool zone = b.nza > RELX_ZDENSE || cp;
-      const bool dense = b.nz_min <= RELX_ZDENSE;
-      ProfScope ps(PK_XILL, s, (zone ? 1 : 0) + (dense ? 2 : 0));
-      int *order = dense ? W.order.as<int>() + base : nullptr;
-      if (dense) launch_xill_order(s, sst, cor, zcor, n, order);
-      RELX_CUDA(launch_xillver(s, tab, n, b.nza, zone, dense, sst, cor, zcor, dist, xill, W.err.as<int>(), order));
-    }
+  if (relxill) {
     {
       ProfScope ps(PK_CONV, s);
       conv_zone_kernel<<<dim3(b.nza, n), kConvThreadsH, conv_smem_bytes(), s>>>(tab, sst, prof, tsum, b.nblk,
@@ -1185,6 +1229,18 @@ static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     if (C.graph_seen.size() >= 32) C.graph_seen.erase(C.graph_seen.begin());
     C.graph_seen.push_back(key);
     return launch_direct(C, W, b, s, false);
+  }
+  // streams and events the captured sequence uses exist before the capture starts
+  if (relx_is_relxill(relx_kind(b.model))) {
+    (void) side_of(C, s);
+    if (b.chunk > 0 && b.n_sets >= 2 * b.chunk) {
+      for (int k = 0; k < 2; k++) {
+        if (!C.aux[k]) RELX_CUDA(cudaStreamCreateWithFlags(&C.aux[k], cudaStreamNonBlocking));
+        if (!C.aux_ev[k]) RELX_CUDA(cudaEventCreateWithFlags(&C.aux_ev[k], cudaEventDisableTiming));
+        (void) side_of(C, C.aux[k]);
+      }
+      if (!C.fork_ev) RELX_CUDA(cudaEventCreateWithFlags(&C.fork_ev, cudaEventDisableTiming));
+    }
   }
   const int64_t l0 = g_launches.load();
   RELX_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
