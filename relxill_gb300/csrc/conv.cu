@@ -409,7 +409,8 @@ struct FinSmem {
 // zone sum, primary continuum (PrimarySource.cpp:66-125), optional 3 keV
 // renormalisation (Relxill.cpp:249-259) and rebin to the caller's grid
 // (rebin_and_normalize_relxill_for_xspec, Relxill.cpp:267-278).
-__global__ void __launch_bounds__(kFinThreads) finalize_relxill_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
+template <int NT>
+__global__ void __launch_bounds__(NT) finalize_relxill_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
                                                                         const RelxSetState *__restrict__ sst,
                                                                         const float *__restrict__ cout, int nza,
                                                                         const double *__restrict__ user_e,
@@ -424,7 +425,7 @@ __global__ void __launch_bounds__(kFinThreads) finalize_relxill_kernel(RelxTable
   double *fo = flux + in.e_off - set;  // flux offsets: e_off counts n+1 edges per set
   if (s.status != RELX_OK || s.model < RELX_RELXILL) {
     if (s.model != RELX_RELCONV || s.status != RELX_OK)
-      for (int i = tid; i < nu; i += kFinThreads) fo[i] = 0.0;
+      for (int i = tid; i < nu; i += NT) fo[i] = 0.0;
     return;
   }
   const double *ce = tab.conv_e;
@@ -441,7 +442,7 @@ __global__ void __launch_bounds__(kFinThreads) finalize_relxill_kernel(RelxTable
     if (tid == 0) m.nth_norm = nth_normfac(tab.nth_grid->x, nth[set].sp, nth[set].n, zp1);
     __syncthreads();
   }
-  for (int k = s.out_lo + tid; k <= s.out_hi; k += kFinThreads) {
+  for (int k = s.out_lo + tid; k <= s.out_hi; k += NT) {
     float r = 0.0f;
     for (int z = 0; z < s.nz; z++) r += cout[((size_t) set * nza + z) * kN + k];
     r *= rfac;
@@ -465,12 +466,12 @@ __global__ void __launch_bounds__(kFinThreads) finalize_relxill_kernel(RelxTable
       m.nrm = (float) ((ce[ind + 1] - ce[ind]) / (double) m.spec[ind]);
     }
     __syncthreads();
-    for (int k = s.out_lo + tid; k <= s.out_hi; k += kFinThreads) m.spec[k] *= m.nrm;
+    for (int k = s.out_lo + tid; k <= s.out_hi; k += NT) m.spec[k] *= m.nrm;
     __syncthreads();
   }
   const double *ue = user_e + in.e_off;
   const double zf = (s.z > 0) ? (1 + s.z) : 1.0;
-  for (int i = tid; i < nu; i += kFinThreads) {
+  for (int i = tid; i < nu; i += NT) {
     double elo = ue[i], ehi = ue[i + 1];
     if (s.z > 0) { elo *= zf; ehi *= zf; }
     fo[i] = rebin_bin(tab, elo, ehi, m.spec);
@@ -546,5 +547,19 @@ __global__ void __launch_bounds__(kFinThreads) finalize_relline_kernel(const Rel
 
 size_t conv_smem_bytes() { return sizeof(ConvSmem); }
 size_t fin_smem_bytes() { return sizeof(FinSmem); }
+
+// wide: 512 threads per set (few sets: one set's bins spread over more threads); otherwise 128.
+// Every output is computed by one thread with the same arithmetic, so both give the same numbers.
+cudaError_t launch_finalize_relxill(cudaStream_t s, bool wide, int n_sets, const RelxTables &tab,
+                                    const RelxSetIn *sin, const RelxSetState *sst, const float *cout, int nza,
+                                    const double *user_e, double *flux, const NthTable *nth) {
+  if (n_sets <= 0) return cudaSuccess;
+  if (wide)
+    finalize_relxill_kernel<512><<<n_sets, 512, sizeof(FinSmem), s>>>(tab, sin, sst, cout, nza, user_e, flux, nth);
+  else
+    finalize_relxill_kernel<kFinThreads><<<n_sets, kFinThreads, sizeof(FinSmem), s>>>(tab, sin, sst, cout, nza, user_e,
+                                                                                     flux, nth);
+  return cudaGetLastError();
+}
 
 }  // namespace relx

@@ -225,8 +225,7 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
     conv_zone_kernel<<<dim3(nza, 1), kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sst, p.prof, p.tsum, ntile_max,
                                                                             kSumBinsH, p.xill, nza, p.cout,
                                                                             p.err);
-    finalize_relxill_kernel<<<1, kFinThreadsH, fin_smem_bytes(), s>>>(tab, p.sin, p.sst, p.cout, nza, d_energy, d_flux,
-                                                                      nullptr);
+    NOALLOC_CUDA(launch_finalize_relxill(s, true, 1, tab, p.sin, p.sst, p.cout, nza, d_energy, d_flux, nullptr));
   } else if (kind == RELX_RELCONV) {
     relconv_conv_kernel<<<1, kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sin, p.sst, p.prof, p.tsum, ntile_max,
                                                                     kSumBinsH, nza, d_energy, d_flux_in, p.cout,

@@ -94,9 +94,10 @@ __global__ void relconv_conv_kernel(RelxTables tab, const RelxSetIn *sin, const 
                                     const double *tsum, int ntile_max, int tile_bins, int nza, const double *user_e,
                                     const double *user_f, float *cout, int *sflag);
 // nth: the nthcomp tables of the sets (Cp models), or null
-__global__ void finalize_relxill_kernel(RelxTables tab, const RelxSetIn *sin, const RelxSetState *sst,
-                                        const float *cout, int nza, const double *user_e, double *flux,
-                                        const NthTable *nth);
+// zone sum, primary continuum and rebin to the caller's grid; wide: 512 threads per set (for few sets)
+cudaError_t launch_finalize_relxill(cudaStream_t s, bool wide, int n_sets, const RelxTables &tab,
+                                    const RelxSetIn *sin, const RelxSetState *sst, const float *cout, int nza,
+                                    const double *user_e, double *flux, const NthTable *nth);
 __global__ void finalize_relconv_kernel(RelxTables tab, const RelxSetIn *sin, const RelxSetState *sst,
                                         const float *cout, int nza, const double *user_e, const int *sflag,
                                         double *flux);

@@ -857,7 +857,6 @@ static int set_kernel_attrs(const Tables &T) {
   if (T.has_cp) RELX_CUDA(xillver_model_set_smem(T.dcp.x_nener, T.dcp.x_nener_pad));
   RELX_CUDA(cudaFuncSetAttribute(conv_zone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
   RELX_CUDA(cudaFuncSetAttribute(relconv_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
-  RELX_CUDA(cudaFuncSetAttribute(finalize_relxill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) fin_smem_bytes()));
   return 0;
 }
 
@@ -1134,8 +1133,7 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     }
     {
       ProfScope ps(PK_FIN, s);
-      finalize_relxill_kernel<<<n, kFinThreadsH, fin_smem_bytes(), s>>>(tab, sin, sst, cout, b.nza, user_e, flux,
-                                                                        ntab);
+      RELX_CUDA(launch_finalize_relxill(s, b.n_sets < 2 * 152, n, tab, sin, sst, cout, b.nza, user_e, flux, ntab));
     }
   } else if (kind == RELX_RELCONV) {
     ProfScope ps(PK_CONV, s, 2);  // convolution and finalize

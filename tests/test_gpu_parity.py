@@ -88,6 +88,17 @@ def test_deterministic_alone_and_in_batch(gpu):
         np.testing.assert_array_equal(one[0], a[i])
 
 
+def test_same_numbers_in_small_and_large_batches(gpu):
+    """Batches of fewer than 304 sets finalize with 512 threads per set, larger ones with 128; a set
+    gives the same numbers either way (and with or without the side stream of the xillver stage)."""
+    params, grids = _random_lp_sets(320, 11)
+    big, st = gpu.eval_batch("relxilllp", params, grids)
+    assert not st.any()
+    for i in (0, 157, 319):
+        one, _ = gpu.eval_batch("relxilllp", params[i:i + 1], grids[i:i + 1])
+        np.testing.assert_array_equal(one[0], big[i])
+
+
 def test_parameter_errors(gpu):
     e = grid(CASES[7][3])
     bad = list(CASES[7][2])
