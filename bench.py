@@ -36,6 +36,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "relxilllp spectra/s batched vs plain GPU at ≤1e-4 rel err; serve p50/p99 ms"
 N_SETS = 4096
+WORKLOAD = ("relxilllp batched, 4096 sets per GPU, per-set grids 300-5000 log bins 0.3-80 keV, "
+            "10 radial zones")
 N_PROF = 8  # kernel kinds of the per-kernel event profiler (relx_profile_name)
 
 
@@ -360,8 +362,9 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": total, "unit": "spectra/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"relxilllp, {per_step} sets per step drawn from the 4096-set batched workload",
-                   "tables": "synthetic full-size (xillver 1 GB)"},
+        "config": {"workload": WORKLOAD, "sets_per_gpu": N_SETS, "parallelism": "CPU processes",
+                   "tables": "synthetic full-size (xillver 1 GB)",
+                   "sample": f"{per_step} sets per step drawn from the 4096-set workload"},
         "cpu_baseline": {"value": total, "unit": "spectra/s", "cores": procs, "kind": "port",
                          "sample": f"{per_step} sets per step x {args.steps} steps on {procs} processes"},
         "e2e": {"value": total, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -636,8 +639,7 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (f64 radii, grids and normalisation sums)", "data": "synthetic",
-        "config": {"workload": "relxilllp batched, 4096 sets per GPU, per-set grids 300-5000 log bins 0.3-80 keV, "
-                               "10 radial zones", "sets_per_gpu": S, "parallelism": f"replicas x{world}",
+        "config": {"workload": WORKLOAD, "sets_per_gpu": S, "parallelism": f"replicas x{world}",
                    "tables": f"synthetic full-size, {tb.value / 1e9:.2f} GB on the device",
                    "l2": "inputs larger than L2 (1 GB xillver table, ~2 GB workspace per step)"},
         "e2e": e2e, "plain_gpu": plain, "batched_over_plain": (value / world / plain["value"]) if plain else None,
