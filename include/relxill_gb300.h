@@ -123,11 +123,12 @@ int relx_eval_batch_device(int model, int n_sets, const double *d_params, const 
  * evaluate (memory owned by another framework's caching allocator, a fixed
  * memory budget, or a loop where cudaMalloc/cudaFree would stall other
  * streams).  Intermediate arrays live in one static device array of about
- * 3 MB shared by all calls: calls whose device work overlaps race on it, so
+ * 3.8 MB shared by all calls: calls whose device work overlaps race on it, so
  * issue them on one stream or synchronise between them.  The first call on a
  * device looks up that array's address; make it before any stream capture.
  * Limits: one set, relline grids of at most 16384 bins, tables loaded by
- * relx_init on the current device beforehand (RELX_ERR_NOTABLE otherwise).
+ * relx_init on the current device beforehand (RELX_ERR_NOTABLE otherwise; the
+ * Cp models also need xillverCp_v3.4.fits).
  * d_params: npar doubles; d_energy: n_bins + 1 edges; d_flux_in: relconv input
  * (n_bins, else NULL); d_flux: n_bins outputs; d_status: one int (may be NULL).
  * Asynchronous on `stream` (a cudaStream_t; NULL: the default stream). */

@@ -16,6 +16,8 @@
 //   * relline: at most kMaxLineBins bins in the caller's grid (the line profile
 //     is computed on that grid); the other models use the fixed conv grid;
 //   * xillver tables with at most kMaxXillBins energy bins;
+//   * the Cp models need the xillverCp table (status RELX_ERR_NOTABLE without it); relxilllpCp
+//     reserves the zones of an ionisation gradient, since its gradient type is a parameter;
 //   * the tables must have been loaded by relx_init on the current device
 //     before the call (loading allocates).
 //
@@ -30,6 +32,7 @@
 // is written in full before it is read.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <mutex>
 
@@ -57,9 +60,11 @@ constexpr size_t kScratchBytes =
     align_up(sizeof(double) * (size_t) ((kMaxLineBins + kSumBinsH - 1) / kSumBinsH) * RELX_NZMAX) +  // block sums
     align_up(sizeof(float) * (size_t) RELX_NZMAX * kMaxXillBins) +                           // xillver spectra
     align_up(sizeof(float) * (size_t) RELX_NZMAX * RELX_NCONV) +                             // convolved spectra
+    align_up(sizeof(double) * (RELX_NZMAX + 1)) + align_up(sizeof(NthTable)) +               // nthcomp (Cp)
+    align_up(sizeof(float4) * (size_t) (RELX_NZMAX + 1) * 900) +                             // nthcomp solve
     3 * kAlign;                                                                              // flags
 
-// the scratch of this entry point (about 3 MB)
+// the scratch of this entry point (about 3.8 MB)
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 struct NoallocPtrs {
@@ -68,8 +73,10 @@ struct NoallocPtrs {
   RelxRadial *rad;
   RelxCorners *cor;
   RelxZoneCorners *zcor;
-  double *line_e, *tsum;
+  double *line_e, *tsum, *nthq;
   float *prof, *dist, *xill, *cout;
+  NthTable *nth;
+  float4 *nthscr;
   int *sflag, *err, *status;
 };
 
@@ -93,6 +100,10 @@ static size_t carve(unsigned char *base, int model, int nza, int nbins, int ntil
   p->tsum = (double *) take(sizeof(double) * ntile_max * nza);
   p->xill = (float *) take(sizeof(float) * (size_t) nza * x_pad);
   p->cout = (float *) take(sizeof(float) * (size_t) nza * RELX_NCONV);
+  const bool cp = relx_is_cp(model);
+  p->nthq = (double *) take(cp ? sizeof(double) * (RELX_NZMAX + 1) : 0);
+  p->nth = (NthTable *) take(cp ? sizeof(NthTable) : 0);
+  p->nthscr = (float4 *) take(cp ? nthcomp_scratch_bytes(1, nza, relx_kind(model) == RELX_XILLVER) : 0);
   p->sflag = (int *) take(sizeof(int));
   p->err = (int *) take(sizeof(int));
   p->status = (int *) take(sizeof(int));
@@ -175,8 +186,7 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
   if (model < 0 || model >= RELX_NMODELS || !d_params || !d_energy || !d_flux || n_bins < 1)
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: bad arguments");
   const int kind = relx_kind(model);
-  if (relx_is_cp(model))
-    return fail(RELX_ERR_UNSUPPORTED, "relx_eval_one_noalloc: the Cp models are evaluated through the batched calls");
+  const bool cp = relx_is_cp(model);
   if (kind == RELX_RELCONV && !d_flux_in)
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: relconv needs the input spectrum");
   if (ion_grad_type < 0 || ion_grad_type > 2)
@@ -188,15 +198,20 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
     return fail(RELX_ERR_ARG, msg);
   }
   int tab_dev = -1, dev = -1;
-  const RelxTables *tp = runtime_tables(&tab_dev);
-  if (!tp) return fail(RELX_ERR_NOTABLE, "relx_eval_one_noalloc: tables not loaded (call relx_init first)");
+  const RelxTables *tp = runtime_tables(&tab_dev, cp);
+  if (!tp)
+    return fail(RELX_ERR_NOTABLE, cp ? "relx_eval_one_noalloc: tables not loaded or xillverCp_v3.4.fits not found"
+                                     : "relx_eval_one_noalloc: tables not loaded (call relx_init first)");
   NOALLOC_CUDA(cudaGetDevice(&dev));
   if (dev != tab_dev) return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: the tables live on another device");
   const RelxTables tab = *tp;
   if ((relx_is_relxill(kind) || kind == RELX_XILLVER) && tab.x_nener_pad > kMaxXillBins)
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: xillver table has more energy bins than the scratch holds");
   int nzones_env = 0, flags = 0;
-  const int nza = runtime_zones(model, ion_grad_type, &nzones_env, &flags);
+  int nza = runtime_zones(model, ion_grad_type, &nzones_env, &flags);
+  // relxilllpCp carries its ionisation-gradient type as a parameter (on the device here): room for
+  // the zones of either choice
+  if (model == RELX_RELXILLLPCP) nza = std::max(nza, runtime_zones(model, 1, nullptr, nullptr));
   if (nza < 1 || nza > RELX_NZMAX) return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: zone count out of range");
   const int gbins = (kind == RELX_RELLINE) ? n_bins : RELX_NCONV;
   const int ntile_max = (gbins + kSumBinsH - 1) / kSumBinsH;  // 256-bin profile-sum blocks
@@ -210,7 +225,9 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
   noalloc_pack_kernel<<<1, 32, 0, s>>>(runtime_nparams(model), d_params, n_bins, ion_grad_type, iongrad_index,
                                        nzones_env, flags, nza, p.sin, p.sflag, p.err);
   if (kind == RELX_XILLVER) {
-    NOALLOC_CUDA(launch_xillver_model(s, tab, 1, p.sin, d_energy, p.sst, d_flux, nullptr, nullptr));
+    if (cp) NOALLOC_CUDA(launch_nthcomp(s, tab, p.sin, p.sst, 1, 1, true, p.nthq, p.nth, nullptr, nullptr, p.nthscr, 1, 0));
+    NOALLOC_CUDA(launch_xillver_model(s, tab, 1, p.sin, d_energy, p.sst, d_flux, cp ? p.nthq : nullptr,
+                                      cp ? p.nth : nullptr));
     noalloc_status_kernel<<<1, 32, 0, s>>>(p.sst, p.sflag, p.err, p.status, d_status);
     NOALLOC_CUDA(cudaGetLastError());
     runtime_set_error(RELX_OK, "");
@@ -218,14 +235,17 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
   }
   setup_kernel<<<1, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, model, p.sin, d_energy, p.line_e, p.sst, p.rad,
                                                             p.cor, p.zcor);
+  if (cp) NOALLOC_CUDA(launch_nthcomp(s, tab, p.sin, p.sst, 1, nza, false, p.nthq, p.nth, p.cor, p.zcor, p.nthscr, nza + 1, 0));
   NOALLOC_CUDA(launch_relline(relx_is_relxill(kind), 1, 512, ntile_max, s, tab, p.sin, p.sst, p.rad, p.line_e, nza,
                               p.prof, p.dist, p.tsum, kind == RELX_RELLINE || kind == RELX_RELCONV));
   if (relx_is_relxill(kind)) {
-    NOALLOC_CUDA(launch_xillver(s, tab, 1, nza, nza > RELX_ZDENSE, nza <= RELX_ZDENSE, p.sst, p.cor, p.zcor, p.dist, p.xill, p.err, nullptr));
+    NOALLOC_CUDA(launch_xillver(s, tab, 1, nza, nza > RELX_ZDENSE || cp, true, p.sst, p.cor, p.zcor, p.dist, p.xill,
+                                p.err, nullptr));
     conv_zone_kernel<<<dim3(nza, 1), kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sst, p.prof, p.tsum, ntile_max,
                                                                             kSumBinsH, p.xill, nza, p.cout,
                                                                             p.err);
-    NOALLOC_CUDA(launch_finalize_relxill(s, true, 1, tab, p.sin, p.sst, p.cout, nza, d_energy, d_flux, nullptr));
+    NOALLOC_CUDA(launch_finalize_relxill(s, true, 1, tab, p.sin, p.sst, p.cout, nza, d_energy, d_flux,
+                                         cp ? p.nth : nullptr));
   } else if (kind == RELX_RELCONV) {
     relconv_conv_kernel<<<1, kConvThreadsH, conv_smem_bytes(), s>>>(tab, p.sin, p.sst, p.prof, p.tsum, ntile_max,
                                                                     kSumBinsH, nza, d_energy, d_flux_in, p.cout,

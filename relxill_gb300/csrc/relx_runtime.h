@@ -8,8 +8,9 @@
 
 namespace relx {
 
-// device tables loaded by relx_init (null until then); *device = the device they live on
-const RelxTables *runtime_tables(int *device);
+// device tables loaded by relx_init (null until then); *device = the device they live on.
+// cp: the descriptor of the Cp models (the xillverCp table; null when that table was not found)
+const RelxTables *runtime_tables(int *device, bool cp = false);
 // radial zones a parameter set uses, and the environment options read for the call
 int runtime_zones(int model, int ion_grad_type, int *nzones_env, int *flags);
 // parameters of a model (-1 for an unknown model)

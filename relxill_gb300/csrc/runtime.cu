@@ -1617,12 +1617,12 @@ int cache_configure(int slots) {
 }
 
 // ---- hooks for the other host translation units (not part of the C ABI) ----
-const RelxTables *runtime_tables(int *device) {
+const RelxTables *runtime_tables(int *device, bool cp) {
   Context &C = ctx();
   std::lock_guard<std::mutex> lock(C.mu);
-  if (!C.T.loaded) return nullptr;
+  if (!C.T.loaded || (cp && !C.T.has_cp)) return nullptr;
   if (device) *device = C.device;
-  return &C.T.d;
+  return cp ? &C.T.dcp : &C.T.d;
 }
 int runtime_zones(int model, int ion_grad_type, int *nzones_env, int *flags) {
   const EnvOpts env = read_env();

@@ -12,7 +12,8 @@ from tolerance import assert_close
 
 pytestmark = pytest.mark.gpu
 
-MODELS = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3, "relline_lp": 4, "relconv_lp": 5, "xillver": 6}
+MODELS = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3, "relline_lp": 4, "relconv_lp": 5, "xillver": 6,
+          "xillverCp": 7, "relxillCp": 8, "relxilllpCp": 9}
 RELX_ERR_ARG = 9
 
 
@@ -60,7 +61,8 @@ def test_noalloc_matches_batch_on_two_calls_in_a_row(gpu):
     torch = pytest.importorskip("torch")
     f = _fn(gpu)
     names = ["relxilllp_a", "relxill_cfg2", "relline_cfg1", "relconv_a", "relxilllp_alpha", "relxilllp_b",
-             "rellinelp_b", "relconvlp_b", "xillver_b", "xillver_d"]
+             "rellinelp_b", "relconvlp_b", "xillver_b", "xillver_d", "xillvercp_a", "xillvercp_b", "relxillcp_b",
+             "relxilllpcp_a", "relxilllpcp_rr", "relxilllpcp_alpha", "relxilllpcp_pl"]
     for name in names:
         _, model, params, gspec, igt, igi = _case(name)
         e = grid(gspec)
