@@ -1083,9 +1083,10 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
                          dist));
   }
   // relxill models: the emission-angle histograms and the xillver zone spectra depend on the set-up
-  // only; they run on a side stream while the line profile runs on s, and s waits for them
+  // only; they run on a side stream while the line profile runs on s, and s waits for them (all on
+  // s while per-kernel timing is on, so that the kernels' intervals do not overlap)
   const bool relxill = relx_is_relxill(kind);
-  Context::Side *sd = relxill ? side_of(C, s) : nullptr;
+  Context::Side *sd = (relxill && !g_prof.on) ? side_of(C, s) : nullptr;
   cudaStream_t xs = sd ? sd->side : s;
   if (sd) {
     RELX_CUDA(cudaEventRecord(sd->fork, s));
