@@ -1446,9 +1446,22 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
 // one group overlap the kernels of the other, and the host copies the results of group g out while
 // the GPU computes the later groups.  Both workspaces are reserved for the largest group before the
 // first one is queued (no buffer is reallocated while a group is in flight).
-static int host_groups(int n_sets) {
-  if (n_sets < 2048) return 1;
-  return std::min(8, n_sets / 1024);
+// group boundaries s0[0..ng]: groups of about `per` sets (RELX_HOST_GROUP_SETS, default 1024), the
+// first and the last a quarter of that, so that the GPU starts early and the last copy out is short
+static std::vector<int> host_groups(int n_sets) {
+  const char *e = std::getenv("RELX_HOST_GROUP_SETS");
+  const int per = (e && std::atoi(e) >= 64) ? std::atoi(e) : 1024;
+  std::vector<int> b{0};
+  if (n_sets < 2 * per) {
+    b.push_back(n_sets);
+    return b;
+  }
+  const int edge = per / 4, mid = n_sets - 2 * edge;
+  const int nm = std::max(1, std::min(14, (mid + per / 2) / per));
+  b.push_back(edge);
+  for (int g = 1; g <= nm; g++) b.push_back(edge + (int) ((int64_t) g * mid / nm));
+  b.push_back(n_sets);
+  return b;
 }
 
 static int eval_host(const HostBatch &hb, double *flux, int *status) {
@@ -1460,13 +1473,12 @@ static int eval_host(const HostBatch &hb, double *flux, int *status) {
   const int n = hb.n_sets;
   if (hb.model < 0 || hb.model >= RELX_NMODELS || n <= 0 || !hb.params || !hb.energy || !hb.eoff)
     return RELX_ERR_ARG;
-  const int ng = host_groups(n);
+  const std::vector<int> s0 = host_groups(n);
+  const int ng = (int) s0.size() - 1;
   const int npar = model_nparams(hb.model);
   const bool conv = relx_kind(hb.model) == RELX_RELCONV;
   std::vector<std::vector<int64_t>> offs(ng);
   std::vector<HostBatch> sub(ng);
-  std::vector<int> s0(ng + 1);
-  for (int g = 0; g <= ng; g++) s0[g] = (int) ((int64_t) g * n / ng);
   for (int g = 0; g < ng; g++) {
     const int a = s0[g], m = s0[g + 1] - a;
     const int64_t e0 = hb.eoff[a];
