@@ -237,7 +237,7 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
                                                             p.cor, p.zcor);
   if (cp) NOALLOC_CUDA(launch_nthcomp(s, tab, p.sin, p.sst, 1, nza, false, p.nthq, p.nth, p.cor, p.zcor, p.nthscr, nza + 1, 0));
   NOALLOC_CUDA(launch_relline(relx_is_relxill(kind), 1, 512, ntile_max, s, tab, p.sin, p.sst, p.rad, p.line_e, nza,
-                              p.prof, p.dist, p.tsum, kind == RELX_RELLINE || kind == RELX_RELCONV));
+                              p.prof, p.dist, p.tsum, kind == RELX_RELLINE || kind == RELX_RELCONV, nza > 1));
   if (relx_is_relxill(kind)) {
     NOALLOC_CUDA(launch_xillver(s, tab, 1, nza, nza > RELX_ZDENSE || cp, true, p.sst, p.cor, p.zcor, p.dist, p.xill,
                                 p.err, nullptr));

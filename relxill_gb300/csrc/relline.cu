@@ -269,6 +269,7 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
   const RelxRadial &R = srad[set];
   const int nr = tab.rel_nr, nm = tab.rel_nmu0, ng = tab.rel_ng;
   const int nz = s.nz;
+  if ((int) blockIdx.z >= nz) return;
   const bool is_line = (s.model == RELX_RELLINE);
   const double *ge = is_line ? (line_e + sin[set].e_off) : tab.conv_e;
   const size_t pbase = is_line ? (size_t) sin[set].e_off : (size_t) set * nza * RELX_NCONV;
@@ -304,7 +305,10 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
 
   const float inv_dgs = (float) ((ng - 1) / (1.0 - 2 * 5e-3));
   const float sH = sqrtf(kH), isq = rsqrtf(kH * (1.0f - kH));
-  for (int z = 0; z < nz; z++) {
+  // with a zone axis in the grid (few sets) each CTA takes one zone; a zone's sums do not depend
+  // on the other zones, so the numbers are the same either way
+  const int zb = gridDim.z > 1 ? (int) blockIdx.z : 0, ze = gridDim.z > 1 ? min((int) blockIdx.z + 1, nz) : nz;
+  for (int z = zb; z < ze; z++) {
     const int i0 = s.zi0[z], i1 = s.zi1[z];
     for (int c0 = i0; c0 <= i1; c0 += kChunk) {
       const int cn = min(kChunk, i1 + 1 - c0);
@@ -442,7 +446,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, c
   HistSmem &m = *reinterpret_cast<HistSmem *>(smem_raw);
   const int set = blockIdx.x;
   const RelxSetState &s = sst[set];
-  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.cached) return;
+  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.cached || (int) blockIdx.y >= s.nz) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const RelxRadial &R = srad[set];
   const int nr = tab.rel_nr, nm = tab.rel_nmu0, ng = tab.rel_ng, n_incl = tab.x_nincl;
@@ -471,7 +475,8 @@ __global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, c
   float(*lh)[32] = m.lh[warp];
   for (int j = 0; j < RELX_MAX_INCL; j++) lh[j][lane] = 0.0f;
   const float c4pi2 = (float) (4.0 * kPi * kPi);
-  for (int z = 0; z < s.nz; z++) {
+  const int zb = gridDim.y > 1 ? (int) blockIdx.y : 0, ze = gridDim.y > 1 ? min((int) blockIdx.y + 1, s.nz) : s.nz;
+  for (int z = zb; z < ze; z++) {
     const int i0 = s.zi0[z], i1 = s.zi1[z];
     for (int c0 = i0; c0 <= i1; c0 += kChunk) {
       const int cn = min(kChunk, i1 + 1 - c0);
@@ -574,10 +579,10 @@ cudaError_t relline_set_smem(int nr, int ng) {
 // tiles of `tile` bins (256 or 512) and, for relxill models, the emission-angle histogram
 cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream_t s, const RelxTables &tab,
                            const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
-                           int nza, float *prof, float *dist, double *tsum, bool any_limb) {
+                           int nza, float *prof, float *dist, double *tsum, bool any_limb, bool zsplit) {
   const int nr = tab.rel_nr, ng = tab.rel_ng;
   const int ntile = (nblk * kSumBins + tile - 1) / tile;
-  const dim3 grid(ntile, n_sets);
+  const dim3 grid(ntile, n_sets, zsplit ? nza : 1);
   if (tile == 256) {
     relline_kernel<false, 256><<<grid, kLineThreads, line_smem_t<false, 256>(nr, ng), s>>>(tab, sin, sst, srad, line_e,
                                                                                            nza, prof, tsum, nblk);
@@ -591,13 +596,15 @@ cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream
       relline_kernel<true, 512><<<grid, kLineThreads, line_smem_t<true, 512>(nr, ng), s>>>(tab, sin, sst, srad, line_e,
                                                                                            nza, prof, tsum, nblk);
   }
-  if (hist) hist_kernel<<<n_sets, kLineThreads, hist_smem_bytes(nr, ng), s>>>(tab, sst, srad, nza, dist);
+  if (hist)
+    hist_kernel<<<dim3(n_sets, zsplit ? nza : 1), kLineThreads, hist_smem_bytes(nr, ng), s>>>(tab, sst, srad, nza, dist);
   return cudaGetLastError();
 }
 
 cudaError_t launch_hist(int n_sets, cudaStream_t s, const RelxTables &tab, const RelxSetState *sst,
-                        const RelxRadial *srad, int nza, float *dist) {
-  hist_kernel<<<n_sets, kLineThreads, hist_smem_bytes(tab.rel_nr, tab.rel_ng), s>>>(tab, sst, srad, nza, dist);
+                        const RelxRadial *srad, int nza, float *dist, bool zsplit) {
+  hist_kernel<<<dim3(n_sets, zsplit ? nza : 1), kLineThreads, hist_smem_bytes(tab.rel_nr, tab.rel_ng), s>>>(
+      tab, sst, srad, nza, dist);
   return cudaGetLastError();
 }
 

@@ -29,10 +29,11 @@ cudaError_t relline_set_smem(int nr, int ng);
 // tile: energy bins per line-kernel CTA (256 or 512); nblk: 256-bin profile-sum blocks per set
 cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream_t s, const RelxTables &tab,
                            const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
-                           int nza, float *prof, float *dist, double *tsum, bool any_limb);
+                           int nza, float *prof, float *dist, double *tsum, bool any_limb,
+                           bool zsplit = false);
 // the emission-angle histograms alone (relxill models), for a launch on its own stream
 cudaError_t launch_hist(int n_sets, cudaStream_t s, const RelxTables &tab, const RelxSetState *sst,
-                        const RelxRadial *srad, int nza, float *dist);
+                        const RelxRadial *srad, int nza, float *dist, bool zsplit = false);
 
 cudaError_t xillver_set_smem(int n_incl);
 // bounded-wait self-test: writes the status of a wait that cannot complete (RELX_ERR_TIMEOUT)

@@ -1092,15 +1092,19 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
     RELX_CUDA(cudaEventRecord(sd->fork, s));
     RELX_CUDA(cudaStreamWaitEvent(xs, sd->fork, 0));
   }
+  // few sets: a CTA per zone as well, so that the line profile and the histograms of a single
+  // spectrum spread over more SMs (the same numbers: zones are summed separately either way)
+  const int ntile = (b.nblk * kSumBinsH + b.line_tile - 1) / b.line_tile;
+  const bool zsplit = b.nza > 1 && (int64_t) n * ntile < 2 * 152;
   {
     ProfScope ps(PK_LINE, s, 1 + (b.any_limb ? 1 : 0));
     RELX_CUDA(launch_relline(false, n, b.line_tile, b.nblk, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza,
-                             prof, dist, tsum, b.any_limb));
+                             prof, dist, tsum, b.any_limb, zsplit));
   }
   if (relxill) {
     {
       ProfScope ps(PK_LINE, xs);
-      RELX_CUDA(launch_hist(n, xs, tab, sst, rad, b.nza, dist));
+      RELX_CUDA(launch_hist(n, xs, tab, sst, rad, b.nza, dist, b.nza > 1 && n < 2 * 152));
     }
     {
       // the zone kernel for sets with more than RELX_ZDENSE zones and for 6-parameter sets whose
