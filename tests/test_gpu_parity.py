@@ -89,13 +89,24 @@ def test_deterministic_alone_and_in_batch(gpu):
 
 
 def test_same_numbers_in_small_and_large_batches(gpu):
-    """Batches of fewer than 304 sets finalize with 512 threads per set, larger ones with 128; a set
-    gives the same numbers either way (and with or without the side stream of the xillver stage)."""
+    """Few sets run the line profile and histograms with a CTA per zone and the finalize with 512
+    threads; many sets with one CTA per tile and 128.  A set gives the same numbers either way, for
+    relxilllp (lamp post) and relxill (broken power law)."""
     params, grids = _random_lp_sets(320, 11)
     big, st = gpu.eval_batch("relxilllp", params, grids)
     assert not st.any()
     for i in (0, 157, 319):
         one, _ = gpu.eval_batch("relxilllp", params[i:i + 1], grids[i:i + 1])
+        np.testing.assert_array_equal(one[0], big[i])
+    rng = np.random.default_rng(12)
+    n = 320
+    q = np.column_stack([rng.uniform(2, 4, n), rng.uniform(2, 4, n), rng.uniform(5, 30, n), rng.uniform(0, 0.998, n),
+                         rng.uniform(10, 80, n), -np.ones(n), np.full(n, 400.0), np.zeros(n), rng.uniform(1.5, 2.8, n),
+                         rng.uniform(0, 4, n), np.ones(n), np.full(n, 300.0), np.ones(n)])
+    big, st = gpu.eval_batch("relxill", q, grids)
+    assert not st.any()
+    for i in (0, 158, 319):
+        one, _ = gpu.eval_batch("relxill", q[i:i + 1], grids[i:i + 1])
         np.testing.assert_array_equal(one[0], big[i])
 
 
