@@ -28,7 +28,13 @@ __device__ __forceinline__ int conv_index(const RelxTables &tab, double e) {
   const double *ge = tab.conv_e;
   const float2 *gf = tab.conv_eff;  // .x = (float) ge
   const float ef = (float) e;
-  int k = (int) floorf((__logf(ef) - tab.conv_lg0) * tab.conv_ilg);
+  // the grid is logarithmic (edge k at exp(log E_0 + k step)), so the float position kf is the bin
+  // up to about 1e-3 of a bin (logf, the rounding of e, of the two constants and of the product);
+  // more than 4e-3 of a bin away from an edge the bin is certain without reading the grid
+  const float kf = (logf(ef) - tab.conv_lg0) * tab.conv_ilg;
+  const float kfl = floorf(kf), fr = kf - kfl;
+  int k = (int) kfl;
+  if (fr > 4e-3f && fr < 1.0f - 4e-3f && kfl >= 0.0f && kfl <= (float) (RELX_NCONV - 1)) return k;
   k = max(0, min(k, RELX_NCONV - 1));
   // ge[k] > e, decided in float unless the float values tie
   while (k > 0 && (gf[k].x > ef || (gf[k].x == ef && ge[k] > e))) k--;
