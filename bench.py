@@ -240,7 +240,7 @@ def _time_device_variant(R, L, torch, dev, steps: int, warmup: int, params, grid
     import oracle_lib
 
     max_err = 0.0
-    for i in range(n_check):
+    for i in range(min(n_check, n)):
         st, ref = oracle_lib.evaluate(model, params[i], grids[i], None, igt_value, 0.0)
         got = out[offs[i] - i: offs[i + 1] - i - 1]
         m = ref > 1e-6 * ref.max()
@@ -596,7 +596,7 @@ def run_gpu(args):
         rrad = run_rrad(R, L, torch, dev, args.steps, args.warmup)
     cp = None
     if not args.no_cp:
-        cp = run_cp(R, L, torch, dev, args.steps, args.warmup)
+        cp = run_cp(R, L, torch, dev, args.steps, args.warmup, n=S)
 
     serve = None
     if not args.no_serve:

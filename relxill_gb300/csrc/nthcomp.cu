@@ -38,7 +38,7 @@
 
 namespace relx {
 
-constexpr int kNthThreads = 64;
+constexpr int kNthThreads = 128;
 constexpr int kNthMaxJ = 899;  // the reference's largest grid index (donthcomp.c:360)
 
 static double lg10_h(double x) { return 0.43429448190325182765 * std::log(x); }
@@ -203,6 +203,15 @@ __global__ void __launch_bounds__(kNthThreads) nthcomp_kernel(const NthGrid *__r
                                                               int per, int n_sets, int nq, double *__restrict__ qout,
                                                               NthTable *__restrict__ tabs, float4 *__restrict__ scr,
                                                               int64_t ncont_all, int64_t c_off) {
+  // the photon grid in shared memory (58 KB, read at every point of both sweeps)
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  NthPoint *Pg = reinterpret_cast<NthPoint *>(smem_raw);
+  {
+    const float4 *src = reinterpret_cast<const float4 *>(G->p);
+    float4 *dst = reinterpret_cast<float4 *>(Pg);
+    for (int i = threadIdx.x; i < (RELX_NTH_N + 1) * 4; i += kNthThreads) dst[i] = src[i];
+  }
+  __syncthreads();
   const int64_t c = (int64_t) blockIdx.x * kNthThreads + threadIdx.x;
   if (c >= (int64_t) n_sets * per) return;
   const int set = (int) (c / per), k = (int) (c - (int64_t) set * per);
@@ -235,23 +244,23 @@ __global__ void __launch_bounds__(kNthThreads) nthcomp_kernel(const NthGrid *__r
   const int jmax = r >= (double) kNthMaxJ ? kNthMaxJ : min((int) r + 1, kNthMaxJ);
   const int jnr = min(G->jnr0, jmax - 1), jrel = min(G->jrel0, jmax);
   const float2 tau = ff_from_double(tautom), th = ff_from_double(theta);
-  const float2 xnr = G->p[jnr].x, invdx = ff_from_double(1.0 / (G->x[jrel] - G->x[jnr]));
+  const float2 xnr = Pg[jnr].x, invdx = ff_from_double(1.0 / (G->x[jrel] - G->x[jnr]));
   float4 *sc = scr + c_off + c;
 
   // forward sweep: a u(j+1) + b u(j) + c u(j-1) = d for j = 2 .. jmax - 1, u(1) = aa u(2), u(jmax) = 0
   // a_j = -A_j, c_j = T_{j-1}, b_j = A_{j-1} - T_j + x_j^3 bt_j with
   // A_j = tautom cd_j (theta iw_j + 1/2), T_j = tautom cd_j (1/2 - theta iw_j)
-  const float2 u1 = ff_mul(th, G->p[1].iw);
+  const float2 u1 = ff_mul(th, Pg[1].iw);
   const float2 aa = ff_mul(ff_addf(u1, .5f), ff_rcp(ff_addf(u1, -.5f)));
   float2 Ap, Tp;
   {
-    const float2 P1 = ff_mul(tau, G->p[1].cd);
+    const float2 P1 = ff_mul(tau, Pg[1].cd);
     Ap = ff_mul(P1, ff_addf(u1, .5f));
     Tp = ff_mul(P1, ff_addf(ff_neg(u1), .5f));
   }
   float2 gm = make_float2(0.f, 0.f), dd = make_float2(0.f, 0.f);
   for (int j = 2; j <= jmax - 1; j++) {
-    const NthPoint P = G->p[j];
+    const NthPoint P = Pg[j];
     const float2 u = ff_mul(th, P.iw);
     const float2 Pj = ff_mul(tau, P.cd);
     const float2 A = ff_mul(Pj, ff_addf(u, .5f)), Tj = ff_mul(Pj, ff_addf(ff_neg(u), .5f));
@@ -275,24 +284,33 @@ __global__ void __launch_bounds__(kNthThreads) nthcomp_kernel(const NthGrid *__r
   // back sweep: u, E F_E = x^4 u bt (donthcomp.c:603-610), the normalisation sum and the table
   const int ih = min(G->ih0, jmax), il = ih - 1;
   float2 un = make_float2(0.f, 0.f), qs = make_float2(0.f, 0.f), s_il = un, s_ih = un;
-  for (int j = jmax - 1; j >= 1; j--) {
-    float2 uj;
-    if (j >= 2) {
-      const float4 v = sc[(size_t) j * ncont_all];
-      uj = ff_add(make_float2(v.z, v.w), ff_neg(ff_mul(make_float2(v.x, v.y), un)));
-    } else {
-      uj = ff_mul(aa, un);
+  // the scratch is read 8 points at a time (independent loads in flight together)
+  for (int j0 = jmax - 1; j0 >= 1; j0 -= 8) {
+    float4 vb[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+      if (j0 - q >= 2) vb[q] = sc[(size_t) (j0 - q) * ncont_all];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int j = j0 - q;
+      if (j < 1) break;
+      float2 uj;
+      if (j >= 2) {
+        uj = ff_add(make_float2(vb[q].z, vb[q].w), ff_neg(ff_mul(make_float2(vb[q].x, vb[q].y), un)));
+      } else {
+        uj = ff_mul(aa, un);
+      }
+      const NthPoint P = Pg[j];
+      const float2 sp = ff_mul(ff_mul(P.x4, uj), nth_bt(P, j, tau, jnr, jrel, xnr, invdx));
+      qs = ff_add(qs, ff_mul(P.g, sp));
+      if (j == il) s_il = sp;
+      if (j == ih) s_ih = sp;
+      if (T) {
+        T->sp[j] = ff_to_double(sp);
+        T->spf[j] = __fadd_rn(sp.x, sp.y);
+      }
+      un = uj;
     }
-    const NthPoint P = G->p[j];
-    const float2 sp = ff_mul(ff_mul(P.x4, uj), nth_bt(P, j, tau, jnr, jrel, xnr, invdx));
-    qs = ff_add(qs, ff_mul(P.g, sp));
-    if (j == il) s_il = sp;
-    if (j == ih) s_ih = sp;
-    if (T) {
-      T->sp[j] = ff_to_double(sp);
-      T->spf[j] = __fadd_rn(sp.x, sp.y);
-    }
-    un = uj;
   }
   if (T) {
     T->sp[jmax] = 0.0;
@@ -340,6 +358,11 @@ __global__ void nthcomp_apply_kernel(RelxSetState *__restrict__ sst, const doubl
   if (tid == 0) s.src_norm = 1.0 / q0;
 }
 
+cudaError_t nthcomp_set_smem() {
+  return cudaFuncSetAttribute(nthcomp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int) (sizeof(NthPoint) * (RELX_NTH_N + 1)));
+}
+
 size_t nthcomp_scratch_bytes(int n_sets, int nza, bool params) {
   return (size_t) n_sets * (params ? 1 : nza + 1) * (kNthMaxJ + 1) * sizeof(float4);
 }
@@ -351,7 +374,7 @@ cudaError_t launch_nthcomp(cudaStream_t s, const RelxTables &tab, const RelxSetI
   const int nq = RELX_NZMAX + 1;
   const int per = params ? 1 : nza + 1;
   const int64_t ncont = (int64_t) n_sets * per;
-  nthcomp_kernel<<<(unsigned) ((ncont + kNthThreads - 1) / kNthThreads), kNthThreads, 0, s>>>(
+  nthcomp_kernel<<<(unsigned) ((ncont + kNthThreads - 1) / kNthThreads), kNthThreads, sizeof(NthPoint) * (RELX_NTH_N + 1), s>>>(
       tab.nth_grid, sin, sst, params, per, n_sets, nq, q, tabs, scr, ncont_all, c_off);
   if (!params) nthcomp_apply_kernel<<<n_sets, 128, 0, s>>>(sst, q, nq, cor, zcor);
   return cudaGetLastError();

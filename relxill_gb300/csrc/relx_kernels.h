@@ -68,6 +68,7 @@ cudaError_t launch_xill_corner_flux(cudaStream_t s, const double *rowflux, const
 // the nthcomp photon grid and its per-point constants (host, FP64); co: the coarse normalisation
 // grid's edges, bins starting inside [band_lo, band_hi] count
 int nth_grid_build(const std::vector<double> &co, double band_lo, double band_hi, NthGrid &G);
+cudaError_t nthcomp_set_smem();
 // scratch of launch_nthcomp for n_sets sets (float4 per grid point and continuum)
 size_t nthcomp_scratch_bytes(int n_sets, int nza, bool params);
 // per set: the normalisation (calcNormWrtXillverTableSpec) of the source continuum (q[set][0]) and of

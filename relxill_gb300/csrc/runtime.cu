@@ -852,6 +852,7 @@ static Context &ctx() {
 static int set_kernel_attrs(const Tables &T) {
   RELX_CUDA(cudaFuncSetAttribute(setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) setup_smem_bytes()));
   RELX_CUDA(relline_set_smem(T.d.rel_nr, T.d.rel_ng));
+  RELX_CUDA(nthcomp_set_smem());
   RELX_CUDA(xillver_set_smem(T.d.x_nincl));
   RELX_CUDA(xillver_model_set_smem(T.d.x_nener, T.d.x_nener_pad));
   if (T.has_cp) RELX_CUDA(xillver_model_set_smem(T.dcp.x_nener, T.dcp.x_nener_pad));
