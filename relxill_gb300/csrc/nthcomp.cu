@@ -324,6 +324,125 @@ __global__ void __launch_bounds__(kNthThreads) nthcomp_kernel(const NthGrid *__r
   *q = ff_to_double(qs) * normfac * (1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi));
 }
 
+// The same continua for few sets, one CTA per continuum: the per-point quantities (the tridiagonal
+// coefficients A and T, tautom times the escape probability, x^3 / seed / x^4 / weight of the grid)
+// are formed by all threads at once into shared memory, and thread 0 runs only the two recurrences
+// and the normalisation sum, with the operations and the order of nthcomp_kernel: the same numbers,
+// with a serial chain a few times shorter.
+struct NthCoopSmem {
+  float2 A[RELX_NTH_N + 1], T[RELX_NTH_N + 1], bt[RELX_NTH_N + 1], b[RELX_NTH_N + 1];
+  float2 xd[RELX_NTH_N + 1], x4[RELX_NTH_N + 1], g[RELX_NTH_N + 1];
+  float2 gm[RELX_NTH_N + 1], dd[RELX_NTH_N + 1], sp[RELX_NTH_N + 1];
+  int skip;
+};
+
+constexpr int kNthCoopThreads = 256;
+
+__global__ void __launch_bounds__(kNthCoopThreads) nthcomp_coop_kernel(const NthGrid *__restrict__ G,
+                                                                       const RelxSetIn *__restrict__ sin,
+                                                                       const RelxSetState *__restrict__ sst,
+                                                                       bool params, int per, int nq,
+                                                                       double *__restrict__ qout,
+                                                                       NthTable *__restrict__ tabs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  NthCoopSmem &m = *reinterpret_cast<NthCoopSmem *>(smem_raw);
+  const int set = blockIdx.x / per, k = blockIdx.x - set * per, tid = threadIdx.x;
+  double gam, kte;
+  if (params) {
+    gam = sin[set].p[0];
+    kte = sin[set].p[2];
+  } else {
+    const RelxSetState &s = sst[set];
+    if (s.status != RELX_OK || s.prim != 1 || k > s.nz) return;  // block-uniform
+    const double shift = k == 0 ? 1.0 : s.zshift[k - 1];
+    if (k > 0 && shift == 1.0) return;
+    gam = s.gam;
+    kte = s.ect_src * shift;
+  }
+  double *q = qout + (size_t) set * nq + k;
+  NthTable *Tt = (k == 0) ? &tabs[set] : nullptr;
+  const double tempbb = .05 / 511., theta = kte / 511.;
+  const double d1 = gam + .5;
+  const double tautom = sqrt(3. / (theta * (d1 * d1 - 2.25)) + 2.25) - 1.5;
+  const double xmin = tempbb * 1e-4, xmax = theta * 40.;
+  const double r = nth_lg10(xmax / xmin) / .02;
+  if (!(r >= 3.0)) {
+    if (tid == 0) {
+      *q = __longlong_as_double(0x7ff8000000000000ll);
+      if (Tt) Tt->n = 0;
+    }
+    return;
+  }
+  const int jmax = r >= (double) kNthMaxJ ? kNthMaxJ : min((int) r + 1, kNthMaxJ);
+  const int jnr = min(G->jnr0, jmax - 1), jrel = min(G->jrel0, jmax);
+  const float2 tau = ff_from_double(tautom), th = ff_from_double(theta);
+  const float2 xnr = G->p[jnr].x, invdx = ff_from_double(1.0 / (G->x[jrel] - G->x[jnr]));
+  // per point, in parallel
+  for (int j = 1 + tid; j <= jmax - 1; j += kNthCoopThreads) {
+    const NthPoint P = G->p[j];
+    const float2 u = ff_mul(th, P.iw);
+    const float2 Pj = ff_mul(tau, P.cd);
+    m.A[j] = ff_mul(Pj, ff_addf(u, .5f));
+    m.T[j] = ff_mul(Pj, ff_addf(ff_neg(u), .5f));
+    m.bt[j] = nth_bt(P, j, tau, jnr, jrel, xnr, invdx);
+    m.xd[j] = P.xd;
+    m.x4[j] = P.x4;
+    m.g[j] = P.g;
+  }
+  __syncthreads();
+  for (int j = 2 + tid; j <= jmax - 1; j += kNthCoopThreads)
+    m.b[j] = ff_add(ff_add(m.A[j - 1], ff_neg(m.T[j])), ff_mul(G->p[j].x3, m.bt[j]));
+  __syncthreads();
+  const int ih = min(G->ih0, jmax), il = ih - 1;
+  if (tid == 0) {
+    const float2 u1 = ff_mul(th, G->p[1].iw);
+    const float2 aa = ff_mul(ff_addf(u1, .5f), ff_rcp(ff_addf(u1, -.5f)));
+    float2 gm = make_float2(0.f, 0.f), dd = make_float2(0.f, 0.f);
+    for (int j = 2; j <= jmax - 1; j++) {
+      const float2 Tp = m.T[j - 1];
+      float2 alp, num;
+      if (j == 2) {
+        alp = ff_add(m.b[j], ff_mul(Tp, aa));
+        num = m.xd[j];
+      } else {
+        alp = ff_add(m.b[j], ff_neg(ff_mul(Tp, gm)));
+        num = ff_add(m.xd[j], ff_neg(ff_mul(Tp, dd)));
+      }
+      const float2 ia = ff_rcp(alp);
+      gm = ff_mul(ff_neg(m.A[j]), ia);
+      dd = ff_mul(num, ia);
+      m.gm[j] = gm;
+      m.dd[j] = dd;
+    }
+    float2 un = make_float2(0.f, 0.f), qs = make_float2(0.f, 0.f), s_il = un, s_ih = un;
+    for (int j = jmax - 1; j >= 1; j--) {
+      const float2 uj = (j >= 2) ? ff_add(m.dd[j], ff_neg(ff_mul(m.gm[j], un))) : ff_mul(aa, un);
+      const float2 spj = ff_mul(ff_mul(m.x4[j], uj), m.bt[j]);
+      qs = ff_add(qs, ff_mul(m.g[j], spj));
+      if (j == il) s_il = spj;
+      if (j == ih) s_ih = spj;
+      m.sp[j] = spj;
+      un = uj;
+    }
+    const double xx = 1 / (1 / (1. / 511.));
+    const double sil = ff_to_double(s_il), sih = ff_to_double(s_ih);
+    const double normfac = 1 / (sil + (sih - sil) * (xx - G->x[il]) / (G->x[ih] - G->x[il]));
+    *q = ff_to_double(qs) * normfac * (1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi));
+  }
+  if (Tt) {
+    __syncthreads();
+    for (int j = 1 + tid; j <= jmax - 1; j += kNthCoopThreads) {
+      Tt->sp[j] = ff_to_double(m.sp[j]);
+      Tt->spf[j] = __fadd_rn(m.sp[j].x, m.sp[j].y);
+    }
+    if (tid == 0) {
+      Tt->sp[jmax] = 0.0;
+      Tt->spf[jmax] = 0.0f;
+      Tt->n = jmax;
+    }
+  }
+}
+
 // normalisation changes of the zones on their corner weights (the de-duplicated list or the per-zone
 // lists), source normalisation of the primary
 __global__ void nthcomp_apply_kernel(RelxSetState *__restrict__ sst, const double *__restrict__ q, int nq,
@@ -359,8 +478,11 @@ __global__ void nthcomp_apply_kernel(RelxSetState *__restrict__ sst, const doubl
 }
 
 cudaError_t nthcomp_set_smem() {
-  return cudaFuncSetAttribute(nthcomp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int) (sizeof(NthPoint) * (RELX_NTH_N + 1)));
+  cudaError_t e = cudaFuncSetAttribute(nthcomp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int) (sizeof(NthPoint) * (RELX_NTH_N + 1)));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(nthcomp_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int) sizeof(NthCoopSmem));
 }
 
 size_t nthcomp_scratch_bytes(int n_sets, int nza, bool params) {
@@ -374,8 +496,14 @@ cudaError_t launch_nthcomp(cudaStream_t s, const RelxTables &tab, const RelxSetI
   const int nq = RELX_NZMAX + 1;
   const int per = params ? 1 : nza + 1;
   const int64_t ncont = (int64_t) n_sets * per;
-  nthcomp_kernel<<<(unsigned) ((ncont + kNthThreads - 1) / kNthThreads), kNthThreads, sizeof(NthPoint) * (RELX_NTH_N + 1), s>>>(
-      tab.nth_grid, sin, sst, params, per, n_sets, nq, q, tabs, scr, ncont_all, c_off);
+  if (ncont <= 2 * 152) {  // few continua: one CTA each, the per-point work spread over its threads
+    nthcomp_coop_kernel<<<(unsigned) ncont, kNthCoopThreads, sizeof(NthCoopSmem), s>>>(tab.nth_grid, sin, sst, params,
+                                                                                     per, nq, q, tabs);
+  } else {
+    nthcomp_kernel<<<(unsigned) ((ncont + kNthThreads - 1) / kNthThreads), kNthThreads,
+                     sizeof(NthPoint) * (RELX_NTH_N + 1), s>>>(tab.nth_grid, sin, sst, params, per, n_sets, nq, q,
+                                                              tabs, scr, ncont_all, c_off);
+  }
   if (!params) nthcomp_apply_kernel<<<n_sets, 128, 0, s>>>(sst, q, nq, cor, zcor);
   return cudaGetLastError();
 }

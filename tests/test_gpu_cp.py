@@ -107,3 +107,30 @@ def test_relxillcp_mixed_zone_counts(gpu, oracle, monkeypatch):
         s, orc = oracle_lib.evaluate("relxillCp", p[i], grids[i], None, int(igt[i]), float(igi[i]))
         assert s == 0
         assert_close(out[i], orc, f"relxillCp set {i} (ion_grad_type {igt[i]})")
+
+
+def test_cp_same_numbers_alone_and_in_batch(gpu, monkeypatch):
+    """Few continua (one set) go through the one-CTA-per-continuum nthcomp kernel, many (64 sets of
+    11 continua) through the one-thread-per-continuum one; both give the same numbers."""
+    monkeypatch.setenv("RELXILL_NUM_RZONES", "10")
+    rng = np.random.default_rng(57)
+    n = 64
+    p = np.column_stack([rng.uniform(10, 80, n), rng.uniform(0.1, 0.998, n), -np.ones(n), np.full(n, 400.0),
+                         rng.uniform(3, 50, n), np.zeros(n), rng.uniform(1.4, 3.0, n), rng.uniform(0, 4.5, n),
+                         rng.uniform(15, 19, n), rng.uniform(0.5, 3, n), rng.uniform(10, 300, n), np.ones(n),
+                         np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(n)])
+    grids = [log_grid(0.3, 80.0, int(rng.integers(300, 1000))) for _ in range(n)]
+    big, st = gpu.eval_batch("relxilllpCp", p, grids)
+    assert not st.any()
+    for i in (0, 31, 63):
+        one, _ = gpu.eval_batch("relxilllpCp", p[i:i + 1], grids[i:i + 1])
+        np.testing.assert_array_equal(one[0], big[i])
+    q = np.column_stack([rng.uniform(1.2, 3.4, 400), rng.uniform(0.5, 3, 400), rng.uniform(5, 400, 400),
+                         rng.uniform(0, 4.7, 400), rng.uniform(15, 20, 400), np.zeros(400), rng.uniform(5, 85, 400),
+                         -np.ones(400)])
+    w = [log_grid(0.1, 500.0, 300)] * 400
+    big, st = gpu.eval_batch("xillverCp", q, w)
+    assert not st.any()
+    for i in (0, 399):
+        one, _ = gpu.eval_batch("xillverCp", q[i:i + 1], w[i:i + 1])
+        np.testing.assert_array_equal(one[0], big[i])
