@@ -272,7 +272,7 @@ def run_rrad(R, L, torch, dev, steps: int, warmup: int, n: int = N_SETS):
     params, grids = workload(n, seed_params=2028, seed_grids=9)
     params = params.copy()
     params[:, 12] = 1.0
-    r = _time_device_variant(R, L, torch, dev, steps, warmup, params, grids, 0)
+    r = _time_device_variant(R, L, torch, dev, steps, warmup, params, grids, 0, profile_steps=2)
     r.update({"zones": 10, "mode": "returning radiation on (Relreturn_Corona.cpp, Relreturn_Table.cpp)"})
     return r
 

@@ -135,7 +135,7 @@ struct RelxTables {
   const double *rr_spin;     // [nspin]
   const double *rr_rlo, *rr_rhi;  // [nspin][RELX_RR_NR]
   const double *rr_tfr;      // [nspin][RELX_RR_NR][RELX_RR_NR], row = incident bin, column = emitting bin
-  const float4 *rr_g;        // [nspin][NR][NR][NG]: frac_g, g, log2 g, 1 if |g - 1| > 1e-3 else 0
+  const float4 *rr_g;        // [nspin][NR incident][NG][NR emitting]: frac_g, g, log2 g, 1 if |g - 1| > 1e-3 else 0
   // nthcomp photon grid of the Cp models (nthcomp.cu)
   const NthGrid *nth_grid;
 };

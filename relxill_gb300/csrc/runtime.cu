@@ -571,7 +571,9 @@ static int load_rrad(const std::string &dir, Tables &T) {
         const double g = (jj + 0.5) / NG * (gmax[i] - gmin[i]) + gmin[i];
         if (!(g > 0.0)) { g_errmsg = "return radiation table: energy shift <= 0"; return RELX_ERR_TABLE; }
         const float boosted = std::fabs(g - 1) > 1e-3 ? 1.0f : 0.0f;
-        g4[((size_t) k * NR * NR + i) * NG + jj] =
+        // [spin][incident bin][sample][emitting bin]: a warp's lanes (emitting bins) read contiguous rows
+        const int ro = i / NR, re = i - ro * NR;
+        g4[(((size_t) k * NR + ro) * NG + jj) * NR + re] =
             make_float4((float) fg[(size_t) i * NG + jj], (float) g, (float) std::log2(g), boosted);
       }
     }

@@ -349,13 +349,13 @@ __device__ void rrad_pass(const RelxTables &tab, RradSmem &q, float gamma, bool 
       double t = tfr[(size_t) ro * NR + re];
       if (j == 0 && i < n - 1) t *= q.area_in;   // get_interpolated_tfr (Relreturn_Table.cpp:540-572)
       if (j == n - 1 && i < n - 2) t *= q.area_out;
-      const float4 *g = gt + ((size_t) ro * NR + re) * NG;
+      const float4 *g = gt + (size_t) ro * NG * NR + re;  // sample k at g[k * NR]
       const bool use_corr = corr && fabs(q.cf_g[j] - 1) > 1e-3;
       const float cg = (float) (corr ? q.cf_g[j] : 1.0);
       float h = 0.0f;
-#pragma unroll 4
+#pragma unroll 5
       for (int k = 0; k < NG; k++) {
-        const float4 v = __ldg(g + k);  // frac_g, g, log2 g, |g - 1| > 1e-3
+        const float4 v = __ldg(g + (size_t) k * NR);  // frac_g, g, log2 g, |g - 1| > 1e-3
         float e = v.x;
         if (use_corr) e *= rrad_corrected_boost_over_g(cg, v.y, v.z, gamma);
         else if (v.w != 0.0f) e *= exp2f((gamma - 1.0f) * v.z);
