@@ -275,10 +275,11 @@ __device__ double rebin_mean_at(const double *x0, const double *y0, int n0, doub
 // returning radiation (Relreturn_Table.cpp:393-611, Relreturn_Corona.cpp:37-321)
 // ---------------------------------------------------------------------------
 
-// get_rrad_fractions for the set (thread 0): spin index (the first table spin >= a), the table
-// bins covering [rin, rout] with the first and last reset to them, their centres and the ring-area
-// corrections of the end bins.  rin, rout: the ends of the fine radial grid (determine_rlo_rhi).
-__device__ int rrad_geometry(const RelxTables &tab, RradSmem &q, double a, double rms, double rin, double rout) {
+// get_rrad_fractions for the set, serial part (thread 0): spin index (the first table spin >= a),
+// the table bins covering [rin, rout] and the ring-area corrections of the end bins, whose first
+// and last bin are reset to rin and rout.  rin, rout: the ends of the fine radial grid
+// (determine_rlo_rhi).
+__device__ int rrad_bins(const RelxTables &tab, RradSmem &q, double a, double rms, double rin, double rout) {
   const int NR = RELX_RR_NR;
   int k = bsearch_asc<double>(tab.rr_spin, tab.rr_nspin, a);
   if (tab.rr_spin[k] < a) k++;
@@ -295,11 +296,6 @@ __device__ int rrad_geometry(const RelxTables &tab, RradSmem &q, double a, doubl
   q.n = n;
   q.klo = klo;
   q.spin = k;
-  for (int i = 0; i < n; i++) {
-    const double lo = (i == 0) ? rin : rlo[klo + i], hi = (i == n - 1) ? rout : rhi[klo + i];
-    q.rad[i] = 0.5 * (lo + hi);
-  }
-  for (int i = 0; i + 1 < n; i++) q.inv_drad[i] = 1.0 / (q.rad[i + 1] - q.rad[i]);
   // get_ring_area_correction_factor (Relreturn_Table.cpp:518-538)
   for (int e = 0; e < 2; e++) {
     const int i = e ? n - 1 : 0;
@@ -314,16 +310,43 @@ __device__ int rrad_geometry(const RelxTables &tab, RradSmem &q, double a, doubl
   return RELX_OK;
 }
 
-// corrected_gshift_fluxboost_factor / g (Relreturn_Corona.cpp:37-86), FP32
-__device__ __forceinline__ float rrad_corrected_boost_over_g(float cg, float g, float lg, float gamma) {
+// get_rrad_fractions, the bin centres and their spacing (all threads, after rrad_bins)
+__device__ void rrad_centres(const RelxTables &tab, RradSmem &q, double rin, double rout, int nt) {
+  const int NR = RELX_RR_NR, n = q.n, klo = q.klo;
+  const double *rlo = tab.rr_rlo + (size_t) q.spin * NR, *rhi = tab.rr_rhi + (size_t) q.spin * NR;
+  for (int i = threadIdx.x; i < n; i += nt) {
+    const double lo = (i == 0) ? rin : rlo[klo + i], hi = (i == n - 1) ? rout : rhi[klo + i];
+    q.rad[i] = 0.5 * (lo + hi);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i + 1 < n; i += nt) q.inv_drad[i] = 1.0 / (q.rad[i + 1] - q.rad[i]);
+  __syncthreads();
+}
+
+// the g-shift correction's linear coefficients of an emitting bin with correction cg
+// (corrected_gshift_fluxboost_factor, Relreturn_Corona.cpp:37-86): a, 1 - a below cg = 1, al, 1 - al above
+__device__ __forceinline__ float2 rrad_corr_coef(float cg) {
   const float g0 = 2.0f / 3.0f;
+  if (cg < 1.0f) {
+    const float a = (cg / g0 - 1.0f) / (g0 - 1.0f);
+    return make_float2(a, 1.0f - a);
+  }
+  const float al = (cg - 1.0f) / (g0 - 1.0f);
+  return make_float2(al, 1.0f - al);
+}
+
+// corrected_gshift_fluxboost_factor / g (Relreturn_Corona.cpp:37-86), FP32; ab from rrad_corr_coef(cg)
+__device__ __forceinline__ float rrad_corrected_boost_over_g(float cg, float2 ab, float g, float lg, float gamma) {
   float gc;
   if (cg < 1.0f) {
-    const float a = (cg / g0 - 1.0f) / (g0 - 1.0f), b = 1.0f - a;
-    gc = (g >= 1.0f) ? 1.0f / g * (1.0f / g * a + b) : g * (g * a + b);
+    if (g >= 1.0f) {
+      const float ig = 1.0f / g;
+      gc = ig * (ig * ab.x + ab.y);
+    } else {
+      gc = g * (g * ab.x + ab.y);
+    }
   } else {
-    const float al = (cg - 1.0f) / (g0 - 1.0f), bl = 1.0f - al;
-    gc = (g >= 1.0f) ? (1.0f / g * al + bl) : (g * al + bl);
+    gc = (g >= 1.0f) ? (1.0f / g * ab.x + ab.y) : (g * ab.x + ab.y);
   }
   float fb = exp2f(gamma * lg) * gc;
   if (g < 1.0f && fb > 1.0f) fb = 1.0f;
@@ -352,12 +375,13 @@ __device__ void rrad_pass(const RelxTables &tab, RradSmem &q, float gamma, bool 
       const float4 *g = gt + (size_t) ro * NG * NR + re;  // sample k at g[k * NR]
       const bool use_corr = corr && fabs(q.cf_g[j] - 1) > 1e-3;
       const float cg = (float) (corr ? q.cf_g[j] : 1.0);
+      const float2 ab = rrad_corr_coef(cg);
       float h = 0.0f;
 #pragma unroll 5
       for (int k = 0; k < NG; k++) {
         const float4 v = __ldg(g + (size_t) k * NR);  // frac_g, g, log2 g, |g - 1| > 1e-3
         float e = v.x;
-        if (use_corr) e *= rrad_corrected_boost_over_g(cg, v.y, v.z, gamma);
+        if (use_corr) e *= rrad_corrected_boost_over_g(cg, ab, v.y, v.z, gamma);
         else if (v.w != 0.0f) e *= exp2f((gamma - 1.0f) * v.z);
         h += e;
       }
@@ -686,10 +710,11 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   const bool rrad = m.return_rad != 0 && m.status == RELX_OK;
   if (rrad) {
     if (tid == 0) {
-      const int e = (tab.rr_nspin > 0) ? rrad_geometry(tab, m.rt.rr, s.a, m.rms, m.re[NR - 1], m.re[0]) : RELX_ERR_TABLE;
+      const int e = (tab.rr_nspin > 0) ? rrad_bins(tab, m.rt.rr, s.a, m.rms, m.re[NR - 1], m.re[0]) : RELX_ERR_TABLE;
       if (e != RELX_OK) m.status = e;
     }
     __syncthreads();
+    if (m.status == RELX_OK) rrad_centres(tab, m.rt.rr, m.re[NR - 1], m.re[0], kSetupThreads);
   }
   if (rrad && m.status == RELX_OK) {
     RradSmem &q = m.rt.rr;
