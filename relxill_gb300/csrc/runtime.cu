@@ -15,6 +15,8 @@
 #include <thread>
 #include <vector>
 
+#include <unistd.h>
+
 #include "../../include/relxill_gb300.h"
 #include "fits_reader.h"
 #include "relx_common.h"
@@ -107,7 +109,8 @@ class CopyPool {
   void run(const std::vector<CopyPiece> &jobs) {
     size_t total = 0;
     for (const auto &j : jobs) total += j.n;
-    if (nthreads_ == 0 || total < kMinParallel) {
+    // serial in a process forked after the workers started (it has no worker threads)
+    if (nthreads_ == 0 || total < kMinParallel || getpid() != pid_) {
       for (const auto &j : jobs)
         if (j.n) std::memcpy(j.dst, j.src, j.n);
       return;
@@ -138,6 +141,7 @@ class CopyPool {
     unsigned hc = std::thread::hardware_concurrency();
     int n = e ? std::atoi(e) : (int) std::min(12u, hc > 1 ? hc - hc / 4 : 0u);
     nthreads_ = std::max(0, std::min(n, 32));
+    pid_ = getpid();
     for (int i = 0; i < nthreads_; i++) std::thread([this] { loop(); }).detach();
   }
   void work() {
@@ -170,6 +174,7 @@ class CopyPool {
     }
   }
   int nthreads_ = 0;
+  pid_t pid_ = 0;
   std::mutex call_mu_, mu_;
   std::condition_variable cv_, done_cv_;
   std::vector<CopyPiece> pieces_;
