@@ -71,6 +71,13 @@ void c_lmodrelxilldensnthcomp(const double *energy, int Nflux, const double *par
                               double *fluxError, const char *init);
 void c_lmodrelxilllpdensnthcomp(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
                                 double *fluxError, const char *init);
+/* The NS flavour of the public model list (lmodel_relxill_public.dat:131-153) is not part of
+ * this library: the symbols exist so that a package built from the whole list links; a call
+ * fills flux with zeros and sets relx_last_status() to 3 (unsupported). */
+void c_lmodxillverns(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                     double *fluxError, const char *init);
+void c_lmodrelxillns(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                     double *fluxError, const char *init);
 
 /* Status of the last call on this process (0 = success).  The reference has
  * no status channel (src/LocalModel.cpp:153-159); this replaces its printed

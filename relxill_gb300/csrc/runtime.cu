@@ -1948,4 +1948,25 @@ void c_lmodrelxilllpdensnthcomp(const double *energy, int Nflux, const double *p
   lmod_eval(RELX_RELXILLLPCP, energy, Nflux, parameter, flux);
 }
 
+// The NS flavour of the public model list (lmodel_relxill_public.dat:131-153: a neutron-star
+// blackbody illuminating the disk, its own xillverNS table) is not part of this library; the
+// symbols exist so that a package built from the whole public model list links, and a call fills
+// flux with zeros and reports RELX_ERR_UNSUPPORTED.
+static void lmod_unsupported(const char *name, double *flux, int Nflux) {
+  if (flux)
+    for (int i = 0; i < Nflux; i++) flux[i] = 0.0;
+  g_errmsg = std::string(name) + ": the NS (blackbody illumination) flavour is not part of this library";
+  g_last_status = RELX_ERR_UNSUPPORTED;
+}
+void c_lmodxillverns(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                     double *fluxError, const char *init) {
+  (void) energy; (void) parameter; (void) spectrum; (void) fluxError; (void) init;
+  lmod_unsupported("xillverNS", flux, Nflux);
+}
+void c_lmodrelxillns(const double *energy, int Nflux, const double *parameter, int spectrum, double *flux,
+                     double *fluxError, const char *init) {
+  (void) energy; (void) parameter; (void) spectrum; (void) fluxError; (void) init;
+  lmod_unsupported("relxillNS", flux, Nflux);
+}
+
 }  // extern "C"

@@ -16,7 +16,8 @@ def declared_functions():
 def test_header_declares_the_reference_entry_points():
     names = declared_functions()
     for n in ("c_lmodrelline", "c_lmodrelconv", "c_lmodrelxill", "c_lmodrelxilllp", "c_lmodrellinelp",
-              "c_lmodrelconvlp", "c_lmodxillver", "relx_eval_batch",
+              "c_lmodrelconvlp", "c_lmodxillver", "c_lmodxillverdensnthcomp", "c_lmodrelxilldensnthcomp",
+              "c_lmodrelxilllpdensnthcomp", "c_lmodxillverns", "c_lmodrelxillns", "relx_eval_batch",
               "relx_eval_batch_device", "relx_last_status", "relx_init"):
         assert n in names
 
@@ -41,3 +42,22 @@ def test_python_layer_refuses_without_library(monkeypatch):
         assert "missing" in str(e)
     else:
         raise AssertionError("no error without the CUDA library")
+
+
+def test_unsupported_public_models_zero_flux_and_report():
+    """xillverNS and relxillNS of the public model list link, return zeros and status 3 (no GPU needed)."""
+    from relxill_gb300 import build
+
+    lib = ctypes.CDLL(build.build())
+    dp = ctypes.POINTER(ctypes.c_double)
+    e = (ctypes.c_double * 11)(*[1.0 + i for i in range(11)])
+    par = (ctypes.c_double * 13)()
+    for name in ("c_lmodxillverns", "c_lmodrelxillns"):
+        f = getattr(lib, name)
+        f.argtypes = [dp, ctypes.c_int, dp, ctypes.c_int, dp, dp, ctypes.c_char_p]
+        f.restype = None
+        flux = (ctypes.c_double * 10)(*([7.0] * 10))
+        f(e, 10, par, 0, flux, None, None)
+        assert list(flux) == [0.0] * 10
+        lib.relx_last_status.restype = ctypes.c_int
+        assert lib.relx_last_status() == 3
