@@ -133,6 +133,8 @@ int relx_eval_batch_device(int model, int n_sets, const double *d_params, const 
  * 3.8 MB shared by all calls: calls whose device work overlaps race on it, so
  * issue them on one stream or synchronise between them.  The first call on a
  * device looks up that array's address; make it before any stream capture.
+ * relx_release (or relx_init with another table path) frees the tables these
+ * calls read: do not run it while such calls are in flight on the device.
  * Limits: one set, relline grids of at most 16384 bins, tables loaded by
  * relx_init on the current device beforehand (RELX_ERR_NOTABLE otherwise; the
  * Cp models also need xillverCp_v3.4.fits).

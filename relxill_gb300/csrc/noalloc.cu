@@ -23,7 +23,14 @@
 //
 // Set-up: the first call on a device looks up the device address of the
 // static array (cudaGetSymbolAddress, which can load the module lazily).  Make
-// that first call before any stream capture.
+// that first call before any stream capture.  relx_release forgets the
+// addresses, so that the first call after it (for instance after the caller
+// reset the device) looks them up again.
+//
+// Tables: each call copies the table descriptor under the runtime's lock and
+// its kernels read the tables until they finish.  relx_init with another table
+// path, relx_release and a device reset free the tables: do not run them while
+// calls of this entry point are in flight on the device.
 //
 // Sharing: every call on every stream uses the same static array, which keeps
 // the contents of the last call.  Calls whose device work overlaps race on it:
@@ -143,6 +150,11 @@ __global__ void noalloc_status_kernel(const RelxSetState *__restrict__ st, const
 static std::mutex g_setup_mu;
 static void *g_scratch_ptr[64] = {nullptr};
 
+void noalloc_forget_devices() {
+  std::lock_guard<std::mutex> lock(g_setup_mu);
+  for (auto &p : g_scratch_ptr) p = nullptr;
+}
+
 static int scratch_for_device(int dev, unsigned char **out) {
   if (dev < 0 || dev >= 64) {
     runtime_set_error(RELX_ERR_ARG, "relx_eval_one_noalloc: device ordinal out of range");
@@ -198,13 +210,12 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
     return fail(RELX_ERR_ARG, msg);
   }
   int tab_dev = -1, dev = -1;
-  const RelxTables *tp = runtime_tables(&tab_dev, cp);
-  if (!tp)
+  RelxTables tab;
+  if (!runtime_tables(&tab, &tab_dev, cp))
     return fail(RELX_ERR_NOTABLE, cp ? "relx_eval_one_noalloc: tables not loaded or xillverCp_v3.4.fits not found"
                                      : "relx_eval_one_noalloc: tables not loaded (call relx_init first)");
   NOALLOC_CUDA(cudaGetDevice(&dev));
   if (dev != tab_dev) return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: the tables live on another device");
-  const RelxTables tab = *tp;
   if ((relx_is_relxill(kind) || kind == RELX_XILLVER) && tab.x_nener_pad > kMaxXillBins)
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: xillver table has more energy bins than the scratch holds");
   int nzones_env = 0, flags = 0;

@@ -8,9 +8,12 @@
 
 namespace relx {
 
-// device tables loaded by relx_init (null until then); *device = the device they live on.
-// cp: the descriptor of the Cp models (the xillverCp table; null when that table was not found)
-const RelxTables *runtime_tables(int *device, bool cp = false);
+// copies the descriptor of the device tables loaded by relx_init into *out (false until then, or
+// for cp when the xillverCp table was not found); *device = the device they live on.
+// cp: the descriptor of the Cp models
+bool runtime_tables(RelxTables *out, int *device, bool cp = false);
+// forgets the per-device scratch addresses of the no-allocation entry point (relx_release)
+void noalloc_forget_devices();
 // radial zones a parameter set uses, and the environment options read for the call
 int runtime_zones(int model, int ion_grad_type, int *nzones_env, int *flags);
 // parameters of a model (-1 for an unknown model)

@@ -861,8 +861,15 @@ static int set_kernel_attrs(const Tables &T) {
   RELX_CUDA(relline_set_smem(T.d.rel_nr, T.d.rel_ng));
   RELX_CUDA(nthcomp_set_smem());
   RELX_CUDA(xillver_set_smem(T.d.x_nincl));
-  RELX_CUDA(xillver_model_set_smem(T.d.x_nener, T.d.x_nener_pad));
-  if (T.has_cp) RELX_CUDA(xillver_model_set_smem(T.dcp.x_nener, T.dcp.x_nener_pad));
+  {
+    // one kernel serves both tables: its dynamic shared-memory limit is the larger of the two
+    int ne = T.d.x_nener, nep = T.d.x_nener_pad;
+    if (T.has_cp && xillver_model_smem_bytes(T.dcp.x_nener, T.dcp.x_nener_pad) > xillver_model_smem_bytes(ne, nep)) {
+      ne = T.dcp.x_nener;
+      nep = T.dcp.x_nener_pad;
+    }
+    RELX_CUDA(xillver_model_set_smem(ne, nep));
+  }
   RELX_CUDA(cudaFuncSetAttribute(conv_zone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
   RELX_CUDA(cudaFuncSetAttribute(relconv_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem_bytes()));
   return 0;
@@ -1642,12 +1649,13 @@ int cache_configure(int slots) {
 }
 
 // ---- hooks for the other host translation units (not part of the C ABI) ----
-const RelxTables *runtime_tables(int *device, bool cp) {
+bool runtime_tables(RelxTables *out, int *device, bool cp) {
   Context &C = ctx();
   std::lock_guard<std::mutex> lock(C.mu);
-  if (!C.T.loaded || (cp && !C.T.has_cp)) return nullptr;
+  if (!C.T.loaded || (cp && !C.T.has_cp)) return false;
   if (device) *device = C.device;
-  return cp ? &C.T.dcp : &C.T.d;
+  *out = cp ? C.T.dcp : C.T.d;
+  return true;
 }
 int runtime_zones(int model, int ion_grad_type, int *nzones_env, int *flags) {
   const EnvOpts env = read_env();
@@ -1866,6 +1874,7 @@ void relx_release(void) {
   for (auto &p : C.pin_groups) p.release();
   C.cache.release();
   C.cache_ev_valid = false;
+  noalloc_forget_devices();
 }
 
 // ---- local-model entry points with the XSPEC signature (create_wrapper_xspec.py:153-162) ----

@@ -3,6 +3,7 @@ intermediate arrays live in a static device array, against the batched entry
 point on the same inputs.  The caller's buffers come from torch; the entry
 point itself allocates nothing."""
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -11,6 +12,15 @@ from cases import CASES, CONV_MODELS, conv_input, grid
 from tolerance import assert_close
 
 pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden_small.npz")
+
+
+@pytest.fixture(autouse=True)
+def _zones_env(monkeypatch):
+    # the golden outputs were made with ten zones for the ionisation gradients
+    monkeypatch.setenv("RELXILL_NUM_RZONES", "10")
+
 
 MODELS = {"relline": 0, "relconv": 1, "relxill": 2, "relxilllp": 3, "relline_lp": 4, "relconv_lp": 5, "xillver": 6,
           "xillverCp": 7, "relxillCp": 8, "relxilllpCp": 9}
@@ -58,11 +68,17 @@ def _case(name):
 
 
 def test_noalloc_matches_batch_on_two_calls_in_a_row(gpu):
+    """Each case twice in a row through the no-allocation entry point, against the batched entry
+    point and against the reference's own output (golden file).  relxilllpcp_alpha and
+    relxilllpcp_pl carry their ionisation gradient in the parameter array (params[14] = 2 and 1)
+    while the call's ion_grad_type argument stays 0."""
     torch = pytest.importorskip("torch")
     f = _fn(gpu)
+    golden = np.load(GOLDEN)
     names = ["relxilllp_a", "relxill_cfg2", "relline_cfg1", "relconv_a", "relxilllp_alpha", "relxilllp_b",
              "rellinelp_b", "relconvlp_b", "xillver_b", "xillver_d", "xillvercp_a", "xillvercp_b", "relxillcp_b",
-             "relxilllpcp_a", "relxilllpcp_rr", "relxilllpcp_alpha", "relxilllpcp_pl"]
+             "relxilllpcp_a", "relxilllpcp_rr", "relxilllpcp_alpha", "relxilllpcp_pl", "relxilllp_rr_a",
+             "rellinelp_rr"]
     for name in names:
         _, model, params, gspec, igt, igi = _case(name)
         e = grid(gspec)
@@ -73,7 +89,9 @@ def test_noalloc_matches_batch_on_two_calls_in_a_row(gpu):
             assert call.run(f) == 0, gpu.last_error()
             torch.cuda.synchronize()
             assert int(call.status.item()) == 0
-            assert_close(call.flux.cpu().numpy(), want, f"{name} no-alloc call {k + 1}")
+            got = call.flux.cpu().numpy()
+            assert_close(got, want, f"{name} no-alloc call {k + 1} vs batch")
+            assert_close(got, golden[name], f"{name} no-alloc call {k + 1} vs reference")
 
 
 def test_noalloc_alternating_sets_keep_their_results(gpu):
