@@ -13,10 +13,19 @@
 //    the zone the rows are summed in warp order: no atomics, so every bin is
 //    the same number in every run and in every batch composition.
 //  * Arithmetic is FP32.  Bin edges and gmin/gmax enter as float-float so
-//    that g* is accurate to an ulp.  Where an abscissa lies within 4e-6 grid
-//    units of a transfer-function grid point (the reference's interpolation
-//    weights are reversed, so the interpolant jumps there) the side is decided
-//    in float-float arithmetic from the reference's own energy abscissa.
+//    that g* is accurate to an ulp.  Two decisions of the reference are
+//    discrete and are taken in higher precision where the FP32 value lies close
+//    to the decision point: the side of a transfer-function grid point (the
+//    reference's interpolation weights are reversed, so the interpolant jumps
+//    there; decided in float-float from the reference's own energy abscissa
+//    within 2e-5 grid units of the point), and Romberg's convergence test
+//    obtprec > 0.02 (a bin whose FP32 test came within 2e-6 of 0.02 is
+//    integrated again with FP64 Romberg: one level more or less changes the bin
+//    by up to about 2%).  Such bins are marked in a per-lane mask and redone
+//    after the radius's other bins by one out-of-line call, so that the bin
+//    loop holds no call (a call there makes the compiler spill its registers).
+//  * The tile is a launch argument, not a template parameter: every tile size
+//    runs the same machine code, so a bin is the same number whatever the tile.
 #include "relx_device.cuh"
 
 namespace relx {
@@ -26,6 +35,11 @@ constexpr int kLineThreads = kLineWarps * 32;
 constexpr int kSumBins = 256;    // profile sums are kept per block of 256 bins, whatever the tile
 static_assert(kSumBins == kLineThreads, "one bin per thread and block in the sums");
 constexpr float kH = 5e-3f;
+constexpr float kSideBand = 2e-5f;  // grid units within which the side of a g* point is taken in float-float
+// |obtprec - 0.02| within which a bin is integrated again in FP64: about five times the error of the
+// FP32 obtprec (the level sums carry a few ulp each, 2-5e-7 of the integral)
+constexpr float kConvBand = 2e-6f;
+constexpr int kTileMax = 512;       // energy bins per CTA at most
 
 // per-radius constants (warp uniform)
 struct RadC {
@@ -60,7 +74,7 @@ __device__ __forceinline__ float2 eval_F(float x, float y, const RadC &rc, const
   float t = (x - kH) * rc.inv_dgs;
   float tr = rintf(t);
   int ind;
-  if (fabsf(t - tr) < 4e-6f && tr >= 1.0f && tr <= (float) (ng - 2)) {
+  if (fabsf(t - tr) < kSideBand && tr >= 1.0f && tr <= (float) (ng - 2)) {
     // side of grid point k from the reference's abscissa (float-float)
     int k = (int) tr;
     const float2 alo = ab.lo_H ? rc.eH : ab.eb[0];
@@ -101,9 +115,10 @@ __device__ __forceinline__ float2 eval_F(float x, float y, const RadC &rc, const
 // romberg_integration (Relprofile.cpp:524-579) over [ga, gb] in g*, both branches in
 // lock step; interior sums reuse the previous level's points; the Romberg table is
 // updated in place (p[ii] holds t[ii][n-ii] of the last completed level).
+// *rare is set when a tested FP32 obtprec lies within kConvBand of 0.02.
 template <bool LIMB>
 __device__ __forceinline__ float romberg2(float ga, float ca, float gb, float cb, const RadC &rc,
-                                          const TW<LIMB> *__restrict__ tw, Absc ab) {
+                                          const TW<LIMB> *__restrict__ tw, Absc ab, bool *rare) {
   const float pas0 = gb - ga;
   ab.n = 0;
   ab.i = 0;
@@ -150,8 +165,16 @@ __device__ __forceinline__ float romberg2(float ga, float ca, float gb, float cb
     p1[n] = t1;
     const float o0 = fabsf(t0 - old0) / t0;
     const float o1 = fabsf(t1 - old1) / t1;
-    if (!c0) { r0 = t0; if (!(o0 > 0.02f)) c0 = true; }
-    if (!c1) { r1 = t1; if (!(o1 > 0.02f)) c1 = true; }
+    if (!c0) {
+      r0 = t0;
+      if (fabsf(o0 - 0.02f) < kConvBand) *rare = true;
+      if (!(o0 > 0.02f)) c0 = true;
+    }
+    if (!c1) {
+      r1 = t1;
+      if (fabsf(o1 - 0.02f) < kConvBand) *rare = true;
+      if (!(o1 > 0.02f)) c1 = true;
+    }
     if (c0 && c1) break;
   }
   return r0 + r1;
@@ -168,18 +191,159 @@ __device__ __forceinline__ float sqrt_diff(float hi, float lo) {
 // g* and 1 - g* of a bin edge, clamped to [0, 1] (integ_relline_bin, Relprofile.cpp:653-666).
 // The side of gmin and gmax is taken from the signs of the float-float differences: the two
 // rounded quotients alone can give g <= 1 with 1 - g < 0 for an edge just above gmax.
+// (a.hi + a.lo) - (b.hi + b.lo) in float: the difference of the high parts is exact where they are
+// within a factor 2 of each other (Sterbenz), so near gmin and gmax the sign is right and the value
+// within about an ulp; elsewhere both roundings are an ulp of the result
+__device__ __forceinline__ float ff_diff(float2 a, float2 b) {
+  return __fadd_rn(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y));
+}
+
 __device__ __forceinline__ float2 edge_gc(float2 E, const RadC &rc) {
-  const float dlo = ff_sub_to_float(E, rc.gmin), dhi = ff_sub_to_float(rc.gmax, E);
+  const float dlo = ff_diff(E, rc.gmin), dhi = ff_diff(rc.gmax, E);
   if (dlo <= 0.0f) return make_float2(0.0f, 1.0f);
   if (dhi <= 0.0f) return make_float2(1.0f, 0.0f);
   return make_float2(fminf(dlo * rc.inv_dg, 1.0f), fminf(dhi * rc.inv_dg, 1.0f));
 }
 
+// what the FP64 Romberg integration needs (read only on the rare path)
+struct RareCtx {
+  const RelxTables *tab;
+  const RelxSetState *s;
+  const double *ge;      // the set's line-profile grid (FP64)
+  const double *ifac_p;  // FP64 radial factor of the radius (RelxRadial::ifac)
+  int itab;              // table radius index
+};
+
+// the radius's transfer functions in FP64 at the table's g* points g0 .. g1 (trf1, trf2, cosne1,
+// cosne2), and its gmin, gmax
+struct Rad64 {
+  double tf[RELX_MAX_NG][4];
+  double gmn, gmx;
+  int ng, g0, g1;
+};
+
+// gmin or gmax of the radius in FP64, as the set-up kernel computes it (Relprofile.cpp:295-300)
+__device__ double gext_fp64(const RelxTables &tab, const RelxSetState &s, int itab, double ifac, bool is_max) {
+  const int nr = tab.rel_nr, nm = tab.rel_nmu0;
+  const size_t b00 = (size_t) s.ind_a * nm + s.ind_mu0, b10 = (size_t) (s.ind_a + 1) * nm + s.ind_mu0;
+  const size_t b01 = b00 + 1, b11 = b10 + 1;
+  const float *a = is_max ? tab.rel_gmax : tab.rel_gmin;
+  const double fa = s.ifac_a, fm = s.ifac_mu0;
+  double v[2];
+  for (int q = 0; q < 2; q++) {
+    const int i = itab + q;
+    v[q] = lerp2(fa, fm, a[b00 * nr + i], a[b10 * nr + i], a[b01 * nr + i], a[b11 * nr + i]);
+  }
+  return lerp1(ifac, v[1], v[0]);
+}
+
+// gmin and gmax of the radius in FP64
+__device__ void rad64_gext(const RareCtx &q, Rad64 &r) {
+  const double ifac = *q.ifac_p;
+  r.ng = q.tab->rel_ng;
+  r.gmn = gext_fp64(*q.tab, *q.s, q.itab, ifac, false);
+  r.gmx = gext_fp64(*q.tab, *q.s, q.itab, ifac, true);
+}
+
+// the last table point g with gstar[g] <= x (binary_search, relutility.c:155-170)
+__device__ __forceinline__ int gstar_index(int ng, double x) {
+  const double h = 5e-3, step = (1.0 - 2 * 5e-3) / (ng - 1);
+  int klo = 0, khi = ng - 1;
+  while (khi - klo > 1) {
+    const int m = (khi + klo) >> 1;
+    if (h + step * (double) (float) m > x) khi = m; else klo = m;
+  }
+  return klo;
+}
+
+// the radius's FP64 transfer functions (interp_lin_2d_float, then interp_lin_1d of the two table
+// rows, Relprofile.cpp:67-77, 280-293) at the table points an integration over [a, b] (energies)
+// reads; limb: the cosne columns as well
+__device__ void rad64_build(const RareCtx &q, Rad64 &r, double a, double b, int limb) {
+  const RelxTables &tab = *q.tab;
+  const RelxSetState &s = *q.s;
+  const int nr = tab.rel_nr, nm = tab.rel_nmu0, ng = tab.rel_ng;
+  const double ifac = *q.ifac_p;
+  const size_t b00 = (size_t) s.ind_a * nm + s.ind_mu0, b10 = (size_t) (s.ind_a + 1) * nm + s.ind_mu0;
+  const size_t b01 = b00 + 1, b11 = b10 + 1;
+  const double fa = s.ifac_a, fm = s.ifac_mu0;
+  const double del_g = 1.0 / (r.gmx - r.gmn);
+  r.g0 = gstar_index(ng, (a - r.gmn) * del_g);
+  r.g1 = gstar_index(ng, (b - r.gmn) * del_g) + 1;
+  const int nc = limb ? 4 : 2;
+  for (int g = r.g0; g <= r.g1; g++) {
+    float4 v[2][4];
+#pragma unroll
+    for (int q2 = 0; q2 < 2; q2++) {  // rows itab (q2 = 0) and itab + 1
+      const size_t row = (size_t) (q.itab + q2) * ng + g;
+      v[q2][0] = __ldg(&tab.rel_tc[b00 * nr * ng + row]);
+      v[q2][1] = __ldg(&tab.rel_tc[b10 * nr * ng + row]);
+      v[q2][2] = __ldg(&tab.rel_tc[b01 * nr * ng + row]);
+      v[q2][3] = __ldg(&tab.rel_tc[b11 * nr * ng + row]);
+    }
+    for (int c = 0; c < nc; c++) {
+      auto comp = [c](float4 x) { return c == 0 ? x.x : c == 1 ? x.y : c == 2 ? x.z : x.w; };
+      const double hi = lerp2(fa, fm, comp(v[0][0]), comp(v[0][1]), comp(v[0][2]), comp(v[0][3]));
+      const double lo = lerp2(fa, fm, comp(v[1][0]), comp(v[1][1]), comp(v[1][2]), comp(v[1][3]));
+      r.tf[g][c] = lerp1(ifac, lo, hi);
+    }
+  }
+}
+
+// relb_func (Relprofile.cpp:489-521) in FP64 without the emissivity factor (it scales every value
+// of one integration alike)
+__device__ double relb_fp64(const Rad64 &r, double eg, int k, int limb) {
+  const int ng = r.ng;
+  const double gmn = r.gmn, gmx = r.gmx;
+  const double del_g = 1.0 / (gmx - gmn);
+  const double egstar = (eg - gmn) * del_g;
+  const double h = 5e-3, step = (1.0 - 2 * 5e-3) / (ng - 1);
+  const int klo = min(max(gstar_index(ng, egstar), r.g0), r.g1 - 1);  // within [g0, g1] up to rounding
+  const double g0 = h + step * (double) (float) klo, g1 = h + step * (double) (float) (klo + 1);
+  const double inte = (egstar - g0) / (g1 - g0), inte1 = 1.0 - inte;
+  const double ftrf = inte * r.tf[klo][k] + inte1 * r.tf[klo + 1][k];
+  double val = eg * eg * eg / ((gmx - gmn) * sqrt(egstar - egstar * egstar)) * ftrf;
+  if (limb != 0) {
+    const double mu = inte * r.tf[klo][2 + k] + inte1 * r.tf[klo + 1][2 + k];
+    val *= (limb == 1) ? (1.0 + 2.06 * mu) : log(1.0 + 1.0 / mu);
+  }
+  return val;
+}
+
+// romberg_integration (Relprofile.cpp:524-579) of branch k in FP64 over the reference's interval
+// (bin j's edges, or gstar2ener(H) / gstar2ener(1 - H) where the edge terms take over), with the
+// emissivity factored out
+__device__ double romberg_fp64(const Rad64 &r, double a, double b, int k, int limb) {
+  double t[7][7];
+  const double ta = (relb_fp64(r, a, k, limb) + relb_fp64(r, b, k, limb)) / 2.0;
+  double pas = b - a;
+  t[0][0] = ta * pas;
+  double obtprec = 1.0;
+  int niter = 0;
+  while (obtprec > 0.02 && niter <= 5) {
+    niter++;
+    pas = pas / 2.0;
+    double sum = ta;
+    for (int ii = 1; ii <= (1 << niter) - 1; ii++) sum += relb_fp64(r, a + pas * ii, k, limb);
+    t[0][niter] = sum * pas;
+    double rr = 1.0;
+    for (int ii = 1; ii <= niter; ii++) {
+      rr *= 4.0;
+      const int jj = niter - ii;
+      t[ii][jj] = (rr * t[ii - 1][jj + 1] - t[ii - 1][jj]) / (rr - 1.0);
+    }
+    obtprec = fabs(t[niter][0] - t[niter - 1][0]) / t[niter][0];
+  }
+  return t[niter][0];
+}
+
 // integ_relline_bin (Relprofile.cpp:650-726) with the emissivity factored out, from the clamped
-// g* of the bin's edges; eb: the bin's edges (for the rare grid-point side decision)
-template <bool LIMB>
+// g* of the bin's edges; eb: the bin's edges (for the rare grid-point side decision).  FP64: the
+// Romberg part through romberg_fp64 (rq, bin j); otherwise through romberg2, which sets *rare.
+template <bool LIMB, bool FP64>
 __device__ __forceinline__ float integ_bin(float glo, float clo, float ghi, float chi, const float2 *eb, bool red_lo,
-                                           const RadC &rc, const TW<LIMB> *__restrict__ tw) {
+                                           const RadC &rc, const TW<LIMB> *__restrict__ tw, bool *rare,
+                                           Rad64 *r64, const RareCtx *rq64, const double *ge, int j) {
   if (ghi == 0.0f) return 0.0f;
   float flu = 0.0f;
   bool has_lo = true, has_hi = true;
@@ -208,7 +372,16 @@ __device__ __forceinline__ float integ_bin(float glo, float clo, float ghi, floa
   }
   if (has_lo && has_hi) {
     if (red) {
-      flu += romberg2<LIMB>(ga, ca, gb, cb, rc, tw, ab);
+      if constexpr (FP64) {
+        // the reference's interval: the bin's edges, or gstar2ener(H) / gstar2ener(1 - H)
+        Rad64 &r = *r64;
+        const double a = ab.lo_H ? (RELX_GFAC_H * (r.gmx - r.gmn) + r.gmn) : ge[j];
+        const double b = ab.hi_H ? ((1 - RELX_GFAC_H) * (r.gmx - r.gmn) + r.gmn) : ge[j + 1];
+        rad64_build(*rq64, r, a, b, rc.limb);
+        flu += (float) (romberg_fp64(r, a, b, 0, rc.limb) + romberg_fp64(r, a, b, 1, rc.limb));
+      } else {
+        flu += romberg2<LIMB>(ga, ca, gb, cb, rc, tw, ab, rare);
+      }
     } else {
       ab.n = -1;
       const float2 f = eval_F<LIMB>(0.5f * (ga + gb), 0.5f * (ca + cb), rc, tw, ab);
@@ -218,26 +391,43 @@ __device__ __forceinline__ float integ_bin(float glo, float clo, float ghi, floa
   return flu;
 }
 
+
 constexpr int kChunk = 128;  // radius records staged per chunk
 
-template <bool LIMB, int TILE>
+template <bool LIMB>
 struct LineSmem {
-  float acc[kLineWarps][TILE];
-  float2 eff[TILE + 1];
-  unsigned char red[TILE];
+  float acc[kLineWarps][kTileMax];
+  float2 eff[kTileMax + 1];
+  unsigned char red[kTileMax];
   TW<LIMB> tw[kLineWarps][RELX_MAX_NG];
   RelxRadRec rec[kChunk];
   float2 gs[RELX_MAX_NG];   // table g* points (Relprofile.cpp:104-106) as float-float
   double red_sum[kLineWarps + 1];
   TW<LIMB> tab[1];          // (a, mu0)-interpolated table [n_r][n_g], dynamic tail
 };
-using LineSmemF512 = LineSmem<false, 512>;
-using LineSmemT512 = LineSmem<true, 512>;
-using LineSmemF256 = LineSmem<false, 256>;
-using LineSmemT256 = LineSmem<true, 256>;
-static_assert(offsetof(LineSmemF512, rec) % 16 == 0 && offsetof(LineSmemT512, rec) % 16 == 0 &&
-                  offsetof(LineSmemF256, rec) % 16 == 0 && offsetof(LineSmemT256, rec) % 16 == 0,
+static_assert(offsetof(LineSmem<false>, rec) % 16 == 0 && offsetof(LineSmem<true>, rec) % 16 == 0,
               "radius records are staged as int4 rows");
+static_assert(kTileMax / 32 <= 32, "a lane's bins of one radius fit a 32-bit mask");
+
+// the bins of one radius that romberg2 marked rare (bit i of rmask: the lane's i-th bin from jlo),
+// integrated again with FP64 Romberg and added
+template <bool LIMB>
+__device__ __noinline__ void rare_bins(float *acc, const float2 *eff, const unsigned char *redv, int lane, int tlo,
+                                       int jlo, const RadC rc, const TW<LIMB> *tw, const RareCtx rq, float ew,
+                                       unsigned rmask) {
+  Rad64 r64;
+  rad64_gext(rq, r64);
+  while (rmask) {
+    const int it = __ffs(rmask) - 1;
+    rmask &= rmask - 1;
+    const int j = jlo + lane + 32 * it, jj = j - tlo;
+    const float2 *eb = &eff[jj];
+    const float2 lo = edge_gc(eb[0], rc), hi = edge_gc(eb[1], rc);
+    const float v =
+        integ_bin<LIMB, true>(lo.x, lo.y, hi.x, hi.y, eb, redv[jj] != 0, rc, tw, nullptr, &r64, &rq, rq.ge, j);
+    acc[jj] += v * ew;
+  }
+}
 
 // limb law at one table point (Relprofile.cpp:512-519)
 __device__ __forceinline__ float limb_factor(int limb, float mu) {
@@ -246,24 +436,23 @@ __device__ __forceinline__ float limb_factor(int limb, float mu) {
   return 1.0f;
 }
 
-// TILE: energy bins per CTA (256 or 512).  tsum holds the profile sum of every (256-bin block,
-// zone), nblk blocks per set, so that the sums do not depend on TILE.
-template <bool LIMB, int TILE>
+// tbins: energy bins per CTA (256 or 512, whole 256-bin sum blocks).  tsum holds the profile sum of
+// every (256-bin block, zone), nblk blocks per set, so that the sums do not depend on the tile.
+template <bool LIMB>
 __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
                                                                   const RelxSetState *__restrict__ sst,
                                                                   const RelxRadial *__restrict__ srad,
                                                                   const double *__restrict__ line_e, int nza,
                                                                   float *__restrict__ prof, double *__restrict__ tsum,
-                                                                  int nblk) {
-  static_assert(TILE % kSumBins == 0, "tiles are whole sum blocks");
+                                                                  int nblk, int tbins) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  LineSmem<LIMB, TILE> &m = *reinterpret_cast<LineSmem<LIMB, TILE> *>(smem_raw);
+  LineSmem<LIMB> &m = *reinterpret_cast<LineSmem<LIMB> *>(smem_raw);
   const int set = blockIdx.y, tile = blockIdx.x;
   const RelxSetState &s = sst[set];
   if (s.status != RELX_OK || s.cached) return;
   if ((s.limb != 0) != LIMB) return;
-  const int tlo = s.win_lo + tile * TILE;
-  const int thi = min(s.win_hi, tlo + TILE);
+  const int tlo = s.win_lo + tile * tbins;
+  const int thi = min(s.win_hi, tlo + tbins);
   if (tlo >= thi) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const RelxRadial &R = srad[set];
@@ -297,7 +486,7 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
     }
     for (int j = tid; j <= thi - tlo; j += kLineThreads) m.eff[j] = ff_split(ge[tlo + j]);
     for (int j = tid; j < thi - tlo; j += kLineThreads) m.red[j] = ge[tlo + j] >= 0.95 ? 1 : 0;
-    for (int i = tid; i < kLineWarps * TILE; i += kLineThreads) (&m.acc[0][0])[i] = 0.0f;
+    for (int i = tid; i < kLineWarps * kTileMax; i += kLineThreads) (&m.acc[0][0])[i] = 0.0f;
     for (int g = tid; g < ng; g += kLineThreads)
       m.gs[g] = ff_from_double(5e-3 + (1.0 - 2 * 5e-3) / (ng - 1) * ((float) g));
   }
@@ -377,19 +566,36 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
         }
         const float ew = rr.ew;
         const int jlo = max(ielo, tlo), jhi = min(iehi, thi - 1);
-        for (int j = jlo + lane; j <= jhi; j += 32) {
+        // bins whose FP32 Romberg test came close to 0.02 are skipped here (bit it of rmask) and
+        // added by rare_bins, before this warp's next radius: each bin still receives this
+        // radius's value at the same place in its sum
+        unsigned rmask = 0;
+        int bi = 0;
+        for (int j = jlo + lane; j <= jhi; j += 32, bi++) {
           const int jj = j - tlo;
           const float2 lo = edge_gc(m.eff[jj], rc), hi = edge_gc(m.eff[jj + 1], rc);
-          const float v = integ_bin<LIMB>(lo.x, lo.y, hi.x, hi.y, &m.eff[jj], m.red[jj] != 0, rc, tw);
-          m.acc[warp][jj] += v * ew;
+          bool rare = false;
+          const float v =
+              integ_bin<LIMB, false>(lo.x, lo.y, hi.x, hi.y, &m.eff[jj], m.red[jj] != 0, rc, tw, &rare, nullptr,
+                                     nullptr, ge, j);
+          if (rare) rmask |= 1u << bi;
+          else m.acc[warp][jj] += v * ew;
+        }
+        if (rmask) {
+          RareCtx rq;
+          rq.tab = &tab;
+          rq.s = &s;
+          rq.ge = ge;
+          rq.ifac_p = &R.ifac[c0 + ci];
+          rq.itab = it;
+          rare_bins<LIMB>(m.acc[warp], m.eff, m.red, lane, tlo, jlo, rc, tw, rq, ew, rmask);
         }
         __syncwarp();
       }
       __syncthreads();
     }
     // zone end: sum the warp rows in order, divide by the bin centre (renorm_relline_profile, Relprofile.cpp:753-762)
-#pragma unroll
-    for (int b = 0; b < TILE / kSumBins; b++) {
+    for (int b = 0; b < tbins / kSumBins; b++) {
       const int jj = b * kSumBins + tid;
       double part = 0.0;
       if (jj < thi - tlo) {
@@ -402,7 +608,7 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
         part = (double) pv;
       }
       const double zs = block_sum_d<kLineThreads>(part, m.red_sum);
-      if (tid == 0 && b * kSumBins < thi - tlo) tsum[((size_t) set * nblk + tile * (TILE / kSumBins) + b) * nza + z] = zs;
+      if (tid == 0 && b * kSumBins < thi - tlo) tsum[((size_t) set * nblk + tile * (tbins / kSumBins) + b) * nza + z] = zs;
     }
     __syncthreads();
   }
@@ -554,23 +760,23 @@ __global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, c
   }
 }
 
-template <bool LIMB, int TILE>
+template <bool LIMB>
 static size_t line_smem_t(int nr, int ng) {
-  return sizeof(LineSmem<LIMB, TILE>) + sizeof(TW<LIMB>) * (size_t) (nr * ng - 1);
+  return sizeof(LineSmem<LIMB>) + sizeof(TW<LIMB>) * (size_t) (nr * ng - 1);
 }
 size_t line_smem_bytes(int nr, int ng, bool limb, int tile) {
-  if (tile == 256) return limb ? line_smem_t<true, 256>(nr, ng) : line_smem_t<false, 256>(nr, ng);
-  return limb ? line_smem_t<true, 512>(nr, ng) : line_smem_t<false, 512>(nr, ng);
+  (void) tile;
+  return limb ? line_smem_t<true>(nr, ng) : line_smem_t<false>(nr, ng);
 }
 size_t hist_smem_bytes(int nr, int ng) { return sizeof(HistSmem) + sizeof(float4) * (size_t) (nr * ng - 1); }
 
 cudaError_t relline_set_smem(int nr, int ng) {
   cudaError_t e;
-#define SET(L, T)                                                                                          \
-  e = cudaFuncSetAttribute(relline_kernel<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,             \
-                           (int) line_smem_t<L, T>(nr, ng));                                               \
+#define SET(L)                                                                                             \
+  e = cudaFuncSetAttribute(relline_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,                \
+                           (int) line_smem_t<L>(nr, ng));                                                  \
   if (e != cudaSuccess) return e;
-  SET(false, 256) SET(true, 256) SET(false, 512) SET(true, 512)
+  SET(false) SET(true)
 #undef SET
   return cudaFuncSetAttribute(hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) hist_smem_bytes(nr, ng));
 }
@@ -581,21 +787,14 @@ cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream
                            const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
                            int nza, float *prof, float *dist, double *tsum, bool any_limb, bool zsplit) {
   const int nr = tab.rel_nr, ng = tab.rel_ng;
+  tile = (tile == 256) ? 256 : 512;
   const int ntile = (nblk * kSumBins + tile - 1) / tile;
   const dim3 grid(ntile, n_sets, zsplit ? nza : 1);
-  if (tile == 256) {
-    relline_kernel<false, 256><<<grid, kLineThreads, line_smem_t<false, 256>(nr, ng), s>>>(tab, sin, sst, srad, line_e,
-                                                                                           nza, prof, tsum, nblk);
-    if (any_limb)
-      relline_kernel<true, 256><<<grid, kLineThreads, line_smem_t<true, 256>(nr, ng), s>>>(tab, sin, sst, srad, line_e,
-                                                                                           nza, prof, tsum, nblk);
-  } else {
-    relline_kernel<false, 512><<<grid, kLineThreads, line_smem_t<false, 512>(nr, ng), s>>>(tab, sin, sst, srad, line_e,
-                                                                                           nza, prof, tsum, nblk);
-    if (any_limb)
-      relline_kernel<true, 512><<<grid, kLineThreads, line_smem_t<true, 512>(nr, ng), s>>>(tab, sin, sst, srad, line_e,
-                                                                                           nza, prof, tsum, nblk);
-  }
+  relline_kernel<false><<<grid, kLineThreads, line_smem_t<false>(nr, ng), s>>>(tab, sin, sst, srad, line_e, nza, prof,
+                                                                               tsum, nblk, tile);
+  if (any_limb)
+    relline_kernel<true><<<grid, kLineThreads, line_smem_t<true>(nr, ng), s>>>(tab, sin, sst, srad, line_e, nza, prof,
+                                                                               tsum, nblk, tile);
   if (hist)
     hist_kernel<<<dim3(n_sets, zsplit ? nza : 1), kLineThreads, hist_smem_bytes(nr, ng), s>>>(tab, sst, srad, nza, dist);
   return cudaGetLastError();
