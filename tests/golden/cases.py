@@ -11,6 +11,7 @@ GRID_LINE = ("line", 0.1, 20.0, 3000)      # relline: 3000 log bins 0.1-20 keV
 GRID_WIDE = ("wide", 0.1, 1000.0, 3000)    # relxill / relxilllp output grid
 GRID_CONV = ("convin", 0.3, 80.0, 500)      # relconv input grid
 GRID_XLOW = ("xlow", 0.01, 2000.0, 1500)    # xillver: a grid reaching past both ends of the table
+GRID_F1 = ("f1", 0.5722, 177.1, 1114)       # the grid of the returning-radiation set below
 CONV_MODELS = ("relconv", "relconv_lp")
 
 CASES = [
@@ -49,6 +50,16 @@ CASES = [
     ("relxilllp_rr_pl", "relxilllp", [10, 0, 0.9, 45, -1, 400, 0, 2.0, 3.1, 1, 300, 1, 1, 0], GRID_WIDE, 1, 0.5),
     ("rellinelp_rr", "relline_lp", [6.4, 6, 0.998, 30, -1, 400, 0, 0, 2.0, 1], GRID_LINE, 0, 0.0),
     ("relconvlp_rr", "relconv_lp", [6, 0.0, 0.7, 30, -1, 400, 0, 2.0, 1], GRID_CONV, 0, 0.0),
+    # returning radiation that stays high out to Rout = 242.088: single outer radii dominate bins, and
+    # one Romberg test of the reference sits at obtprec 0.0200002 (switch 1, then -1)
+    ("relxilllp_rr_rout", "relxilllp", [7.819159105467463, 0.06318223691180253, 0.7520664936838367,
+                                        20.839453254507205, -1, 242.08828763042303, 0.0, 1.2155558003015097,
+                                        1.2222305853986382, 9.569424921641735, 210.91094357446238,
+                                        5.727814656047778, 1, 0], GRID_F1, 0, 0.0),
+    ("relxilllp_rr_rout_only", "relxilllp", [7.819159105467463, 0.06318223691180253, 0.7520664936838367,
+                                             20.839453254507205, -1, 242.08828763042303, 0.0, 1.2155558003015097,
+                                             1.2222305853986382, 9.569424921641735, 210.91094357446238,
+                                             5.727814656047778, -1, 0], GRID_F1, 0, 0.0),
     # Cp flavour: nthcomp continuum, 6-parameter xillverCp table (lmodel_relxill_public.dat:86-129)
     ("xillvercp_a", "xillverCp", [2.0, 1.0, 60, 3.1, 15, 0, 30, -1], GRID_WIDE, 0, 0.0),
     ("xillvercp_b", "xillverCp", [1.7, 3.0, 25, 1.5, 17.0, 0.05, 60, 2.0], GRID_WIDE, 0, 0.0),
