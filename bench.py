@@ -38,7 +38,8 @@ METRIC = "relxilllp spectra/s batched vs plain GPU at ≤1e-4 rel err; serve p50
 N_SETS = 4096
 WORKLOAD = ("relxilllp batched, 4096 sets per GPU, per-set grids 300-5000 log bins 0.3-80 keV, "
             "10 radial zones")
-N_PROF = 8  # kernel kinds of the per-kernel event profiler (relx_profile_name)
+N_PROF = 9  # kernel kinds of the per-kernel event profiler (relx_profile_name)
+FLOPS_PER_EVAL = 25  # FP32 operations of one integrand evaluation (relb_func, Relprofile.cpp:489-521)
 
 
 def workload(n: int, seed_params: int = 2026, seed_grids: int = 7):
@@ -317,9 +318,13 @@ def _oracle_init(tdir: str):
 
 
 def _oracle_eval(args):
+    """One oracle evaluation: its status and the integrand evaluations it made."""
     p, e = args
+    lib = _oracle.lib()
+    lib.relxo_relb_calls.restype = ctypes.c_longlong
+    lib.relxo_relb_calls(1)
     st, f = _oracle.evaluate("relxilllp", p, e)
-    return st
+    return st, int(lib.relxo_relb_calls(1))
 
 
 def cpu_pool(tdir: str, procs: int):
@@ -332,11 +337,13 @@ def cpu_pool(tdir: str, procs: int):
 
 
 def cpu_rate(pool, params, grids, idx):
+    """Spectra per second of the oracle over the sets idx, the seconds taken, and the integrand
+    evaluations per set (the line profile's algorithmic work, counted by the oracle)."""
     t0 = time.perf_counter()
-    sts = pool.map(_oracle_eval, [(params[i], grids[i]) for i in idx], chunksize=1)
+    res = pool.map(_oracle_eval, [(params[i], grids[i]) for i in idx], chunksize=1)
     dt = time.perf_counter() - t0
-    assert not any(sts)
-    return len(idx) / dt, dt
+    assert not any(st for st, _ in res)
+    return len(idx) / dt, dt, sum(n for _, n in res) / max(len(res), 1)
 
 
 def run_reference(args):
@@ -354,7 +361,7 @@ def run_reference(args):
         cpu_rate(pool, params, grids, rng.choice(N_SETS, per_step, replace=False))
     times = []
     for _ in range(args.steps):
-        r, dt = cpu_rate(pool, params, grids, rng.choice(N_SETS, per_step, replace=False))
+        r, dt, _ = cpu_rate(pool, params, grids, rng.choice(N_SETS, per_step, replace=False))
         times.append(dt)
     pool.close()
     total = per_step * args.steps / sum(times)
@@ -571,19 +578,21 @@ def run_gpu(args):
     import oracle_lib
 
     oracle_lib.lib(tdir)
-    max_err = 0.0
+    max_err = max_tot = 0.0
     for i in range(min(4, S)):
         s, ref = oracle_lib.evaluate("relxilllp", params[i], grids[i])
         got = out[offs[i] - i: offs[i + 1] - i - 1]
         m = ref > 1e-6 * ref.max()
         max_err = max(max_err, float(np.max(np.abs(got[m] / ref[m] - 1))))
+        max_tot = max(max_tot, abs(float(got.sum() / ref.sum()) - 1))
 
-    # CPU baseline on a bounded sample
+    # CPU baseline on a bounded sample; the oracle also counts the integrand evaluations per set
     cpu = None
+    evals_per_set = None
     if pool is not None:
         idx = np.arange(min(args.cpu_sample, S))
         cpu_rate(pool, params, grids, idx[: procs])  # warm the workers
-        r, dt = cpu_rate(pool, params, grids, idx)
+        r, dt, evals_per_set = cpu_rate(pool, params, grids, idx)
         pool.close()
         cpu = {"value": r, "unit": "spectra/s", "cores": procs, "kind": "port",
                "sample": f"{len(idx)} sets of the workload on {procs} spawned processes ({dt:.1f} s)"}
@@ -602,7 +611,12 @@ def run_gpu(args):
     if not args.no_serve:
         serve = run_serve(R, args.serve_seconds, args.serve_rate, args.walkers, args.serve_budget_gb)
 
-    # roofline of the dominant kernel
+    # rooflines.  The line-profile kernel is bound by FP32 instruction issue: its algorithmic work is
+    # the oracle's count of integrand evaluations (one branch each) times FLOPS_PER_EVAL, over the
+    # FP32 FMA rate measured on this GPU (relx_fp32_rate); its memory term (the four transfer-function
+    # corner tables of the set, the radius records, the profile written) is printed beside it.  The
+    # xillver kernel reads its corner rows through L2 (sets are visited in table-row order, so
+    # neighbouring sets share rows): its algorithmic row bytes over its time are an L2 rate.
     names = [L.relx_profile_name(k).decode() for k in range(N_PROF)]
     per = {names[k]: (ms_k[k] / max(n_k[k], 1), int(n_k[k])) for k in range(N_PROF)}
     total_k = sum(ms_k[k] for k in range(N_PROF))
@@ -613,46 +627,91 @@ def run_gpu(args):
     except OSError:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    L.relx_fp32_rate.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    fp32 = ctypes.c_double(0.0)
+    fp32_gflops = fp32.value if L.relx_fp32_rate(ctypes.byref(fp32)) == 0 else None
+    line_ms = per["relline"][0]
+    roof = {"kernel": "relline", "bound": "fp32", "achieved": None, "peak": None, "unit": "TFLOP/s", "frac": None,
+            "traffic": None, "peak_source": "measured FP32 FMA rate (relx_fp32_rate, CUDA events)"}
+    if evals_per_set is not None and fp32_gflops:
+        flops = evals_per_set * FLOPS_PER_EVAL * S
+        roof.update({"achieved": flops / (line_ms * 1e-3) / 1e12, "peak": fp32_gflops / 1e3,
+                     "algorithmic_flops": flops, "evals_per_set": evals_per_set,
+                     "flops_per_eval": FLOPS_PER_EVAL})
+        roof["frac"] = roof["achieved"] / roof["peak"]
+    ng, nr_tab = 40, 100
+    line_bytes = S * (4 * nr_tab * ng * 16 + 1000 * 64) + int(st6[2]) * int(st6[1] // max(S, 1) or 1) * 4
+    roof["hbm_term"] = {"algorithmic_bytes": line_bytes, "achieved_gbs": line_bytes / (line_ms * 1e-3) / 1e9,
+                        "peak_gbs": hbm_peak, "frac": line_bytes / (line_ms * 1e-3) / 1e9 / hbm_peak}
     x_pad = 3000
     ucount = int(st6[0])
     nz_sum = int(st6[1])
     # algorithmic bytes of the xillver kernel per launch: unique corner rows x incl x energies (read) + zone spectra (write)
     xill_bytes = ucount * 10 * x_pad * 4 + nz_sum * x_pad * 4
     xill_ms = per["xillver"][0]
-    roof = {"kernel": "xillver", "bound": "hbm", "achieved": xill_bytes / (xill_ms * 1e-3) / 1e9, "peak": hbm_peak,
-            "unit": "GB/s", "frac": None, "traffic": None, "peak_source": "measured" if peaks else "fallback",
-            "algorithmic_bytes": xill_bytes}
-    roof["frac"] = roof["achieved"] / roof["peak"]
-    # DRAM bytes of the same launch from a one-pass ncu capture of this workload (committed summary)
-    try:
-        tr = json.load(open(os.path.join(ROOT, "profiles", "dram_traffic_relxilllp_4096sets.json")))
-        k = tr["kernels"]["xillver_dense_kernel"]
-        if S == N_SETS:
-            roof["traffic"] = k["dram_read_bytes"] + k["dram_write_bytes"]
-            roof["traffic_source"] = "profiles/dram_traffic_relxilllp_4096sets.json (ncu, one pass, full-size launch)"
-            roof["l2_bytes"] = k["l2_bytes"]
-    except (OSError, KeyError, ValueError):
-        pass
+    xill_roof = {"kernel": "xillver", "bound": "l2", "achieved": xill_bytes / (xill_ms * 1e-3) / 1e9,
+                 "unit": "GB/s", "algorithmic_bytes": xill_bytes,
+                 "note": "rows shared by neighbouring sets come from L2; DRAM sees a small fraction of the "
+                         "algorithmic bytes (ncu summary in the profiles folder)"}
     kernels = {n: {"ms_per_launch": round(per[n][0], 4), "launches": per[n][1],
                    "share": round(ms_k[k] / total_k, 4) if total_k else None} for k, n in enumerate(names)}
+    # the long, descriptive entries first and the headline last, so that a reader of the line's tail
+    # (a log that keeps the end) still sees the numbers
     line = {
-        "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (f64 radii, grids and normalisation sums)", "data": "synthetic",
+        "tuning": R.tuning_report(), "graphs": "step replayed as a CUDA graph after its second launch",
+        "kernels": kernels, "rooflines_other": [xill_roof],
+        "serve": serve, "ion_gradient": iongrad, "returning_radiation": rrad, "cp_flavour": cp,
+        "table_load": {"seconds": table_load_s, "bytes": int(tb.value)},
         "config": {"workload": WORKLOAD, "sets_per_gpu": S, "parallelism": f"replicas x{world}",
                    "tables": f"synthetic full-size, {tb.value / 1e9:.2f} GB on the device",
                    "l2": "inputs larger than L2 (1 GB xillver table, ~2 GB workspace per step)"},
-        "e2e": e2e, "plain_gpu": plain, "batched_over_plain": (value / world / plain["value"]) if plain else None,
-        "max_rel_err_vs_oracle": max_err, "gpu_launches": int(launches), "clocks": clk,
-        "tuning": R.tuning_report(), "graphs": "step replayed as a CUDA graph after its second launch",
-        "roofline": roof, "dominant_kernel": names[dom],
-        "dominant_kernel_bound": {"bound": "instruction issue (FP32 ALU and FMA)", "issue_active": 0.686,
-                                  "active_threads_per_instruction": 20.3, "source": "profiles/relline_kernel_512sets.md (ncu)"},
-        "kernels": kernels, "cpu_baseline": cpu,
-        "serve": serve, "ion_gradient": iongrad, "returning_radiation": rrad, "cp_flavour": cp,
-        "table_load": {"seconds": table_load_s, "bytes": int(tb.value)},
+        "clocks": clk, "roofline": roof, "dominant_kernel": names[dom], "cpu_baseline": cpu,
+        "max_rel_err_vs_oracle": max_err, "max_total_err_vs_oracle": max_tot, "gpu_launches": int(launches),
+        "plain_gpu": plain, "batched_over_plain": (value / world / plain["value"]) if plain else None,
+        "serve_p50_ms": serve["p50_ms"] if serve else None, "serve_p99_ms": serve["p99_ms"] if serve else None,
+        "metric": METRIC, "unit": "spectra/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 radii, grids and normalisation sums)", "data": "synthetic",
+        "e2e": e2e, "value": value,
     }
     print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def spawn_replicas(args) -> int:
+    """--gpus N without a launcher: one process per GPU through torch.distributed.run on this node
+    (RANK, LOCAL_RANK and WORLD_SIZE set for each), the same command line otherwise."""
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
+def run_dry(args) -> int:
+    """The replica bookkeeping without a GPU (for tests of the launch path): gloo ranks, a fixed
+    sleep per step in place of the batch, max over ranks, whole-job throughput."""
+    from relxill_gb300 import replicas
+
+    rank, world, local = replicas.rank_info()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        time.sleep(0.01)
+    dt = replicas.max_over_ranks(time.perf_counter() - t0, dist)
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": replicas.job_throughput(args.sets, args.steps, world, dt),
+                          "unit": "spectra/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "dry_run": True, "ranks": world, "local_rank": local}))
     if dist is not None:
         dist.destroy_process_group()
     return 0
@@ -677,7 +736,12 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=50000.0)
     ap.add_argument("--walkers", type=int, default=256)
     ap.add_argument("--serve-budget-gb", type=float, default=160.0)
+    ap.add_argument("--dry-run", action="store_true", help="replica bookkeeping only, no GPU (tests)")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return spawn_replicas(args)
+    if args.dry_run:
+        return run_dry(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -206,7 +206,7 @@ int relx_tuning_report(double *out, int max);
 /* Measurement hooks (no counterpart in the reference).  When enabled, every
  * kernel of every batch is bracketed by CUDA events on its launching stream;
  * relx_profile_read synchronises and returns the accumulated milliseconds
- * and launch counts per kernel kind (relx_profile_name(k), k < 8). */
+ * and launch counts per kernel kind (relx_profile_name(k), k < 9). */
 int relx_profile_enable(int on);
 int relx_profile_read(double *ms, int64_t *launches, int n);
 const char *relx_profile_name(int k);
@@ -215,6 +215,10 @@ int64_t relx_launch_count(void);
 /* statistics of the last batch of n_sets sets: out[0] de-duplicated xillver
  * corners, out[1] radial zones, out[2] line-profile window bins (sums) */
 int relx_batch_stats(int n_sets, int64_t *out);
+/* the FP32 FMA rate of the current device in GFLOP/s (2 FLOPs per FMA), timed
+ * with CUDA events over a kernel of independent FMA chains on every SM: the
+ * denominator of the line-profile kernel's roofline */
+int relx_fp32_rate(double *gflops);
 
 #ifdef __cplusplus
 }

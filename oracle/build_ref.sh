@@ -13,7 +13,8 @@
 # quietly when they are absent.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF_SRC="${REF_SRC:-/root/reference/src}"
+# the reference's sources beside the repository unless REF_SRC names them
+REF_SRC="${REF_SRC:-$HERE/../../reference/src}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF_SRC/Relxill.cpp" ]; then
   echo "build_ref: reference sources not found at $REF_SRC; skipping" >&2

@@ -1213,8 +1213,17 @@ typedef struct {
   const double *trff, *cosne, *gstar;  /* [ng][2] at this radius */
 } RelbFunc;
 
+/* evaluations of relb_func since the last reset (the algorithmic work of the line profile) */
+static long long g_relb_calls = 0;
+long long relxo_relb_calls(int reset) {
+  const long long n = g_relb_calls;
+  if (reset) g_relb_calls = 0;
+  return n;
+}
+
 /* relb_func, Relprofile.cpp:489-521 */
 static double relb_func(double eg, int k, const RelbFunc *s) {
+  g_relb_calls++;
   double egstar = (eg - s->gmin) * s->del_g;
   int ind = binary_search(s->gstar, s->ng, egstar);
   double inte = (egstar - s->gstar[ind]) / (s->gstar[ind + 1] - s->gstar[ind]);

@@ -36,6 +36,8 @@ void relxo_conv_grid(double *out);
 void relxo_nthcomp(const double *ear, int ne, double gamma, double kte, double z, double *photar);
 int relxo_relline_profile_zones(int model, const double *params, const double *ener, int n_ener, int *nzones_out,
                                 double *flux, int n_incl, double *dist);
+/* integrand evaluations (relb_func, one branch each) since the last reset; reset != 0 resets */
+long long relxo_relb_calls(int reset);
 
 #ifdef __cplusplus
 }

@@ -18,7 +18,8 @@ OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "librelxill_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-Xptxas", "-v"]
-SOURCES = ["setup.cu", "relline.cu", "xillver.cu", "xillver_model.cu", "conv.cu", "runtime.cu", "relcache.cu", "serve.cu", "noalloc.cu", "table_ingest.cu", "nthcomp.cu", "fits_reader.cpp"]
+SOURCES = ["setup.cu", "relline.cu", "xillver.cu", "xillver_model.cu", "conv.cu", "runtime.cu", "relcache.cu", "serve.cu",
+           "noalloc.cu", "table_ingest.cu", "nthcomp.cu", "measure.cu", "fits_reader.cpp"]
 
 
 def nvcc() -> str:

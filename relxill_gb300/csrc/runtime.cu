@@ -923,8 +923,9 @@ __global__ void status_kernel(int n_sets, const RelxSetState *__restrict__ st, c
 }
 
 // ---- optional per-kernel timing with CUDA events on the launching stream ----
-enum ProfKernel { PK_PACK, PK_SETUP, PK_LINE, PK_XILL, PK_CONV, PK_FIN, PK_STATUS, PK_NTH, PK_N };
-static const char *kProfNames[PK_N] = {"pack", "setup", "relline", "xillver", "conv", "finalize", "status", "nthcomp"};
+enum ProfKernel { PK_PACK, PK_SETUP, PK_LINE, PK_XILL, PK_CONV, PK_FIN, PK_STATUS, PK_NTH, PK_HIST, PK_N };
+static const char *kProfNames[PK_N] = {"pack",     "setup",  "relline", "xillver", "conv",
+                                       "finalize", "status", "nthcomp", "hist"};
 struct Profiler {
   bool on = false;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> rec;
@@ -1118,7 +1119,7 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   }
   if (relxill) {
     {
-      ProfScope ps(PK_LINE, xs);
+      ProfScope ps(PK_HIST, xs);
       RELX_CUDA(launch_hist(n, xs, tab, sst, rad, b.nza, dist, b.nza > 1 && n < 2 * 152));
     }
     {

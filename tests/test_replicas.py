@@ -62,3 +62,22 @@ def test_set_ranges_cover_the_batch():
 
 def test_single_process_max_is_identity():
     assert replicas.max_over_ranks(3.5) == 3.5
+
+
+def test_bench_gpus_two_spawns_two_ranks():
+    """bench.py --gpus 2 without a launcher starts two ranks through torch.distributed.run (here with
+    the GPU work replaced by the dry run): the line reports both ranks."""
+    pytest.importorskip("torch")
+    import json
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2", "--steps", "3", "--warmup", "1",
+                        "--sets", "16", "--dry-run"], capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1  # rank 0 alone prints
+    assert lines[0]["n_gpus"] == 2 and lines[0]["ranks"] == 2
+    assert abs(lines[0]["value"] - 2 * 16 * 3 / (3 * 0.01)) / lines[0]["value"] < 0.5
