@@ -64,6 +64,32 @@ def workload(n: int, seed_params: int = 2026, seed_grids: int = 7):
     return p, grids
 
 
+def iongrad_workload(n: int):
+    """The relxilllp draws of the ionisation-gradient leg (ALPHA gradient, 10 zones; the gradient type
+    travels beside the parameters)."""
+    return workload(n, seed_params=2027, seed_grids=8)
+
+
+def rrad_workload(n: int):
+    """The relxilllp draws with returning radiation on ($switch_returnrad = 1)."""
+    params, grids = workload(n, seed_params=2028, seed_grids=9)
+    params = params.copy()
+    params[:, 12] = 1.0
+    return params, grids
+
+
+def cp_workload(n: int):
+    """relxilllpCp sets from the same draws: logN 15-19, kTe 20-300 keV (lmodel_relxill_public.dat:112-129)."""
+    base, grids = workload(n, seed_params=2029, seed_grids=10)
+    rng = np.random.default_rng(2030)
+    p = np.zeros((n, 17))
+    p[:, 0], p[:, 1], p[:, 2], p[:, 3] = base[:, 3], base[:, 2], -1.0, 400.0   # Incl, a, Rin, Rout
+    p[:, 4], p[:, 5], p[:, 6], p[:, 7] = base[:, 0], 0.0, base[:, 7], base[:, 8]  # h, beta, gamma, logxi
+    p[:, 8] = rng.uniform(15.0, 19.0, n)                                         # logN
+    p[:, 9], p[:, 10], p[:, 11] = 1.0, rng.uniform(20.0, 300.0, n), 1.0          # Afe, kTe, refl_frac
+    return p, grids
+
+
 # ----------------------------------------------------------------------------
 # serving workload: walkers of a sampler, Poisson arrivals
 # ----------------------------------------------------------------------------
@@ -258,7 +284,7 @@ def run_iongrad(R, L, torch, dev, steps: int, warmup: int, n: int = 2048):
     2048 sets of the same draws, device buffers, CUDA events on the launching stream."""
     os.environ["RELXILL_NUM_RZONES"] = "10"
     try:
-        params, grids = workload(n, seed_params=2027, seed_grids=8)
+        params, grids = iongrad_workload(n)
         r = _time_device_variant(R, L, torch, dev, steps, warmup, params, grids, 2)
         r.update({"zones": 10, "mode": "ALPHA ionisation gradient (IonGradient.cpp:128-171)"})
         return r
@@ -270,9 +296,7 @@ def run_rrad(R, L, torch, dev, steps: int, warmup: int, n: int = N_SETS):
     """The 4096-set relxilllp workload with returning radiation switched on ($switch_returnrad = 1,
     the reference's default): the return-table emissivity, the zones' xillver flux corrections for
     a > 0 and the emissivity recomputed with them (Relxill.cpp:336-344)."""
-    params, grids = workload(n, seed_params=2028, seed_grids=9)
-    params = params.copy()
-    params[:, 12] = 1.0
+    params, grids = rrad_workload(n)
     r = _time_device_variant(R, L, torch, dev, steps, warmup, params, grids, 0, profile_steps=2)
     r.update({"zones": 10, "mode": "returning radiation on (Relreturn_Corona.cpp, Relreturn_Table.cpp)"})
     return r
@@ -281,13 +305,7 @@ def run_rrad(R, L, torch, dev, steps: int, warmup: int, n: int = N_SETS):
 def run_cp(R, L, torch, dev, steps: int, warmup: int, n: int = N_SETS):
     """The 4096-set workload as relxilllpCp: nthcomp continua for the source and the 10 zones
     (donthcomp.c), 6-parameter xillverCp brackets (32 corners per zone), logN 15-19, kTe 20-300 keV."""
-    base, grids = workload(n, seed_params=2029, seed_grids=10)
-    rng = np.random.default_rng(2030)
-    p = np.zeros((n, 17))
-    p[:, 0], p[:, 1], p[:, 2], p[:, 3] = base[:, 3], base[:, 2], -1.0, 400.0   # Incl, a, Rin, Rout
-    p[:, 4], p[:, 5], p[:, 6], p[:, 7] = base[:, 0], 0.0, base[:, 7], base[:, 8]  # h, beta, gamma, logxi
-    p[:, 8] = rng.uniform(15.0, 19.0, n)                                         # logN
-    p[:, 9], p[:, 10], p[:, 11] = 1.0, rng.uniform(20.0, 300.0, n), 1.0          # Afe, kTe, refl_frac
+    p, grids = cp_workload(n)
     r = _time_device_variant(R, L, torch, dev, steps, warmup, p, grids, 0, model="relxilllpCp", profile_steps=2)
     r.update({"zones": 10, "mode": "relxilllpCp: nthcomp primary and zone normalisations, 6-parameter xillverCp table "
                                    "(synthetic, 4x3x4x4x3 grid x 10 inclinations)"})
@@ -735,7 +753,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-rate", type=float, default=50000.0)
     ap.add_argument("--walkers", type=int, default=256)
-    ap.add_argument("--serve-budget-gb", type=float, default=160.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=8.0)
     ap.add_argument("--dry-run", action="store_true", help="replica bookkeeping only, no GPU (tests)")
     args = ap.parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:

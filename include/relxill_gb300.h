@@ -161,10 +161,13 @@ int relx_cache_stats(int64_t *out);
  * scheduler thread forms a batch of waiting requests (one model, arrival
  * order) whenever one of two batch slots is free, so a new batch is staged
  * while the previous one runs; a completion thread copies results to the
- * clients' buffers.  hbm_budget_bytes bounds the device workspace of the two
- * slots (admission control); max_batch bounds a batch; cache_slots > 0 turns
- * on the line-profile cache with that many entries.  Results do not depend
- * on which requests share a batch. */
+ * clients' buffers.  hbm_budget_bytes is the device workspace of the two
+ * slots: each slot allocates half of it here and carves every batch from it
+ * (admission control keeps a batch within it; a single request that needs
+ * more completes with RELX_ERR_NOMEM), so serving allocates no device memory.
+ * Returns NULL when the budget cannot be allocated.  max_batch bounds a
+ * batch; cache_slots > 0 turns on the line-profile cache with that many
+ * entries.  Results do not depend on which requests share a batch. */
 typedef struct relx_server relx_server;
 relx_server *relx_serve_create(int64_t hbm_budget_bytes, int max_batch, int cache_slots);
 /* Queue one evaluation.  energy (n_bins + 1 edges), flux_in (relconv) and

@@ -191,13 +191,7 @@ __device__ __forceinline__ float sqrt_diff(float hi, float lo) {
 // g* and 1 - g* of a bin edge, clamped to [0, 1] (integ_relline_bin, Relprofile.cpp:653-666).
 // The side of gmin and gmax is taken from the signs of the float-float differences: the two
 // rounded quotients alone can give g <= 1 with 1 - g < 0 for an edge just above gmax.
-// (a.hi + a.lo) - (b.hi + b.lo) in float: the difference of the high parts is exact where they are
-// within a factor 2 of each other (Sterbenz), so near gmin and gmax the sign is right and the value
-// within about an ulp; elsewhere both roundings are an ulp of the result
-__device__ __forceinline__ float ff_diff(float2 a, float2 b) {
-  return __fadd_rn(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y));
-}
-
+// (ff_diff: near gmin and gmax the sign is right and the value within about an ulp)
 __device__ __forceinline__ float2 edge_gc(float2 E, const RadC &rc) {
   const float dlo = ff_diff(E, rc.gmin), dhi = ff_diff(rc.gmax, E);
   if (dlo <= 0.0f) return make_float2(0.0f, 1.0f);

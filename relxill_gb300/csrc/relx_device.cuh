@@ -22,12 +22,91 @@ __device__ __forceinline__ int bsearch_asc(const T *arr, int n, T val) {
   }
   return klo;
 }
+// ---- FP64 values handled on the integer pipes ------------------------------
+// On this part the FP64 pipe issues 2 lanes per clock per SM, and the double <-> float conversion
+// instructions run on it as well.  Conversions are done here with integer operations, and
+// comparisons of positive doubles as comparisons of their bit patterns (which order like the
+// values for non-negative finite doubles).
+// (float) d, rounded to nearest even, every case on the integer pipes (a conversion instruction
+// on the rare path would be if-converted into every call)
+__device__ __forceinline__ float d2f(double d) {
+  const unsigned long long b = (unsigned long long) __double_as_longlong(d);
+  const unsigned int sgn = (unsigned int) (b >> 32) & 0x80000000u;
+  const int eb = (int) (b >> 52) & 0x7ff;
+  const unsigned long long frac = b & 0xfffffffffffffull;
+  const int E = eb - 1023 + 127;  // biased float exponent
+  unsigned int f;
+  if (eb == 0x7ff) {
+    f = frac ? 0x7fc00000u : 0x7f800000u;  // NaN, infinity
+  } else if (E >= 255) {
+    f = 0x7f800000u;  // overflow
+  } else if (E > 0) {
+    const unsigned int m = (unsigned int) (frac >> 29);           // leading 23 fraction bits
+    const unsigned int rem = (unsigned int) frac & 0x1fffffffu;   // the 29 bits dropped
+    f = ((unsigned int) E << 23) | m;
+    f += (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;  // a carry moves the exponent
+  } else if (eb == 0 || E < -24) {
+    f = 0u;  // below half the smallest float denormal
+  } else {  // float denormal: the 53-bit significand shifted by 30 - E, rounded
+    const unsigned long long m = (1ull << 52) | frac;
+    const int sh = 30 - E;  // 30 .. 54
+    const unsigned long long q = m >> sh, rem = m & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    f = (unsigned int) q + ((rem > half || (rem == half && (q & 1ull))) ? 1u : 0u);
+  }
+  return __uint_as_float(f | sgn);
+}
+// (double) f, exact, every case on the integer pipes
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int e = (u >> 23) & 0xffu, frac = u & 0x7fffffu;
+  unsigned long long b = (unsigned long long) (u & 0x80000000u) << 32;
+  if (e == 255u) {
+    b |= (0x7ffull << 52) | ((unsigned long long) frac << 29);  // infinity, NaN
+  } else if (e != 0u) {
+    b |= ((unsigned long long) (e + 896u) << 52) | ((unsigned long long) frac << 29);
+  } else if (frac != 0u) {  // float denormal: frac * 2^-149 with its leading bit at p
+    const int p = 31 - __clz(frac);
+    b |= ((unsigned long long) (p - 149 + 1023) << 52) | (((unsigned long long) frac << (52 - p)) & 0xfffffffffffffull);
+  }
+  return __longlong_as_double((long long) b);
+}
+// a > b and a >= b where b > 0 and a is not NaN (a may be negative)
+__device__ __forceinline__ bool dgt(double a, double b) { return __double_as_longlong(a) > __double_as_longlong(b); }
+__device__ __forceinline__ bool dge(double a, double b) { return __double_as_longlong(a) >= __double_as_longlong(b); }
+// bsearch_asc of an ascending array of positive values (largest k in [0, n-2] with a[k] <= v)
+__device__ __forceinline__ int bsearch_asc_pos(const double *a, int n, double v) {
+  int lo = 0, hi = n;  // count of entries <= v
+  while (lo < hi) {
+    const int k = (lo + hi) >> 1;
+    if (!dgt(a[k], v)) lo = k + 1; else hi = k;
+  }
+  return max(0, min(lo - 1, n - 2));
+}
+// number of entries > v of a descending array of positive values
+__device__ __forceinline__ int count_gt_desc_pos(const double *a, int n, double v) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int k = (lo + hi) >> 1;
+    if (dgt(a[k], v)) lo = k + 1; else hi = k;
+  }
+  return lo;
+}
+// bsearch_desc of a descending array of positive values (largest k in [0, n-2] with a[k] >= v)
+__device__ __forceinline__ int bsearch_desc_pos(const double *a, int n, double v) {
+  int lo = 0, hi = n;  // count of entries >= v
+  while (lo < hi) {
+    const int k = (lo + hi) >> 1;
+    if (dge(a[k], v)) lo = k + 1; else hi = k;
+  }
+  return max(0, min(lo - 1, n - 2));
+}
+
 // index k of the log conv grid with ge[k] <= e < ge[k+1] (clamped to [0, N-1]), as
 // binary_search would return it: a first guess from the logarithm, then exact comparisons
 __device__ __forceinline__ int conv_index(const RelxTables &tab, double e) {
   const double *ge = tab.conv_e;
   const float2 *gf = tab.conv_eff;  // .x = (float) ge
-  const float ef = (float) e;
+  const float ef = d2f(e);
   // the grid is logarithmic (edge k at exp(log E_0 + k step)), so the float position kf is the bin
   // up to about 1e-3 of a bin (logf, the rounding of e, of the two constants and of the product);
   // more than 4e-3 of a bin away from an edge the bin is certain without reading the grid
@@ -37,8 +116,8 @@ __device__ __forceinline__ int conv_index(const RelxTables &tab, double e) {
   if (fr > 4e-3f && fr < 1.0f - 4e-3f && kfl >= 0.0f && kfl <= (float) (RELX_NCONV - 1)) return k;
   k = max(0, min(k, RELX_NCONV - 1));
   // ge[k] > e, decided in float unless the float values tie
-  while (k > 0 && (gf[k].x > ef || (gf[k].x == ef && ge[k] > e))) k--;
-  while (k < RELX_NCONV - 1 && (gf[k + 1].x < ef || (gf[k + 1].x == ef && ge[k + 1] <= e))) k++;
+  while (k > 0 && (gf[k].x > ef || (gf[k].x == ef && dgt(ge[k], e)))) k--;
+  while (k < RELX_NCONV - 1 && (gf[k + 1].x < ef || (gf[k + 1].x == ef && !dgt(ge[k + 1], e)))) k++;
   return k;
 }
 
@@ -63,6 +142,17 @@ __device__ __forceinline__ int bsearch_asc_exact(const double *a, const float *a
     if (af[k] < vf) lo = k + 1; else hi = k;
   }
   while (lo < n && af[lo] == vf && a[lo] <= v) lo++;  // lo = count of entries <= v
+  return max(0, min(lo - 1, n - 2));
+}
+// bsearch_desc of a strictly descending array (the largest k in [0, n-2] with a[k] >= v, 0 when
+// there is none), guided by the float copy af
+__device__ __forceinline__ int bsearch_desc_exact(const double *a, const float *af, int n, double v, float vf) {
+  int lo = 0, hi = n;  // count of entries > v in float
+  while (lo < hi) {
+    const int k = (lo + hi) >> 1;
+    if (af[k] > vf) lo = k + 1; else hi = k;
+  }
+  while (lo < n && af[lo] == vf && a[lo] >= v) lo++;  // lo = count of entries >= v
   return max(0, min(lo - 1, n - 2));
 }
 // descending arr (inv_binary_search, relutility.c:195-211)
@@ -129,12 +219,13 @@ __device__ __forceinline__ float2 ff_from_double(double d) {
 }
 // double -> float-float without the FP64 pipe (which runs at 2 lanes/clk/SM): hi keeps the
 // leading 24 significant bits of d (truncated), lo is the rest rounded to float, so hi + lo = d to
-// about 2^-48 relative.  For |d| in [2^-60, 2^61); other values use the conversion instructions.
+// about 2^-48 relative.  For |d| in [2^-60, 2^61); other values give (float) d and 0 (integer
+// operations throughout: a conversion instruction on a rare path is if-converted into every call).
 __device__ __forceinline__ float2 ff_split(double d) {
   const unsigned long long b = (unsigned long long) __double_as_longlong(d);
   const unsigned long long ab = b & 0x7fffffffffffffffull;
   const int e = (int) (ab >> 52) - 1023;
-  if (e < -60 || e > 60) return ff_from_double(d);
+  if (e < -60 || e > 60) return make_float2(d2f(d), 0.0f);  // not met by the values split here
   const unsigned int sgn = (unsigned int) (b >> 32) & 0x80000000u;
   const float hi = __uint_as_float(sgn | ((unsigned int) (e + 127) << 23) | ((unsigned int) (ab >> 29) & 0x7fffffu));
   const float r = __uint2float_rn((unsigned int) (ab & 0x1fffffffull));
@@ -142,6 +233,16 @@ __device__ __forceinline__ float2 ff_split(double d) {
   const float lo = __uint_as_float(__float_as_uint(r * sc) | sgn);
   return make_float2(hi, lo);
 }
+// (a.hi + a.lo) - (b.hi + b.lo) in float: the difference of the high parts is exact where they are
+// within a factor 2 of each other (Sterbenz), so the sign is right and the value within about an
+// ulp there; elsewhere both roundings are an ulp of the result
+__device__ __forceinline__ float ff_diff(float2 a, float2 b) {
+  return __fadd_rn(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y));
+}
+// a > b and a >= b for doubles with their float roundings af, bf: rounding to float is monotone,
+// so float copies that differ decide, and only tied copies are compared in FP64
+__device__ __forceinline__ bool gt_f(double a, float af, double b, float bf) { return af != bf ? af > bf : a > b; }
+__device__ __forceinline__ bool ge_f(double a, float af, double b, float bf) { return af != bf ? af > bf : a >= b; }
 // (a.hi + a.lo) - (b.hi + b.lo) rounded to float, error ~1 ulp of the result
 __device__ __forceinline__ float ff_sub_to_float(float2 a, float2 b) {
   float s = __fsub_rn(a.x, b.x);
@@ -279,7 +380,7 @@ __device__ __forceinline__ double primary_qsum_warp(const RelxTables &tab, float
     u.y = __shfl_xor_sync(0xffffffffu, part.y, o);
     part = ff_add(part, u);
   }
-  return ff_to_double(part) * 1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi);
+  return ff_to_double(part) * (1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi));  // one product, not a division
 }
 
 // E F_E of the table interpolated at photon energy e [keV] in the frame shifted by 1 + z, from the

@@ -35,15 +35,18 @@ struct HostBatch {
 // A batch slot owns a workspace, pinned staging, a stream and a completion event, so that
 // batches on different slots are in flight together (serving engine).
 struct BatchSlot;
-int slot_create(BatchSlot **out);
+// arena_bytes: the device region every batch of the slot is carved from (allocated here, so that
+// serving allocates no device memory); pinned_bytes: the initial host staging
+int slot_create(BatchSlot **out, size_t arena_bytes, size_t pinned_bytes);
 void slot_destroy(BatchSlot *b);
 // queue a batch on the slot (asynchronous); the slot's previous batch must have been waited for
 int slot_enqueue(BatchSlot *b, const HostBatch &hb, bool use_cache);
 // wait for the slot's batch; flux (flux layout of relx_eval_batch) and statuses in pinned memory,
 // valid until the next slot_enqueue
 int slot_wait(BatchSlot *b, const double **flux, const int **status);
-// device workspace bytes of a batch (admission control)
-size_t batch_device_bytes(int model, int n_sets, int64_t n_edges, int nza);
+// device workspace bytes of a batch (admission control; an upper bound of what the slot carves):
+// n_edges energy edges in all, max_bins the largest set's bins, nza zones
+size_t batch_device_bytes(int model, int n_sets, int64_t n_edges, int max_bins, int nza);
 // (re)create the line-profile cache with `slots` entries (0: off)
 int cache_configure(int slots);
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -41,11 +42,30 @@ static std::atomic<int> g_last_status{0};
 // ---------------------------------------------------------------------------
 // device buffers
 // ---------------------------------------------------------------------------
+// a device region the buffers of one batch are carved from (the workspaces of the serving slots):
+// carving is a bump of an offset, and the offset returns to 0 before each batch
+struct Arena {
+  unsigned char *base = nullptr;
+  size_t bytes = 0, off = 0;
+};
+
 struct DevBuf {
   void *p = nullptr;
   size_t bytes = 0;
+  Arena *ar = nullptr;  // carve from this region instead of allocating
   int reserve(size_t n) {
     if (n <= bytes) return 0;
+    if (ar) {
+      const size_t want = (std::max(n, (size_t) 256) + 255) / 256 * 256;
+      if (ar->off + want > ar->bytes) {
+        g_errmsg = "batch needs more than the slot's " + std::to_string(ar->bytes) + " device bytes";
+        return RELX_ERR_NOMEM;
+      }
+      p = ar->base + ar->off;
+      bytes = want;
+      ar->off += want;
+      return 0;
+    }
     if (p) cudaFree(p);
     p = nullptr;
     bytes = 0;
@@ -61,27 +81,28 @@ struct DevBuf {
   template <typename T>
   T *as() const { return reinterpret_cast<T *>(p); }
   void release() {
-    if (p) cudaFree(p);
+    if (p && !ar) cudaFree(p);
     p = nullptr;
     bytes = 0;
   }
 };
 
-// page-locked host staging buffer (grown on demand)
+// page-locked host staging buffer (grown on demand, by at least half its size)
 struct Pinned {
   void *h = nullptr;
   size_t bytes = 0;
   int reserve(size_t n) {
     if (n <= bytes) return 0;
+    const size_t want = std::max(n, bytes + bytes / 2);
     if (h) cudaFreeHost(h);
     h = nullptr;
     bytes = 0;
-    if (cudaMallocHost(&h, n) != cudaSuccess) {
+    if (cudaMallocHost(&h, want) != cudaSuccess) {
       cudaGetLastError();
-      g_errmsg = "cudaMallocHost of " + std::to_string(n) + " bytes failed";
+      g_errmsg = "cudaMallocHost of " + std::to_string(want) + " bytes failed";
       return RELX_ERR_NOMEM;
     }
-    bytes = n;
+    bytes = want;
     return 0;
   }
   void release() {
@@ -796,11 +817,27 @@ static int zones_for(int model, int ion_grad_type, int envn) {
 struct Workspace {
   DevBuf setin, st, rad, corners, zcorners, line_e, prof, dist, tsum, xill, cout, user_e, user_f, flux, sflag,
       status, err, params, eoff, igt, igi, order, cslot, nthq, nthtab, nthscr;
+  Arena arena;  // set by use_arena: every buffer is carved from it
+  std::array<DevBuf *, 26> all() {
+    return {&setin, &st, &rad, &corners, &zcorners, &line_e, &prof, &dist, &tsum, &xill, &cout, &user_e,
+            &user_f, &flux, &sflag, &status, &err, &params, &eoff, &igt, &igi, &order, &cslot, &nthq,
+            &nthtab, &nthscr};
+  }
+  // carve the buffers from [base, base + bytes) from now on (the workspace holds no allocation)
+  void use_arena(void *base, size_t bytes) {
+    release();
+    arena.base = (unsigned char *) base;
+    arena.bytes = bytes;
+    arena.off = 0;
+    for (DevBuf *b : all()) b->ar = &arena;
+  }
+  // before a batch: no buffer of the previous batch stays addressable
+  void arena_reset() {
+    for (DevBuf *b : all()) b->release();
+    arena.off = 0;
+  }
   void release() {
-    for (DevBuf *b : {&setin, &st, &rad, &corners, &zcorners, &line_e, &prof, &dist, &tsum, &xill, &cout, &user_e,
-                      &user_f, &flux, &sflag, &status, &err, &params, &eoff, &igt, &igi, &order, &cslot, &nthq,
-                      &nthtab, &nthscr})
-      b->release();
+    for (DevBuf *b : all()) b->release();
   }
 };
 
@@ -1301,7 +1338,8 @@ static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStrea
 // it.  Every candidate gives the same numbers (the profile sums are per 256-bin block whatever the
 // tile, and the chunks only reorder independent sets), so the last trial's results stand.  The
 // trials synchronise the stream.
-static int tuned_launch(Context &C, Workspace &W, BatchShape &b, cudaStream_t s, bool use_cache) {
+static int tuned_launch(Context &C, Workspace &W, BatchShape &b, cudaStream_t s, bool use_cache,
+                        bool allow_tune = true) {
   const bool cached = use_cache && C.cache.enabled() && relx_kind(b.model) != RELX_RELLINE &&
                       b.model != RELX_XILLVER;
   int sclass = 0;
@@ -1319,8 +1357,8 @@ static int tuned_launch(Context &C, Workspace &W, BatchShape &b, cudaStream_t s,
   } else {
     b.line_tile = b.n_sets <= 1024 ? 256 : 512;  // small batches: more CTAs per set
   }
-  if (known || !C.autotune_on || g_prof.on || cached || explicit_choice || relx_kind(b.model) == RELX_RELLINE ||
-      b.model == RELX_XILLVER)
+  if (known || !allow_tune || !C.autotune_on || g_prof.on || cached || explicit_choice ||
+      relx_kind(b.model) == RELX_RELLINE || b.model == RELX_XILLVER)
     return launch_batch(C, W, b, s, use_cache);
   struct Cand { int tile, chunk; };
   std::vector<Cand> cands = {{512, 0}, {256, 0}};
@@ -1391,7 +1429,7 @@ static int batch_shape(int model, int n_sets, const int64_t *eoff_host, const in
 // copies of the results (flux, then per-set statuses) back into pinned memory, all asynchronous on
 // s.  *o_flux / *o_status: their offsets in P.  Caller holds C.mu.
 static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t s, const HostBatch &hb,
-                              bool use_cache, size_t *o_flux, size_t *o_status) {
+                              bool use_cache, size_t *o_flux, size_t *o_status, bool allow_tune = true) {
   const int model = hb.model, n_sets = hb.n_sets;
   if (model < 0 || model >= RELX_NMODELS || n_sets <= 0 || !hb.params || !hb.energy || !hb.eoff) return RELX_ERR_ARG;
   const bool conv = relx_kind(model) == RELX_RELCONV;
@@ -1454,7 +1492,7 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
                                                      hb.igi ? W.igi.as<double>() : nullptr, env.nzones_env, env.flags,
                                                      b.nza, W.setin.as<RelxSetIn>());
   }
-  if ((st = tuned_launch(C, W, b, s, use_cache))) return st;
+  if ((st = tuned_launch(C, W, b, s, use_cache, allow_tune))) return st;
   RELX_CUDA(cudaMemcpyAsync(h + *o_flux, W.flux.p, nflux * sizeof(double), cudaMemcpyDeviceToHost, s));
   RELX_CUDA(cudaMemcpyAsync(h + *o_status, W.status.p, sizeof(int) * n_sets, cudaMemcpyDeviceToHost, s));
   return 0;
@@ -1566,13 +1604,25 @@ static int eval_host(const HostBatch &hb, double *flux, int *status) {
 struct BatchSlot {
   Workspace W;
   Pinned P;
+  void *arena = nullptr;  // the device region of W
   cudaStream_t s = nullptr;
   cudaEvent_t done = nullptr;
   size_t o_flux = 0, o_status = 0;
   bool pending = false;
 };
 
-int slot_create(BatchSlot **out) {
+void slot_destroy(BatchSlot *b) {
+  if (!b) return;
+  if (b->s) cudaStreamSynchronize(b->s);
+  b->W.release();
+  if (b->arena) cudaFree(b->arena);
+  b->P.release();
+  if (b->done) cudaEventDestroy(b->done);
+  if (b->s) cudaStreamDestroy(b->s);
+  delete b;
+}
+
+int slot_create(BatchSlot **out, size_t arena_bytes, size_t pinned_bytes) {
   Context &C = ctx();
   std::lock_guard<std::mutex> lock(C.mu);
   int st = ensure_init(C, nullptr);
@@ -1581,28 +1631,33 @@ int slot_create(BatchSlot **out) {
   if (cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
-    delete b;
+    slot_destroy(b);
     g_errmsg = "slot stream or event creation failed";
     return RELX_ERR_CUDA;
+  }
+  if (cudaMalloc(&b->arena, arena_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    b->arena = nullptr;
+    slot_destroy(b);
+    g_errmsg = "cudaMalloc of the slot's " + std::to_string(arena_bytes) + " bytes failed";
+    return RELX_ERR_NOMEM;
+  }
+  b->W.use_arena(b->arena, arena_bytes);
+  if ((st = b->P.reserve(pinned_bytes))) {
+    slot_destroy(b);
+    return st;
   }
   *out = b;
   return 0;
 }
 
-void slot_destroy(BatchSlot *b) {
-  if (!b) return;
-  if (b->s) cudaStreamSynchronize(b->s);
-  b->W.release();
-  b->P.release();
-  if (b->done) cudaEventDestroy(b->done);
-  if (b->s) cudaStreamDestroy(b->s);
-  delete b;
-}
-
 int slot_enqueue(BatchSlot *b, const HostBatch &hb, bool use_cache) {
   Context &C = ctx();
   std::lock_guard<std::mutex> lock(C.mu);
-  int st = enqueue_host_batch(C, b->W, b->P, b->s, hb, use_cache, &b->o_flux, &b->o_status);
+  // the previous batch of the slot has been waited for: its buffers may be carved again; no
+  // autotuning trials here (they would hold the batch for several launches)
+  b->W.arena_reset();
+  int st = enqueue_host_batch(C, b->W, b->P, b->s, hb, use_cache, &b->o_flux, &b->o_status, false);
   if (st) return st;
   RELX_CUDA(cudaEventRecord(b->done, b->s));
   b->pending = true;
@@ -1622,19 +1677,28 @@ int slot_wait(BatchSlot *b, const double **flux, const int **status) {
   return 0;
 }
 
-size_t batch_device_bytes(int model, int n_sets, int64_t n_edges, int nza) {
+size_t batch_device_bytes(int model, int n_sets, int64_t n_edges, int max_bins, int nza) {
   const int kind = relx_kind(model);
+  const size_t S = (size_t) n_sets, E = (size_t) n_edges;
+  // parameters, grid offsets and the ionisation-gradient arrays (enqueue_host_batch), and the
+  // 256-byte rounding of each of the workspace's 26 buffers
+  const size_t staged = S * (sizeof(double) * RELX_NPARAM_MAX + sizeof(int64_t) + sizeof(int) + sizeof(double)) +
+                        sizeof(int64_t) + 26 * 256 + 256;
+  const size_t cp = relx_is_cp(model) ? S * (sizeof(NthTable) + sizeof(double) * (RELX_NZMAX + 1)) : 0;
   if (kind == RELX_XILLVER)
-    return (sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(int) * 4 +
-            (relx_is_cp(model) ? sizeof(NthTable) + sizeof(double) * (RELX_NZMAX + 1) : 0)) *
-               (size_t) n_sets +
-           (relx_is_cp(model) ? nthcomp_scratch_bytes(n_sets, 1, true) : 0) + sizeof(double) * 2 * (size_t) n_edges;
+    return staged + cp + S * (sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(int) * 4) + sizeof(int) +
+           (relx_is_cp(model) ? nthcomp_scratch_bytes(n_sets, 1, true) : 0) + sizeof(double) * 2 * E;
+  const int gmax = (kind == RELX_RELLINE) ? std::max(max_bins, 1) : RELX_NCONV;
+  const size_t nblk = (size_t) (gmax + kSumBinsH - 1) / kSumBinsH;
   size_t per_set = sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(RelxRadial) + sizeof(int) * 4 +
-                   sizeof(float) * nza * RELX_MAX_INCL + sizeof(double) * (RELX_NCONV / kSumBinsH) * nza;
+                   sizeof(float) * nza * RELX_MAX_INCL + sizeof(double) * nblk * nza;
+  size_t per_edge = sizeof(double) * 2;                                      // user grid, flux
+  if (kind == RELX_RELLINE) per_edge += sizeof(double) + sizeof(float);     // line grid, profile
+  else per_edge += (kind == RELX_RELCONV) ? sizeof(double) : 0;              // relconv input
   if (kind != RELX_RELLINE) per_set += 2 * sizeof(float) * (size_t) nza * RELX_NCONV;
   if (relx_is_relxill(kind)) per_set += sizeof(RelxCorners) + sizeof(float) * (size_t) nza * 4096;
-  if (relx_is_cp(model)) per_set += sizeof(RelxZoneCorners) + sizeof(NthTable) + sizeof(double) * (RELX_NZMAX + 1);
-  return per_set * (size_t) n_sets + sizeof(double) * 3 * (size_t) n_edges +
+  if (relx_is_cp(model) || nza > RELX_ZDENSE) per_set += sizeof(RelxZoneCorners);
+  return staged + cp + per_set * S + per_edge * E + sizeof(int) +
          (relx_is_cp(model) ? nthcomp_scratch_bytes(n_sets, nza, false) : 0);
 }
 

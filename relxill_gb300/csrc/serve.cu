@@ -8,7 +8,8 @@
 // event), so a new batch is staged and queued while the previous one runs on
 // the GPU.  A batch holds requests of one model, in arrival order, up to the
 // engine's maximum batch size and up to the device memory the slot may use
-// (admission by the HBM budget given at creation).  A completion thread waits
+// (admission by the HBM budget given at creation; each slot allocates its half of the budget at
+// creation and carves every batch from it).  A completion thread waits
 // for the slots in order, copies each result to the client's buffer and
 // records the request's latency.  The line-profile cache (relcache.cu), when
 // enabled, lets requests whose relativistic parameters repeat skip the
@@ -101,14 +102,17 @@ void Server::scheduler() {
     const int model = pending.front().model;
     S.reqs.clear();
     int64_t edges = 0;
-    int nza = 1;
+    int nza = 1, max_bins = 0;
     for (auto it = pending.begin(); it != pending.end() && (int) S.reqs.size() < max_batch;) {
       if (it->model != model) { ++it; continue; }
-      const int z = std::max(nza, it->nza);
-      const size_t need = batch_device_bytes(model, (int) S.reqs.size() + 1, edges + it->n_bins + 1, z);
+      const int z = std::max(nza, it->nza), mb = std::max(max_bins, it->n_bins);
+      const size_t need = batch_device_bytes(model, (int) S.reqs.size() + 1, edges + it->n_bins + 1, mb, z);
+      // a request that alone needs more than the slot's memory forms a batch of its own, which the
+      // slot refuses (status RELX_ERR_NOMEM)
       if (!S.reqs.empty() && need > slot_bytes) break;
       edges += it->n_bins + 1;
       nza = z;
+      max_bins = mb;
       S.reqs.push_back(*it);
       it = pending.erase(it);
     }
@@ -214,8 +218,13 @@ relx_server *relx_serve_create(int64_t hbm_budget_bytes, int max_batch, int cach
   S.max_batch = max_batch;
   S.use_cache = cache_slots > 0;
   S.slot_bytes = (size_t) (hbm_budget_bytes / 2);
+  // each slot allocates its half of the budget here, and every batch is carved from it: serving
+  // itself allocates no device memory.  Host staging starts at max_batch spectra of the 4096-bin
+  // convolution grid (at most 256 MB) and grows by half when a batch needs more.
+  const size_t per_req = sizeof(double) * (RELX_NPARAM_MAX + 3 * 4097) + 64;
+  const size_t pinned = std::min((size_t) 256 << 20, per_req * (size_t) max_batch);
   for (auto &sl : S.slots) {
-    if (slot_create(&sl.slot) != 0) {
+    if (slot_create(&sl.slot, S.slot_bytes, pinned) != 0) {
       for (auto &t : S.slots) slot_destroy(t.slot);
       delete h;
       return nullptr;

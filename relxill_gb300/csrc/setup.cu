@@ -22,12 +22,13 @@ constexpr int kSetupThreads = 256;
 struct RradSmem {
   int n, klo, spin;                  // trimmed bins, first table bin, table spin index
   double rad[RELX_RR_NR];            // bin centres (ascending)
+  float cg_f[RELX_RR_NR];            // g-shift correction of the emitting bin, as float
+  unsigned char use_corr[RELX_RR_NR];  // that correction differs from 1 by more than 1e-3
   double inv_drad[RELX_RR_NR];       // 1 / (rad[k + 1] - rad[k])
   double area_in, area_out;          // ring-area corrections of the first and last bin
   float emis_in[RELX_RR_NR];         // direct emissivity at the bin centres
   float er[RELX_RR_NR], dl[RELX_RR_NR];  // returning emissivity per bin, log2(er[k + 1] / er[k])
   float cf_flux[RELX_RR_NR];         // xillver correction factors on the table bins
-  double cf_g[RELX_RR_NR];
   double zcf_flux[RELX_NZMAX], zcf_g[RELX_NZMAX];  // per ionisation zone
 };
 
@@ -43,8 +44,7 @@ struct SetupSmem {
     } rt;
   };
   double inv_dtab[RELX_MAX_NRTAB];
-  float re_tab_f[RELX_MAX_NRTAB];    // float copies guide the searches; FP64 decides float ties only
-  float jet_rad_f[RELX_MAX_NRADLP], rgrid_f[RELX_NZMAX + 1];
+  float jet_rad_f[RELX_MAX_NRADLP];
   float lp_dle[RELX_MAX_NRADLP], lp_dlr[RELX_MAX_NRADLP], lp_d[RELX_MAX_NRADLP], lp_di[RELX_MAX_NRADLP];
   float lp_e[RELX_MAX_NRADLP], inv_jr_f[RELX_MAX_NRADLP], inv_drad_f[RELX_MAX_NRADLP];
   unsigned char lp_log[RELX_MAX_NRADLP];  // logarithmic radial factor (emission angle above 75 deg)
@@ -61,6 +61,7 @@ struct SetupSmem {
   int return_rad, flags, is_relxill;
   // lamp post interpolation
   int lp_ind_a, ind_h[2];
+  double ginf_pow;   // g_inf^Gamma of the primary's flux factor (computed early, beside other work)
   double lp_ifac_a, ifac_h[2];
   // zones
   double rmean[RELX_NZMAX], shift[RELX_NZMAX], zlxi[RELX_NZMAX], zdens[RELX_NZMAX], xscale[RELX_NZMAX];
@@ -263,7 +264,7 @@ __device__ double rebin_mean_at(const double *x0, const double *y0, int n0, doub
   int klo = 0, khi = n0 - 1;  // count of x0 > xn via bisection
   while (khi - klo > 1) {
     int k = (khi + klo) >> 1;
-    if (x0[k] > xn) klo = k; else khi = k;
+    if (dgt(x0[k], xn)) klo = k; else khi = k;
   }
   int ii = klo;
   double f = (xn - x0[ii + 1]) / (x0[ii] - x0[ii + 1]);
@@ -373,8 +374,8 @@ __device__ void rrad_pass(const RelxTables &tab, RradSmem &q, float gamma, bool 
       if (j == 0 && i < n - 1) t *= q.area_in;   // get_interpolated_tfr (Relreturn_Table.cpp:540-572)
       if (j == n - 1 && i < n - 2) t *= q.area_out;
       const float4 *g = gt + (size_t) ro * NG * NR + re;  // sample k at g[k * NR]
-      const bool use_corr = corr && fabs(q.cf_g[j] - 1) > 1e-3;
-      const float cg = (float) (corr ? q.cf_g[j] : 1.0);
+      const bool use_corr = corr && q.use_corr[j];
+      const float cg = corr ? q.cg_f[j] : 1.0f;
       const float2 ab = rrad_corr_coef(cg);
       float h = 0.0f;
 #pragma unroll 5
@@ -385,7 +386,7 @@ __device__ void rrad_pass(const RelxTables &tab, RradSmem &q, float gamma, bool 
         else if (v.w != 0.0f) e *= exp2f((gamma - 1.0f) * v.z);
         h += e;
       }
-      acc += h * (float) t * q.emis_in[j];
+      acc += h * d2f(t) * q.emis_in[j];
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -397,17 +398,12 @@ __device__ void rrad_pass(const RelxTables &tab, RradSmem &q, float gamma, bool 
 // bins clamped to [0, n-2], linear radial factor (the profile's emission angles are 0), logarithmic
 // interpolation of the emissivity
 __device__ __forceinline__ double rrad_at(const RradSmem &q, double r) {
-  int lo = 0, hi = q.n;  // count of centres <= r
-  while (lo < hi) {
-    const int k = (lo + hi) >> 1;
-    if (q.rad[k] <= r) lo = k + 1; else hi = k;
-  }
-  const int kk = max(0, min(lo - 1, q.n - 2));
-  const float inter = (float) ((r - q.rad[kk]) * q.inv_drad[kk]);
-  return (double) (q.er[kk] * exp2f(inter * q.dl[kk]));
+  const int kk = bsearch_asc_pos(q.rad, q.n, r);
+  const float inter = d2f(r - q.rad[kk]) * d2f(q.inv_drad[kk]);
+  return f2d(q.er[kk] * exp2f(inter * q.dl[kk]));
 }
 
-__global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, int model, const RelxSetIn *__restrict__ sin,
+__global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab, int model, const RelxSetIn *__restrict__ sin,
                                                                const double *__restrict__ user_e, double *__restrict__ line_e,
                                                                RelxSetState *__restrict__ sout, RelxRadial *__restrict__ rout,
                                                                RelxCorners *__restrict__ cout, RelxZoneCorners *__restrict__ zcout) {
@@ -451,28 +447,31 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
 
   // ---- relline table in the (a, mu0) plane on the table radii (Relprofile.cpp:159-223)
   const int nr = tab.rel_nr, nm = tab.rel_nmu0;
-  if (tid == 0) {
+  if (tid == 32) {  // warp 1, beside warp 0's zone grid
     double mu0 = cos(s.incl);
-    int ia = bsearch_asc<float>(tab.rel_a, tab.rel_na, (float) s.a);
-    int im = bsearch_asc<float>(tab.rel_mu0, nm, (float) mu0);
+    const float af = d2f(s.a), muf = d2f(mu0);
+    int ia = bsearch_asc<float>(tab.rel_a, tab.rel_na, af);
+    int im = bsearch_asc<float>(tab.rel_mu0, nm, muf);
     s.ind_a = ia;
     s.ind_mu0 = im;
-    s.ifac_a = ((float) s.a - tab.rel_a[ia]) / (tab.rel_a[ia + 1] - tab.rel_a[ia]);
-    s.ifac_mu0 = ((float) mu0 - tab.rel_mu0[im]) / (tab.rel_mu0[im + 1] - tab.rel_mu0[im]);
+    s.ifac_a = (af - tab.rel_a[ia]) / (tab.rel_a[ia + 1] - tab.rel_a[ia]);
+    s.ifac_mu0 = (muf - tab.rel_mu0[im]) / (tab.rel_mu0[im + 1] - tab.rel_mu0[im]);
     s.g_n = gn;
   }
   if (tid < 32) zone_grid_warp(s.rin, s.rout, s.nz, s.height, s.rgrid);
+  if (tid == 64) m.ginf_pow = pow(s.g_inf, s.gam);  // warp 2, beside warps 0 and 1
   __syncthreads();
   {
     const size_t b00 = (size_t) s.ind_a * nm + s.ind_mu0, b10 = (size_t) (s.ind_a + 1) * nm + s.ind_mu0;
     const size_t b01 = b00 + 1, b11 = b10 + 1;
-    const double fa = s.ifac_a, fm = s.ifac_mu0;
+    const double fa = f2d(s.ifac_a), fm = f2d(s.ifac_mu0);
     for (int i = tid; i < nr; i += kSetupThreads) {
-      m.re_tab[i] = lerp1(fa, tab.rel_r[b00 * nr + i], tab.rel_r[b10 * nr + i]);
-      m.gmin_t[i] = lerp2(fa, fm, tab.rel_gmin[b00 * nr + i], tab.rel_gmin[b10 * nr + i], tab.rel_gmin[b01 * nr + i],
-                          tab.rel_gmin[b11 * nr + i]);
-      m.gmax_t[i] = lerp2(fa, fm, tab.rel_gmax[b00 * nr + i], tab.rel_gmax[b10 * nr + i], tab.rel_gmax[b01 * nr + i],
-                          tab.rel_gmax[b11 * nr + i]);
+      // the float table values widened on the integer pipes (f2d is exact)
+      m.re_tab[i] = lerp1(fa, f2d(tab.rel_r[b00 * nr + i]), f2d(tab.rel_r[b10 * nr + i]));
+      m.gmin_t[i] = lerp2(fa, fm, f2d(tab.rel_gmin[b00 * nr + i]), f2d(tab.rel_gmin[b10 * nr + i]),
+                          f2d(tab.rel_gmin[b01 * nr + i]), f2d(tab.rel_gmin[b11 * nr + i]));
+      m.gmax_t[i] = lerp2(fa, fm, f2d(tab.rel_gmax[b00 * nr + i]), f2d(tab.rel_gmax[b10 * nr + i]),
+                          f2d(tab.rel_gmax[b01 * nr + i]), f2d(tab.rel_gmax[b11 * nr + i]));
     }
   }
   // fine radial grid (relutility.c:666-677)
@@ -480,7 +479,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     const double r1 = 1.0 / sqrt(s.rout), r2 = 1.0 / sqrt(s.rin);
     const double du = (r2 - r1) / (NR - 1);  // the step once, not a division per radius
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
-      double u = ((double) ii) * du + r1;
+      double u = f2d((float) ii) * du + r1;  // ii < 2^24: exact
       double iu = __drcp_rn(u);
       m.re[ii] = iu * iu;
       m.sqre[ii] = iu;
@@ -488,68 +487,74 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   }
   __syncthreads();
   if (tid == 0) {
-    const double rms = m.rms;
-    if (m.re_tab[nr - 1] > rms && (m.re_tab[nr - 1] - rms) / m.re_tab[nr - 1] < 1e-3) m.re_tab[nr - 1] = rms;
-    m.ind_rmin = bsearch_desc(m.re_tab, nr, s.rin);
-    m.ind_rmax = bsearch_desc(m.re_tab, nr, s.rout);
+    // (re - rms) / re < 1e-3 as a product: a division is a long FP64 chain on one thread
+    const double rms = m.rms, rl = m.re_tab[nr - 1];
+    if (rl > rms && (rl - rms) < 1e-3 * rl) m.re_tab[nr - 1] = rms;
+    m.ind_rmin = bsearch_desc_pos(m.re_tab, nr, s.rin);
+    m.ind_rmax = bsearch_desc_pos(m.re_tab, nr, s.rout);
     if (m.re_tab[m.ind_rmax] < 1000.0 && m.re_tab[m.ind_rmax] * 1.01 > 1000.0) m.re_tab[m.ind_rmax] = 1000.0;
   }
   __syncthreads();
   for (int i = tid; i < nr - 1; i += kSetupThreads) m.inv_dtab[i] = 1.0 / (m.re_tab[i] - m.re_tab[i + 1]);
-  for (int i = tid; i < nr; i += kSetupThreads) m.re_tab_f[i] = (float) m.re_tab[i];
-  for (int i = tid; i <= s.nz; i += kSetupThreads) m.rgrid_f[i] = (float) s.rgrid[i];
   __syncthreads();
 
   RelxRadial &R = rout[set];
-  // ---- per fine radius: table radius, interpolation factor, gmin/gmax, weight, zone, bin range
+  // ---- per fine radius: table radius, interpolation factor, gmin/gmax, weight, zone, bin range.
+  // FP64 arithmetic for the interpolation factor and gmin/gmax as the reference computes them (the
+  // radial factor and the line's energy range); conversions and comparisons of these positive
+  // values on the integer pipes (d2f, dgt); the trapezoid weight from a float-float difference of
+  // neighbouring radii.
   int my_lo = 1 << 30, my_hi = -1;
+  const double ge0 = ge[0], gen = ge[gn];
+  const float wt_c = (float) (kPi / 2);
   for (int ii = tid; ii < NR; ii += kSetupThreads) {
-    double r = m.re[ii];
-    const float rf = (float) r;
+    const double r = m.re[ii];
     // index ind with re_tab[ind+1] <= r < re_tab[ind], as the walk of Relprofile.cpp:252-266
-    const int lo = count_gt_desc(m.re_tab, m.re_tab_f, nr, r, rf);  // count of table radii > r
+    const int lo = count_gt_desc_pos(m.re_tab, nr, r);  // count of table radii > r
     int ind = lo - 1;
     if (ind > m.ind_rmin) ind = m.ind_rmin;
     if (ind < 0) {
       if (r - RELX_RELTABLE_MAX_R <= 1e-6) ind = 0; else atomicExch(&m.status, RELX_ERR_GRID);
     }
     if (ind < 0) ind = 0;
-    double ifac = (r - m.re_tab[ind + 1]) * m.inv_dtab[ind];
-    if (ifac > 1.0 && ind > 0) atomicExch(&m.status, RELX_ERR_GRID);
-    double gmn = lerp1(ifac, m.gmin_t[ind + 1], m.gmin_t[ind]);
-    double gmx = lerp1(ifac, m.gmax_t[ind + 1], m.gmax_t[ind]);
+    const double ifac = (r - m.re_tab[ind + 1]) * m.inv_dtab[ind];
+    if (ind > 0 && dgt(ifac, 1.0)) atomicExch(&m.status, RELX_ERR_GRID);
+    const double gmn = lerp1(ifac, m.gmin_t[ind + 1], m.gmin_t[ind]);
+    const double gmx = lerp1(ifac, m.gmax_t[ind + 1], m.gmax_t[ind]);
+    const double dg = gmx - gmn;
     R.re[ii] = r;
     R.ifac[ii] = ifac;
     RelxRadRec rr;
     rr.gmin = ff_split(gmn);
     rr.gmax = ff_split(gmx);
-    rr.dg = ff_split(gmx - gmn);
-    rr.inv_dg = 1.0f / (float) (gmx - gmn);
+    rr.dg = ff_split(dg);
+    rr.inv_dg = 1.0f / d2f(dg);
     {
-      double eh = RELX_GFAC_H * (gmx - gmn) + gmn;
+      const double eh = RELX_GFAC_H * dg + gmn;
       rr.eH = ff_split(eh);
-      rr.e1H = ff_split((1 - RELX_GFAC_H) * (gmx - gmn) + gmn);
-      rr.red_H = eh >= 0.95 ? 1 : 0;
+      rr.e1H = ff_split((1 - RELX_GFAC_H) * dg + gmn);
+      rr.red_H = dge(eh, 0.95) ? 1 : 0;
     }
     rr.itab = (short) ind;
-    rr.ifac = (float) ifac;
+    rr.ifac = d2f(ifac);
     rr.ew = 0.0f;  // set with the emissivity below
-    // trapez_integ_single / 2 (relutility.c:233-244)
-    double dr;
-    if (ii == 0) dr = 0.5 * (m.re[0] - m.re[1]);
-    else if (ii == NR - 1) dr = 0.5 * (m.re[ii - 1] - m.re[ii]);
-    else dr = 0.5 * (m.re[ii - 1] - m.re[ii + 1]);
-    R.wt[ii] = (float) (r * dr * kPi / 2);
-    rr.zone = (unsigned char) bsearch_asc_exact(s.rgrid, m.rgrid_f, s.nz + 1, r, rf);
+    // trapez_integ_single / 2 (relutility.c:233-244): r * dr * pi / 2 with dr half the difference of
+    // the neighbouring radii (one-sided at the ends), from their float-float splits (the high words
+    // of neighbouring radii differ by less than a factor 2, so their difference is exact)
+    {
+      const int ia = (ii == 0) ? 0 : ii - 1, ib = (ii == NR - 1) ? NR - 1 : ii + 1;
+      const float dr = 0.5f * ff_diff(ff_split(m.re[ia]), ff_split(m.re[ib]));
+      R.wt[ii] = d2f(r) * dr * wt_c;
+    }
+    rr.zone = (unsigned char) bsearch_asc_pos(s.rgrid, s.nz + 1, r);
     // bins of the line-profile grid touched by this radius (Relprofile.cpp:863-878)
     int ielo = -1, iehi = -1;
-    double egmin = gmn, egmax = gmx;
-    if (egmax > ge[0] && egmin < ge[gn]) {
-      if (egmin < ge[0]) egmin = ge[0];
-      if (egmax > ge[gn]) egmax = ge[gn];
+    if (dgt(gmx, ge0) && dgt(gen, gmn)) {
+      const double egmin = dgt(ge0, gmn) ? ge0 : gmn;
+      const double egmax = dgt(gmx, gen) ? gen : gmx;
       if (kind == RELX_RELLINE) {
-        ielo = bsearch_asc<double>(ge, gn + 1, egmin);
-        iehi = bsearch_asc<double>(ge, gn + 1, egmax);
+        ielo = bsearch_asc_pos(ge, gn + 1, egmin);
+        iehi = bsearch_asc_pos(ge, gn + 1, egmax);
       } else {
         ielo = conv_index(tab, egmin);
         iehi = conv_index(tab, egmax);
@@ -578,32 +583,31 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   // ---- emissivity
   if (s.emis_type == RELX_EMIS_BKN) {
     // get_emis_bkn + norm_emis_profile (Rellp.cpp:91-109,421-437)
-    double part = 0.0;
+    // the power law in FP32 (r / Rbr as a float product), the normalisation integral sum(e 4 wt)
+    // as a float-float sum per thread (wt = r dr pi / 2 from the records above)
+    const float inv_rbr = (float) (1.0 / m.rbr);
+    const float a1 = d2f(-m.emis1), a2 = d2f(-m.emis2);
+    float2 part = make_float2(0.0f, 0.0f);
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
-      double r = m.re[ii];
-      double alpha = (r > m.rbr) ? m.emis2 : m.emis1;
-      double e = (double) powf((float) (r / m.rbr), (float) -alpha);
-      m.emis[ii] = e;
+      const double r = m.re[ii];
+      const float e = powf(d2f(r) * inv_rbr, dgt(r, m.rbr) ? a2 : a1);
+      m.emis[ii] = f2d(e);
       m.del_emit[ii] = -1.0;
       m.del_inc[ii] = -1.0;
-      double dr;
-      if (ii == 0) dr = 0.5 * (m.re[0] - m.re[1]);
-      else if (ii == NR - 1) dr = 0.5 * (m.re[ii - 1] - m.re[ii]);
-      else dr = 0.5 * (m.re[ii - 1] - m.re[ii + 1]);
-      part += e * (r * dr * kPi * 2);
+      part = ff_add(part, ff_mulf(make_float2(e, 0.0f), 4.0f * R.wt[ii]));
     }
-    double integ = block_sum_d<kSetupThreads>(part, m.red);
-    for (int ii = tid; ii < NR; ii += kSetupThreads) m.emis[ii] /= integ;
+    const double inv_integ = 1.0 / block_sum_d<kSetupThreads>(ff_to_double(part), m.red);
+    for (int ii = tid; ii < NR; ii += kSetupThreads) m.emis[ii] *= inv_integ;
     if (tid == 0) { s.f_inf_rest = 0; s.refl_frac_lp = 0; }
   } else {
     // lamp post: interpol_lptable (Rellp.cpp:190-247)
     const int nh = tab.lp_nh, nrad = tab.lp_nrad;
     if (tid == 0) {
-      float fa = (float) s.a;
+      float fa = d2f(s.a);
       int ia = bsearch_asc<float>(tab.lp_a, tab.lp_na, fa);
       m.lp_ind_a = ia;
       m.lp_ifac_a = (fa - tab.lp_a[ia]) / (tab.lp_a[ia + 1] - tab.lp_a[ia]);
-      float fh = (float) s.height;
+      float fh = d2f(s.height);
       for (int q = 0; q < 2; q++) {
         const float *hg = tab.lp_h + (size_t) (ia + q) * nh;
         int ih = bsearch_asc<float>(hg, nh, fh);
@@ -615,16 +619,16 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     {
       const int ia = m.lp_ind_a;
       const double fa = m.lp_ifac_a;
-      const float faf = (float) fa, f0f = (float) m.ifac_h[0], f1f = (float) m.ifac_h[1];
+      const float faf = d2f(fa), f0f = d2f(m.ifac_h[0]), f1f = d2f(m.ifac_h[1]);
       for (int k = tid; k < nrad; k += kSetupThreads) {
-        m.jet_rad[k] = lerp1(fa, tab.lp_rad[(size_t) ia * nrad + k], tab.lp_rad[(size_t) (ia + 1) * nrad + k]);
+        m.jet_rad[k] = lerp1(fa, f2d(tab.lp_rad[(size_t) ia * nrad + k]), f2d(tab.lp_rad[(size_t) (ia + 1) * nrad + k]));
 #define TV(arr, q, h) (arr)[(((size_t) (ia + (q)) * nh) + (h)) * nrad + k]
         const int h0 = m.ind_h[0], h1 = m.ind_h[1];
         const double f0 = m.ifac_h[0], f1 = m.ifac_h[1];
         // the emission angle decides the radial interpolation mode and the reflection fraction: FP64;
         // the intensity and the incidence angle only enter FP32 arithmetic: FP32
-        m.d_tab[k] = (1.0 - fa) * lerp1(f0, (double) TV(tab.lp_del, 0, h0), (double) TV(tab.lp_del, 0, h0 + 1))
-            + fa * lerp1(f1, (double) TV(tab.lp_del, 1, h1), (double) TV(tab.lp_del, 1, h1 + 1));
+        m.d_tab[k] = (1.0 - fa) * lerp1(f0, f2d(TV(tab.lp_del, 0, h0)), f2d(TV(tab.lp_del, 0, h0 + 1)))
+            + fa * lerp1(f1, f2d(TV(tab.lp_del, 1, h1)), f2d(TV(tab.lp_del, 1, h1 + 1)));
         m.lp_e[k] = (1.0f - faf) * lerp1(f0f, TV(tab.lp_intens, 0, h0), TV(tab.lp_intens, 0, h0 + 1))
             + faf * lerp1(f1f, TV(tab.lp_intens, 1, h1), TV(tab.lp_intens, 1, h1 + 1));
         m.lp_di[k] = (1.0f - faf) * lerp1(f0f, TV(tab.lp_delinc, 0, h0), TV(tab.lp_delinc, 0, h0 + 1))
@@ -635,40 +639,58 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     __syncthreads();
     for (int k = tid; k < nrad; k += kSetupThreads) {
       if (k < nrad - 1) {
-        m.inv_drad_f[k] = 1.0f / (float) (m.jet_rad[k + 1] - m.jet_rad[k]);
+        m.inv_drad_f[k] = 1.0f / d2f(m.jet_rad[k + 1] - m.jet_rad[k]);
         m.lp_dle[k] = logf(m.lp_e[k + 1] / m.lp_e[k]);                        // log e_hi - log e_lo
-        m.lp_dlr[k] = logf((float) (m.jet_rad[k + 1] / m.jet_rad[k]));       // log r_hi - log r_lo
+        m.lp_dlr[k] = logf(d2f(m.jet_rad[k + 1] / m.jet_rad[k]));            // log r_hi - log r_lo
       }
-      m.jet_rad_f[k] = (float) m.jet_rad[k];
+      m.jet_rad_f[k] = d2f(m.jet_rad[k]);
       m.inv_jr_f[k] = 1.0f / m.jet_rad_f[k];
-      m.lp_d[k] = (float) m.d_tab[k];
+      m.lp_d[k] = d2f(m.d_tab[k]);
       m.lp_log[k] = (m.d_tab[k] / kPi * 180.0 <= 75.0) ? 0 : 1;
     }
     __syncthreads();
-    // rebin_emisprofile_on_radial_grid (Rellp.cpp:120-175)
+    // rebin_emisprofile_on_radial_grid (Rellp.cpp:120-175) and the flux boost of the emissivity
+    // (apply_emis_fluxboost_source_disk, Rellp.cpp:249-253, Relphysics.cpp:301-311) per fine radius.
+    // gi_potential_lp with sqrt(r) = 1/u of the fine grid; r^2 - 3r + 2a sqrt(r) cancels near the
+    // ISCO and stays FP64, as do r - rlo and r^1.5 + a; the rest runs in FP32.
+    const double hh = s.height, aa = s.a;
+    const float ut_h = (float) sqrt((hh * hh + aa * aa) / (hh * hh - 2 * hh + aa * aa));
+    const bool moving = fabs(s.beta) >= 1e-6, boosted = s.beta > 1e-6;
+    const float gam_f = d2f(s.gamma);
+    const double jr_last = m.jet_rad[nrad - 1];
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
-      double r = m.re[ii];
-      int kk = bsearch_asc_exact(m.jet_rad, m.jet_rad_f, nrad, r, (float) r);
-      if (r >= m.jet_rad[nrad - 1] && r - RELX_RELTABLE_MAX_R > 1e-6) atomicExch(&m.status, RELX_ERR_GRID);
-      // get_ipol_factor_radius (relutility.c:407-417); r - rlo in FP64, the rest in FP32
-      const float dr = (float) (r - m.jet_rad[kk]);
+      const double r = m.re[ii], sr = m.sqre[ii];
+      const int kk = bsearch_asc_pos(m.jet_rad, nrad, r);
+      if (dge(r, jr_last) && r - RELX_RELTABLE_MAX_R > 1e-6) atomicExch(&m.status, RELX_ERR_GRID);
+      // get_ipol_factor_radius (relutility.c:407-417)
+      const float dr = d2f(r - m.jet_rad[kk]);
       float inter;
       if (!m.lp_log[kk]) {
         inter = dr * m.inv_drad_f[kk];
       } else {
         inter = log1pf(dr * m.inv_jr_f[kk]) / m.lp_dlr[kk];
       }
-      // interp_log_1d (relutility.c:41-43) as e_lo * exp(inter * (log e_hi - log e_lo))
-      m.emis[ii] = (double) (m.lp_e[kk] * expf(inter * m.lp_dle[kk]));
-      m.del_emit[ii] = (double) (inter * m.lp_d[kk + 1] + (1.0f - inter) * m.lp_d[kk]);
-      m.del_inc[ii] = (double) (inter * m.lp_di[kk + 1] + (1.0f - inter) * m.lp_di[kk]);
+      const float del_e = inter * m.lp_d[kk + 1] + (1.0f - inter) * m.lp_d[kk];
+      m.del_emit[ii] = f2d(del_e);
+      m.del_inc[ii] = f2d(inter * m.lp_di[kk + 1] + (1.0f - inter) * m.lp_di[kk]);
+      const double t = r * r - 3 * r + 2 * aa * sr;
+      const float ut_d = d2f(r * sr + aa) / (d2f(sr) * sqrtf(d2f(t)));
+      float gi = ut_d / ut_h;
+      if (moving) gi = (float) gi_potential_lp(r, aa, hh, s.beta, f2d(del_e));
+      float boost = powf(gi, gam_f);
+      if (boosted) {
+        const float d = (float) doppler_factor(f2d(del_e), s.beta);
+        boost *= d * d;
+      }
+      // interp_log_1d (relutility.c:41-43) as e_lo * exp(inter * (log e_hi - log e_lo)), boosted
+      m.emis[ii] = f2d(m.lp_e[kk] * expf(inter * m.lp_dle[kk]) * boost);
     }
     __syncthreads();
     if (tid < 32) {
       // calc_refl_frac (Rellp.cpp:36-89); the three cosines on three lanes
       double ad_max = m.d_tab[nrad - 1];
-      double del_bh = m.del_emit[bsearch_desc(m.re, NR, s.rin)];
-      double del_ad = m.del_emit[bsearch_desc(m.re, NR, s.rout)];
+      double del_bh = m.del_emit[bsearch_desc_pos(m.re, NR, s.rin)];
+      double del_ad = m.del_emit[bsearch_desc_pos(m.re, NR, s.rout)];
       if (ad_max < kPi / 2.0) ad_max = kPi / 2.0;
       double ad_obs = ad_max;
       if (s.beta > 1e-6) {
@@ -687,23 +709,6 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
         s.refl_frac_lp = f_ad / f_inf;
       }
     }
-    // apply_emis_fluxboost_source_disk (Rellp.cpp:249-253, Relphysics.cpp:301-311).  gi_potential_lp
-    // with sqrt(r) = 1/u of the fine grid; r^2 - 3r + 2a sqrt(r) cancels near the ISCO and stays FP64.
-    const double hh = s.height, aa = s.a;
-    const float ut_h = (float) sqrt((hh * hh + aa * aa) / (hh * hh - 2 * hh + aa * aa));
-    for (int ii = tid; ii < NR; ii += kSetupThreads) {
-      const double r = m.re[ii], sr = m.sqre[ii];
-      const double t = r * r - 3 * r + 2 * aa * sr;
-      const float ut_d = (float) (r * sr + aa) / ((float) sr * sqrtf((float) t));
-      float gi = ut_d / ut_h;
-      if (fabs(s.beta) >= 1e-6) gi = (float) gi_potential_lp(r, aa, hh, s.beta, m.del_emit[ii]);
-      float boost = powf(gi, (float) s.gamma);
-      if (s.beta > 1e-6) {
-        float d = (float) doppler_factor(m.del_emit[ii], s.beta);
-        boost *= d * d;
-      }
-      m.emis[ii] *= (double) boost;
-    }
   }
   __syncthreads();
   // ---- returning radiation without xillver corrections (calc_emis_profile, Rellp.cpp:556-558)
@@ -718,22 +723,20 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   }
   if (rrad && m.status == RELX_OK) {
     RradSmem &q = m.rt.rr;
-    for (int j = tid; j < q.n; j += kSetupThreads) q.emis_in[j] = (float) rebin_mean_at(m.re, m.emis, NR, q.rad[j]);
+    for (int j = tid; j < q.n; j += kSetupThreads) q.emis_in[j] = d2f(rebin_mean_at(m.re, m.emis, NR, q.rad[j]));
     __syncthreads();
-    rrad_pass(tab, q, (float) s.gamma, false);
+    rrad_pass(tab, q, d2f(s.gamma), false);
     __syncthreads();
     for (int k = tid; k + 1 < q.n; k += kSetupThreads) q.dl[k] = log2f(q.er[k + 1] / q.er[k]);
     __syncthreads();
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
-      m.rt.emis_lp[ii] = (float) m.emis[ii];
+      m.rt.emis_lp[ii] = d2f(m.emis[ii]);
       const double r = rrad_at(q, m.re[ii]);
       m.emis[ii] = (m.return_rad == 1) ? m.emis[ii] + r : r;
     }
     __syncthreads();
   }
-  for (int ii = tid; ii < NR; ii += kSetupThreads) {
-    R.rec[ii].ew = (float) (m.emis[ii] * (double) R.wt[ii]);
-  }
+  for (int ii = tid; ii < NR; ii += kSetupThreads) R.rec[ii].ew = d2f(m.emis[ii]) * R.wt[ii];
 
   // ---- zones: fine-radius index ranges (zone is non-increasing with the radius index)
   for (int z = tid; z < s.nz; z += kSetupThreads) { s.zi0[z] = 1; s.zi1[z] = 0; }
@@ -812,11 +815,11 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     double ect_z = s.ect_src * m.shift[z];
     float inp[10];
     for (int q = 0; q < 10; q++) inp[q] = 0.0f;
-    inp[0] = (float) s.gam;
-    inp[1] = (float) m.afe;
-    inp[2] = (float) m.zlxi[z];
-    inp[3] = (float) ect_z;
-    inp[4] = (float) m.zdens[z];
+    inp[0] = d2f(s.gam);
+    inp[1] = d2f(m.afe);
+    inp[2] = d2f(m.zlxi[z]);
+    inp[3] = d2f(ect_z);
+    inp[4] = d2f(m.zdens[z]);
     inp[7] = (float) (s.incl * 180 / kPi);
     for (int q = 0; q < npar; q++) {
       const float *pv = tab.x_vals + q * tab.x_maxvals;
@@ -832,10 +835,10 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
         else if (val > pv[nv - 1]) val = pv[nv - 1];
       }
       float f = (val - pv[ind]) / (pv[ind + 1] - pv[ind]);
-      m.zfac[z][q] = (double) f;
+      m.zfac[z][q] = f2d(f);
       if (pi == 3) {  // ensure_ecut_within_boundarys (xilltable.c:1054-1067)
-        if (ect_z <= pv[0]) m.zfac[z][q] = 0.0;
-        if (ect_z >= pv[nv - 1]) m.zfac[z][q] = 1.0;
+        if (!dgt(ect_z, f2d(pv[0]))) m.zfac[z][q] = 0.0;  // the Ecut grid is positive
+        if (dge(ect_z, f2d(pv[nv - 1]))) m.zfac[z][q] = 1.0;
       }
     }
   }
@@ -848,22 +851,24 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     if (tid == 0) s.src_norm = 0.0;
     for (int z = tid; z < nz; z += kSetupThreads) m.xscale[z] = 1.0;
   } else {
-    const float gam = (float) s.gam;
+    const float gam = d2f(s.gam);
     const int lane = tid & 31, warp = tid >> 5;
     for (int b = tid; b < RELX_NCOARSE; b += kSetupThreads) m.cpow[b] = powf(tab.coarse_t[b].x, -gam);
     __syncthreads();
     for (int qq = warp; qq <= nz; qq += kSetupThreads / 32) {
       const double shift = (qq == 0) ? 1.0 : m.shift[qq - 1];
       if (qq > 0 && shift == 1.0) continue;
-      const float ecut = (float) (s.ect_src * shift);
+      const float ecut = d2f(s.ect_src * shift);
       const double q = primary_qsum_warp(tab, gam, ecut, m.cpow);
       if (lane == 0) m.qsum[qq] = q;
     }
     __syncthreads();
-    const double src_norm = 1.0 / m.qsum[0];
-    if (tid == 0) s.src_norm = src_norm;
-    for (int z = tid; z < nz; z += kSetupThreads)
-      m.xscale[z] = (m.shift[z] == 1.0) ? 1.0 : m.qsum[z + 1] * src_norm;  // 1 / (disk factor / source factor)
+    if (tid < 32) {  // one warp: the reciprocal is a chain of FP64 operations
+      const double src_norm = 1.0 / m.qsum[0];
+      if (tid == 0) s.src_norm = src_norm;
+      for (int z = tid; z < nz; z += 32)
+        m.xscale[z] = (m.shift[z] == 1.0) ? 1.0 : m.qsum[z + 1] * src_norm;  // 1 / (disk factor / source factor)
+    }
   }
   __syncthreads();
   const int ni = tab.x_nincl;
@@ -887,7 +892,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
         w *= up ? f : (1.0 - f);
       }
       zcout[set].row[z][c] = (int) (row * ni);
-      zcout[set].w[z][c] = (float) (w * m.xscale[z]);
+      zcout[set].w[z][c] = d2f(w * m.xscale[z]);
     }
     if (tid == 0) {
       s.ucount = 0;
@@ -925,7 +930,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       double d = m.zdens[m.cfirst[e] / ncz];
       if (fabs(d - 15) > 1e-6) dscale = 1.0 / pow(10.0, d - 15);
     }
-    m.cw[e] = (float) (w * dscale * m.xscale[z]);
+    m.cw[e] = d2f(w * dscale * m.xscale[z]);
     m.clive[e] = 0;
   }
   __syncthreads();
@@ -982,11 +987,16 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
   // keep the one above
   if (rrad && m.is_relxill && s.a > 0.0 && m.status == RELX_OK) {
     RradSmem &q = m.rt.rr;
-    if (tid < nz) {  // get_xillver_fluxcorrection_factors (Xillspec.cpp:500-526) from per-corner integrals
-      const int z = tid;
-      const int nq = tab.x_npar - 1;  // parameters bracketed per corner
+    // get_xillver_fluxcorrection_factors (Xillspec.cpp:500-526) from per-corner integrals: a warp per
+    // zone, a lane per corner, the corner terms summed across the lanes; the factors themselves in
+    // FP32 (they enter the FP32 returning-radiation pass)
+    const int nq = tab.x_npar - 1, ncorner = 1 << nq;  // parameters bracketed per corner (<= 5)
+    const int lane = tid & 31, warp = tid >> 5;
+    const float p15 = powf(1.5f, d2f(s.gam));
+    for (int z = warp; z < nz; z += kSetupThreads / 32) {
       double ef = 0.0, pf = 0.0, pfz = 0.0;
-      for (int c = 0; c < (1 << nq); c++) {
+      if (lane < ncorner) {
+        const int c = lane;
         double w = 1.0;
         long corner = 0;
         for (int qq = 0; qq < nq; qq++) {
@@ -995,53 +1005,63 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
           w *= up ? f : (1.0 - f);
           corner = corner * tab.x_nvals[qq] + m.zind[z][qq] + up;
         }
-        if (w == 0.0) continue;
-        if (!tab.x_has_dens) {
-          const double d = m.zdens[m.cfirst[z * 16 + c] >> 4];
-          if (fabs(d - 15) > 1e-6) w *= 1.0 / pow(10.0, d - 15);
+        if (w != 0.0) {
+          if (!tab.x_has_dens) {
+            const double d = m.zdens[m.cfirst[z * 16 + c] >> 4];
+            if (fabs(d - 15) > 1e-6) w *= 1.0 / pow(10.0, d - 15);
+          }
+          const double *fc = tab.x_fcorr + (size_t) corner * 3;
+          ef = w * fc[0];
+          pf = w * fc[1];
+          pfz = w * fc[2];
         }
-        const double *fc = tab.x_fcorr + (size_t) corner * 3;
-        ef += w * fc[0];
-        pf += w * fc[1];
-        pfz += w * fc[2];
       }
-      // energy flux of the normalised direct spectrum in 0.1-1000 keV: the table normalisation,
-      // less the coarse bins outside that band (Xillspec.cpp:179-205, 344-361)
-      const double qz = (m.shift[z] == 1.0) ? m.qsum[0] : m.qsum[z + 1];
-      const float ecut = (float) (s.ect_src * m.shift[z]);
-      double x = 0.0;
-      for (int e2 = 0; e2 < 2; e2++) {
-        const int b = tab.coarse_b2_skip[e2];
-        if (b < 0) continue;
-        if (s.prim == 1) {  // the end-bin correction is only restated for the cut-off power law
-          m.status = RELX_ERR_UNSUPPORTED;
-          continue;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ef += __shfl_xor_sync(0xffffffffu, ef, o);
+        pf += __shfl_xor_sync(0xffffffffu, pf, o);
+        pfz += __shfl_xor_sync(0xffffffffu, pfz, o);
+      }
+      if (lane == 0) {
+        // energy flux of the normalised direct spectrum in 0.1-1000 keV: the table normalisation,
+        // less the coarse bins outside that band (Xillspec.cpp:179-205, 344-361)
+        const double qz = (m.shift[z] == 1.0) ? m.qsum[0] : m.qsum[z + 1];
+        const float ecut = d2f(s.ect_src * m.shift[z]);
+        double x = 0.0;
+        for (int e2 = 0; e2 < 2; e2++) {
+          const int b = tab.coarse_b2_skip[e2];
+          if (b < 0) continue;
+          if (s.prim == 1) {  // the end-bin correction is only restated for the cut-off power law
+            m.status = RELX_ERR_UNSUPPORTED;
+            continue;
+          }
+          const float4 t = tab.coarse_t[b];
+          const float term = expf(1.0f / ecut) * m.cpow[b] * expf(-t.x / ecut) * t.y;
+          x += f2d(term) * (f2d(t.z) + f2d(t.w));
         }
-        const float4 t = tab.coarse_t[b];
-        const float term = expf(1.0f / ecut) * m.cpow[b] * expf(-t.x / ecut) * t.y;
-        x += (double) term * ((double) t.z + (double) t.w);
+        const float ef_direct = (float) ((1e15 / 4.0 / kPi) / (1e20 * 1.602177e-09)) - d2f(x) / d2f(qz);
+        q.zcf_flux[z] = f2d(d2f(ef) / ef_direct);
+        q.zcf_g[z] = f2d(d2f(pf) / d2f(pfz) / p15);
       }
-      const double ef_direct = (1e15 / 4.0 / kPi) / (1e20 * 1.602177e-09) - x / qz;
-      q.zcf_flux[z] = ef / ef_direct;
-      q.zcf_g[z] = (pf / pfz) / pow(1.5, s.gam);
     }
     __syncthreads();
     for (int k = tid; k < q.n; k += kSetupThreads) {  // rebin_to_grid (Relreturn_Corona.cpp:208-222)
-      int zi = bsearch_asc<double>(s.rgrid, nz + 1, q.rad[k]);
+      int zi = bsearch_asc_pos(s.rgrid, nz + 1, q.rad[k]);
       if (q.rad[k] < s.rgrid[0]) zi = 0;
       else if (q.rad[k] > s.rgrid[nz]) zi = nz - 1;
-      q.cf_flux[k] = (float) q.zcf_flux[zi];
-      q.cf_g[k] = q.zcf_g[zi];
+      q.cf_flux[k] = d2f(q.zcf_flux[zi]);
+      q.cg_f[k] = d2f(q.zcf_g[zi]);
+      q.use_corr[k] = fabs(q.zcf_g[zi] - 1) > 1e-3;
     }
     __syncthreads();
-    rrad_pass(tab, q, (float) s.gamma, true);
+    rrad_pass(tab, q, d2f(s.gamma), true);
     __syncthreads();
     for (int k = tid; k + 1 < q.n; k += kSetupThreads) q.dl[k] = log2f(q.er[k + 1] / q.er[k]);
     __syncthreads();
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
       const double r = rrad_at(q, m.re[ii]);
-      const double e = (m.return_rad == 1) ? (double) m.rt.emis_lp[ii] + r : r;
-      R.rec[ii].ew = (float) (e * (double) R.wt[ii]);
+      const double e = (m.return_rad == 1) ? f2d(m.rt.emis_lp[ii]) + r : r;
+      R.rec[ii].ew = d2f(e) * R.wt[ii];
     }
     if (tid == 0) s.rr_corr = 1;
   }
@@ -1053,7 +1073,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
     } else {
       double rfi = s.refl_frac;
       if (s.boost_switch) rfi *= s.refl_frac_lp;
-      double pf = s.f_inf_rest / 0.5 * pow(s.g_inf, s.gam);
+      double pf = s.f_inf_rest / 0.5 * m.ginf_pow;
       if (s.beta > 1e-4) {
         double d = doppler_factor(kPi - s.incl, s.beta);
         pf *= d * d;
@@ -1061,7 +1081,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(RelxTables tab, in
       s.prim_fac = pf;
       s.norm_fac_refl = fabs(rfi) / s.refl_frac_lp;
     }
-    for (int z = 0; z < nz; z++) s.inv_nc[z] = (float) m.xscale[z];
+    for (int z = 0; z < nz; z++) s.inv_nc[z] = d2f(m.xscale[z]);
     if (m.status != RELX_OK) s.status = m.status;
   }
   __syncthreads();

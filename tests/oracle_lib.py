@@ -6,6 +6,7 @@ infrastructure); it is built here with make and never used by the product.
 from __future__ import annotations
 
 import ctypes
+import multiprocessing as mp
 import os
 import subprocess
 
@@ -76,3 +77,27 @@ def conv_grid() -> np.ndarray:
     g = np.zeros(4097)
     lib().relxo_conv_grid(g.ctypes.data_as(_dp))
     return g
+
+
+def _pool_init(table_path: str, env: dict) -> None:
+    os.environ.update(env)
+    lib(table_path)
+
+
+def _pool_eval(args):
+    model, params, energy, flux_in, igt, igi = args
+    return evaluate(model, params, energy, flux_in, igt, igi)
+
+
+def pool(table_path: str, procs: int | None = None, env: dict | None = None):
+    """A pool of spawned processes, each with the oracle on table_path (the oracle keeps the first
+    tables it loads, so other tables need other processes).  env: variables the children set first
+    (RELXILL_NUM_RZONES)."""
+    build()
+    n = procs or max(1, min(16, os.cpu_count() or 1))
+    return mp.get_context("spawn").Pool(n, initializer=_pool_init, initargs=(table_path, dict(env or {})))
+
+
+def evaluate_many(pl, jobs):
+    """jobs: (model, params, energy, flux_in, ion_grad_type, iongrad_index) tuples; [(status, flux)]."""
+    return pl.map(_pool_eval, jobs, chunksize=1)

@@ -159,3 +159,43 @@ def test_tiles_chunks_and_graphs_give_the_same_numbers(gpu, monkeypatch):
         assert any(t["model"] == 3 for t in gpu.tuning_report())
     finally:
         gpu.tuning_config(autotune=True, graphs=True)
+
+
+def test_serve_allocates_nothing_and_refuses_request_beyond_slot(gpu):
+    """Each slot carves its batches from the half of the budget it allocated at creation: device
+    memory does not change while serving, and a request that alone needs more than a slot completes
+    with RELX_ERR_NOMEM (7) while the requests around it complete normally.  With a 600 KB budget a
+    relline set of 200 bins (about 100 KB of workspace) fits a slot and one of 16000 bins (about
+    600 KB: 32 bytes per energy edge) does not."""
+    torch = pytest.importorskip("torch")
+    p = np.array([6.4, 3, 3, 15, 0.9, 30, -1, 400, 0, 0], dtype=float)
+    small = [log_grid(1.0, 10.0, 200 + 7 * k) for k in range(5)]
+    big = log_grid(1.0, 10.0, 16000)
+    want = [_batch(gpu, "relline", p[None], [g])[0] for g in small]
+    with gpu.Server(hbm_budget_bytes=600 << 10, max_batch=8) as srv:
+        o = np.empty(len(small[0]) - 1)  # first batch: the streams the slots launch on are set up
+        srv.submit("relline", p, small[0], o)
+        t0 = time.time()
+        while not srv.poll() and time.time() - t0 < 60:
+            time.sleep(0.001)
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        outs, ids = [], []
+        for k, g in enumerate(small[:3] + [big] + small[3:]):
+            o = np.empty(len(g) - 1)
+            outs.append(o)
+            ids.append(srv.submit("relline", p, g, o))
+        st = {}
+        t0 = time.time()
+        while len(st) < len(ids) and time.time() - t0 < 60:
+            for rid, s, _ in srv.poll():
+                st[rid] = s
+            time.sleep(0.001)
+        assert len(st) == len(ids)
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free0
+    assert st[ids[3]] == 7
+    got = [outs[k] for k in (0, 1, 2, 4, 5)]
+    for k, (a, b) in enumerate(zip(got, want)):
+        assert st[ids[k if k < 3 else k + 1]] == 0
+        np.testing.assert_array_equal(a, b)
