@@ -895,6 +895,8 @@ static Context &ctx() {
 
 static int set_kernel_attrs(const Tables &T) {
   RELX_CUDA(cudaFuncSetAttribute(setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) setup_smem_bytes()));
+  // four set-up CTAs per SM (52 KB each): the largest shared-memory carve-out
+  RELX_CUDA(cudaFuncSetAttribute(setup_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   RELX_CUDA(relline_set_smem(T.d.rel_nr, T.d.rel_ng));
   RELX_CUDA(nthcomp_set_smem());
   RELX_CUDA(xillver_set_smem(T.d.x_nincl));

@@ -17,6 +17,10 @@
 namespace relx {
 
 constexpr int kSetupThreads = 256;
+constexpr int kQGroup = 8;
+constexpr double kDeg75 = 75.0 / 180.0 * 3.14159265358979323846;  // 75 degrees in radians  // continua summed together (normalisation of the primary continuum)
+// the table normalisation's unit factor (Xillspec.cpp:179-205), one product
+constexpr double kQsumScale = 1e20 * 1.602177e-09 / (1e15 / 4.0 / kPi);
 
 // returning radiation of one set on the radial bins of the return table (Relreturn_Corona.cpp)
 struct RradSmem {
@@ -35,7 +39,7 @@ struct RradSmem {
 struct SetupSmem {
   RelxSetState s;
   double re_tab[RELX_MAX_NRTAB], gmin_t[RELX_MAX_NRTAB], gmax_t[RELX_MAX_NRTAB];
-  double re[RELX_NFRAD], emis[RELX_NFRAD], del_emit[RELX_NFRAD], del_inc[RELX_NFRAD];
+  double re[RELX_NFRAD];
   union {
     double sqre[RELX_NFRAD];   // 1/u of the fine grid, i.e. sqrt(re) (lamp-post flux boost only)
     struct {                   // returning radiation, after the lamp-post emissivity
@@ -49,6 +53,8 @@ struct SetupSmem {
   float lp_e[RELX_MAX_NRADLP], inv_jr_f[RELX_MAX_NRADLP], inv_drad_f[RELX_MAX_NRADLP];
   unsigned char lp_log[RELX_MAX_NRADLP];  // logarithmic radial factor (emission angle above 75 deg)
   double qsum[RELX_NZMAX + 1];       // normalisation sums of the primary continuum
+  float qecut[RELX_NZMAX + 1];       // their cut-off energies
+  float2 qpart[kSetupThreads / 32][8];  // per-warp partial sums of a group of continua
   float cpow[RELX_NCOARSE];          // E^-Gamma at the coarse-grid bin centres
   double jet_rad[RELX_MAX_NRADLP], d_tab[RELX_MAX_NRADLP];
   double red[40];
@@ -62,17 +68,28 @@ struct SetupSmem {
   // lamp post interpolation
   int lp_ind_a, ind_h[2];
   double ginf_pow;   // g_inf^Gamma of the primary's flux factor (computed early, beside other work)
+  double fg_r1, fg_du;  // fine radial grid: u = 1/sqrt(r) of Rout and the step in u
+  float ut_h, inv_rbr;  // lamp-post u^t of the source; 1 / Rbr
   double lp_ifac_a, ifac_h[2];
   // zones
   double rmean[RELX_NZMAX], shift[RELX_NZMAX], zlxi[RELX_NZMAX], zdens[RELX_NZMAX], xscale[RELX_NZMAX];
   double zdel_emit[RELX_NZMAX];
   int zind[RELX_NZMAX][RELX_MAX_XPAR];
   double zfac[RELX_NZMAX][RELX_MAX_XPAR];
-  int crow[RELX_NZMAX * 16];
-  short cfirst[RELX_NZMAX * 16];
-  short cuniq[RELX_NZMAX * 16];
-  float cw[RELX_NZMAX * 16];            // weight of every (zone, corner) entry
-  unsigned char clive[RELX_NZMAX * 16]; // row has a non-zero weight in some zone
+  // the emissivity of the fine radii (FP32 values) is read up to the zones' ionisation, the corner
+  // lists only after it: they share their storage
+  union {
+    struct {
+      float emis[RELX_NFRAD], del_emit[RELX_NFRAD], del_inc[RELX_NFRAD];
+    } pr;
+    struct {
+      int crow[RELX_NZMAX * 16];
+      short cfirst[RELX_NZMAX * 16];
+      short cuniq[RELX_NZMAX * 16];
+      float cw[RELX_NZMAX * 16];            // weight of every (zone, corner) entry
+      unsigned char clive[RELX_NZMAX * 16]; // row has a non-zero weight in some zone
+    } cr;
+  };
 };
 static_assert(sizeof(RradSmem) + sizeof(float) * RELX_NFRAD <= sizeof(double) * RELX_NFRAD,
               "returning-radiation scratch fits in the lamp-post scratch it reuses");
@@ -260,7 +277,7 @@ __device__ void zone_grid_warp(double rmin, double rmax, int nz, double h, doubl
 }
 
 // x0 descending; index ii with x0[ii] > xn >= x0[ii+1] (inv_rebin_mean, relutility.c:636-663)
-__device__ double rebin_mean_at(const double *x0, const double *y0, int n0, double xn) {
+__device__ double rebin_mean_at(const double *x0, const float *y0, int n0, double xn) {
   int klo = 0, khi = n0 - 1;  // count of x0 > xn via bisection
   while (khi - klo > 1) {
     int k = (khi + klo) >> 1;
@@ -268,7 +285,7 @@ __device__ double rebin_mean_at(const double *x0, const double *y0, int n0, doub
   }
   int ii = klo;
   double f = (xn - x0[ii + 1]) / (x0[ii] - x0[ii + 1]);
-  return lerp1(f, y0[ii + 1], y0[ii]);
+  return lerp1(f, f2d(y0[ii + 1]), f2d(y0[ii]));
 }
 
 
@@ -403,7 +420,22 @@ __device__ __forceinline__ double rrad_at(const RradSmem &q, double r) {
   return f2d(q.er[kk] * exp2f(inter * q.dl[kk]));
 }
 
-__global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab, int model, const RelxSetIn *__restrict__ sin,
+// the ionisation and density of zone z without an emissivity-based gradient: a power law in the
+// zone's mean radius (ion_grad_type 1, IonGradient.cpp:128-138) or the set's values, clamped to
+// the table's logxi range
+__device__ void zone_ionisation(SetupSmem &m, const RelxSetState &s, int z) {
+  if (s.ion_grad_type == 1) {
+    double l = exp(m.lxi) * pow(m.rmean[z] / (0.5 * (s.rgrid[0] + s.rgrid[1])), -1.0 * m.iongrad_index);
+    m.zlxi[z] = log(l);
+  } else {
+    m.zlxi[z] = m.lxi;
+  }
+  m.zdens[z] = m.dens;
+  if (m.zlxi[z] < 0.0) m.zlxi[z] = 0.0;
+  else if (m.zlxi[z] > 4.7) m.zlxi[z] = 4.7;
+}
+
+__global__ void __launch_bounds__(kSetupThreads, 4) setup_kernel(RelxTables tab, int model, const RelxSetIn *__restrict__ sin,
                                                                const double *__restrict__ user_e, double *__restrict__ line_e,
                                                                RelxSetState *__restrict__ sout, RelxRadial *__restrict__ rout,
                                                                RelxCorners *__restrict__ cout, RelxZoneCorners *__restrict__ zcout) {
@@ -458,9 +490,34 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
     s.ifac_mu0 = (muf - tab.rel_mu0[im]) / (tab.rel_mu0[im + 1] - tab.rel_mu0[im]);
     s.g_n = gn;
   }
-  if (tid < 32) zone_grid_warp(s.rin, s.rout, s.nz, s.height, s.rgrid);
-  if (tid == 64) m.ginf_pow = pow(s.g_inf, s.gam);  // warp 2, beside warps 0 and 1
+  if (tid == 96) {  // warp 3: the set's FP64 constants of the per-radius loops, computed once
+    m.fg_r1 = 1.0 / sqrt(s.rout);
+    m.fg_du = (1.0 / sqrt(s.rin) - m.fg_r1) / (NR - 1);
+    if (s.emis_type == RELX_EMIS_LP) {
+      const double hh = s.height, aa = s.a;
+      m.ut_h = (float) sqrt((hh * hh + aa * aa) / (hh * hh - 2 * hh + aa * aa));
+    } else {
+      m.inv_rbr = (float) (1.0 / m.rbr);
+    }
+  }
   __syncthreads();
+  // warp 0: the zone grid, then the zone means and, where they need no emission angle, the zones'
+  // energy shifts and ionisation (IonGradient.cpp:128-171, 340-390); warp 2: g_inf^Gamma.  Both are
+  // FP64 chains on a few lanes; the other warps start the table interpolation and the fine grid,
+  // which need neither, and warps 0 and 2 join them after.
+  const bool early_shift = s.emis_type != RELX_EMIS_LP || fabs(s.beta) < 1e-6;
+  if (tid < 32) {
+    zone_grid_warp(s.rin, s.rout, s.nz, s.height, s.rgrid);
+    if (m.is_relxill) {
+      for (int z = tid; z < s.nz; z += 32) {
+        m.rmean[z] = 0.5 * (s.rgrid[z] + s.rgrid[z + 1]);
+        if (early_shift)  // a source at rest: gi_potential_lp does not read the emission angle
+          m.shift[z] = (s.emis_type == RELX_EMIS_LP) ? gi_potential_lp(m.rmean[z], s.a, s.height, s.beta, 0.0) : 1.0;
+        if (s.ion_grad_type != 2) zone_ionisation(m, s, z);
+      }
+    }
+  }
+  if (tid == 64) m.ginf_pow = pow(s.g_inf, s.gam);
   {
     const size_t b00 = (size_t) s.ind_a * nm + s.ind_mu0, b10 = (size_t) (s.ind_a + 1) * nm + s.ind_mu0;
     const size_t b01 = b00 + 1, b11 = b10 + 1;
@@ -476,8 +533,7 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
   }
   // fine radial grid (relutility.c:666-677)
   {
-    const double r1 = 1.0 / sqrt(s.rout), r2 = 1.0 / sqrt(s.rin);
-    const double du = (r2 - r1) / (NR - 1);  // the step once, not a division per radius
+    const double r1 = m.fg_r1, du = m.fg_du;  // 1/sqrt(rout) and the step in u
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
       double u = f2d((float) ii) * du + r1;  // ii < 2^24: exact
       double iu = __drcp_rn(u);
@@ -585,19 +641,20 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
     // get_emis_bkn + norm_emis_profile (Rellp.cpp:91-109,421-437)
     // the power law in FP32 (r / Rbr as a float product), the normalisation integral sum(e 4 wt)
     // as a float-float sum per thread (wt = r dr pi / 2 from the records above)
-    const float inv_rbr = (float) (1.0 / m.rbr);
+    const float inv_rbr = m.inv_rbr;
     const float a1 = d2f(-m.emis1), a2 = d2f(-m.emis2);
     float2 part = make_float2(0.0f, 0.0f);
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
       const double r = m.re[ii];
       const float e = powf(d2f(r) * inv_rbr, dgt(r, m.rbr) ? a2 : a1);
-      m.emis[ii] = f2d(e);
-      m.del_emit[ii] = -1.0;
-      m.del_inc[ii] = -1.0;
+      m.pr.emis[ii] = e;
+      m.pr.del_emit[ii] = -1.0f;
+      m.pr.del_inc[ii] = -1.0f;
       part = ff_add(part, ff_mulf(make_float2(e, 0.0f), 4.0f * R.wt[ii]));
     }
     const double inv_integ = 1.0 / block_sum_d<kSetupThreads>(ff_to_double(part), m.red);
-    for (int ii = tid; ii < NR; ii += kSetupThreads) m.emis[ii] *= inv_integ;
+    for (int ii = tid; ii < NR; ii += kSetupThreads) m.pr.emis[ii] = d2f(f2d(m.pr.emis[ii]) * inv_integ);
+    __syncthreads();
     if (tid == 0) { s.f_inf_rest = 0; s.refl_frac_lp = 0; }
   } else {
     // lamp post: interpol_lptable (Rellp.cpp:190-247)
@@ -639,14 +696,15 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
     __syncthreads();
     for (int k = tid; k < nrad; k += kSetupThreads) {
       if (k < nrad - 1) {
-        m.inv_drad_f[k] = 1.0f / d2f(m.jet_rad[k + 1] - m.jet_rad[k]);
+        const float djr = d2f(m.jet_rad[k + 1] - m.jet_rad[k]);
+        m.inv_drad_f[k] = 1.0f / djr;
         m.lp_dle[k] = logf(m.lp_e[k + 1] / m.lp_e[k]);                        // log e_hi - log e_lo
-        m.lp_dlr[k] = logf(d2f(m.jet_rad[k + 1] / m.jet_rad[k]));            // log r_hi - log r_lo
+        m.lp_dlr[k] = log1pf(djr / d2f(m.jet_rad[k]));  // log r_hi - log r_lo (no FP64 division)
       }
       m.jet_rad_f[k] = d2f(m.jet_rad[k]);
       m.inv_jr_f[k] = 1.0f / m.jet_rad_f[k];
       m.lp_d[k] = d2f(m.d_tab[k]);
-      m.lp_log[k] = (m.d_tab[k] / kPi * 180.0 <= 75.0) ? 0 : 1;
+      m.lp_log[k] = dgt(m.d_tab[k], kDeg75) ? 1 : 0;  // emission angle above 75 degrees
     }
     __syncthreads();
     // rebin_emisprofile_on_radial_grid (Rellp.cpp:120-175) and the flux boost of the emissivity
@@ -654,7 +712,7 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
     // gi_potential_lp with sqrt(r) = 1/u of the fine grid; r^2 - 3r + 2a sqrt(r) cancels near the
     // ISCO and stays FP64, as do r - rlo and r^1.5 + a; the rest runs in FP32.
     const double hh = s.height, aa = s.a;
-    const float ut_h = (float) sqrt((hh * hh + aa * aa) / (hh * hh - 2 * hh + aa * aa));
+    const float ut_h = m.ut_h;
     const bool moving = fabs(s.beta) >= 1e-6, boosted = s.beta > 1e-6;
     const float gam_f = d2f(s.gamma);
     const double jr_last = m.jet_rad[nrad - 1];
@@ -671,8 +729,8 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
         inter = log1pf(dr * m.inv_jr_f[kk]) / m.lp_dlr[kk];
       }
       const float del_e = inter * m.lp_d[kk + 1] + (1.0f - inter) * m.lp_d[kk];
-      m.del_emit[ii] = f2d(del_e);
-      m.del_inc[ii] = f2d(inter * m.lp_di[kk + 1] + (1.0f - inter) * m.lp_di[kk]);
+      m.pr.del_emit[ii] = del_e;
+      m.pr.del_inc[ii] = inter * m.lp_di[kk + 1] + (1.0f - inter) * m.lp_di[kk];
       const double t = r * r - 3 * r + 2 * aa * sr;
       const float ut_d = d2f(r * sr + aa) / (d2f(sr) * sqrtf(d2f(t)));
       float gi = ut_d / ut_h;
@@ -683,14 +741,15 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
         boost *= d * d;
       }
       // interp_log_1d (relutility.c:41-43) as e_lo * exp(inter * (log e_hi - log e_lo)), boosted
-      m.emis[ii] = f2d(m.lp_e[kk] * expf(inter * m.lp_dle[kk]) * boost);
+      m.pr.emis[ii] = m.lp_e[kk] * expf(inter * m.lp_dle[kk]) * boost;
     }
     __syncthreads();
-    if (tid < 32) {
-      // calc_refl_frac (Rellp.cpp:36-89); the three cosines on three lanes
+    if (tid >= kSetupThreads - 32) {
+      // calc_refl_frac (Rellp.cpp:36-89) on the last warp, which joins the next loops after it (its
+      // results are read at the end); the three cosines on three lanes
       double ad_max = m.d_tab[nrad - 1];
-      double del_bh = m.del_emit[bsearch_desc_pos(m.re, NR, s.rin)];
-      double del_ad = m.del_emit[bsearch_desc_pos(m.re, NR, s.rout)];
+      double del_bh = f2d(m.pr.del_emit[bsearch_desc_pos(m.re, NR, s.rin)]);
+      double del_ad = f2d(m.pr.del_emit[bsearch_desc_pos(m.re, NR, s.rout)]);
       if (ad_max < kPi / 2.0) ad_max = kPi / 2.0;
       double ad_obs = ad_max;
       if (s.beta > 1e-6) {
@@ -698,7 +757,7 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
         del_ad = relat_abberation(del_ad, -1. * s.beta);
         ad_obs = relat_abberation(ad_max, -1. * s.beta);
       }
-      const int lane = tid;
+      const int lane = tid & 31;
       const double cx = cos(lane == 0 ? del_bh : lane == 1 ? del_ad : lane == 2 ? ad_max : ad_obs);
       const double c_bh = __shfl_sync(0xffffffffu, cx, 0), c_ad = __shfl_sync(0xffffffffu, cx, 1);
       const double c_max = __shfl_sync(0xffffffffu, cx, 2), c_obs = __shfl_sync(0xffffffffu, cx, 3);
@@ -710,7 +769,7 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
       }
     }
   }
-  __syncthreads();
+  // (the lamp-post branch ends behind a barrier after its per-radius loop)
   // ---- returning radiation without xillver corrections (calc_emis_profile, Rellp.cpp:556-558)
   const bool rrad = m.return_rad != 0 && m.status == RELX_OK;
   if (rrad) {
@@ -723,20 +782,20 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
   }
   if (rrad && m.status == RELX_OK) {
     RradSmem &q = m.rt.rr;
-    for (int j = tid; j < q.n; j += kSetupThreads) q.emis_in[j] = d2f(rebin_mean_at(m.re, m.emis, NR, q.rad[j]));
+    for (int j = tid; j < q.n; j += kSetupThreads) q.emis_in[j] = d2f(rebin_mean_at(m.re, m.pr.emis, NR, q.rad[j]));
     __syncthreads();
     rrad_pass(tab, q, d2f(s.gamma), false);
     __syncthreads();
     for (int k = tid; k + 1 < q.n; k += kSetupThreads) q.dl[k] = log2f(q.er[k + 1] / q.er[k]);
     __syncthreads();
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
-      m.rt.emis_lp[ii] = d2f(m.emis[ii]);
+      m.rt.emis_lp[ii] = m.pr.emis[ii];
       const double r = rrad_at(q, m.re[ii]);
-      m.emis[ii] = (m.return_rad == 1) ? m.emis[ii] + r : r;
+      m.pr.emis[ii] = d2f((m.return_rad == 1) ? f2d(m.pr.emis[ii]) + r : r);
     }
     __syncthreads();
   }
-  for (int ii = tid; ii < NR; ii += kSetupThreads) R.rec[ii].ew = d2f(m.emis[ii]) * R.wt[ii];
+  for (int ii = tid; ii < NR; ii += kSetupThreads) R.rec[ii].ew = m.pr.emis[ii] * R.wt[ii];
 
   // ---- zones: fine-radius index ranges (zone is non-increasing with the radius index)
   for (int z = tid; z < s.nz; z += kSetupThreads) { s.zi0[z] = 1; s.zi1[z] = 0; }
@@ -775,36 +834,30 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
 
   // ---- ionisation gradient (IonGradient.cpp:128-211, 340-390)
   const int nz = s.nz;
-  if (tid < nz) {
+  if (tid < nz && (!early_shift || s.ion_grad_type == 2)) {
     int z = tid;
-    m.rmean[z] = 0.5 * (s.rgrid[z] + s.rgrid[z + 1]);
-    m.zdel_emit[z] = rebin_mean_at(m.re, m.del_emit, NR, m.rmean[z]);
-    m.shift[z] = (s.emis_type == RELX_EMIS_LP) ? gi_potential_lp(m.rmean[z], s.a, s.height, s.beta, m.zdel_emit[z]) : 1.0;
-    if (s.ion_grad_type == 1) {
-      double l = exp(m.lxi) * pow(m.rmean[z] / (0.5 * (s.rgrid[0] + s.rgrid[1])), -1.0 * m.iongrad_index);
-      m.zlxi[z] = log(l);
-      m.zdens[z] = m.dens;
-    } else if (s.ion_grad_type == 2) {
+    if (!early_shift) {
+      m.zdel_emit[z] = rebin_mean_at(m.re, m.pr.del_emit, NR, m.rmean[z]);
+      m.shift[z] = gi_potential_lp(m.rmean[z], s.a, s.height, s.beta, m.zdel_emit[z]);
+    }
+    if (s.ion_grad_type == 2) {
       double rin = s.rgrid[0];
-      double irr = rebin_mean_at(m.re, m.emis, NR, m.rmean[z]);
-      double dinc = rebin_mean_at(m.re, m.del_inc, NR, m.rmean[z]);
+      double irr = rebin_mean_at(m.re, m.pr.emis, NR, m.rmean[z]);
+      double dinc = rebin_mean_at(m.re, m.pr.del_inc, NR, m.rmean[z]);
       double rad_lxi = (11. / 9.) * (11. / 9.) * rin;
       int kk = bsearch_desc(m.re, NR, rad_lxi);
       double ip = (rad_lxi - m.re[kk + 1]) / (m.re[kk] - m.re[kk + 1]);
-      double emis_r = lerp1(ip, m.emis[kk + 1], m.emis[kk]);
-      double dinc_r = lerp1(ip, m.del_inc[kk + 1], m.del_inc[kk]);
+      double emis_r = lerp1(ip, f2d(m.pr.emis[kk + 1]), f2d(m.pr.emis[kk]));
+      double dinc_r = lerp1(ip, f2d(m.pr.del_inc[kk + 1]), f2d(m.pr.del_inc[kk]));
       double lxi_max = log10(4.0 * kPi * emis_r / density_ss73_zone_a(rad_lxi, rin) * (cos(kPi / 4) / cos(dinc_r)));
       double fac = m.lxi - lxi_max;
       double dmin = density_ss73_zone_a((25. / 9.) * rin, rin);
       double dn = (m.flags & 4) ? 1.0 : density_ss73_zone_a(m.rmean[z], rin) / dmin;
       m.zdens[z] = log10(dn) + m.dens;
       m.zlxi[z] = log10(4.0 * kPi * irr / dn * (cos(kPi / 4) / cos(dinc))) + fac;
-    } else {
-      m.zlxi[z] = m.lxi;
-      m.zdens[z] = m.dens;
+      if (m.zlxi[z] < 0.0) m.zlxi[z] = 0.0;
+      else if (m.zlxi[z] > 4.7) m.zlxi[z] = 4.7;
     }
-    if (m.zlxi[z] < 0.0) m.zlxi[z] = 0.0;
-    else if (m.zlxi[z] > 4.7) m.zlxi[z] = 4.7;
   }
   __syncthreads();
 
@@ -854,15 +907,52 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
     const float gam = d2f(s.gam);
     const int lane = tid & 31, warp = tid >> 5;
     for (int b = tid; b < RELX_NCOARSE; b += kSetupThreads) m.cpow[b] = powf(tab.coarse_t[b].x, -gam);
+    for (int qq = tid; qq <= nz; qq += kSetupThreads) m.qecut[qq] = d2f(s.ect_src * (qq == 0 ? 1.0 : m.shift[qq - 1]));
     __syncthreads();
-    for (int qq = warp; qq <= nz; qq += kSetupThreads / 32) {
-      const double shift = (qq == 0) ? 1.0 : m.shift[qq - 1];
-      if (qq > 0 && shift == 1.0) continue;
-      const float ecut = d2f(s.ect_src * shift);
-      const double q = primary_qsum_warp(tab, gam, ecut, m.cpow);
-      if (lane == 0) m.qsum[qq] = q;
+    // the continua (the source, then the zones) in groups of kQGroup over the whole block: every
+    // thread sums the terms of its coarse bins for each continuum of the group (independent sums),
+    // the warps reduce with shuffles and one thread per continuum adds the warps' sums in warp order;
+    // float-float sums of FP32 terms (calcNormWrtXillverTableSpec, Xillspec.cpp:179-233)
+    for (int q0 = 0; q0 <= nz; q0 += kQGroup) {
+      const int nq = min(kQGroup, nz + 1 - q0);
+      float2 part[kQGroup];
+      float ecut[kQGroup], e0[kQGroup];
+#pragma unroll
+      for (int k = 0; k < kQGroup; k++) {
+        part[k] = make_float2(0.0f, 0.0f);
+        ecut[k] = m.qecut[q0 + min(k, nq - 1)];
+        e0[k] = expf(1.0f / ecut[k]);
+      }
+      for (int b = tid; b < RELX_NCOARSE; b += kSetupThreads) {
+        const float4 t = tab.coarse_t[b];  // bin centre, width, centre as float-float (0 outside the band)
+        const float pw = m.cpow[b];
+#pragma unroll
+        for (int k = 0; k < kQGroup; k++) {
+          if (k < nq) {  // uniform over the block
+            const float term = e0[k] * pw * expf(-t.x / ecut[k]) * t.y;
+            part[k] = ff_add(part[k], ff_mulf(make_float2(t.z, t.w), term));
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kQGroup; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          float2 u;
+          u.x = __shfl_xor_sync(0xffffffffu, part[k].x, o);
+          u.y = __shfl_xor_sync(0xffffffffu, part[k].y, o);
+          part[k] = ff_add(part[k], u);
+        }
+        if (lane == 0) m.qpart[warp][k] = part[k];
+      }
+      __syncthreads();
+      if (tid < nq) {
+        float2 a = m.qpart[0][tid];
+        for (int w = 1; w < kSetupThreads / 32; w++) a = ff_add(a, m.qpart[w][tid]);
+        m.qsum[q0 + tid] = (f2d(a.x) + f2d(a.y)) * kQsumScale;
+      }
+      __syncthreads();
     }
-    __syncthreads();
     if (tid < 32) {  // one warp: the reciprocal is a chain of FP64 operations
       const double src_norm = 1.0 / m.qsum[0];
       if (tid == 0) s.src_norm = src_norm;
@@ -907,14 +997,14 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
     long row = 0;
     for (int q = 0; q < nbits; q++) row = row * tab.x_nvals[q] + m.zind[z][q] + ((c >> q) & 1);
     row = row * ni;  // incl index 0
-    m.crow[e] = (int) row;
+    m.cr.crow[e] = (int) row;
   }
   __syncthreads();
   for (int e = tid; e < ncor; e += kSetupThreads) {
     int first = e;
     for (int f = 0; f < e; f++)
-      if (m.crow[f] == m.crow[e]) { first = f; break; }
-    m.cfirst[e] = (short) first;
+      if (m.cr.crow[f] == m.cr.crow[e]) { first = f; break; }
+    m.cr.cfirst[e] = (short) first;
   }
   __syncthreads();
   for (int e = tid; e < ncor; e += kSetupThreads) {
@@ -927,27 +1017,27 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
     // density division of the row by the zone that loads it first (xilltable.c:478-511)
     double dscale = 1.0;
     if (!tab.x_has_dens) {
-      double d = m.zdens[m.cfirst[e] / ncz];
+      double d = m.zdens[m.cr.cfirst[e] / ncz];
       if (fabs(d - 15) > 1e-6) dscale = 1.0 / pow(10.0, d - 15);
     }
-    m.cw[e] = d2f(w * dscale * m.xscale[z]);
-    m.clive[e] = 0;
+    m.cr.cw[e] = d2f(w * dscale * m.xscale[z]);
+    m.cr.clive[e] = 0;
   }
   __syncthreads();
   // a row is read only if some zone gives it a non-zero weight (a parameter on a grid value
   // puts exactly zero weight on the upper bracket)
   for (int e = tid; e < ncor; e += kSetupThreads)
-    if (m.cw[e] != 0.0f) m.clive[m.cfirst[e]] = 1;
+    if (m.cr.cw[e] != 0.0f) m.cr.clive[m.cr.cfirst[e]] = 1;
   __syncthreads();
   if (tid < 32 && listed) {  // number the live rows in entry order (warp prefix sums)
     const int lane = tid;
     int base = 0;
     for (int e0 = 0; e0 < ncor; e0 += 32) {
       const int e = e0 + lane;
-      const bool first = e < ncor && m.cfirst[e] == e;
-      const bool live = first && m.clive[e];
+      const bool first = e < ncor && m.cr.cfirst[e] == e;
+      const bool live = first && m.cr.clive[e];
       const unsigned int mask = __ballot_sync(0xffffffffu, live);
-      if (first) m.cuniq[e] = live ? (short) (base + __popc(mask & ((1u << lane) - 1u))) : (short) -1;
+      if (first) m.cr.cuniq[e] = live ? (short) (base + __popc(mask & ((1u << lane) - 1u))) : (short) -1;
       base += __popc(mask);
     }
     if (lane == 0) {
@@ -957,7 +1047,7 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
   }
   __syncthreads();
   for (int e = tid; e < ncor; e += kSetupThreads)
-    if (m.cfirst[e] != e) m.cuniq[e] = m.cuniq[m.cfirst[e]];  // the first entry is numbered above
+    if (m.cr.cfirst[e] != e) m.cr.cuniq[e] = m.cr.cuniq[m.cr.cfirst[e]];  // the first entry is numbered above
   // dense: at most RELX_ZDENSE zones and RELX_MAX_UCORNER distinct live rows (always so for the
   // 5-parameter table: 16 corners x 16 zones)
   const bool dense = listed && nz <= RELX_ZDENSE && m.ired[0] <= RELX_MAX_UCORNER;
@@ -972,14 +1062,14 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
     const int z = e / ncz, c = e - z * ncz;
     if (dense) {
       RelxCorners &C = cout[set];
-      const int u = m.cuniq[e];
+      const int u = m.cr.cuniq[e];
       if (u >= 0) {
-        C.w[u][z] = m.cw[e];  // each (u, z) pair is written by exactly one entry
-        if (m.cfirst[e] == e) C.row[u] = m.crow[e];
+        C.w[u][z] = m.cr.cw[e];  // each (u, z) pair is written by exactly one entry
+        if (m.cr.cfirst[e] == e) C.row[u] = m.cr.crow[e];
       }
     } else {
-      zcout[set].row[z][c] = m.crow[e];
-      zcout[set].w[z][c] = m.cw[e];
+      zcout[set].row[z][c] = m.cr.crow[e];
+      zcout[set].w[z][c] = m.cr.cw[e];
     }
   }
   // ---- returning radiation with the xillver flux-correction factors of the zones, for relxill models
@@ -1007,7 +1097,7 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
         }
         if (w != 0.0) {
           if (!tab.x_has_dens) {
-            const double d = m.zdens[m.cfirst[z * 16 + c] >> 4];
+            const double d = m.zdens[m.cr.cfirst[z * 16 + c] >> 4];
             if (fabs(d - 15) > 1e-6) w *= 1.0 / pow(10.0, d - 15);
           }
           const double *fc = tab.x_fcorr + (size_t) corner * 3;
@@ -1025,7 +1115,6 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
       if (lane == 0) {
         // energy flux of the normalised direct spectrum in 0.1-1000 keV: the table normalisation,
         // less the coarse bins outside that band (Xillspec.cpp:179-205, 344-361)
-        const double qz = (m.shift[z] == 1.0) ? m.qsum[0] : m.qsum[z + 1];
         const float ecut = d2f(s.ect_src * m.shift[z]);
         double x = 0.0;
         for (int e2 = 0; e2 < 2; e2++) {
@@ -1039,7 +1128,10 @@ __global__ void __launch_bounds__(kSetupThreads, 3) setup_kernel(RelxTables tab,
           const float term = expf(1.0f / ecut) * m.cpow[b] * expf(-t.x / ecut) * t.y;
           x += f2d(term) * (f2d(t.z) + f2d(t.w));
         }
-        const float ef_direct = (float) ((1e15 / 4.0 / kPi) / (1e20 * 1.602177e-09)) - d2f(x) / d2f(qz);
+        // the normalisation sum qz exists for the cut-off power law only (the nthcomp continuum has
+        // no end bins to take off here)
+        float ef_direct = (float) ((1e15 / 4.0 / kPi) / (1e20 * 1.602177e-09));
+        if (x != 0.0) ef_direct -= d2f(x) / d2f((m.shift[z] == 1.0) ? m.qsum[0] : m.qsum[z + 1]);
         q.zcf_flux[z] = f2d(d2f(ef) / ef_direct);
         q.zcf_g[z] = f2d(d2f(pf) / d2f(pfz) / p15);
       }
