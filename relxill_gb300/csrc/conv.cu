@@ -27,12 +27,13 @@ constexpr int kPre = 4;            // prefix sums are kept at every kPre-th bin
 constexpr int kXStage = 3072;      // xillver bins staged in shared memory (larger tables read global memory)
 static_assert(kN % (kConvThreads * kPre) == 0, "scan tiling");
 
-__device__ __forceinline__ int skew(int m) { return m + (m >> 4); }
+// xs is stored in rows of 16 bins, each followed by 4 padding floats: the 16-byte loads of the
+// threads of a quarter warp (16 bins apart) then fall in distinct banks
+__device__ __forceinline__ int skew(int m) { return m + ((m >> 4) << 2); }
 
 struct ConvSmem {
-  float xs[kN + kN / 16];      // x * cf, skewed
+  alignas(16) float xs[kN + kN / 4];  // x * cf, skewed
   float hr[kN + kConvR];       // rel * cf over the zone's profile window, zero padded (16-byte aligned)
-  float2 pre[kN / kPre + 1];   // float-float prefix sums of xs at bins 0, kPre, 2 kPre, ...
   float2 red[kConvThreads / 32 + 2];
   float2 wsum[kConvThreads / 32];
   double dred[kConvThreads / 32 + 2];
@@ -40,23 +41,32 @@ struct ConvSmem {
   float bc[2];                 // broadcast scalars
   int abort_flag;
   uint64_t bar;                // completion of the bulk copy of the zone's xillver spectrum
-  alignas(16) float xz[kXStage];  // the zone's xillver spectrum (bulk copy)
+  union {                      // the staged spectrum is read before the prefix sums are formed
+    alignas(16) float xz[kXStage];  // the zone's xillver spectrum (bulk copy)
+    float2 pre[kN / kPre + 1];   // float-float prefix sums of xs at bins 0, kPre, 2 kPre, ...
+  };
 };
 static_assert(offsetof(ConvSmem, hr) % 16 == 0, "the profile window is read as float4");
 
 // y[k0 + r] = sum_{i in [clo, chi)} hr[i - wlo] * xs[(k0 + r + p - i) mod N]; hr is zero padded
 // past the window, so chi - clo need not be a multiple of kConvD.  Register tile: kConvR outputs x
-// kConvD window bins per step, kConvR + kConvD - 1 loads of xs and kConvD/4 float4 loads of hr for
-// kConvR * kConvD FMAs.
+// kConvD window bins per step, (kConvR + kConvD) / 4 float4 loads of xs and kConvD/4 float4 loads
+// of hr for kConvR * kConvD FMAs.  k0 + p - clo must be a multiple of 4 (the xs loads are aligned).
 __device__ __forceinline__ void conv_tile(const ConvSmem &m, int k0, int p, int wlo, int clo, int chi,
                                           float y[kConvR]) {
 #pragma unroll
   for (int r = 0; r < kConvR; r++) y[r] = 0.0f;
   for (int i0 = clo; i0 < chi; i0 += kConvD) {
-    const int base = k0 + p - i0 - (kConvD - 1);
-    float xr[kConvR + kConvD - 1];
+    const int base = k0 + p - i0 - (kConvD - 1) - 1;  // one bin lower: a multiple of 4
+    float xr[kConvR + kConvD];
 #pragma unroll
-    for (int c = 0; c < kConvR + kConvD - 1; c++) xr[c] = m.xs[skew((base + c) & (kN - 1))];
+    for (int c4 = 0; c4 < (kConvR + kConvD) / 4; c4++) {
+      const float4 v = *reinterpret_cast<const float4 *>(&m.xs[skew((base + 4 * c4) & (kN - 1))]);
+      xr[4 * c4] = v.x;
+      xr[4 * c4 + 1] = v.y;
+      xr[4 * c4 + 2] = v.z;
+      xr[4 * c4 + 3] = v.w;
+    }
     const float4 *h4 = reinterpret_cast<const float4 *>(&m.hr[i0 - wlo]);
 #pragma unroll
     for (int d4 = 0; d4 < kConvD / 4; d4++) {
@@ -66,7 +76,7 @@ __device__ __forceinline__ void conv_tile(const ConvSmem &m, int k0, int p, int 
       for (int e = 0; e < 4; e++) {
         const int d = d4 * 4 + e;
 #pragma unroll
-        for (int r = 0; r < kConvR; r++) y[r] = fmaf(hs[e], xr[r - d + kConvD - 1], y[r]);
+        for (int r = 0; r < kConvR; r++) y[r] = fmaf(hs[e], xr[r - d + kConvD], y[r]);
       }
     }
   }
@@ -116,11 +126,12 @@ __device__ __forceinline__ int split_cost(int nt, int nc, int S) {
 
 // Convolution of xs with hr, normalised as calcFFTNormFactor (Relbase.cpp:199-222), written for the
 // conv bins [olo, ohi] the caller's grid needs.  The 0.01-1000 keV sum of the convolution is
-// sum_i hr_i * (window sum of xs) / cf, from prefix sums of xs (cf = E/dE is the same in every
-// bin of the log grid up to rounding), so bins outside [olo, ohi] are never convolved.  The sums
-// are float-float (about 48 significant bits, on the FP32 pipe).
+// sum_i hr_i * (window sum of xs) / cf, from prefix sums of xs, and the band sum of the xillver
+// spectrum is the band's window sum of xs / cf (cf = E/dE is the same in every bin of the log grid
+// up to rounding, and cancels), so bins outside [olo, ohi] are never convolved.  The sums are
+// float-float (about 48 significant bits, on the FP32 pipe).
 __device__ void conv_normalize_store(ConvSmem &m, const RelxTables &tab, int wlo, int whi, int olo, int ohi,
-                                     float2 sx, float2 sr, float *out) {
+                                     float2 sr, float *out) {
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   // prefix sums of xs at every kPre-th bin
   {
@@ -172,12 +183,14 @@ __device__ void conv_normalize_store(ConvSmem &m, const RelxTables &tab, int wlo
   }
   const float2 scf = block_sum_ff<kConvThreads>(part, m.red);
   if (tid == 0) {
-    const double sc = ff_to_double(scf) / (double) tab.conv_cf[blo];
-    m.bc[1] = (float) (ff_to_double(sr) * ff_to_double(sx) / sc);
+    const float2 sxw = ff_add(prefix_at(m, blo + L), ff_neg(prefix_at(m, blo)));  // band sum of xs
+    m.bc[1] = (float) (ff_to_double(sr) * ff_to_double(sxw) / ff_to_double(scf));
   }
   __syncthreads();
   const float norm = m.bc[1];
   if (olo > ohi) return;
+  const int olo_out = olo;
+  olo -= (olo + p - wlo) & 3;  // tiles start where the xs loads of conv_tile are 16-byte aligned
   // work items: (16-bin output tile, window segment).  The window is split into S (a power of two)
   // segments so that narrow output ranges still occupy every thread; the S partials of a tile sit
   // in adjacent lanes and are added by a fixed shuffle tree, so the result depends only on this
@@ -210,7 +223,7 @@ __device__ void conv_normalize_store(ConvSmem &m, const RelxTables &tab, int wlo
 #pragma unroll
       for (int r = 0; r < kConvR; r++) {
         const int k = olo + t * kConvR + r;
-        if (k <= ohi) out[k] = y[r] / tab.conv_cf[k] * norm;
+        if (k >= olo_out && k <= ohi) out[k] = y[r] * __frcp_rn(tab.conv_cf[k]) * norm;
       }
     }
   }
@@ -273,7 +286,6 @@ __global__ void __launch_bounds__(kConvThreads) conv_zone_kernel(RelxTables tab,
   }
   const float *xs_src = staged ? m.xz : xz;
   // xillver spectrum of the zone rebinned onto the conv grid (_rebin_spectrum, relutility.c:549-601)
-  float2 px = make_float2(0.0f, 0.0f);
   for (int j = tid; j < kN; j += kConvThreads) {
     const int4 rb = tab.rb_pack[j];  // first and last xillver bin, end fractions
     const int i0 = rb.x, i1 = rb.y;
@@ -287,12 +299,10 @@ __global__ void __launch_bounds__(kConvThreads) conv_zone_kernel(RelxTables tab,
         for (int q = i0 + 1; q <= i1 - 1; q++) v += xs_src[q];
       }
     }
-    if (j >= tab.conv_band_lo && j <= tab.conv_band_hi) px = ff_addf(px, v);
     m.xs[skew(j)] = v * tab.conv_cf[j];
   }
   const float2 sr = block_sum_ff<kConvThreads>(pr, m.red);
-  const float2 sx = block_sum_ff<kConvThreads>(px, m.red);
-  conv_normalize_store(m, tab, wlo, whi, s.out_lo, s.out_hi, sx, sr, out);
+  conv_normalize_store(m, tab, wlo, whi, s.out_lo, s.out_hi, sr, out);
 }
 
 // relconv (relconv_kernel, Relbase.cpp:257-289): the caller's spectrum is
@@ -339,7 +349,6 @@ __global__ void __launch_bounds__(kConvThreads) relconv_conv_kernel(RelxTables t
     m.hr[i] = v;
   }
   // _rebin_spectrum(conv grid <- user grid)
-  float2 px = make_float2(0.0f, 0.0f);
   const double *ce = tab.conv_e;
   for (int j = tid; j < kN; j += kConvThreads) {
     const double elo0 = ce[j], ehi0 = ce[j + 1];
@@ -368,12 +377,10 @@ __global__ void __launch_bounds__(kConvThreads) relconv_conv_kernel(RelxTables t
         v = (float) acc;
       }
     }
-    if (j >= tab.conv_band_lo && j <= tab.conv_band_hi) px = ff_addf(px, v);
     m.xs[skew(j)] = v * tab.conv_cf[j];
   }
   const float2 sr = block_sum_ff<kConvThreads>(pr, m.red);
-  const float2 sx = block_sum_ff<kConvThreads>(px, m.red);
-  conv_normalize_store(m, tab, wlo, whi, s.out_lo, s.out_hi, sx, sr, out);
+  conv_normalize_store(m, tab, wlo, whi, s.out_lo, s.out_hi, sr, out);
 }
 
 // _rebin_spectrum (relutility.c:549-601) of one output bin from the conv grid; the bin indices
