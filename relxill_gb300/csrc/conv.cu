@@ -25,6 +25,7 @@ constexpr int kConvD = 16;         // window bins per step of the register tile
 constexpr int kN = RELX_NCONV;
 constexpr int kPre = 4;            // prefix sums are kept at every kPre-th bin
 constexpr int kXStage = 3072;      // xillver bins staged in shared memory (larger tables read global memory)
+constexpr int kTsumStage = 256;    // (tile, zone) profile sums staged in shared memory at once        // conv bins per thread whose rebin map entries are loaded together
 static_assert(kN % (kConvThreads * kPre) == 0, "scan tiling");
 
 // xs is stored in rows of 16 bins, each followed by 4 padding floats: the 16-byte loads of the
@@ -38,7 +39,9 @@ struct ConvSmem {
   float2 wsum[kConvThreads / 32];
   double dred[kConvThreads / 32 + 2];
   double zsum[RELX_NZMAX];
+  double tz[kTsumStage];       // the set's per-(tile, zone) profile sums
   float bc[2];                 // broadcast scalars
+  float2 sxw;                  // band sum of xs
   int abort_flag;
   uint64_t bar;                // completion of the bulk copy of the zone's xillver spectrum
   union {                      // the staged spectrum is read before the prefix sums are formed
@@ -89,23 +92,34 @@ __device__ __forceinline__ void conv_tile(const ConvSmem &m, int k0, int p, int 
 __device__ void profile_sums(ConvSmem &m, const RelxSetState &s, const double *tsum, int set, int ntile_max, int nza,
                              int tile_bins) {
   const int tid = threadIdx.x;
+  const int ntiles = (s.win_hi - s.win_lo + tile_bins - 1) / tile_bins;
+  const bool staged = ntiles * s.nz <= kTsumStage;
+  if (staged) {  // every (tile, zone) sum loaded at once
+    for (int q = tid; q < ntiles * s.nz; q += kConvThreads) {
+      const int t = q / s.nz, z = q - t * s.nz;
+      m.tz[q] = tsum[((size_t) set * ntile_max + t) * nza + z];
+    }
+    __syncthreads();
+  }
   if (tid < 32) {
-    const int ntiles = (s.win_hi - s.win_lo + tile_bins - 1) / tile_bins;
     for (int z = tid; z < s.nz; z += 32) {
       double zs = 0.0;
-      for (int t = 0; t < ntiles; t++) zs += tsum[((size_t) set * ntile_max + t) * nza + z];
+      for (int t = 0; t < ntiles; t++) zs += staged ? m.tz[t * s.nz + z] : tsum[((size_t) set * ntile_max + t) * nza + z];
       m.zsum[z] = zs;
     }
-    __syncwarp();
-    if (tid == 0) {
-      double scale = 1.0;
-      if (s.relline_norm > 0.0) {
+    if (s.relline_norm > 0.0) {  // renormalised profile: the zones' total in zone order, then each zone scaled
+      __syncwarp();
+      double scale = 0.0;
+      if (tid == 0) {
         double sum = 0.0;
         for (int z = 0; z < s.nz; z++) sum += m.zsum[z];
         scale = s.relline_norm / sum;
+        m.bc[0] = (float) scale;
       }
-      for (int z = 0; z < s.nz; z++) m.zsum[z] *= scale;
-      m.bc[0] = (float) scale;
+      scale = __shfl_sync(0xffffffffu, scale, 0);
+      for (int z = tid; z < s.nz; z += 32) m.zsum[z] *= scale;
+    } else if (tid == 0) {
+      m.bc[0] = 1.0f;
     }
   }
   __syncthreads();
@@ -173,6 +187,7 @@ __device__ void conv_normalize_store(ConvSmem &m, const RelxTables &tab, int wlo
   }
   const int p = tab.conv_pos1;
   const int blo = tab.conv_band_lo, L = tab.conv_band_hi - tab.conv_band_lo + 1;
+  if (tid == 32) m.sxw = ff_add(prefix_at(m, blo + L), ff_neg(prefix_at(m, blo)));  // band sum of xs
   float2 part = make_float2(0.0f, 0.0f);
   for (int i = wlo + tid; i < whi; i += kConvThreads) {
     const int a = (blo + p - i) & (kN - 1);
@@ -182,10 +197,7 @@ __device__ void conv_normalize_store(ConvSmem &m, const RelxTables &tab, int wlo
     part = ff_add(part, ff_mulf(ws, m.hr[i - wlo]));
   }
   const float2 scf = block_sum_ff<kConvThreads>(part, m.red);
-  if (tid == 0) {
-    const float2 sxw = ff_add(prefix_at(m, blo + L), ff_neg(prefix_at(m, blo)));  // band sum of xs
-    m.bc[1] = (float) (ff_to_double(sr) * ff_to_double(sxw) / ff_to_double(scf));
-  }
+  if (tid == 0) m.bc[1] = ff_div_to_float(ff_mul(sr, m.sxw), scf);  // the barrier of block_sum_ff orders m.sxw
   __syncthreads();
   const float norm = m.bc[1];
   if (olo > ohi) return;
@@ -249,16 +261,17 @@ __global__ void __launch_bounds__(kConvThreads) conv_zone_kernel(RelxTables tab,
   const int wlo = s.zw_lo[z], whi = s.zw_hi[z];  // the zone's profile is zero outside
   const float fscale = m.bc[0];
   const float *pz = prof + ((size_t) set * nza + z) * kN;
-  // the zone's xillver spectrum: one bulk copy into shared memory, overlapped with the profile loads
-  const float *xz = xill + ((size_t) set * nza + z) * tab.x_nener_pad;
-  // bulk copies need 16-byte aligned rows of a 16-byte multiple (the loader pads rows to 4 floats)
-  const bool staged = tab.x_nener_pad <= kXStage && (tab.x_nener_pad & 3) == 0 && (((uintptr_t) xz) & 15) == 0;
+  // the zone's xillver spectrum on the conv grid (x E/dE): one bulk copy into shared memory,
+  // overlapped with the profile loads
+  const float *xz = xill + ((size_t) set * nza + z) * tab.x_cpad;
+  // bulk copies need 16-byte aligned rows of a 16-byte multiple (rows are padded to 4 floats)
+  const bool staged = tab.x_cpad <= kXStage && (tab.x_cpad & 3) == 0 && (((uintptr_t) xz) & 15) == 0;
   if (staged && tid == 0) {
     m.abort_flag = 0;
     mbar_init(&m.bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    mbar_expect_tx(&m.bar, (uint32_t) tab.x_nener_pad * 4u);
-    bulk_g2s(m.xz, xz, (uint32_t) tab.x_nener_pad * 4u, &m.bar);
+    mbar_expect_tx(&m.bar, (uint32_t) tab.x_cpad * 4u);
+    bulk_g2s(m.xz, xz, (uint32_t) tab.x_cpad * 4u, &m.bar);
   }
   // relline profile weighted by E/dE over its window; band sum of the profile
   float2 pr = make_float2(0.0f, 0.0f);
@@ -285,21 +298,12 @@ __global__ void __launch_bounds__(kConvThreads) conv_zone_kernel(RelxTables tab,
     }
   }
   const float *xs_src = staged ? m.xz : xz;
-  // xillver spectrum of the zone rebinned onto the conv grid (_rebin_spectrum, relutility.c:549-601)
+  // the zone's spectrum, already rebinned onto the conv grid and weighted by E/dE (the table rows
+  // are, and the zone spectrum is linear in them): bins outside the table's reach are zero
+  const int clo = tab.x_clo, cn = tab.x_cn;
   for (int j = tid; j < kN; j += kConvThreads) {
-    const int4 rb = tab.rb_pack[j];  // first and last xillver bin, end fractions
-    const int i0 = rb.x, i1 = rb.y;
-    float v = 0.0f;
-    if (i0 >= 0) {
-      const float fmin = __int_as_float(rb.z), fmax = __int_as_float(rb.w);
-      if (i0 == i1) {
-        v = fmin * xs_src[i0];
-      } else {
-        v = xs_src[i0] * fmin + xs_src[i1] * fmax;
-        for (int q = i0 + 1; q <= i1 - 1; q++) v += xs_src[q];
-      }
-    }
-    m.xs[skew(j)] = v * tab.conv_cf[j];
+    const int q = j - clo;
+    m.xs[skew(j)] = (q >= 0 && q < cn) ? xs_src[q] : 0.0f;
   }
   const float2 sr = block_sum_ff<kConvThreads>(pr, m.red);
   conv_normalize_store(m, tab, wlo, whi, s.out_lo, s.out_hi, sr, out);

@@ -216,7 +216,7 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
                                      : "relx_eval_one_noalloc: tables not loaded (call relx_init first)");
   NOALLOC_CUDA(cudaGetDevice(&dev));
   if (dev != tab_dev) return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: the tables live on another device");
-  if ((relx_is_relxill(kind) || kind == RELX_XILLVER) && tab.x_nener_pad > kMaxXillBins)
+  if ((relx_is_relxill(kind) && tab.x_cpad > kMaxXillBins) || (kind == RELX_XILLVER && tab.x_nener_pad > kMaxXillBins))
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: xillver table has more energy bins than the scratch holds");
   int nzones_env = 0, flags = 0;
   int nza = runtime_zones(model, ion_grad_type, &nzones_env, &flags);
@@ -230,7 +230,7 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
   int st = scratch_for_device(dev, &base);
   if (st) return st;
   NoallocPtrs p;
-  if (carve(base, model, nza, n_bins, ntile_max, tab.x_nener_pad, &p) > kScratchBytes)
+  if (carve(base, model, nza, n_bins, ntile_max, tab.x_cpad, &p) > kScratchBytes)
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: request exceeds the static scratch");
 
   noalloc_pack_kernel<<<1, 32, 0, s>>>(runtime_nparams(model), d_params, n_bins, ion_grad_type, iongrad_index,

@@ -107,6 +107,10 @@ struct RelxTables {
   int x_maxvals;
   const float *x_spec;       // [rows][x_nener_pad], each row divided by 10^logXi of its grid point
   int64_t x_rows;
+  // the same rows rebinned onto the conv grid and weighted by E/dE of the conv bin (the form the
+  // convolution reads): conv bins [x_clo, x_clo + x_cn), rows of x_cpad floats (a multiple of 4)
+  const float *x_cspec;
+  int x_clo, x_cn, x_cpad;
   // conv grid and precomputed maps
   const double *conv_e;      // [RELX_NCONV+1]
   const float2 *conv_eff;    // float-float edges

@@ -284,6 +284,12 @@ __device__ __forceinline__ bool ff_ge(float2 a, float2 b) {
   return d.x > 0.0f || (d.x == 0.0f && d.y >= 0.0f);
 }
 
+// a / b rounded to float from float-float operands (one correction step of the float quotient)
+__device__ __forceinline__ float ff_div_to_float(float2 a, float2 b) {
+  const float q1 = a.x / b.x;
+  const float2 r = ff_add(a, ff_neg(ff_mulf(b, q1)));  // a - q1 b
+  return q1 + r.x / b.x;
+}
 __device__ __forceinline__ float2 ff_addf(float2 a, float b) {
   float2 s = two_sum(a.x, b);
   return qts(s.x, __fadd_rn(s.y, a.y));

@@ -62,6 +62,9 @@ struct XillIngest {
   unsigned long long *bad;  // count of values that are not finite
 };
 cudaError_t launch_xill_ingest(cudaStream_t s, const XillIngest &g, const unsigned char *raw, int64_t row0, int nrows);
+// every table row rebinned onto the conv bins [clo, clo + cn) and weighted by cf, rows of cpad floats
+cudaError_t launch_xill_conv_rows(cudaStream_t s, const float *spec, int pitch, int64_t rows, const int4 *rb_pack,
+                                  const float *cf, int clo, int cn, int cpad, float *out);
 cudaError_t launch_xill_corner_flux(cudaStream_t s, const double *rowflux, const double *incl_w, int n_incl,
                                     int64_t n_corners, double *fcorr);
 

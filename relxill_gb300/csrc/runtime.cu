@@ -223,9 +223,10 @@ struct Tables {
   DevBuf lp_a, lp_h, lp_rad, lp_intens, lp_del, lp_delinc;
   // one xillver table: the standard one (x) and the nthcomp one of the Cp models (xcp)
   struct XillBufs {
-    DevBuf vals, spec, e, ew, fcorr, rb_imin, rb_imax, rb_fmin, rb_fmax, rb_pack;
+    DevBuf vals, spec, e, ew, fcorr, rb_imin, rb_imax, rb_fmin, rb_fmax, rb_pack, cspec;
     void release() {
-      for (DevBuf *b : {&vals, &spec, &e, &ew, &fcorr, &rb_imin, &rb_imax, &rb_fmin, &rb_fmax, &rb_pack}) b->release();
+      for (DevBuf *b : {&vals, &spec, &e, &ew, &fcorr, &rb_imin, &rb_imax, &rb_fmin, &rb_fmax, &rb_pack, &cspec})
+        b->release();
     }
   } x, xcp;
   RelxTables dcp{};     // d with the xillver fields of the nthcomp table (valid if has_cp)
@@ -704,7 +705,7 @@ static int load_tables(const std::string &dir, Tables &T) {
     ct[b] = make_float4(hi, (float) (co[b + 1] - co[b]), in_band ? hi : 0.0f, in_band ? (float) (em - (double) hi) : 0.0f);
   }
   // rebin map xillver grid -> conv grid, per xillver table
-  auto rebin_tables = [&](const std::vector<double> &xg, Tables::XillBufs &X, RelxTables &d) {
+  auto rebin_tables = [&](const std::vector<double> &xg, Tables::XillBufs &X, RelxTables &d) -> int {
     std::vector<int> imn, imx;
     std::vector<float> fmn, fmx;
     rebin_map(ce, xg, imn, imx, fmn, fmx);
@@ -724,6 +725,17 @@ static int load_tables(const std::string &dir, Tables &T) {
     d.rb_fmin = X.rb_fmin.as<float>();
     d.rb_fmax = X.rb_fmax.as<float>();
     d.rb_pack = X.rb_pack.as<int4>();
+    // the conv bins the table reaches: its rows on the conv grid are kept for these only
+    int clo = -1, chi = -1;
+    for (size_t j = 0; j < imn.size(); j++)
+      if (imn[j] >= 0) { if (clo < 0) clo = (int) j; chi = (int) j; }
+    if (clo < 0) {
+      g_errmsg = "xillver table: its energy grid does not overlap the convolution grid";
+      return RELX_ERR_TABLE;
+    }
+    d.x_clo = clo;
+    d.x_cn = chi + 1 - clo;
+    d.x_cpad = (d.x_cn + 3) & ~3;
     return 0;
   };
   if ((st = rebin_tables(xe, T.x, T.d)) || (has_cp && (st = rebin_tables(xe_cp, T.xcp, T.dcp)))) return st;
@@ -743,6 +755,18 @@ static int load_tables(const std::string &dir, Tables &T) {
   T.d.conv_band_hi = band_hi;
   T.d.coarse_e = T.coarse_e.as<double>();
   T.d.coarse_t = T.coarse_t.as<float4>();
+  // the table rows on the conv grid, weighted by E/dE (the convolution's input)
+  auto conv_rows = [&](Tables::XillBufs &X, RelxTables &d) -> int {
+    int r;
+    if ((r = X.cspec.reserve(sizeof(float) * (size_t) d.x_rows * d.x_cpad))) return r;
+    RELX_CUDA(launch_xill_conv_rows(nullptr, d.x_spec, d.x_nener_pad, d.x_rows, d.rb_pack, T.d.conv_cf, d.x_clo,
+                                    d.x_cn, d.x_cpad, X.cspec.as<float>()));
+    RELX_CUDA(cudaDeviceSynchronize());
+    d.x_cspec = X.cspec.as<float>();
+    T.bytes_total += (size_t) d.x_rows * d.x_cpad * 4;
+    return 0;
+  };
+  if ((st = conv_rows(T.x, T.d)) || (has_cp && (st = conv_rows(T.xcp, T.dcp)))) return st;
   {  // the nthcomp photon grid of the Cp models
     std::vector<NthGrid> g(1);
     if ((st = nth_grid_build(co, RELX_EMIN_NORM, RELX_EMAX_NORM, g[0])) || (st = upload(T.nth_grid, g))) return st;
@@ -763,6 +787,7 @@ static int load_tables(const std::string &dir, Tables &T) {
     c.x_ew = x.x_ew;
     c.x_fcorr = x.x_fcorr;
     c.rb_imin = x.rb_imin; c.rb_imax = x.rb_imax; c.rb_fmin = x.rb_fmin; c.rb_fmax = x.rb_fmax; c.rb_pack = x.rb_pack;
+    c.x_cspec = x.x_cspec; c.x_clo = x.x_clo; c.x_cn = x.x_cn; c.x_cpad = x.x_cpad;
     T.dcp = c;
   }
   T.has_cp = has_cp;
@@ -1055,7 +1080,7 @@ static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b,
   }
   if (relx_is_relxill(kind)) {
     if ((st = W.corners.reserve(S * sizeof(RelxCorners))) || (st = W.order.reserve(S * sizeof(int))) ||
-        (st = W.xill.reserve(S * nza * (size_t) std::max(T.d.x_nener_pad, T.dcp.x_nener_pad) * sizeof(float))))
+        (st = W.xill.reserve(S * nza * (size_t) std::max(T.d.x_cpad, T.dcp.x_cpad) * sizeof(float))))
       return st;
     if (need_zone_corners && (st = W.zcorners.reserve(S * sizeof(RelxZoneCorners)))) return st;
   }
@@ -1100,7 +1125,7 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   float *prof = conv_grid ? W.prof.as<float>() + (size_t) base * nza * RELX_NCONV : W.prof.as<float>();
   float *dist = W.dist.as<float>() + (size_t) base * nza * RELX_MAX_INCL;
   double *tsum = W.tsum.as<double>() + (size_t) base * b.nblk * nza;
-  float *xill = W.xill.p ? W.xill.as<float>() + (size_t) base * nza * tab.x_nener_pad : nullptr;
+  float *xill = W.xill.p ? W.xill.as<float>() + (size_t) base * nza * tab.x_cpad : nullptr;
   float *cout = W.cout.p ? W.cout.as<float>() + (size_t) base * nza * RELX_NCONV : nullptr;
   int *sflag = W.sflag.as<int>() + base;
   double *flux = W.flux.as<double>() - base;  // kernels address set i at e_off(i) - i

@@ -17,7 +17,11 @@
 //    linear map with coefficients pfz_coef; Xillspec.cpp:132-160, 457-495),
 //  * and counts values that are not finite (table validation).
 // A second kernel averages the row integrals over the inclinations of each
-// corner with the reference's inclination weights.
+// corner with the reference's inclination weights.  A third writes every row
+// rebinned onto the conv grid (_rebin_spectrum, relutility.c:549-601, in FP64)
+// and weighted by E/dE of the conv bin, the form the convolution reads: the
+// interpolation of the zone spectra and the weighting are linear, so the
+// zones' spectra then arrive on the conv grid directly.
 #include "relx_device.cuh"
 #include "relx_kernels.h"
 
@@ -101,6 +105,41 @@ cudaError_t launch_xill_corner_flux(cudaStream_t s, const double *rowflux, const
   if (n_corners <= 0) return cudaSuccess;
   xill_corner_flux_kernel<<<(unsigned) ((n_corners + 127) / 128), 128, 0, s>>>(rowflux, incl_w, n_incl, n_corners,
                                                                              fcorr);
+  return cudaGetLastError();
+}
+
+// one CTA per table row
+__global__ void __launch_bounds__(kIngestThreads) xill_conv_rows_kernel(const float *__restrict__ spec, int pitch,
+                                                                     const int4 *__restrict__ rb_pack,
+                                                                     const float *__restrict__ cf, int clo, int cn,
+                                                                     int cpad, float *__restrict__ out) {
+  const float *x = spec + (size_t) blockIdx.x * pitch;
+  float *o = out + (size_t) blockIdx.x * cpad;
+  for (int q = threadIdx.x; q < cpad; q += kIngestThreads) {
+    float v = 0.0f;
+    if (q < cn) {
+      const int4 rb = rb_pack[clo + q];  // first and last xillver bin, end fractions
+      const int i0 = rb.x, i1 = rb.y;
+      double a = 0.0;
+      if (i0 >= 0) {
+        const double fmin = __int_as_float(rb.z), fmax = __int_as_float(rb.w);
+        if (i0 == i1) {
+          a = fmin * x[i0];
+        } else {
+          a = x[i0] * fmin + x[i1] * fmax;
+          for (int k = i0 + 1; k <= i1 - 1; k++) a += x[k];
+        }
+      }
+      v = (float) (a * (double) cf[clo + q]);
+    }
+    o[q] = v;
+  }
+}
+
+cudaError_t launch_xill_conv_rows(cudaStream_t s, const float *spec, int pitch, int64_t rows, const int4 *rb_pack,
+                                  const float *cf, int clo, int cn, int cpad, float *out) {
+  if (rows <= 0) return cudaSuccess;
+  xill_conv_rows_kernel<<<(unsigned) rows, kIngestThreads, 0, s>>>(spec, pitch, rb_pack, cf, clo, cn, cpad, out);
   return cudaGetLastError();
 }
 

@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(kXillThreads, 3) xillver_dense_kernel(RelxTabl
   constexpr int NIU = NI > 0 ? NI : RELX_MAX_INCL;
   const int tid = threadIdx.x;
   const int nz = s.nz, U = s.ucount, ni = NI > 0 ? NI : tab.x_nincl;
-  const int pitch = tab.x_nener_pad;
+  const int pitch = tab.x_cpad;  // table rows on the conv grid
   const int e0 = tile * kXillTile;
   if (e0 >= pitch) return;
   const int len = min(kXillTile, pitch - e0);  // multiple of 4 floats (16 bytes)
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(kXillThreads, 3) xillver_dense_kernel(RelxTabl
   auto issue = [&](int u) {
     const int st = u % kXillStages;
     mbar_expect_tx(&m.full[st], bytes_row * (uint32_t) ni);
-    const float *src = tab.x_spec + (size_t) m.row[u] * pitch + e0;
+    const float *src = tab.x_cspec + (size_t) m.row[u] * pitch + e0;
     for (int i = 0; i < ni; i++)
       bulk_g2s(&m.stage[(st * ni + i) * (kXillTile / 4)], src + (size_t) i * pitch, bytes_row, &m.full[st]);
   };
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(kXillThreads) xillver_zone_kernel(RelxTables t
   if (s.status != RELX_OK || s.model < RELX_RELXILL || s.xdense) return;
   const int ncz = tab.x_npar == 6 ? 32 : 16;  // corners per zone (16, or 32 for the 6-parameter table)
   __shared__ float dist[RELX_MAX_INCL];
-  const int tid = threadIdx.x, ni = tab.x_nincl, pitch = tab.x_nener_pad;
+  const int tid = threadIdx.x, ni = tab.x_nincl, pitch = tab.x_cpad;  // table rows on the conv grid
   const int e0 = tile * kXillTile;
   if (e0 >= pitch) return;
   const int len = min(kXillTile, pitch - e0);
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(kXillThreads) xillver_zone_kernel(RelxTables t
     for (int c = 0; c < ncz; c++) {
       const float wz = zcor[set].w[z][c];
       if (wz == 0.0f) continue;  // zero weight: the row adds exactly nothing
-      const float4 *src = reinterpret_cast<const float4 *>(tab.x_spec + (size_t) zcor[set].row[z][c] * pitch + e0) + q;
+      const float4 *src = reinterpret_cast<const float4 *>(tab.x_cspec + (size_t) zcor[set].row[z][c] * pitch + e0) + q;
       float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
       for (int i = 0; i < ni; i++) {
         float4 v = __ldg(src + (size_t) i * (pitch / 4));
@@ -283,7 +283,7 @@ cudaError_t xillver_set_smem(int n_incl) {
 cudaError_t launch_xillver(cudaStream_t s, const RelxTables &tab, int n_sets, int nza, bool zone, bool dense,
                            const RelxSetState *sst, const RelxCorners *cor, const RelxZoneCorners *zcor,
                            const float *dist, float *xout, int *err, const int *order) {
-  const dim3 grid((tab.x_nener_pad + kXillTile - 1) / kXillTile, n_sets);
+  const dim3 grid((tab.x_cpad + kXillTile - 1) / kXillTile, n_sets);
   if (zone) xillver_zone_kernel<<<grid, kXillThreads, 0, s>>>(tab, sst, zcor, dist, nza, xout);
   if (!dense) return cudaGetLastError();
   const int nzk = nza <= 1 ? 1 : (nza <= 10 ? 10 : 16);
