@@ -391,23 +391,25 @@ __global__ void __launch_bounds__(kConvThreads) relconv_conv_kernel(RelxTables t
 // are those of the reference's walk, found from the logarithm and exact comparisons
 __device__ __forceinline__ double rebin_bin(const RelxTables &tab, double elo0, double ehi0,
                                            const float *__restrict__ f0) {
+  // energies are positive: comparisons of their bit patterns and conversions on the integer pipes
+  // (d2f, f2d); the FP64 pipe keeps the three differences of edges
   constexpr int n0 = kN;
   const double *e0 = tab.conv_e;
-  if (!(e0[0] <= ehi0 && e0[n0] >= elo0)) return 0.0;
+  if (!(dge(ehi0, e0[0]) && dge(e0[n0], elo0))) return 0.0;
   const int imin = conv_index(tab, elo0);
   const int imax = conv_index(tab, ehi0);
-  const double elo = elo0 < e0[imin] ? e0[imin] : elo0;
-  const double ehi = ehi0 > e0[imax + 1] ? e0[imax + 1] : ehi0;
+  const double elo = dgt(e0[imin], elo0) ? e0[imin] : elo0;
+  const double ehi = dgt(ehi0, e0[imax + 1]) ? e0[imax + 1] : ehi0;
   // bin widths of the conv grid as floats, (float) (e0[k + 1] - e0[k])
   if (imax == imin) {
-    float fr = (float) (ehi - elo) / tab.conv_cw[imin].y;
-    return (double) (fr * f0[imin]);
+    float fr = d2f(ehi - elo) / tab.conv_cw[imin].y;
+    return f2d(fr * f0[imin]);
   }
-  float dmin = (float) (e0[imin + 1] - elo) / tab.conv_cw[imin].y;
-  float dmax = (float) (ehi - e0[imax]) / tab.conv_cw[imax].y;
+  float dmin = d2f(e0[imin + 1] - elo) / tab.conv_cw[imin].y;
+  float dmax = d2f(ehi - e0[imax]) / tab.conv_cw[imax].y;
   float acc = f0[imin] * dmin + f0[imax] * dmax;
   for (int q = imin + 1; q <= imax - 1; q++) acc += f0[q];
-  return (double) acc;
+  return f2d(acc);
 }
 
 struct FinSmem {
