@@ -36,6 +36,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "relxilllp spectra/s batched vs plain GPU at ≤1e-4 rel err; serve p50/p99 ms"
 N_SETS = 4096
+LINE_DRAM_BYTES_4096 = 384.7e6 + 472.0e6  # line kernel, one launch over the 4096-set workload (ncu)
 WORKLOAD = ("relxilllp batched, 4096 sets per GPU, per-set grids 300-5000 log bins 0.3-80 keV, "
             "10 radial zones")
 N_PROF = 9  # kernel kinds of the per-kernel event profiler (relx_profile_name)
@@ -512,7 +513,7 @@ def run_gpu(args):
         step()
     torch.cuda.synchronize()
     assert int((d_status != 0).sum()) == 0, "sets failed"
-    st6 = (ctypes.c_int64 * 3)()
+    st6 = (ctypes.c_int64 * 5)()
     L.relx_batch_stats(S, st6)
 
     # timed region: the production path (autotuned tiles, the step replayed as a CUDA graph)
@@ -657,14 +658,20 @@ def run_gpu(args):
                      "algorithmic_flops": flops, "evals_per_set": evals_per_set,
                      "flops_per_eval": FLOPS_PER_EVAL})
         roof["frac"] = roof["achieved"] / roof["peak"]
+    # DRAM bytes (read + write) of one line-kernel launch over the 4096-set workload (512-bin tiles), from
+    # the one-pass ncu capture in the profiles folder (dram_traffic_relxilllp_4096sets.md); other batch
+    # sizes are scaled by their set count
+    roof["traffic"] = LINE_DRAM_BYTES_4096 * S / 4096
+    roof["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum, 4096-set launch, scaled by sets"
     ng, nr_tab = 40, 100
     line_bytes = S * (4 * nr_tab * ng * 16 + 1000 * 64) + int(st6[2]) * int(st6[1] // max(S, 1) or 1) * 4
     roof["hbm_term"] = {"algorithmic_bytes": line_bytes, "achieved_gbs": line_bytes / (line_ms * 1e-3) / 1e9,
                         "peak_gbs": hbm_peak, "frac": line_bytes / (line_ms * 1e-3) / 1e9 / hbm_peak}
-    x_pad = 3000
+    x_pad = int(st6[3])  # floats per table row on the convolution grid
     ucount = int(st6[0])
     nz_sum = int(st6[1])
-    # algorithmic bytes of the xillver kernel per launch: unique corner rows x incl x energies (read) + zone spectra (write)
+    # algorithmic bytes of the xillver kernel per launch: unique corner rows x incl x conv-grid bins (read) + zone
+    # spectra (write)
     xill_bytes = ucount * 10 * x_pad * 4 + nz_sum * x_pad * 4
     xill_ms = per["xillver"][0]
     xill_roof = {"kernel": "xillver", "bound": "l2", "achieved": xill_bytes / (xill_ms * 1e-3) / 1e9,

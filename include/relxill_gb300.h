@@ -216,7 +216,10 @@ const char *relx_profile_name(int k);
 /* number of kernel launches issued by the library since load */
 int64_t relx_launch_count(void);
 /* statistics of the last batch of n_sets sets: out[0] de-duplicated xillver
- * corners, out[1] radial zones, out[2] line-profile window bins (sums) */
+ * corners, out[1] radial zones, out[2] line-profile window bins (sums);
+ * out[3] floats per xillver table row on the convolution grid (the rows the
+ * relxill models read), out[4] floats per row on the table's own grid; out
+ * holds 5 values */
 int relx_batch_stats(int n_sets, int64_t *out);
 /* the FP32 FMA rate of the current device in GFLOP/s (2 FLOPs per FMA), timed
  * with CUDA events over a kernel of independent FMA chains on every SM: the

@@ -1873,6 +1873,8 @@ int relx_batch_stats(int n_sets, int64_t *out) {
   RELX_CUDA(cudaStreamSynchronize(C.stream));
   RELX_CUDA(cudaMemcpy(st.data(), C.W.st.p, sizeof(RelxSetState) * n_sets, cudaMemcpyDeviceToHost));
   out[0] = out[1] = out[2] = 0;
+  out[3] = C.T.d.x_cpad;
+  out[4] = C.T.d.x_nener_pad;
   for (auto &x : st) {
     if (x.status) continue;
     out[0] += x.ucount;
