@@ -293,9 +293,11 @@ def cache_stats() -> Dict[str, int]:
 class Server:
     """Serving engine (relx_serve_*): continuous batching of single-spectrum requests.
 
-    The energy grid, the input spectrum (relconv) and the output array of a
-    request must stay alive until the request completes; `submit` keeps
-    references to them."""
+    The HBM budget is allocated here (half per batch slot) and every batch is
+    carved from it; a request that alone needs more than half of it completes
+    with status 7.  The energy grid, the input spectrum (relconv) and the
+    output array of a request must stay alive until the request completes;
+    `submit` keeps references to them."""
 
     STATS = ("completed", "batches", "mean_batch", "p50_ms", "p99_ms", "max_ms", "waiting", "last_error")
 
