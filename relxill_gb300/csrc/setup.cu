@@ -48,6 +48,7 @@ struct SetupSmem {
     } rt;
   };
   double inv_dtab[RELX_MAX_NRTAB];
+  double dgmin_t[RELX_MAX_NRTAB], dgmax_t[RELX_MAX_NRTAB];  // gmin, gmax of table radius i less those of i + 1
   float jet_rad_f[RELX_MAX_NRADLP];
   float lp_dle[RELX_MAX_NRADLP], lp_dlr[RELX_MAX_NRADLP], lp_d[RELX_MAX_NRADLP], lp_di[RELX_MAX_NRADLP];
   float lp_e[RELX_MAX_NRADLP], inv_jr_f[RELX_MAX_NRADLP], inv_drad_f[RELX_MAX_NRADLP];
@@ -536,7 +537,11 @@ __global__ void __launch_bounds__(kSetupThreads, 4) setup_kernel(RelxTables tab,
     const double r1 = m.fg_r1, du = m.fg_du;  // 1/sqrt(rout) and the step in u
     for (int ii = tid; ii < NR; ii += kSetupThreads) {
       double u = f2d((float) ii) * du + r1;  // ii < 2^24: exact
-      double iu = __drcp_rn(u);
+      // 1/u: the float reciprocal refined by two Newton steps in FP64 (within an ulp of the
+      // correctly rounded quotient)
+      double iu = f2d(__frcp_rn(d2f(u)));
+      iu = fma(iu, fma(-u, iu, 1.0), iu);
+      iu = fma(iu, fma(-u, iu, 1.0), iu);
       m.re[ii] = iu * iu;
       m.sqre[ii] = iu;
     }
@@ -551,7 +556,11 @@ __global__ void __launch_bounds__(kSetupThreads, 4) setup_kernel(RelxTables tab,
     if (m.re_tab[m.ind_rmax] < 1000.0 && m.re_tab[m.ind_rmax] * 1.01 > 1000.0) m.re_tab[m.ind_rmax] = 1000.0;
   }
   __syncthreads();
-  for (int i = tid; i < nr - 1; i += kSetupThreads) m.inv_dtab[i] = 1.0 / (m.re_tab[i] - m.re_tab[i + 1]);
+  for (int i = tid; i < nr - 1; i += kSetupThreads) {
+    m.inv_dtab[i] = 1.0 / (m.re_tab[i] - m.re_tab[i + 1]);
+    m.dgmin_t[i] = m.gmin_t[i] - m.gmin_t[i + 1];  // the interpolation below as lo + f (hi - lo)
+    m.dgmax_t[i] = m.gmax_t[i] - m.gmax_t[i + 1];
+  }
   __syncthreads();
 
   RelxRadial &R = rout[set];
@@ -575,8 +584,9 @@ __global__ void __launch_bounds__(kSetupThreads, 4) setup_kernel(RelxTables tab,
     if (ind < 0) ind = 0;
     const double ifac = (r - m.re_tab[ind + 1]) * m.inv_dtab[ind];
     if (ind > 0 && dgt(ifac, 1.0)) atomicExch(&m.status, RELX_ERR_GRID);
-    const double gmn = lerp1(ifac, m.gmin_t[ind + 1], m.gmin_t[ind]);
-    const double gmx = lerp1(ifac, m.gmax_t[ind + 1], m.gmax_t[ind]);
+    // interp_lin_1d (relutility.c:24-26) as lo + f (hi - lo), one FMA each
+    const double gmn = fma(ifac, m.dgmin_t[ind], m.gmin_t[ind + 1]);
+    const double gmx = fma(ifac, m.dgmax_t[ind], m.gmax_t[ind + 1]);
     const double dg = gmx - gmn;
     R.re[ii] = r;
     R.ifac[ii] = ifac;
@@ -585,11 +595,10 @@ __global__ void __launch_bounds__(kSetupThreads, 4) setup_kernel(RelxTables tab,
     rr.gmax = ff_split(gmx);
     rr.dg = ff_split(dg);
     rr.inv_dg = 1.0f / d2f(dg);
-    {
-      const double eh = RELX_GFAC_H * dg + gmn;
-      rr.eH = ff_split(eh);
-      rr.e1H = ff_split((1 - RELX_GFAC_H) * dg + gmn);
-      rr.red_H = dge(eh, 0.95) ? 1 : 0;
+    {  // gstar2ener(H) and gstar2ener(1 - H) in float-float from the splits (FP32 pipe)
+      rr.eH = ff_add(rr.gmin, ff_mul(rr.dg, ff_split(RELX_GFAC_H)));
+      rr.e1H = ff_add(rr.gmin, ff_mul(rr.dg, ff_split(1 - RELX_GFAC_H)));
+      rr.red_H = ff_ge(rr.eH, ff_split(0.95)) ? 1 : 0;
     }
     rr.itab = (short) ind;
     rr.ifac = d2f(ifac);
@@ -732,7 +741,8 @@ __global__ void __launch_bounds__(kSetupThreads, 4) setup_kernel(RelxTables tab,
       m.pr.del_emit[ii] = del_e;
       m.pr.del_inc[ii] = inter * m.lp_di[kk + 1] + (1.0f - inter) * m.lp_di[kk];
       const double t = r * r - 3 * r + 2 * aa * sr;
-      const float ut_d = d2f(r * sr + aa) / (d2f(sr) * sqrtf(d2f(t)));
+      const float srf = d2f(sr);
+      const float ut_d = fmaf(d2f(r), srf, d2f(aa)) / (srf * sqrtf(d2f(t)));
       float gi = ut_d / ut_h;
       if (moving) gi = (float) gi_potential_lp(r, aa, hh, s.beta, f2d(del_e));
       float boost = powf(gi, gam_f);
