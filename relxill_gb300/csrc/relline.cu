@@ -687,7 +687,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, c
         for (int q = tid; q < cn; q += kLineThreads) m.re[q] = (float) R.re[c0 + q];
       }
       __syncthreads();
-      // four radii per warp: 8 lanes per radius, each lane takes table points g = sub, sub + 8, ...
+      // four radii per warp: 8 lanes per radius, each lane takes a block of consecutive table points
       const int grp = lane >> 3, sub = lane & 7;
       for (int cb = warp * 4; cb < cn; cb += kLineWarps * 4) {
         const int ci = cb + grp;
@@ -699,10 +699,12 @@ __global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, c
         const float re = m.re[ci];
         const float c = re * re * re * c4pi2 * rr.ew;
         const float dg = rr.dg.x, gmn = rr.gmin.x;
-        // consecutive table points mostly fall into the same angle bin: add runs, flush on a change
+        // consecutive table points mostly fall into the same angle bin: each lane takes a block of
+        // consecutive points, adds runs and flushes a run on a change of bin
         int cur0 = -1, cur1 = -1;
         float run0 = 0.0f, run1 = 0.0f;
-        for (int g = sub; g < ng; g += 8) {
+        const int gper = (ng + 7) >> 3, g_end = min(ng, (sub + 1) * gper);
+        for (int g = sub * gper; g < g_end; g++) {
           // trf(g*) and cosne(g*) at this radius: interp_lin_1d(ifac_r, T[ind+1], T[ind]) (Relprofile.cpp:280-293)
           const float4 lo = m.tab[(it + 1) * ng + g], hi = m.tab[it * ng + g];
           const float ge_ = m.gsf[g] * dg + gmn;
