@@ -69,6 +69,7 @@ constexpr size_t kScratchBytes =
     align_up(sizeof(float) * (size_t) RELX_NZMAX * RELX_NCONV) +                             // convolved spectra
     align_up(sizeof(double) * (RELX_NZMAX + 1)) + align_up(sizeof(NthTable)) +               // nthcomp (Cp)
     align_up(sizeof(float4) * (size_t) (RELX_NZMAX + 1) * 900) +                             // nthcomp solve
+    align_up(sizeof(float4) * (size_t) RELX_MAX_NRTAB * RELX_MAX_NG) +                      // interpolated table
     3 * kAlign;                                                                              // flags
 
 // the scratch of this entry point (about 3.8 MB)
@@ -83,12 +84,13 @@ struct NoallocPtrs {
   double *line_e, *tsum, *nthq;
   float *prof, *dist, *xill, *cout;
   NthTable *nth;
-  float4 *nthscr;
+  float4 *nthscr, *htab;
   int *sflag, *err, *status;
 };
 
 // carve the arrays of one call from the scratch; returns the bytes used
-static size_t carve(unsigned char *base, int model, int nza, int nbins, int ntile_max, int x_pad, NoallocPtrs *p) {
+static size_t carve(unsigned char *base, int model, int nza, int nbins, int ntile_max, int x_pad, int nrg,
+                    NoallocPtrs *p) {
   size_t off = 0;
   auto take = [&](size_t bytes) {
     unsigned char *q = base + off;
@@ -111,6 +113,7 @@ static size_t carve(unsigned char *base, int model, int nza, int nbins, int ntil
   p->nthq = (double *) take(cp ? sizeof(double) * (RELX_NZMAX + 1) : 0);
   p->nth = (NthTable *) take(cp ? sizeof(NthTable) : 0);
   p->nthscr = (float4 *) take(cp ? nthcomp_scratch_bytes(1, nza, relx_kind(model) == RELX_XILLVER) : 0);
+  p->htab = (float4 *) take(relx_is_relxill(relx_kind(model)) ? sizeof(float4) * (size_t) nrg : 0);
   p->sflag = (int *) take(sizeof(int));
   p->err = (int *) take(sizeof(int));
   p->status = (int *) take(sizeof(int));
@@ -230,7 +233,7 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
   int st = scratch_for_device(dev, &base);
   if (st) return st;
   NoallocPtrs p;
-  if (carve(base, model, nza, n_bins, ntile_max, tab.x_cpad, &p) > kScratchBytes)
+  if (carve(base, model, nza, n_bins, ntile_max, tab.x_cpad, tab.rel_nr * tab.rel_ng, &p) > kScratchBytes)
     return fail(RELX_ERR_ARG, "relx_eval_one_noalloc: request exceeds the static scratch");
 
   noalloc_pack_kernel<<<1, 32, 0, s>>>(runtime_nparams(model), d_params, n_bins, ion_grad_type, iongrad_index,
@@ -248,7 +251,7 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
                                                             p.cor, p.zcor);
   if (cp) NOALLOC_CUDA(launch_nthcomp(s, tab, p.sin, p.sst, 1, nza, false, p.nthq, p.nth, p.cor, p.zcor, p.nthscr, nza + 1, 0));
   NOALLOC_CUDA(launch_relline(relx_is_relxill(kind), 1, 512, ntile_max, s, tab, p.sin, p.sst, p.rad, p.line_e, nza,
-                              p.prof, p.dist, p.tsum, kind == RELX_RELLINE || kind == RELX_RELCONV, nza > 1));
+                              p.prof, p.dist, p.tsum, kind == RELX_RELLINE || kind == RELX_RELCONV, nza > 1, p.htab));
   if (relx_is_relxill(kind)) {
     NOALLOC_CUDA(launch_xillver(s, tab, 1, nza, nza > RELX_ZDENSE || cp, true, p.sst, p.cor, p.zcor, p.dist, p.xill,
                                 p.err, nullptr));

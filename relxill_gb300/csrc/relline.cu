@@ -27,6 +27,7 @@
 //  * The tile is a launch argument, not a template parameter: every tile size
 //    runs the same machine code, so a bin is the same number whatever the tile.
 #include "relx_device.cuh"
+#include "relx_kernels.h"
 
 namespace relx {
 
@@ -609,7 +610,10 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
 }
 
 // ---------------------------------------------------------------------------
-// emission-angle distribution per zone (Relprofile.cpp:908-938), one CTA per set
+// emission-angle distribution per zone (Relprofile.cpp:908-938), one CTA per set.  The set's
+// (a, mu0)-interpolated transfer functions and emission-angle cosines on all table radii are
+// written once per set by hist_table_kernel and read through the read-only cache, so that the
+// histogram CTA's shared memory stays small (four CTAs per SM).
 // ---------------------------------------------------------------------------
 struct HistSmem {
   RelxRadRec rec[kChunk];    // radius records of the current chunk
@@ -618,8 +622,28 @@ struct HistSmem {
   float hist[kLineWarps][RELX_MAX_INCL];
   float gfac[RELX_MAX_NG];   // d_gstar / sqrt(g*(1-g*))
   float gsf[RELX_MAX_NG];
-  float4 tab[1];             // (a, mu0)-interpolated table [n_r][n_g], dynamic tail
 };
+
+// interpol_a_mu0 (Relprofile.cpp:39-80) of (trff1, trff2, cosne1, cosne2) at every (table radius,
+// g*) of a set: grid (chunks of kLineThreads entries, sets)
+__global__ void __launch_bounds__(kLineThreads) hist_table_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
+                                                                  float4 *__restrict__ htab) {
+  const int set = blockIdx.y;
+  const RelxSetState &s = sst[set];
+  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.cached) return;
+  const int nr = tab.rel_nr, nm = tab.rel_nmu0, ng = tab.rel_ng;
+  const int q = blockIdx.x * kLineThreads + threadIdx.x;
+  if (q >= nr * ng) return;
+  const size_t b00 = (size_t) s.ind_a * nm + s.ind_mu0, b10 = (size_t) (s.ind_a + 1) * nm + s.ind_mu0;
+  const size_t b01 = b00 + 1, b11 = b10 + 1;
+  const float f1 = s.ifac_a, f2 = s.ifac_mu0;
+  const float w00 = (1.0f - f1) * (1.0f - f2), w10 = f1 * (1.0f - f2), w01 = (1.0f - f1) * f2, w11 = f1 * f2;
+  const float4 a = __ldg(&tab.rel_tc[b00 * nr * ng + q]), b = __ldg(&tab.rel_tc[b10 * nr * ng + q]);
+  const float4 c = __ldg(&tab.rel_tc[b01 * nr * ng + q]), d = __ldg(&tab.rel_tc[b11 * nr * ng + q]);
+  htab[(size_t) set * nr * ng + q] =
+      make_float4(w00 * a.x + w10 * b.x + w01 * c.x + w11 * d.x, w00 * a.y + w10 * b.y + w01 * c.y + w11 * d.y,
+                  w00 * a.z + w10 * b.z + w01 * c.z + w11 * d.z, w00 * a.w + w10 * b.w + w01 * c.w + w11 * d.w);
+}
 static_assert(offsetof(HistSmem, rec) % 16 == 0, "radius records are staged as int4 rows");
 
 // FP64 emission-angle cosine of one fine radius, table point g, branch k
@@ -639,9 +663,9 @@ __device__ double cosne_fp64(const RelxTables &tab, const RelxSetState &s, int i
   return lerp1(ifac, v[0], v[1]);
 }
 
-__global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
+__global__ void __launch_bounds__(kLineThreads, 4) hist_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
                                                             const RelxRadial *__restrict__ srad, int nza,
-                                                            float *__restrict__ dist) {
+                                                            const float4 *__restrict__ htab, float *__restrict__ dist) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   HistSmem &m = *reinterpret_cast<HistSmem *>(smem_raw);
   const int set = blockIdx.x;
@@ -649,18 +673,9 @@ __global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, c
   if (s.status != RELX_OK || s.model < RELX_RELXILL || s.cached || (int) blockIdx.y >= s.nz) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const RelxRadial &R = srad[set];
-  const int nr = tab.rel_nr, nm = tab.rel_nmu0, ng = tab.rel_ng, n_incl = tab.x_nincl;
+  const int nr = tab.rel_nr, ng = tab.rel_ng, n_incl = tab.x_nincl;
+  const float4 *__restrict__ T = htab + (size_t) set * nr * ng;  // the set's interpolated table
   {
-    const size_t b00 = (size_t) s.ind_a * nm + s.ind_mu0, b10 = (size_t) (s.ind_a + 1) * nm + s.ind_mu0;
-    const size_t b01 = b00 + 1, b11 = b10 + 1;
-    const float f1 = s.ifac_a, f2 = s.ifac_mu0;
-    const float w00 = (1.0f - f1) * (1.0f - f2), w10 = f1 * (1.0f - f2), w01 = (1.0f - f1) * f2, w11 = f1 * f2;
-    for (int q = tid; q < nr * ng; q += kLineThreads) {
-      const float4 a = __ldg(&tab.rel_tc[b00 * nr * ng + q]), b = __ldg(&tab.rel_tc[b10 * nr * ng + q]);
-      const float4 c = __ldg(&tab.rel_tc[b01 * nr * ng + q]), d = __ldg(&tab.rel_tc[b11 * nr * ng + q]);
-      m.tab[q] = make_float4(w00 * a.x + w10 * b.x + w01 * c.x + w11 * d.x, w00 * a.y + w10 * b.y + w01 * c.y + w11 * d.y,
-                             w00 * a.z + w10 * b.z + w01 * c.z + w11 * d.z, w00 * a.w + w10 * b.w + w01 * c.w + w11 * d.w);
-    }
     for (int g = tid; g < ng; g += kLineThreads) {
       double gs = 5e-3 + (1.0 - 2 * 5e-3) / (ng - 1) * ((float) g);
       double gs1 = 5e-3 + (1.0 - 2 * 5e-3) / (ng - 1) * ((float) 1);
@@ -706,7 +721,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) hist_kernel(RelxTables tab, c
         const int gper = (ng + 7) >> 3, g_end = min(ng, (sub + 1) * gper);
         for (int g = sub * gper; g < g_end; g++) {
           // trf(g*) and cosne(g*) at this radius: interp_lin_1d(ifac_r, T[ind+1], T[ind]) (Relprofile.cpp:280-293)
-          const float4 lo = m.tab[(it + 1) * ng + g], hi = m.tab[it * ng + g];
+          const float4 lo = __ldg(&T[(it + 1) * ng + g]), hi = __ldg(&T[it * ng + g]);
           const float ge_ = m.gsf[g] * dg + gmn;
           const float cg = c * ge_ * ge_ * m.gfac[g];
 #pragma unroll
@@ -764,7 +779,11 @@ size_t line_smem_bytes(int nr, int ng, bool limb, int tile) {
   (void) tile;
   return limb ? line_smem_t<true>(nr, ng) : line_smem_t<false>(nr, ng);
 }
-size_t hist_smem_bytes(int nr, int ng) { return sizeof(HistSmem) + sizeof(float4) * (size_t) (nr * ng - 1); }
+size_t hist_smem_bytes(int nr, int ng) {
+  (void) nr;
+  (void) ng;
+  return sizeof(HistSmem);
+}
 
 cudaError_t relline_set_smem(int nr, int ng) {
   cudaError_t e;
@@ -781,7 +800,7 @@ cudaError_t relline_set_smem(int nr, int ng) {
 // tiles of `tile` bins (256 or 512) and, for relxill models, the emission-angle histogram
 cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream_t s, const RelxTables &tab,
                            const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
-                           int nza, float *prof, float *dist, double *tsum, bool any_limb, bool zsplit) {
+                           int nza, float *prof, float *dist, double *tsum, bool any_limb, bool zsplit, float4 *htab) {
   const int nr = tab.rel_nr, ng = tab.rel_ng;
   tile = (tile == 256) ? 256 : 512;
   const int ntile = (nblk * kSumBins + tile - 1) / tile;
@@ -791,15 +810,16 @@ cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream
   if (any_limb)
     relline_kernel<true><<<grid, kLineThreads, line_smem_t<true>(nr, ng), s>>>(tab, sin, sst, srad, line_e, nza, prof,
                                                                                tsum, nblk, tile);
-  if (hist)
-    hist_kernel<<<dim3(n_sets, zsplit ? nza : 1), kLineThreads, hist_smem_bytes(nr, ng), s>>>(tab, sst, srad, nza, dist);
+  if (hist) return launch_hist(n_sets, s, tab, sst, srad, nza, dist, zsplit, htab);
   return cudaGetLastError();
 }
 
 cudaError_t launch_hist(int n_sets, cudaStream_t s, const RelxTables &tab, const RelxSetState *sst,
-                        const RelxRadial *srad, int nza, float *dist, bool zsplit) {
+                        const RelxRadial *srad, int nza, float *dist, bool zsplit, float4 *htab) {
+  const int nq = tab.rel_nr * tab.rel_ng;
+  hist_table_kernel<<<dim3((nq + kLineThreads - 1) / kLineThreads, n_sets), kLineThreads, 0, s>>>(tab, sst, htab);
   hist_kernel<<<dim3(n_sets, zsplit ? nza : 1), kLineThreads, hist_smem_bytes(tab.rel_nr, tab.rel_ng), s>>>(
-      tab, sst, srad, nza, dist);
+      tab, sst, srad, nza, htab, dist);
   return cudaGetLastError();
 }
 

@@ -29,11 +29,12 @@ cudaError_t relline_set_smem(int nr, int ng);
 // tile: energy bins per line-kernel CTA (256 or 512); nblk: 256-bin profile-sum blocks per set
 cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream_t s, const RelxTables &tab,
                            const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
-                           int nza, float *prof, float *dist, double *tsum, bool any_limb,
-                           bool zsplit = false);
-// the emission-angle histograms alone (relxill models), for a launch on its own stream
+                           int nza, float *prof, float *dist, double *tsum, bool any_limb, bool zsplit,
+                           float4 *htab);
+// the emission-angle histograms alone (relxill models), for a launch on its own stream; htab: the
+// sets' interpolated transfer-function tables (rel_nr x rel_ng float4 per set), written here
 cudaError_t launch_hist(int n_sets, cudaStream_t s, const RelxTables &tab, const RelxSetState *sst,
-                        const RelxRadial *srad, int nza, float *dist, bool zsplit = false);
+                        const RelxRadial *srad, int nza, float *dist, bool zsplit, float4 *htab);
 
 cudaError_t xillver_set_smem(int n_incl);
 // bounded-wait self-test: writes the status of a wait that cannot complete (RELX_ERR_TIMEOUT)

@@ -841,12 +841,12 @@ static int zones_for(int model, int ion_grad_type, int envn) {
 
 struct Workspace {
   DevBuf setin, st, rad, corners, zcorners, line_e, prof, dist, tsum, xill, cout, user_e, user_f, flux, sflag,
-      status, err, params, eoff, igt, igi, order, cslot, nthq, nthtab, nthscr;
+      status, err, params, eoff, igt, igi, order, cslot, nthq, nthtab, nthscr, htab;
   Arena arena;  // set by use_arena: every buffer is carved from it
-  std::array<DevBuf *, 26> all() {
+  std::array<DevBuf *, 27> all() {
     return {&setin, &st, &rad, &corners, &zcorners, &line_e, &prof, &dist, &tsum, &xill, &cout, &user_e,
             &user_f, &flux, &sflag, &status, &err, &params, &eoff, &igt, &igi, &order, &cslot, &nthq,
-            &nthtab, &nthscr};
+            &nthtab, &nthscr, &htab};
   }
   // carve the buffers from [base, base + bytes) from now on (the workspace holds no allocation)
   void use_arena(void *base, size_t bytes) {
@@ -1080,7 +1080,8 @@ static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b,
   }
   if (relx_is_relxill(kind)) {
     if ((st = W.corners.reserve(S * sizeof(RelxCorners))) || (st = W.order.reserve(S * sizeof(int))) ||
-        (st = W.xill.reserve(S * nza * (size_t) std::max(T.d.x_cpad, T.dcp.x_cpad) * sizeof(float))))
+        (st = W.xill.reserve(S * nza * (size_t) std::max(T.d.x_cpad, T.dcp.x_cpad) * sizeof(float))) ||
+        (st = W.htab.reserve(S * (size_t) T.d.rel_nr * T.d.rel_ng * sizeof(float4))))
       return st;
     if (need_zone_corners && (st = W.zcorners.reserve(S * sizeof(RelxZoneCorners)))) return st;
   }
@@ -1179,12 +1180,13 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   {
     ProfScope ps(PK_LINE, s, 1 + (b.any_limb ? 1 : 0));
     RELX_CUDA(launch_relline(false, n, b.line_tile, b.nblk, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza,
-                             prof, dist, tsum, b.any_limb, zsplit));
+                             prof, dist, tsum, b.any_limb, zsplit, nullptr));
   }
   if (relxill) {
     {
       ProfScope ps(PK_HIST, xs);
-      RELX_CUDA(launch_hist(n, xs, tab, sst, rad, b.nza, dist, b.nza > 1 && n < 2 * 152));
+      RELX_CUDA(launch_hist(n, xs, tab, sst, rad, b.nza, dist, b.nza > 1 && n < 2 * 152,
+                            W.htab.as<float4>() + (size_t) base * tab.rel_nr * tab.rel_ng));
     }
     {
       // the zone kernel for sets with more than RELX_ZDENSE zones and for 6-parameter sets whose
@@ -1710,9 +1712,9 @@ size_t batch_device_bytes(int model, int n_sets, int64_t n_edges, int max_bins, 
   const int kind = relx_kind(model);
   const size_t S = (size_t) n_sets, E = (size_t) n_edges;
   // parameters, grid offsets and the ionisation-gradient arrays (enqueue_host_batch), and the
-  // 256-byte rounding of each of the workspace's 26 buffers
+  // 256-byte rounding of each of the workspace's 27 buffers
   const size_t staged = S * (sizeof(double) * RELX_NPARAM_MAX + sizeof(int64_t) + sizeof(int) + sizeof(double)) +
-                        sizeof(int64_t) + 26 * 256 + 256;
+                        sizeof(int64_t) + 27 * 256 + 256;
   const size_t cp = relx_is_cp(model) ? S * (sizeof(NthTable) + sizeof(double) * (RELX_NZMAX + 1)) : 0;
   if (kind == RELX_XILLVER)
     return staged + cp + S * (sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(int) * 4) + sizeof(int) +
@@ -1725,7 +1727,9 @@ size_t batch_device_bytes(int model, int n_sets, int64_t n_edges, int max_bins, 
   if (kind == RELX_RELLINE) per_edge += sizeof(double) + sizeof(float);     // line grid, profile
   else per_edge += (kind == RELX_RELCONV) ? sizeof(double) : 0;              // relconv input
   if (kind != RELX_RELLINE) per_set += 2 * sizeof(float) * (size_t) nza * RELX_NCONV;
-  if (relx_is_relxill(kind)) per_set += sizeof(RelxCorners) + sizeof(float) * (size_t) nza * 4096;
+  if (relx_is_relxill(kind))
+    per_set += sizeof(RelxCorners) + sizeof(float) * (size_t) nza * 4096 +
+               sizeof(float4) * (size_t) RELX_MAX_NRTAB * RELX_MAX_NG;  // the interpolated table of the histograms
   if (relx_is_cp(model) || nza > RELX_ZDENSE) per_set += sizeof(RelxZoneCorners);
   return staged + cp + per_set * S + per_edge * E + sizeof(int) +
          (relx_is_cp(model) ? nthcomp_scratch_bytes(n_sets, nza, false) : 0);
