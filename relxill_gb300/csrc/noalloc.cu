@@ -113,7 +113,7 @@ static size_t carve(unsigned char *base, int model, int nza, int nbins, int ntil
   p->nthq = (double *) take(cp ? sizeof(double) * (RELX_NZMAX + 1) : 0);
   p->nth = (NthTable *) take(cp ? sizeof(NthTable) : 0);
   p->nthscr = (float4 *) take(cp ? nthcomp_scratch_bytes(1, nza, relx_kind(model) == RELX_XILLVER) : 0);
-  p->htab = (float4 *) take(relx_is_relxill(relx_kind(model)) ? sizeof(float4) * (size_t) nrg : 0);
+  p->htab = (float4 *) take(relx_kind(model) != RELX_XILLVER ? sizeof(float4) * (size_t) nrg : 0);
   p->sflag = (int *) take(sizeof(int));
   p->err = (int *) take(sizeof(int));
   p->status = (int *) take(sizeof(int));
@@ -250,8 +250,9 @@ static int eval_one_noalloc(int model, const double *d_params, const double *d_e
   setup_kernel<<<1, kSetupThreadsH, setup_smem_bytes(), s>>>(tab, model, p.sin, d_energy, p.line_e, p.sst, p.rad,
                                                             p.cor, p.zcor);
   if (cp) NOALLOC_CUDA(launch_nthcomp(s, tab, p.sin, p.sst, 1, nza, false, p.nthq, p.nth, p.cor, p.zcor, p.nthscr, nza + 1, 0));
-  NOALLOC_CUDA(launch_relline(relx_is_relxill(kind), 1, 512, ntile_max, s, tab, p.sin, p.sst, p.rad, p.line_e, nza,
-                              p.prof, p.dist, p.tsum, kind == RELX_RELLINE || kind == RELX_RELCONV, nza > 1, p.htab));
+  NOALLOC_CUDA(launch_line_table(1, s, tab, p.sst, p.htab));
+  NOALLOC_CUDA(launch_relline(relx_is_relxill(kind), 1, ntile_max, s, tab, p.sin, p.sst, p.rad, p.line_e, nza, p.prof,
+                              p.dist, p.tsum, kind == RELX_RELLINE || kind == RELX_RELCONV, nza > 1, p.htab));
   if (relx_is_relxill(kind)) {
     NOALLOC_CUDA(launch_xillver(s, tab, 1, nza, nza > RELX_ZDENSE || cp, true, p.sst, p.cor, p.zcor, p.dist, p.xill,
                                 p.err, nullptr));

@@ -2,13 +2,15 @@
 // integration of every (radius, energy bin) pair and binning into radial zones
 // and the emission-angle histogram (Relprofile.cpp:39-80, 141-303, 489-958).
 //
-// Launch: one CTA per (energy-bin tile, parameter set), 8 warps.
-//  * The (a, mu0)-interpolated transfer functions of the set on all table radii
-//    are staged once in shared memory (float4 trff1, trff2, cosne1, cosne2).
+// line_table_kernel writes each set's (a, mu0)-interpolated transfer functions on
+// all table radii once (two float2 planes: trff1/trff2, cosne1/cosne2); the line
+// profile and the histogram read them through the read-only cache.
+//
+// Line profile: one CTA per (512-bin tile, parameter set), 8 warps, four CTAs per SM.
 //  * Zone by zone, warps take fine radii round robin; per radius a warp builds
-//    the radial interpolation trf(g*) (40 x float4) and its lanes integrate
-//    consecutive energy bins (Romberg with the reference's prec 0.02 /
-//    itermax 5, midpoint below 0.95 keV, sqrt edge terms within 5e-3 of
+//    the radial interpolation trf(g*) (40 points) from the set's table and its
+//    lanes integrate consecutive energy bins (Romberg with the reference's prec
+//    0.02 / itermax 5, midpoint below 0.95 keV, sqrt edge terms within 5e-3 of
 //    g* = 0 and 1).  Each warp adds into its own shared row; at the end of
 //    the zone the rows are summed in warp order: no atomics, so every bin is
 //    the same number in every run and in every batch composition.
@@ -24,8 +26,6 @@
 //    by up to about 2%).  Such bins are marked in a per-lane mask and redone
 //    after the radius's other bins by one out-of-line call, so that the bin
 //    loop holds no call (a call there makes the compiler spill its registers).
-//  * The tile is a launch argument, not a template parameter: every tile size
-//    runs the same machine code, so a bin is the same number whatever the tile.
 #include "relx_device.cuh"
 #include "relx_kernels.h"
 
@@ -40,7 +40,7 @@ constexpr float kSideBand = 2e-5f;  // grid units within which the side of a g* 
 // |obtprec - 0.02| within which a bin is integrated again in FP64: about five times the error of the
 // FP32 obtprec (the level sums carry a few ulp each, 2-5e-7 of the integral)
 constexpr float kConvBand = 2e-6f;
-constexpr int kTileMax = 512;       // energy bins per CTA at most
+constexpr int kLineTile = 512;      // energy bins per CTA
 
 // per-radius constants (warp uniform)
 struct RadC {
@@ -388,21 +388,21 @@ __device__ __forceinline__ float integ_bin(float glo, float clo, float ghi, floa
 
 
 constexpr int kChunk = 128;  // radius records staged per chunk
+static_assert(kLineTile % kSumBins == 0 && kLineTile == kLineTileH, "whole profile-sum blocks per tile");
 
 template <bool LIMB>
 struct LineSmem {
-  float acc[kLineWarps][kTileMax];
-  float2 eff[kTileMax + 1];
-  unsigned char red[kTileMax];
+  float acc[kLineWarps][kLineTile];
+  float2 eff[kLineTile + 1];
+  unsigned char red[kLineTile];
   TW<LIMB> tw[kLineWarps][RELX_MAX_NG];
   RelxRadRec rec[kChunk];
   float2 gs[RELX_MAX_NG];   // table g* points (Relprofile.cpp:104-106) as float-float
   double red_sum[kLineWarps + 1];
-  TW<LIMB> tab[1];          // (a, mu0)-interpolated table [n_r][n_g], dynamic tail
 };
 static_assert(offsetof(LineSmem<false>, rec) % 16 == 0 && offsetof(LineSmem<true>, rec) % 16 == 0,
               "radius records are staged as int4 rows");
-static_assert(kTileMax / 32 <= 32, "a lane's bins of one radius fit a 32-bit mask");
+static_assert(kLineTile / 32 <= 32, "a lane's bins of one radius fit a 32-bit mask");
 
 // the bins of one radius that romberg2 marked rare (bit i of rmask: the lane's i-th bin from jlo),
 // integrated again with FP64 Romberg and added
@@ -431,57 +431,39 @@ __device__ __forceinline__ float limb_factor(int limb, float mu) {
   return 1.0f;
 }
 
-// tbins: energy bins per CTA (256 or 512, whole 256-bin sum blocks).  tsum holds the profile sum of
-// every (256-bin block, zone), nblk blocks per set, so that the sums do not depend on the tile.
+// tsum holds the profile sum of every (256-bin block, zone), nblk blocks per set.  htab: the sets'
+// (a, mu0)-interpolated transfer functions (line_table_kernel).
 template <bool LIMB>
-__global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab, const RelxSetIn *__restrict__ sin,
-                                                                  const RelxSetState *__restrict__ sst,
-                                                                  const RelxRadial *__restrict__ srad,
-                                                                  const double *__restrict__ line_e, int nza,
-                                                                  float *__restrict__ prof, double *__restrict__ tsum,
-                                                                  int nblk, int tbins) {
+__global__ void __launch_bounds__(kLineThreads, 4) relline_kernel(
+    RelxTables tab, const RelxSetIn *__restrict__ sin, const RelxSetState *__restrict__ sst,
+    const RelxRadial *__restrict__ srad, const double *__restrict__ line_e, const float4 *__restrict__ htab, int nza,
+    float *__restrict__ prof, double *__restrict__ tsum, int nblk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   LineSmem<LIMB> &m = *reinterpret_cast<LineSmem<LIMB> *>(smem_raw);
   const int set = blockIdx.y, tile = blockIdx.x;
   const RelxSetState &s = sst[set];
   if (s.status != RELX_OK || s.cached) return;
   if ((s.limb != 0) != LIMB) return;
-  const int tlo = s.win_lo + tile * tbins;
-  const int thi = min(s.win_hi, tlo + tbins);
+  const int tlo = s.win_lo + tile * kLineTile;
+  const int thi = min(s.win_hi, tlo + kLineTile);
   if (tlo >= thi) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const RelxRadial &R = srad[set];
-  const int nr = tab.rel_nr, nm = tab.rel_nmu0, ng = tab.rel_ng;
+  const int nr = tab.rel_nr, ng = tab.rel_ng;
   const int nz = s.nz;
   if ((int) blockIdx.z >= nz) return;
   const bool is_line = (s.model == RELX_RELLINE);
   const double *ge = is_line ? (line_e + sin[set].e_off) : tab.conv_e;
   const size_t pbase = is_line ? (size_t) sin[set].e_off : (size_t) set * nza * RELX_NCONV;
   const size_t zstride = is_line ? 0 : RELX_NCONV;
-  TW<LIMB> *tabI = m.tab;
+  // the set's interpolated table: (trff1, trff2) plane, then (cosne1, cosne2)
+  const float2 *__restrict__ T = reinterpret_cast<const float2 *>(htab + (size_t) set * nr * ng);
+  const float2 *__restrict__ C = T + nr * ng;
 
-  // stage the (a, mu0) interpolation of the transfer functions (interpol_a_mu0, Relprofile.cpp:39-80)
   {
-    const size_t b00 = (size_t) s.ind_a * nm + s.ind_mu0, b10 = (size_t) (s.ind_a + 1) * nm + s.ind_mu0;
-    const size_t b01 = b00 + 1, b11 = b10 + 1;
-    const float f1 = s.ifac_a, f2 = s.ifac_mu0;
-    const float w00 = (1.0f - f1) * (1.0f - f2), w10 = f1 * (1.0f - f2), w01 = (1.0f - f1) * f2, w11 = f1 * f2;
-    for (int q = tid; q < nr * ng; q += kLineThreads) {
-      const float4 a = __ldg(&tab.rel_tc[b00 * nr * ng + q]), b = __ldg(&tab.rel_tc[b10 * nr * ng + q]);
-      const float4 c = __ldg(&tab.rel_tc[b01 * nr * ng + q]), d = __ldg(&tab.rel_tc[b11 * nr * ng + q]);
-      if constexpr (!LIMB) {
-        tabI[q].t = make_float2(w00 * a.x + w10 * b.x + w01 * c.x + w11 * d.x,
-                                w00 * a.y + w10 * b.y + w01 * c.y + w11 * d.y);
-      } else {
-        tabI[q].t = make_float4(w00 * a.x + w10 * b.x + w01 * c.x + w11 * d.x,
-                                w00 * a.y + w10 * b.y + w01 * c.y + w11 * d.y,
-                                w00 * a.z + w10 * b.z + w01 * c.z + w11 * d.z,
-                                w00 * a.w + w10 * b.w + w01 * c.w + w11 * d.w);
-      }
-    }
     for (int j = tid; j <= thi - tlo; j += kLineThreads) m.eff[j] = ff_split(ge[tlo + j]);
     for (int j = tid; j < thi - tlo; j += kLineThreads) m.red[j] = ge[tlo + j] >= 0.95 ? 1 : 0;
-    for (int i = tid; i < kLineWarps * kTileMax; i += kLineThreads) (&m.acc[0][0])[i] = 0.0f;
+    for (int i = tid; i < kLineWarps * kLineTile; i += kLineThreads) (&m.acc[0][0])[i] = 0.0f;
     for (int g = tid; g < ng; g += kLineThreads)
       m.gs[g] = ff_from_double(5e-3 + (1.0 - 2 * 5e-3) / (ng - 1) * ((float) g));
   }
@@ -511,12 +493,13 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
         const int it = rr.itab;
         const float fr = rr.ifac;
         for (int g = lane; g < ng; g += 32) {
-          const auto lo = tabI[(it + 1) * ng + g].t, hi = tabI[it * ng + g].t;
+          const float2 lo = __ldg(&T[(it + 1) * ng + g]), hi = __ldg(&T[it * ng + g]);
           if constexpr (!LIMB) {
             m.tw[warp][g].t = make_float2(fr * hi.x + (1.0f - fr) * lo.x, fr * hi.y + (1.0f - fr) * lo.y);
           } else {
+            const float2 clo = __ldg(&C[(it + 1) * ng + g]), chi = __ldg(&C[it * ng + g]);
             m.tw[warp][g].t = make_float4(fr * hi.x + (1.0f - fr) * lo.x, fr * hi.y + (1.0f - fr) * lo.y,
-                                          fr * hi.z + (1.0f - fr) * lo.z, fr * hi.w + (1.0f - fr) * lo.w);
+                                          fr * chi.x + (1.0f - fr) * clo.x, fr * chi.y + (1.0f - fr) * clo.y);
           }
         }
         __syncwarp();
@@ -590,7 +573,7 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
       __syncthreads();
     }
     // zone end: sum the warp rows in order, divide by the bin centre (renorm_relline_profile, Relprofile.cpp:753-762)
-    for (int b = 0; b < tbins / kSumBins; b++) {
+    for (int b = 0; b < kLineTile / kSumBins; b++) {
       const int jj = b * kSumBins + tid;
       double part = 0.0;
       if (jj < thi - tlo) {
@@ -603,7 +586,7 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
         part = (double) pv;
       }
       const double zs = block_sum_d<kLineThreads>(part, m.red_sum);
-      if (tid == 0 && b * kSumBins < thi - tlo) tsum[((size_t) set * nblk + tile * (tbins / kSumBins) + b) * nza + z] = zs;
+      if (tid == 0 && b * kSumBins < thi - tlo) tsum[((size_t) set * nblk + tile * (kLineTile / kSumBins) + b) * nza + z] = zs;
     }
     __syncthreads();
   }
@@ -612,8 +595,9 @@ __global__ void __launch_bounds__(kLineThreads, 3) relline_kernel(RelxTables tab
 // ---------------------------------------------------------------------------
 // emission-angle distribution per zone (Relprofile.cpp:908-938), one CTA per set.  The set's
 // (a, mu0)-interpolated transfer functions and emission-angle cosines on all table radii are
-// written once per set by hist_table_kernel and read through the read-only cache, so that the
-// histogram CTA's shared memory stays small (four CTAs per SM).
+// written once per set by line_table_kernel (which the line profile reads as well) and read
+// through the read-only cache, so that the histogram CTA's shared memory stays small (four CTAs
+// per SM).
 // ---------------------------------------------------------------------------
 struct HistSmem {
   RelxRadRec rec[kChunk];    // radius records of the current chunk
@@ -625,12 +609,14 @@ struct HistSmem {
 };
 
 // interpol_a_mu0 (Relprofile.cpp:39-80) of (trff1, trff2, cosne1, cosne2) at every (table radius,
-// g*) of a set: grid (chunks of kLineThreads entries, sets)
-__global__ void __launch_bounds__(kLineThreads) hist_table_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
+// g*) of a set, for the line profile and the histogram: grid (chunks of kLineThreads entries, sets).
+// A set's rel_nr x rel_ng float4 slot holds two planes of float2: (trff1, trff2), then (cosne1,
+// cosne2), so that the line profile without a limb law reads half the bytes.
+__global__ void __launch_bounds__(kLineThreads) line_table_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
                                                                   float4 *__restrict__ htab) {
   const int set = blockIdx.y;
   const RelxSetState &s = sst[set];
-  if (s.status != RELX_OK || s.model < RELX_RELXILL || s.cached) return;
+  if (s.status != RELX_OK || s.cached) return;
   const int nr = tab.rel_nr, nm = tab.rel_nmu0, ng = tab.rel_ng;
   const int q = blockIdx.x * kLineThreads + threadIdx.x;
   if (q >= nr * ng) return;
@@ -640,9 +626,10 @@ __global__ void __launch_bounds__(kLineThreads) hist_table_kernel(RelxTables tab
   const float w00 = (1.0f - f1) * (1.0f - f2), w10 = f1 * (1.0f - f2), w01 = (1.0f - f1) * f2, w11 = f1 * f2;
   const float4 a = __ldg(&tab.rel_tc[b00 * nr * ng + q]), b = __ldg(&tab.rel_tc[b10 * nr * ng + q]);
   const float4 c = __ldg(&tab.rel_tc[b01 * nr * ng + q]), d = __ldg(&tab.rel_tc[b11 * nr * ng + q]);
-  htab[(size_t) set * nr * ng + q] =
-      make_float4(w00 * a.x + w10 * b.x + w01 * c.x + w11 * d.x, w00 * a.y + w10 * b.y + w01 * c.y + w11 * d.y,
-                  w00 * a.z + w10 * b.z + w01 * c.z + w11 * d.z, w00 * a.w + w10 * b.w + w01 * c.w + w11 * d.w);
+  float2 *ht = reinterpret_cast<float2 *>(htab + (size_t) set * nr * ng);
+  ht[q] = make_float2(w00 * a.x + w10 * b.x + w01 * c.x + w11 * d.x, w00 * a.y + w10 * b.y + w01 * c.y + w11 * d.y);
+  ht[nr * ng + q] =
+      make_float2(w00 * a.z + w10 * b.z + w01 * c.z + w11 * d.z, w00 * a.w + w10 * b.w + w01 * c.w + w11 * d.w);
 }
 static_assert(offsetof(HistSmem, rec) % 16 == 0, "radius records are staged as int4 rows");
 
@@ -674,7 +661,9 @@ __global__ void __launch_bounds__(kLineThreads, 4) hist_kernel(RelxTables tab, c
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const RelxRadial &R = srad[set];
   const int nr = tab.rel_nr, ng = tab.rel_ng, n_incl = tab.x_nincl;
-  const float4 *__restrict__ T = htab + (size_t) set * nr * ng;  // the set's interpolated table
+  // the set's interpolated table: (trff1, trff2) plane, then (cosne1, cosne2)
+  const float2 *__restrict__ T = reinterpret_cast<const float2 *>(htab + (size_t) set * nr * ng);
+  const float2 *__restrict__ C = T + nr * ng;
   {
     for (int g = tid; g < ng; g += kLineThreads) {
       double gs = 5e-3 + (1.0 - 2 * 5e-3) / (ng - 1) * ((float) g);
@@ -721,13 +710,14 @@ __global__ void __launch_bounds__(kLineThreads, 4) hist_kernel(RelxTables tab, c
         const int gper = (ng + 7) >> 3, g_end = min(ng, (sub + 1) * gper);
         for (int g = sub * gper; g < g_end; g++) {
           // trf(g*) and cosne(g*) at this radius: interp_lin_1d(ifac_r, T[ind+1], T[ind]) (Relprofile.cpp:280-293)
-          const float4 lo = __ldg(&T[(it + 1) * ng + g]), hi = __ldg(&T[it * ng + g]);
+          const float2 lo = __ldg(&T[(it + 1) * ng + g]), hi = __ldg(&T[it * ng + g]);
+          const float2 clo = __ldg(&C[(it + 1) * ng + g]), chi = __ldg(&C[it * ng + g]);
           const float ge_ = m.gsf[g] * dg + gmn;
           const float cg = c * ge_ * ge_ * m.gfac[g];
 #pragma unroll
           for (int k = 0; k < 2; k++) {
             const float trf = k ? fr * hi.y + (1.0f - fr) * lo.y : fr * hi.x + (1.0f - fr) * lo.x;
-            const float mu = k ? fr * hi.w + (1.0f - fr) * lo.w : fr * hi.z + (1.0f - fr) * lo.z;
+            const float mu = k ? fr * chi.y + (1.0f - fr) * clo.y : fr * chi.x + (1.0f - fr) * clo.x;
             const float xb = (float) n_incl * (1.0f - mu);
             int b;
             if (fabsf(xb - rintf(xb)) < 1e-5f) {
@@ -772,12 +762,14 @@ __global__ void __launch_bounds__(kLineThreads, 4) hist_kernel(RelxTables tab, c
 }
 
 template <bool LIMB>
-static size_t line_smem_t(int nr, int ng) {
-  return sizeof(LineSmem<LIMB>) + sizeof(TW<LIMB>) * (size_t) (nr * ng - 1);
+static size_t line_smem_t(int ng) {
+  (void) ng;
+  return sizeof(LineSmem<LIMB>);
 }
 size_t line_smem_bytes(int nr, int ng, bool limb, int tile) {
+  (void) nr;
   (void) tile;
-  return limb ? line_smem_t<true>(nr, ng) : line_smem_t<false>(nr, ng);
+  return limb ? line_smem_t<true>(ng) : line_smem_t<false>(ng);
 }
 size_t hist_smem_bytes(int nr, int ng) {
   (void) nr;
@@ -786,38 +778,45 @@ size_t hist_smem_bytes(int nr, int ng) {
 }
 
 cudaError_t relline_set_smem(int nr, int ng) {
+  (void) nr;
   cudaError_t e;
 #define SET(L)                                                                                             \
   e = cudaFuncSetAttribute(relline_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,                \
-                           (int) line_smem_t<L>(nr, ng));                                                  \
+                           (int) line_smem_t<L>(ng));                                                      \
   if (e != cudaSuccess) return e;
   SET(false) SET(true)
 #undef SET
   return cudaFuncSetAttribute(hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) hist_smem_bytes(nr, ng));
 }
 
-// launches the line profile (both variants: a set runs in the one matching its limb law) with
-// tiles of `tile` bins (256 or 512) and, for relxill models, the emission-angle histogram
-cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream_t s, const RelxTables &tab,
+cudaError_t launch_line_table(int n_sets, cudaStream_t s, const RelxTables &tab, const RelxSetState *sst,
+                              float4 *htab) {
+  const int nq = tab.rel_nr * tab.rel_ng;
+  line_table_kernel<<<dim3((nq + kLineThreads - 1) / kLineThreads, n_sets), kLineThreads, 0, s>>>(tab, sst, htab);
+  return cudaGetLastError();
+}
+
+// launches the line profile (both variants: a set runs in the one matching its limb law) in tiles of
+// kLineTile bins and, for relxill models, the emission-angle histogram; htab: written by
+// launch_line_table
+cudaError_t launch_relline(bool hist, int n_sets, int nblk, cudaStream_t s, const RelxTables &tab,
                            const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
-                           int nza, float *prof, float *dist, double *tsum, bool any_limb, bool zsplit, float4 *htab) {
-  const int nr = tab.rel_nr, ng = tab.rel_ng;
-  tile = (tile == 256) ? 256 : 512;
-  const int ntile = (nblk * kSumBins + tile - 1) / tile;
+                           int nza, float *prof, float *dist, double *tsum, bool any_limb, bool zsplit,
+                           const float4 *htab) {
+  const int ng = tab.rel_ng;
+  const int ntile = (nblk * kSumBins + kLineTile - 1) / kLineTile;
   const dim3 grid(ntile, n_sets, zsplit ? nza : 1);
-  relline_kernel<false><<<grid, kLineThreads, line_smem_t<false>(nr, ng), s>>>(tab, sin, sst, srad, line_e, nza, prof,
-                                                                               tsum, nblk, tile);
+  relline_kernel<false><<<grid, kLineThreads, line_smem_t<false>(ng), s>>>(tab, sin, sst, srad, line_e, htab, nza, prof,
+                                                                           tsum, nblk);
   if (any_limb)
-    relline_kernel<true><<<grid, kLineThreads, line_smem_t<true>(nr, ng), s>>>(tab, sin, sst, srad, line_e, nza, prof,
-                                                                               tsum, nblk, tile);
+    relline_kernel<true><<<grid, kLineThreads, line_smem_t<true>(ng), s>>>(tab, sin, sst, srad, line_e, htab, nza, prof,
+                                                                           tsum, nblk);
   if (hist) return launch_hist(n_sets, s, tab, sst, srad, nza, dist, zsplit, htab);
   return cudaGetLastError();
 }
 
 cudaError_t launch_hist(int n_sets, cudaStream_t s, const RelxTables &tab, const RelxSetState *sst,
-                        const RelxRadial *srad, int nza, float *dist, bool zsplit, float4 *htab) {
-  const int nq = tab.rel_nr * tab.rel_ng;
-  hist_table_kernel<<<dim3((nq + kLineThreads - 1) / kLineThreads, n_sets), kLineThreads, 0, s>>>(tab, sst, htab);
+                        const RelxRadial *srad, int nza, float *dist, bool zsplit, const float4 *htab) {
   hist_kernel<<<dim3(n_sets, zsplit ? nza : 1), kLineThreads, hist_smem_bytes(tab.rel_nr, tab.rel_ng), s>>>(
       tab, sst, srad, nza, htab, dist);
   return cudaGetLastError();

@@ -12,6 +12,7 @@ namespace relx {
 constexpr int kSetupThreadsH = 256;
 constexpr int kLineThreadsH = 256;
 constexpr int kSumBinsH = 256;   // bins per profile-sum block (tsum)
+constexpr int kLineTileH = 512;  // energy bins per line-profile CTA
 constexpr int kConvThreadsH = 256;
 constexpr int kFinThreadsH = 128;
 constexpr int kXmodThreadsH = 256;  // xillver model kernel
@@ -26,15 +27,18 @@ __global__ void setup_kernel(RelxTables tab, int model, const RelxSetIn *sin, co
                              RelxSetState *sout, RelxRadial *rout, RelxCorners *cout, RelxZoneCorners *zcout);
 
 cudaError_t relline_set_smem(int nr, int ng);
-// tile: energy bins per line-kernel CTA (256 or 512); nblk: 256-bin profile-sum blocks per set
-cudaError_t launch_relline(bool hist, int n_sets, int tile, int nblk, cudaStream_t s, const RelxTables &tab,
+// the sets' (a, mu0)-interpolated transfer-function tables (rel_nr x rel_ng float4 per set), read
+// by the line profile and the emission-angle histogram
+cudaError_t launch_line_table(int n_sets, cudaStream_t s, const RelxTables &tab, const RelxSetState *sst,
+                              float4 *htab);
+// nblk: 256-bin profile-sum blocks per set; htab: written by launch_line_table
+cudaError_t launch_relline(bool hist, int n_sets, int nblk, cudaStream_t s, const RelxTables &tab,
                            const RelxSetIn *sin, const RelxSetState *sst, const RelxRadial *srad, const double *line_e,
                            int nza, float *prof, float *dist, double *tsum, bool any_limb, bool zsplit,
-                           float4 *htab);
-// the emission-angle histograms alone (relxill models), for a launch on its own stream; htab: the
-// sets' interpolated transfer-function tables (rel_nr x rel_ng float4 per set), written here
+                           const float4 *htab);
+// the emission-angle histograms alone (relxill models), for a launch on its own stream
 cudaError_t launch_hist(int n_sets, cudaStream_t s, const RelxTables &tab, const RelxSetState *sst,
-                        const RelxRadial *srad, int nza, float *dist, bool zsplit, float4 *htab);
+                        const RelxRadial *srad, int nza, float *dist, bool zsplit, const float4 *htab);
 
 cudaError_t xillver_set_smem(int n_incl);
 // bounded-wait self-test: writes the status of a wait that cannot complete (RELX_ERR_TIMEOUT)

@@ -1045,7 +1045,7 @@ struct BatchShape {
   int model, n_sets, nza;
   int nz_min = 1;     // the smallest zone count of the batch's sets
   int nblk;           // 256-bin profile-sum blocks per set
-  int line_tile = 512;  // energy bins per line-kernel CTA (256 or 512)
+  int line_tile = kLineTileH;  // energy bins per line-kernel CTA
   int chunk = 0;      // sets per pipelined chunk (0: one range)
   bool any_limb = false;  // some set uses a limb-darkening law (relline / relconv limb parameter)
   int64_t n_edges;  // total energy edges
@@ -1067,7 +1067,8 @@ static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b,
     return st;
   if (kind == RELX_XILLVER) return 0;  // no line profile, no convolution
   if ((st = W.rad.reserve(S * sizeof(RelxRadial))) || (st = W.dist.reserve(S * nza * RELX_MAX_INCL * sizeof(float))) ||
-      (st = W.tsum.reserve(S * b.nblk * nza * sizeof(double))))
+      (st = W.tsum.reserve(S * b.nblk * nza * sizeof(double))) ||
+      (st = W.htab.reserve(S * (size_t) T.d.rel_nr * T.d.rel_ng * sizeof(float4))))
     return st;
   if (kind == RELX_RELLINE) {
     if ((st = W.line_e.reserve(b.n_edges * sizeof(double))) || (st = W.prof.reserve(b.n_edges * sizeof(float))))
@@ -1080,8 +1081,7 @@ static int reserve_workspace(const Tables &T, Workspace &W, const BatchShape &b,
   }
   if (relx_is_relxill(kind)) {
     if ((st = W.corners.reserve(S * sizeof(RelxCorners))) || (st = W.order.reserve(S * sizeof(int))) ||
-        (st = W.xill.reserve(S * nza * (size_t) std::max(T.d.x_cpad, T.dcp.x_cpad) * sizeof(float))) ||
-        (st = W.htab.reserve(S * (size_t) T.d.rel_nr * T.d.rel_ng * sizeof(float4))))
+        (st = W.xill.reserve(S * nza * (size_t) std::max(T.d.x_cpad, T.dcp.x_cpad) * sizeof(float))))
       return st;
     if (need_zone_corners && (st = W.zcorners.reserve(S * sizeof(RelxZoneCorners)))) return st;
   }
@@ -1166,6 +1166,12 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   // relxill models: the emission-angle histograms and the xillver zone spectra depend on the set-up
   // only; they run on a side stream while the line profile runs on s, and s waits for them (all on
   // s while per-kernel timing is on, so that the kernels' intervals do not overlap)
+  // the sets' interpolated transfer-function tables, for the line profile and the histograms
+  float4 *htab = W.htab.as<float4>() + (size_t) base * tab.rel_nr * tab.rel_ng;
+  {
+    ProfScope ps(PK_LINE, s);
+    RELX_CUDA(launch_line_table(n, s, tab, sst, htab));
+  }
   const bool relxill = relx_is_relxill(kind);
   Context::Side *sd = (relxill && !g_prof.on) ? side_of(C, s) : nullptr;
   cudaStream_t xs = sd ? sd->side : s;
@@ -1175,18 +1181,17 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   }
   // few sets: a CTA per zone as well, so that the line profile and the histograms of a single
   // spectrum spread over more SMs (the same numbers: zones are summed separately either way)
-  const int ntile = (b.nblk * kSumBinsH + b.line_tile - 1) / b.line_tile;
+  const int ntile = (b.nblk * kSumBinsH + kLineTileH - 1) / kLineTileH;
   const bool zsplit = b.nza > 1 && (int64_t) n * ntile < 2 * 152;
   {
     ProfScope ps(PK_LINE, s, 1 + (b.any_limb ? 1 : 0));
-    RELX_CUDA(launch_relline(false, n, b.line_tile, b.nblk, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza,
-                             prof, dist, tsum, b.any_limb, zsplit, nullptr));
+    RELX_CUDA(launch_relline(false, n, b.nblk, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza, prof, dist, tsum,
+                             b.any_limb, zsplit, htab));
   }
   if (relxill) {
     {
       ProfScope ps(PK_HIST, xs);
-      RELX_CUDA(launch_hist(n, xs, tab, sst, rad, b.nza, dist, b.nza > 1 && n < 2 * 152,
-                            W.htab.as<float4>() + (size_t) base * tab.rel_nr * tab.rel_ng));
+      RELX_CUDA(launch_hist(n, xs, tab, sst, rad, b.nza, dist, b.nza > 1 && n < 2 * 152, htab));
     }
     {
       // the zone kernel for sets with more than RELX_ZDENSE zones and for 6-parameter sets whose
@@ -1376,22 +1381,19 @@ static int tuned_launch(Context &C, Workspace &W, BatchShape &b, cudaStream_t s,
   const Context::TuneEntry *known = nullptr;
   for (const auto &t : C.tune)
     if (t.model == b.model && t.sclass == sclass && t.nza == b.nza) known = &t;
-  const char *tile_env = std::getenv("RELX_LINE_TILE");
-  const bool explicit_choice = tile_env || std::getenv("RELX_CHUNK_SETS") != nullptr;
-  if (tile_env) {
-    b.line_tile = std::atoi(tile_env) == 256 ? 256 : 512;  // explicit choice
-  } else if (known) {
-    b.line_tile = known->line_tile;
-    if (!cached && !explicit_choice) b.chunk = known->chunk;
-  } else {
-    b.line_tile = b.n_sets <= 1024 ? 256 : 512;  // small batches: more CTAs per set
-  }
+  const bool explicit_choice = std::getenv("RELX_CHUNK_SETS") != nullptr;
+  b.line_tile = kLineTileH;
+  if (known && !cached && !explicit_choice) b.chunk = known->chunk;
+  // the candidates: one range, or pipelined chunks of 1024 sets for large batches
   if (known || !allow_tune || !C.autotune_on || g_prof.on || cached || explicit_choice ||
       relx_kind(b.model) == RELX_RELLINE || b.model == RELX_XILLVER)
     return launch_batch(C, W, b, s, use_cache);
+  if (b.n_sets < 2048) {  // one candidate: recorded without trials
+    C.tune.push_back(Context::TuneEntry{b.model, sclass, b.nza, kLineTileH, 0, {0, 0, 0, 0}});
+    return launch_batch(C, W, b, s, use_cache);
+  }
   struct Cand { int tile, chunk; };
-  std::vector<Cand> cands = {{512, 0}, {256, 0}};
-  if (b.n_sets >= 2048) cands.push_back({512, 1024});
+  std::vector<Cand> cands = {{kLineTileH, 0}, {kLineTileH, 1024}};
   cudaEvent_t e0, e1;
   RELX_CUDA(cudaEventCreate(&e0));
   RELX_CUDA(cudaEventCreate(&e1));
@@ -1722,14 +1724,14 @@ size_t batch_device_bytes(int model, int n_sets, int64_t n_edges, int max_bins, 
   const int gmax = (kind == RELX_RELLINE) ? std::max(max_bins, 1) : RELX_NCONV;
   const size_t nblk = (size_t) (gmax + kSumBinsH - 1) / kSumBinsH;
   size_t per_set = sizeof(RelxSetIn) + sizeof(RelxSetState) + sizeof(RelxRadial) + sizeof(int) * 4 +
-                   sizeof(float) * nza * RELX_MAX_INCL + sizeof(double) * nblk * nza;
+                   sizeof(float) * nza * RELX_MAX_INCL + sizeof(double) * nblk * nza +
+                   sizeof(float4) * (size_t) RELX_MAX_NRTAB * RELX_MAX_NG;  // the interpolated transfer functions
   size_t per_edge = sizeof(double) * 2;                                      // user grid, flux
   if (kind == RELX_RELLINE) per_edge += sizeof(double) + sizeof(float);     // line grid, profile
   else per_edge += (kind == RELX_RELCONV) ? sizeof(double) : 0;              // relconv input
   if (kind != RELX_RELLINE) per_set += 2 * sizeof(float) * (size_t) nza * RELX_NCONV;
   if (relx_is_relxill(kind))
-    per_set += sizeof(RelxCorners) + sizeof(float) * (size_t) nza * 4096 +
-               sizeof(float4) * (size_t) RELX_MAX_NRTAB * RELX_MAX_NG;  // the interpolated table of the histograms
+    per_set += sizeof(RelxCorners) + sizeof(float) * (size_t) nza * 4096;
   if (relx_is_cp(model) || nza > RELX_ZDENSE) per_set += sizeof(RelxZoneCorners);
   return staged + cp + per_set * S + per_edge * E + sizeof(int) +
          (relx_is_cp(model) ? nthcomp_scratch_bytes(n_sets, nza, false) : 0);

@@ -136,18 +136,13 @@ def test_serve_results_match_batch_alone(gpu):
     gpu.cache_config(0)
 
 
-def test_tiles_chunks_and_graphs_give_the_same_numbers(gpu, monkeypatch):
-    """Line-kernel tiles of 256 and 512 bins, pipelined chunks and CUDA-graph replay change nothing."""
+def test_chunks_and_graphs_give_the_same_numbers(gpu, monkeypatch):
+    """Pipelined chunks and CUDA-graph replay change nothing."""
     lp = _lp_sets(9, 31)
     g = _grids(9, 32)
     gpu.tuning_config(autotune=False, graphs=False)
     try:
         want = _batch(gpu, "relxilllp", lp, g)
-        for tile in ("256", "512"):
-            monkeypatch.setenv("RELX_LINE_TILE", tile)
-            for a, b in zip(_batch(gpu, "relxilllp", lp, g), want):
-                np.testing.assert_array_equal(a, b)
-        monkeypatch.delenv("RELX_LINE_TILE")
         monkeypatch.setenv("RELX_CHUNK_SETS", "2")
         for a, b in zip(_batch(gpu, "relxilllp", lp, g), want):
             np.testing.assert_array_equal(a, b)
