@@ -36,7 +36,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "relxilllp spectra/s batched vs plain GPU at ≤1e-4 rel err; serve p50/p99 ms"
 N_SETS = 4096
-LINE_DRAM_BYTES_4096 = 384.7e6 + 472.0e6  # line kernel, one launch over the 4096-set workload (ncu)
+# DRAM bytes (read + write) of one step's line-profile launches over the 4096-set workload (ncu, one-pass
+# capture): the per-set interpolated table (line_table_kernel) and the line profile (relline_kernel)
+LINE_DRAM_BYTES_4096 = (33.64e6 + 205.33e6) + (391.13e6 + 561.29e6)
 WORKLOAD = ("relxilllp batched, 4096 sets per GPU, per-set grids 300-5000 log bins 0.3-80 keV, "
             "10 radial zones")
 N_PROF = 9  # kernel kinds of the per-kernel event profiler (relx_profile_name)
@@ -633,7 +635,8 @@ def run_gpu(args):
     # rooflines.  The line-profile kernel is bound by FP32 instruction issue: its algorithmic work is
     # the oracle's count of integrand evaluations (one branch each) times FLOPS_PER_EVAL, over the
     # FP32 FMA rate measured on this GPU (relx_fp32_rate); its memory term (the four transfer-function
-    # corner tables of the set, the radius records, the profile written) is printed beside it.  The
+    # corner tables of the set read and the set's interpolated table written by the table kernel, the
+    # interpolated table and the radius records read, the profile written) is printed beside it.  The
     # xillver kernel reads its corner rows through L2 (sets are visited in table-row order, so
     # neighbouring sets share rows): its algorithmic row bytes over its time are an L2 rate.
     names = [L.relx_profile_name(k).decode() for k in range(N_PROF)]
@@ -650,7 +653,8 @@ def run_gpu(args):
     fp32 = ctypes.c_double(0.0)
     fp32_gflops = fp32.value if L.relx_fp32_rate(ctypes.byref(fp32)) == 0 else None
     line_ms = per["relline"][0]
-    roof = {"kernel": "relline", "bound": "fp32", "achieved": None, "peak": None, "unit": "TFLOP/s", "frac": None,
+    roof = {"kernel": "relline", "launches": ["line_table_kernel", "relline_kernel"], "bound": "fp32",
+            "achieved": None, "peak": None, "unit": "TFLOP/s", "frac": None,
             "traffic": None, "peak_source": "measured FP32 FMA rate (relx_fp32_rate, CUDA events)"}
     if evals_per_set is not None and fp32_gflops:
         flops = evals_per_set * FLOPS_PER_EVAL * S
@@ -658,13 +662,15 @@ def run_gpu(args):
                      "algorithmic_flops": flops, "evals_per_set": evals_per_set,
                      "flops_per_eval": FLOPS_PER_EVAL})
         roof["frac"] = roof["achieved"] / roof["peak"]
-    # DRAM bytes (read + write) of one line-kernel launch over the 4096-set workload (512-bin tiles), from
+    # DRAM bytes (read + write) of the line-profile launches of one step over the 4096-set workload, from
     # the one-pass ncu capture in the profiles folder (dram_traffic_relxilllp_4096sets.md); other batch
     # sizes are scaled by their set count
     roof["traffic"] = LINE_DRAM_BYTES_4096 * S / 4096
-    roof["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum, 4096-set launch, scaled by sets"
+    roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of line_table_kernel and relline_kernel, "
+                              "4096-set launch, scaled by sets")
     ng, nr_tab = 40, 100
-    line_bytes = S * (4 * nr_tab * ng * 16 + 1000 * 64) + int(st6[2]) * int(st6[1] // max(S, 1) or 1) * 4
+    line_bytes = (S * (4 * nr_tab * ng * 16 + nr_tab * ng * 16 + nr_tab * ng * 8 + 1000 * 64) +
+                  int(st6[2]) * int(st6[1] // max(S, 1) or 1) * 4)
     roof["hbm_term"] = {"algorithmic_bytes": line_bytes, "achieved_gbs": line_bytes / (line_ms * 1e-3) / 1e9,
                         "peak_gbs": hbm_peak, "frac": line_bytes / (line_ms * 1e-3) / 1e9 / hbm_peak}
     x_pad = int(st6[3])  # floats per table row on the convolution grid

@@ -1166,25 +1166,23 @@ static int launch_range(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   // relxill models: the emission-angle histograms and the xillver zone spectra depend on the set-up
   // only; they run on a side stream while the line profile runs on s, and s waits for them (all on
   // s while per-kernel timing is on, so that the kernels' intervals do not overlap)
-  // the sets' interpolated transfer-function tables, for the line profile and the histograms
+  // the sets' interpolated transfer-function tables (line_table_kernel), then the line profile on
+  // s; the histograms and the xillver zone spectra on the side stream after the tables
   float4 *htab = W.htab.as<float4>() + (size_t) base * tab.rel_nr * tab.rel_ng;
-  {
-    ProfScope ps(PK_LINE, s);
-    RELX_CUDA(launch_line_table(n, s, tab, sst, htab));
-  }
   const bool relxill = relx_is_relxill(kind);
   Context::Side *sd = (relxill && !g_prof.on) ? side_of(C, s) : nullptr;
   cudaStream_t xs = sd ? sd->side : s;
-  if (sd) {
-    RELX_CUDA(cudaEventRecord(sd->fork, s));
-    RELX_CUDA(cudaStreamWaitEvent(xs, sd->fork, 0));
-  }
   // few sets: a CTA per zone as well, so that the line profile and the histograms of a single
   // spectrum spread over more SMs (the same numbers: zones are summed separately either way)
   const int ntile = (b.nblk * kSumBinsH + kLineTileH - 1) / kLineTileH;
   const bool zsplit = b.nza > 1 && (int64_t) n * ntile < 2 * 152;
   {
-    ProfScope ps(PK_LINE, s, 1 + (b.any_limb ? 1 : 0));
+    ProfScope ps(PK_LINE, s, 2 + (b.any_limb ? 1 : 0));
+    RELX_CUDA(launch_line_table(n, s, tab, sst, htab));
+    if (sd) {
+      RELX_CUDA(cudaEventRecord(sd->fork, s));
+      RELX_CUDA(cudaStreamWaitEvent(xs, sd->fork, 0));
+    }
     RELX_CUDA(launch_relline(false, n, b.nblk, s, tab, sin, sst, rad, W.line_e.as<double>(), b.nza, prof, dist, tsum,
                              b.any_limb, zsplit, htab));
   }
