@@ -1536,16 +1536,21 @@ static int enqueue_host_batch(Context &C, Workspace &W, Pinned &P, cudaStream_t 
 // the GPU computes the later groups.  Both workspaces are reserved for the largest group before the
 // first one is queued (no buffer is reallocated while a group is in flight).
 // group boundaries s0[0..ng]: groups of about `per` sets (RELX_HOST_GROUP_SETS, default 1024), the
-// first and the last a quarter of that, so that the GPU starts early and the last copy out is short
+// first and the last smaller (RELX_HOST_EDGE_SETS, default half of `per`), so that the GPU starts
+// early and the last copy out is short.  Measured on the 4096-set relxilllp workload (ms per step,
+// host buffers): ends of 512 and 1024-set groups 9.84, ends of 256 10.16, 128 10.43, one group
+// 11.08 -- a small group leaves the GPU partly idle for longer than its copies take.
 static std::vector<int> host_groups(int n_sets) {
   const char *e = std::getenv("RELX_HOST_GROUP_SETS");
   const int per = (e && std::atoi(e) >= 64) ? std::atoi(e) : 1024;
+  const char *ee = std::getenv("RELX_HOST_EDGE_SETS");
+  const int edge = (ee && std::atoi(ee) >= 16 && std::atoi(ee) <= per) ? std::atoi(ee) : per / 2;
   std::vector<int> b{0};
   if (n_sets < 2 * per) {
     b.push_back(n_sets);
     return b;
   }
-  const int edge = per / 4, mid = n_sets - 2 * edge;
+  const int mid = n_sets - 2 * edge;
   const int nm = std::max(1, std::min(14, (mid + per / 2) / per));
   b.push_back(edge);
   for (int g = 1; g <= nm; g++) b.push_back(edge + (int) ((int64_t) g * mid / nm));
