@@ -59,7 +59,7 @@ def test_device_buffers_match_host_buffers(gpu):
 
 
 def test_large_host_batch_in_groups(gpu, oracle):
-    """2100 sets through the host buffers run as groups of consecutive sets (256, 794, 794, 256)
+    """2100 sets through the host buffers run as groups of consecutive sets (512, 1076, 512)
     alternating over two streams; each set equals the same set in one device-buffer launch of all
     2100, and the oracle."""
     params, grids = _lp_sets(2100, 32, 40, 160)
@@ -68,7 +68,7 @@ def test_large_host_batch_in_groups(gpu, oracle):
     dev = _device(gpu, "relxilllp", params, grids)
     for i in range(len(grids)):
         np.testing.assert_array_equal(host[i], dev[i])
-    for i in (0, 255, 256, 1049, 1050, 1843, 1844, 2099):  # the ends of the groups
+    for i in (0, 511, 512, 1587, 1588, 2099):  # the ends of the groups
         s, orc = oracle_lib.evaluate("relxilllp", params[i], grids[i])
         assert s == 0
         assert_close(host[i], orc, f"set {i}")
