@@ -4,7 +4,8 @@
 //
 // line_table_kernel writes each set's (a, mu0)-interpolated transfer functions on
 // all table radii once (two float2 planes: trff1/trff2, cosne1/cosne2); the line
-// profile and the histogram read them through the read-only cache.
+// profile stages the rows a chunk of radii reads in shared memory, the histogram
+// reads them through the read-only cache.
 //
 // Line profile: one CTA per (512-bin tile, parameter set), 8 warps, four CTAs per SM.
 //  * Zone by zone, warps take fine radii round robin; per radius a warp builds
@@ -399,7 +400,12 @@ struct LineSmem {
   RelxRadRec rec[kChunk];
   float2 gs[RELX_MAX_NG];   // table g* points (Relprofile.cpp:104-106) as float-float
   double red_sum[kLineWarps + 1];
+  int row0, nrow;           // the set-table rows staged for the chunk: row0 .. row0 + nrow - 1
+  TW<LIMB> rows[1];         // [line_rows<LIMB>()][ng] those rows, dynamic tail
 };
+// set-table rows staged per chunk at most (a zone of about 100 fine radii reads 8 rows typically,
+// about 30 in the outermost zones); a chunk that reads more takes its rows from the read-only cache
+template <bool LIMB> constexpr int line_rows() { return LIMB ? 16 : 32; }
 static_assert(offsetof(LineSmem<false>, rec) % 16 == 0 && offsetof(LineSmem<true>, rec) % 16 == 0,
               "radius records are staged as int4 rows");
 static_assert(kLineTile / 32 <= 32, "a lane's bins of one radius fit a 32-bit mask");
@@ -485,6 +491,37 @@ __global__ void __launch_bounds__(kLineThreads, 4) relline_kernel(
         for (int q = tid; q < cn * 4; q += kLineThreads) dst[q] = src[q];
       }
       __syncthreads();
+      if (warp == 0) {
+        // the set-table rows the chunk's radii read (itab and itab + 1 of each)
+        int lo = 1 << 30, hi = -1;
+        for (int q = lane; q < cn; q += 32) {
+          const RelxRadRec &r = m.rec[q];
+          if (r.ielo >= 0 && r.ielo < thi && r.iehi >= tlo) {
+            lo = min(lo, (int) r.itab);
+            hi = max(hi, (int) r.itab);
+          }
+        }
+        lo = __reduce_min_sync(0xffffffffu, lo);
+        hi = __reduce_max_sync(0xffffffffu, hi);
+        if (lane == 0) {
+          m.row0 = lo;
+          m.nrow = hi >= lo ? hi + 2 - lo : 0;
+        }
+      }
+      __syncthreads();
+      const int row0 = m.row0;
+      const bool staged = m.nrow <= line_rows<LIMB>();
+      if (staged) {
+        for (int q = tid; q < m.nrow * ng; q += kLineThreads) {
+          if constexpr (!LIMB) {
+            m.rows[q].t = __ldg(&T[row0 * ng + q]);
+          } else {
+            const float2 t = __ldg(&T[row0 * ng + q]), c = __ldg(&C[row0 * ng + q]);
+            m.rows[q].t = make_float4(t.x, t.y, c.x, c.y);
+          }
+        }
+      }
+      __syncthreads();
       for (int ci = warp; ci < cn; ci += kLineWarps) {
         const RelxRadRec &rr = m.rec[ci];
         const int ielo = rr.ielo, iehi = rr.iehi;
@@ -493,13 +530,23 @@ __global__ void __launch_bounds__(kLineThreads, 4) relline_kernel(
         const int it = rr.itab;
         const float fr = rr.ifac;
         for (int g = lane; g < ng; g += 32) {
-          const float2 lo = __ldg(&T[(it + 1) * ng + g]), hi = __ldg(&T[it * ng + g]);
           if constexpr (!LIMB) {
+            const float2 lo = staged ? m.rows[(it + 1 - row0) * ng + g].t : __ldg(&T[(it + 1) * ng + g]);
+            const float2 hi = staged ? m.rows[(it - row0) * ng + g].t : __ldg(&T[it * ng + g]);
             m.tw[warp][g].t = make_float2(fr * hi.x + (1.0f - fr) * lo.x, fr * hi.y + (1.0f - fr) * lo.y);
           } else {
-            const float2 clo = __ldg(&C[(it + 1) * ng + g]), chi = __ldg(&C[it * ng + g]);
+            float4 lo, hi;
+            if (staged) {
+              lo = m.rows[(it + 1 - row0) * ng + g].t;
+              hi = m.rows[(it - row0) * ng + g].t;
+            } else {
+              const float2 tl = __ldg(&T[(it + 1) * ng + g]), th = __ldg(&T[it * ng + g]);
+              const float2 cl = __ldg(&C[(it + 1) * ng + g]), ch = __ldg(&C[it * ng + g]);
+              lo = make_float4(tl.x, tl.y, cl.x, cl.y);
+              hi = make_float4(th.x, th.y, ch.x, ch.y);
+            }
             m.tw[warp][g].t = make_float4(fr * hi.x + (1.0f - fr) * lo.x, fr * hi.y + (1.0f - fr) * lo.y,
-                                          fr * chi.x + (1.0f - fr) * clo.x, fr * chi.y + (1.0f - fr) * clo.y);
+                                          fr * hi.z + (1.0f - fr) * lo.z, fr * hi.w + (1.0f - fr) * lo.w);
           }
         }
         __syncwarp();
@@ -763,8 +810,7 @@ __global__ void __launch_bounds__(kLineThreads, 4) hist_kernel(RelxTables tab, c
 
 template <bool LIMB>
 static size_t line_smem_t(int ng) {
-  (void) ng;
-  return sizeof(LineSmem<LIMB>);
+  return sizeof(LineSmem<LIMB>) + sizeof(TW<LIMB>) * (size_t) (line_rows<LIMB>() * ng - 1);
 }
 size_t line_smem_bytes(int nr, int ng, bool limb, int tile) {
   (void) nr;
