@@ -581,17 +581,20 @@ def run_gpu(args):
             dist.destroy_process_group()
         return 0
 
-    # plain path: one synchronous c_lmodrelxilllp call per spectrum
+    # plain path: one synchronous c_lmodrelxilllp call per spectrum, every call evaluated (the output
+    # cache of the local-model calls would serve the warm-up sets again)
     plain = None
     if not args.no_plain:
         n_plain = min(64, S)
+        R.output_cache_config(0)
         for i in range(min(4, S)):
             R.relxilllp(grids[i], params[i])
         t0 = time.perf_counter()
         for i in range(n_plain):
             R.relxilllp(grids[i], params[i])
         plain = {"value": n_plain / (time.perf_counter() - t0), "unit": "spectra/s",
-                 "sample": f"{n_plain} single c_lmodrelxilllp calls"}
+                 "sample": f"{n_plain} single c_lmodrelxilllp calls, output cache off"}
+        R.output_cache_config(50)
 
     # parity spot check against the oracle (outside the timed region)
     out = d_flux.cpu().numpy()

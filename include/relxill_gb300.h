@@ -156,6 +156,20 @@ int relx_cache_config(int slots);
 /* out[0] lookups, out[1] hits, out[2] slots */
 int relx_cache_stats(int64_t *out);
 
+/* Output cache of the local-model entry points (c_lmod*), the counterpart of
+ * the reference's RelxillCache (src/Relcache.h:182-251, src/Relxill.cpp:295-400):
+ * a relxill, relxilllp, relxillCp or relxilllpCp call whose parameters all lie
+ * within 1e-8 of a recent call's (the reference's CACHE_LIMIT), on the same
+ * energy grid and with the same environment options (RELXILL_NUM_RZONES,
+ * RELLINE_PHYSICAL_NORM, RELXILL_RENORMALIZE, RELXILL_CONSTANT_DENSITY), returns
+ * that call's flux without evaluating.  The last max_entries successful calls
+ * are kept (50 by default, the reference's RELXILL_CACHE_SIZE); 0 turns it
+ * off.  relx_init with other tables empties it.  Batched, device and serving
+ * calls do not use it. */
+int relx_output_cache_config(int max_entries);
+/* out[0] lookups, out[1] hits, out[2] entries held */
+int relx_output_cache_stats(int64_t *out);
+
 /* Serving engine (no counterpart in the reference): continuous batching of
  * single-spectrum requests from many clients onto the batched path.  A
  * scheduler thread forms a batch of waiting requests (one model, arrival

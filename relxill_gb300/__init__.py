@@ -105,6 +105,10 @@ def lib() -> ctypes.CDLL:
     L.relx_cache_config.restype = ctypes.c_int
     L.relx_cache_stats.argtypes = [_lp]
     L.relx_cache_stats.restype = ctypes.c_int
+    L.relx_output_cache_config.argtypes = [ctypes.c_int]
+    L.relx_output_cache_config.restype = ctypes.c_int
+    L.relx_output_cache_stats.argtypes = [_lp]
+    L.relx_output_cache_stats.restype = ctypes.c_int
     L.relx_serve_create.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int]
     L.relx_serve_create.restype = ctypes.c_void_p
     L.relx_serve_submit.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_int, _dp, _dp, ctypes.c_int,
@@ -288,6 +292,22 @@ def cache_stats() -> Dict[str, int]:
     if st:
         raise RelxillError(st, last_error())
     return {"lookups": int(out[0]), "hits": int(out[1]), "slots": int(out[2])}
+
+
+def output_cache_config(max_entries: int) -> None:
+    """Output cache of the local-model calls (relxill family): the last `max_entries` calls are kept
+    (50 by default, as the reference's RelxillCache); 0 turns it off."""
+    st = lib().relx_output_cache_config(int(max_entries))
+    if st:
+        raise RelxillError(st, last_error())
+
+
+def output_cache_stats() -> Dict[str, int]:
+    out = np.zeros(3, dtype=np.int64)
+    st = lib().relx_output_cache_stats(_ptr(out, _lp))
+    if st:
+        raise RelxillError(st, last_error())
+    return {"lookups": int(out[0]), "hits": int(out[1]), "entries": int(out[2])}
 
 
 class Server:

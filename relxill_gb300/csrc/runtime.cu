@@ -12,6 +12,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <mutex>
+#include <deque>
 #include <string>
 #include <thread>
 #include <vector>
@@ -830,6 +831,62 @@ static EnvOpts read_env() {
   return o;
 }
 
+// ---- output cache of the local-model entry points: the counterpart of the reference's RelxillCache
+// (Relcache.h:182-251, used by relxill_kernel, Relxill.cpp:295-400).  A relxill-family call whose
+// parameters all lie within 1e-8 of a recent call's (CACHE_LIMIT, Relcache.h:32, Relcache.cpp:46-48)
+// returns that call's flux without evaluating.  The reference keys on the parameters alone and
+// rebins its cached spectrum onto each call's grid; here the flux is kept on the caller's grid,
+// so the grid and the environment options that change a spectrum are part of the key.  Newest
+// first; the oldest is dropped beyond max_entries (RELXILL_CACHE_SIZE 50, Relcache.h:37).
+struct OutEntry {
+  int model;
+  EnvOpts env;
+  std::vector<double> par, ener, flux;
+};
+struct OutCache {
+  std::mutex mu;
+  std::deque<OutEntry> q;
+  size_t max_entries = 50;
+  int64_t lookups = 0, hits = 0;
+};
+static OutCache &outcache() {
+  static OutCache c;
+  return c;
+}
+static void outcache_clear() {
+  OutCache &oc = outcache();
+  std::lock_guard<std::mutex> lock(oc.mu);
+  oc.q.clear();
+}
+static bool outcache_find(int model, const EnvOpts &env, const double *par, int npar, const double *energy,
+                          int nflux, double *flux) {
+  OutCache &oc = outcache();
+  std::lock_guard<std::mutex> lock(oc.mu);
+  if (oc.max_entries == 0) return false;
+  oc.lookups++;
+  for (const OutEntry &e : oc.q) {
+    if (e.model != model || e.env.nzones_env != env.nzones_env || e.env.flags != env.flags ||
+        (int) e.flux.size() != nflux)
+      continue;
+    bool same = true;
+    for (int q = 0; q < npar && same; q++) same = !(std::fabs(e.par[q] - par[q]) > 1e-8);
+    if (!same || std::memcmp(e.ener.data(), energy, sizeof(double) * (size_t) (nflux + 1)) != 0) continue;
+    std::memcpy(flux, e.flux.data(), sizeof(double) * (size_t) nflux);
+    oc.hits++;
+    return true;
+  }
+  return false;
+}
+static void outcache_add(int model, const EnvOpts &env, const double *par, int npar, const double *energy, int nflux,
+                         const double *flux) {
+  OutCache &oc = outcache();
+  std::lock_guard<std::mutex> lock(oc.mu);
+  if (oc.max_entries == 0) return;
+  oc.q.push_front(OutEntry{model, env, std::vector<double>(par, par + npar),
+                           std::vector<double>(energy, energy + nflux + 1), std::vector<double>(flux, flux + nflux)});
+  while (oc.q.size() > oc.max_entries) oc.q.pop_back();
+}
+
 // number of zones a set will use (get_num_zones, relutility.c:506-544)
 static int zones_for(int model, int ion_grad_type, int envn) {
   const int kind = relx_kind(model);
@@ -953,6 +1010,7 @@ static int ensure_init(Context &C, const char *path) {
   if (st) return st;
   C.table_dir = dir;
   RELX_CUDA(C.cache.clear(C.stream));  // cached profiles belong to the previous tables
+  outcache_clear();
   graphs_clear(C);
   if ((st = set_kernel_attrs(C.T))) return st;
   return 0;
@@ -1959,6 +2017,25 @@ int relx_cache_stats(int64_t *out) {
   return 0;
 }
 
+int relx_output_cache_config(int max_entries) {
+  if (max_entries < 0) return RELX_ERR_ARG;
+  OutCache &oc = outcache();
+  std::lock_guard<std::mutex> lock(oc.mu);
+  oc.max_entries = (size_t) max_entries;
+  while (oc.q.size() > oc.max_entries) oc.q.pop_back();
+  return 0;
+}
+
+int relx_output_cache_stats(int64_t *out) {
+  if (!out) return RELX_ERR_ARG;
+  OutCache &oc = outcache();
+  std::lock_guard<std::mutex> lock(oc.mu);
+  out[0] = oc.lookups;
+  out[1] = oc.hits;
+  out[2] = (int64_t) oc.q.size();
+  return 0;
+}
+
 int relx_table_bytes(int64_t *bytes) {
   Context &C = ctx();
   std::lock_guard<std::mutex> lock(C.mu);
@@ -1988,6 +2065,14 @@ static void lmod_eval(int model, const double *energy, int Nflux, const double *
     g_last_status = RELX_ERR_ARG;
     return;
   }
+  const int kind = relx_kind(model);
+  const bool cacheable = kind == RELX_RELXILL || kind == RELX_RELXILLLP;  // relxill_kernel's models
+  const EnvOpts env = read_env();
+  const int npar = model_nparams(model);
+  if (cacheable && outcache_find(model, env, parameter, npar, energy, Nflux, flux)) {
+    g_last_status = RELX_OK;
+    return;
+  }
   int64_t eoff[2] = {0, (int64_t) Nflux + 1};
   int status = 0;
   std::vector<double> out((size_t) Nflux);
@@ -2005,6 +2090,7 @@ static void lmod_eval(int model, const double *energy, int Nflux, const double *
   g_last_status = st ? st : status;
   if (st == 0 || st == status) {
     std::memcpy(flux, out.data(), sizeof(double) * Nflux);
+    if (cacheable && st == 0 && status == 0) outcache_add(model, env, parameter, npar, energy, Nflux, flux);
   } else {
     std::fprintf(stderr, " *** relxill-gb300 error %d: %s\n", st, g_errmsg.c_str());
     for (int i = 0; i < Nflux; i++) flux[i] = 0.0;

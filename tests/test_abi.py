@@ -61,3 +61,16 @@ def test_unsupported_public_models_zero_flux_and_report():
         assert list(flux) == [0.0] * 10
         lib.relx_last_status.restype = ctypes.c_int
         assert lib.relx_last_status() == 3
+
+
+def test_output_cache_bookkeeping_without_a_gpu():
+    """The local-model output cache's configuration and counters need no GPU."""
+    from relxill_gb300 import build
+
+    lib = ctypes.CDLL(build.build())
+    out = (ctypes.c_int64 * 3)()
+    assert lib.relx_output_cache_config(ctypes.c_int(-1)) != 0
+    assert lib.relx_output_cache_config(ctypes.c_int(3)) == 0
+    assert lib.relx_output_cache_stats(out) == 0
+    assert out[2] == 0
+    assert lib.relx_output_cache_config(ctypes.c_int(50)) == 0
