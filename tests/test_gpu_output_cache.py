@@ -89,3 +89,22 @@ def test_cache_off_and_bounded(gpu):
         assert _delta(gpu, s1) == (2, 1)
     finally:
         gpu.output_cache_config(50)
+
+
+def test_cache_emptied_when_tables_are_loaded_again(gpu, small_tables):
+    """relx_init with another table path reloads the tables and drops every cached flux (an entry
+    belongs to the tables it was computed with)."""
+    import os
+
+    gpu.output_cache_config(50)
+    e = _grid(350)
+    gpu.relxilllp(e, P)
+    assert gpu.output_cache_stats()["entries"] >= 1
+    try:
+        gpu.init(small_tables.rstrip("/") + os.sep)  # the same files under another path string
+        assert gpu.output_cache_stats()["entries"] == 0
+        s0 = gpu.output_cache_stats()
+        gpu.relxilllp(e, P)
+        assert _delta(gpu, s0) == (1, 0)
+    finally:
+        gpu.init(small_tables)
