@@ -209,9 +209,11 @@ void relx_serve_destroy(relx_server *s);
 int relx_selftest_wait_timeout(double limit_ms, int *status);
 
 /* Launch tuning (no counterpart in the reference).  autotune != 0: the first
- * batch of a (model, batch-size class, zone count) is run once per candidate
- * of (line-kernel tile of 256 or 512 bins, pipelined chunks of 1024 sets) and
- * the fastest is kept for the class; that batch synchronises its stream.
+ * batch of 2048 sets or more of a (model, batch-size class, zone count) is run
+ * once per candidate (one range, or pipelined chunks of 1024 sets) and the
+ * fastest is kept for the class; that batch synchronises its stream (smaller
+ * batches have one candidate, recorded without trials; the line-kernel tile is
+ * fixed at 512 bins).
  * graphs != 0: a batch shape that recurs on the same workspace is captured
  * into a CUDA graph on its second launch and replayed afterwards.  Both are on
  * by default; every choice gives the same numbers. */
