@@ -9,14 +9,16 @@
 // dist is the zone's normalised emission-angle histogram.
 //
 // Launch: one CTA of 128 threads per (energy tile of 512 bins, parameter set),
-// three CTAs per SM.  The corner list of a set is de-duplicated across zones by
+// four CTAs per SM.  The corner list of a set is de-duplicated across zones by
 // the setup kernel and holds only rows with a non-zero weight, so every table
 // row a set needs is read once; sets are visited in table-row order
 // (xill_order_kernel) so that sets sharing rows find them in L2.  The n_incl
 // row segments of a corner (contiguous rows, incl is the fastest table index)
 // are streamed into shared memory with cp.async.bulk (TMA bulk copies)
-// completing on an mbarrier, three corners in flight per CTA; all waits are
-// bounded and report a timeout through the error flag instead of hanging.
+// completing on an mbarrier, two corners in flight per CTA (a third stage cost
+// the fourth CTA per SM: 0.91 ms per 4096-set step against 0.78 with two); all
+// waits are bounded and report a timeout through the error flag instead of
+// hanging.
 #include "relx_device.cuh"
 #include "relx_tma.cuh"
 
@@ -24,7 +26,7 @@ namespace relx {
 
 constexpr int kXillThreads = 128;
 constexpr int kXillTile = 512;    // floats per row segment (2 KB), one float4 per thread
-constexpr int kXillStages = 3;
+constexpr int kXillStages = 2;
 static_assert(kXillTile == 4 * kXillThreads, "one float4 per thread");
 
 // Self-test of the timeout path: one thread waits, with a short limit, on an mbarrier that
@@ -109,7 +111,7 @@ void launch_xill_order(cudaStream_t s, const RelxSetState *sst, const RelxCorner
 // NZ: zones held in registers (a set with more zones runs in a wider instance);
 // NI: inclinations unrolled at compile time (0: any count up to RELX_MAX_INCL).
 template <int NZ, int NI>
-__global__ void __launch_bounds__(kXillThreads, 3) xillver_dense_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
+__global__ void __launch_bounds__(kXillThreads, 4) xillver_dense_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
                                                                         const RelxCorners *__restrict__ scor,
                                                                         const float *__restrict__ dist_raw, int nza,
                                                                         float *__restrict__ xout, int *__restrict__ err,
