@@ -643,8 +643,8 @@ __global__ void __launch_bounds__(kLineThreads, 4) relline_kernel(
 // emission-angle distribution per zone (Relprofile.cpp:908-938), one CTA per set.  The set's
 // (a, mu0)-interpolated transfer functions and emission-angle cosines on all table radii are
 // written once per set by line_table_kernel (which the line profile reads as well) and read
-// through the read-only cache, so that the histogram CTA's shared memory stays small (four CTAs
-// per SM).
+// through the read-only cache, so that the histogram CTA's shared memory stays small; five CTAs
+// per SM (48 registers: 0.82 -> 0.77 ms per 4096-set step against four; six spill).
 // ---------------------------------------------------------------------------
 struct HistSmem {
   RelxRadRec rec[kChunk];    // radius records of the current chunk
@@ -697,7 +697,7 @@ __device__ double cosne_fp64(const RelxTables &tab, const RelxSetState &s, int i
   return lerp1(ifac, v[0], v[1]);
 }
 
-__global__ void __launch_bounds__(kLineThreads, 4) hist_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
+__global__ void __launch_bounds__(kLineThreads, 5) hist_kernel(RelxTables tab, const RelxSetState *__restrict__ sst,
                                                             const RelxRadial *__restrict__ srad, int nza,
                                                             const float4 *__restrict__ htab, float *__restrict__ dist) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
