@@ -34,7 +34,7 @@ namespace relx {
 
 constexpr int kLineWarps = 8;
 constexpr int kLineThreads = kLineWarps * 32;
-constexpr int kSumBins = 256;    // profile sums are kept per block of 256 bins, whatever the tile
+constexpr int kSumBins = 256;    // profile sums are kept per block of 256 bins (two per tile)
 static_assert(kSumBins == kLineThreads, "one bin per thread and block in the sums");
 constexpr float kH = 5e-3f;
 constexpr float kSideBand = 2e-5f;  // grid units within which the side of a g* point is taken in float-float

@@ -957,7 +957,7 @@ struct Context {
   std::vector<std::vector<uintptr_t>> graph_seen;  // shapes launched once (captured on the second launch)
   uint64_t graph_clock = 0;
   bool graphs_on = true;
-  // autotuned line tile and chunking per (model, batch-size class, zones)
+  // autotuned chunking per (model, batch-size class, zones); the line tile is recorded (fixed)
   struct TuneEntry {
     int model, sclass, nza, line_tile, chunk;
     double ms[4];
@@ -1423,11 +1423,11 @@ static int launch_batch(Context &C, Workspace &W, const BatchShape &b, cudaStrea
   return 0;
 }
 
-// Autotuner: the first batch of a (model, batch-size class, zone count) runs once with every
-// candidate of (line tile, pipelined chunk) and keeps the fastest; later batches of the class use
-// it.  Every candidate gives the same numbers (the profile sums are per 256-bin block whatever the
-// tile, and the chunks only reorder independent sets), so the last trial's results stand.  The
-// trials synchronise the stream.
+// Autotuner: the first batch of 2048 sets or more of a (model, batch-size class, zone count) runs
+// once with every candidate (one range, or pipelined chunks of 1024 sets) and keeps the fastest;
+// later batches of the class use it.  Every candidate gives the same numbers (the chunks only
+// reorder independent sets), so the last trial's results stand.  The trials synchronise the
+// stream.  Smaller batches have one candidate, recorded without trials.
 static int tuned_launch(Context &C, Workspace &W, BatchShape &b, cudaStream_t s, bool use_cache,
                         bool allow_tune = true) {
   const bool cached = use_cache && C.cache.enabled() && relx_kind(b.model) != RELX_RELLINE &&
